@@ -1,0 +1,317 @@
+"""ctypes binding of ``libdns3d_gpu.so`` and a host-side mirror of the
+reference's time-loop interface.
+
+The reference program (``DNS_pressure_BC_3D.f90``) advances the flow with five
+argument-less subroutines called in a fixed order from its time loop
+(DNS_pressure_BC_3D.f90:314-326).  :class:`ChannelDNS` exposes the same five
+names as methods over one GPU handle, plus ``step(n)`` for the fused,
+graph-replayed loop body, state transfer and diagnostics.
+
+There is no CPU fallback: if the shared library is missing or no GPU is
+present, constructing :class:`ChannelDNS` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, fields as dc_fields
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libdns3d_gpu.so")
+
+DNS3D_OK = 0
+DNS3D_E_INVALID = 1
+DNS3D_E_OOM = 2
+DNS3D_E_SINGULAR = 3
+DNS3D_E_NONFINITE = 4
+DNS3D_E_CUDA = 5
+DNS3D_E_UNSUPPORTED = 6
+DNS3D_E_IO = 7
+DNS3D_E_NODEVICE = 8
+PREC_FP64 = 0
+
+#: every symbol declared in include/dns3d_capi.h
+EXPORTED_SYMBOLS = (
+    "dns3d_config_defaults", "dns3d_config_read_namelist", "dns3d_create", "dns3d_destroy",
+    "dns3d_initialize_fields", "dns3d_set_state", "dns3d_get_state", "dns3d_set_clock",
+    "dns3d_compute_source_terms", "dns3d_viscous_step", "dns3d_solve_pressure",
+    "dns3d_pressure_correction", "dns3d_apply_boundary_conditions", "dns3d_step",
+    "dns3d_synchronize", "dns3d_diagnostics", "dns3d_footprint_bytes", "dns3d_strerror",
+    "dns3d_last_error",
+)
+
+
+class CConfig(C.Structure):
+    """``dns3d_config`` (field order of include/dns3d_capi.h)."""
+
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("istart", C.c_int), ("nsteps", C.c_int), ("nwrt", C.c_int), ("restart_write_freq", C.c_int),
+        ("dt", C.c_double),
+        ("re", C.c_double), ("xlen", C.c_double), ("ylen", C.c_double), ("u_centerline", C.c_double),
+        ("use_crank_nicolson", C.c_int),
+        ("flow_control_method", C.c_int),
+        ("target_pressure_gradient", C.c_double), ("target_bulk_velocity", C.c_double),
+        ("controller_gain", C.c_double),
+        ("controller_update_freq", C.c_int),
+        ("enable_perturbations", C.c_int),
+        ("perturbation_amplitude", C.c_double),
+        ("zero_w_perturbations", C.c_int), ("use_analytical_perturbations", C.c_int),
+        ("analytical_mode_x", C.c_int), ("analytical_mode_y", C.c_int),
+        ("use_weak_form_divergence", C.c_int),
+        ("use_dealias_23_rule", C.c_int),
+        ("lgl_dmatrix_guard", C.c_int),
+        ("precision", C.c_int),
+        ("device", C.c_int),
+    ]
+
+
+class CPIState(C.Structure):
+    _fields_ = [
+        ("current_pressure_gradient", C.c_double), ("current_bulk_velocity", C.c_double),
+        ("bulk_velocity_error", C.c_double), ("bulk_velocity_error_integral", C.c_double),
+        ("bulk_velocity_error_prev", C.c_double), ("pressure_gradient_sum", C.c_double),
+        ("avg_pressure_gradient", C.c_double), ("pressure_gradient_count", C.c_int),
+        ("pad_", C.c_int),
+    ]
+
+
+class CDiag(C.Structure):
+    _fields_ = [
+        ("umax", C.c_double), ("vmax", C.c_double), ("wmax", C.c_double), ("energy", C.c_double),
+        ("u_bulk", C.c_double), ("dpdx", C.c_double), ("dpdx_avg", C.c_double),
+        ("max_div", C.c_double), ("time", C.c_double), ("step", C.c_int), ("pad_", C.c_int),
+    ]
+
+
+class Dns3DError(RuntimeError):
+    """A non-zero status from the C-ABI (the reference would ``stop`` here)."""
+
+    def __init__(self, code: int, where: str, detail: str = ""):
+        self.code = code
+        msg = f"{where}: {strerror(code)} (status {code})"
+        if detail:
+            msg += f": {detail}"
+        super().__init__(msg)
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load ``libdns3d_gpu.so`` (built by ``f90_dns_gb300.build``)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is missing: build it with `python -m f90_dns_gb300.build`")
+    lib = C.CDLL(p)
+    vp, ip, dp = C.c_void_p, C.c_int, C.POINTER(C.c_double)
+    hp = C.c_void_p
+    lib.dns3d_config_defaults.argtypes = [C.POINTER(CConfig)]
+    lib.dns3d_config_read_namelist.argtypes = [C.c_char_p, C.POINTER(CConfig)]
+    lib.dns3d_create.argtypes = [C.POINTER(CConfig), C.POINTER(hp)]
+    lib.dns3d_destroy.argtypes = [hp]
+    lib.dns3d_initialize_fields.argtypes = [hp]
+    lib.dns3d_set_state.argtypes = [hp] + [vp] * 8 + [C.POINTER(CPIState)]
+    lib.dns3d_get_state.argtypes = [hp] + [vp] * 8 + [C.POINTER(CPIState)]
+    lib.dns3d_set_clock.argtypes = [hp, ip, C.c_double]
+    for n in ("dns3d_compute_source_terms", "dns3d_viscous_step", "dns3d_solve_pressure",
+              "dns3d_pressure_correction", "dns3d_apply_boundary_conditions", "dns3d_synchronize"):
+        getattr(lib, n).argtypes = [hp]
+    lib.dns3d_step.argtypes = [hp, ip]
+    lib.dns3d_diagnostics.argtypes = [hp, C.POINTER(CDiag)]
+    lib.dns3d_footprint_bytes.argtypes = [C.POINTER(CConfig), C.POINTER(C.c_ulonglong)]
+    lib.dns3d_strerror.argtypes = [ip]
+    lib.dns3d_strerror.restype = C.c_char_p
+    lib.dns3d_last_error.argtypes = [hp]
+    lib.dns3d_last_error.restype = C.c_char_p
+    for n in EXPORTED_SYMBOLS:
+        if n not in ("dns3d_strerror", "dns3d_last_error"):
+            getattr(lib, n).restype = ip
+    del dp
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def strerror(code: int) -> str:
+    try:
+        return load_library().dns3d_strerror(code).decode()
+    except Exception:  # pragma: no cover - library absent
+        return f"status {code}"
+
+
+def default_config(**overrides) -> CConfig:
+    """``dns3d_config`` with the reference defaults (3D:571-603) and overrides."""
+    cfg = CConfig()
+    rc = load_library().dns3d_config_defaults(C.byref(cfg))
+    if rc:
+        raise Dns3DError(rc, "dns3d_config_defaults")
+    for k, v in overrides.items():
+        if not hasattr(cfg, k):
+            raise KeyError(k)
+        setattr(cfg, k, int(v) if isinstance(v, bool) else v)
+    return cfg
+
+
+def read_namelist(path: str, base: CConfig | None = None) -> CConfig:
+    """Parse an ``input.dat`` with the eight namelist groups of read_input_3d."""
+    cfg = base if base is not None else default_config()
+    rc = load_library().dns3d_config_read_namelist(os.fsencode(path), C.byref(cfg))
+    if rc:
+        raise Dns3DError(rc, "dns3d_config_read_namelist", path)
+    return cfg
+
+
+def config_from(obj, **overrides) -> CConfig:
+    """Build a ``dns3d_config`` from any object/dict carrying namelist names."""
+    cfg = default_config()
+    src = obj if isinstance(obj, dict) else {f.name: getattr(obj, f.name) for f in dc_fields(obj)}
+    names = {n for n, _ in CConfig._fields_}
+    for k, v in src.items():
+        if k in names:
+            setattr(cfg, k, int(v) if isinstance(v, bool) else v)
+    for k, v in overrides.items():
+        setattr(cfg, k, int(v) if isinstance(v, bool) else v)
+    return cfg
+
+
+def footprint_bytes(cfg: CConfig) -> int:
+    out = C.c_ulonglong(0)
+    rc = load_library().dns3d_footprint_bytes(C.byref(cfg), C.byref(out))
+    if rc:
+        raise Dns3DError(rc, "dns3d_footprint_bytes")
+    return int(out.value)
+
+
+@dataclass
+class Diagnostics:
+    umax: float
+    vmax: float
+    wmax: float
+    energy: float
+    u_bulk: float
+    dpdx: float
+    dpdx_avg: float
+    max_div: float
+    time: float
+    step: int
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class ChannelDNS:
+    """One channel-flow run resident on a GPU (the reference program's state).
+
+    Arrays are numpy ``float64`` of shape ``(nz, ny, nx)``: the memory order of
+    the reference's Fortran ``u(nx,ny,nz)``.
+    """
+
+    def __init__(self, cfg: CConfig):
+        self.lib = load_library()
+        self.cfg = cfg
+        self._h = C.c_void_p()
+        rc = self.lib.dns3d_create(C.byref(cfg), C.byref(self._h))
+        if rc:
+            raise Dns3DError(rc, "dns3d_create")
+        self.shape = (cfg.nz, cfg.ny, cfg.nx)
+
+    # -- lifetime -------------------------------------------------------------
+    def close(self) -> None:
+        if self._h:
+            self.lib.dns3d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, where: str) -> None:
+        if rc:
+            raise Dns3DError(rc, where, self.lib.dns3d_last_error(self._h).decode())
+
+    # -- the reference's five time-loop subroutines (3D:314-326) -------------
+    def compute_source_terms_3d(self) -> None:
+        self._check(self.lib.dns3d_compute_source_terms(self._h), "compute_source_terms_3d")
+
+    def viscous_step_3d(self) -> None:
+        self._check(self.lib.dns3d_viscous_step(self._h), "viscous_step_3d")
+
+    def solve_pressure_3d(self) -> None:
+        self._check(self.lib.dns3d_solve_pressure(self._h), "solve_pressure_3d")
+
+    def pressure_correction_3d(self) -> None:
+        self._check(self.lib.dns3d_pressure_correction(self._h), "pressure_correction_3d")
+
+    def apply_boundary_conditions_3d(self) -> None:
+        self._check(self.lib.dns3d_apply_boundary_conditions(self._h), "apply_boundary_conditions_3d")
+
+    # -- fused loop body --------------------------------------------------------
+    def step(self, nsteps: int = 1) -> None:
+        self._check(self.lib.dns3d_step(self._h, int(nsteps)), "dns3d_step")
+
+    def synchronize(self) -> None:
+        self._check(self.lib.dns3d_synchronize(self._h), "dns3d_synchronize")
+
+    def initialize_fields_3d(self) -> None:
+        self._check(self.lib.dns3d_initialize_fields(self._h), "initialize_fields_3d")
+
+    def set_clock(self, step: int, time: float) -> None:
+        self._check(self.lib.dns3d_set_clock(self._h, int(step), float(time)), "dns3d_set_clock")
+
+    # -- state ------------------------------------------------------------------
+    def get_state(self, walls: bool = True) -> dict:
+        nz, ny, nx = self.shape
+        out = {k: np.empty(self.shape) for k in ("u", "v", "w", "p_total")}
+        gp = {k: np.empty((ny, nx)) for k in ("gpx_w1", "gpx_w2", "gpy_w1", "gpy_w2")} if walls else {}
+        pi = CPIState()
+        rc = self.lib.dns3d_get_state(self._h, _ptr(out["u"]), _ptr(out["v"]), _ptr(out["w"]),
+                                      _ptr(out["p_total"]), _ptr(gp.get("gpx_w1")),
+                                      _ptr(gp.get("gpx_w2")), _ptr(gp.get("gpy_w1")),
+                                      _ptr(gp.get("gpy_w2")), C.byref(pi))
+        self._check(rc, "dns3d_get_state")
+        out.update(gp)
+        out["pi"] = {n: getattr(pi, n) for n, _ in CPIState._fields_ if n != "pad_"}
+        return out
+
+    def set_state(self, u=None, v=None, w=None, p_total=None, gpx_w1=None, gpx_w2=None,
+                  gpy_w1=None, gpy_w2=None, pi: dict | None = None) -> None:
+        def arr(a, shape):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.shape != shape:
+                raise ValueError(f"expected shape {shape}, got {a.shape}")
+            return a
+        nz, ny, nx = self.shape
+        f = [arr(x, self.shape) for x in (u, v, w, p_total)]
+        g = [arr(x, (ny, nx)) for x in (gpx_w1, gpx_w2, gpy_w1, gpy_w2)]
+        cpi = None
+        if pi is not None:
+            cpi = CPIState()
+            for k, val in pi.items():
+                setattr(cpi, k, val)
+        rc = self.lib.dns3d_set_state(self._h, *[_ptr(x) for x in f], *[_ptr(x) for x in g],
+                                      C.byref(cpi) if cpi is not None else None)
+        self._check(rc, "dns3d_set_state")
+
+    def diagnostics(self) -> Diagnostics:
+        d = CDiag()
+        rc = self.lib.dns3d_diagnostics(self._h, C.byref(d))
+        self._check(rc, "dns3d_diagnostics")
+        return Diagnostics(d.umax, d.vmax, d.wmax, d.energy, d.u_bulk, d.dpdx, d.dpdx_avg,
+                           d.max_div, d.time, d.step)

@@ -1,0 +1,631 @@
+// C-ABI entry points of libdns3d_gpu.so (declared in include/dns3d_capi.h).
+//
+// The handle owns the device state of one channel run: the spectra of u, v,
+// w and p_total, the wall planes of grad(p_total) the next step's Kim & Moin
+// boundary condition reads, the PI controller state, the LGL operators and
+// the per-mode operator inverses.  The five stage entry points run the same
+// kernels that dns3d_step() captures into a CUDA graph.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dns3d_internal.cuh"
+
+using namespace dns3d;
+
+struct dns3d_handle {
+    dns3d_config cfg{};
+    GridDev g{};
+    cudaStream_t stream = nullptr;
+    FftCtx fft{};
+    Ops ops{};
+    StepParams sp{};
+    PIParams pp{};
+    double2 *U = nullptr, *V = nullptr, *W = nullptr, *P = nullptr, *GP = nullptr;
+    double2 *SU = nullptr, *SV = nullptr, *SW = nullptr;
+    double2 *US = nullptr, *VS = nullptr, *WS = nullptr, *PHI = nullptr;
+    double* phys[6] = {nullptr};
+    dns3d_pi_state* d_pi = nullptr;
+    double* d_red = nullptr;
+    double* d_out = nullptr;
+    int* d_flag = nullptr;
+    int red_blocks = 0;
+    std::vector<double> zpts, zwts;
+    std::vector<void*> allocs;
+    int step = 0;
+    double time = 0.0;
+    cudaGraphExec_t graph = nullptr;
+    std::string err;
+};
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;  // 4*atan(1), DNS_pressure_BC_3D.f90:43
+
+int cuda_fail(dns3d_handle* h, cudaError_t e, const char* what) {
+    if (h) {
+        h->err = std::string(what) + ": " + cudaGetErrorString(e);
+    }
+    return (e == cudaErrorMemoryAllocation) ? DNS3D_E_OOM : DNS3D_E_CUDA;
+}
+
+#define CK(h, call)                                              \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
+    } while (0)
+
+template <typename T>
+int dev_alloc(dns3d_handle* h, T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T) > 0 ? count * sizeof(T) : 1);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
+    h->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return DNS3D_OK;
+}
+
+size_t spec_elems(const dns3d_config& c) { return (size_t)(c.nx / 2 + 1) * c.ny * c.nz; }
+size_t phys_elems(const dns3d_config& c) { return (size_t)c.nx * c.ny * c.nz; }
+int n_unique_q(const dns3d_config& c) { return (c.ny / 2 + 1) * (c.nx / 2 + 1); }
+
+int validate(const dns3d_config* c) {
+    if (!c) return DNS3D_E_INVALID;
+    if (c->nx < 4 || c->ny < 4 || (c->nx % 2) || (c->ny % 2)) return DNS3D_E_UNSUPPORTED;
+    if (!fft_length_supported(c->ny) || !fft_length_supported(c->nx / 2)) return DNS3D_E_UNSUPPORTED;
+    if (c->nx > 1024 || c->ny > 1024) return DNS3D_E_UNSUPPORTED;
+    if (c->nz < 3 || c->nz > 129) return DNS3D_E_UNSUPPORTED;
+    if (!(c->dt > 0.0) || !(c->re > 0.0) || !(c->xlen > 0.0) || !(c->ylen > 0.0)) return DNS3D_E_INVALID;
+    // parameter validation of read_input_3d (3D:649-679)
+    if (c->flow_control_method != 1 && c->flow_control_method != 2) return DNS3D_E_INVALID;
+    if (c->flow_control_method == 2) {
+        if (!(c->target_bulk_velocity > 0.0) || !(c->controller_gain > 0.0) || c->controller_update_freq <= 0)
+            return DNS3D_E_INVALID;
+    }
+    if (c->enable_perturbations && !c->use_analytical_perturbations) return DNS3D_E_UNSUPPORTED;
+    if (c->precision != DNS3D_PREC_FP64) return DNS3D_E_UNSUPPORTED;
+    return DNS3D_OK;
+}
+
+// Physical initial condition of initialize_fields_3d (3D:909-962) with
+// generate_analytical_perturbations (perturbation_analytical_simple.f90:24-155).
+void initial_fields(const dns3d_config& c, const std::vector<double>& z, std::vector<double>& u,
+                    std::vector<double>& v, std::vector<double>& w) {
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    const size_t pl = (size_t)nx * ny;
+    u.assign(pl * nz, 0.0);
+    v.assign(pl * nz, 0.0);
+    w.assign(pl * nz, 0.0);
+    for (int k = 0; k < nz; ++k)
+        for (size_t i = 0; i < pl; ++i) u[k * pl + i] = c.u_centerline * (1.0 - z[k] * z[k]);
+    if (!c.enable_perturbations) return;
+    const double kx = 2.0 * kPi * (double)c.analytical_mode_x / c.xlen;
+    const double ky = 2.0 * kPi * (double)c.analytical_mode_y / c.ylen;
+    std::vector<double> up(pl * nz), vp(pl * nz);
+    double cur = 0.0;
+    for (int k = 0; k < nz; ++k) {
+        const double damp = 1.0 - z[k] * z[k];
+        for (int j = 0; j < ny; ++j) {
+            const double y = (double)j * c.ylen / (double)ny;
+            for (int i = 0; i < nx; ++i) {
+                const double x = (double)i * c.xlen / (double)nx;
+                const size_t o = k * pl + (size_t)j * nx + i;
+                up[o] = -ky * std::sin(kx * x) * std::cos(ky * y) * damp;
+                vp[o] = kx * std::cos(kx * x) * std::sin(ky * y) * damp;
+                const double mag = std::sqrt(up[o] * up[o] + vp[o] * vp[o]);
+                if (mag > cur) cur = mag;
+            }
+        }
+    }
+    if (cur > 1.0e-12) {  // scale_perturbations (:110-133)
+        const double s = c.perturbation_amplitude / cur;
+        for (size_t o = 0; o < pl * nz; ++o) { up[o] *= s; vp[o] *= s; }
+    } else {
+        std::fill(up.begin(), up.end(), 0.0);
+        std::fill(vp.begin(), vp.end(), 0.0);
+    }
+    for (size_t o = 0; o < pl * nz; ++o) { u[o] += up[o]; v[o] += vp[o]; }
+    for (int k : {0, nz - 1})  // enforce_wall_boundaries + apply_boundary_conditions_3d (3D:3253)
+        for (size_t i = 0; i < pl; ++i) { u[k * pl + i] = 0.0; v[k * pl + i] = 0.0; w[k * pl + i] = 0.0; }
+}
+
+int upload(dns3d_handle* h, void* dst, const void* src, size_t bytes) {
+    CK(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    return DNS3D_OK;
+}
+
+int run_source_terms(dns3d_handle* h) {
+    const GridDev& g = h->g;
+    CK(h, launch_pi_update(g, h->ops, h->pp, h->U, h->d_pi, h->stream));
+    // vorticity into the u*,v*,w* buffers (free until the viscous step)
+    CK(h, launch_vorticity(g, h->ops, h->U, h->V, h->W, h->US, h->VS, h->WS, h->stream));
+    Fields spec{};
+    spec.p[0] = h->U; spec.p[1] = h->V; spec.p[2] = h->W;
+    spec.p[3] = h->US; spec.p[4] = h->VS; spec.p[5] = h->WS;
+    RFields phys{};
+    for (int f = 0; f < 6; ++f) phys.p[f] = h->phys[f];
+    CK(h, fft_c2r(h->fft, g, spec, phys, 6, g.nz, h->stream));
+    RFields prod{};
+    for (int f = 0; f < 3; ++f) prod.p[f] = h->phys[f];
+    CK(h, launch_products(g, phys, prod, h->stream));
+    Fields src{};
+    src.p[0] = h->SU; src.p[1] = h->SV; src.p[2] = h->SW;
+    CK(h, fft_r2c(h->fft, g, prod, src, 3, g.nz, h->stream));
+    return DNS3D_OK;
+}
+
+int run_viscous(dns3d_handle* h) {
+    Fields F{}, S{}, O{};
+    F.p[0] = h->U; F.p[1] = h->V; F.p[2] = h->W;
+    S.p[0] = h->SU; S.p[1] = h->SV; S.p[2] = h->SW;
+    O.p[0] = h->US; O.p[1] = h->VS; O.p[2] = h->WS;
+    CK(h, launch_viscous(h->g, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->stream));
+    return DNS3D_OK;
+}
+
+int run_pressure(dns3d_handle* h) {
+    CK(h, launch_pressure(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->stream));
+    return DNS3D_OK;
+}
+
+int run_correction(dns3d_handle* h) {
+    CK(h, launch_correction(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
+                            h->GP, h->stream));
+    return DNS3D_OK;
+}
+
+int run_bc(dns3d_handle* h) {
+    CK(h, launch_apply_bc(h->g, h->U, h->V, h->W, h->stream));
+    return DNS3D_OK;
+}
+
+int run_step_body(dns3d_handle* h) {
+    int rc;
+    if ((rc = run_source_terms(h))) return rc;
+    if ((rc = run_viscous(h))) return rc;
+    if ((rc = run_pressure(h))) return rc;
+    if ((rc = run_correction(h))) return rc;
+    return run_bc(h);
+}
+
+void release(dns3d_handle* h) {
+    if (!h) return;
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (void* p : h->allocs) cudaFree(p);
+    h->allocs.clear();
+    fft_release(h->fft);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int dns3d_config_defaults(dns3d_config* c) {
+    if (!c) return DNS3D_E_INVALID;
+    std::memset(c, 0, sizeof(*c));
+    c->nx = 128; c->ny = 32; c->nz = 33;
+    c->istart = 0; c->nsteps = 1000; c->nwrt = 100; c->restart_write_freq = 1000;
+    c->dt = 0.01; c->re = 180.0;
+    c->xlen = 2.0 * kPi; c->ylen = 2.0 * kPi;
+    c->u_centerline = 1.5;
+    c->use_crank_nicolson = 1;
+    c->flow_control_method = 1;
+    c->target_pressure_gradient = 0.03;
+    c->target_bulk_velocity = 1.0;
+    c->controller_gain = 0.15;
+    c->controller_update_freq = 7;
+    c->enable_perturbations = 0;
+    c->perturbation_amplitude = 0.01;
+    c->zero_w_perturbations = 0;
+    c->use_analytical_perturbations = 0;
+    c->analytical_mode_x = 1; c->analytical_mode_y = 1;
+    c->use_weak_form_divergence = 0;
+    c->use_dealias_23_rule = 0;
+    c->lgl_dmatrix_guard = 1;
+    c->precision = DNS3D_PREC_FP64;
+    c->device = 0;
+    return DNS3D_OK;
+}
+
+int dns3d_config_read_namelist(const char* path, dns3d_config* cfg) {
+    if (!path || !cfg) return DNS3D_E_INVALID;
+    return read_namelist_file(path, cfg);
+}
+
+int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
+    if (!c || !bytes) return DNS3D_E_INVALID;
+    const size_t se = spec_elems(*c), pe = phys_elems(*c);
+    const size_t nm = (size_t)(c->nx / 2 + 1) * c->ny;
+    const size_t nq = (size_t)n_unique_q(*c);
+    const size_t nz2 = (size_t)c->nz * c->nz;
+    size_t b = 0;
+    b += 11 * se * sizeof(double2);          // U V W P SU SV SW US VS WS PHI
+    b += 4 * nm * sizeof(double2);           // GP
+    b += 6 * se * sizeof(double2);           // FFT scratch
+    b += 6 * pe * sizeof(double);            // physical fields
+    b += (2 * nq + 1) * nz2 * sizeof(double);  // inverses
+    b += 16ull << 20;                        // operators, tables, reductions
+    *bytes = b;
+    return DNS3D_OK;
+}
+
+int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
+    if (!out) return DNS3D_E_INVALID;
+    *out = nullptr;
+    int rc = validate(cfg);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DNS3D_E_NODEVICE;
+    if (cfg->device < 0 || cfg->device >= ndev) return DNS3D_E_INVALID;
+    dns3d_handle* h = new dns3d_handle();
+    h->cfg = *cfg;
+    const dns3d_config& c = h->cfg;
+    auto fail = [&](int code) { release(h); delete h; return code; };
+    if (cudaSetDevice(c.device) != cudaSuccess) return fail(DNS3D_E_CUDA);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(DNS3D_E_CUDA);
+
+    GridDev& g = h->g;
+    g.nx = c.nx; g.ny = c.ny; g.nz = c.nz;
+    g.nxh = c.nx / 2; g.nxhp = c.nx / 2 + 1; g.nm = g.nxhp * c.ny;
+    g.nkyu = c.ny / 2 + 1;
+    g.inv_nxny = 1.0 / ((double)c.nx * (double)c.ny);
+    const int nz = c.nz;
+
+    // setup_grid_3d (3D:740-742) and setup_spectral_3d (3D:769-809)
+    const double ybar = 2.0;
+    const double zs = 2.0 / ybar;
+    const double alpha = 2.0 * kPi / c.xlen;
+    std::vector<double> xw(g.nxhp), yw(c.ny);
+    for (int i = 0; i < g.nxhp; ++i) xw[i] = (double)i * alpha;
+    for (int j = 1; j <= c.ny; ++j)
+        yw[j - 1] = (j <= c.ny / 2 + 1) ? (double)(j - 1) * 2.0 * kPi / c.ylen
+                                        : (double)(j - 1 - c.ny) * 2.0 * kPi / c.ylen;
+    std::vector<double> d1, d2((size_t)nz * nz, 0.0);
+    lgl_nodes_weights(nz, h->zpts, h->zwts);
+    lgl_diff_matrix(h->zpts, c.lgl_dmatrix_guard != 0, d1);
+    for (int i = 0; i < nz; ++i)  // d2 = matmul(d1, d1) (3D:801)
+        for (int j = 0; j < nz; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < nz; ++k) s += d1[(size_t)i * nz + k] * d1[(size_t)k * nz + j];
+            d2[(size_t)i * nz + j] = s;
+        }
+    // stiffness S_kn = sum_m d1(m,k) d1(m,n) zwts(m) (2/ybar)  (3D:1467-1471)
+    std::vector<double> S((size_t)nz * nz);
+    for (int k = 0; k < nz; ++k)
+        for (int n = 0; n < nz; ++n) {
+            double s = 0.0;
+            for (int m = 0; m < nz; ++m) s += d1[(size_t)m * nz + k] * d1[(size_t)m * nz + n] * h->zwts[m];
+            S[(size_t)k * nz + n] = s * (2.0 / ybar);
+        }
+    const double theta = c.use_crank_nicolson ? 0.5 : 1.0;
+    const double helm_f = theta * c.dt / c.re;
+    std::vector<double> D1s((size_t)nz * nz), D2s((size_t)nz * nz), wh(nz), S0(nz), Sn(nz),
+        W1T((size_t)nz * nz);
+    for (size_t t = 0; t < (size_t)nz * nz; ++t) { D1s[t] = zs * d1[t]; D2s[t] = zs * zs * d2[t]; }
+    for (int k = 0; k < nz; ++k) {
+        wh[k] = h->zwts[k] * (ybar / 2.0);
+        S0[k] = helm_f * S[(size_t)k * nz + 0];
+        Sn[k] = helm_f * S[(size_t)k * nz + nz - 1];
+        for (int m = 0; m < nz; ++m) W1T[(size_t)k * nz + m] = d1[(size_t)m * nz + k] * h->zwts[m] * (2.0 / ybar);
+    }
+    const int nq = n_unique_q(c);
+    std::vector<double> ksq(nq);
+    for (int kya = 0; kya <= c.ny / 2; ++kya)
+        for (int kx = 0; kx < g.nxhp; ++kx) ksq[(size_t)kya * g.nxhp + kx] = xw[kx] * xw[kx] + yw[kya] * yw[kya];
+
+    Ops& ops = h->ops;
+    ops.nq = nq;
+    const size_t nz2 = (size_t)nz * nz;
+    double* dS = nullptr;
+    if ((rc = dev_alloc(h, &ops.D1, nz2)) || (rc = dev_alloc(h, &ops.D2, nz2)) ||
+        (rc = dev_alloc(h, &ops.wh, nz)) || (rc = dev_alloc(h, &ops.zw, nz)) ||
+        (rc = dev_alloc(h, &ops.S0, nz)) || (rc = dev_alloc(h, &ops.Sn, nz)) ||
+        (rc = dev_alloc(h, &ops.W1T, nz2)) || (rc = dev_alloc(h, &ops.xw, g.nxhp)) ||
+        (rc = dev_alloc(h, &ops.yw, c.ny)) || (rc = dev_alloc(h, &ops.ksq, nq)) ||
+        (rc = dev_alloc(h, &dS, nz2)) || (rc = dev_alloc(h, &ops.HinvT, (size_t)nq * nz2)) ||
+        (rc = dev_alloc(h, &ops.PinvT, (size_t)(nq + 1) * nz2)))
+        return fail(rc);
+    struct Up { void* d; const void* s; size_t b; } ups[] = {
+        {ops.D1, D1s.data(), nz2 * 8}, {ops.D2, D2s.data(), nz2 * 8}, {ops.wh, wh.data(), (size_t)nz * 8},
+        {ops.zw, h->zwts.data(), (size_t)nz * 8}, {ops.S0, S0.data(), (size_t)nz * 8},
+        {ops.Sn, Sn.data(), (size_t)nz * 8}, {ops.W1T, W1T.data(), nz2 * 8},
+        {ops.xw, xw.data(), (size_t)g.nxhp * 8}, {ops.yw, yw.data(), (size_t)c.ny * 8},
+        {ops.ksq, ksq.data(), (size_t)nq * 8}, {dS, S.data(), nz2 * 8}};
+    for (auto& u : ups)
+        if ((rc = upload(h, u.d, u.s, u.b))) return fail(rc);
+
+    // state and work buffers
+    const size_t se = spec_elems(c), pe = phys_elems(c);
+    double2** specs[] = {&h->U, &h->V, &h->W, &h->P, &h->SU, &h->SV, &h->SW, &h->US, &h->VS, &h->WS, &h->PHI};
+    for (auto p : specs)
+        if ((rc = dev_alloc(h, p, se))) return fail(rc);
+    if ((rc = dev_alloc(h, &h->GP, (size_t)4 * g.nm))) return fail(rc);
+    for (int f = 0; f < 6; ++f)
+        if ((rc = dev_alloc(h, &h->phys[f], pe))) return fail(rc);
+    h->fft.tmp_fields = 6;
+    if ((rc = dev_alloc(h, &h->fft.tmp, 6 * se))) return fail(rc);
+    if ((rc = dev_alloc(h, &h->d_pi, 1))) return fail(rc);
+    h->red_blocks = 152 * 4;
+    if ((rc = dev_alloc(h, &h->d_red, (size_t)4 * h->red_blocks))) return fail(rc);
+    if ((rc = dev_alloc(h, &h->d_out, 16))) return fail(rc);
+    if ((rc = dev_alloc(h, &h->d_flag, 4))) return fail(rc);
+
+    cudaError_t e;
+    if ((e = fft_setup(h->fft, g)) != cudaSuccess) { cuda_fail(h, e, "fft_setup"); return fail(DNS3D_E_CUDA); }
+    if ((e = prepare_step_kernels(g)) != cudaSuccess) { cuda_fail(h, e, "prepare"); return fail(DNS3D_E_CUDA); }
+
+    // per-mode operator inverses
+    if (cudaMemsetAsync(h->d_flag, 0, 4 * sizeof(int), h->stream) != cudaSuccess) return fail(DNS3D_E_CUDA);
+    if ((e = build_inverses(g, dS, ops.wh, helm_f, ops.ksq, nq, ops.HinvT, ops.PinvT, h->d_flag, h->stream)))
+        return fail(DNS3D_E_CUDA);
+    int info = 0;
+    if (cudaMemcpyAsync(&info, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+        return fail(DNS3D_E_CUDA);
+    if (info != 0) return fail(DNS3D_E_SINGULAR);
+
+    // step parameters
+    StepParams& sp = h->sp;
+    sp.dt = c.dt;
+    sp.cn_fac = c.use_crank_nicolson ? 0.5 * c.dt / c.re : 0.0;
+    sp.helm_f = helm_f;
+    sp.forcing_scale = (double)c.nx * (double)c.ny;
+    sp.dealias = c.use_dealias_23_rule;
+    sp.kx_max = (c.nx / 2) * 2 / 3;
+    sp.ky_max = (c.ny / 2) * 2 / 3;
+    sp.weak_form = c.use_weak_form_divergence;
+    PIParams& pp = h->pp;
+    pp.method = c.flow_control_method;
+    pp.istart = c.istart;
+    pp.update_freq = c.controller_update_freq > 0 ? c.controller_update_freq : 1;
+    pp.target_dpdx = c.target_pressure_gradient;
+    pp.target_ub = c.target_bulk_velocity;
+    pp.gain = c.controller_gain;
+    pp.re = c.re;
+    pp.dt = c.dt;
+    double wsum = 0.0;
+    for (int k = 0; k < nz; ++k) wsum += h->zwts[k];
+    pp.inv_nxny_wsum = 1.0 / ((double)c.nx * (double)c.ny * wsum);
+
+    if ((rc = dns3d_initialize_fields(h))) return fail(rc);
+    *out = h;
+    return DNS3D_OK;
+}
+
+int dns3d_destroy(dns3d_handle* h) {
+    if (!h) return DNS3D_E_INVALID;
+    cudaSetDevice(h->cfg.device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    release(h);
+    delete h;
+    return DNS3D_OK;
+}
+
+int dns3d_initialize_fields(dns3d_handle* h) {
+    if (!h) return DNS3D_E_INVALID;
+    std::vector<double> u, v, w;
+    initial_fields(h->cfg, h->zpts, u, v, w);
+    std::vector<double> p(u.size(), 0.0);
+    const size_t pl = (size_t)h->cfg.nx * h->cfg.ny;
+    std::vector<double> zero(pl, 0.0);
+    dns3d_pi_state pi{};
+    pi.current_pressure_gradient = h->cfg.target_pressure_gradient;  // 3D:623
+    pi.avg_pressure_gradient = h->cfg.target_pressure_gradient;      // 3D:635
+    int rc = dns3d_set_state(h, u.data(), v.data(), w.data(), p.data(), zero.data(), zero.data(),
+                             zero.data(), zero.data(), &pi);
+    if (rc) return rc;
+    h->step = 0;
+    h->time = 0.0;
+    return DNS3D_OK;
+}
+
+int dns3d_set_state(dns3d_handle* h, const double* u, const double* v, const double* w,
+                    const double* p_total, const double* gpx_w1, const double* gpx_w2,
+                    const double* gpy_w1, const double* gpy_w2, const dns3d_pi_state* pi) {
+    if (!h) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    const GridDev& g = h->g;
+    const size_t pe = phys_elems(h->cfg);
+    const double* src[4] = {u, v, w, p_total};
+    double2* dst[4] = {h->U, h->V, h->W, h->P};
+    int rc;
+    for (int f = 0; f < 4; ++f) {
+        if (!src[f]) continue;
+        if ((rc = upload(h, h->phys[f], src[f], pe * sizeof(double)))) return rc;
+        RFields ph{}; ph.p[0] = h->phys[f];
+        Fields sp{}; sp.p[0] = dst[f];
+        CK(h, fft_r2c(h->fft, g, ph, sp, 1, g.nz, h->stream));
+    }
+    const double* gps[4] = {gpx_w1, gpx_w2, gpy_w1, gpy_w2};
+    const bool any_gp = gpx_w1 || gpx_w2 || gpy_w1 || gpy_w2;
+    const size_t pl = (size_t)g.nx * g.ny;
+    if (any_gp) {
+        for (int i = 0; i < 4; ++i) {
+            if (!gps[i]) continue;
+            if ((rc = upload(h, h->phys[4], gps[i], pl * sizeof(double)))) return rc;
+            RFields ph{}; ph.p[0] = h->phys[4];
+            Fields sp{}; sp.p[0] = h->GP + (size_t)i * g.nm;
+            CK(h, fft_r2c(h->fft, g, ph, sp, 1, 1, h->stream));
+        }
+    } else if (p_total) {
+        CK(h, launch_grad_walls(g, h->ops, h->P, h->GP, h->stream));
+    }
+    if (pi) {
+        if ((rc = upload(h, h->d_pi, pi, sizeof(*pi)))) return rc;
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    return DNS3D_OK;
+}
+
+int dns3d_get_state(dns3d_handle* h, double* u, double* v, double* w, double* p_total,
+                    double* gpx_w1, double* gpx_w2, double* gpy_w1, double* gpy_w2,
+                    dns3d_pi_state* pi) {
+    if (!h) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    const GridDev& g = h->g;
+    const size_t pe = phys_elems(h->cfg);
+    double* dst[4] = {u, v, w, p_total};
+    double2* src[4] = {h->U, h->V, h->W, h->P};
+    for (int f = 0; f < 4; ++f) {
+        if (!dst[f]) continue;
+        Fields sp{}; sp.p[0] = src[f];
+        RFields ph{}; ph.p[0] = h->phys[f];
+        CK(h, fft_c2r(h->fft, g, sp, ph, 1, g.nz, h->stream));
+        CK(h, cudaMemcpyAsync(dst[f], h->phys[f], pe * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    double* gps[4] = {gpx_w1, gpx_w2, gpy_w1, gpy_w2};
+    const size_t pl = (size_t)g.nx * g.ny;
+    for (int i = 0; i < 4; ++i) {
+        if (!gps[i]) continue;
+        Fields sp{}; sp.p[0] = h->GP + (size_t)i * g.nm;
+        RFields ph{}; ph.p[0] = h->phys[4];
+        CK(h, fft_c2r(h->fft, g, sp, ph, 1, 1, h->stream));
+        CK(h, cudaMemcpyAsync(gps[i], h->phys[4], pl * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    if (pi) CK(h, cudaMemcpyAsync(pi, h->d_pi, sizeof(*pi), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return DNS3D_OK;
+}
+
+int dns3d_set_clock(dns3d_handle* h, int step, double time) {
+    if (!h) return DNS3D_E_INVALID;
+    h->step = step;
+    h->time = time;
+    return DNS3D_OK;
+}
+
+int dns3d_compute_source_terms(dns3d_handle* h) {
+    if (!h) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    return run_source_terms(h);
+}
+int dns3d_viscous_step(dns3d_handle* h) {
+    if (!h) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    return run_viscous(h);
+}
+int dns3d_solve_pressure(dns3d_handle* h) {
+    if (!h) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    return run_pressure(h);
+}
+int dns3d_pressure_correction(dns3d_handle* h) {
+    if (!h) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    return run_correction(h);
+}
+int dns3d_apply_boundary_conditions(dns3d_handle* h) {
+    if (!h) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    return run_bc(h);
+}
+
+int dns3d_step(dns3d_handle* h, int nsteps) {
+    if (!h || nsteps < 0) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    if (nsteps == 0) return DNS3D_OK;
+    if (!h->graph) {
+        cudaGraph_t graph = nullptr;
+        CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = run_step_body(h);
+        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&h->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            h->graph = nullptr;
+            return cuda_fail(h, e, "cudaGraphInstantiate");
+        }
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        CK(h, cudaGraphLaunch(h->graph, h->stream));
+        h->step += 1;
+        h->time += h->cfg.dt;  // 3D:296
+    }
+    return DNS3D_OK;
+}
+
+int dns3d_synchronize(dns3d_handle* h) {
+    if (!h) return DNS3D_E_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    return DNS3D_OK;
+}
+
+int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out) {
+    if (!h || !out) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    const GridDev& g = h->g;
+    const dns3d_config& c = h->cfg;
+    Fields sp{};
+    sp.p[0] = h->U; sp.p[1] = h->V; sp.p[2] = h->W;
+    RFields ph{};
+    for (int f = 0; f < 3; ++f) ph.p[f] = h->phys[f];
+    CK(h, fft_c2r(h->fft, g, sp, ph, 3, g.nz, h->stream));
+    CK(h, launch_diag_reduce(g, h->ops, h->phys[0], h->phys[1], h->phys[2], h->d_red, h->red_blocks, h->d_out,
+                             h->stream));
+    // check_divergence_3d: max |DX u + DY v + Dz w| in physical space
+    // (the divergence spectrum goes to the last FFT scratch slot, which a
+    // one-field c2r does not touch, so diagnostics never clobber step state)
+    double2* div = h->fft.tmp + (size_t)5 * spec_elems(c);
+    CK(h, launch_divergence(g, h->ops, h->U, h->V, h->W, div, h->stream));
+    Fields dv{}; dv.p[0] = div;
+    RFields dp{}; dp.p[0] = h->phys[3];
+    CK(h, fft_c2r(h->fft, g, dv, dp, 1, g.nz, h->stream));
+    CK(h, launch_maxabs(g, h->phys[3], phys_elems(c), h->d_red, h->red_blocks, h->d_out + 4, h->stream));
+    double res[5];
+    dns3d_pi_state pi{};
+    CK(h, cudaMemcpyAsync(res, h->d_out, sizeof(res), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(&pi, h->d_pi, sizeof(pi), cudaMemcpyDeviceToHost, h->stream));
+    std::vector<double2> mean(g.nz);
+    CK(h, cudaMemcpy2DAsync(mean.data(), sizeof(double2), h->U, (size_t)g.nm * sizeof(double2), sizeof(double2),
+                            g.nz, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    const double ybar = 2.0;
+    const double fac = (c.xlen / c.nx) * (c.ylen / c.ny) * (ybar / 2.0);
+    out->umax = res[0];
+    out->vmax = res[1];
+    out->wmax = res[2];
+    out->energy = res[3] * fac / (c.xlen * c.ylen * ybar);  // 3D:2110-2128
+    out->max_div = res[4];
+    out->dpdx = pi.current_pressure_gradient;
+    out->dpdx_avg = pi.avg_pressure_gradient;
+    double vol = 0.0;
+    for (int k = 0; k < g.nz; ++k) vol += mean[k].x * h->zwts[k];
+    out->u_bulk = vol * h->pp.inv_nxny_wsum;
+    out->time = h->time;
+    out->step = h->step;
+    if (!std::isfinite(out->energy) || !std::isfinite(out->umax) || !std::isfinite(out->max_div))
+        return DNS3D_E_NONFINITE;
+    return DNS3D_OK;
+}
+
+const char* dns3d_strerror(int code) {
+    switch (code) {
+        case DNS3D_OK: return "ok";
+        case DNS3D_E_INVALID: return "invalid argument or configuration";
+        case DNS3D_E_OOM: return "device memory allocation failed";
+        case DNS3D_E_SINGULAR: return "singular per-mode operator";
+        case DNS3D_E_NONFINITE: return "non-finite value in the state";
+        case DNS3D_E_CUDA: return "CUDA error";
+        case DNS3D_E_UNSUPPORTED: return "unsupported grid size or option";
+        case DNS3D_E_IO: return "input file could not be read or parsed";
+        case DNS3D_E_NODEVICE: return "no CUDA device";
+        default: return "unknown error";
+    }
+}
+
+const char* dns3d_last_error(dns3d_handle* h) {
+    if (!h) return "";
+    return h->err.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+// Internal declarations shared by the translation units of libdns3d_gpu.so.
+//
+// Data layout in HBM (all FP64):
+//   spectral field : double2 [nz][ny][nxhp]   (nxhp = nx/2+1, FFTW r2c order,
+//                    kx fastest; the same memory order as the reference's
+//                    complex(nxhp,ny) planes, DNS_pressure_BC_3D.f90:1442)
+//   physical field : double  [nz][ny][nx]     (Fortran u(nx,ny,nz))
+//   z-operators    : double  [nz][nz] row-major, A[z][z'] (applied as A . f(:))
+//   per-mode inverses : double [nq][nz][nz] stored TRANSPOSED, Ainv^T[q][z'][z],
+//                    so that threads indexed by the output row z read
+//                    consecutive addresses for a fixed z'.
+// A "mode" m = ky*nxhp + kx indexes one complex column of length nz; a plane
+// holds nm = nxhp*ny modes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/dns3d_capi.h"
+
+namespace dns3d {
+
+constexpr int kMaxFields = 8;
+constexpr int kMaxStages = 12;
+
+struct Fields {
+    double2* p[kMaxFields];
+};
+struct RFields {
+    double* p[kMaxFields];
+};
+
+// Radix schedule of one complex FFT length (Stockham autosort, radices 4/2/3).
+struct FftPlan1D {
+    int n;
+    int nstages;
+    int radix[kMaxStages];
+};
+
+FftPlan1D make_plan(int n);
+bool fft_length_supported(int n);
+
+// Grid constants passed by value to kernels.
+struct GridDev {
+    int nx, ny, nz, nxh, nxhp, nm;
+    int nkyu;            // ny/2 + 1 unique |ky|
+    double inv_nxny;     // 1/(nx*ny), c2r normalisation
+};
+
+// Maps a spectral mode (ky, kx) to the index of its per-mode operator: the
+// operators depend on kx^2 + ky^2 only, so ky and ny-ky share one.
+__host__ __device__ inline int mode_q(int ky, int kx, int ny, int nxhp) {
+    int kya = ky <= ny / 2 ? ky : ny - ky;
+    return kya * nxhp + kx;
+}
+
+// ---------------------------------------------------------------- fft.cu
+// Batched real 2D transforms over planes of the listed fields.  c2r keeps
+// FFTW's semantics for non-Hermitian input: inverse c2c along y, then a 1D
+// c2r along x that ignores Im of the kx=0 and kx=nx/2 entries; output scaled
+// by 1/(nx*ny) (fftw3_dns_module.f90:127-130).
+struct FftCtx {
+    FftPlan1D py;        // length ny complex
+    FftPlan1D px2;       // length nx/2 complex (packed real transform)
+    double2* tw_ny;      // e^{-2 pi i t/ny}, t < ny
+    double2* tw_nx2;     // e^{-2 pi i t/(nx/2)}
+    double2* tw_nx;      // e^{-2 pi i t/nx}, t < nx/2+1
+    double2* tmp;        // spectral scratch for nf fields
+    int tmp_fields;
+};
+cudaError_t fft_setup(FftCtx& ctx, const GridDev& g);
+void fft_release(FftCtx& ctx);
+// spec[f] (spectral, read only) -> phys[f]; uses ctx.tmp (nf <= tmp_fields).
+cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, int nf,
+                    int nplanes, cudaStream_t s);
+// phys[f] -> spec[f].
+cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf,
+                    int nplanes, cudaStream_t s);
+
+// ---------------------------------------------------------------- step.cu
+struct StepParams {
+    double dt;
+    double cn_fac;        // 0.5*dt/Re if Crank-Nicolson else 0 (3D:1374)
+    double helm_f;        // theta*dt/Re (3D:1459)
+    double forcing_scale; // nx*ny: physical constant -> (0,0) coefficient
+    int dealias;          // use_dealias_23_rule
+    int kx_max, ky_max;   // 2/3 limits (3D:1169-1170)
+    int weak_form;        // use_weak_form_divergence
+};
+
+struct Ops {
+    double* D1;      // (2/ybar) d1             [nz][nz]
+    double* D2;      // (2/ybar)^2 d2           [nz][nz]
+    double* wh;      // zwts * ybar/2           [nz]
+    double* zw;      // zwts                    [nz]
+    double* S0;      // helm_f * S[z][0]        [nz]
+    double* Sn;      // helm_f * S[z][nz-1]     [nz]
+    double* W1T;     // zwts[m]*(2/ybar)*d1(m,z), weak-form vertical part, [z][m]
+    double* xw;      // [nxhp]
+    double* yw;      // [ny]
+    double* ksq;     // xsq+ysq per unique q     [nq]
+    double* HinvT;   // Helmholtz inverses, transposed  [nq][nz][nz]
+    double* PinvT;   // Poisson inverses, transposed    [nq+1][nz][nz]; q=nq is the pinned (0,0)
+    int nq;
+};
+
+struct PIParams {
+    int method;
+    int istart;
+    int update_freq;
+    double target_dpdx, target_ub, gain, re, dt;
+    double inv_nxny_wsum;   // 1/(nx*ny*sum(zwts))
+};
+
+// Sets the dynamic shared-memory limits of the kernels below (call once per
+// grid, outside stream capture).
+cudaError_t prepare_step_kernels(const GridDev& g);
+cudaError_t launch_pi_update(const GridDev& g, const Ops& ops, const PIParams& pp,
+                             const double2* U, dns3d_pi_state* pi, cudaStream_t s);
+cudaError_t launch_vorticity(const GridDev& g, const Ops& ops, const double2* U,
+                             const double2* V, const double2* W, double2* OX, double2* OY,
+                             double2* OZ, cudaStream_t s);
+cudaError_t launch_products(const GridDev& g, RFields in6, RFields out3, cudaStream_t s);
+cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& sp,
+                           Fields F, Fields Src, const double2* GP,
+                           const dns3d_pi_state* pi, Fields Out, cudaStream_t s);
+cudaError_t launch_pressure(const GridDev& g, const Ops& ops, const StepParams& sp,
+                            const double2* US, const double2* VS, const double2* WS,
+                            double2* PHI, cudaStream_t s);
+cudaError_t launch_correction(const GridDev& g, const Ops& ops, const StepParams& sp,
+                              const double2* US, const double2* VS, const double2* WS,
+                              const double2* PHI, double2* U, double2* V, double2* W,
+                              double2* P, double2* GP, cudaStream_t s);
+cudaError_t launch_apply_bc(const GridDev& g, double2* U, double2* V, double2* W,
+                            cudaStream_t s);
+cudaError_t launch_divergence(const GridDev& g, const Ops& ops, const double2* U,
+                              const double2* V, const double2* W, double2* DIV,
+                              cudaStream_t s);
+cudaError_t launch_grad_walls(const GridDev& g, const Ops& ops, const double2* P,
+                              double2* GP, cudaStream_t s);
+// Reductions over physical fields.  out[0..3] = max|u|, max|v|, max|w|,
+// sum 0.5(u^2+v^2+w^2) zwts[k]; partial buffer must hold 4*nblocks doubles.
+cudaError_t launch_diag_reduce(const GridDev& g, const Ops& ops, const double* u,
+                               const double* v, const double* w, double* partial,
+                               int nblocks, double* out, cudaStream_t s);
+cudaError_t launch_maxabs(const GridDev& g, const double* f, size_t n, double* partial,
+                          int nblocks, double* out, cudaStream_t s);
+cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaStream_t s);
+
+// ---------------------------------------------------------------- setup.cu
+// Build the per-mode operator inverses on the device by Gauss-Jordan with
+// partial pivoting.  info[0] receives 1 + index of the first singular matrix.
+cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh,
+                           double helm_f, const double* ksq, int nq, double* HinvT,
+                           double* PinvT, int* info, cudaStream_t s);
+
+// ---------------------------------------------------------------- lgl.cpp
+void lgl_nodes_weights(int n, std::vector<double>& x, std::vector<double>& w);
+void lgl_diff_matrix(const std::vector<double>& x, bool guard, std::vector<double>& d);
+
+// ---------------------------------------------------------------- namelist.cpp
+int read_namelist_file(const char* path, dns3d_config* cfg);
+
+}  // namespace dns3d

@@ -1,0 +1,148 @@
+// Per-mode operator inverses, built once per handle on the device.
+//
+// The reference assembles and factors an nz x nz system for every (kx, ky)
+// mode at every call: the Helmholtz operator (solve_viscous_helmholtz,
+// DNS_pressure_BC_3D.f90:1464-1505) and the Galerkin Poisson operator
+// (solve_pressure_3d_standard, 3D:1680-1714) with zgesv.  Both depend on the
+// mode only through k^2 = xsq(kx) + ysq(ky) and are constant in time, so here
+// each distinct operator is inverted once (Gauss-Jordan, partial pivoting,
+// FP64, one CTA per matrix in shared memory) and every step applies the
+// inverse as one matrix-vector product per mode.
+//
+//   Helmholtz, q < nq:  A = f S + diag((1 + f k^2) w ybar/2), rows 1 and nz
+//                       replaced by identity rows (3D:1480-1502)
+//   Poisson,   q < nq:  P = -S - diag(k^2 w ybar/2)              (3D:1684-1692)
+//   Poisson,   q = nq:  the pinned (0,0) operator: -S with row 1 and column 1
+//                       zeroed and P(1,1) = 1                     (3D:1702-1711)
+// Outputs are stored transposed: out[q][z'][z] = inverse[z][z'].
+#include "dns3d_internal.cuh"
+
+namespace dns3d {
+namespace {
+
+// In-place Gauss-Jordan inversion of a[n][n] (shared memory) with partial
+// pivoting; the row interchanges are undone as column interchanges at the end.
+// Returns false if a zero pivot was met.
+__device__ bool gj_invert(double* a, int n, int* perm, double* colk, int* flag) {
+    __shared__ int piv_row;
+    if (threadIdx.x == 0) *flag = 0;
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        if (threadIdx.x < 32) {
+            double best = -1.0;
+            int bi = k;
+            for (int i = k + threadIdx.x; i < n; i += 32) {
+                const double v = fabs(a[i * n + k]);
+                if (v > best) { best = v; bi = i; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (threadIdx.x == 0) {
+                piv_row = bi;
+                perm[k] = bi;
+                if (!(best > 0.0)) *flag = 1;
+            }
+        }
+        __syncthreads();
+        if (*flag) return false;
+        const int p = piv_row;
+        if (p != k) {
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                const double t = a[k * n + j];
+                a[k * n + j] = a[p * n + j];
+                a[p * n + j] = t;
+            }
+            __syncthreads();
+        }
+        const double pivinv = 1.0 / a[k * n + k];
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) a[k * n + j] = (j == k) ? pivinv : a[k * n + j] * pivinv;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) colk[i] = a[i * n + k];
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int i = t / n, j = t - i * n;
+            if (i == k) continue;
+            const double base = (j == k) ? 0.0 : a[t];
+            a[t] = base - a[k * n + j] * colk[i];
+        }
+        __syncthreads();
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        const int p = perm[k];
+        if (p != k) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const double t = a[i * n + k];
+                a[i * n + k] = a[i * n + p];
+                a[i * n + p] = t;
+            }
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_build_inverses(int nz, const double* __restrict__ S,
+                                                        const double* __restrict__ wh, double helm_f,
+                                                        const double* __restrict__ ksq, int nq,
+                                                        double* __restrict__ HinvT,
+                                                        double* __restrict__ PinvT, int* info) {
+    extern __shared__ double sm[];
+    double* a = sm;
+    double* colk = sm + nz * nz;
+    int* perm = reinterpret_cast<int*>(colk + nz);
+    __shared__ int flag;
+    const int job = blockIdx.x;  // [0, nq): Helmholtz q;  [nq, 2nq+1): Poisson q - nq
+    const bool helm = job < nq;
+    const int q = helm ? job : job - nq;
+    double* out = helm ? HinvT + (size_t)q * nz * nz : PinvT + (size_t)q * nz * nz;
+    if (!helm && q == 0) {  // k^2 = 0 unpinned Poisson operator is singular and never used
+        for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) out[t] = 0.0;
+        return;
+    }
+    for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) {
+        const int i = t / nz, j = t - i * nz;
+        double v;
+        if (helm) {
+            const double k2 = ksq[q];
+            v = helm_f * S[t];
+            if (i == j) v += (1.0 + helm_f * k2) * wh[i];
+            if (i == 0 || i == nz - 1) v = (i == j) ? 1.0 : 0.0;
+        } else if (q < nq) {
+            v = -S[t];
+            if (i == j) v -= ksq[q] * wh[i];
+        } else {
+            v = -S[t];
+            if (i == 0 || j == 0) v = (i == 0 && j == 0) ? 1.0 : 0.0;
+        }
+        a[t] = v;
+    }
+    __syncthreads();
+    const bool ok = gj_invert(a, nz, perm, colk, &flag);
+    if (!ok) {
+        if (threadIdx.x == 0) atomicCAS(info, 0, job + 1);
+        return;
+    }
+    for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) {
+        const int zp = t / nz, z = t - zp * nz;
+        out[t] = a[z * nz + zp];
+    }
+}
+
+}  // namespace
+
+cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh, double helm_f,
+                           const double* ksq, int nq, double* HinvT, double* PinvT, int* info,
+                           cudaStream_t s) {
+    const int nz = g.nz;
+    const size_t sm = (size_t)nz * nz * sizeof(double) + nz * sizeof(double) + nz * sizeof(int);
+    if (sm > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_build_inverses, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e) return e;
+    k_build_inverses<<<2 * nq + 1, 256, sm, s>>>(nz, S, wh, helm_f, ksq, nq, HinvT, PinvT, info);
+    return cudaGetLastError();
+}
+
+}  // namespace dns3d

@@ -1,0 +1,619 @@
+// Spectral-resident kernels of the time step (FP64).
+//
+// The reference works in physical space and round-trips every derivative
+// through r2c/c2r per plane (compute_derivatives_3d, DNS_pressure_BC_3D.f90:
+// 2321-2407).  For a real field f with spectrum F those round trips are the
+// exact spectral maps
+//   DX(F) = i xw(kx) F,  except the kx = nx/2 column, which the c2r discards
+//   DY(F) = i yw(ky) F,  except (ky = ny/2, kx in {0, nx/2}), likewise
+//   Dz(F) = (2/ybar) d1 . F(:)   (the physical d1 column product commutes with
+//                                  the x-y transforms)
+// so the state (u, v, w, p_total) is kept as spectra and only the nonlinear
+// product is formed in physical space.
+//
+// "Mode-tile" kernels: one CTA owns TC consecutive modes m = ky*nxhp + kx and
+// all nz levels of them, so z-contractions (nz x nz operator times a column)
+// and the per-mode solves run out of shared memory with coalesced HBM access
+// along m.
+#include "dns3d_internal.cuh"
+
+namespace dns3d {
+namespace {
+
+__device__ __forceinline__ double2 i_times(double a, double2 f) {  // (i a) * f
+    return make_double2(-a * f.y, a * f.x);
+}
+
+struct ModeInfo {
+    int ky, kx;
+    double ax, ay;  // DX / DY multipliers with the Nyquist rules applied
+};
+
+__device__ __forceinline__ ModeInfo mode_info(const GridDev& g, int m, const double* __restrict__ xw,
+                                              const double* __restrict__ yw) {
+    ModeInfo mi;
+    mi.ky = m / g.nxhp;
+    mi.kx = m - mi.ky * g.nxhp;
+    mi.ax = (mi.kx == g.nxh) ? 0.0 : __ldg(&xw[mi.kx]);
+    mi.ay = (mi.ky == g.ny / 2 && (mi.kx == 0 || mi.kx == g.nxh)) ? 0.0 : __ldg(&yw[mi.ky]);
+    return mi;
+}
+
+// tile[f][z][c] <- field f at (z, m0 + c); zero beyond nm.
+__device__ __forceinline__ void load_tile(double2* tile, const double2* __restrict__ src,
+                                          const GridDev& g, int m0, int tc) {
+    for (int t = threadIdx.x; t < g.nz * tc; t += blockDim.x) {
+        const int z = t / tc, c = t - z * tc;
+        const int m = m0 + c;
+        tile[t] = (m < g.nm) ? src[(size_t)z * g.nm + m] : make_double2(0.0, 0.0);
+    }
+}
+
+// ------------------------------------------------------------------ PI / forcing
+// update_pressure_gradient_3d (3D:2488-2549) called with the namelist istart
+// (3D:1118), and calculate_bulk_velocity_3d (3D:2434-2464) from the (0,0) mode:
+// sum_ij u(i,j,k) = Re U[k][0][0].
+__global__ void k_pi_update(GridDev g, const double* __restrict__ zw, PIParams pp,
+                            const double2* __restrict__ U, dns3d_pi_state* pi) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (pp.method == 1) {
+        pi->current_pressure_gradient = pp.target_dpdx;
+        return;
+    }
+    if (pp.method != 2) return;
+    if (pp.istart % pp.update_freq != 0) return;
+    double vol = 0.0;
+    for (int k = 0; k < g.nz; ++k) vol += U[(size_t)k * g.nm].x * zw[k];
+    const double ub = vol * pp.inv_nxny_wsum;
+    pi->current_bulk_velocity = ub;
+    const double err = pp.target_ub - ub;
+    pi->bulk_velocity_error = err;
+    const double kp = pp.gain, ki = 0.05 * pp.gain;
+    const double unclamped = 3.0 / pp.re + kp * err + ki * pi->bulk_velocity_error_integral;
+    const double clamped = fmax(0.0, fmin(10.0, unclamped));
+    if (fabs(clamped - unclamped) < 1.0e-12) {
+        if (pp.istart <= pp.update_freq)
+            pi->bulk_velocity_error_integral += err * pp.dt;
+        else
+            pi->bulk_velocity_error_integral += 0.5 * pp.dt * (pi->bulk_velocity_error_prev + err);
+    }
+    pi->bulk_velocity_error_prev = err;
+    pi->current_pressure_gradient = clamped;
+    pi->pressure_gradient_sum += clamped;
+    pi->pressure_gradient_count += 1;
+    pi->avg_pressure_gradient = pi->pressure_gradient_sum / (double)pi->pressure_gradient_count;
+}
+
+// ------------------------------------------------------------------ vorticity
+// omega = (wy - vz, uz - wx, vx - uy)  (3D:1077-1079), spectrally.
+__global__ void __launch_bounds__(256) k_vorticity(GridDev g, Ops ops, const double2* __restrict__ U,
+                                                   const double2* __restrict__ V,
+                                                   const double2* __restrict__ W,
+                                                   double2* __restrict__ OX, double2* __restrict__ OY,
+                                                   double2* __restrict__ OZ, int tc) {
+    extern __shared__ double2 sm[];
+    double2* tu = sm;
+    double2* tv = sm + g.nz * tc;
+    const int m0 = blockIdx.x * tc;
+    load_tile(tu, U, g, m0, tc);
+    load_tile(tv, V, g, m0, tc);
+    __syncthreads();
+    const int nz = g.nz;
+    for (int t = threadIdx.x; t < nz * tc; t += blockDim.x) {
+        const int z = t / tc, c = t - z * tc;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        const double* __restrict__ drow = ops.D1 + (size_t)z * nz;
+        double2 du = make_double2(0.0, 0.0), dv = make_double2(0.0, 0.0);
+        for (int zp = 0; zp < nz; ++zp) {
+            const double d = __ldg(&drow[zp]);
+            const double2 a = tu[zp * tc + c], b = tv[zp * tc + c];
+            du.x = fma(d, a.x, du.x);
+            du.y = fma(d, a.y, du.y);
+            dv.x = fma(d, b.x, dv.x);
+            dv.y = fma(d, b.y, dv.y);
+        }
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const size_t o = (size_t)z * g.nm + m;
+        const double2 w = W[o];
+        const double2 u = tu[t], v = tv[t];
+        const double2 wy = i_times(mi.ay, w), wx = i_times(mi.ax, w);
+        const double2 vx = i_times(mi.ax, v), uy = i_times(mi.ay, u);
+        OX[o] = make_double2(wy.x - dv.x, wy.y - dv.y);
+        OY[o] = make_double2(du.x - wx.x, du.y - wx.y);
+        OZ[o] = make_double2(vx.x - uy.x, vx.y - uy.y);
+    }
+}
+
+// ------------------------------------------------------------------ products
+// S = u x omega (3D:1085-1095) on physical fields: in = u,v,w,ox,oy,oz.
+__global__ void k_products(RFields in, RFields out, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double u = in.p[0][i], v = in.p[1][i], w = in.p[2][i];
+        const double ox = in.p[3][i], oy = in.p[4][i], oz = in.p[5][i];
+        out.p[0][i] = v * oz - w * oy;
+        out.p[1][i] = w * ox - u * oz;
+        out.p[2][i] = u * oy - v * ox;
+    }
+}
+
+// ------------------------------------------------------------------ viscous step
+// viscous_step_3d (3D:1285-1332) + solve_viscous_helmholtz (3D:1425-1521) for
+// all three components of a mode tile:
+//   R   = F + dt*(mask(S) + dpdx*[comp==u, mode (0,0)]) + cn*(D2.F - k^2 F)
+//   b_k = R_k w_k ybar/2,   k interior: b_k -= H(k,1) bc1 + H(k,nz) bc2
+//   b_1 = bc1, b_nz = bc2;   F* = A_q^{-1} b   (A_q: rows 1, nz are identity,
+//   columns kept, so the wall data enters twice, as in the reference)
+// bc: u -> -dt dp/dx|wall, v -> -dt dp/dy|wall (previous total pressure,
+// 3D:1325-1326), w -> 0 (3D:1328).
+__global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams sp, Fields F,
+                                                 Fields Src, const double2* __restrict__ GP,
+                                                 const dns3d_pi_state* __restrict__ pi, Fields Out,
+                                                 int tc) {
+    extern __shared__ double2 sm[];
+    const int nz = g.nz;
+    const int tsz = nz * tc;
+    double2* tf = sm;             // [3][nz][tc]
+    double2* tb = sm + 3 * tsz;   // [3][nz][tc]
+    const int m0 = blockIdx.x * tc;
+    for (int comp = 0; comp < 3; ++comp) {
+        load_tile(tf + comp * tsz, F.p[comp], g, m0, tc);
+        load_tile(tb + comp * tsz, Src.p[comp], g, m0, tc);
+    }
+    __syncthreads();
+    const double dpdx = pi->current_pressure_gradient;
+    for (int t = threadIdx.x; t < 3 * tsz; t += blockDim.x) {
+        const int comp = t / tsz;
+        const int r = t - comp * tsz;
+        const int z = r / tc, c = r - z * tc;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+        const double2* col = tf + comp * tsz;
+        double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
+        if (comp < 2) {
+            const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
+            const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+            bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
+            bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
+        }
+        double2 b;
+        if (z == 0) {
+            b = bc1;
+        } else if (z == nz - 1) {
+            b = bc2;
+        } else {
+            double2 s = tb[t];
+            if (sp.dealias) {  // apply_dealias_truncation (3D:1163-1193)
+                const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
+                if (kx > sp.kx_max || kyi > sp.ky_max) s = make_double2(0.0, 0.0);
+            }
+            if (comp == 0 && m == 0) s.x += dpdx * sp.forcing_scale;  // 3D:1123-1145
+            const double2 f = col[z * tc + c];
+            double2 rr = make_double2(f.x + sp.dt * s.x, f.y + sp.dt * s.y);
+            if (sp.cn_fac != 0.0) {  // add_explicit_diffusion (3D:1355-1381)
+                const double* __restrict__ drow = ops.D2 + (size_t)z * nz;
+                double2 lap = make_double2(0.0, 0.0);
+                for (int zp = 0; zp < nz; ++zp) {
+                    const double d = __ldg(&drow[zp]);
+                    const double2 a = col[zp * tc + c];
+                    lap.x = fma(d, a.x, lap.x);
+                    lap.y = fma(d, a.y, lap.y);
+                }
+                const double ksq = __ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+                lap.x -= ksq * f.x;
+                lap.y -= ksq * f.y;
+                rr.x += sp.cn_fac * lap.x;
+                rr.y += sp.cn_fac * lap.y;
+            }
+            const double whz = __ldg(&ops.wh[z]);
+            const double s0 = __ldg(&ops.S0[z]), sn = __ldg(&ops.Sn[z]);
+            b.x = rr.x * whz - (s0 * bc1.x + sn * bc2.x);
+            b.y = rr.y * whz - (s0 * bc1.y + sn * bc2.y);
+        }
+        tb[t] = b;  // each element is read and written by its own thread only
+    }
+    __syncthreads();
+    // F* = A_q^{-1} b, one matrix per mode, applied to the three components.
+    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
+        const int c = t / nz, z = t - c * nz;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+        const double* __restrict__ Ainv = ops.HinvT + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * nz * nz;
+        double2 a0 = make_double2(0.0, 0.0), a1 = a0, a2 = a0;
+        for (int zp = 0; zp < nz; ++zp) {
+            const double h = __ldg(&Ainv[(size_t)zp * nz + z]);
+            const double2 b0 = tb[zp * tc + c], b1 = tb[tsz + zp * tc + c], b2 = tb[2 * tsz + zp * tc + c];
+            a0.x = fma(h, b0.x, a0.x); a0.y = fma(h, b0.y, a0.y);
+            a1.x = fma(h, b1.x, a1.x); a1.y = fma(h, b1.y, a1.y);
+            a2.x = fma(h, b2.x, a2.x); a2.y = fma(h, b2.y, a2.y);
+        }
+        const size_t o = (size_t)z * g.nm + m;
+        Out.p[0][o] = a0;
+        Out.p[1][o] = a1;
+        Out.p[2][o] = a2;
+    }
+}
+
+// ------------------------------------------------------------------ pressure
+// solve_pressure_3d_standard (3D:1654-1733): b = (DX u* + DY v* + Dz w*)/dt *
+// w ybar/2; or _weak_form (3D:1749-1835): b = (-(DX u* + DY v*) w ybar/2 -
+// sum_m d1(m,k) w*_m zwts_m (2/ybar)) / dt.  Mode (0,0): b_1 = 0 and the
+// pinned operator (3D:1702-1711).  phi = P_q^{-1} b.
+__global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams sp,
+                                                  const double2* __restrict__ US,
+                                                  const double2* __restrict__ VS,
+                                                  const double2* __restrict__ WS,
+                                                  double2* __restrict__ PHI, int tc) {
+    extern __shared__ double2 sm[];
+    const int nz = g.nz;
+    const int tsz = nz * tc;
+    double2* tw = sm;        // w* tile
+    double2* tb = sm + tsz;  // rhs tile
+    const int m0 = blockIdx.x * tc;
+    load_tile(tw, WS, g, m0, tc);
+    __syncthreads();
+    const double inv_dt = 1.0 / sp.dt;
+    const double* __restrict__ A = sp.weak_form ? ops.W1T : ops.D1;
+    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
+        const int z = t / tc, c = t - z * tc;
+        const int m = m0 + c;
+        if (m >= g.nm) { tb[t] = make_double2(0.0, 0.0); continue; }
+        const double* __restrict__ drow = A + (size_t)z * nz;
+        double2 dz = make_double2(0.0, 0.0);
+        for (int zp = 0; zp < nz; ++zp) {
+            const double d = __ldg(&drow[zp]);
+            const double2 a = tw[zp * tc + c];
+            dz.x = fma(d, a.x, dz.x);
+            dz.y = fma(d, a.y, dz.y);
+        }
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const size_t o = (size_t)z * g.nm + m;
+        const double2 hx = i_times(mi.ax, US[o]);
+        const double2 hy = i_times(mi.ay, VS[o]);
+        const double whz = __ldg(&ops.wh[z]);
+        double2 b;
+        if (!sp.weak_form) {
+            b.x = ((hx.x + hy.x) + dz.x) * inv_dt * whz;
+            b.y = ((hx.y + hy.y) + dz.y) * inv_dt * whz;
+        } else {
+            b.x = (-(hx.x + hy.x) * whz - dz.x) * inv_dt;
+            b.y = (-(hx.y + hy.y) * whz - dz.y) * inv_dt;
+        }
+        if (m == 0 && z == 0) b = make_double2(0.0, 0.0);
+        tb[t] = b;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
+        const int c = t / nz, z = t - c * nz;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+        const int q = (m == 0) ? ops.nq : mode_q(ky, kx, g.ny, g.nxhp);
+        const double* __restrict__ Ainv = ops.PinvT + (size_t)q * nz * nz;
+        double2 a = make_double2(0.0, 0.0);
+        for (int zp = 0; zp < nz; ++zp) {
+            const double h = __ldg(&Ainv[(size_t)zp * nz + z]);
+            const double2 bb = tb[zp * tc + c];
+            a.x = fma(h, bb.x, a.x);
+            a.y = fma(h, bb.y, a.y);
+        }
+        PHI[(size_t)z * g.nm + m] = a;
+    }
+}
+
+// ------------------------------------------------------------------ correction
+// pressure_correction_3d (3D:1903-1929): u = u* - dt grad(phi), p += phi,
+// grad_p_prev = grad(p_total); only its wall planes are consumed (3D:1325-1326).
+__global__ void __launch_bounds__(256) k_correction(GridDev g, Ops ops, StepParams sp,
+                                                    const double2* __restrict__ US,
+                                                    const double2* __restrict__ VS,
+                                                    const double2* __restrict__ WS,
+                                                    const double2* __restrict__ PHI,
+                                                    double2* __restrict__ U, double2* __restrict__ V,
+                                                    double2* __restrict__ W, double2* __restrict__ P,
+                                                    double2* __restrict__ GP, int tc) {
+    extern __shared__ double2 sm[];
+    const int nz = g.nz;
+    const int tsz = nz * tc;
+    double2* tp = sm;
+    const int m0 = blockIdx.x * tc;
+    load_tile(tp, PHI, g, m0, tc);
+    __syncthreads();
+    const double dt = sp.dt;
+    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
+        const int z = t / tc, c = t - z * tc;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        const double* __restrict__ drow = ops.D1 + (size_t)z * nz;
+        double2 dz = make_double2(0.0, 0.0);
+        for (int zp = 0; zp < nz; ++zp) {
+            const double d = __ldg(&drow[zp]);
+            const double2 a = tp[zp * tc + c];
+            dz.x = fma(d, a.x, dz.x);
+            dz.y = fma(d, a.y, dz.y);
+        }
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const size_t o = (size_t)z * g.nm + m;
+        const double2 ph = tp[t];
+        const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
+        const double2 us = US[o], vs = VS[o], ws = WS[o];
+        U[o] = make_double2(us.x - dt * px.x, us.y - dt * px.y);
+        V[o] = make_double2(vs.x - dt * py.x, vs.y - dt * py.y);
+        W[o] = make_double2(ws.x - dt * dz.x, ws.y - dt * dz.y);
+        double2 p = P[o];
+        p.x += ph.x;
+        p.y += ph.y;
+        P[o] = p;
+        if (z == 0 || z == nz - 1) {
+            const int wall = (z == 0) ? 0 : 1;
+            GP[(size_t)wall * g.nm + m] = i_times(mi.ax, p);
+            GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, p);
+        }
+    }
+}
+
+// Wall-plane gradients of p_total alone (used when the state is set).
+__global__ void k_grad_walls(GridDev g, Ops ops, const double2* __restrict__ P, double2* __restrict__ GP) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= g.nm) return;
+    const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+    for (int wall = 0; wall < 2; ++wall) {
+        const double2 p = P[(size_t)(wall ? g.nz - 1 : 0) * g.nm + m];
+        GP[(size_t)wall * g.nm + m] = i_times(mi.ax, p);
+        GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, p);
+    }
+}
+
+// apply_boundary_conditions_3d (3D:1953-1972): wall planes := 0 (the wall
+// arrays are all zero, 3D:987-999), i.e. spectral planes k=1, nz := 0.
+__global__ void k_apply_bc(GridDev g, double2* U, double2* V, double2* W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * g.nm) return;
+    const int wall = i / g.nm, m = i - wall * g.nm;
+    const size_t o = (size_t)(wall ? g.nz - 1 : 0) * g.nm + m;
+    const double2 z = make_double2(0.0, 0.0);
+    U[o] = z;
+    V[o] = z;
+    W[o] = z;
+}
+
+// Divergence spectrum DX u + DY v + Dz w (compute_divergence_3d, 3D:1858-1879).
+__global__ void __launch_bounds__(256) k_divergence(GridDev g, Ops ops, const double2* __restrict__ U,
+                                                    const double2* __restrict__ V,
+                                                    const double2* __restrict__ W,
+                                                    double2* __restrict__ DIV, int tc) {
+    extern __shared__ double2 sm[];
+    const int nz = g.nz;
+    double2* tw = sm;
+    const int m0 = blockIdx.x * tc;
+    load_tile(tw, W, g, m0, tc);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nz * tc; t += blockDim.x) {
+        const int z = t / tc, c = t - z * tc;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        const double* __restrict__ drow = ops.D1 + (size_t)z * nz;
+        double2 dz = make_double2(0.0, 0.0);
+        for (int zp = 0; zp < nz; ++zp) {
+            const double d = __ldg(&drow[zp]);
+            const double2 a = tw[zp * tc + c];
+            dz.x = fma(d, a.x, dz.x);
+            dz.y = fma(d, a.y, dz.y);
+        }
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const size_t o = (size_t)z * g.nm + m;
+        const double2 hx = i_times(mi.ax, U[o]);
+        const double2 hy = i_times(mi.ay, V[o]);
+        DIV[o] = make_double2((hx.x + hy.x) + dz.x, (hx.y + hy.y) + dz.y);
+    }
+}
+
+// ------------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Per-block partials of max|u|, max|v|, max|w| and sum 0.5|u|^2 zwts[k].
+__global__ void __launch_bounds__(256) k_diag_partial(GridDev g, const double* __restrict__ zw,
+                                                      const double* __restrict__ u,
+                                                      const double* __restrict__ v,
+                                                      const double* __restrict__ w,
+                                                      double* __restrict__ partial) {
+    const size_t n = (size_t)g.nx * g.ny * g.nz;
+    const size_t plane = (size_t)g.nx * g.ny;
+    double mu = 0.0, mv = 0.0, mw = 0.0, e = 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double a = u[i], b = v[i], c = w[i];
+        mu = fmax(mu, fabs(a));
+        mv = fmax(mv, fabs(b));
+        mw = fmax(mw, fabs(c));
+        e += 0.5 * (a * a + b * b + c * c) * __ldg(&zw[i / plane]);
+    }
+    __shared__ double red[4][8];
+    mu = warp_max(mu); mv = warp_max(mv); mw = warp_max(mw); e = warp_sum(e);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { red[0][wid] = mu; red[1][wid] = mv; red[2][wid] = mw; red[3][wid] = e; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            mu = fmax(mu, red[0][k]); mv = fmax(mv, red[1][k]); mw = fmax(mw, red[2][k]); e += red[3][k];
+        }
+        partial[4 * blockIdx.x + 0] = mu;
+        partial[4 * blockIdx.x + 1] = mv;
+        partial[4 * blockIdx.x + 2] = mw;
+        partial[4 * blockIdx.x + 3] = e;
+    }
+}
+
+__global__ void k_diag_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+    if (threadIdx.x != 0) return;
+    double mu = 0.0, mv = 0.0, mw = 0.0, e = 0.0;
+    for (int b = 0; b < nb; ++b) {
+        mu = fmax(mu, partial[4 * b]);
+        mv = fmax(mv, partial[4 * b + 1]);
+        mw = fmax(mw, partial[4 * b + 2]);
+        e += partial[4 * b + 3];
+    }
+    out[0] = mu; out[1] = mv; out[2] = mw; out[3] = e;
+}
+
+__global__ void __launch_bounds__(256) k_maxabs_partial(const double* __restrict__ f, size_t n,
+                                                        double* __restrict__ partial) {
+    double m = 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) m = fmax(m, fabs(f[i]));
+    __shared__ double red[8];
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = fmax(m, red[k]);
+        partial[blockIdx.x] = m;
+    }
+}
+
+__global__ void k_max_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+    if (threadIdx.x != 0) return;
+    double m = 0.0;
+    for (int b = 0; b < nb; ++b) m = fmax(m, partial[b]);
+    out[0] = m;
+}
+
+__global__ void k_nonfinite(const double2* __restrict__ f, size_t n, int* flag) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    int bad = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double2 a = f[i];
+        if (!isfinite(a.x) || !isfinite(a.y)) bad = 1;
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+int tile_cols(const GridDev& g, int narrays) {
+    // Largest TC in {32,16,8,4} whose tiles fit ~96 KB and that still gives
+    // at least two CTAs per SM on 152 SMs; never below 4.
+    int tc = 32;
+    while (tc > 4 && ((size_t)narrays * g.nz * tc * sizeof(double2) > 96 * 1024 ||
+                      (g.nm + tc - 1) / tc < 304))
+        tc >>= 1;
+    return tc;
+}
+
+template <typename K>
+cudaError_t set_smem(K kern, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+}  // namespace
+
+cudaError_t prepare_step_kernels(const GridDev& g) {
+    cudaError_t e;
+    if ((e = set_smem(k_vorticity, 2 * (size_t)g.nz * tile_cols(g, 2) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_viscous, 6 * (size_t)g.nz * tile_cols(g, 6) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_pressure, 2 * (size_t)g.nz * tile_cols(g, 2) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_correction, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_divergence, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
+    return cudaSuccess;
+}
+
+cudaError_t launch_pi_update(const GridDev& g, const Ops& ops, const PIParams& pp, const double2* U,
+                             dns3d_pi_state* pi, cudaStream_t s) {
+    k_pi_update<<<1, 32, 0, s>>>(g, ops.zw, pp, U, pi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vorticity(const GridDev& g, const Ops& ops, const double2* U, const double2* V,
+                             const double2* W, double2* OX, double2* OY, double2* OZ, cudaStream_t s) {
+    const int tc = tile_cols(g, 2);
+    const size_t sm = 2 * (size_t)g.nz * tc * sizeof(double2);
+    k_vorticity<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, U, V, W, OX, OY, OZ, tc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_products(const GridDev& g, RFields in6, RFields out3, cudaStream_t s) {
+    const size_t n = (size_t)g.nx * g.ny * g.nz;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_products<<<blocks, 256, 0, s>>>(in6, out3, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F,
+                           Fields Src, const double2* GP, const dns3d_pi_state* pi, Fields Out,
+                           cudaStream_t s) {
+    const int tc = tile_cols(g, 6);
+    const size_t sm = 6 * (size_t)g.nz * tc * sizeof(double2);
+    k_viscous<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, F, Src, GP, pi, Out, tc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                            const double2* VS, const double2* WS, double2* PHI, cudaStream_t s) {
+    const int tc = tile_cols(g, 2);
+    const size_t sm = 2 * (size_t)g.nz * tc * sizeof(double2);
+    k_pressure<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, US, VS, WS, PHI, tc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_correction(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                              const double2* VS, const double2* WS, const double2* PHI, double2* U,
+                              double2* V, double2* W, double2* P, double2* GP, cudaStream_t s) {
+    const int tc = tile_cols(g, 1);
+    const size_t sm = (size_t)g.nz * tc * sizeof(double2);
+    k_correction<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, US, VS, WS, PHI, U, V, W, P, GP, tc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_bc(const GridDev& g, double2* U, double2* V, double2* W, cudaStream_t s) {
+    k_apply_bc<<<(2 * g.nm + 255) / 256, 256, 0, s>>>(g, U, V, W);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_divergence(const GridDev& g, const Ops& ops, const double2* U, const double2* V,
+                              const double2* W, double2* DIV, cudaStream_t s) {
+    const int tc = tile_cols(g, 1);
+    const size_t sm = (size_t)g.nz * tc * sizeof(double2);
+    k_divergence<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, U, V, W, DIV, tc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grad_walls(const GridDev& g, const Ops& ops, const double2* P, double2* GP,
+                              cudaStream_t s) {
+    k_grad_walls<<<(g.nm + 255) / 256, 256, 0, s>>>(g, ops, P, GP);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diag_reduce(const GridDev& g, const Ops& ops, const double* u, const double* v,
+                               const double* w, double* partial, int nblocks, double* out,
+                               cudaStream_t s) {
+    k_diag_partial<<<nblocks, 256, 0, s>>>(g, ops.zw, u, v, w, partial);
+    k_diag_final<<<1, 32, 0, s>>>(partial, nblocks, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_maxabs(const GridDev& g, const double* f, size_t n, double* partial, int nblocks,
+                          double* out, cudaStream_t s) {
+    (void)g;
+    k_maxabs_partial<<<nblocks, 256, 0, s>>>(f, n, partial);
+    k_max_final<<<1, 32, 0, s>>>(partial, nblocks, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaStream_t s) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_nonfinite<<<blocks, 256, 0, s>>>(f, n, flag);
+    return cudaGetLastError();
+}
+
+}  // namespace dns3d

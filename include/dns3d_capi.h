@@ -1,0 +1,155 @@
+/*
+ * dns3d_capi.h -- C-ABI of the GB300 (sm_103a) 3D channel-flow time step.
+ *
+ * Drop-in for the time loop of DNS_pressure_BC_3D.f90 (chandc/F90_DNS).  The
+ * reference step is five argument-less internal subroutines that share state
+ * through host-associated arrays (DNS_pressure_BC_3D.f90:108-178, called at
+ * :314-326).  Here that state lives on the GPU inside an opaque handle; the
+ * five subroutines become five entry points with the same names and order, so
+ * a Fortran driver binds them with ISO_C_BINDING and keeps its loop.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: DNS3D_OK (0) or a DNS3D_E_*
+ *    code.  Nothing here exits, prints or throws (the reference `stop`s, e.g.
+ *    DNS_pressure_BC_3D.f90:837-875, 1506, 1715-1718).
+ *  - Host arrays are caller-owned, contiguous, Fortran order u(nx,ny,nz)
+ *    (i fastest), i.e. C u[k][j][i]; k = 1 is the wall z = -1.  The library
+ *    copies in and out; device state is library-owned and stays resident.
+ *  - One host thread per handle.  Distinct handles are independent.
+ */
+#ifndef DNS3D_CAPI_H
+#define DNS3D_CAPI_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DNS3D_OK 0
+#define DNS3D_E_INVALID 1      /* bad argument or configuration value        */
+#define DNS3D_E_OOM 2          /* device allocation failed                   */
+#define DNS3D_E_SINGULAR 3     /* a per-mode operator could not be inverted  */
+#define DNS3D_E_NONFINITE 4    /* NaN/Inf detected in the state              */
+#define DNS3D_E_CUDA 5         /* CUDA runtime / launch error                */
+#define DNS3D_E_UNSUPPORTED 6  /* grid size or option not supported          */
+#define DNS3D_E_IO 7           /* input file could not be read / parsed      */
+#define DNS3D_E_NODEVICE 8     /* no CUDA device                              */
+
+#define DNS3D_PREC_FP64 0      /* plain FP64 path                            */
+
+/* Namelist parameters of read_input_3d (DNS_pressure_BC_3D.f90:559-568,
+ * defaults 571-603).  alpha, beta and ybar are derived (3D:740-742), the
+ * read-but-unused ta, cs, u00, wavlen, cgstol, iform, iles are not carried. */
+typedef struct dns3d_config {
+    int nx, ny, nz;                    /* &grid nx_input, ny_input, nz_input */
+    int istart, nsteps, nwrt, restart_write_freq;  /* &time_control */
+    double dt;
+    double re, xlen, ylen, u_centerline;            /* &simulation */
+    int use_crank_nicolson;
+    int flow_control_method;                        /* &flow_control: 1 or 2 */
+    double target_pressure_gradient, target_bulk_velocity, controller_gain;
+    int controller_update_freq;
+    int enable_perturbations;                       /* &perturbations */
+    double perturbation_amplitude;
+    int zero_w_perturbations, use_analytical_perturbations;
+    int analytical_mode_x, analytical_mode_y;
+    int use_weak_form_divergence;                   /* &pressure_solver */
+    int use_dealias_23_rule;                        /* &computational */
+    /* 1 (default) = the reference's differentiation_matrix, which zeroes any
+     * entry whose Lagrange denominator is <= 1e-15 (lgl_module.f90:247-251);
+     * for nz >= 58 that is every off-diagonal entry and the pinned Poisson
+     * mode is singular, so dns3d_create fails with DNS3D_E_SINGULAR, as the
+     * reference stops in zgesv (3D:1715-1718).  0 = the same Lagrange formula
+     * without that cutoff.  Read from &computational as an extension key. */
+    int lgl_dmatrix_guard;
+    int precision;                                  /* DNS3D_PREC_*        */
+    int device;                                     /* CUDA device ordinal */
+} dns3d_config;
+
+/* PI controller globals (DNS_pressure_BC_3D.f90:75-89). */
+typedef struct dns3d_pi_state {
+    double current_pressure_gradient;
+    double current_bulk_velocity;
+    double bulk_velocity_error;
+    double bulk_velocity_error_integral;
+    double bulk_velocity_error_prev;
+    double pressure_gradient_sum;
+    double avg_pressure_gradient;
+    int pressure_gradient_count;
+    int pad_;
+} dns3d_pi_state;
+
+/* Observables of output_diagnostics_3d (3D:2094-2146) and check_divergence_3d
+ * (3D:2171-2190). */
+typedef struct dns3d_diag {
+    double umax, vmax, wmax, energy;
+    double u_bulk, dpdx, dpdx_avg;
+    double max_div;
+    double time;
+    int step;
+    int pad_;
+} dns3d_diag;
+
+typedef struct dns3d_handle dns3d_handle;
+
+/* Defaults of read_input_3d (3D:571-603). */
+int dns3d_config_defaults(dns3d_config* cfg);
+
+/* Parse a Fortran namelist input file with the eight groups of read_input_3d
+ * (3D:606-616).  Unknown keys are ignored; missing groups keep defaults. */
+int dns3d_config_read_namelist(const char* path, dns3d_config* cfg);
+
+/* Grid/spectral setup, LGL operators, per-mode operators, device allocation
+ * (setup_grid_3d 3D:728, setup_spectral_3d 3D:769, allocate_arrays_3d 3D:831,
+ * setup_fftw3_plans_dns fftw3_dns_module.f90:60).  The state starts at the
+ * initial condition of initialize_fields_3d (3D:909-962). */
+int dns3d_create(const dns3d_config* cfg, dns3d_handle** out);
+int dns3d_destroy(dns3d_handle* h);
+
+/* initialize_fields_3d (3D:909-962) incl. the analytical perturbation
+ * (perturbation_analytical_simple.f90:24-155); resets step and time. */
+int dns3d_initialize_fields(dns3d_handle* h);
+
+/* Copy state in/out.  Any pointer may be NULL (that field is left as is /
+ * not returned).  gp*_w1/_w2 are the wall planes k=1 and k=nz of
+ * grad_p_prev_x/_y (nx*ny each), the only part of those arrays the step
+ * reads (3D:1325-1326).  In dns3d_set_state, if all four are NULL and
+ * p_total is given, the wall gradients are recomputed from p_total (the
+ * relation pressure_correction_3d leaves behind, 3D:1923). */
+int dns3d_set_state(dns3d_handle* h, const double* u, const double* v, const double* w,
+                    const double* p_total, const double* gpx_w1, const double* gpx_w2,
+                    const double* gpy_w1, const double* gpy_w2, const dns3d_pi_state* pi);
+int dns3d_get_state(dns3d_handle* h, double* u, double* v, double* w, double* p_total,
+                    double* gpx_w1, double* gpx_w2, double* gpy_w1, double* gpy_w2,
+                    dns3d_pi_state* pi);
+int dns3d_set_clock(dns3d_handle* h, int step, double time);
+
+/* The five subroutines of the time loop, in the reference's order
+ * (DNS_pressure_BC_3D.f90:314-326). */
+int dns3d_compute_source_terms(dns3d_handle* h);   /* 3D:1032-1148 */
+int dns3d_viscous_step(dns3d_handle* h);           /* 3D:1285-1521 */
+int dns3d_solve_pressure(dns3d_handle* h);         /* 3D:1631-1835 */
+int dns3d_pressure_correction(dns3d_handle* h);    /* 3D:1903-1929 */
+int dns3d_apply_boundary_conditions(dns3d_handle* h); /* 3D:1953-1972 */
+
+/* nsteps passes of the loop body (3D:286-361 without IO): time += dt and the
+ * five subroutines, fused and replayed as a CUDA graph. */
+int dns3d_step(dns3d_handle* h, int nsteps);
+
+/* Wait for all work queued on the handle's stream. */
+int dns3d_synchronize(dns3d_handle* h);
+
+/* output_diagnostics_3d observables plus check_divergence_3d's max |div u|. */
+int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out);
+
+/* Device bytes held by a handle for a given config (admission control). */
+int dns3d_footprint_bytes(const dns3d_config* cfg, unsigned long long* bytes);
+
+const char* dns3d_strerror(int code);
+
+/* Last CUDA error text recorded on the handle ("" if none). */
+const char* dns3d_last_error(dns3d_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DNS3D_CAPI_H */

@@ -1,0 +1,167 @@
+"""GPU parity: the sm_103a library against the CPU oracle (FP64).
+
+Bar: max |GPU - oracle| <= 1e-10 x (velocity scale max(|u|,|v|,|w|)) per
+velocity component over the 50-step horizon, p_total relative to max|p|.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from f90_dns_gb300 import ChannelDNS, Dns3DError, config_from
+from f90_dns_gb300.capi import DNS3D_E_SINGULAR
+from f90_dns_gb300.workloads import WORKLOADS
+from oracle import dns3d_ref as ref
+from tests.helpers import oracle_config, velocity_errors
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+C1 = WORKLOADS["channel_32x32x33_re180_dpdx"]
+
+
+def gpu_run(wl, nsteps, stage_api=False):
+    with ChannelDNS(config_from(wl)) as d:
+        if stage_api:
+            for _ in range(nsteps):
+                d.compute_source_terms_3d()
+                d.viscous_step_3d()
+                d.solve_pressure_3d()
+                d.pressure_correction_3d()
+                d.apply_boundary_conditions_3d()
+        else:
+            d.step(nsteps)
+        st = d.get_state()
+        diag = d.diagnostics()
+    return st, diag
+
+
+def oracle_run(wl, nsteps):
+    cfg = oracle_config(wl)
+    g, st, hist = ref.run(cfg, nsteps, record_every=nsteps)
+    return cfg, g, st, hist
+
+
+def check(wl, nsteps, tol=TOL):
+    gst, gdiag = gpu_run(wl, nsteps)
+    cfg, g, st, hist = oracle_run(wl, nsteps)
+    err = velocity_errors(gst, st)
+    assert max(err["u"], err["v"], err["w"]) <= tol, err
+    assert err["p_total"] <= tol, err
+    d = hist[-1]
+    for k in ("umax", "vmax", "wmax", "energy"):
+        assert abs(getattr(gdiag, k) - d[k]) <= tol * max(abs(d[k]), d["umax"]), (k, getattr(gdiag, k), d[k])
+    assert abs(gdiag.dpdx - d["dpdx"]) <= 1e-12 * max(1.0, abs(d["dpdx"]))
+    return gst, st, err
+
+
+def test_c1_50_steps_matches_oracle(built_lib):
+    check(C1, 50)
+
+
+def test_stage_api_equals_fused_step(built_lib):
+    a, _ = gpu_run(C1, 5, stage_api=True)
+    b, _ = gpu_run(C1, 5, stage_api=False)
+    for k in ("u", "v", "w", "p_total", "gpx_w1", "gpy_w2"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_deterministic(built_lib):
+    a, _ = gpu_run(C1, 10)
+    b, _ = gpu_run(C1, 10)
+    for k in ("u", "v", "w", "p_total"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("key", ["standard", "weak_form"])
+def test_reference_trace(built_lib, key):
+    """The reference's own captured run (5 printed digits per step)."""
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_traces.json")) as f:
+        tr = json.load(f)
+    p = tr["params"]
+    wl = dict(nx=32, ny=32, nz=17, re=500.0, dt=0.002, xlen=2 * ref.PI, ylen=ref.PI, u_centerline=1.5,
+              use_crank_nicolson=True, flow_control_method=1, target_pressure_gradient=0.006,
+              enable_perturbations=True, use_analytical_perturbations=True, perturbation_amplitude=0.01,
+              analytical_mode_x=1, analytical_mode_y=1, use_weak_form_divergence=(key == "weak_form"))
+    assert p["nz"] == wl["nz"]
+    with ChannelDNS(config_from(wl)) as d:
+        d0 = d.diagnostics()
+        assert d0.max_div < 1e-13
+        for row in tr[key]["steps"]:
+            d.step(1)
+            dg = d.diagnostics()
+            assert dg.step == row["step"]
+            for k in ("umax", "vmax", "wmax", "energy", "dpdx"):
+                want = row[k]
+                assert abs(getattr(dg, k) - want) <= 0.51e-4 * abs(want) + 1e-300, (row["step"], k, getattr(dg, k), want)
+
+
+@pytest.mark.parametrize("variant", [
+    dict(use_dealias_23_rule=False),
+    dict(use_weak_form_divergence=True, perturbation_amplitude=0.001),
+    dict(use_crank_nicolson=False),
+    dict(flow_control_method=2, target_bulk_velocity=2.0 / 3.0, perturbation_amplitude=0.05,
+         analytical_mode_x=2),
+    dict(flow_control_method=2, target_bulk_velocity=0.7, istart=3),
+    dict(analytical_mode_y=0),
+])
+def test_variants_match_oracle(built_lib, variant):
+    wl = dict(C1)
+    wl.update(variant)
+    check(wl, 20)
+
+
+@pytest.mark.parametrize("nx,ny,nz", [(48, 96, 17), (96, 48, 25), (64, 32, 33)])
+def test_radix3_and_rectangular_grids(built_lib, nx, ny, nz):
+    wl = dict(C1, nx=nx, ny=ny, nz=nz, analytical_mode_x=2, analytical_mode_y=1, perturbation_amplitude=0.05)
+    check(wl, 10)
+
+
+def test_nyquist_content_matches_oracle(built_lib):
+    """Random state with energy at kx = nx/2 and ky = ny/2: exercises FFTW's
+    c2r treatment of the non-Hermitian derivative spectra."""
+    wl = dict(C1, nx=16, ny=12, nz=17)
+    cfg = oracle_config(wl)
+    g = ref.setup_grid(cfg)
+    rng = np.random.default_rng(7)
+    shp = (g.nz, g.ny, g.nx)
+    u, v, w, p = (rng.standard_normal(shp) * s for s in (0.3, 0.2, 0.1, 1.0))
+    for a in (u, v, w):
+        a[0] = 0.0
+        a[-1] = 0.0
+    st = ref.initial_state(cfg, g)
+    st.u, st.v, st.w, st.p_total = u.copy(), v.copy(), w.copy(), p.copy()
+    st.gpx, st.gpy, st.gpz = ref.derivatives(g, p)
+    with ChannelDNS(config_from(wl)) as d:
+        d.set_state(u=u, v=v, w=w, p_total=p)
+        d.step(2)
+        gst = d.get_state()
+    for _ in range(2):
+        ref.step(cfg, g, st)
+    err = velocity_errors(gst, st)
+    assert max(err["u"], err["v"], err["w"]) <= TOL, err
+
+
+def test_guarded_dmatrix_is_singular_at_nz65(built_lib):
+    wl = dict(C1, nz=65, lgl_dmatrix_guard=True)
+    with pytest.raises(Dns3DError) as ei:
+        ChannelDNS(config_from(wl))
+    assert ei.value.code == DNS3D_E_SINGULAR
+
+
+def test_unguarded_nz65_matches_oracle(built_lib):
+    wl = dict(C1, nx=16, ny=16, nz=65, lgl_dmatrix_guard=False, flow_control_method=2,
+              target_bulk_velocity=2.0 / 3.0, perturbation_amplitude=0.05, analytical_mode_x=2)
+    check(wl, 10)
+
+
+def test_state_roundtrip(built_lib):
+    wl = dict(C1, nx=32, ny=16, nz=17)
+    rng = np.random.default_rng(3)
+    shp = (17, 16, 32)
+    u = rng.standard_normal(shp)
+    with ChannelDNS(config_from(wl)) as d:
+        d.set_state(u=u)
+        st = d.get_state()
+    assert np.max(np.abs(st["u"] - u)) < 1e-13
