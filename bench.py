@@ -1,0 +1,312 @@
+"""Benchmark: grid-point-steps/s of the 3D channel time step on GB300.
+
+Workload: the single 128x128x65 channel (Re 180, dt 0.002, PI control to
+U_bulk = 2/3, analytical perturbation amplitude 0.05, mode (2,1), 2/3 filter,
+Crank-Nicolson), FP64 plain path.  A "step" is one pass of the reference's
+time-loop body (DNS_pressure_BC_3D.f90:286-361 without IO).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value`` : device-timed throughput with the state resident in HBM (K graph
+            replays bracketed by CUDA events on the library's stream).
+``e2e``   : the same metric through the C-ABI with host-resident state: every
+            step uploads u, v, w, p_total from pinned host memory, advances one
+            step and downloads u, v, w, p_total and the diagnostics line.
+With N > 1 (torchrun), every rank advances its own independent replica.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import signal
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = "channel_128x128x65_re180_pi"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return ws, rank, local, dist
+    return 1, 0, local, None
+
+
+def _barrier(dist):
+    if dist is not None:
+        import torch
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def _max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.send_signal(signal.SIGTERM)
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_flops(wl: dict) -> dict:
+    """FP64 flops per step of the spectral-resident algorithm, by kernel.
+
+    Per complex mode column, one nz x nz real operator applied to it costs
+    4 nz^2 flops.  Per step: vorticity 2 (D.u, D.v), viscous 6 (3 x D2, 3 x
+    Helmholtz inverse), pressure 2 (D.w*, Poisson inverse), correction 1
+    (D.phi): 11 operator applications = 44 nz^2 Nm.  Transforms: 9 real 2D
+    FFTs per z-plane at 2.5 n log2 n flops (n = nx ny).
+    """
+    nx, ny, nz = wl["nx"], wl["ny"], wl["nz"]
+    nm = (nx // 2 + 1) * ny
+    op = 4.0 * nz * nz * nm
+    n = nx * ny
+    fft = 2.5 * n * math.log2(n) * nz
+    return {"vorticity": 2 * op, "viscous_helmholtz": 6 * op, "pressure_poisson": 2 * op,
+            "pressure_correction": 1 * op, "fft_total": 9 * fft, "z_total": 11 * op,
+            "total": 11 * op + 9 * fft}
+
+
+def cpu_sample(wl_name: str, steps: int, threads: int) -> dict:
+    """Time the CPU oracle (numpy restatement) on `steps` steps of the workload
+    in a subprocess with the given BLAS/OpenMP thread count."""
+    env = dict(os.environ)
+    for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        env[k] = str(threads)
+    code = (
+        "import json,sys,time; sys.path.insert(0, %r)\n"
+        "from f90_dns_gb300.workloads import WORKLOADS\n"
+        "from oracle import dns3d_ref as ref\n"
+        "wl = WORKLOADS[%r]\n"
+        "names = set(ref.Config.__dataclass_fields__)\n"
+        "cfg = ref.Config(**{k: v for k, v in wl.items() if k in names})\n"
+        "g = ref.setup_grid(cfg); st = ref.initial_state(cfg, g)\n"
+        "ref.step(cfg, g, st)\n"
+        "t = time.perf_counter()\n"
+        "for _ in range(%d): ref.step(cfg, g, st)\n"
+        "dt = time.perf_counter() - t\n"
+        "print(json.dumps({'seconds': dt}))\n" % (ROOT, wl_name, steps))
+    res = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
+    if res.returncode != 0:
+        raise RuntimeError("cpu baseline failed: " + res.stderr[-2000:])
+    sec = json.loads(res.stdout.strip().splitlines()[-1])["seconds"]
+    return {"seconds": sec, "steps": steps}
+
+
+def run_reference(args) -> None:
+    """The reference arm: the CPU restatement of the reference algorithm timed
+    on this host with all its cores available to BLAS (rank 0 only)."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    from f90_dns_gb300.workloads import WORKLOADS, point_count
+    wl = WORKLOADS[args.workload]
+    pts = point_count(wl)
+    threads = os.cpu_count() or 1
+    nsteps = max(2, int(round(args.ref_sample_frac * args.steps)))
+    samp = cpu_sample(args.workload, nsteps, threads)
+    value = pts * samp["steps"] / samp["seconds"]
+    line = {
+        "impl": "reference", "metric": "point-steps/s", "value": value, "unit": "point-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * samp["seconds"] / samp["steps"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "grid": [wl["nx"], wl["ny"], wl["nz"]], "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": "point-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{samp['steps']} steps of {args.workload} after 1 warm-up step: numpy FP64 "
+                                   "restatement of DNS_pressure_BC_3D.f90 (the Fortran reference needs gfortran, "
+                                   "FFTW3 and LAPACK, none of which exist here); BLAS threads = cores"},
+        "e2e": {"value": value, "unit": "point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    ws, rank, local, dist = _dist()
+    from f90_dns_gb300 import ChannelDNS, build, config_from
+    from f90_dns_gb300.capi import measure_fp64_tflops
+    from f90_dns_gb300.workloads import WORKLOADS, point_count
+    if not os.path.exists(os.path.join(ROOT, "f90_dns_gb300", "libdns3d_gpu.so")):
+        build.build()
+    wl = WORKLOADS[args.workload]
+    pts = point_count(wl)
+    cfg = config_from(wl, device=local)
+    d = ChannelDNS(cfg)
+    d.step(args.warmup)
+    d.synchronize()
+
+    sampler = ClockSampler(local)
+    with sampler:
+        _barrier(dist)
+        ms = d.step_timed(args.steps)
+        _barrier(dist)
+    ms = _max_over_ranks(dist, ms)
+    clocks = sampler.summary()
+    value = ws * pts * args.steps / (ms * 1e-3)
+    launches = d.launches_per_step() * args.steps
+
+    # per-kernel device times (eager replay, events between launches)
+    prof = d.profile_kernels(args.profile_steps)
+    total_prof = sum(t for _, t in prof.values())
+    flops = algorithmic_flops(wl)
+    kernels = {k: {"launches": n, "avg_ms": t / n, "share": t / total_prof} for k, (n, t) in prof.items()}
+    dom = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
+    fp64_peak = measure_fp64_tflops(local)
+    roofline = None
+    if dom in flops:
+        ach = flops[dom] / (kernels[dom]["avg_ms"] * 1e-3) / 1e12
+        roofline = {"bound": "fp64", "kernel": dom, "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                    "frac": ach / fp64_peak, "traffic": args.traffic,
+                    "peak_source": "FP64 FMA probe timed in this run (dns3d_measure_fp64_tflops); "
+                                   "MEASURED_PEAKS.json has no FP64 figure",
+                    "algorithmic_flops_per_launch": flops[dom]}
+    step_roof = {"flops_per_step": flops["total"], "t_roof_ms": flops["total"] / (fp64_peak * 1e12) * 1e3,
+                 "t_meas_ms": ms / args.steps,
+                 "frac": (flops["total"] / (fp64_peak * 1e12) * 1e3) / (ms / args.steps)}
+
+    # end-to-end through the C-ABI with host-resident state (pinned buffers)
+    e2e = None
+    if args.e2e_steps > 0:
+        import numpy as np
+        try:
+            import torch
+            pin = lambda: torch.empty(d.shape, dtype=torch.float64, pin_memory=True).numpy()
+        except Exception:  # pragma: no cover
+            pin = lambda: np.empty(d.shape)
+        st = d.get_state(walls=False)
+        bufs = {k: pin() for k in ("u", "v", "w", "p_total")}
+        for k in bufs:
+            bufs[k][...] = st[k]
+        _barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            d.set_state(u=bufs["u"], v=bufs["v"], w=bufs["w"], p_total=bufs["p_total"])
+            d.step(1)
+            d.get_state_into(bufs["u"], bufs["v"], bufs["w"], bufs["p_total"])
+            diag = d.diagnostics()
+        _barrier(dist)
+        el = _max_over_ranks(dist, time.perf_counter() - t0)
+        n = pts * 8
+        e2e = {"value": ws * pts * args.e2e_steps / el, "unit": "point-steps/s",
+               "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n + 80,
+               "steps": args.e2e_steps,
+               "path": "dns3d_set_state(u,v,w,p_total) + dns3d_step(1) + dns3d_get_state + dns3d_diagnostics"}
+        del diag
+
+    cpu = None
+    if rank == 0 and args.cpu_steps > 0:
+        samp = cpu_sample(args.workload, args.cpu_steps, 1)
+        cpu = {"value": pts * samp["steps"] / samp["seconds"], "unit": "point-steps/s", "cores": 1,
+               "kind": "port",
+               "sample": f"{samp['steps']} steps of {args.workload} after 1 warm-up step, numpy FP64 restatement "
+                         "(oracle/dns3d_ref.py), BLAS threads 1"}
+    d.close()
+    if rank == 0:
+        line = {
+            "metric": "point-steps/s", "value": value, "unit": "point-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "grid": [wl["nx"], wl["ny"], wl["nz"]], "precision": "fp64",
+                       "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "working set > 129 MB L2 (per-mode inverses 0.29 GB + fields 0.2 GB), no flush"},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "step_roofline": step_roof,
+            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--profile-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--ref-sample-frac", type=float, default=0.01,
+                    help="reference arm: CPU steps timed per requested step (bounded sample, >= 2)")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu DRAM bytes per launch of the dominant kernel, if captured")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -39,7 +39,8 @@ EXPORTED_SYMBOLS = (
     "dns3d_compute_source_terms", "dns3d_viscous_step", "dns3d_solve_pressure",
     "dns3d_pressure_correction", "dns3d_apply_boundary_conditions", "dns3d_step",
     "dns3d_synchronize", "dns3d_diagnostics", "dns3d_footprint_bytes", "dns3d_strerror",
-    "dns3d_last_error",
+    "dns3d_last_error", "dns3d_step_timed", "dns3d_profile_kernels", "dns3d_launches_per_step",
+    "dns3d_measure_fp64_tflops",
 )
 
 
@@ -86,6 +87,10 @@ class CDiag(C.Structure):
     ]
 
 
+class CKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("launches", C.c_int), ("pad_", C.c_int), ("total_ms", C.c_double)]
+
+
 class Dns3DError(RuntimeError):
     """A non-zero status from the C-ABI (the reference would ``stop`` here)."""
 
@@ -127,6 +132,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_footprint_bytes.argtypes = [C.POINTER(CConfig), C.POINTER(C.c_ulonglong)]
     lib.dns3d_strerror.argtypes = [ip]
     lib.dns3d_strerror.restype = C.c_char_p
+    lib.dns3d_step_timed.argtypes = [hp, ip, C.POINTER(C.c_double)]
+    lib.dns3d_profile_kernels.argtypes = [hp, ip, C.POINTER(CKernelTime), ip, C.POINTER(C.c_int)]
+    lib.dns3d_launches_per_step.argtypes = [hp, C.POINTER(C.c_int)]
+    lib.dns3d_measure_fp64_tflops.argtypes = [ip, C.POINTER(C.c_double)]
     lib.dns3d_last_error.argtypes = [hp]
     lib.dns3d_last_error.restype = C.c_char_p
     for n in EXPORTED_SYMBOLS:
@@ -178,6 +187,14 @@ def config_from(obj, **overrides) -> CConfig:
     for k, v in overrides.items():
         setattr(cfg, k, int(v) if isinstance(v, bool) else v)
     return cfg
+
+
+def measure_fp64_tflops(device: int = 0) -> float:
+    out = C.c_double(0.0)
+    rc = load_library().dns3d_measure_fp64_tflops(int(device), C.byref(out))
+    if rc:
+        raise Dns3DError(rc, "dns3d_measure_fp64_tflops")
+    return float(out.value)
 
 
 def footprint_bytes(cfg: CConfig) -> int:
@@ -264,6 +281,25 @@ class ChannelDNS:
     def step(self, nsteps: int = 1) -> None:
         self._check(self.lib.dns3d_step(self._h, int(nsteps)), "dns3d_step")
 
+    def step_timed(self, nsteps: int) -> float:
+        """Run ``nsteps`` graph replays bracketed by CUDA events; device ms."""
+        ms = C.c_double(0.0)
+        self._check(self.lib.dns3d_step_timed(self._h, int(nsteps), C.byref(ms)), "dns3d_step_timed")
+        return float(ms.value)
+
+    def profile_kernels(self, nsteps: int) -> dict:
+        """Per-kernel {name: (launches, total_ms)} over ``nsteps`` eager loop bodies."""
+        buf = (CKernelTime * 64)()
+        n = C.c_int(0)
+        self._check(self.lib.dns3d_profile_kernels(self._h, int(nsteps), buf, 64, C.byref(n)),
+                    "dns3d_profile_kernels")
+        return {buf[i].name.decode(): (buf[i].launches, buf[i].total_ms) for i in range(n.value)}
+
+    def launches_per_step(self) -> int:
+        n = C.c_int(0)
+        self._check(self.lib.dns3d_launches_per_step(self._h, C.byref(n)), "dns3d_launches_per_step")
+        return int(n.value)
+
     def synchronize(self) -> None:
         self._check(self.lib.dns3d_synchronize(self._h), "dns3d_synchronize")
 
@@ -287,6 +323,16 @@ class ChannelDNS:
         out.update(gp)
         out["pi"] = {n: getattr(pi, n) for n, _ in CPIState._fields_ if n != "pad_"}
         return out
+
+    def get_state_into(self, u=None, v=None, w=None, p_total=None) -> None:
+        """Copy u, v, w, p_total into caller-owned contiguous float64 arrays
+        (e.g. pinned host buffers); None skips a field."""
+        for a in (u, v, w, p_total):
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != self.shape):
+                raise ValueError("arrays must be C-contiguous float64 of shape (nz, ny, nx)")
+        rc = self.lib.dns3d_get_state(self._h, _ptr(u), _ptr(v), _ptr(w), _ptr(p_total),
+                                      None, None, None, None, None)
+        self._check(rc, "dns3d_get_state")
 
     def set_state(self, u=None, v=None, w=None, p_total=None, gpx_w1=None, gpx_w2=None,
                   gpy_w1=None, gpy_w2=None, pi: dict | None = None) -> None:

@@ -39,6 +39,12 @@ struct dns3d_handle {
     double time = 0.0;
     cudaGraphExec_t graph = nullptr;
     std::string err;
+    // profiling marks: an event recorded after every kernel launch
+    bool prof = false;
+    std::vector<cudaEvent_t> ev;
+    std::vector<const char*> evname;
+    size_t nev = 0;
+    int launches = 0;  // kernel launches of the last step body
 };
 
 namespace {
@@ -132,6 +138,22 @@ void initial_fields(const dns3d_config& c, const std::vector<double>& z, std::ve
         for (size_t i = 0; i < pl; ++i) { u[k * pl + i] = 0.0; v[k * pl + i] = 0.0; w[k * pl + i] = 0.0; }
 }
 
+void mark(dns3d_handle* h, const char* name) {
+    h->launches += 1;
+    if (!h->prof) return;
+    if (h->nev == h->ev.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        h->ev.push_back(e);
+        h->evname.push_back(nullptr);
+    }
+    cudaEventRecord(h->ev[h->nev], h->stream);
+    h->evname[h->nev] = name;
+    h->nev += 1;
+}
+
+void fft_hook(void* ctx, const char* name) { mark(static_cast<dns3d_handle*>(ctx), name); }
+
 int upload(dns3d_handle* h, void* dst, const void* src, size_t bytes) {
     CK(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
     return DNS3D_OK;
@@ -140,8 +162,10 @@ int upload(dns3d_handle* h, void* dst, const void* src, size_t bytes) {
 int run_source_terms(dns3d_handle* h) {
     const GridDev& g = h->g;
     CK(h, launch_pi_update(g, h->ops, h->pp, h->U, h->d_pi, h->stream));
+    mark(h, "pi_update");
     // vorticity into the u*,v*,w* buffers (free until the viscous step)
     CK(h, launch_vorticity(g, h->ops, h->U, h->V, h->W, h->US, h->VS, h->WS, h->stream));
+    mark(h, "vorticity");
     Fields spec{};
     spec.p[0] = h->U; spec.p[1] = h->V; spec.p[2] = h->W;
     spec.p[3] = h->US; spec.p[4] = h->VS; spec.p[5] = h->WS;
@@ -151,6 +175,7 @@ int run_source_terms(dns3d_handle* h) {
     RFields prod{};
     for (int f = 0; f < 3; ++f) prod.p[f] = h->phys[f];
     CK(h, launch_products(g, phys, prod, h->stream));
+    mark(h, "products");
     Fields src{};
     src.p[0] = h->SU; src.p[1] = h->SV; src.p[2] = h->SW;
     CK(h, fft_r2c(h->fft, g, prod, src, 3, g.nz, h->stream));
@@ -163,27 +188,34 @@ int run_viscous(dns3d_handle* h) {
     S.p[0] = h->SU; S.p[1] = h->SV; S.p[2] = h->SW;
     O.p[0] = h->US; O.p[1] = h->VS; O.p[2] = h->WS;
     CK(h, launch_viscous(h->g, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->stream));
+    mark(h, "viscous_helmholtz");
     return DNS3D_OK;
 }
 
 int run_pressure(dns3d_handle* h) {
     CK(h, launch_pressure(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->stream));
+    mark(h, "pressure_poisson");
     return DNS3D_OK;
 }
 
 int run_correction(dns3d_handle* h) {
     CK(h, launch_correction(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
                             h->GP, h->stream));
+    mark(h, "pressure_correction");
     return DNS3D_OK;
 }
 
 int run_bc(dns3d_handle* h) {
     CK(h, launch_apply_bc(h->g, h->U, h->V, h->W, h->stream));
+    mark(h, "apply_bc");
     return DNS3D_OK;
 }
 
 int run_step_body(dns3d_handle* h) {
     int rc;
+    h->launches = 0;
+    h->fft.hook = fft_hook;
+    h->fft.hook_ctx = h;
     if ((rc = run_source_terms(h))) return rc;
     if ((rc = run_viscous(h))) return rc;
     if ((rc = run_pressure(h))) return rc;
@@ -194,6 +226,8 @@ int run_step_body(dns3d_handle* h) {
 void release(dns3d_handle* h) {
     if (!h) return;
     if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (cudaEvent_t e : h->ev) cudaEventDestroy(e);
+    h->ev.clear();
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     fft_release(h->fft);
@@ -552,6 +586,75 @@ int dns3d_step(dns3d_handle* h, int nsteps) {
         h->time += h->cfg.dt;  // 3D:296
     }
     return DNS3D_OK;
+}
+
+int dns3d_step_timed(dns3d_handle* h, int nsteps, double* elapsed_ms) {
+    if (!h || !elapsed_ms || nsteps < 1) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    if (!h->graph) {  // capture outside the timed region
+        int rc = dns3d_step(h, 1);
+        if (rc) return rc;
+    }
+    cudaEvent_t e0, e1;
+    CK(h, cudaEventCreate(&e0));
+    CK(h, cudaEventCreate(&e1));
+    CK(h, cudaEventRecord(e0, h->stream));
+    int rc = dns3d_step(h, nsteps);
+    CK(h, cudaEventRecord(e1, h->stream));
+    CK(h, cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(h, cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *elapsed_ms = ms;
+    return rc;
+}
+
+int dns3d_profile_kernels(dns3d_handle* h, int nsteps, dns3d_kernel_time* out, int cap, int* n) {
+    if (!h || !out || !n || cap < 1 || nsteps < 1) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    std::vector<dns3d_kernel_time> acc;
+    for (int s = 0; s < nsteps; ++s) {
+        h->prof = true;
+        h->nev = 0;
+        mark(h, "start");
+        int rc = run_step_body(h);
+        h->prof = false;
+        if (rc) return rc;
+        CK(h, cudaStreamSynchronize(h->stream));
+        h->step += 1;
+        h->time += h->cfg.dt;
+        for (size_t i = 1; i < h->nev; ++i) {
+            float ms = 0.f;
+            CK(h, cudaEventElapsedTime(&ms, h->ev[i - 1], h->ev[i]));
+            const char* nm = h->evname[i];
+            size_t j = 0;
+            while (j < acc.size() && std::strcmp(acc[j].name, nm) != 0) ++j;
+            if (j == acc.size()) acc.push_back(dns3d_kernel_time{nm, 0, 0, 0.0});
+            acc[j].launches += 1;
+            acc[j].total_ms += ms;
+        }
+    }
+    const int m = (int)acc.size() < cap ? (int)acc.size() : cap;
+    for (int i = 0; i < m; ++i) out[i] = acc[i];
+    *n = m;
+    return DNS3D_OK;
+}
+
+int dns3d_launches_per_step(dns3d_handle* h, int* n) {
+    if (!h || !n) return DNS3D_E_INVALID;
+    if (h->launches == 0) {  // count by a dry capture-free pass is not possible; run one step
+        int rc = dns3d_step(h, 1);
+        if (rc) return rc;
+    }
+    *n = h->launches;
+    return DNS3D_OK;
+}
+
+int dns3d_measure_fp64_tflops(int device, double* tflops) {
+    if (!tflops) return DNS3D_E_INVALID;
+    cudaError_t e = measure_fp64_tflops(device, tflops);
+    return e == cudaSuccess ? DNS3D_OK : DNS3D_E_CUDA;
 }
 
 int dns3d_synchronize(dns3d_handle* h) {

@@ -71,6 +71,9 @@ struct FftCtx {
     double2* tw_nx;      // e^{-2 pi i t/nx}, t < nx/2+1
     double2* tmp;        // spectral scratch for nf fields
     int tmp_fields;
+    // optional per-launch hook (profiling): called after each kernel launch
+    void (*hook)(void*, const char*) = nullptr;
+    void* hook_ctx = nullptr;
 };
 cudaError_t fft_setup(FftCtx& ctx, const GridDev& g);
 void fft_release(FftCtx& ctx);
@@ -157,6 +160,9 @@ cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaSt
 cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh,
                            double helm_f, const double* ksq, int nq, double* HinvT,
                            double* PinvT, int* info, cudaStream_t s);
+
+// Dense FP64 FMA throughput probe (TFLOP/s).
+cudaError_t measure_fp64_tflops(int device, double* tflops);
 
 // ---------------------------------------------------------------- lgl.cpp
 void lgl_nodes_weights(int n, std::vector<double>& x, std::vector<double>& w);

@@ -301,11 +301,13 @@ cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields ph
     dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
     k_fft_y<+1><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(double2), s>>>(spec, tmp, g, ctx.py,
                                                                        ctx.tw_ny, cx);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_y_inverse");
     const int rx = pick_rx(g.nxh);
     const int nrows = nplanes * g.ny;
     dim3 gx((nrows + rx - 1) / rx, nf);
     k_c2r_x<<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(double2), s>>>(tmp, phys, g, ctx.px2,
                                                                     ctx.tw_nx2, ctx.tw_nx, rx, nrows);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_c2r");
     return cudaGetLastError();
 }
 
@@ -317,10 +319,12 @@ cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields sp
     dim3 gx((nrows + rx - 1) / rx, nf);
     k_r2c_x<<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(double2), s>>>(phys, spec, g, ctx.px2,
                                                                     ctx.tw_nx2, ctx.tw_nx, rx, nrows);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_r2c");
     const int cx = pick_cx(g.ny);
     dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
     k_fft_y<-1><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(double2), s>>>(spec, spec, g, ctx.py,
                                                                        ctx.tw_ny, cx);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_y_forward");
     return cudaGetLastError();
 }
 

@@ -131,7 +131,57 @@ __global__ void __launch_bounds__(256) k_build_inverses(int nz, const double* __
     }
 }
 
+// Eight independent FMA chains per thread; one store per thread keeps the
+// chains live.
+__global__ void __launch_bounds__(256) k_fma_probe(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = threadIdx.x + i;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) x[i] = fma(x[i], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += x[i];
+    out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
+
+cudaError_t measure_fp64_tflops(int device, double* tflops) {
+    cudaError_t e;
+    if ((e = cudaSetDevice(device))) return e;
+    int sms = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device))) return e;
+    const int blocks = sms * 8, threads = 256, iters = 4000;
+    double* out = nullptr;
+    if ((e = cudaMalloc(&out, sizeof(double) * blocks * threads))) return e;
+    cudaStream_t s;
+    cudaEvent_t e0, e1;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_fma_probe<<<blocks, threads, 0, s>>>(out, 64, 0.999, 0.001);
+    double best = 0.0;
+    for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(e0, s);
+        k_fma_probe<<<blocks, threads, 0, s>>>(out, iters, 0.999, 0.001);
+        cudaEventRecord(e1, s);
+        e = cudaEventSynchronize(e1);
+        if (e) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double tf = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+        if (tf > best) best = tf;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    cudaFree(out);
+    *tflops = best;
+    return e ? e : cudaGetLastError();
+}
 
 cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh, double helm_f,
                            const double* ksq, int nq, double* HinvT, double* PinvT, int* info,

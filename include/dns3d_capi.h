@@ -141,6 +141,27 @@ int dns3d_synchronize(dns3d_handle* h);
 /* output_diagnostics_3d observables plus check_divergence_3d's max |div u|. */
 int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out);
 
+/* Measurement helpers (no counterpart in the reference, whose only timing is
+ * cpu_time around each step, 3D:287-360).
+ * dns3d_step_timed: dns3d_step with CUDA events recorded on the handle's
+ * stream around the nsteps graph replays; waits and returns the elapsed ms.
+ * dns3d_profile_kernels: runs nsteps loop bodies launch by launch with an
+ * event between consecutive kernels and returns, per kernel name, the launch
+ * count and total device ms (names are static strings). */
+typedef struct dns3d_kernel_time {
+    const char* name;
+    int launches;
+    int pad_;
+    double total_ms;
+} dns3d_kernel_time;
+int dns3d_step_timed(dns3d_handle* h, int nsteps, double* elapsed_ms);
+int dns3d_profile_kernels(dns3d_handle* h, int nsteps, dns3d_kernel_time* out, int cap, int* n);
+/* Kernel launches one dns3d_step issues per time step. */
+int dns3d_launches_per_step(dns3d_handle* h, int* n);
+/* Dense FP64 FMA throughput of `device` in TFLOP/s (FMA = 2 flops), timed with
+ * CUDA events: the peak that bounds the FP64 kernels. */
+int dns3d_measure_fp64_tflops(int device, double* tflops);
+
 /* Device bytes held by a handle for a given config (admission control). */
 int dns3d_footprint_bytes(const dns3d_config* cfg, unsigned long long* bytes);
 
