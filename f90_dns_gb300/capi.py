@@ -40,7 +40,7 @@ EXPORTED_SYMBOLS = (
     "dns3d_pressure_correction", "dns3d_apply_boundary_conditions", "dns3d_step",
     "dns3d_synchronize", "dns3d_diagnostics", "dns3d_footprint_bytes", "dns3d_strerror",
     "dns3d_last_error", "dns3d_step_timed", "dns3d_profile_kernels", "dns3d_launches_per_step",
-    "dns3d_measure_fp64_tflops",
+    "dns3d_measure_fp64_tflops", "dns3d_flow_stats_noalloc",
 )
 
 
@@ -136,6 +136,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_profile_kernels.argtypes = [hp, ip, C.POINTER(CKernelTime), ip, C.POINTER(C.c_int)]
     lib.dns3d_launches_per_step.argtypes = [hp, C.POINTER(C.c_int)]
     lib.dns3d_measure_fp64_tflops.argtypes = [ip, C.POINTER(C.c_double)]
+    lib.dns3d_flow_stats_noalloc.argtypes = [vp, vp, vp, ip, ip, ip, vp, vp]
     lib.dns3d_last_error.argtypes = [hp]
     lib.dns3d_last_error.restype = C.c_char_p
     for n in EXPORTED_SYMBOLS:

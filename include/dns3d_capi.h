@@ -162,6 +162,25 @@ int dns3d_launches_per_step(dns3d_handle* h, int* n);
  * CUDA events: the peak that bounds the FP64 kernels. */
 int dns3d_measure_fp64_tflops(int device, double* tflops);
 
+/* Flow statistics without any device allocation.  No counterpart in the
+ * reference.  For callers that cannot let a library allocate device memory
+ * (a driver that reserves nearly all HBM for its own pool, a job with a fixed
+ * memory budget) and so cannot create a handle just to read diagnostics.
+ * Given caller-owned device arrays u, v, w (nx*ny*nz doubles each, the layout
+ * of dns3d_get_state), writes to the caller-owned device buffer out4:
+ *   out4[0..2] = max|u|, max|v|, max|w|,
+ *   out4[3]    = kinetic energy, as dns3d_diagnostics() reports them.
+ * Runs on the calling thread's current device, asynchronously on `stream`
+ * (a cudaStream_t; NULL = legacy default stream).  Its scratch is a fixed
+ * 32 KB array inside the library, present on every GPU that loads it until
+ * the process exits; it allocates nothing.  The first call on a device looks
+ * up that array's device address (make that first call before any stream
+ * capture).  All calls share the array, so calls that overlap on the GPU race.
+ * nz above DNS3D_NOALLOC_MAX_NZ is rejected with DNS3D_E_UNSUPPORTED. */
+#define DNS3D_NOALLOC_MAX_NZ 129
+int dns3d_flow_stats_noalloc(const double* u, const double* v, const double* w, int nx, int ny,
+                             int nz, double* out4, void* stream);
+
 /* Device bytes held by a handle for a given config (admission control). */
 int dns3d_footprint_bytes(const dns3d_config* cfg, unsigned long long* bytes);
 
