@@ -54,12 +54,22 @@ def _barrier(dist):
 
 
 def _max_over_ranks(dist, x: float) -> float:
+    """Slowest rank's value (NCCL groups reduce on the GPU, gloo on the CPU)."""
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(dist, world_size: int, points: int, steps: int, local_ms: float) -> tuple:
+    """Whole-job point-steps/s of independent replicas: every rank advances its
+    own run of `points` points for `steps` steps; the job takes as long as the
+    slowest rank.  Returns (value, max_ms)."""
+    ms = _max_over_ranks(dist, local_ms)
+    return world_size * points * steps / (ms * 1e-3), ms
 
 
 class ClockSampler:
@@ -207,9 +217,8 @@ def run_ours(args) -> None:
         _barrier(dist)
         ms = d.step_timed(args.steps)
         _barrier(dist)
-    ms = _max_over_ranks(dist, ms)
+    value, ms = replica_throughput(dist, ws, pts, args.steps, ms)
     clocks = sampler.summary()
-    value = ws * pts * args.steps / (ms * 1e-3)
     launches = d.launches_per_step() * args.steps
 
     # per-kernel device times (eager replay, events between launches)
