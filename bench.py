@@ -127,22 +127,29 @@ class ClockSampler:
 
 
 def algorithmic_flops(wl: dict) -> dict:
-    """FP64 flops per step of the spectral-resident algorithm, by kernel.
+    """FP64 flops per step of the spectral-resident, parity-folded algorithm.
 
-    Per complex mode column, one nz x nz real operator applied to it costs
-    4 nz^2 flops.  Per step: vorticity 2 (D.u, D.v), viscous 6 (3 x D2, 3 x
-    Helmholtz inverse), pressure 2 (D.w*, Poisson inverse), correction 1
-    (D.phi): 11 operator applications = 44 nz^2 Nm.  Transforms: 9 real 2D
-    FFTs per z-plane at 2.5 n log2 n flops (n = nx ny).
+    Per complex mode column (Nm = (nx/2+1) ny columns per z-level) one nz x nz
+    real operator costs, folded into its even/odd blocks (he = nz - nz/2,
+    ho = nz/2): symmetric 4 (he^2 + ho^2) flops, antisymmetric 8 he ho flops.
+    Per step: vorticity 2 antisymmetric (D.u, D.v); viscous 6 symmetric
+    (3 x D2, 3 x Helmholtz inverse); pressure 1 antisymmetric + 1 symmetric
+    (D.w*, Poisson inverse); correction 1 antisymmetric (D.phi).
+    Transforms: 9 real 2D FFTs per z-plane at 2.5 n log2 n flops (n = nx ny).
     """
     nx, ny, nz = wl["nx"], wl["ny"], wl["nz"]
     nm = (nx // 2 + 1) * ny
-    op = 4.0 * nz * nz * nm
+    ho = nz // 2
+    he = nz - ho
+    sym = 4.0 * (he * he + ho * ho) * nm
+    anti = 8.0 * he * ho * nm
     n = nx * ny
     fft = 2.5 * n * math.log2(n) * nz
-    return {"vorticity": 2 * op, "viscous_helmholtz": 6 * op, "pressure_poisson": 2 * op,
-            "pressure_correction": 1 * op, "fft_total": 9 * fft, "z_total": 11 * op,
-            "total": 11 * op + 9 * fft}
+    out = {"vorticity": 2 * anti, "viscous_helmholtz": 6 * sym, "pressure_poisson": anti + sym,
+           "pressure_correction": anti, "fft_total": 9 * fft}
+    out["z_total"] = out["vorticity"] + out["viscous_helmholtz"] + out["pressure_poisson"] + out["pressure_correction"]
+    out["total"] = out["z_total"] + out["fft_total"]
+    return out
 
 
 def cpu_sample(wl_name: str, steps: int, threads: int) -> dict:

@@ -154,6 +154,40 @@ void mark(dns3d_handle* h, const char* name) {
 
 void fft_hook(void* ctx, const char* name) { mark(static_cast<dns3d_handle*>(ctx), name); }
 
+// Parity folding of a full row-major operator (see step.cu): antisymmetric
+// D -> De [he][ho], Do [ho][he]; symmetric A -> Ae [he][he], Ao [ho][ho].
+void fold_antisymmetric(const std::vector<double>& D, int n, std::vector<double>& De, std::vector<double>& Do) {
+    const int h = n / 2, he = n - h, ho = h;
+    De.assign((size_t)he * ho, 0.0);
+    Do.assign((size_t)ho * he, 0.0);
+    for (int i = 0; i < h; ++i) {
+        for (int j = 0; j < h; ++j) {
+            De[(size_t)i * ho + j] = 0.5 * (D[(size_t)i * n + j] - D[(size_t)i * n + n - 1 - j]);
+            Do[(size_t)i * he + j] = 0.5 * (D[(size_t)i * n + j] + D[(size_t)i * n + n - 1 - j]);
+        }
+        if (n % 2) Do[(size_t)i * he + h] = D[(size_t)i * n + h];
+    }
+    if (n % 2)
+        for (int j = 0; j < h; ++j) De[(size_t)h * ho + j] = D[(size_t)h * n + j];
+}
+
+void fold_symmetric(const std::vector<double>& A, int n, std::vector<double>& Ae, std::vector<double>& Ao) {
+    const int h = n / 2, he = n - h, ho = h;
+    Ae.assign((size_t)he * he, 0.0);
+    Ao.assign((size_t)ho * ho, 0.0);
+    for (int i = 0; i < h; ++i) {
+        for (int j = 0; j < h; ++j) {
+            Ae[(size_t)i * he + j] = 0.5 * (A[(size_t)i * n + j] + A[(size_t)i * n + n - 1 - j]);
+            Ao[(size_t)i * ho + j] = 0.5 * (A[(size_t)i * n + j] - A[(size_t)i * n + n - 1 - j]);
+        }
+        if (n % 2) Ae[(size_t)i * he + h] = A[(size_t)i * n + h];
+    }
+    if (n % 2) {
+        for (int j = 0; j < h; ++j) Ae[(size_t)h * he + j] = A[(size_t)h * n + j];
+        Ae[(size_t)h * he + h] = A[(size_t)h * n + h];
+    }
+}
+
 int upload(dns3d_handle* h, void* dst, const void* src, size_t bytes) {
     CK(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
     return DNS3D_OK;
@@ -281,7 +315,8 @@ int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
     b += 4 * nm * sizeof(double2);           // GP
     b += 6 * se * sizeof(double2);           // FFT scratch
     b += 6 * pe * sizeof(double);            // physical fields
-    b += (2 * nq + 1) * nz2 * sizeof(double);  // inverses
+    const size_t hz = (size_t)c->nz / 2, ez = (size_t)c->nz - hz;
+    b += (2 * nq * (ez * ez + hz * hz) + 2 * nz2) * sizeof(double);  // folded inverses, pinned, S
     b += 16ull << 20;                        // operators, tables, reductions
     *bytes = b;
     return DNS3D_OK;
@@ -350,23 +385,34 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     std::vector<double> ksq(nq);
     for (int kya = 0; kya <= c.ny / 2; ++kya)
         for (int kx = 0; kx < g.nxhp; ++kx) ksq[(size_t)kya * g.nxhp + kx] = xw[kx] * xw[kx] + yw[kya] * yw[kya];
+    std::vector<double> D1e, D1o, D2e, D2o, W1e, W1o;
+    fold_antisymmetric(D1s, nz, D1e, D1o);
+    fold_symmetric(D2s, nz, D2e, D2o);
+    fold_antisymmetric(W1T, nz, W1e, W1o);
 
     Ops& ops = h->ops;
     ops.nq = nq;
+    ops.ho = nz / 2;
+    ops.he = nz - ops.ho;
     const size_t nz2 = (size_t)nz * nz;
+    const size_t qstride = (size_t)ops.he * ops.he + (size_t)ops.ho * ops.ho;
     double* dS = nullptr;
-    if ((rc = dev_alloc(h, &ops.D1, nz2)) || (rc = dev_alloc(h, &ops.D2, nz2)) ||
+    if ((rc = dev_alloc(h, &ops.D1e, D1e.size())) || (rc = dev_alloc(h, &ops.D1o, D1o.size())) ||
+        (rc = dev_alloc(h, &ops.D2e, D2e.size())) || (rc = dev_alloc(h, &ops.D2o, D2o.size())) ||
+        (rc = dev_alloc(h, &ops.W1e, W1e.size())) || (rc = dev_alloc(h, &ops.W1o, W1o.size())) ||
         (rc = dev_alloc(h, &ops.wh, nz)) || (rc = dev_alloc(h, &ops.zw, nz)) ||
         (rc = dev_alloc(h, &ops.S0, nz)) || (rc = dev_alloc(h, &ops.Sn, nz)) ||
-        (rc = dev_alloc(h, &ops.W1T, nz2)) || (rc = dev_alloc(h, &ops.xw, g.nxhp)) ||
-        (rc = dev_alloc(h, &ops.yw, c.ny)) || (rc = dev_alloc(h, &ops.ksq, nq)) ||
-        (rc = dev_alloc(h, &dS, nz2)) || (rc = dev_alloc(h, &ops.HinvT, (size_t)nq * nz2)) ||
-        (rc = dev_alloc(h, &ops.PinvT, (size_t)(nq + 1) * nz2)))
+        (rc = dev_alloc(h, &ops.xw, g.nxhp)) || (rc = dev_alloc(h, &ops.yw, c.ny)) ||
+        (rc = dev_alloc(h, &ops.ksq, nq)) || (rc = dev_alloc(h, &dS, nz2)) ||
+        (rc = dev_alloc(h, &ops.HinvF, (size_t)nq * qstride)) ||
+        (rc = dev_alloc(h, &ops.PinvF, (size_t)nq * qstride)) || (rc = dev_alloc(h, &ops.PpinT, nz2)))
         return fail(rc);
     struct Up { void* d; const void* s; size_t b; } ups[] = {
-        {ops.D1, D1s.data(), nz2 * 8}, {ops.D2, D2s.data(), nz2 * 8}, {ops.wh, wh.data(), (size_t)nz * 8},
-        {ops.zw, h->zwts.data(), (size_t)nz * 8}, {ops.S0, S0.data(), (size_t)nz * 8},
-        {ops.Sn, Sn.data(), (size_t)nz * 8}, {ops.W1T, W1T.data(), nz2 * 8},
+        {ops.D1e, D1e.data(), D1e.size() * 8}, {ops.D1o, D1o.data(), D1o.size() * 8},
+        {ops.D2e, D2e.data(), D2e.size() * 8}, {ops.D2o, D2o.data(), D2o.size() * 8},
+        {ops.W1e, W1e.data(), W1e.size() * 8}, {ops.W1o, W1o.data(), W1o.size() * 8},
+        {ops.wh, wh.data(), (size_t)nz * 8}, {ops.zw, h->zwts.data(), (size_t)nz * 8},
+        {ops.S0, S0.data(), (size_t)nz * 8}, {ops.Sn, Sn.data(), (size_t)nz * 8},
         {ops.xw, xw.data(), (size_t)g.nxhp * 8}, {ops.yw, yw.data(), (size_t)c.ny * 8},
         {ops.ksq, ksq.data(), (size_t)nq * 8}, {dS, S.data(), nz2 * 8}};
     for (auto& u : ups)
@@ -394,7 +440,8 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
 
     // per-mode operator inverses
     if (cudaMemsetAsync(h->d_flag, 0, 4 * sizeof(int), h->stream) != cudaSuccess) return fail(DNS3D_E_CUDA);
-    if ((e = build_inverses(g, dS, ops.wh, helm_f, ops.ksq, nq, ops.HinvT, ops.PinvT, h->d_flag, h->stream)))
+    if ((e = build_inverses(g, dS, ops.wh, helm_f, ops.ksq, nq, ops.HinvF, ops.PinvF, ops.PpinT, h->d_flag,
+                            h->stream)))
         return fail(DNS3D_E_CUDA);
     int info = 0;
     if (cudaMemcpyAsync(&info, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||

@@ -95,19 +95,27 @@ struct StepParams {
     int weak_form;        // use_weak_form_divergence
 };
 
+// z-operators in parity-folded form (see step.cu): for nz levels,
+// he = nz - nz/2 even-part and ho = nz/2 odd-part values per column.
+//   antisymmetric D: De [he][ho] (acts on the odd part), Do [ho][he]
+//   symmetric A:     Ae [he][he], Ao [ho][ho]
+// Per-mode inverses: per q, [GeT (he*he) | GoT (ho*ho)], each block stored
+// transposed.
 struct Ops {
-    double* D1;      // (2/ybar) d1             [nz][nz]
-    double* D2;      // (2/ybar)^2 d2           [nz][nz]
+    int he, ho;
+    double* D1e; double* D1o;   // (2/ybar) d1
+    double* D2e; double* D2o;   // (2/ybar)^2 d2
+    double* W1e; double* W1o;   // zwts[m]*(2/ybar)*d1(m,z) as [z][m] (weak-form vertical part)
     double* wh;      // zwts * ybar/2           [nz]
     double* zw;      // zwts                    [nz]
     double* S0;      // helm_f * S[z][0]        [nz]
     double* Sn;      // helm_f * S[z][nz-1]     [nz]
-    double* W1T;     // zwts[m]*(2/ybar)*d1(m,z), weak-form vertical part, [z][m]
     double* xw;      // [nxhp]
     double* yw;      // [ny]
     double* ksq;     // xsq+ysq per unique q     [nq]
-    double* HinvT;   // Helmholtz inverses, transposed  [nq][nz][nz]
-    double* PinvT;   // Poisson inverses, transposed    [nq+1][nz][nz]; q=nq is the pinned (0,0)
+    double* HinvF;   // folded Helmholtz inverses      [nq][he*he + ho*ho]
+    double* PinvF;   // folded Poisson inverses        [nq][he*he + ho*ho]
+    double* PpinT;   // pinned (0,0) Poisson inverse, unfolded, transposed [nz][nz]
     int nq;
 };
 
@@ -157,9 +165,11 @@ cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaSt
 // ---------------------------------------------------------------- setup.cu
 // Build the per-mode operator inverses on the device by Gauss-Jordan with
 // partial pivoting.  info[0] receives 1 + index of the first singular matrix.
+// Outputs: HinvF/PinvF folded per q (layout of Ops), PpinT the unfolded
+// transposed inverse of the pinned (0,0) Poisson operator.
 cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh,
-                           double helm_f, const double* ksq, int nq, double* HinvT,
-                           double* PinvT, int* info, cudaStream_t s);
+                           double helm_f, const double* ksq, int nq, double* HinvF,
+                           double* PinvF, double* PpinT, int* info, cudaStream_t s);
 
 // Dense FP64 FMA throughput probe (TFLOP/s).
 cudaError_t measure_fp64_tflops(int device, double* tflops);

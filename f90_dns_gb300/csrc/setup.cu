@@ -14,7 +14,10 @@
 //   Poisson,   q < nq:  P = -S - diag(k^2 w ybar/2)              (3D:1684-1692)
 //   Poisson,   q = nq:  the pinned (0,0) operator: -S with row 1 and column 1
 //                       zeroed and P(1,1) = 1                     (3D:1702-1711)
-// Outputs are stored transposed: out[q][z'][z] = inverse[z][z'].
+// Outputs are stored parity-folded per q (the operators are centro-symmetric,
+// so only the two diagonal blocks of the folded inverse are non-zero), each
+// block transposed; the pinned operator is not centro-symmetric and is stored
+// unfolded and transposed: out[z'][z] = inverse[z][z'].
 #include "dns3d_internal.cuh"
 
 namespace dns3d {
@@ -87,8 +90,9 @@ __device__ bool gj_invert(double* a, int n, int* perm, double* colk, int* flag) 
 __global__ void __launch_bounds__(256) k_build_inverses(int nz, const double* __restrict__ S,
                                                         const double* __restrict__ wh, double helm_f,
                                                         const double* __restrict__ ksq, int nq,
-                                                        double* __restrict__ HinvT,
-                                                        double* __restrict__ PinvT, int* info) {
+                                                        double* __restrict__ HinvF,
+                                                        double* __restrict__ PinvF,
+                                                        double* __restrict__ PpinT, int* info) {
     extern __shared__ double sm[];
     double* a = sm;
     double* colk = sm + nz * nz;
@@ -97,9 +101,12 @@ __global__ void __launch_bounds__(256) k_build_inverses(int nz, const double* __
     const int job = blockIdx.x;  // [0, nq): Helmholtz q;  [nq, 2nq+1): Poisson q - nq
     const bool helm = job < nq;
     const int q = helm ? job : job - nq;
-    double* out = helm ? HinvT + (size_t)q * nz * nz : PinvT + (size_t)q * nz * nz;
+    const int h = nz / 2, he = nz - h, ho = h;
+    const size_t qstride = (size_t)he * he + (size_t)ho * ho;
+    const bool pinned = !helm && q == nq;
+    double* out = pinned ? PpinT : (helm ? HinvF : PinvF) + (size_t)q * qstride;
     if (!helm && q == 0) {  // k^2 = 0 unpinned Poisson operator is singular and never used
-        for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) out[t] = 0.0;
+        for (int t = threadIdx.x; t < (int)qstride; t += blockDim.x) out[t] = 0.0;
         return;
     }
     for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) {
@@ -125,9 +132,26 @@ __global__ void __launch_bounds__(256) k_build_inverses(int nz, const double* __
         if (threadIdx.x == 0) atomicCAS(info, 0, job + 1);
         return;
     }
-    for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) {
-        const int zp = t / nz, z = t - zp * nz;
-        out[t] = a[z * nz + zp];
+    if (pinned) {
+        for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) {
+            const int zp = t / nz, z = t - zp * nz;
+            out[t] = a[z * nz + zp];
+        }
+        return;
+    }
+    // Ge[k][j] (k, j < he) and Go[k][j] (k, j < ho), stored as GeT[j][k], GoT[j][k]
+    for (int t = threadIdx.x; t < he * he; t += blockDim.x) {
+        const int j = t / he, k = t - j * he;
+        double v;
+        if (k < h && j < h) v = 0.5 * (a[k * nz + j] + a[k * nz + nz - 1 - j]);
+        else if (k < h) v = a[k * nz + h];       // j = middle
+        else if (j < h) v = a[h * nz + j];       // k = middle
+        else v = a[h * nz + h];
+        out[t] = v;
+    }
+    for (int t = threadIdx.x; t < ho * ho; t += blockDim.x) {
+        const int j = t / ho, k = t - j * ho;
+        out[(size_t)he * he + t] = 0.5 * (a[k * nz + j] - a[k * nz + nz - 1 - j]);
     }
 }
 
@@ -184,14 +208,14 @@ cudaError_t measure_fp64_tflops(int device, double* tflops) {
 }
 
 cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh, double helm_f,
-                           const double* ksq, int nq, double* HinvT, double* PinvT, int* info,
+                           const double* ksq, int nq, double* HinvF, double* PinvF, double* PpinT, int* info,
                            cudaStream_t s) {
     const int nz = g.nz;
     const size_t sm = (size_t)nz * nz * sizeof(double) + nz * sizeof(double) + nz * sizeof(int);
     if (sm > 200 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_build_inverses, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e) return e;
-    k_build_inverses<<<2 * nq + 1, 256, sm, s>>>(nz, S, wh, helm_f, ksq, nq, HinvT, PinvT, info);
+    k_build_inverses<<<2 * nq + 1, 256, sm, s>>>(nz, S, wh, helm_f, ksq, nq, HinvF, PinvF, PpinT, info);
     return cudaGetLastError();
 }
 

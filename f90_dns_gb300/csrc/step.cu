@@ -84,6 +84,91 @@ __global__ void k_pi_update(GridDev g, const double* __restrict__ zw, PIParams p
     pi->avg_pressure_gradient = pi->pressure_gradient_sum / (double)pi->pressure_gradient_count;
 }
 
+// ------------------------------------------------------------------ parity folding
+// The LGL operators are centro-symmetric (D2, the Helmholtz and Poisson
+// inverses: A[n-1-i][n-1-j] = A[i][j]) or centro-antisymmetric (D, the
+// weak-form operator).  With s_i = x_i + x_{n-1-i}, d_i = x_i - x_{n-1-i}
+// (i < n/2) and the middle value x_m when nz is odd, a column splits into an
+// even part fe = [s; x_m] (he = nz - nz/2 values) and an odd part fo = d
+// (ho = nz/2 values), and every operator becomes two half-size blocks:
+//   symmetric A:  ye = Ae fe,  yo = Ao fo
+//   antisym.  D:  ye = De fo,  yo = Do fe
+//   y_i = ye_i + yo_i,  y_{n-1-i} = ye_i - yo_i,  y_m = ye_m
+// which halves the FP64 multiply-adds of every z-contraction.  The blocks are
+// built from the full operators (host: dns3d_create; device: the inverses).
+
+// tile = [fe (he x tc) | fo (ho x tc)] of field src, modes m0 .. m0+tc-1.
+__device__ __forceinline__ void fold_load(double2* tile, const double2* __restrict__ src, const GridDev& g,
+                                          int m0, int tc, int he, int ho) {
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        double2 fe = make_double2(0.0, 0.0), fo = fe;
+        if (m < g.nm) {
+            const double2 a = src[(size_t)k * g.nm + m];
+            if (k < ho) {
+                const double2 b = src[(size_t)(g.nz - 1 - k) * g.nm + m];
+                fe = make_double2(a.x + b.x, a.y + b.y);
+                fo = make_double2(a.x - b.x, a.y - b.y);
+            } else {
+                fe = a;
+            }
+        }
+        tile[t] = fe;
+        if (k < ho) tile[(he + k) * tc + c] = fo;
+    }
+}
+
+// ye = sum_j E[k][j] * in[j] over j < len (E row-major with leading dim len);
+// in is a folded tile part with column stride tc.
+__device__ __forceinline__ double2 fold_dot(const double* __restrict__ erow, const double2* in, int len, int tc,
+                                            int c) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int j = 0; j < len; ++j) {
+        const double e = __ldg(&erow[j]);
+        const double2 a = in[j * tc + c];
+        acc.x = fma(e, a.x, acc.x);
+        acc.y = fma(e, a.y, acc.y);
+    }
+    return acc;
+}
+
+// Antisymmetric operator (De [he][ho], Do [ho][he]) on a folded tile: returns
+// the output pair (y at z = k, y at z = nz-1-k); for the middle row only .a.
+struct Pair {
+    double2 a, b;
+};
+__device__ __forceinline__ Pair anti_apply(const double* __restrict__ De, const double* __restrict__ Do,
+                                           const double2* tile, int k, int c, int tc, int he, int ho) {
+    const double2 ye = fold_dot(De + (size_t)k * ho, tile + he * tc, ho, tc, c);
+    Pair p;
+    if (k < ho) {
+        const double2 yo = fold_dot(Do + (size_t)k * he, tile, he, tc, c);
+        p.a = make_double2(ye.x + yo.x, ye.y + yo.y);
+        p.b = make_double2(ye.x - yo.x, ye.y - yo.y);
+    } else {
+        p.a = ye;
+        p.b = ye;
+    }
+    return p;
+}
+__device__ __forceinline__ Pair sym_apply(const double* __restrict__ Ae, const double* __restrict__ Ao,
+                                          const double2* tile, int k, int c, int tc, int he, int ho) {
+    const double2 ye = fold_dot(Ae + (size_t)k * he, tile, he, tc, c);
+    Pair p;
+    if (k < ho) {
+        const double2 yo = fold_dot(Ao + (size_t)k * ho, tile + he * tc, ho, tc, c);
+        p.a = make_double2(ye.x + yo.x, ye.y + yo.y);
+        p.b = make_double2(ye.x - yo.x, ye.y - yo.y);
+    } else {
+        p.a = ye;
+        p.b = ye;
+    }
+    return p;
+}
+
+__device__ __forceinline__ double2 c2sub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
 // ------------------------------------------------------------------ vorticity
 // omega = (wy - vz, uz - wx, vx - uy)  (3D:1077-1079), spectrally.
 __global__ void __launch_bounds__(256) k_vorticity(GridDev g, Ops ops, const double2* __restrict__ U,
@@ -92,36 +177,31 @@ __global__ void __launch_bounds__(256) k_vorticity(GridDev g, Ops ops, const dou
                                                    double2* __restrict__ OX, double2* __restrict__ OY,
                                                    double2* __restrict__ OZ, int tc) {
     extern __shared__ double2 sm[];
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
     double2* tu = sm;
-    double2* tv = sm + g.nz * tc;
+    double2* tv = sm + nz * tc;
     const int m0 = blockIdx.x * tc;
-    load_tile(tu, U, g, m0, tc);
-    load_tile(tv, V, g, m0, tc);
+    fold_load(tu, U, g, m0, tc, he, ho);
+    fold_load(tv, V, g, m0, tc, he, ho);
     __syncthreads();
-    const int nz = g.nz;
-    for (int t = threadIdx.x; t < nz * tc; t += blockDim.x) {
-        const int z = t / tc, c = t - z * tc;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
         const int m = m0 + c;
         if (m >= g.nm) continue;
-        const double* __restrict__ drow = ops.D1 + (size_t)z * nz;
-        double2 du = make_double2(0.0, 0.0), dv = make_double2(0.0, 0.0);
-        for (int zp = 0; zp < nz; ++zp) {
-            const double d = __ldg(&drow[zp]);
-            const double2 a = tu[zp * tc + c], b = tv[zp * tc + c];
-            du.x = fma(d, a.x, du.x);
-            du.y = fma(d, a.y, du.y);
-            dv.x = fma(d, b.x, dv.x);
-            dv.y = fma(d, b.y, dv.y);
-        }
+        const Pair du = anti_apply(ops.D1e, ops.D1o, tu, k, c, tc, he, ho);
+        const Pair dv = anti_apply(ops.D1e, ops.D1o, tv, k, c, tc, he, ho);
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-        const size_t o = (size_t)z * g.nm + m;
-        const double2 w = W[o];
-        const double2 u = tu[t], v = tv[t];
-        const double2 wy = i_times(mi.ay, w), wx = i_times(mi.ax, w);
-        const double2 vx = i_times(mi.ax, v), uy = i_times(mi.ay, u);
-        OX[o] = make_double2(wy.x - dv.x, wy.y - dv.y);
-        OY[o] = make_double2(du.x - wx.x, du.y - wx.y);
-        OZ[o] = make_double2(vx.x - uy.x, vx.y - uy.y);
+        const int npt = (k < ho) ? 2 : 1;
+        for (int p = 0; p < npt; ++p) {
+            const int z = p ? nz - 1 - k : k;
+            const size_t o = (size_t)z * g.nm + m;
+            const double2 w = W[o], u = U[o], v = V[o];
+            const double2 wy = i_times(mi.ay, w), wx = i_times(mi.ax, w);
+            const double2 vx = i_times(mi.ax, v), uy = i_times(mi.ay, u);
+            OX[o] = c2sub(wy, p ? dv.b : dv.a);
+            OY[o] = c2sub(p ? du.b : du.a, wx);
+            OZ[o] = c2sub(vx, uy);
+        }
     }
 }
 
@@ -138,6 +218,37 @@ __global__ void k_products(RFields in, RFields out, size_t n) {
     }
 }
 
+// Per-mode folded inverse x = G b for the output pair k of column c:
+// GT points at [GeT (he x he) | GoT (ho x ho)] stored transposed
+// (GeT[j][k] = Ge[k][j]) so that threads of consecutive k read consecutive
+// addresses.  bt is the folded rhs tile.
+__device__ __forceinline__ Pair inv_apply(const double* __restrict__ GT, const double2* bt, int k, int c, int tc,
+                                          int he, int ho) {
+    double2 xe = make_double2(0.0, 0.0), xo = xe;
+    for (int j = 0; j < he; ++j) {
+        const double gv = __ldg(&GT[(size_t)j * he + k]);
+        const double2 b = bt[j * tc + c];
+        xe.x = fma(gv, b.x, xe.x);
+        xe.y = fma(gv, b.y, xe.y);
+    }
+    Pair p;
+    if (k < ho) {
+        const double* __restrict__ GoT = GT + (size_t)he * he;
+        for (int j = 0; j < ho; ++j) {
+            const double gv = __ldg(&GoT[(size_t)j * ho + k]);
+            const double2 b = bt[(he + j) * tc + c];
+            xo.x = fma(gv, b.x, xo.x);
+            xo.y = fma(gv, b.y, xo.y);
+        }
+        p.a = make_double2(xe.x + xo.x, xe.y + xo.y);
+        p.b = make_double2(xe.x - xo.x, xe.y - xo.y);
+    } else {
+        p.a = xe;
+        p.b = xe;
+    }
+    return p;
+}
+
 // ------------------------------------------------------------------ viscous step
 // viscous_step_3d (3D:1285-1332) + solve_viscous_helmholtz (3D:1425-1521) for
 // all three components of a mode tile:
@@ -147,30 +258,52 @@ __global__ void k_products(RFields in, RFields out, size_t n) {
 //   columns kept, so the wall data enters twice, as in the reference)
 // bc: u -> -dt dp/dx|wall, v -> -dt dp/dy|wall (previous total pressure,
 // 3D:1325-1326), w -> 0 (3D:1328).
+__device__ __forceinline__ double2 viscous_rhs(const GridDev& g, const Ops& ops, const StepParams& sp, int comp,
+                                               int z, int m, int ky, int kx, double2 f, double2 s, double2 lap,
+                                               double2 bc1, double2 bc2, double dpdx) {
+    if (z == 0) return bc1;
+    if (z == g.nz - 1) return bc2;
+    if (sp.dealias) {  // apply_dealias_truncation (3D:1163-1193)
+        const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
+        if (kx > sp.kx_max || kyi > sp.ky_max) s = make_double2(0.0, 0.0);
+    }
+    if (comp == 0 && m == 0) s.x += dpdx * sp.forcing_scale;  // 3D:1123-1145
+    double2 rr = make_double2(f.x + sp.dt * s.x, f.y + sp.dt * s.y);
+    if (sp.cn_fac != 0.0) {  // add_explicit_diffusion (3D:1355-1381)
+        const double ksq = __ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+        rr.x += sp.cn_fac * (lap.x - ksq * f.x);
+        rr.y += sp.cn_fac * (lap.y - ksq * f.y);
+    }
+    const double whz = __ldg(&ops.wh[z]);
+    const double s0 = __ldg(&ops.S0[z]), sn = __ldg(&ops.Sn[z]);
+    return make_double2(rr.x * whz - (s0 * bc1.x + sn * bc2.x), rr.y * whz - (s0 * bc1.y + sn * bc2.y));
+}
+
 __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams sp, Fields F,
                                                  Fields Src, const double2* __restrict__ GP,
                                                  const dns3d_pi_state* __restrict__ pi, Fields Out,
                                                  int tc) {
     extern __shared__ double2 sm[];
-    const int nz = g.nz;
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
     const int tsz = nz * tc;
-    double2* tf = sm;             // [3][nz][tc]
-    double2* tb = sm + 3 * tsz;   // [3][nz][tc]
+    double2* tf = sm;             // [3] folded F tiles
+    double2* tb = sm + 3 * tsz;   // [3] folded rhs tiles
     const int m0 = blockIdx.x * tc;
-    for (int comp = 0; comp < 3; ++comp) {
-        load_tile(tf + comp * tsz, F.p[comp], g, m0, tc);
-        load_tile(tb + comp * tsz, Src.p[comp], g, m0, tc);
-    }
+    for (int comp = 0; comp < 3; ++comp) fold_load(tf + comp * tsz, F.p[comp], g, m0, tc, he, ho);
     __syncthreads();
     const double dpdx = pi->current_pressure_gradient;
-    for (int t = threadIdx.x; t < 3 * tsz; t += blockDim.x) {
-        const int comp = t / tsz;
-        const int r = t - comp * tsz;
-        const int z = r / tc, c = r - z * tc;
+    for (int t = threadIdx.x; t < 3 * he * tc; t += blockDim.x) {
+        const int comp = t / (he * tc);
+        const int r = t - comp * he * tc;
+        const int k = r / tc, c = r - k * tc;
         const int m = m0 + c;
-        if (m >= g.nm) continue;
+        double2* bt = tb + comp * tsz;
+        if (m >= g.nm) {
+            bt[k * tc + c] = make_double2(0.0, 0.0);
+            if (k < ho) bt[(he + k) * tc + c] = make_double2(0.0, 0.0);
+            continue;
+        }
         const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
-        const double2* col = tf + comp * tsz;
         double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
         if (comp < 2) {
             const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
@@ -178,62 +311,35 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
             bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
             bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
         }
-        double2 b;
-        if (z == 0) {
-            b = bc1;
-        } else if (z == nz - 1) {
-            b = bc2;
+        Pair lap;
+        lap.a = lap.b = make_double2(0.0, 0.0);
+        if (sp.cn_fac != 0.0) lap = sym_apply(ops.D2e, ops.D2o, tf + comp * tsz, k, c, tc, he, ho);
+        const int z1 = k, z2 = nz - 1 - k;
+        const size_t o1 = (size_t)z1 * g.nm + m, o2 = (size_t)z2 * g.nm + m;
+        const double2 b1 = viscous_rhs(g, ops, sp, comp, z1, m, ky, kx, F.p[comp][o1], Src.p[comp][o1], lap.a,
+                                       bc1, bc2, dpdx);
+        if (k < ho) {
+            const double2 b2 = viscous_rhs(g, ops, sp, comp, z2, m, ky, kx, F.p[comp][o2], Src.p[comp][o2],
+                                           lap.b, bc1, bc2, dpdx);
+            bt[k * tc + c] = make_double2(b1.x + b2.x, b1.y + b2.y);
+            bt[(he + k) * tc + c] = make_double2(b1.x - b2.x, b1.y - b2.y);
         } else {
-            double2 s = tb[t];
-            if (sp.dealias) {  // apply_dealias_truncation (3D:1163-1193)
-                const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
-                if (kx > sp.kx_max || kyi > sp.ky_max) s = make_double2(0.0, 0.0);
-            }
-            if (comp == 0 && m == 0) s.x += dpdx * sp.forcing_scale;  // 3D:1123-1145
-            const double2 f = col[z * tc + c];
-            double2 rr = make_double2(f.x + sp.dt * s.x, f.y + sp.dt * s.y);
-            if (sp.cn_fac != 0.0) {  // add_explicit_diffusion (3D:1355-1381)
-                const double* __restrict__ drow = ops.D2 + (size_t)z * nz;
-                double2 lap = make_double2(0.0, 0.0);
-                for (int zp = 0; zp < nz; ++zp) {
-                    const double d = __ldg(&drow[zp]);
-                    const double2 a = col[zp * tc + c];
-                    lap.x = fma(d, a.x, lap.x);
-                    lap.y = fma(d, a.y, lap.y);
-                }
-                const double ksq = __ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
-                lap.x -= ksq * f.x;
-                lap.y -= ksq * f.y;
-                rr.x += sp.cn_fac * lap.x;
-                rr.y += sp.cn_fac * lap.y;
-            }
-            const double whz = __ldg(&ops.wh[z]);
-            const double s0 = __ldg(&ops.S0[z]), sn = __ldg(&ops.Sn[z]);
-            b.x = rr.x * whz - (s0 * bc1.x + sn * bc2.x);
-            b.y = rr.y * whz - (s0 * bc1.y + sn * bc2.y);
+            bt[k * tc + c] = b1;
         }
-        tb[t] = b;  // each element is read and written by its own thread only
     }
     __syncthreads();
-    // F* = A_q^{-1} b, one matrix per mode, applied to the three components.
-    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
-        const int c = t / nz, z = t - c * nz;
+    const size_t qstride = (size_t)he * he + (size_t)ho * ho;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int c = t / he, k = t - c * he;
         const int m = m0 + c;
         if (m >= g.nm) continue;
         const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
-        const double* __restrict__ Ainv = ops.HinvT + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * nz * nz;
-        double2 a0 = make_double2(0.0, 0.0), a1 = a0, a2 = a0;
-        for (int zp = 0; zp < nz; ++zp) {
-            const double h = __ldg(&Ainv[(size_t)zp * nz + z]);
-            const double2 b0 = tb[zp * tc + c], b1 = tb[tsz + zp * tc + c], b2 = tb[2 * tsz + zp * tc + c];
-            a0.x = fma(h, b0.x, a0.x); a0.y = fma(h, b0.y, a0.y);
-            a1.x = fma(h, b1.x, a1.x); a1.y = fma(h, b1.y, a1.y);
-            a2.x = fma(h, b2.x, a2.x); a2.y = fma(h, b2.y, a2.y);
+        const double* __restrict__ GT = ops.HinvF + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * qstride;
+        for (int comp = 0; comp < 3; ++comp) {
+            const Pair x = inv_apply(GT, tb + comp * tsz, k, c, tc, he, ho);
+            Out.p[comp][(size_t)k * g.nm + m] = x.a;
+            if (k < ho) Out.p[comp][(size_t)(nz - 1 - k) * g.nm + m] = x.b;
         }
-        const size_t o = (size_t)z * g.nm + m;
-        Out.p[0][o] = a0;
-        Out.p[1][o] = a1;
-        Out.p[2][o] = a2;
     }
 }
 
@@ -241,66 +347,89 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
 // solve_pressure_3d_standard (3D:1654-1733): b = (DX u* + DY v* + Dz w*)/dt *
 // w ybar/2; or _weak_form (3D:1749-1835): b = (-(DX u* + DY v*) w ybar/2 -
 // sum_m d1(m,k) w*_m zwts_m (2/ybar)) / dt.  Mode (0,0): b_1 = 0 and the
-// pinned operator (3D:1702-1711).  phi = P_q^{-1} b.
+// pinned operator (3D:1702-1711), which is not centro-symmetric and is applied
+// unfolded.  phi = P_q^{-1} b.
+__device__ __forceinline__ double2 pressure_rhs(const GridDev& g, const Ops& ops, const StepParams& sp, int z,
+                                                int m, const ModeInfo& mi, const double2* __restrict__ US,
+                                                const double2* __restrict__ VS, double2 dz) {
+    const size_t o = (size_t)z * g.nm + m;
+    const double2 hx = i_times(mi.ax, US[o]);
+    const double2 hy = i_times(mi.ay, VS[o]);
+    const double whz = __ldg(&ops.wh[z]);
+    const double inv_dt = 1.0 / sp.dt;
+    double2 b;
+    if (!sp.weak_form) {
+        b.x = ((hx.x + hy.x) + dz.x) * inv_dt * whz;
+        b.y = ((hx.y + hy.y) + dz.y) * inv_dt * whz;
+    } else {
+        b.x = (-(hx.x + hy.x) * whz - dz.x) * inv_dt;
+        b.y = (-(hx.y + hy.y) * whz - dz.y) * inv_dt;
+    }
+    if (m == 0 && z == 0) b = make_double2(0.0, 0.0);
+    return b;
+}
+
 __global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams sp,
                                                   const double2* __restrict__ US,
                                                   const double2* __restrict__ VS,
                                                   const double2* __restrict__ WS,
                                                   double2* __restrict__ PHI, int tc) {
     extern __shared__ double2 sm[];
-    const int nz = g.nz;
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
     const int tsz = nz * tc;
-    double2* tw = sm;        // w* tile
-    double2* tb = sm + tsz;  // rhs tile
+    double2* tw = sm;            // folded w* tile
+    double2* tb = sm + tsz;      // folded rhs tile
+    double2* bpin = sm + 2 * tsz;  // unfolded rhs of mode (0,0)
     const int m0 = blockIdx.x * tc;
-    load_tile(tw, WS, g, m0, tc);
+    fold_load(tw, WS, g, m0, tc, he, ho);
     __syncthreads();
-    const double inv_dt = 1.0 / sp.dt;
-    const double* __restrict__ A = sp.weak_form ? ops.W1T : ops.D1;
-    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
-        const int z = t / tc, c = t - z * tc;
+    const double* __restrict__ Ae = sp.weak_form ? ops.W1e : ops.D1e;
+    const double* __restrict__ Ao = sp.weak_form ? ops.W1o : ops.D1o;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
         const int m = m0 + c;
-        if (m >= g.nm) { tb[t] = make_double2(0.0, 0.0); continue; }
-        const double* __restrict__ drow = A + (size_t)z * nz;
-        double2 dz = make_double2(0.0, 0.0);
-        for (int zp = 0; zp < nz; ++zp) {
-            const double d = __ldg(&drow[zp]);
-            const double2 a = tw[zp * tc + c];
-            dz.x = fma(d, a.x, dz.x);
-            dz.y = fma(d, a.y, dz.y);
+        if (m >= g.nm) {
+            tb[t] = make_double2(0.0, 0.0);
+            if (k < ho) tb[(he + k) * tc + c] = make_double2(0.0, 0.0);
+            continue;
         }
+        const Pair dz = anti_apply(Ae, Ao, tw, k, c, tc, he, ho);
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-        const size_t o = (size_t)z * g.nm + m;
-        const double2 hx = i_times(mi.ax, US[o]);
-        const double2 hy = i_times(mi.ay, VS[o]);
-        const double whz = __ldg(&ops.wh[z]);
-        double2 b;
-        if (!sp.weak_form) {
-            b.x = ((hx.x + hy.x) + dz.x) * inv_dt * whz;
-            b.y = ((hx.y + hy.y) + dz.y) * inv_dt * whz;
+        const double2 b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
+        if (k < ho) {
+            const double2 b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
+            tb[t] = make_double2(b1.x + b2.x, b1.y + b2.y);
+            tb[(he + k) * tc + c] = make_double2(b1.x - b2.x, b1.y - b2.y);
+            if (m == 0) { bpin[k] = b1; bpin[nz - 1 - k] = b2; }
         } else {
-            b.x = (-(hx.x + hy.x) * whz - dz.x) * inv_dt;
-            b.y = (-(hx.y + hy.y) * whz - dz.y) * inv_dt;
+            tb[t] = b1;
+            if (m == 0) bpin[k] = b1;
         }
-        if (m == 0 && z == 0) b = make_double2(0.0, 0.0);
-        tb[t] = b;
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
-        const int c = t / nz, z = t - c * nz;
+    const size_t qstride = (size_t)he * he + (size_t)ho * ho;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int c = t / he, k = t - c * he;
         const int m = m0 + c;
         if (m >= g.nm) continue;
-        const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
-        const int q = (m == 0) ? ops.nq : mode_q(ky, kx, g.ny, g.nxhp);
-        const double* __restrict__ Ainv = ops.PinvT + (size_t)q * nz * nz;
-        double2 a = make_double2(0.0, 0.0);
-        for (int zp = 0; zp < nz; ++zp) {
-            const double h = __ldg(&Ainv[(size_t)zp * nz + z]);
-            const double2 bb = tb[zp * tc + c];
-            a.x = fma(h, bb.x, a.x);
-            a.y = fma(h, bb.y, a.y);
+        Pair x;
+        if (m == 0) {
+            double2 a = make_double2(0.0, 0.0), b = a;
+            for (int zp = 0; zp < nz; ++zp) {
+                const double2 bb = bpin[zp];
+                const double h1 = __ldg(&ops.PpinT[(size_t)zp * nz + k]);
+                const double h2 = __ldg(&ops.PpinT[(size_t)zp * nz + nz - 1 - k]);
+                a.x = fma(h1, bb.x, a.x); a.y = fma(h1, bb.y, a.y);
+                b.x = fma(h2, bb.x, b.x); b.y = fma(h2, bb.y, b.y);
+            }
+            x.a = a;
+            x.b = b;
+        } else {
+            const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+            x = inv_apply(ops.PinvF + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * qstride, tb, k, c, tc, he, ho);
         }
-        PHI[(size_t)z * g.nm + m] = a;
+        PHI[(size_t)k * g.nm + m] = x.a;
+        if (k < ho) PHI[(size_t)(nz - 1 - k) * g.nm + m] = x.b;
     }
 }
 
@@ -316,41 +445,38 @@ __global__ void __launch_bounds__(256) k_correction(GridDev g, Ops ops, StepPara
                                                     double2* __restrict__ W, double2* __restrict__ P,
                                                     double2* __restrict__ GP, int tc) {
     extern __shared__ double2 sm[];
-    const int nz = g.nz;
-    const int tsz = nz * tc;
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
     double2* tp = sm;
     const int m0 = blockIdx.x * tc;
-    load_tile(tp, PHI, g, m0, tc);
+    fold_load(tp, PHI, g, m0, tc, he, ho);
     __syncthreads();
     const double dt = sp.dt;
-    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
-        const int z = t / tc, c = t - z * tc;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
         const int m = m0 + c;
         if (m >= g.nm) continue;
-        const double* __restrict__ drow = ops.D1 + (size_t)z * nz;
-        double2 dz = make_double2(0.0, 0.0);
-        for (int zp = 0; zp < nz; ++zp) {
-            const double d = __ldg(&drow[zp]);
-            const double2 a = tp[zp * tc + c];
-            dz.x = fma(d, a.x, dz.x);
-            dz.y = fma(d, a.y, dz.y);
-        }
+        const Pair dz = anti_apply(ops.D1e, ops.D1o, tp, k, c, tc, he, ho);
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-        const size_t o = (size_t)z * g.nm + m;
-        const double2 ph = tp[t];
-        const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
-        const double2 us = US[o], vs = VS[o], ws = WS[o];
-        U[o] = make_double2(us.x - dt * px.x, us.y - dt * px.y);
-        V[o] = make_double2(vs.x - dt * py.x, vs.y - dt * py.y);
-        W[o] = make_double2(ws.x - dt * dz.x, ws.y - dt * dz.y);
-        double2 p = P[o];
-        p.x += ph.x;
-        p.y += ph.y;
-        P[o] = p;
-        if (z == 0 || z == nz - 1) {
-            const int wall = (z == 0) ? 0 : 1;
-            GP[(size_t)wall * g.nm + m] = i_times(mi.ax, p);
-            GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, p);
+        const int npt = (k < ho) ? 2 : 1;
+        for (int p = 0; p < npt; ++p) {
+            const int z = p ? nz - 1 - k : k;
+            const double2 d = p ? dz.b : dz.a;
+            const size_t o = (size_t)z * g.nm + m;
+            const double2 ph = PHI[o];
+            const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
+            const double2 us = US[o], vs = VS[o], ws = WS[o];
+            U[o] = make_double2(us.x - dt * px.x, us.y - dt * px.y);
+            V[o] = make_double2(vs.x - dt * py.x, vs.y - dt * py.y);
+            W[o] = make_double2(ws.x - dt * d.x, ws.y - dt * d.y);
+            double2 pp = P[o];
+            pp.x += ph.x;
+            pp.y += ph.y;
+            P[o] = pp;
+            if (z == 0 || z == nz - 1) {
+                const int wall = (z == 0) ? 0 : 1;
+                GP[(size_t)wall * g.nm + m] = i_times(mi.ax, pp);
+                GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, pp);
+            }
         }
     }
 }
@@ -386,28 +512,26 @@ __global__ void __launch_bounds__(256) k_divergence(GridDev g, Ops ops, const do
                                                     const double2* __restrict__ W,
                                                     double2* __restrict__ DIV, int tc) {
     extern __shared__ double2 sm[];
-    const int nz = g.nz;
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
     double2* tw = sm;
     const int m0 = blockIdx.x * tc;
-    load_tile(tw, W, g, m0, tc);
+    fold_load(tw, W, g, m0, tc, he, ho);
     __syncthreads();
-    for (int t = threadIdx.x; t < nz * tc; t += blockDim.x) {
-        const int z = t / tc, c = t - z * tc;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
         const int m = m0 + c;
         if (m >= g.nm) continue;
-        const double* __restrict__ drow = ops.D1 + (size_t)z * nz;
-        double2 dz = make_double2(0.0, 0.0);
-        for (int zp = 0; zp < nz; ++zp) {
-            const double d = __ldg(&drow[zp]);
-            const double2 a = tw[zp * tc + c];
-            dz.x = fma(d, a.x, dz.x);
-            dz.y = fma(d, a.y, dz.y);
-        }
+        const Pair dz = anti_apply(ops.D1e, ops.D1o, tw, k, c, tc, he, ho);
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-        const size_t o = (size_t)z * g.nm + m;
-        const double2 hx = i_times(mi.ax, U[o]);
-        const double2 hy = i_times(mi.ay, V[o]);
-        DIV[o] = make_double2((hx.x + hy.x) + dz.x, (hx.y + hy.y) + dz.y);
+        const int npt = (k < ho) ? 2 : 1;
+        for (int p = 0; p < npt; ++p) {
+            const int z = p ? nz - 1 - k : k;
+            const double2 d = p ? dz.b : dz.a;
+            const size_t o = (size_t)z * g.nm + m;
+            const double2 hx = i_times(mi.ax, U[o]);
+            const double2 hy = i_times(mi.ay, V[o]);
+            DIV[o] = make_double2((hx.x + hy.x) + d.x, (hx.y + hy.y) + d.y);
+        }
     }
 }
 
@@ -520,7 +644,7 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
     cudaError_t e;
     if ((e = set_smem(k_vorticity, 2 * (size_t)g.nz * tile_cols(g, 2) * sizeof(double2)))) return e;
     if ((e = set_smem(k_viscous, 6 * (size_t)g.nz * tile_cols(g, 6) * sizeof(double2)))) return e;
-    if ((e = set_smem(k_pressure, 2 * (size_t)g.nz * tile_cols(g, 2) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_pressure, (2 * (size_t)g.nz * tile_cols(g, 2) + g.nz) * sizeof(double2)))) return e;
     if ((e = set_smem(k_correction, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
     if ((e = set_smem(k_divergence, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
     return cudaSuccess;
@@ -560,7 +684,7 @@ cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& s
 cudaError_t launch_pressure(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
                             const double2* VS, const double2* WS, double2* PHI, cudaStream_t s) {
     const int tc = tile_cols(g, 2);
-    const size_t sm = 2 * (size_t)g.nz * tc * sizeof(double2);
+    const size_t sm = (2 * (size_t)g.nz * tc + g.nz) * sizeof(double2);
     k_pressure<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, US, VS, WS, PHI, tc);
     return cudaGetLastError();
 }
