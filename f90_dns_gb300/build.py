@@ -18,6 +18,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libdns3d_gpu.so")
+RUNNER = os.path.join(PKG, "dns3d_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -64,6 +65,15 @@ def build(verbose: bool = False) -> str:
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    # the driver executable (host C++ over the C-ABI)
+    src = os.path.join(CSRC, "dns3d_run.cpp")
+    if not os.path.exists(RUNNER) or os.path.getmtime(RUNNER) < max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", RUNNER,
+               "-L", PKG, "-ldns3d_gpu", "-Wl,-rpath,$ORIGIN"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     if verbose:
         print(LIB)
     return LIB
