@@ -228,6 +228,40 @@ def run_ours(args) -> None:
     clocks = sampler.summary()
     launches = d.launches_per_step() * args.steps
 
+    # the mixed-precision form on the same workload, and its error against
+    # FP64 after the same number of steps from the same initial condition
+    mixed = None
+    if args.mixed:
+        from f90_dns_gb300.capi import PREC_MIXED
+        dm = ChannelDNS(config_from(wl, device=local, precision=PREC_MIXED))
+        dm.step(args.warmup)
+        dm.synchronize()
+        _barrier(dist)
+        ms_m = dm.step_timed(args.steps)
+        value_m, ms_m = replica_throughput(dist, ws, pts, args.steps, ms_m)
+        prof_m = dm.profile_kernels(args.profile_steps)
+        dm.close()
+        # error: both forms from the initial condition for err_steps steps
+        nerr = args.mixed_err_steps
+        a = ChannelDNS(config_from(wl, device=local))
+        b = ChannelDNS(config_from(wl, device=local, precision=PREC_MIXED))
+        a.step(nerr)
+        b.step(nerr)
+        sa, sb = a.get_state(walls=False), b.get_state(walls=False)
+        da, db = a.diagnostics(), b.diagnostics()
+        a.close()
+        b.close()
+        import numpy as np
+        scale = max(float(np.max(np.abs(sa[k]))) for k in ("u", "v", "w"))
+        vel_err = max(float(np.max(np.abs(sa[k] - sb[k]))) for k in ("u", "v", "w")) / scale
+        tot_m = sum(t for _, t in prof_m.values())
+        mixed = {"value": value_m, "unit": "point-steps/s", "ms_per_step": ms_m / args.steps,
+                 "speedup_vs_fp64": value_m / value, "dtype": "f32+f64",
+                 "error_vs_fp64": {"steps": nerr, "max_rel_velocity": vel_err,
+                                   "max_div_fp64": da.max_div, "max_div_mixed": db.max_div,
+                                   "max_div_abs_diff": abs(da.max_div - db.max_div)},
+                 "kernels": {k: {"launches": n, "avg_ms": t / n, "share": t / tot_m} for k, (n, t) in prof_m.items()}}
+
     # per-kernel device times (eager replay, events between launches)
     prof = d.profile_kernels(args.profile_steps)
     total_prof = sum(t for _, t in prof.values())
@@ -294,7 +328,7 @@ def run_ours(args) -> None:
                        "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "working set > 129 MB L2 (per-mode inverses 0.29 GB + fields 0.2 GB), no flush"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "step_roofline": step_roof,
-            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu,
+            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu, "mixed": mixed,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -313,6 +347,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--ref-sample-frac", type=float, default=0.01,
                     help="reference arm: CPU steps timed per requested step (bounded sample, >= 2)")
+    ap.add_argument("--no-mixed", dest="mixed", action="store_false",
+                    help="skip the mixed-precision measurement")
+    ap.add_argument("--mixed-err-steps", type=int, default=200)
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu DRAM bytes per launch of the dominant kernel, if captured")
     args = ap.parse_args()

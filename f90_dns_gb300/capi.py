@@ -31,6 +31,7 @@ DNS3D_E_UNSUPPORTED = 6
 DNS3D_E_IO = 7
 DNS3D_E_NODEVICE = 8
 PREC_FP64 = 0
+PREC_MIXED = 1
 
 #: every symbol declared in include/dns3d_capi.h
 EXPORTED_SYMBOLS = (

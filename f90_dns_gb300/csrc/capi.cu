@@ -22,11 +22,17 @@ struct dns3d_handle {
     cudaStream_t stream = nullptr;
     FftCtx fft{};
     Ops ops{};
+    MixedOps mx{};
+    bool mixed = false;
+    float2* spec32[6] = {nullptr};  // mixed: u, v, w, ox, oy, oz (FP32 spectra)
+    float2* src32[3] = {nullptr};   // mixed: nonlinear source spectra
+    float* phys32[6] = {nullptr};   // mixed: physical planes
     StepParams sp{};
     PIParams pp{};
     double2 *U = nullptr, *V = nullptr, *W = nullptr, *P = nullptr, *GP = nullptr;
     double2 *SU = nullptr, *SV = nullptr, *SW = nullptr;
     double2 *US = nullptr, *VS = nullptr, *WS = nullptr, *PHI = nullptr;
+    double2* PHIZ = nullptr;  // mixed: dphi/dz
     double* phys[6] = {nullptr};
     dns3d_pi_state* d_pi = nullptr;
     double* d_red = nullptr;
@@ -92,7 +98,7 @@ int validate(const dns3d_config* c) {
             return DNS3D_E_INVALID;
     }
     if (c->enable_perturbations && !c->use_analytical_perturbations) return DNS3D_E_UNSUPPORTED;
-    if (c->precision != DNS3D_PREC_FP64) return DNS3D_E_UNSUPPORTED;
+    if (c->precision != DNS3D_PREC_FP64 && c->precision != DNS3D_PREC_MIXED) return DNS3D_E_UNSUPPORTED;
     return DNS3D_OK;
 }
 
@@ -193,10 +199,30 @@ int upload(dns3d_handle* h, void* dst, const void* src, size_t bytes) {
     return DNS3D_OK;
 }
 
+int run_source_terms_mixed(dns3d_handle* h) {
+    const GridDev& g = h->g;
+    FFields sp{};
+    for (int f = 0; f < 6; ++f) sp.p[f] = h->spec32[f];
+    CK(h, launch_vorticity_mixed(g, h->mx, h->ops, h->U, h->V, h->W, sp, h->stream));
+    mark(h, "vorticity32");
+    FRFields ph{};
+    for (int f = 0; f < 6; ++f) ph.p[f] = h->phys32[f];
+    CK(h, fft_c2r32(h->fft, g, sp, ph, 6, g.nz, h->stream));
+    FRFields prod{};
+    for (int f = 0; f < 3; ++f) prod.p[f] = h->phys32[f];
+    CK(h, launch_products32(g, ph, prod, h->stream));
+    mark(h, "products32");
+    FFields src{};
+    for (int f = 0; f < 3; ++f) src.p[f] = h->src32[f];
+    CK(h, fft_r2c32(h->fft, g, prod, src, 3, g.nz, h->stream));
+    return DNS3D_OK;
+}
+
 int run_source_terms(dns3d_handle* h) {
     const GridDev& g = h->g;
     CK(h, launch_pi_update(g, h->ops, h->pp, h->U, h->d_pi, h->stream));
     mark(h, "pi_update");
+    if (h->mixed) return run_source_terms_mixed(h);
     // vorticity into the u*,v*,w* buffers (free until the viscous step)
     CK(h, launch_vorticity(g, h->ops, h->U, h->V, h->W, h->US, h->VS, h->WS, h->stream));
     mark(h, "vorticity");
@@ -217,6 +243,16 @@ int run_source_terms(dns3d_handle* h) {
 }
 
 int run_viscous(dns3d_handle* h) {
+    if (h->mixed) {
+        Fields F{}, O{};
+        FFields S{};
+        F.p[0] = h->U; F.p[1] = h->V; F.p[2] = h->W;
+        O.p[0] = h->US; O.p[1] = h->VS; O.p[2] = h->WS;
+        for (int f = 0; f < 3; ++f) S.p[f] = h->src32[f];
+        CK(h, launch_viscous_mixed(h->g, h->mx, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->stream));
+        mark(h, "viscous_mixed");
+        return DNS3D_OK;
+    }
     Fields F{}, S{}, O{};
     F.p[0] = h->U; F.p[1] = h->V; F.p[2] = h->W;
     S.p[0] = h->SU; S.p[1] = h->SV; S.p[2] = h->SW;
@@ -227,12 +263,23 @@ int run_viscous(dns3d_handle* h) {
 }
 
 int run_pressure(dns3d_handle* h) {
+    if (h->mixed) {
+        CK(h, launch_pressure_mixed(h->g, h->mx, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->stream));
+        mark(h, "pressure_mixed");
+        return DNS3D_OK;
+    }
     CK(h, launch_pressure(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->stream));
     mark(h, "pressure_poisson");
     return DNS3D_OK;
 }
 
 int run_correction(dns3d_handle* h) {
+    if (h->mixed) {
+        CK(h, launch_correction_mixed(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->U, h->V, h->W,
+                                      h->P, h->GP, h->stream));
+        mark(h, "correction_mixed");
+        return DNS3D_OK;
+    }
     CK(h, launch_correction(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
                             h->GP, h->stream));
     mark(h, "pressure_correction");
@@ -317,6 +364,8 @@ int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
     b += 6 * pe * sizeof(double);            // physical fields
     const size_t hz = (size_t)c->nz / 2, ez = (size_t)c->nz - hz;
     b += (2 * nq * (ez * ez + hz * hz) + 2 * nz2) * sizeof(double);  // folded inverses, pinned, S
+    if (c->precision == DNS3D_PREC_MIXED)
+        b += (6 + 3 + 6) * se * sizeof(float2) + 6 * pe * sizeof(float) + se * sizeof(double2);  // + dphi/dz
     b += 16ull << 20;                        // operators, tables, reductions
     *bytes = b;
     return DNS3D_OK;
@@ -448,6 +497,82 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
         cudaStreamSynchronize(h->stream) != cudaSuccess)
         return fail(DNS3D_E_CUDA);
     if (info != 0) return fail(DNS3D_E_SINGULAR);
+
+    if (c.precision == DNS3D_PREC_MIXED) {
+        h->mixed = true;
+        // eigenbasis of the interior Helmholtz problem, S_II V = M_II V Lambda
+        const int ni = nz - 2;
+        std::vector<double> C((size_t)ni * ni), lam, Y;
+        for (int i = 0; i < ni; ++i)
+            for (int j = 0; j < ni; ++j)
+                C[(size_t)i * ni + j] = S[(size_t)(i + 1) * nz + (j + 1)] / std::sqrt(wh[i + 1] * wh[j + 1]);
+        jacobi_eigen(ni, C, lam, Y);
+        const int nip = (ni + 3) / 4 * 4, nzp = (nz + 3) / 4 * 4;
+        std::vector<float> Vf((size_t)ni * nip, 0.f), VtMf((size_t)ni * nip, 0.f), lamf(ni), s0f(ni), snf(ni);
+        for (int i = 0; i < ni; ++i)
+            for (int j = 0; j < ni; ++j) {
+                const double y = Y[(size_t)i * ni + j];
+                Vf[(size_t)j * nip + i] = (float)(y / std::sqrt(wh[i + 1]));     // V[i][j] at [j][i]
+                VtMf[(size_t)i * nip + j] = (float)(y * std::sqrt(wh[i + 1]));   // (V^T M)[j][i] at [i][j]
+            }
+        for (int j = 0; j < ni; ++j) {
+            double a0 = 0.0, an = 0.0;
+            for (int i = 0; i < ni; ++i) {
+                const double v = Y[(size_t)i * ni + j] / std::sqrt(wh[i + 1]);
+                a0 += v * S[(size_t)(i + 1) * nz + 0];
+                an += v * S[(size_t)(i + 1) * nz + nz - 1];
+            }
+            lamf[j] = (float)lam[j];
+            s0f[j] = (float)a0;
+            snf[j] = (float)an;
+        }
+        std::vector<float> D1e32(D1e.begin(), D1e.end()), D1o32(D1o.begin(), D1o.end());
+        // eigenbasis of the full Neumann problem S V' = M V' Lambda'
+        std::vector<double> Cf((size_t)nz * nz), plam, PY;
+        for (int i = 0; i < nz; ++i)
+            for (int j = 0; j < nz; ++j) Cf[(size_t)i * nz + j] = S[(size_t)i * nz + j] / std::sqrt(wh[i] * wh[j]);
+        jacobi_eigen(nz, Cf, plam, PY);
+        std::vector<float> PV((size_t)nz * nzp, 0.f), PVT((size_t)nz * nzp, 0.f), PDVT((size_t)nz * nzp, 0.f),
+            plamf(nz);
+        for (int z = 0; z < nz; ++z)
+            for (int j = 0; j < nz; ++j) {
+                const double v = PY[(size_t)z * nz + j] / std::sqrt(wh[z]);
+                PV[(size_t)z * nzp + j] = (float)v;
+                PVT[(size_t)j * nzp + z] = (float)v;
+            }
+        for (int z = 0; z < nz; ++z)
+            for (int j = 0; j < nz; ++j) {
+                double a = 0.0;
+                for (int q = 0; q < nz; ++q) a += D1s[(size_t)z * nz + q] * PY[(size_t)q * nz + j] / std::sqrt(wh[q]);
+                PDVT[(size_t)j * nzp + z] = (float)a;
+            }
+        for (int j = 0; j < nz; ++j) plamf[j] = (float)plam[j];
+        MixedOps& mx = h->mx;
+        mx.nip = nip;
+        mx.nzp = nzp;
+        if ((rc = dev_alloc(h, &mx.VT, Vf.size())) || (rc = dev_alloc(h, &mx.VtMT, VtMf.size())) ||
+            (rc = dev_alloc(h, &mx.lam, ni)) || (rc = dev_alloc(h, &mx.s0, ni)) || (rc = dev_alloc(h, &mx.sn, ni)) ||
+            (rc = dev_alloc(h, &mx.D1e, D1e32.size())) || (rc = dev_alloc(h, &mx.D1o, D1o32.size())) ||
+            (rc = dev_alloc(h, &mx.PV, PV.size())) || (rc = dev_alloc(h, &mx.PVT, PVT.size())) ||
+            (rc = dev_alloc(h, &mx.PDVT, PDVT.size())) || (rc = dev_alloc(h, &mx.plam, nz)) ||
+            (rc = dev_alloc(h, &h->PHIZ, se)))
+            return fail(rc);
+        struct Up32 { void* d; const void* s; size_t b; } u32[] = {
+            {mx.VT, Vf.data(), Vf.size() * 4}, {mx.VtMT, VtMf.data(), VtMf.size() * 4},
+            {mx.lam, lamf.data(), (size_t)ni * 4}, {mx.s0, s0f.data(), (size_t)ni * 4},
+            {mx.sn, snf.data(), (size_t)ni * 4}, {mx.D1e, D1e32.data(), D1e32.size() * 4},
+            {mx.D1o, D1o32.data(), D1o32.size() * 4}, {mx.PV, PV.data(), PV.size() * 4},
+            {mx.PVT, PVT.data(), PVT.size() * 4}, {mx.PDVT, PDVT.data(), PDVT.size() * 4},
+            {mx.plam, plamf.data(), (size_t)nz * 4}};
+        for (auto& u : u32)
+            if ((rc = upload(h, u.d, u.s, u.b))) return fail(rc);
+        for (int f = 0; f < 6; ++f)
+            if ((rc = dev_alloc(h, &h->spec32[f], se)) || (rc = dev_alloc(h, &h->phys32[f], pe))) return fail(rc);
+        for (int f = 0; f < 3; ++f)
+            if ((rc = dev_alloc(h, &h->src32[f], se))) return fail(rc);
+        if ((rc = dev_alloc(h, &h->fft.tmp32, 6 * se))) return fail(rc);
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(DNS3D_E_CUDA);
+    }
 
     // step parameters
     StepParams& sp = h->sp;

@@ -27,12 +27,14 @@ namespace dns3d {
 constexpr int kMaxFields = 8;
 constexpr int kMaxStages = 12;
 
-struct Fields {
-    double2* p[kMaxFields];
+template <typename C>
+struct FieldsT {
+    C* p[kMaxFields];
 };
-struct RFields {
-    double* p[kMaxFields];
-};
+using Fields = FieldsT<double2>;    // FP64 spectral
+using RFields = FieldsT<double>;    // FP64 physical
+using FFields = FieldsT<float2>;    // FP32 spectral
+using FRFields = FieldsT<float>;    // FP32 physical
 
 // Radix schedule of one complex FFT length (Stockham autosort, radices 4/2/3).
 struct FftPlan1D {
@@ -69,7 +71,11 @@ struct FftCtx {
     double2* tw_ny;      // e^{-2 pi i t/ny}, t < ny
     double2* tw_nx2;     // e^{-2 pi i t/(nx/2)}
     double2* tw_nx;      // e^{-2 pi i t/nx}, t < nx/2+1
+    float2* tw32_ny;     // FP32 copies of the tables (mixed path)
+    float2* tw32_nx2;
+    float2* tw32_nx;
     double2* tmp;        // spectral scratch for nf fields
+    float2* tmp32 = nullptr;  // FP32 spectral scratch (mixed path)
     int tmp_fields;
     // optional per-launch hook (profiling): called after each kernel launch
     void (*hook)(void*, const char*) = nullptr;
@@ -83,6 +89,11 @@ cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields ph
 // phys[f] -> spec[f].
 cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf,
                     int nplanes, cudaStream_t s);
+// FP32 versions (same transform definitions), scratch ctx.tmp32.
+cudaError_t fft_c2r32(const FftCtx& ctx, const GridDev& g, FFields spec, FRFields phys, int nf,
+                      int nplanes, cudaStream_t s);
+cudaError_t fft_r2c32(const FftCtx& ctx, const GridDev& g, FRFields phys, FFields spec, int nf,
+                      int nplanes, cudaStream_t s);
 
 // ---------------------------------------------------------------- step.cu
 struct StepParams {
@@ -119,6 +130,29 @@ struct Ops {
     int nq;
 };
 
+// Mixed-precision operators (FP32): folded D for the nonlinear term and the
+// eigenbasis of the interior Helmholtz problem S_II V = M_II V Lambda
+// (ni = nz - 2 interior levels).
+// Mixed-precision operators (FP32): folded D for the nonlinear term, the
+// eigenbasis of the interior Helmholtz problem S_II V = M_II V Lambda
+// (ni = nz - 2 interior levels) and of the full Neumann problem
+// S V' = M V' Lambda'.  The GEMM operands are stored with their output-row
+// index innermost and padded to a multiple of 4 (nip, nzp) with zeros, so one
+// float4 load feeds four output rows.
+struct MixedOps {
+    float* D1e; float* D1o;  // folded (2/ybar) d1, FP32
+    int nip, nzp;            // ni and nz rounded up to multiples of 4
+    float* VtMT;             // [ni][nip]  (V^T M_II)[j][i] stored at [i][j]
+    float* VT;               // [ni][nip]  V[i][j] stored at [j][i]
+    float* lam;              // [ni]       eigenvalues
+    float* s0;               // [ni]       V^T S_I1
+    float* sn;               // [ni]       V^T S_In
+    float* PV;               // [nz][nzp]  V'[z][j] stored at [z][j]
+    float* PVT;              // [nz][nzp]  V'[z][j] stored at [j][z]
+    float* PDVT;             // [nz][nzp]  (D V')[z][j] stored at [j][z]
+    float* plam;             // [nz]       eigenvalues l'_j
+};
+
 struct PIParams {
     int method;
     int istart;
@@ -139,6 +173,20 @@ cudaError_t launch_products(const GridDev& g, RFields in6, RFields out3, cudaStr
 cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& sp,
                            Fields F, Fields Src, const double2* GP,
                            const dns3d_pi_state* pi, Fields Out, cudaStream_t s);
+cudaError_t launch_vorticity_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops,
+                                   const double2* U, const double2* V, const double2* W, FFields out,
+                                   cudaStream_t s);
+cudaError_t launch_pressure_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops,
+                                  const StepParams& sp, const double2* US, const double2* VS,
+                                  const double2* WS, double2* PHI, double2* PHIZ, cudaStream_t s);
+cudaError_t launch_correction_mixed(const GridDev& g, const Ops& ops, const StepParams& sp,
+                                    const double2* US, const double2* VS, const double2* WS,
+                                    const double2* PHI, const double2* PHIZ, double2* U, double2* V,
+                                    double2* W, double2* P, double2* GP, cudaStream_t s);
+cudaError_t launch_products32(const GridDev& g, FRFields in6, FRFields out3, cudaStream_t s);
+cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops,
+                                 const StepParams& sp, Fields F, FFields Src, const double2* GP,
+                                 const dns3d_pi_state* pi, Fields Out, cudaStream_t s);
 cudaError_t launch_pressure(const GridDev& g, const Ops& ops, const StepParams& sp,
                             const double2* US, const double2* VS, const double2* WS,
                             double2* PHI, cudaStream_t s);
@@ -177,6 +225,10 @@ cudaError_t measure_fp64_tflops(int device, double* tflops);
 // ---------------------------------------------------------------- lgl.cpp
 void lgl_nodes_weights(int n, std::vector<double>& x, std::vector<double>& w);
 void lgl_diff_matrix(const std::vector<double>& x, bool guard, std::vector<double>& d);
+// Symmetric eigen-decomposition (cyclic Jacobi, FP64): a (n x n, row-major,
+// destroyed) = Y diag(w) Y^T; Y returned row-major with eigenvectors as columns,
+// eigenvalues ascending.
+void jacobi_eigen(int n, std::vector<double>& a, std::vector<double>& w, std::vector<double>& y);
 
 // ---------------------------------------------------------------- namelist.cpp
 int read_namelist_file(const char* path, dns3d_config* cfg);

@@ -43,17 +43,23 @@ FftPlan1D make_plan(int n) {
 
 namespace {
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+template <typename T> struct Cx;
+template <> struct Cx<double> { using type = double2; };
+template <> struct Cx<float> { using type = float2; };
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype(C::x) b) { C r; r.x = a; r.y = b; return r; }
+
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
 
 // One Stockham pass over `count` transforms of length n stored at a[c*ld + t].
 // SIGN = -1 forward (e^{-i}), +1 inverse.  tw[t] = e^{-2 pi i t/n}.
-template <int SIGN>
-__device__ void stockham_pass(const double2* __restrict__ a, double2* __restrict__ b, int count,
-                              int ld, int n, int R, int Ns, const double2* __restrict__ tw) {
+template <int SIGN, typename C>
+__device__ void stockham_pass(const C* __restrict__ a, C* __restrict__ b, int count,
+                              int ld, int n, int R, int Ns, const C* __restrict__ tw) {
+    using R_t = decltype(C::x);
     const int nb = n / R;
     const int total = count * nb;
     const int tstep = n / (Ns * R);
@@ -61,8 +67,8 @@ __device__ void stockham_pass(const double2* __restrict__ a, double2* __restrict
         const int c = t / nb;
         const int j = t - c * nb;
         const int k = j % Ns;
-        const double2* src = a + c * ld;
-        double2 v[4];
+        const C* src = a + c * ld;
+        C v[4];
 #pragma unroll
         for (int r = 0; r < 4; ++r)
             if (r < R) v[r] = src[j + r * nb];
@@ -70,18 +76,18 @@ __device__ void stockham_pass(const double2* __restrict__ a, double2* __restrict
 #pragma unroll
             for (int r = 1; r < 4; ++r) {
                 if (r < R) {
-                    double2 w = __ldg(&tw[r * k * tstep]);
+                    C w = tw[r * k * tstep];
                     if (SIGN > 0) w.y = -w.y;
                     v[r] = cmul(v[r], w);
                 }
             }
         }
-        double2 y[4];
+        C y[4];
         if (R == 4) {
-            const double2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-            const double2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+            const C s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+            const C s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
             // (SIGN i) * d13
-            const double2 id13 = SIGN > 0 ? make_double2(-d13.y, d13.x) : make_double2(d13.y, -d13.x);
+            const C id13 = SIGN > 0 ? mk<C>(-d13.y, d13.x) : mk<C>(d13.y, -d13.x);
             y[0] = cadd(s02, s13);
             y[2] = csub(s02, s13);
             y[1] = cadd(d02, id13);
@@ -90,17 +96,17 @@ __device__ void stockham_pass(const double2* __restrict__ a, double2* __restrict
             y[0] = cadd(v[0], v[1]);
             y[1] = csub(v[0], v[1]);
         } else {  // R == 3
-            const double h = 0.86602540378443864676;  // sqrt(3)/2
-            const double2 t1 = cadd(v[1], v[2]);
-            const double2 d = csub(v[1], v[2]);
-            const double2 m = make_double2(v[0].x - 0.5 * t1.x, v[0].y - 0.5 * t1.y);
+            const R_t h = (R_t)0.86602540378443864676;  // sqrt(3)/2
+            const C t1 = cadd(v[1], v[2]);
+            const C d = csub(v[1], v[2]);
+            const C m = mk<C>(v[0].x - (R_t)0.5 * t1.x, v[0].y - (R_t)0.5 * t1.y);
             // (SIGN i h) * d
-            const double2 id = SIGN > 0 ? make_double2(-h * d.y, h * d.x) : make_double2(h * d.y, -h * d.x);
+            const C id = SIGN > 0 ? mk<C>(-h * d.y, h * d.x) : mk<C>(h * d.y, -h * d.x);
             y[0] = cadd(v[0], t1);
             y[1] = cadd(m, id);
             y[2] = csub(m, id);
         }
-        double2* dst = b + c * ld;
+        C* dst = b + c * ld;
         const int base = (j / Ns) * Ns * R + k;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
@@ -109,15 +115,14 @@ __device__ void stockham_pass(const double2* __restrict__ a, double2* __restrict
 }
 
 // Runs all passes; returns the buffer holding the result.
-template <int SIGN>
-__device__ double2* stockham(double2* a, double2* b, int count, int ld, const FftPlan1D& pl,
-                             const double2* __restrict__ tw) {
+template <int SIGN, typename C>
+__device__ C* stockham(C* a, C* b, int count, int ld, const FftPlan1D& pl, const C* __restrict__ tw) {
     int Ns = 1;
     for (int s = 0; s < pl.nstages; ++s) {
         const int R = pl.radix[s];
         stockham_pass<SIGN>(a, b, count, ld, pl.n, R, Ns, tw);
         __syncthreads();
-        double2* t = a;
+        C* t = a;
         a = b;
         b = t;
         Ns *= R;
@@ -127,24 +132,25 @@ __device__ double2* stockham(double2* a, double2* b, int count, int ld, const Ff
 
 // Complex FFT along y of kx-columns [kx0, kx0+cx) of one plane.
 // grid (ceil(nxhp/cx), nplanes, nf); smem 2*cx*(ny+1) double2.
-template <int SIGN>
-__global__ void __launch_bounds__(256) k_fft_y(Fields src, Fields dst, GridDev g, FftPlan1D pl,
-                                               const double2* __restrict__ tw, int cx) {
-    extern __shared__ double2 smem[];
+template <int SIGN, typename C>
+__global__ void __launch_bounds__(256) k_fft_y(FieldsT<C> src, FieldsT<C> dst, GridDev g, FftPlan1D pl,
+                                               const C* __restrict__ tw, int cx) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* smem = reinterpret_cast<C*>(smem_raw);
     const int ld = g.ny + 1;
-    double2* a = smem;
-    double2* b = smem + cx * ld;
+    C* a = smem;
+    C* b = smem + cx * ld;
     const int kx0 = blockIdx.x * cx;
     const size_t plane = (size_t)blockIdx.y * g.nm;
-    const double2* __restrict__ s = src.p[blockIdx.z] + plane;
-    double2* d = dst.p[blockIdx.z] + plane;
+    const C* __restrict__ s = src.p[blockIdx.z] + plane;
+    C* d = dst.p[blockIdx.z] + plane;
     const int ncol = min(cx, g.nxhp - kx0);
     for (int t = threadIdx.x; t < g.ny * cx; t += blockDim.x) {
         const int y = t / cx, c = t - y * cx;
         if (c < ncol) a[c * ld + y] = s[(size_t)y * g.nxhp + kx0 + c];
     }
     __syncthreads();
-    double2* r = stockham<SIGN>(a, b, ncol, ld, pl, tw);
+    C* r = stockham<SIGN>(a, b, ncol, ld, pl, tw);
     for (int t = threadIdx.x; t < g.ny * cx; t += blockDim.x) {
         const int y = t / cx, c = t - y * cx;
         if (c < ncol) d[(size_t)y * g.nxhp + kx0 + c] = r[c * ld + y];
@@ -153,79 +159,85 @@ __global__ void __launch_bounds__(256) k_fft_y(Fields src, Fields dst, GridDev g
 
 // c2r along x for rows [row0, row0+rx) (row = plane*ny + y) of one field.
 // grid (ceil(nrows/rx), nf); smem 2*rx*(nx/2+2) double2.
-__global__ void __launch_bounds__(256) k_c2r_x(Fields src, RFields dst, GridDev g, FftPlan1D pl,
-                                               const double2* __restrict__ tw_nx2,
-                                               const double2* __restrict__ tw_nx, int rx,
+template <typename T>
+__global__ void __launch_bounds__(256) k_c2r_x(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst, GridDev g,
+                                               FftPlan1D pl, const typename Cx<T>::type* __restrict__ tw_nx2,
+                                               const typename Cx<T>::type* __restrict__ tw_nx, int rx,
                                                int nrows) {
-    extern __shared__ double2 smem[];
+    using C = typename Cx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* smem = reinterpret_cast<C*>(smem_raw);
     const int n2 = g.nxh;
     const int ld = n2 + 2;
-    double2* a = smem;
-    double2* b = smem + rx * ld;
+    C* a = smem;
+    C* b = smem + rx * ld;
     const int row0 = blockIdx.x * rx;
     const int nr = min(rx, nrows - row0);
-    const double2* __restrict__ s = src.p[blockIdx.y] + (size_t)row0 * g.nxhp;
-    double2* d = reinterpret_cast<double2*>(dst.p[blockIdx.y] + (size_t)row0 * g.nx);
+    const C* __restrict__ s = src.p[blockIdx.y] + (size_t)row0 * g.nxhp;
+    C* d = reinterpret_cast<C*>(dst.p[blockIdx.y] + (size_t)row0 * g.nx);
     for (int t = threadIdx.x; t < nr * g.nxhp; t += blockDim.x) {
         const int r = t / g.nxhp, k = t - r * g.nxhp;
-        double2 v = s[t];
-        if (k == 0 || k == n2) v.y = 0.0;  // c2r uses Re only at kx = 0, nx/2
+        C v = s[t];
+        if (k == 0 || k == n2) v.y = (T)0;  // c2r uses Re only at kx = 0, nx/2
         a[r * ld + k] = v;
     }
     __syncthreads();
     // Z[k] = (X[k] + conj(X[n2-k])) + i e^{+2 pi i k/nx} (X[k] - conj(X[n2-k]))
     for (int t = threadIdx.x; t < nr * n2; t += blockDim.x) {
         const int r = t / n2, k = t - r * n2;
-        const double2 xa = a[r * ld + k];
-        const double2 xb = a[r * ld + n2 - k];
-        const double2 sm = make_double2(xa.x + xb.x, xa.y - xb.y);
-        const double2 df = make_double2(xa.x - xb.x, xa.y + xb.y);
-        double2 w = __ldg(&tw_nx[k]);
+        const C xa = a[r * ld + k];
+        const C xb = a[r * ld + n2 - k];
+        const C sm = mk<C>(xa.x + xb.x, xa.y - xb.y);
+        const C df = mk<C>(xa.x - xb.x, xa.y + xb.y);
+        C w = tw_nx[k];
         w.y = -w.y;
-        const double2 p = cmul(w, df);
-        b[r * ld + k] = make_double2(sm.x - p.y, sm.y + p.x);
+        const C p = cmul(w, df);
+        b[r * ld + k] = mk<C>(sm.x - p.y, sm.y + p.x);
     }
     __syncthreads();
-    double2* res = stockham<+1>(b, a, nr, ld, pl, tw_nx2);
-    const double sc = g.inv_nxny;
+    C* res = stockham<+1>(b, a, nr, ld, pl, tw_nx2);
+    const T sc = (T)g.inv_nxny;
     for (int t = threadIdx.x; t < nr * n2; t += blockDim.x) {
         const int r = t / n2, k = t - r * n2;
-        const double2 z = res[r * ld + k];
-        d[(size_t)r * n2 + k] = make_double2(z.x * sc, z.y * sc);
+        const C z = res[r * ld + k];
+        d[(size_t)r * n2 + k] = mk<C>(z.x * sc, z.y * sc);
     }
 }
 
 // r2c along x: rows of nx reals -> nxhp complex.
-__global__ void __launch_bounds__(256) k_r2c_x(RFields src, Fields dst, GridDev g, FftPlan1D pl,
-                                               const double2* __restrict__ tw_nx2,
-                                               const double2* __restrict__ tw_nx, int rx,
+template <typename T>
+__global__ void __launch_bounds__(256) k_r2c_x(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, GridDev g,
+                                               FftPlan1D pl, const typename Cx<T>::type* __restrict__ tw_nx2,
+                                               const typename Cx<T>::type* __restrict__ tw_nx, int rx,
                                                int nrows) {
-    extern __shared__ double2 smem[];
+    using C = typename Cx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* smem = reinterpret_cast<C*>(smem_raw);
     const int n2 = g.nxh;
     const int ld = n2 + 2;
-    double2* a = smem;
-    double2* b = smem + rx * ld;
+    C* a = smem;
+    C* b = smem + rx * ld;
     const int row0 = blockIdx.x * rx;
     const int nr = min(rx, nrows - row0);
-    const double2* __restrict__ s =
-        reinterpret_cast<const double2*>(src.p[blockIdx.y] + (size_t)row0 * g.nx);
-    double2* d = dst.p[blockIdx.y] + (size_t)row0 * g.nxhp;
+    const C* __restrict__ s = reinterpret_cast<const C*>(src.p[blockIdx.y] + (size_t)row0 * g.nx);
+    C* d = dst.p[blockIdx.y] + (size_t)row0 * g.nxhp;
     for (int t = threadIdx.x; t < nr * n2; t += blockDim.x) {
         const int r = t / n2, k = t - r * n2;
         a[r * ld + k] = s[t];  // z[m] = x[2m] + i x[2m+1]
     }
     __syncthreads();
-    double2* res = stockham<-1>(a, b, nr, ld, pl, tw_nx2);
-    double2* out = (res == a) ? b : a;
+    C* res = stockham<-1>(a, b, nr, ld, pl, tw_nx2);
+    C* out = (res == a) ? b : a;
     // X[k] = E + e^{-2 pi i k/nx} O,  E = (Z[k]+conj(Z[n2-k]))/2,  O = (Z[k]-conj(Z[n2-k]))/(2i)
     for (int t = threadIdx.x; t < nr * (n2 + 1); t += blockDim.x) {
         const int r = t / (n2 + 1), k = t - r * (n2 + 1);
-        const double2 za = res[r * ld + (k == n2 ? 0 : k)];
-        const double2 zb = res[r * ld + (k == 0 ? 0 : n2 - k)];
-        const double2 e = make_double2(0.5 * (za.x + zb.x), 0.5 * (za.y - zb.y));
-        const double2 o = make_double2(0.5 * (za.y + zb.y), -0.5 * (za.x - zb.x));
-        const double2 p = cmul(__ldg(&tw_nx[k]), o);
-        out[r * ld + k] = make_double2(e.x + p.x, e.y + p.y);
+        const C za = res[r * ld + (k == n2 ? 0 : k)];
+        const C zb = res[r * ld + (k == 0 ? 0 : n2 - k)];
+        const T hf = (T)0.5;
+        const C e = mk<C>(hf * (za.x + zb.x), hf * (za.y - zb.y));
+        const C o = mk<C>(hf * (za.y + zb.y), -hf * (za.x - zb.x));
+        const C p = cmul(tw_nx[k], o);
+        out[r * ld + k] = mk<C>(e.x + p.x, e.y + p.y);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < nr * g.nxhp; t += blockDim.x) {
@@ -247,21 +259,28 @@ int pick_rx(int n2) {
     return rx;
 }
 
-double2* upload_table(int n, int count) {
+template <typename C>
+C* upload_table(int n, int count) {
     // e^{-2 pi i t/n}, t < count, computed in long double and rounded once.
-    std::vector<double2> h(count);
+    std::vector<C> h(count);
     const long double pi = 3.141592653589793238462643383279502884L;
     for (int t = 0; t < count; ++t) {
         const long double ang = -2.0L * pi * (long double)t / (long double)n;
-        h[t] = make_double2((double)cosl(ang), (double)sinl(ang));
+        h[t].x = (decltype(C::x))cosl(ang);
+        h[t].y = (decltype(C::x))sinl(ang);
     }
-    double2* d = nullptr;
-    if (cudaMalloc(&d, sizeof(double2) * count) != cudaSuccess) return nullptr;
-    if (cudaMemcpy(d, h.data(), sizeof(double2) * count, cudaMemcpyHostToDevice) != cudaSuccess) {
+    C* d = nullptr;
+    if (cudaMalloc(&d, sizeof(C) * count) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, h.data(), sizeof(C) * count, cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(d);
         return nullptr;
     }
     return d;
+}
+
+template <typename K>
+cudaError_t smem_attr(K k, int bytes) {
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 }  // namespace
@@ -269,19 +288,24 @@ double2* upload_table(int n, int count) {
 cudaError_t fft_setup(FftCtx& ctx, const GridDev& g) {
     ctx.py = make_plan(g.ny);
     ctx.px2 = make_plan(g.nxh);
-    ctx.tw_ny = upload_table(g.ny, g.ny);
-    ctx.tw_nx2 = upload_table(g.nxh, g.nxh);
-    ctx.tw_nx = upload_table(g.nx, g.nxh + 1);
-    if (!ctx.tw_ny || !ctx.tw_nx2 || !ctx.tw_nx) return cudaErrorMemoryAllocation;
+    ctx.tw_ny = upload_table<double2>(g.ny, g.ny);
+    ctx.tw_nx2 = upload_table<double2>(g.nxh, g.nxh);
+    ctx.tw_nx = upload_table<double2>(g.nx, g.nxh + 1);
+    ctx.tw32_ny = upload_table<float2>(g.ny, g.ny);
+    ctx.tw32_nx2 = upload_table<float2>(g.nxh, g.nxh);
+    ctx.tw32_nx = upload_table<float2>(g.nx, g.nxh + 1);
+    if (!ctx.tw_ny || !ctx.tw_nx2 || !ctx.tw_nx || !ctx.tw32_ny || !ctx.tw32_nx2 || !ctx.tw32_nx)
+        return cudaErrorMemoryAllocation;
     const int cx = pick_cx(g.ny);
     const int rx = pick_rx(g.nxh);
     const int sy = 2 * cx * (g.ny + 1) * (int)sizeof(double2);
     const int sx = 2 * rx * (g.nxh + 2) * (int)sizeof(double2);
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_fft_y<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sy))) return e;
-    if ((e = cudaFuncSetAttribute(k_fft_y<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sy))) return e;
-    if ((e = cudaFuncSetAttribute(k_c2r_x, cudaFuncAttributeMaxDynamicSharedMemorySize, sx))) return e;
-    if ((e = cudaFuncSetAttribute(k_r2c_x, cudaFuncAttributeMaxDynamicSharedMemorySize, sx))) return e;
+    if ((e = smem_attr(k_fft_y<-1, double2>, sy)) || (e = smem_attr(k_fft_y<+1, double2>, sy)) ||
+        (e = smem_attr(k_c2r_x<double>, sx)) || (e = smem_attr(k_r2c_x<double>, sx)) ||
+        (e = smem_attr(k_fft_y<-1, float2>, sy / 2)) || (e = smem_attr(k_fft_y<+1, float2>, sy / 2)) ||
+        (e = smem_attr(k_c2r_x<float>, sx / 2)) || (e = smem_attr(k_r2c_x<float>, sx / 2)))
+        return e;
     return cudaSuccess;
 }
 
@@ -289,43 +313,78 @@ void fft_release(FftCtx& ctx) {
     cudaFree(ctx.tw_ny);
     cudaFree(ctx.tw_nx2);
     cudaFree(ctx.tw_nx);
+    cudaFree(ctx.tw32_ny);
+    cudaFree(ctx.tw32_nx2);
+    cudaFree(ctx.tw32_nx);
     ctx.tw_ny = ctx.tw_nx2 = ctx.tw_nx = nullptr;
+    ctx.tw32_ny = ctx.tw32_nx2 = ctx.tw32_nx = nullptr;
 }
 
-cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, int nf,
-                    int nplanes, cudaStream_t s) {
+namespace {
+
+template <typename T>
+cudaError_t c2r_impl(const FftCtx& ctx, const GridDev& g, FieldsT<typename Cx<T>::type> spec, FieldsT<T> phys,
+                     FieldsT<typename Cx<T>::type> tmp, int nf, int nplanes, cudaStream_t s,
+                     const typename Cx<T>::type* twy, const typename Cx<T>::type* twx2,
+                     const typename Cx<T>::type* twx) {
+    using C = typename Cx<T>::type;
+    const int cx = pick_cx(g.ny);
+    dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
+    k_fft_y<+1, C><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(C), s>>>(spec, tmp, g, ctx.py, twy, cx);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_inverse" : "fft32_y_inverse");
+    const int rx = pick_rx(g.nxh);
+    const int nrows = nplanes * g.ny;
+    dim3 gx((nrows + rx - 1) / rx, nf);
+    k_c2r_x<T><<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(C), s>>>(tmp, phys, g, ctx.px2, twx2, twx, rx, nrows);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_x_c2r" : "fft32_x_c2r");
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t r2c_impl(const FftCtx& ctx, const GridDev& g, FieldsT<T> phys, FieldsT<typename Cx<T>::type> spec,
+                     int nf, int nplanes, cudaStream_t s, const typename Cx<T>::type* twy,
+                     const typename Cx<T>::type* twx2, const typename Cx<T>::type* twx) {
+    using C = typename Cx<T>::type;
+    const int rx = pick_rx(g.nxh);
+    const int nrows = nplanes * g.ny;
+    dim3 gx((nrows + rx - 1) / rx, nf);
+    k_r2c_x<T><<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(C), s>>>(phys, spec, g, ctx.px2, twx2, twx, rx, nrows);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_x_r2c" : "fft32_x_r2c");
+    const int cx = pick_cx(g.ny);
+    dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
+    k_fft_y<-1, C><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(C), s>>>(spec, spec, g, ctx.py, twy, cx);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_forward" : "fft32_y_forward");
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, int nf, int nplanes,
+                    cudaStream_t s) {
     if (nf > ctx.tmp_fields || nf > kMaxFields) return cudaErrorInvalidValue;
     Fields tmp{};
     for (int f = 0; f < nf; ++f) tmp.p[f] = ctx.tmp + (size_t)f * g.nm * g.nz;
-    const int cx = pick_cx(g.ny);
-    dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
-    k_fft_y<+1><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(double2), s>>>(spec, tmp, g, ctx.py,
-                                                                       ctx.tw_ny, cx);
-    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_y_inverse");
-    const int rx = pick_rx(g.nxh);
-    const int nrows = nplanes * g.ny;
-    dim3 gx((nrows + rx - 1) / rx, nf);
-    k_c2r_x<<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(double2), s>>>(tmp, phys, g, ctx.px2,
-                                                                    ctx.tw_nx2, ctx.tw_nx, rx, nrows);
-    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_c2r");
-    return cudaGetLastError();
+    return c2r_impl<double>(ctx, g, spec, phys, tmp, nf, nplanes, s, ctx.tw_ny, ctx.tw_nx2, ctx.tw_nx);
 }
 
-cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf,
-                    int nplanes, cudaStream_t s) {
+cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf, int nplanes,
+                    cudaStream_t s) {
     if (nf > kMaxFields) return cudaErrorInvalidValue;
-    const int rx = pick_rx(g.nxh);
-    const int nrows = nplanes * g.ny;
-    dim3 gx((nrows + rx - 1) / rx, nf);
-    k_r2c_x<<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(double2), s>>>(phys, spec, g, ctx.px2,
-                                                                    ctx.tw_nx2, ctx.tw_nx, rx, nrows);
-    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_r2c");
-    const int cx = pick_cx(g.ny);
-    dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
-    k_fft_y<-1><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(double2), s>>>(spec, spec, g, ctx.py,
-                                                                       ctx.tw_ny, cx);
-    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_y_forward");
-    return cudaGetLastError();
+    return r2c_impl<double>(ctx, g, phys, spec, nf, nplanes, s, ctx.tw_ny, ctx.tw_nx2, ctx.tw_nx);
+}
+
+cudaError_t fft_c2r32(const FftCtx& ctx, const GridDev& g, FFields spec, FRFields phys, int nf, int nplanes,
+                      cudaStream_t s) {
+    if (nf > ctx.tmp_fields || nf > kMaxFields || !ctx.tmp32) return cudaErrorInvalidValue;
+    FFields tmp{};
+    for (int f = 0; f < nf; ++f) tmp.p[f] = ctx.tmp32 + (size_t)f * g.nm * g.nz;
+    return c2r_impl<float>(ctx, g, spec, phys, tmp, nf, nplanes, s, ctx.tw32_ny, ctx.tw32_nx2, ctx.tw32_nx);
+}
+
+cudaError_t fft_r2c32(const FftCtx& ctx, const GridDev& g, FRFields phys, FFields spec, int nf, int nplanes,
+                      cudaStream_t s) {
+    if (nf > kMaxFields) return cudaErrorInvalidValue;
+    return r2c_impl<float>(ctx, g, phys, spec, nf, nplanes, s, ctx.tw32_ny, ctx.tw32_nx2, ctx.tw32_nx);
 }
 
 }  // namespace dns3d

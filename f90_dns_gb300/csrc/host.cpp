@@ -4,6 +4,7 @@
 //
 // Built with -ffp-contract=off so that the operators are the same on every
 // host architecture (no fused multiply-add contraction in the recurrences).
+#include <algorithm>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -102,6 +103,56 @@ void lgl_diff_matrix(const std::vector<double>& x, bool guard, std::vector<doubl
             }
         }
     }
+}
+
+// Cyclic Jacobi rotations until the off-diagonal mass is at rounding level.
+void jacobi_eigen(int n, std::vector<double>& a, std::vector<double>& w, std::vector<double>& y) {
+    y.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) y[(size_t)i * n + i] = 1.0;
+    auto A = [&](int i, int j) -> double& { return a[(size_t)i * n + j]; };
+    double diag2 = 0.0;
+    for (int i = 0; i < n; ++i) diag2 += A(i, i) * A(i, i);
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) off += A(p, q) * A(p, q);
+        if (off <= 1e-32 * diag2) break;
+        for (int p = 0; p < n; ++p) {
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A(p, q);
+                if (std::fabs(apq) < 1e-300) continue;
+                const double theta = (A(q, q) - A(p, p)) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; ++k) {
+                    const double akp = A(k, p), akq = A(k, q);
+                    A(k, p) = c * akp - s * akq;
+                    A(k, q) = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double apk = A(p, k), aqk = A(q, k);
+                    A(p, k) = c * apk - s * aqk;
+                    A(q, k) = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double ykp = y[(size_t)k * n + p], ykq = y[(size_t)k * n + q];
+                    y[(size_t)k * n + p] = c * ykp - s * ykq;
+                    y[(size_t)k * n + q] = s * ykp + c * ykq;
+                }
+            }
+        }
+    }
+    // sort ascending
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int i, int j) { return A(i, i) < A(j, j); });
+    w.resize(n);
+    std::vector<double> ys((size_t)n * n);
+    for (int c = 0; c < n; ++c) {
+        w[c] = A(idx[c], idx[c]);
+        for (int r = 0; r < n; ++r) ys[(size_t)r * n + c] = y[(size_t)r * n + idx[c]];
+    }
+    y.swap(ys);
 }
 
 // ------------------------------------------------------------------ namelist

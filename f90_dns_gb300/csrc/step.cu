@@ -279,8 +279,12 @@ __device__ __forceinline__ double2 viscous_rhs(const GridDev& g, const Ops& ops,
     return make_double2(rr.x * whz - (s0 * bc1.x + sn * bc2.x), rr.y * whz - (s0 * bc1.y + sn * bc2.y));
 }
 
+__device__ __forceinline__ double2 to_d2(double2 a) { return a; }
+__device__ __forceinline__ double2 to_d2(float2 a) { return make_double2((double)a.x, (double)a.y); }
+
+template <typename SrcC>
 __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams sp, Fields F,
-                                                 Fields Src, const double2* __restrict__ GP,
+                                                 FieldsT<SrcC> Src, const double2* __restrict__ GP,
                                                  const dns3d_pi_state* __restrict__ pi, Fields Out,
                                                  int tc) {
     extern __shared__ double2 sm[];
@@ -316,11 +320,11 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
         if (sp.cn_fac != 0.0) lap = sym_apply(ops.D2e, ops.D2o, tf + comp * tsz, k, c, tc, he, ho);
         const int z1 = k, z2 = nz - 1 - k;
         const size_t o1 = (size_t)z1 * g.nm + m, o2 = (size_t)z2 * g.nm + m;
-        const double2 b1 = viscous_rhs(g, ops, sp, comp, z1, m, ky, kx, F.p[comp][o1], Src.p[comp][o1], lap.a,
-                                       bc1, bc2, dpdx);
+        const double2 b1 = viscous_rhs(g, ops, sp, comp, z1, m, ky, kx, F.p[comp][o1], to_d2(Src.p[comp][o1]),
+                                       lap.a, bc1, bc2, dpdx);
         if (k < ho) {
-            const double2 b2 = viscous_rhs(g, ops, sp, comp, z2, m, ky, kx, F.p[comp][o2], Src.p[comp][o2],
-                                           lap.b, bc1, bc2, dpdx);
+            const double2 b2 = viscous_rhs(g, ops, sp, comp, z2, m, ky, kx, F.p[comp][o2],
+                                           to_d2(Src.p[comp][o2]), lap.b, bc1, bc2, dpdx);
             bt[k * tc + c] = make_double2(b1.x + b2.x, b1.y + b2.y);
             bt[(he + k) * tc + c] = make_double2(b1.x - b2.x, b1.y - b2.y);
         } else {
@@ -535,6 +539,421 @@ __global__ void __launch_bounds__(256) k_divergence(GridDev g, Ops ops, const do
     }
 }
 
+// ------------------------------------------------------------------ mixed precision
+// FP32 vorticity: the FP64 spectra of u, v, w are rounded to FP32 once and
+// omega is formed in FP32 (folded FP32 D); outputs u, v, w, ox, oy, oz (FP32)
+// feed the FP32 inverse transforms of the nonlinear term.
+__device__ __forceinline__ void fold_load32(float2* tile, const double2* __restrict__ src, const GridDev& g,
+                                            int m0, int tc, int he, int ho) {
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        float2 fe = make_float2(0.f, 0.f), fo = fe;
+        if (m < g.nm) {
+            const double2 a = src[(size_t)k * g.nm + m];
+            if (k < ho) {
+                const double2 b = src[(size_t)(g.nz - 1 - k) * g.nm + m];
+                const float ax = (float)a.x, ay = (float)a.y, bx = (float)b.x, by = (float)b.y;
+                fe = make_float2(ax + bx, ay + by);
+                fo = make_float2(ax - bx, ay - by);
+            } else {
+                fe = make_float2((float)a.x, (float)a.y);
+            }
+        }
+        tile[t] = fe;
+        if (k < ho) tile[(he + k) * tc + c] = fo;
+    }
+}
+
+__device__ __forceinline__ float2 fold_dot32(const float* __restrict__ erow, const float2* in, int len, int tc,
+                                             int c) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int j = 0; j < len; ++j) {
+        const float e = __ldg(&erow[j]);
+        const float2 a = in[j * tc + c];
+        acc.x = fmaf(e, a.x, acc.x);
+        acc.y = fmaf(e, a.y, acc.y);
+    }
+    return acc;
+}
+
+__global__ void __launch_bounds__(256) k_vorticity_mixed(GridDev g, MixedOps mx, Ops ops,
+                                                         const double2* __restrict__ U,
+                                                         const double2* __restrict__ V,
+                                                         const double2* __restrict__ W, FFields out, int tc) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* tu = reinterpret_cast<float2*>(smraw);
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
+    float2* tv = tu + nz * tc;
+    const int m0 = blockIdx.x * tc;
+    fold_load32(tu, U, g, m0, tc, he, ho);
+    fold_load32(tv, V, g, m0, tc, he, ho);
+    __syncthreads();
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        float2 due = fold_dot32(mx.D1e + (size_t)k * ho, tu + he * tc, ho, tc, c);
+        float2 dve = fold_dot32(mx.D1e + (size_t)k * ho, tv + he * tc, ho, tc, c);
+        float2 duo = make_float2(0.f, 0.f), dvo = duo;
+        if (k < ho) {
+            duo = fold_dot32(mx.D1o + (size_t)k * he, tu, he, tc, c);
+            dvo = fold_dot32(mx.D1o + (size_t)k * he, tv, he, tc, c);
+        }
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const float ax = (float)mi.ax, ay = (float)mi.ay;
+        const int npt = (k < ho) ? 2 : 1;
+        for (int p = 0; p < npt; ++p) {
+            const int z = p ? nz - 1 - k : k;
+            const size_t o = (size_t)z * g.nm + m;
+            const double2 wd = W[o], ud = U[o], vd = V[o];
+            const float2 w = make_float2((float)wd.x, (float)wd.y);
+            const float2 u = make_float2((float)ud.x, (float)ud.y);
+            const float2 v = make_float2((float)vd.x, (float)vd.y);
+            const float2 du = p ? make_float2(due.x - duo.x, due.y - duo.y) : make_float2(due.x + duo.x, due.y + duo.y);
+            const float2 dv = p ? make_float2(dve.x - dvo.x, dve.y - dvo.y) : make_float2(dve.x + dvo.x, dve.y + dvo.y);
+            // (i a) f = (-a f.y, a f.x)
+            out.p[0][o] = u;
+            out.p[1][o] = v;
+            out.p[2][o] = w;
+            out.p[3][o] = make_float2(-ay * w.y - dv.x, ay * w.x - dv.y);          // wy - vz
+            out.p[4][o] = make_float2(du.x + ax * w.y, du.y - ax * w.x);           // uz - wx
+            out.p[5][o] = make_float2(-ax * v.y + ay * u.y, ax * v.x - ay * u.x);  // vx - uy
+        }
+    }
+}
+
+__global__ void k_products32(FRFields in, FRFields out, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float u = in.p[0][i], v = in.p[1][i], w = in.p[2][i];
+        const float ox = in.p[3][i], oy = in.p[4][i], oz = in.p[5][i];
+        out.p[0][i] = v * oz - w * oy;
+        out.p[1][i] = w * ox - u * oz;
+        out.p[2][i] = u * oy - v * ox;
+    }
+}
+
+// Viscous step as an increment in the eigenbasis of the interior Helmholtz
+// problem.  With S_II V = M_II V Lambda, V^T M_II V = I, and the identity
+// M_I (d2 u)_I = -(S u)_I (LGL quadrature is exact for these products), the
+// reference's system H_II x_I = M_I rhs_I - 2 f (S_I1 bc1 + S_In bc2) gives
+//   x_I - u_I = V y,  y_j = -(c+f)(k^2+l_j) g_j ut_j
+//                          + g_j (dt St_j - c (s0_j u_1 + sn_j u_n) - 2f (s0_j bc1 + sn_j bc2))
+// with g_j = 1/(1 + f(k^2 + l_j)), ut = V^T M_I u_I, St = V^T M_I S_I,
+// s0 = V^T S_I1, sn = V^T S_In (c = explicit-diffusion factor, f = theta dt/Re).
+// All products are FP32; the increment is added to the FP64 state, so the
+// FP32 error scales with the (small) increment.  Mode (0,0) is skipped: it is
+// advanced in FP64 by k_viscous.
+__global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
+                                                       Fields F, FFields Src, const double2* __restrict__ GP,
+                                                       Fields Out, int tc) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int ni = g.nz - 2;
+    const int np = mx.nip;           // ni rounded up to a multiple of 4 (operators zero-padded)
+    const int nb = np / 4;           // row blocks of 4
+    const int tsz = np * tc;
+    float4* sA = reinterpret_cast<float4*>(smraw);   // VtMT [ni][nb] float4
+    float4* sB = sA + (size_t)ni * nb;                // VT   [ni][nb] float4
+    float2* tu = reinterpret_cast<float2*>(sB + (size_t)ni * nb);  // [np][tc] interior u (one component)
+    float2* ts = tu + tsz;                           // [np][tc] interior S
+    float2* ty = ts + tsz;                           // [np][tc] eigen-space update
+    float4* tw = reinterpret_cast<float4*>(ty + tsz);  // [tc] wall terms (x0, y0, xn, yn)
+    float* tk = reinterpret_cast<float*>(tw + tc);     // [tc] k^2 of the column (or -1: skip)
+    const int m0 = blockIdx.x * tc;
+    {
+        const float4* A = reinterpret_cast<const float4*>(mx.VtMT);
+        const float4* B = reinterpret_cast<const float4*>(mx.VT);
+        for (int t = threadIdx.x; t < ni * nb; t += blockDim.x) {
+            sA[t] = __ldg(&A[t]);
+            sB[t] = __ldg(&B[t]);
+        }
+    }
+    const float dt = (float)sp.dt, cf = (float)sp.cn_fac, ff = (float)sp.helm_f;
+    for (int comp = 0; comp < 3; ++comp) {
+        for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
+            const int i = t / tc, c = t - i * tc;
+            const int m = m0 + c;
+            float2 a = make_float2(0.f, 0.f), b = a;
+            if (m < g.nm && i < ni) {
+                const size_t o = (size_t)(i + 1) * g.nm + m;
+                const double2 u = F.p[comp][o];
+                a = make_float2((float)u.x, (float)u.y);
+                b = Src.p[comp][o];
+            }
+            tu[t] = a;
+            ts[t] = b;
+        }
+        for (int c = threadIdx.x; c < tc; c += blockDim.x) {
+            const int m = m0 + c;
+            float k2 = -1.f;
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (m < g.nm && m != 0) {
+                const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+                bool keep = true;
+                if (sp.dealias) {
+                    const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
+                    keep = !(kx > sp.kx_max || kyi > sp.ky_max);
+                }
+                k2 = (float)__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+                if (!keep) k2 = -2.f - k2;  // masked source: flag in the sign, k2 recovered below
+                const double2 u0 = F.p[comp][(size_t)m], un = F.p[comp][(size_t)(g.nz - 1) * g.nm + m];
+                double2 b1 = make_double2(0.0, 0.0), b2 = b1;
+                if (comp < 2) {
+                    const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
+                    const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                    b1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
+                    b2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
+                }
+                w = make_float4(cf * (float)u0.x + 2.0f * ff * (float)b1.x, cf * (float)u0.y + 2.0f * ff * (float)b1.y,
+                                cf * (float)un.x + 2.0f * ff * (float)b2.x, cf * (float)un.y + 2.0f * ff * (float)b2.y);
+            }
+            tk[c] = k2;
+            tw[c] = w;
+        }
+        __syncthreads();
+        // ut = V^T M u, st = V^T M S for 4 eigen-rows j0..j0+3 of one column
+        for (int t = threadIdx.x; t < nb * tc; t += blockDim.x) {
+            const int jb = t / tc, c = t - jb * tc;
+            const int j0 = 4 * jb;
+            float k2 = tk[c];
+            if (k2 == -1.f) {
+                for (int q = 0; q < 4; ++q) ty[(j0 + q) * tc + c] = make_float2(0.f, 0.f);
+                continue;
+            }
+            const bool keep = k2 >= 0.f;
+            if (!keep) k2 = -2.f - k2;
+            float2 ut[4], st[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) { ut[q] = make_float2(0.f, 0.f); st[q] = ut[q]; }
+            for (int i = 0; i < ni; ++i) {
+                const float4 e = sA[i * nb + jb];
+                const float2 a = tu[i * tc + c];
+                const float2 b = ts[i * tc + c];
+                ut[0].x = fmaf(e.x, a.x, ut[0].x); ut[0].y = fmaf(e.x, a.y, ut[0].y);
+                ut[1].x = fmaf(e.y, a.x, ut[1].x); ut[1].y = fmaf(e.y, a.y, ut[1].y);
+                ut[2].x = fmaf(e.z, a.x, ut[2].x); ut[2].y = fmaf(e.z, a.y, ut[2].y);
+                ut[3].x = fmaf(e.w, a.x, ut[3].x); ut[3].y = fmaf(e.w, a.y, ut[3].y);
+                st[0].x = fmaf(e.x, b.x, st[0].x); st[0].y = fmaf(e.x, b.y, st[0].y);
+                st[1].x = fmaf(e.y, b.x, st[1].x); st[1].y = fmaf(e.y, b.y, st[1].y);
+                st[2].x = fmaf(e.z, b.x, st[2].x); st[2].y = fmaf(e.z, b.y, st[2].y);
+                st[3].x = fmaf(e.w, b.x, st[3].x); st[3].y = fmaf(e.w, b.y, st[3].y);
+            }
+            if (!keep) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) st[q] = make_float2(0.f, 0.f);
+            }
+            const float4 w = tw[c];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = j0 + q;
+                if (j >= ni) { ty[j * tc + c] = make_float2(0.f, 0.f); continue; }
+                const float k2l = k2 + __ldg(&mx.lam[j]);
+                const float gj = 1.0f / (1.0f + ff * k2l);
+                const float cu_ = -(cf + ff) * k2l * gj;
+                const float s0 = __ldg(&mx.s0[j]), sn = __ldg(&mx.sn[j]);
+                const float lx = dt * st[q].x - (s0 * w.x + sn * w.z);
+                const float ly = dt * st[q].y - (s0 * w.y + sn * w.w);
+                ty[j * tc + c] = make_float2(cu_ * ut[q].x + gj * lx, cu_ * ut[q].y + gj * ly);
+            }
+        }
+        __syncthreads();
+        // delta_I = V y for 4 rows i0..i0+3; walls are the boundary values
+        for (int t = threadIdx.x; t < nb * tc; t += blockDim.x) {
+            const int ib = t / tc, c = t - ib * tc;
+            const int m = m0 + c;
+            if (tk[c] == -1.f) continue;
+            float2 d[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) d[q] = make_float2(0.f, 0.f);
+            for (int j = 0; j < ni; ++j) {
+                const float4 e = sB[j * nb + ib];
+                const float2 y = ty[j * tc + c];
+                d[0].x = fmaf(e.x, y.x, d[0].x); d[0].y = fmaf(e.x, y.y, d[0].y);
+                d[1].x = fmaf(e.y, y.x, d[1].x); d[1].y = fmaf(e.y, y.y, d[1].y);
+                d[2].x = fmaf(e.z, y.x, d[2].x); d[2].y = fmaf(e.z, y.y, d[2].y);
+                d[3].x = fmaf(e.w, y.x, d[3].x); d[3].y = fmaf(e.w, y.y, d[3].y);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int i = 4 * ib + q;
+                if (i >= ni) break;
+                const size_t o = (size_t)(i + 1) * g.nm + m;
+                const double2 u = F.p[comp][o];
+                Out.p[comp][o] = make_double2(u.x + (double)d[q].x, u.y + (double)d[q].y);
+            }
+            if (ib == 0) {  // x_1 = bc1, x_n = bc2 (identity rows)
+                for (int wall = 0; wall < 2; ++wall) {
+                    double2 bc = make_double2(0.0, 0.0);
+                    if (comp < 2) {
+                        const double2 gp = GP[(size_t)(2 * comp + wall) * g.nm + m];
+                        bc = make_double2(-sp.dt * gp.x, -sp.dt * gp.y);
+                    }
+                    Out.p[comp][(size_t)(wall ? g.nz - 1 : 0) * g.nm + m] = bc;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Pressure for the mixed form.  The right-hand side (the collocation
+// divergence of u*, or the weak form) is formed in FP64: D applied to the
+// full FP64 w* must not see FP32 rounding of w* (|D| ~ nz^2 would amplify it).
+// The Neumann Poisson operator is diagonal in the eigenbasis of the full
+// problem, S V' = M V' Lambda', V'^T M V' = I:
+//   phi = -V' diag(1/(l'_j + k^2)) V'^T b,   dphi/dz = -(D V') diag(...) V'^T b
+// evaluated in FP32; computing dphi/dz through the precomputed D V' keeps its
+// FP32 error relative to dphi/dz itself.  Mode (0,0) (pinned) is left to the
+// FP64 kernels.
+__global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
+                                                        const double2* __restrict__ US,
+                                                        const double2* __restrict__ VS,
+                                                        const double2* __restrict__ WS,
+                                                        double2* __restrict__ PHI, double2* __restrict__ PHIZ,
+                                                        int tc) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
+    const int np = mx.nzp, nb = np / 4;
+    double2* tw = reinterpret_cast<double2*>(smraw);   // folded w* (FP64)  [nz][tc]
+    float2* tb = reinterpret_cast<float2*>(tw + nz * tc);   // rhs b (FP32)  [np][tc]
+    float2* tp = tb + np * tc;                              // phi~ (FP32)  [np][tc]
+    const int m0 = blockIdx.x * tc;
+    fold_load(tw, WS, g, m0, tc, he, ho);
+    for (int t = threadIdx.x; t < (np - nz) * tc; t += blockDim.x) tb[nz * tc + t] = make_float2(0.f, 0.f);
+    __syncthreads();
+    const double* __restrict__ Ae = sp.weak_form ? ops.W1e : ops.D1e;
+    const double* __restrict__ Ao = sp.weak_form ? ops.W1o : ops.D1o;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        if (m >= g.nm || m == 0) {
+            tb[k * tc + c] = make_float2(0.f, 0.f);
+            tb[(nz - 1 - k) * tc + c] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const Pair dz = anti_apply(Ae, Ao, tw, k, c, tc, he, ho);
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const double2 b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
+        tb[k * tc + c] = make_float2((float)b1.x, (float)b1.y);
+        if (k < ho) {
+            const double2 b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
+            tb[(nz - 1 - k) * tc + c] = make_float2((float)b2.x, (float)b2.y);
+        }
+    }
+    __syncthreads();
+    // phi~_j = -(V'^T b)_j / (l'_j + k^2) for 4 rows j0..j0+3
+    for (int t = threadIdx.x; t < nb * tc; t += blockDim.x) {
+        const int jb = t / tc, c = t - jb * tc;
+        const int m = m0 + c;
+        const int j0 = 4 * jb;
+        float2 acc[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] = make_float2(0.f, 0.f);
+        if (m < g.nm && m != 0) {
+            const float4* __restrict__ A = reinterpret_cast<const float4*>(mx.PV) + jb;  // V'[z][j0..j0+3]
+            for (int z = 0; z < nz; ++z) {
+                const float4 e = __ldg(&A[(size_t)z * nb]);
+                const float2 b = tb[z * tc + c];
+                acc[0].x = fmaf(e.x, b.x, acc[0].x); acc[0].y = fmaf(e.x, b.y, acc[0].y);
+                acc[1].x = fmaf(e.y, b.x, acc[1].x); acc[1].y = fmaf(e.y, b.y, acc[1].y);
+                acc[2].x = fmaf(e.z, b.x, acc[2].x); acc[2].y = fmaf(e.z, b.y, acc[2].y);
+                acc[3].x = fmaf(e.w, b.x, acc[3].x); acc[3].y = fmaf(e.w, b.y, acc[3].y);
+            }
+            const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+            const float k2 = (float)__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = j0 + q;
+                const float sc = j < nz ? -1.0f / (__ldg(&mx.plam[j]) + k2) : 0.f;
+                acc[q] = make_float2(sc * acc[q].x, sc * acc[q].y);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tp[(j0 + q) * tc + c] = acc[q];
+    }
+    __syncthreads();
+    // phi = V' phi~, dphi/dz = (D V') phi~ for 4 rows z0..z0+3
+    for (int t = threadIdx.x; t < nb * tc; t += blockDim.x) {
+        const int zb = t / tc, c = t - zb * tc;
+        const int m = m0 + c;
+        if (m >= g.nm || m == 0) continue;
+        float2 ph[4], pz[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { ph[q] = make_float2(0.f, 0.f); pz[q] = ph[q]; }
+        const float4* __restrict__ A = reinterpret_cast<const float4*>(mx.PVT) + zb;    // V'[z0..z0+3][j]
+        const float4* __restrict__ B = reinterpret_cast<const float4*>(mx.PDVT) + zb;   // (D V')[z0..z0+3][j]
+        for (int j = 0; j < nz; ++j) {
+            const float4 a = __ldg(&A[(size_t)j * nb]);
+            const float4 d = __ldg(&B[(size_t)j * nb]);
+            const float2 q2 = tp[j * tc + c];
+            ph[0].x = fmaf(a.x, q2.x, ph[0].x); ph[0].y = fmaf(a.x, q2.y, ph[0].y);
+            ph[1].x = fmaf(a.y, q2.x, ph[1].x); ph[1].y = fmaf(a.y, q2.y, ph[1].y);
+            ph[2].x = fmaf(a.z, q2.x, ph[2].x); ph[2].y = fmaf(a.z, q2.y, ph[2].y);
+            ph[3].x = fmaf(a.w, q2.x, ph[3].x); ph[3].y = fmaf(a.w, q2.y, ph[3].y);
+            pz[0].x = fmaf(d.x, q2.x, pz[0].x); pz[0].y = fmaf(d.x, q2.y, pz[0].y);
+            pz[1].x = fmaf(d.y, q2.x, pz[1].x); pz[1].y = fmaf(d.y, q2.y, pz[1].y);
+            pz[2].x = fmaf(d.z, q2.x, pz[2].x); pz[2].y = fmaf(d.z, q2.y, pz[2].y);
+            pz[3].x = fmaf(d.w, q2.x, pz[3].x); pz[3].y = fmaf(d.w, q2.y, pz[3].y);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int z = 4 * zb + q;
+            if (z >= nz) break;
+            const size_t o = (size_t)z * g.nm + m;
+            PHI[o] = make_double2((double)ph[q].x, (double)ph[q].y);
+            PHIZ[o] = make_double2((double)pz[q].x, (double)pz[q].y);
+        }
+    }
+}
+
+// dphi/dz of mode (0,0) in FP64 (one CTA), after k_pressure has written phi.
+__global__ void __launch_bounds__(256) k_dz_mean_mode(GridDev g, Ops ops, const double2* __restrict__ PHI,
+                                                      double2* __restrict__ PHIZ) {
+    extern __shared__ double2 sm[];
+    const int he = ops.he, ho = ops.ho;
+    fold_load(sm, PHI, g, 0, 1, he, ho);
+    __syncthreads();
+    for (int k = threadIdx.x; k < he; k += blockDim.x) {
+        const Pair d = anti_apply(ops.D1e, ops.D1o, sm, k, 0, 1, he, ho);
+        PHIZ[(size_t)k * g.nm] = d.a;
+        if (k < ho) PHIZ[(size_t)(g.nz - 1 - k) * g.nm] = d.b;
+    }
+}
+
+// Pointwise correction of the mixed form (pressure_correction_3d, 3D:1903-1929)
+// with dphi/dz precomputed: u = u* - dt DX phi, v = v* - dt DY phi,
+// w = w* - dt dphi/dz, p += phi, wall gradients of the new p.
+__global__ void k_correction_mixed(GridDev g, Ops ops, StepParams sp, const double2* __restrict__ US,
+                                   const double2* __restrict__ VS, const double2* __restrict__ WS,
+                                   const double2* __restrict__ PHI, const double2* __restrict__ PHIZ,
+                                   double2* __restrict__ U, double2* __restrict__ V, double2* __restrict__ W,
+                                   double2* __restrict__ P, double2* __restrict__ GP) {
+    const size_t n = (size_t)g.nz * g.nm;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const double dt = sp.dt;
+    for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += stride) {
+        const int z = (int)(o / g.nm);
+        const int m = (int)(o - (size_t)z * g.nm);
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const double2 ph = PHI[o], pz = PHIZ[o];
+        const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
+        const double2 us = US[o], vs = VS[o], ws = WS[o];
+        U[o] = make_double2(us.x - dt * px.x, us.y - dt * px.y);
+        V[o] = make_double2(vs.x - dt * py.x, vs.y - dt * py.y);
+        W[o] = make_double2(ws.x - dt * pz.x, ws.y - dt * pz.y);
+        double2 pp = P[o];
+        pp.x += ph.x;
+        pp.y += ph.y;
+        P[o] = pp;
+        if (z == 0 || z == g.nz - 1) {
+            const int wall = (z == 0) ? 0 : 1;
+            GP[(size_t)wall * g.nm + m] = i_times(mi.ax, pp);
+            GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, pp);
+        }
+    }
+}
+
 // ------------------------------------------------------------------ reductions
 __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -640,10 +1059,33 @@ cudaError_t set_smem(K kern, size_t bytes) {
 
 }  // namespace
 
+int pad4(int n) { return (n + 3) / 4 * 4; }
+
+size_t viscous_mixed_smem(const GridDev& g, int tc) {
+    const size_t ni = g.nz - 2, np = pad4(g.nz - 2);
+    return 2 * ni * np * sizeof(float) + 3 * np * tc * sizeof(float2) + tc * (sizeof(float4) + sizeof(float));
+}
+
+int tile_cols_mixed(const GridDev& g) {
+    int tc = 32;
+    while (tc > 4 && (viscous_mixed_smem(g, tc) > 110 * 1024 || (g.nm + tc - 1) / tc < 152)) tc >>= 1;
+    return tc;
+}
+
+size_t pressure_mixed_smem(const GridDev& g, int tc) {
+    return (size_t)g.nz * tc * sizeof(double2) + 2 * (size_t)pad4(g.nz) * tc * sizeof(float2);
+}
+
 cudaError_t prepare_step_kernels(const GridDev& g) {
     cudaError_t e;
+    if ((e = set_smem(k_pressure, (2 * (size_t)g.nz + g.nz) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_correction, (size_t)g.nz * sizeof(double2)))) return e;
+    if ((e = set_smem(k_pressure_mixed, pressure_mixed_smem(g, tile_cols(g, 2))))) return e;
+    if ((e = set_smem(k_viscous<float2>, 6 * (size_t)g.nz * sizeof(double2)))) return e;
+    if ((e = set_smem(k_vorticity_mixed, 2 * (size_t)g.nz * tile_cols(g, 1) * sizeof(float2)))) return e;
+    if ((e = set_smem(k_viscous_mixed, viscous_mixed_smem(g, tile_cols_mixed(g))))) return e;
     if ((e = set_smem(k_vorticity, 2 * (size_t)g.nz * tile_cols(g, 2) * sizeof(double2)))) return e;
-    if ((e = set_smem(k_viscous, 6 * (size_t)g.nz * tile_cols(g, 6) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_viscous<double2>, 6 * (size_t)g.nz * tile_cols(g, 6) * sizeof(double2)))) return e;
     if ((e = set_smem(k_pressure, (2 * (size_t)g.nz * tile_cols(g, 2) + g.nz) * sizeof(double2)))) return e;
     if ((e = set_smem(k_correction, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
     if ((e = set_smem(k_divergence, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
@@ -677,7 +1119,56 @@ cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& s
                            cudaStream_t s) {
     const int tc = tile_cols(g, 6);
     const size_t sm = 6 * (size_t)g.nz * tc * sizeof(double2);
-    k_viscous<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, F, Src, GP, pi, Out, tc);
+    k_viscous<double2><<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, F, Src, GP, pi, Out, tc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vorticity_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const double2* U,
+                                   const double2* V, const double2* W, FFields out, cudaStream_t s) {
+    const int tc = tile_cols(g, 1);
+    const size_t sm = 2 * (size_t)g.nz * tc * sizeof(float2);
+    k_vorticity_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, U, V, W, out, tc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const StepParams& sp,
+                                  const double2* US, const double2* VS, const double2* WS, double2* PHI,
+                                  double2* PHIZ, cudaStream_t s) {
+    // mode (0,0) in FP64: pinned Poisson, then its dphi/dz
+    k_pressure<<<1, 256, (2 * (size_t)g.nz + g.nz) * sizeof(double2), s>>>(g, ops, sp, US, VS, WS, PHI, 1);
+    k_dz_mean_mode<<<1, 64, (size_t)g.nz * sizeof(double2), s>>>(g, ops, PHI, PHIZ);
+    const int tc = tile_cols(g, 2);
+    const size_t sm = pressure_mixed_smem(g, tc);
+    k_pressure_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_correction_mixed(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                                    const double2* VS, const double2* WS, const double2* PHI, const double2* PHIZ,
+                                    double2* U, double2* V, double2* W, double2* P, double2* GP, cudaStream_t s) {
+    const size_t n = (size_t)g.nz * g.nm;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_correction_mixed<<<blocks, 256, 0, s>>>(g, ops, sp, US, VS, WS, PHI, PHIZ, U, V, W, P, GP);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_products32(const GridDev& g, FRFields in6, FRFields out3, cudaStream_t s) {
+    const size_t n = (size_t)g.nx * g.ny * g.nz;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_products32<<<blocks, 256, 0, s>>>(in6, out3, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const StepParams& sp,
+                                 Fields F, FFields Src, const double2* GP, const dns3d_pi_state* pi, Fields Out,
+                                 cudaStream_t s) {
+    // mode (0,0): FP64 Helmholtz with the forcing (one CTA, one mode)
+    k_viscous<float2><<<1, 256, 6 * (size_t)g.nz * sizeof(double2), s>>>(g, ops, sp, F, Src, GP, pi, Out, 1);
+    const int tc = tile_cols_mixed(g);
+    const size_t sm = viscous_mixed_smem(g, tc);
+    k_viscous_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, F, Src, GP, Out, tc);
     return cudaGetLastError();
 }
 

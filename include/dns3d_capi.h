@@ -35,6 +35,9 @@ extern "C" {
 #define DNS3D_E_NODEVICE 8     /* no CUDA device                              */
 
 #define DNS3D_PREC_FP64 0      /* plain FP64 path                            */
+#define DNS3D_PREC_MIXED 1     /* FP32 nonlinear term and viscous increment;
+                                  FP64 state, (0,0) mode, PI controller, wall
+                                  rows, pressure projection and diagnostics  */
 
 /* Namelist parameters of read_input_3d (DNS_pressure_BC_3D.f90:559-568,
  * defaults 571-603).  alpha, beta and ybar are derived (3D:740-742), the
