@@ -262,6 +262,29 @@ def run_ours(args) -> None:
                                    "max_div_abs_diff": abs(da.max_div - db.max_div)},
                  "kernels": {k: {"launches": n, "avg_ms": t / n, "share": t / tot_m} for k, (n, t) in prof_m.items()}}
 
+    # batched ensemble: seed-drawn runs of uneven grids, one graph launch per step
+    ensemble = None
+    if args.ensemble_runs > 0:
+        from f90_dns_gb300 import Ensemble
+        from f90_dns_gb300.capi import PREC_MIXED
+        from f90_dns_gb300.workloads import ensemble_draws
+        draws = ensemble_draws(args.ensemble_runs, seed=args.seed)
+        res = {}
+        for label, prec in (("mixed", PREC_MIXED), ("fp64", 0)):
+            with Ensemble([config_from(d, device=local, precision=prec) for d in draws]) as ens:
+                ens.step(args.warmup)
+                _barrier(dist)
+                ms_e = ens.step_timed(args.ensemble_steps)
+                pts_e = sum(point_count(d) for d in draws)
+                v_e, ms_e = replica_throughput(dist, ws, pts_e, args.ensemble_steps, ms_e)
+                res[label] = {"value": v_e, "unit": "point-steps/s", "ms_per_step": ms_e / args.ensemble_steps}
+        ensemble = {"runs": args.ensemble_runs, "seed": args.seed, "steps": args.ensemble_steps,
+                    "points_per_step": sum(point_count(d) for d in draws),
+                    "grids": sorted({f"{d['nx']}x{d['ny']}x{d['nz']}" for d in draws}),
+                    "mixed": res["mixed"], "fp64": res["fp64"],
+                    "mixed_speedup_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+                    "launch": "one CUDA graph per step, one branch per run"}
+
     # per-kernel device times (eager replay, events between launches)
     prof = d.profile_kernels(args.profile_steps)
     total_prof = sum(t for _, t in prof.values())
@@ -328,7 +351,7 @@ def run_ours(args) -> None:
                        "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "working set > 129 MB L2 (per-mode inverses 0.29 GB + fields 0.2 GB), no flush"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "step_roofline": step_roof,
-            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu, "mixed": mixed,
+            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu, "mixed": mixed, "ensemble": ensemble,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -350,6 +373,9 @@ def main():
     ap.add_argument("--no-mixed", dest="mixed", action="store_false",
                     help="skip the mixed-precision measurement")
     ap.add_argument("--mixed-err-steps", type=int, default=200)
+    ap.add_argument("--ensemble-runs", type=int, default=64)
+    ap.add_argument("--ensemble-steps", type=int, default=50)
+    ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu DRAM bytes per launch of the dominant kernel, if captured")
     args = ap.parse_args()

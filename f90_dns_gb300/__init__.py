@@ -9,6 +9,7 @@ PI bulk-velocity control) runs on one GPU behind the C-ABI declared in
 from .capi import (  # noqa: F401
     ChannelDNS,
     Dns3DError,
+    Ensemble,
     Diagnostics,
     config_from,
     default_config,

@@ -42,6 +42,8 @@ EXPORTED_SYMBOLS = (
     "dns3d_synchronize", "dns3d_diagnostics", "dns3d_footprint_bytes", "dns3d_strerror",
     "dns3d_last_error", "dns3d_step_timed", "dns3d_profile_kernels", "dns3d_launches_per_step",
     "dns3d_measure_fp64_tflops", "dns3d_flow_stats_noalloc",
+    "dns3d_ensemble_create", "dns3d_ensemble_destroy", "dns3d_ensemble_size", "dns3d_ensemble_run",
+    "dns3d_ensemble_step", "dns3d_ensemble_step_timed",
 )
 
 
@@ -138,6 +140,12 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_launches_per_step.argtypes = [hp, C.POINTER(C.c_int)]
     lib.dns3d_measure_fp64_tflops.argtypes = [ip, C.POINTER(C.c_double)]
     lib.dns3d_flow_stats_noalloc.argtypes = [vp, vp, vp, ip, ip, ip, vp, vp]
+    lib.dns3d_ensemble_create.argtypes = [C.POINTER(CConfig), ip, C.POINTER(hp)]
+    lib.dns3d_ensemble_destroy.argtypes = [hp]
+    lib.dns3d_ensemble_size.argtypes = [hp, C.POINTER(C.c_int)]
+    lib.dns3d_ensemble_run.argtypes = [hp, ip, C.POINTER(hp)]
+    lib.dns3d_ensemble_step.argtypes = [hp, ip]
+    lib.dns3d_ensemble_step_timed.argtypes = [hp, ip, C.POINTER(C.c_double)]
     lib.dns3d_last_error.argtypes = [hp]
     lib.dns3d_last_error.restype = C.c_char_p
     for n in EXPORTED_SYMBOLS:
@@ -232,20 +240,24 @@ class ChannelDNS:
     the reference's Fortran ``u(nx,ny,nz)``.
     """
 
-    def __init__(self, cfg: CConfig):
+    def __init__(self, cfg: CConfig, _handle=None):
         self.lib = load_library()
         self.cfg = cfg
-        self._h = C.c_void_p()
-        rc = self.lib.dns3d_create(C.byref(cfg), C.byref(self._h))
-        if rc:
-            raise Dns3DError(rc, "dns3d_create")
+        self._owned = _handle is None
+        if _handle is not None:
+            self._h = _handle
+        else:
+            self._h = C.c_void_p()
+            rc = self.lib.dns3d_create(C.byref(cfg), C.byref(self._h))
+            if rc:
+                raise Dns3DError(rc, "dns3d_create")
         self.shape = (cfg.nz, cfg.ny, cfg.nx)
 
     # -- lifetime -------------------------------------------------------------
     def close(self) -> None:
-        if self._h:
+        if self._h and self._owned:
             self.lib.dns3d_destroy(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __enter__(self):
         return self
@@ -363,3 +375,60 @@ class ChannelDNS:
         self._check(rc, "dns3d_diagnostics")
         return Diagnostics(d.umax, d.vmax, d.wmax, d.energy, d.u_bulk, d.dpdx, d.dpdx_avg,
                            d.max_div, d.time, d.step)
+
+
+class Ensemble:
+    """Independent runs of any grids advanced together: one CUDA graph with a
+    branch per run, launched once per step.  ``run(i)`` is a view of run i
+    (a :class:`ChannelDNS` that the ensemble owns)."""
+
+    def __init__(self, cfgs):
+        self.lib = load_library()
+        self.cfgs = list(cfgs)
+        arr = (CConfig * len(self.cfgs))(*self.cfgs)
+        self._e = C.c_void_p()
+        rc = self.lib.dns3d_ensemble_create(arr, len(self.cfgs), C.byref(self._e))
+        if rc:
+            raise Dns3DError(rc, "dns3d_ensemble_create")
+        self._views = []
+        for i, cfg in enumerate(self.cfgs):
+            h = C.c_void_p()
+            self._check(self.lib.dns3d_ensemble_run(self._e, i, C.byref(h)), "dns3d_ensemble_run")
+            self._views.append(ChannelDNS(cfg, _handle=h))
+
+    def _check(self, rc, where):
+        if rc:
+            msgs = []
+            for i, v in enumerate(getattr(self, "_views", [])):
+                m = self.lib.dns3d_last_error(v._h).decode() if v._h else ""
+                if m:
+                    msgs.append(f"run {i}: {m}")
+            raise Dns3DError(rc, where, "; ".join(msgs))
+
+    def __len__(self):
+        return len(self.cfgs)
+
+    def run(self, i: int) -> ChannelDNS:
+        return self._views[i]
+
+    def step(self, nsteps: int = 1) -> None:
+        self._check(self.lib.dns3d_ensemble_step(self._e, int(nsteps)), "dns3d_ensemble_step")
+
+    def step_timed(self, nsteps: int) -> float:
+        ms = C.c_double(0.0)
+        self._check(self.lib.dns3d_ensemble_step_timed(self._e, int(nsteps), C.byref(ms)),
+                    "dns3d_ensemble_step_timed")
+        return float(ms.value)
+
+    def close(self) -> None:
+        if self._e:
+            for v in self._views:
+                v._h = C.c_void_p()
+            self.lib.dns3d_ensemble_destroy(self._e)
+            self._e = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -883,6 +883,168 @@ int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out) {
     return DNS3D_OK;
 }
 
+}  // extern "C"
+
+// ------------------------------------------------------------------ ensembles
+struct dns3d_ensemble {
+    std::vector<dns3d_handle*> runs;
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+    cudaGraphExec_t graph = nullptr;
+    int device = 0;
+};
+
+namespace {
+
+void ensemble_release(dns3d_ensemble* e) {
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    for (auto* h : e->runs) dns3d_destroy(h);
+    for (auto ev : e->joins) cudaEventDestroy(ev);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->origin) cudaStreamDestroy(e->origin);
+}
+
+// One graph: origin -> fork -> (run i's loop body on run i's stream) -> join.
+int ensemble_capture(dns3d_ensemble* e) {
+    cudaGraph_t graph = nullptr;
+    dns3d_handle* h0 = e->runs[0];
+    CK(h0, cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeThreadLocal));
+    int rc = DNS3D_OK;
+    cudaError_t ce = cudaEventRecord(e->fork, e->origin);
+    for (size_t i = 0; i < e->runs.size() && !rc && ce == cudaSuccess; ++i) {
+        dns3d_handle* h = e->runs[i];
+        ce = cudaStreamWaitEvent(h->stream, e->fork, 0);
+        if (ce == cudaSuccess) rc = run_step_body(h);
+        if (!rc && ce == cudaSuccess) ce = cudaEventRecord(e->joins[i], h->stream);
+        if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(e->origin, e->joins[i], 0);
+    }
+    cudaError_t ee = cudaStreamEndCapture(e->origin, &graph);
+    if (rc || ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (rc) return rc;
+        return cuda_fail(h0, ce != cudaSuccess ? ce : ee, "ensemble capture");
+    }
+    cudaError_t ie = cudaGraphInstantiate(&e->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        e->graph = nullptr;
+        return cuda_fail(h0, ie, "cudaGraphInstantiate (ensemble)");
+    }
+    return DNS3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dns3d_ensemble_create(const dns3d_config* cfgs, int nruns, dns3d_ensemble** out) {
+    if (!cfgs || nruns < 1 || !out) return DNS3D_E_INVALID;
+    *out = nullptr;
+    for (int i = 0; i < nruns; ++i)
+        if (cfgs[i].device != cfgs[0].device) return DNS3D_E_INVALID;
+    dns3d_ensemble* e = new dns3d_ensemble();
+    e->device = cfgs[0].device;
+    for (int i = 0; i < nruns; ++i) {
+        dns3d_handle* h = nullptr;
+        const int rc = dns3d_create(&cfgs[i], &h);
+        if (rc) {
+            ensemble_release(e);
+            delete e;
+            return rc;
+        }
+        e->runs.push_back(h);
+    }
+    cudaSetDevice(e->device);
+    if (cudaStreamCreateWithFlags(&e->origin, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
+        ensemble_release(e);
+        delete e;
+        return DNS3D_E_CUDA;
+    }
+    e->joins.resize(nruns, nullptr);
+    for (int i = 0; i < nruns; ++i)
+        if (cudaEventCreateWithFlags(&e->joins[i], cudaEventDisableTiming) != cudaSuccess) {
+            ensemble_release(e);
+            delete e;
+            return DNS3D_E_CUDA;
+        }
+    *out = e;
+    return DNS3D_OK;
+}
+
+int dns3d_ensemble_destroy(dns3d_ensemble* e) {
+    if (!e) return DNS3D_E_INVALID;
+    cudaSetDevice(e->device);
+    if (e->origin) cudaStreamSynchronize(e->origin);
+    ensemble_release(e);
+    delete e;
+    return DNS3D_OK;
+}
+
+int dns3d_ensemble_size(dns3d_ensemble* e, int* nruns) {
+    if (!e || !nruns) return DNS3D_E_INVALID;
+    *nruns = (int)e->runs.size();
+    return DNS3D_OK;
+}
+
+int dns3d_ensemble_run(dns3d_ensemble* e, int i, dns3d_handle** h) {
+    if (!e || !h || i < 0 || i >= (int)e->runs.size()) return DNS3D_E_INVALID;
+    *h = e->runs[i];
+    return DNS3D_OK;
+}
+
+int dns3d_ensemble_step(dns3d_ensemble* e, int nsteps) {
+    if (!e || nsteps < 0) return DNS3D_E_INVALID;
+    dns3d_handle* h0 = e->runs[0];
+    CK(h0, cudaSetDevice(e->device));
+    if (nsteps == 0) return DNS3D_OK;
+    // the runs' own streams must be idle before the graph (which orders after
+    // the origin stream only) touches their state
+    for (auto* h : e->runs) CK(h, cudaStreamSynchronize(h->stream));
+    if (!e->graph) {
+        const int rc = ensemble_capture(e);
+        if (rc) return rc;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        CK(h0, cudaGraphLaunch(e->graph, e->origin));
+        for (auto* h : e->runs) {
+            h->step += 1;
+            h->time += h->cfg.dt;
+        }
+    }
+    CK(h0, cudaStreamSynchronize(e->origin));
+    return DNS3D_OK;
+}
+
+int dns3d_ensemble_step_timed(dns3d_ensemble* e, int nsteps, double* elapsed_ms) {
+    if (!e || !elapsed_ms || nsteps < 1) return DNS3D_E_INVALID;
+    dns3d_handle* h0 = e->runs[0];
+    if (!e->graph) {
+        const int rc = dns3d_ensemble_step(e, 1);
+        if (rc) return rc;
+    }
+    cudaEvent_t a, b;
+    CK(h0, cudaEventCreate(&a));
+    CK(h0, cudaEventCreate(&b));
+    CK(h0, cudaEventRecord(a, e->origin));
+    for (int s = 0; s < nsteps; ++s) {
+        CK(h0, cudaGraphLaunch(e->graph, e->origin));
+        for (auto* h : e->runs) {
+            h->step += 1;
+            h->time += h->cfg.dt;
+        }
+    }
+    CK(h0, cudaEventRecord(b, e->origin));
+    CK(h0, cudaEventSynchronize(b));
+    float ms = 0.f;
+    CK(h0, cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *elapsed_ms = ms;
+    return DNS3D_OK;
+}
+
 const char* dns3d_strerror(int code) {
     switch (code) {
         case DNS3D_OK: return "ok";

@@ -278,9 +278,19 @@ C* upload_table(int n, int count) {
     return d;
 }
 
+// Raised to the device's opt-in maximum: the limit belongs to the kernel
+// function and is shared by every handle (every grid) in the process.
 template <typename K>
 cudaError_t smem_attr(K k, int bytes) {
-    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev))) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, k))) return e;
+    const int limit = optin - (int)fa.sharedSizeBytes;  // static + dynamic <= opt-in maximum
+    if (bytes > limit) return cudaErrorInvalidValue;
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
 }
 
 }  // namespace

@@ -213,8 +213,15 @@ cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh, 
     const int nz = g.nz;
     const size_t sm = (size_t)nz * nz * sizeof(double) + nz * sizeof(double) + nz * sizeof(int);
     if (sm > 200 * 1024) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_build_inverses, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e) return e;
+    if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev))) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, k_build_inverses))) return e;
+    const int limit = optin - (int)fa.sharedSizeBytes;
+    if ((int)sm > limit) return cudaErrorInvalidValue;
+    if ((e = cudaFuncSetAttribute(k_build_inverses, cudaFuncAttributeMaxDynamicSharedMemorySize, limit))) return e;
     k_build_inverses<<<2 * nq + 1, 256, sm, s>>>(nz, S, wh, helm_f, ksq, nq, HinvF, PinvF, PpinT, info);
     return cudaGetLastError();
 }

@@ -1051,10 +1051,21 @@ int tile_cols(const GridDev& g, int narrays) {
     return tc;
 }
 
+// The dynamic shared-memory limit is a property of the kernel function, shared
+// by every handle in the process, so it is raised to the device's opt-in
+// maximum rather than to one grid's need (a smaller grid's handle would
+// otherwise lower it below what a larger grid's launches request).
 template <typename K>
 cudaError_t set_smem(K kern, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev))) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, kern))) return e;
+    const int limit = optin - (int)fa.sharedSizeBytes;  // static + dynamic <= opt-in maximum
+    if (bytes > (size_t)limit) return cudaErrorInvalidValue;
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
 }
 
 }  // namespace

@@ -184,6 +184,22 @@ int dns3d_measure_fp64_tflops(int device, double* tflops);
 int dns3d_flow_stats_noalloc(const double* u, const double* v, const double* w, int nx, int ny,
                              int nz, double* out4, void* stream);
 
+/* Ensembles: many independent runs (any mix of grids, parameters and
+ * precisions) advanced together.  No counterpart in the reference, which runs
+ * one channel per process.  Each run keeps its own handle and stream; the
+ * ensemble captures every run's loop body into one CUDA graph with one branch
+ * per run, so a single graph launch advances all runs by one step and their
+ * kernels overlap on the GPU.  Runs are numbered 0..nruns-1 in config order. */
+typedef struct dns3d_ensemble dns3d_ensemble;
+int dns3d_ensemble_create(const dns3d_config* cfgs, int nruns, dns3d_ensemble** out);
+int dns3d_ensemble_destroy(dns3d_ensemble* e);
+int dns3d_ensemble_size(dns3d_ensemble* e, int* nruns);
+/* The handle of run i (state transfer, diagnostics); owned by the ensemble. */
+int dns3d_ensemble_run(dns3d_ensemble* e, int i, dns3d_handle** h);
+int dns3d_ensemble_step(dns3d_ensemble* e, int nsteps);
+/* As dns3d_ensemble_step, bracketed by CUDA events; waits, returns device ms. */
+int dns3d_ensemble_step_timed(dns3d_ensemble* e, int nsteps, double* elapsed_ms);
+
 /* Device bytes held by a handle for a given config (admission control). */
 int dns3d_footprint_bytes(const dns3d_config* cfg, unsigned long long* bytes);
 
