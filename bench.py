@@ -205,6 +205,47 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def serving_leg(args, device: int) -> dict:
+    """Serving stream: Poisson arrivals (mean `serve_rate` runs/s, seeded) of
+    runs drawn as in the ensemble, 10% of them 256x256x97, each 200..2000
+    steps, mixed precision, admitted by device footprint under 160 GiB."""
+    import numpy as np
+    from f90_dns_gb300 import Server, config_from
+    from f90_dns_gb300.capi import PREC_MIXED
+    from f90_dns_gb300.workloads import WORKLOADS, ensemble_draws, point_count
+    rng = np.random.default_rng(args.seed + 1)
+    draws = ensemble_draws(args.serve_requests, seed=args.seed + 2)
+    big = WORKLOADS["channel_256x256x97_re180_dpdx"]
+    reqs = []
+    t = 0.0
+    for d in draws:
+        if rng.random() < 0.1:
+            d = dict(big, re=d["re"], target_pressure_gradient=2.0 / d["re"],
+                     perturbation_amplitude=d["perturbation_amplitude"],
+                     analytical_mode_x=d["analytical_mode_x"], analytical_mode_y=d["analytical_mode_y"])
+        t += float(rng.exponential(1.0 / args.serve_rate))
+        reqs.append((t, d, int(rng.integers(200, 2001))))
+    with Server(max_bytes=160 << 30, steps_per_round=args.serve_round, device=device) as srv:
+        t0 = time.perf_counter()
+        ids = []
+        for at, d, n in reqs:
+            dly = at - (time.perf_counter() - t0)
+            if dly > 0:
+                time.sleep(dly)
+            ids.append(srv.submit(config_from(d, device=device, precision=PREC_MIXED), n))
+        infos = [srv.wait(i, timeout=1800.0) for i in ids]
+    lat = np.array([i.latency for i in infos])
+    work = sum(point_count(d) * n for (_, d, n) in reqs)
+    span = max(i.t_finish for i in infos) - min(i.t_submit for i in infos)
+    return {"requests": len(reqs), "arrival_rate_per_s": args.serve_rate, "seed": args.seed + 1,
+            "large_256x256x97": sum(1 for (_, d, _) in reqs if d["nx"] == 256),
+            "completed": sum(1 for i in infos if i.status == 2),
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "aggregate_point_steps_per_s": work / span, "span_s": span,
+            "precision": "mixed", "admission": "device footprint <= 160 GiB, FIFO",
+            "steps_per_round": args.serve_round}
+
+
 def run_ours(args) -> None:
     ws, rank, local, dist = _dist()
     from f90_dns_gb300 import ChannelDNS, build, config_from
@@ -285,6 +326,11 @@ def run_ours(args) -> None:
                     "mixed_speedup_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"],
                     "launch": "one CUDA graph per step, one branch per run"}
 
+    # serving: Poisson arrivals of seed-drawn runs, continuous batching
+    serving = None
+    if args.serve_requests > 0 and rank == 0:
+        serving = serving_leg(args, local)
+
     # per-kernel device times (eager replay, events between launches)
     prof = d.profile_kernels(args.profile_steps)
     total_prof = sum(t for _, t in prof.values())
@@ -351,7 +397,7 @@ def run_ours(args) -> None:
                        "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "working set > 129 MB L2 (per-mode inverses 0.29 GB + fields 0.2 GB), no flush"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "step_roofline": step_roof,
-            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu, "mixed": mixed, "ensemble": ensemble,
+            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu, "mixed": mixed, "ensemble": ensemble, "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -376,6 +422,9 @@ def main():
     ap.add_argument("--ensemble-runs", type=int, default=64)
     ap.add_argument("--ensemble-steps", type=int, default=50)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=4.0)
+    ap.add_argument("--serve-round", type=int, default=20)
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu DRAM bytes per launch of the dominant kernel, if captured")
     args = ap.parse_args()

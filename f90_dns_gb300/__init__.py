@@ -10,6 +10,7 @@ from .capi import (  # noqa: F401
     ChannelDNS,
     Dns3DError,
     Ensemble,
+    Server,
     Diagnostics,
     config_from,
     default_config,

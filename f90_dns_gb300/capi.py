@@ -30,6 +30,9 @@ DNS3D_E_CUDA = 5
 DNS3D_E_UNSUPPORTED = 6
 DNS3D_E_IO = 7
 DNS3D_E_NODEVICE = 8
+DNS3D_E_TIMEOUT = 9
+DNS3D_E_CANCELLED = 10
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 PREC_FP64 = 0
 PREC_MIXED = 1
 
@@ -44,6 +47,9 @@ EXPORTED_SYMBOLS = (
     "dns3d_measure_fp64_tflops", "dns3d_flow_stats_noalloc",
     "dns3d_ensemble_create", "dns3d_ensemble_destroy", "dns3d_ensemble_size", "dns3d_ensemble_run",
     "dns3d_ensemble_step", "dns3d_ensemble_step_timed",
+    "dns3d_server_opts_defaults", "dns3d_server_create", "dns3d_server_submit", "dns3d_server_poll",
+    "dns3d_server_wait", "dns3d_server_result_state", "dns3d_server_release", "dns3d_server_get_stats",
+    "dns3d_server_destroy",
 )
 
 
@@ -92,6 +98,22 @@ class CDiag(C.Structure):
 
 class CKernelTime(C.Structure):
     _fields_ = [("name", C.c_char_p), ("launches", C.c_int), ("pad_", C.c_int), ("total_ms", C.c_double)]
+
+
+class CServerOpts(C.Structure):
+    _fields_ = [("max_bytes", C.c_ulonglong), ("max_runs", C.c_int), ("steps_per_round", C.c_int),
+                ("device", C.c_int), ("pad_", C.c_int)]
+
+
+class CRequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("error", C.c_int), ("steps_done", C.c_int), ("nsteps", C.c_int),
+                ("bytes", C.c_ulonglong), ("t_submit", C.c_double), ("t_start", C.c_double),
+                ("t_finish", C.c_double), ("diag", CDiag)]
+
+
+class CServerStats(C.Structure):
+    _fields_ = [("queued", C.c_int), ("running", C.c_int), ("bytes_in_use", C.c_ulonglong),
+                ("point_steps_done", C.c_ulonglong), ("uptime_s", C.c_double)]
 
 
 class Dns3DError(RuntimeError):
@@ -146,6 +168,15 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_ensemble_run.argtypes = [hp, ip, C.POINTER(hp)]
     lib.dns3d_ensemble_step.argtypes = [hp, ip]
     lib.dns3d_ensemble_step_timed.argtypes = [hp, ip, C.POINTER(C.c_double)]
+    lib.dns3d_server_opts_defaults.argtypes = [C.POINTER(CServerOpts)]
+    lib.dns3d_server_create.argtypes = [C.POINTER(CServerOpts), C.POINTER(hp)]
+    lib.dns3d_server_submit.argtypes = [hp, C.POINTER(CConfig), ip, ip, C.POINTER(C.c_longlong)]
+    lib.dns3d_server_poll.argtypes = [hp, C.c_longlong, C.POINTER(CRequestInfo)]
+    lib.dns3d_server_wait.argtypes = [hp, C.c_longlong, C.c_double, C.POINTER(CRequestInfo)]
+    lib.dns3d_server_result_state.argtypes = [hp, C.c_longlong, vp, vp, vp, vp]
+    lib.dns3d_server_release.argtypes = [hp, C.c_longlong]
+    lib.dns3d_server_get_stats.argtypes = [hp, C.POINTER(CServerStats)]
+    lib.dns3d_server_destroy.argtypes = [hp]
     lib.dns3d_last_error.argtypes = [hp]
     lib.dns3d_last_error.restype = C.c_char_p
     for n in EXPORTED_SYMBOLS:
@@ -426,6 +457,105 @@ class Ensemble:
                 v._h = C.c_void_p()
             self.lib.dns3d_ensemble_destroy(self._e)
             self._e = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+@dataclass
+class RequestInfo:
+    status: int
+    error: int
+    steps_done: int
+    nsteps: int
+    bytes: int
+    t_submit: float
+    t_start: float
+    t_finish: float
+    diag: Diagnostics
+
+    @property
+    def latency(self) -> float:
+        return self.t_finish - self.t_submit
+
+
+def _info(ci: CRequestInfo) -> RequestInfo:
+    d = ci.diag
+    return RequestInfo(ci.status, ci.error, ci.steps_done, ci.nsteps, int(ci.bytes), ci.t_submit, ci.t_start,
+                       ci.t_finish, Diagnostics(d.umax, d.vmax, d.wmax, d.energy, d.u_bulk, d.dpdx, d.dpdx_avg,
+                                                d.max_div, d.time, d.step))
+
+
+class Server:
+    """Continuous-batching request loop over one GPU (see dns3d_server_* in
+    include/dns3d_capi.h): submit runs, wait or poll, read final state."""
+
+    def __init__(self, max_bytes: int | None = None, max_runs: int | None = None,
+                 steps_per_round: int | None = None, device: int = 0):
+        self.lib = load_library()
+        o = CServerOpts()
+        self.lib.dns3d_server_opts_defaults(C.byref(o))
+        if max_bytes is not None:
+            o.max_bytes = int(max_bytes)
+        if max_runs is not None:
+            o.max_runs = int(max_runs)
+        if steps_per_round is not None:
+            o.steps_per_round = int(steps_per_round)
+        o.device = device
+        self.opts = o
+        self._s = C.c_void_p()
+        rc = self.lib.dns3d_server_create(C.byref(o), C.byref(self._s))
+        if rc:
+            raise Dns3DError(rc, "dns3d_server_create")
+        self._shapes = {}
+
+    def submit(self, cfg: CConfig, nsteps: int, keep_state: bool = False) -> int:
+        rid = C.c_longlong(0)
+        rc = self.lib.dns3d_server_submit(self._s, C.byref(cfg), int(nsteps), int(keep_state), C.byref(rid))
+        if rc:
+            raise Dns3DError(rc, "dns3d_server_submit")
+        self._shapes[rid.value] = (cfg.nz, cfg.ny, cfg.nx)
+        return int(rid.value)
+
+    def poll(self, rid: int) -> RequestInfo:
+        ci = CRequestInfo()
+        rc = self.lib.dns3d_server_poll(self._s, rid, C.byref(ci))
+        if rc:
+            raise Dns3DError(rc, "dns3d_server_poll")
+        return _info(ci)
+
+    def wait(self, rid: int, timeout: float = -1.0) -> RequestInfo:
+        ci = CRequestInfo()
+        rc = self.lib.dns3d_server_wait(self._s, rid, float(timeout), C.byref(ci))
+        if rc:
+            raise Dns3DError(rc, "dns3d_server_wait")
+        return _info(ci)
+
+    def result_state(self, rid: int) -> dict:
+        shp = self._shapes[rid]
+        out = {k: np.empty(shp) for k in ("u", "v", "w", "p_total")}
+        rc = self.lib.dns3d_server_result_state(self._s, rid, *[_ptr(out[k]) for k in ("u", "v", "w", "p_total")])
+        if rc:
+            raise Dns3DError(rc, "dns3d_server_result_state")
+        return out
+
+    def release(self, rid: int) -> None:
+        rc = self.lib.dns3d_server_release(self._s, rid)
+        if rc:
+            raise Dns3DError(rc, "dns3d_server_release")
+
+    def stats(self) -> dict:
+        st = CServerStats()
+        self.lib.dns3d_server_get_stats(self._s, C.byref(st))
+        return {n: getattr(st, n) for n, _ in CServerStats._fields_}
+
+    def close(self) -> None:
+        if self._s:
+            self.lib.dns3d_server_destroy(self._s)
+            self._s = C.c_void_p()
 
     def __enter__(self):
         return self

@@ -1056,6 +1056,8 @@ const char* dns3d_strerror(int code) {
         case DNS3D_E_UNSUPPORTED: return "unsupported grid size or option";
         case DNS3D_E_IO: return "input file could not be read or parsed";
         case DNS3D_E_NODEVICE: return "no CUDA device";
+        case DNS3D_E_TIMEOUT: return "timed out";
+        case DNS3D_E_CANCELLED: return "request cancelled";
         default: return "unknown error";
     }
 }

@@ -1,0 +1,296 @@
+// Request-serving loop over the C-ABI: continuous batching of independent
+// channel runs on one GPU.  No counterpart in the reference (one run per
+// process, DNS_pressure_BC_3D.f90:184-428).
+//
+// A worker thread owns all GPU work.  Requests wait in FIFO order until their
+// device footprint (dns3d_footprint_bytes) fits under the byte budget and a
+// slot is free; admitted runs each keep their own handle and stream and are
+// advanced `steps_per_round` steps per round, all runs' graph launches queued
+// before any wait, so their kernels overlap on the device.  A finished run's
+// diagnostics (and, on request, its final u, v, w, p_total) are kept, its
+// handle is destroyed at once so its memory admits the next request.
+//
+// Built only on the public entry points of include/dns3d_capi.h.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "dns3d_capi.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    long long id = 0;
+    dns3d_config cfg{};
+    int nsteps = 0;
+    int keep_state = 0;
+    int status = DNS3D_REQ_QUEUED;
+    int error = DNS3D_OK;
+    int steps_done = 0;
+    unsigned long long bytes = 0;
+    Clock::time_point t_submit, t_start, t_finish;
+    dns3d_handle* h = nullptr;
+    dns3d_diag diag{};
+    std::vector<double> state;  // u, v, w, p_total when keep_state
+};
+
+double seconds(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double>(b - a).count();
+}
+
+}  // namespace
+
+struct dns3d_server {
+    dns3d_server_opts opts{};
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<Request>> queue;
+    std::vector<std::shared_ptr<Request>> active;
+    std::map<long long, std::shared_ptr<Request>> all;
+    long long next_id = 1;
+    bool stop = false;
+    unsigned long long bytes_in_use = 0;
+    unsigned long long point_steps = 0;
+    Clock::time_point t0;
+    std::thread worker;
+
+    void loop();
+    void admit_locked(std::vector<std::shared_ptr<Request>>& to_create);
+};
+
+void dns3d_server::admit_locked(std::vector<std::shared_ptr<Request>>& to_create) {
+    while (!queue.empty() && (int)(active.size() + to_create.size()) < opts.max_runs) {
+        auto r = queue.front();
+        if (bytes_in_use + r->bytes > opts.max_bytes) break;  // FIFO: the head waits for memory
+        queue.pop_front();
+        bytes_in_use += r->bytes;
+        to_create.push_back(r);
+    }
+}
+
+void dns3d_server::loop() {
+    for (;;) {
+        std::vector<std::shared_ptr<Request>> to_create;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_work.wait(lk, [&] { return stop || !active.empty() || !queue.empty(); });
+            if (stop && active.empty() && queue.empty()) return;
+            if (stop) {  // cancel everything: queued and running requests end as failed
+                for (auto& r : queue) {
+                    r->status = DNS3D_REQ_FAILED;
+                    r->error = DNS3D_E_CANCELLED;
+                }
+                queue.clear();
+                for (auto& r : active) {
+                    dns3d_destroy(r->h);
+                    r->h = nullptr;
+                    r->status = DNS3D_REQ_FAILED;
+                    r->error = DNS3D_E_CANCELLED;
+                    r->t_finish = Clock::now();
+                    bytes_in_use -= r->bytes;
+                }
+                active.clear();
+                cv_done.notify_all();
+                return;
+            }
+            admit_locked(to_create);
+        }
+        for (auto& r : to_create) {  // handle creation outside the lock
+            dns3d_config c = r->cfg;
+            c.device = opts.device;
+            const int rc = dns3d_create(&c, &r->h);
+            std::lock_guard<std::mutex> lk(mu);
+            if (rc) {
+                r->status = DNS3D_REQ_FAILED;
+                r->error = rc;
+                r->t_finish = Clock::now();
+                bytes_in_use -= r->bytes;
+                cv_done.notify_all();
+            } else {
+                r->status = DNS3D_REQ_RUNNING;
+                r->t_start = Clock::now();
+                active.push_back(r);
+            }
+        }
+        if (active.empty()) continue;
+        // one round: queue every run's steps, then wait for all
+        std::vector<int> adv(active.size(), 0);
+        for (size_t i = 0; i < active.size(); ++i) {
+            auto& r = active[i];
+            const int k = std::min(opts.steps_per_round, r->nsteps - r->steps_done);
+            if (k > 0 && dns3d_step(r->h, k) == DNS3D_OK) adv[i] = k;
+            else if (k > 0) r->error = DNS3D_E_CUDA;
+        }
+        for (size_t i = 0; i < active.size(); ++i) {
+            auto& r = active[i];
+            if (dns3d_synchronize(r->h) != DNS3D_OK && !r->error) r->error = DNS3D_E_CUDA;
+            r->steps_done += adv[i];
+        }
+        std::vector<std::shared_ptr<Request>> done;
+        for (auto& r : active)
+            if (r->error || r->steps_done >= r->nsteps) done.push_back(r);
+        for (auto& r : done) {
+            if (!r->error) {
+                const int rc = dns3d_diagnostics(r->h, &r->diag);
+                if (rc && rc != DNS3D_E_NONFINITE) r->error = rc;
+                if (!r->error && r->keep_state) {
+                    const size_t n = (size_t)r->cfg.nx * r->cfg.ny * r->cfg.nz;
+                    r->state.resize(4 * n);
+                    const int rs = dns3d_get_state(r->h, r->state.data(), r->state.data() + n, r->state.data() + 2 * n,
+                                                   r->state.data() + 3 * n, nullptr, nullptr, nullptr, nullptr, nullptr);
+                    if (rs) r->error = rs;
+                }
+            }
+            dns3d_destroy(r->h);
+            r->h = nullptr;
+            std::lock_guard<std::mutex> lk(mu);
+            r->t_finish = Clock::now();
+            r->status = r->error ? DNS3D_REQ_FAILED : DNS3D_REQ_DONE;
+            bytes_in_use -= r->bytes;
+            point_steps += (unsigned long long)r->steps_done * r->cfg.nx * r->cfg.ny * r->cfg.nz;
+            active.erase(std::find(active.begin(), active.end(), r));
+            cv_done.notify_all();
+        }
+    }
+}
+
+namespace {
+
+void fill_info(const Request& r, const Clock::time_point t0, dns3d_request_info* info) {
+    std::memset(info, 0, sizeof(*info));
+    info->status = r.status;
+    info->error = r.error;
+    info->steps_done = r.steps_done;
+    info->nsteps = r.nsteps;
+    info->bytes = r.bytes;
+    info->t_submit = seconds(t0, r.t_submit);
+    info->t_start = r.status >= DNS3D_REQ_RUNNING || r.t_start != Clock::time_point() ? seconds(t0, r.t_start) : -1.0;
+    info->t_finish = (r.status == DNS3D_REQ_DONE || r.status == DNS3D_REQ_FAILED) ? seconds(t0, r.t_finish) : -1.0;
+    info->diag = r.diag;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dns3d_server_opts_defaults(dns3d_server_opts* o) {
+    if (!o) return DNS3D_E_INVALID;
+    std::memset(o, 0, sizeof(*o));
+    o->max_bytes = 160ull << 30;
+    o->max_runs = 256;
+    o->steps_per_round = 10;
+    o->device = 0;
+    return DNS3D_OK;
+}
+
+int dns3d_server_create(const dns3d_server_opts* opts, dns3d_server** out) {
+    if (!opts || !out || opts->max_runs < 1 || opts->steps_per_round < 1 || opts->max_bytes == 0)
+        return DNS3D_E_INVALID;
+    auto* s = new dns3d_server();
+    s->opts = *opts;
+    s->t0 = Clock::now();
+    s->worker = std::thread([s] { s->loop(); });
+    *out = s;
+    return DNS3D_OK;
+}
+
+int dns3d_server_submit(dns3d_server* s, const dns3d_config* cfg, int nsteps, int keep_state, long long* id) {
+    if (!s || !cfg || nsteps < 1 || !id) return DNS3D_E_INVALID;
+    auto r = std::make_shared<Request>();
+    r->cfg = *cfg;
+    r->nsteps = nsteps;
+    r->keep_state = keep_state;
+    const int rc = dns3d_footprint_bytes(cfg, &r->bytes);
+    if (rc) return rc;
+    if (r->bytes > s->opts.max_bytes) return DNS3D_E_OOM;  // could never be admitted
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return DNS3D_E_INVALID;
+    r->id = s->next_id++;
+    r->t_submit = Clock::now();
+    s->queue.push_back(r);
+    s->all[r->id] = r;
+    *id = r->id;
+    s->cv_work.notify_one();
+    return DNS3D_OK;
+}
+
+int dns3d_server_poll(dns3d_server* s, long long id, dns3d_request_info* info) {
+    if (!s || !info) return DNS3D_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return DNS3D_E_INVALID;
+    fill_info(*it->second, s->t0, info);
+    return DNS3D_OK;
+}
+
+int dns3d_server_wait(dns3d_server* s, long long id, double timeout_s, dns3d_request_info* info) {
+    if (!s || !info) return DNS3D_E_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return DNS3D_E_INVALID;
+    auto r = it->second;
+    const auto pred = [&] { return r->status == DNS3D_REQ_DONE || r->status == DNS3D_REQ_FAILED; };
+    if (timeout_s < 0) s->cv_done.wait(lk, pred);
+    else s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred);
+    fill_info(*r, s->t0, info);
+    return pred() ? DNS3D_OK : DNS3D_E_TIMEOUT;
+}
+
+int dns3d_server_result_state(dns3d_server* s, long long id, double* u, double* v, double* w, double* p_total) {
+    if (!s) return DNS3D_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return DNS3D_E_INVALID;
+    const Request& r = *it->second;
+    if (r.status != DNS3D_REQ_DONE || r.state.empty()) return DNS3D_E_INVALID;
+    const size_t n = (size_t)r.cfg.nx * r.cfg.ny * r.cfg.nz;
+    double* dst[4] = {u, v, w, p_total};
+    for (int f = 0; f < 4; ++f)
+        if (dst[f]) std::memcpy(dst[f], r.state.data() + f * n, n * sizeof(double));
+    return DNS3D_OK;
+}
+
+int dns3d_server_release(dns3d_server* s, long long id) {
+    if (!s) return DNS3D_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return DNS3D_E_INVALID;
+    if (it->second->status != DNS3D_REQ_DONE && it->second->status != DNS3D_REQ_FAILED) return DNS3D_E_INVALID;
+    s->all.erase(it);
+    return DNS3D_OK;
+}
+
+int dns3d_server_get_stats(dns3d_server* s, dns3d_server_stats* st) {
+    if (!s || !st) return DNS3D_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::memset(st, 0, sizeof(*st));
+    st->queued = (int)s->queue.size();
+    st->running = (int)s->active.size();
+    st->bytes_in_use = s->bytes_in_use;
+    st->point_steps_done = s->point_steps;
+    st->uptime_s = seconds(s->t0, Clock::now());
+    return DNS3D_OK;
+}
+
+int dns3d_server_destroy(dns3d_server* s) {
+    if (!s) return DNS3D_E_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    delete s;
+    return DNS3D_OK;
+}
+
+}  // extern "C"

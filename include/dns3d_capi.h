@@ -33,6 +33,8 @@ extern "C" {
 #define DNS3D_E_UNSUPPORTED 6  /* grid size or option not supported          */
 #define DNS3D_E_IO 7           /* input file could not be read / parsed      */
 #define DNS3D_E_NODEVICE 8     /* no CUDA device                              */
+#define DNS3D_E_TIMEOUT 9      /* a wait ran out of time                      */
+#define DNS3D_E_CANCELLED 10   /* a served request was cancelled              */
 
 #define DNS3D_PREC_FP64 0      /* plain FP64 path                            */
 #define DNS3D_PREC_MIXED 1     /* FP32 nonlinear term and viscous increment;
@@ -199,6 +201,56 @@ int dns3d_ensemble_run(dns3d_ensemble* e, int i, dns3d_handle** h);
 int dns3d_ensemble_step(dns3d_ensemble* e, int nsteps);
 /* As dns3d_ensemble_step, bracketed by CUDA events; waits, returns device ms. */
 int dns3d_ensemble_step_timed(dns3d_ensemble* e, int nsteps, double* elapsed_ms);
+
+/* Serving: continuous batching of requested runs on one GPU.  No counterpart
+ * in the reference.  A worker thread owned by the server admits requests in
+ * FIFO order while their device footprint fits under max_bytes and fewer than
+ * max_runs are running, advances all running requests steps_per_round steps
+ * per round on their own streams (their kernels overlap), and frees a run's
+ * device memory as soon as it completes.  Times are seconds since server
+ * creation.  dns3d_server_destroy cancels queued and running requests. */
+#define DNS3D_REQ_QUEUED 0
+#define DNS3D_REQ_RUNNING 1
+#define DNS3D_REQ_DONE 2
+#define DNS3D_REQ_FAILED 3
+typedef struct dns3d_server dns3d_server;
+typedef struct dns3d_server_opts {
+    unsigned long long max_bytes;  /* device memory budget (default 160 GiB) */
+    int max_runs;                  /* concurrent runs (default 256)           */
+    int steps_per_round;           /* steps per run between waits (default 10)*/
+    int device;
+    int pad_;
+} dns3d_server_opts;
+typedef struct dns3d_request_info {
+    int status;                    /* DNS3D_REQ_*                             */
+    int error;                     /* DNS3D_OK or the failing status          */
+    int steps_done, nsteps;
+    unsigned long long bytes;      /* admitted footprint                      */
+    double t_submit, t_start, t_finish;  /* -1 if not reached                 */
+    dns3d_diag diag;               /* final diagnostics (when done)           */
+} dns3d_request_info;
+typedef struct dns3d_server_stats {
+    int queued, running;
+    unsigned long long bytes_in_use;
+    unsigned long long point_steps_done;  /* of completed requests           */
+    double uptime_s;
+} dns3d_server_stats;
+int dns3d_server_opts_defaults(dns3d_server_opts* opts);
+int dns3d_server_create(const dns3d_server_opts* opts, dns3d_server** out);
+/* Queue a run of `nsteps` steps of cfg (from its initial condition); with
+ * keep_state the final u, v, w, p_total are kept for
+ * dns3d_server_result_state until dns3d_server_release. */
+int dns3d_server_submit(dns3d_server* s, const dns3d_config* cfg, int nsteps, int keep_state,
+                        long long* request_id);
+int dns3d_server_poll(dns3d_server* s, long long request_id, dns3d_request_info* info);
+/* Wait until the request is done or failed (timeout_s < 0: no limit);
+ * DNS3D_E_TIMEOUT if the time ran out. */
+int dns3d_server_wait(dns3d_server* s, long long request_id, double timeout_s, dns3d_request_info* info);
+int dns3d_server_result_state(dns3d_server* s, long long request_id, double* u, double* v, double* w,
+                              double* p_total);
+int dns3d_server_release(dns3d_server* s, long long request_id);
+int dns3d_server_get_stats(dns3d_server* s, dns3d_server_stats* stats);
+int dns3d_server_destroy(dns3d_server* s);
 
 /* Device bytes held by a handle for a given config (admission control). */
 int dns3d_footprint_bytes(const dns3d_config* cfg, unsigned long long* bytes);

@@ -41,6 +41,9 @@ def test_library_contains_sm103a_code(built_lib):
 
 
 STRUCTS = {
+    "dns3d_server_opts": capi.CServerOpts,
+    "dns3d_request_info": capi.CRequestInfo,
+    "dns3d_server_stats": capi.CServerStats,
     "dns3d_config": capi.CConfig,
     "dns3d_pi_state": capi.CPIState,
     "dns3d_diag": capi.CDiag,
@@ -170,3 +173,29 @@ def test_null_handle_is_rejected(built_lib):
               "dns3d_pressure_correction", "dns3d_apply_boundary_conditions", "dns3d_destroy"):
         assert getattr(built_lib, n)(None) == capi.DNS3D_E_INVALID
     assert built_lib.dns3d_step(None, 1) == capi.DNS3D_E_INVALID
+
+
+@pytest.mark.skipif(_has_gpu(), reason="a GPU is present")
+def test_server_host_logic_without_gpu(built_lib):
+    """Queueing, failure reporting, waits and shutdown of the serving loop work
+    on a host without a GPU: every request fails with DNS3D_E_NODEVICE."""
+    cfg = capi.default_config(nx=32, ny=32, nz=17)
+    with capi.Server(max_runs=2) as srv:
+        ids = [srv.submit(cfg, 5) for _ in range(4)]
+        infos = [srv.wait(i, timeout=30.0) for i in ids]
+        for inf in infos:
+            assert inf.status == capi.REQ_FAILED and inf.error == capi.DNS3D_E_NODEVICE
+            assert inf.t_finish >= inf.t_submit >= 0.0
+        st = srv.stats()
+        assert st["queued"] == 0 and st["running"] == 0 and st["bytes_in_use"] == 0
+        srv.release(ids[0])
+        with pytest.raises(capi.Dns3DError):
+            srv.poll(ids[0])
+
+
+def test_server_rejects_request_larger_than_budget(built_lib):
+    cfg = capi.default_config(nx=128, ny=128, nz=65, lgl_dmatrix_guard=0)
+    with capi.Server(max_bytes=1 << 20) as srv:
+        with pytest.raises(capi.Dns3DError) as ei:
+            srv.submit(cfg, 10)
+        assert ei.value.code == capi.DNS3D_E_OOM
