@@ -87,71 +87,100 @@ __device__ bool gj_invert(double* a, int n, int* perm, double* colk, int* flag) 
     return true;
 }
 
-__global__ void __launch_bounds__(256) k_build_inverses(int nz, const double* __restrict__ S,
-                                                        const double* __restrict__ wh, double helm_f,
-                                                        const double* __restrict__ ksq, int nq,
-                                                        double* __restrict__ HinvF,
-                                                        double* __restrict__ PinvF,
-                                                        double* __restrict__ PpinT, int* info) {
+// Element (i, j) of the full operator of job (helm | poisson, q).
+__device__ __forceinline__ double op_elem(bool helm, int i, int j, int nz, const double* __restrict__ S,
+                                          const double* __restrict__ wh, double helm_f, double k2) {
+    if (helm) {
+        if (i == 0 || i == nz - 1) return (i == j) ? 1.0 : 0.0;
+        double v = helm_f * S[i * nz + j];
+        if (i == j) v += (1.0 + helm_f * k2) * wh[i];
+        return v;
+    }
+    double v = -S[i * nz + j];
+    if (i == j) v -= k2 * wh[i];
+    return v;
+}
+
+// Regular modes: the operators are centro-symmetric, so in the parity-folded
+// basis they are block diagonal.  With Ae, Ao the folded blocks of A (the
+// fold of step.cu) the folded blocks of A^{-1} are
+//   Ge = Dm^{-1} Ae^{-1} Dm^{-1},  Dm = diag(2, ..., 2, 1 [middle, odd nz]),
+//   Go = Ao^{-1} / 4,
+// so each job inverts two ~nz/2 blocks instead of one nz x nz matrix.
+__global__ void __launch_bounds__(256) k_build_inverses_folded(int nz, const double* __restrict__ S,
+                                                               const double* __restrict__ wh, double helm_f,
+                                                               const double* __restrict__ ksq, int nq,
+                                                               double* __restrict__ HinvF,
+                                                               double* __restrict__ PinvF, int* info) {
+    extern __shared__ double sm[];
+    const int h = nz / 2, he = nz - h, ho = h;
+    double* ae = sm;                       // [he][he]
+    double* ao = sm + he * he;             // [ho][ho]
+    double* colk = ao + ho * ho;           // [he]
+    int* perm = reinterpret_cast<int*>(colk + he);
+    __shared__ int flag;
+    const int job = blockIdx.x;  // [0, nq): Helmholtz q;  [nq, 2nq): Poisson q - nq
+    const bool helm = job < nq;
+    const int q = helm ? job : job - nq;
+    const size_t qstride = (size_t)he * he + (size_t)ho * ho;
+    double* out = (helm ? HinvF : PinvF) + (size_t)q * qstride;
+    if (!helm && q == 0) {  // k^2 = 0 unpinned Poisson operator is singular and never used
+        for (int t = threadIdx.x; t < (int)qstride; t += blockDim.x) out[t] = 0.0;
+        return;
+    }
+    const double k2 = ksq[q];
+    for (int t = threadIdx.x; t < he * he; t += blockDim.x) {
+        const int i = t / he, j = t - i * he;
+        double v;
+        if (i < h && j < h) v = 0.5 * (op_elem(helm, i, j, nz, S, wh, helm_f, k2) +
+                                       op_elem(helm, i, nz - 1 - j, nz, S, wh, helm_f, k2));
+        else v = op_elem(helm, i, j, nz, S, wh, helm_f, k2);  // middle row / column (odd nz)
+        ae[t] = v;
+    }
+    for (int t = threadIdx.x; t < ho * ho; t += blockDim.x) {
+        const int i = t / ho, j = t - i * ho;
+        ao[t] = 0.5 * (op_elem(helm, i, j, nz, S, wh, helm_f, k2) - op_elem(helm, i, nz - 1 - j, nz, S, wh, helm_f, k2));
+    }
+    __syncthreads();
+    bool ok = gj_invert(ae, he, perm, colk, &flag);
+    if (ok && ho > 0) ok = gj_invert(ao, ho, perm, colk, &flag);
+    if (!ok) {
+        if (threadIdx.x == 0) atomicCAS(info, 0, job + 1);
+        return;
+    }
+    // GeT[j][k] = Ge[k][j] = ae^{-1}[k][j] / (dm_k dm_j);  GoT[j][k] = ao^{-1}[k][j] / 4
+    for (int t = threadIdx.x; t < he * he; t += blockDim.x) {
+        const int j = t / he, k = t - j * he;
+        const double dk = (k < h) ? 2.0 : 1.0, dj = (j < h) ? 2.0 : 1.0;
+        out[t] = ae[k * he + j] / (dk * dj);
+    }
+    for (int t = threadIdx.x; t < ho * ho; t += blockDim.x) {
+        const int j = t / ho, k = t - j * ho;
+        out[(size_t)he * he + t] = 0.25 * ao[k * ho + j];
+    }
+}
+
+// The pinned (0,0) Poisson operator (row and column 1 zeroed, P(1,1) = 1) is
+// not centro-symmetric: inverted at full size, stored unfolded and transposed.
+__global__ void __launch_bounds__(256) k_build_pinned(int nz, const double* __restrict__ S,
+                                                      double* __restrict__ PpinT, int* info) {
     extern __shared__ double sm[];
     double* a = sm;
     double* colk = sm + nz * nz;
     int* perm = reinterpret_cast<int*>(colk + nz);
     __shared__ int flag;
-    const int job = blockIdx.x;  // [0, nq): Helmholtz q;  [nq, 2nq+1): Poisson q - nq
-    const bool helm = job < nq;
-    const int q = helm ? job : job - nq;
-    const int h = nz / 2, he = nz - h, ho = h;
-    const size_t qstride = (size_t)he * he + (size_t)ho * ho;
-    const bool pinned = !helm && q == nq;
-    double* out = pinned ? PpinT : (helm ? HinvF : PinvF) + (size_t)q * qstride;
-    if (!helm && q == 0) {  // k^2 = 0 unpinned Poisson operator is singular and never used
-        for (int t = threadIdx.x; t < (int)qstride; t += blockDim.x) out[t] = 0.0;
+    for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) {
+        const int i = t / nz, j = t - i * nz;
+        a[t] = (i == 0 || j == 0) ? ((i == 0 && j == 0) ? 1.0 : 0.0) : -S[t];
+    }
+    __syncthreads();
+    if (!gj_invert(a, nz, perm, colk, &flag)) {
+        if (threadIdx.x == 0) atomicCAS(info, 0, 1);
         return;
     }
     for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) {
-        const int i = t / nz, j = t - i * nz;
-        double v;
-        if (helm) {
-            const double k2 = ksq[q];
-            v = helm_f * S[t];
-            if (i == j) v += (1.0 + helm_f * k2) * wh[i];
-            if (i == 0 || i == nz - 1) v = (i == j) ? 1.0 : 0.0;
-        } else if (q < nq) {
-            v = -S[t];
-            if (i == j) v -= ksq[q] * wh[i];
-        } else {
-            v = -S[t];
-            if (i == 0 || j == 0) v = (i == 0 && j == 0) ? 1.0 : 0.0;
-        }
-        a[t] = v;
-    }
-    __syncthreads();
-    const bool ok = gj_invert(a, nz, perm, colk, &flag);
-    if (!ok) {
-        if (threadIdx.x == 0) atomicCAS(info, 0, job + 1);
-        return;
-    }
-    if (pinned) {
-        for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) {
-            const int zp = t / nz, z = t - zp * nz;
-            out[t] = a[z * nz + zp];
-        }
-        return;
-    }
-    // Ge[k][j] (k, j < he) and Go[k][j] (k, j < ho), stored as GeT[j][k], GoT[j][k]
-    for (int t = threadIdx.x; t < he * he; t += blockDim.x) {
-        const int j = t / he, k = t - j * he;
-        double v;
-        if (k < h && j < h) v = 0.5 * (a[k * nz + j] + a[k * nz + nz - 1 - j]);
-        else if (k < h) v = a[k * nz + h];       // j = middle
-        else if (j < h) v = a[h * nz + j];       // k = middle
-        else v = a[h * nz + h];
-        out[t] = v;
-    }
-    for (int t = threadIdx.x; t < ho * ho; t += blockDim.x) {
-        const int j = t / ho, k = t - j * ho;
-        out[(size_t)he * he + t] = 0.5 * (a[k * nz + j] - a[k * nz + nz - 1 - j]);
+        const int zp = t / nz, z = t - zp * nz;
+        PpinT[t] = a[z * nz + zp];
     }
 }
 
@@ -210,19 +239,25 @@ cudaError_t measure_fp64_tflops(int device, double* tflops) {
 cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh, double helm_f,
                            const double* ksq, int nq, double* HinvF, double* PinvF, double* PpinT, int* info,
                            cudaStream_t s) {
-    const int nz = g.nz;
-    const size_t sm = (size_t)nz * nz * sizeof(double) + nz * sizeof(double) + nz * sizeof(int);
-    if (sm > 200 * 1024) return cudaErrorInvalidValue;
+    const int nz = g.nz, h = nz / 2, he = nz - h, ho = h;
+    const size_t sm_f = ((size_t)he * he + (size_t)ho * ho + he) * sizeof(double) + he * sizeof(int);
+    const size_t sm_p = ((size_t)nz * nz + nz) * sizeof(double) + nz * sizeof(int);
     int dev = 0, optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e) return e;
     if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev))) return e;
     cudaFuncAttributes fa;
-    if ((e = cudaFuncGetAttributes(&fa, k_build_inverses))) return e;
-    const int limit = optin - (int)fa.sharedSizeBytes;
-    if ((int)sm > limit) return cudaErrorInvalidValue;
-    if ((e = cudaFuncSetAttribute(k_build_inverses, cudaFuncAttributeMaxDynamicSharedMemorySize, limit))) return e;
-    k_build_inverses<<<2 * nq + 1, 256, sm, s>>>(nz, S, wh, helm_f, ksq, nq, HinvF, PinvF, PpinT, info);
+    if ((e = cudaFuncGetAttributes(&fa, k_build_inverses_folded))) return e;
+    int limit = optin - (int)fa.sharedSizeBytes;
+    if ((int)sm_f > limit) return cudaErrorInvalidValue;
+    if ((e = cudaFuncSetAttribute(k_build_inverses_folded, cudaFuncAttributeMaxDynamicSharedMemorySize, limit)))
+        return e;
+    if ((e = cudaFuncGetAttributes(&fa, k_build_pinned))) return e;
+    limit = optin - (int)fa.sharedSizeBytes;
+    if ((int)sm_p > limit) return cudaErrorInvalidValue;
+    if ((e = cudaFuncSetAttribute(k_build_pinned, cudaFuncAttributeMaxDynamicSharedMemorySize, limit))) return e;
+    k_build_inverses_folded<<<2 * nq, 256, sm_f, s>>>(nz, S, wh, helm_f, ksq, nq, HinvF, PinvF, info);
+    k_build_pinned<<<1, 256, sm_p, s>>>(nz, S, PpinT, info);
     return cudaGetLastError();
 }
 

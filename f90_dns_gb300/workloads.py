@@ -82,3 +82,27 @@ def ensemble_draws(n: int = 64, seed: int = 0) -> list[dict]:
 
 def point_count(wl: dict) -> int:
     return int(wl["nx"]) * int(wl["ny"]) * int(wl["nz"])
+
+
+def white_noise(wl: dict, seed: int = 0, amplitude: float = 1.0e-3):
+    """Seeded white noise for the large workload: uniform in [-amplitude,
+    amplitude) on u, v, w at every point (numpy PCG64 stream of `seed`),
+    arrays (nz, ny, nx).  Not a reference feature; it is added to the
+    analytical initial condition and the walls are zeroed again."""
+    rng = np.random.default_rng(seed)
+    shp = (int(wl["nz"]), int(wl["ny"]), int(wl["nx"]))
+    return tuple(rng.uniform(-amplitude, amplitude, shp) for _ in range(3))
+
+
+def noisy_initial_state(d, wl: dict, seed: int = 0, amplitude: float = 1.0e-3) -> None:
+    """Add white_noise() to the analytical initial condition held by the
+    ChannelDNS `d` and re-impose the no-slip walls (planes k=1, nz)."""
+    st = d.get_state(walls=False)
+    noise = white_noise(wl, seed, amplitude)
+    out = {}
+    for k, nz_ in zip(("u", "v", "w"), noise):
+        a = st[k] + nz_
+        a[0] = 0.0
+        a[-1] = 0.0
+        out[k] = a
+    d.set_state(u=out["u"], v=out["v"], w=out["w"])
