@@ -49,7 +49,8 @@ EXPORTED_SYMBOLS = (
     "dns3d_ensemble_step", "dns3d_ensemble_step_timed",
     "dns3d_server_opts_defaults", "dns3d_server_create", "dns3d_server_submit", "dns3d_server_poll",
     "dns3d_server_wait", "dns3d_server_result_state", "dns3d_server_release", "dns3d_server_get_stats",
-    "dns3d_server_destroy",
+    "dns3d_server_destroy", "dns3d_restart_write", "dns3d_restart_read", "dns3d_save_restart",
+    "dns3d_load_restart", "dns3d_get_config",
 )
 
 
@@ -116,6 +117,12 @@ class CServerStats(C.Structure):
                 ("point_steps_done", C.c_ulonglong), ("uptime_s", C.c_double)]
 
 
+class CRestartHeader(C.Structure):
+    _fields_ = [("istep", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("time", C.c_double), ("dt", C.c_double), ("re", C.c_double), ("alpha", C.c_double),
+                ("beta", C.c_double)]
+
+
 class Dns3DError(RuntimeError):
     """A non-zero status from the C-ABI (the reference would ``stop`` here)."""
 
@@ -177,6 +184,11 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_server_release.argtypes = [hp, C.c_longlong]
     lib.dns3d_server_get_stats.argtypes = [hp, C.POINTER(CServerStats)]
     lib.dns3d_server_destroy.argtypes = [hp]
+    lib.dns3d_restart_write.argtypes = [C.c_char_p, C.POINTER(CRestartHeader)] + [vp] * 7 + [C.POINTER(CPIState)]
+    lib.dns3d_restart_read.argtypes = [C.c_char_p, C.POINTER(CRestartHeader)] + [vp] * 7 + [C.POINTER(CPIState)]
+    lib.dns3d_save_restart.argtypes = [hp, C.c_char_p, ip, C.c_double]
+    lib.dns3d_load_restart.argtypes = [hp, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    lib.dns3d_get_config.argtypes = [hp, C.POINTER(CConfig)]
     lib.dns3d_last_error.argtypes = [hp]
     lib.dns3d_last_error.restype = C.c_char_p
     for n in EXPORTED_SYMBOLS:
@@ -400,6 +412,19 @@ class ChannelDNS:
                                       C.byref(cpi) if cpi is not None else None)
         self._check(rc, "dns3d_set_state")
 
+    def save_restart(self, path: str, istep: int, time: float) -> None:
+        """Write the state as a restart file in the reference's format."""
+        self._check(self.lib.dns3d_save_restart(self._h, os.fsencode(path), int(istep), float(time)),
+                    "dns3d_save_restart")
+
+    def load_restart(self, path: str) -> tuple:
+        """Load a restart file; returns (istep, time).  grad_p_prev stays zero,
+        as in the reference's restart."""
+        st, tm = C.c_int(0), C.c_double(0.0)
+        self._check(self.lib.dns3d_load_restart(self._h, os.fsencode(path), C.byref(st), C.byref(tm)),
+                    "dns3d_load_restart")
+        return int(st.value), float(tm.value)
+
     def diagnostics(self) -> Diagnostics:
         d = CDiag()
         rc = self.lib.dns3d_diagnostics(self._h, C.byref(d))
@@ -562,3 +587,35 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def restart_write(path: str, istep: int, time: float, dt: float, re: float, alpha: float, beta: float,
+                  u, v, w, un=None, vn=None, wn=None, p_total=None, pi: dict | None = None) -> None:
+    """Encode a restart file (no GPU); arrays (nz, ny, nx) float64."""
+    nz, ny, nx = np.shape(u)
+    hdr = CRestartHeader(istep, nx, ny, nz, time, dt, re, alpha, beta)
+    arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, w, un, vn, wn, p_total)]
+    cpi = None
+    if pi is not None:
+        cpi = CPIState()
+        for k, val in pi.items():
+            setattr(cpi, k, val)
+    rc = load_library().dns3d_restart_write(os.fsencode(path), C.byref(hdr), *[_ptr(a) for a in arrs],
+                                            C.byref(cpi) if cpi is not None else None)
+    if rc:
+        raise Dns3DError(rc, "dns3d_restart_write", path)
+
+
+def restart_read(path: str, nx: int, ny: int, nz: int) -> dict:
+    """Decode a restart file written for an nx x ny x nz grid (no GPU)."""
+    hdr = CRestartHeader(0, nx, ny, nz, 0.0, 0.0, 0.0, 0.0, 0.0)
+    out = {k: np.empty((nz, ny, nx)) for k in ("u", "v", "w", "un", "vn", "wn", "p_total")}
+    pi = CPIState()
+    rc = load_library().dns3d_restart_read(os.fsencode(path), C.byref(hdr),
+                                           *[_ptr(out[k]) for k in ("u", "v", "w", "un", "vn", "wn", "p_total")],
+                                           C.byref(pi))
+    if rc:
+        raise Dns3DError(rc, "dns3d_restart_read", path)
+    out.update({n: getattr(hdr, n) for n, _ in CRestartHeader._fields_})
+    out["pi"] = {n: getattr(pi, n) for n, _ in CPIState._fields_ if n != "pad_"}
+    return out

@@ -698,6 +698,12 @@ int dns3d_get_state(dns3d_handle* h, double* u, double* v, double* w, double* p_
     return DNS3D_OK;
 }
 
+int dns3d_get_config(dns3d_handle* h, dns3d_config* cfg) {
+    if (!h || !cfg) return DNS3D_E_INVALID;
+    *cfg = h->cfg;
+    return DNS3D_OK;
+}
+
 int dns3d_set_clock(dns3d_handle* h, int step, double time) {
     if (!h) return DNS3D_E_INVALID;
     h->step = step;

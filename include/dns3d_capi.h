@@ -252,6 +252,43 @@ int dns3d_server_release(dns3d_server* s, long long request_id);
 int dns3d_server_get_stats(dns3d_server* s, dns3d_server_stats* stats);
 int dns3d_server_destroy(dns3d_server* s);
 
+/* Restart files in the reference's format (write_restart_file_3d /
+ * read_restart_file_3d, DNS_pressure_BC_3D.f90:2976-3209): Fortran stream
+ * unformatted, no record markers, little-endian:
+ *   'DNS3D_RESTART_v1.0' (18 bytes); istep (int32), time, dt (f64);
+ *   nx, ny, nz (int32); re, alpha, beta (f64); u, v, w, un, vn, wn, p_total
+ *   (f64, u(nx,ny,nz) order each); current_pressure_gradient,
+ *   current_bulk_velocity, bulk_velocity_error_integral,
+ *   bulk_velocity_error_prev (f64).
+ * The two host functions encode and decode a file from caller arrays (no GPU);
+ * NULL arrays are written as zeros / skipped on read.  A grid mismatch on read
+ * returns DNS3D_E_INVALID (the reference then ignores the file); a file that
+ * ends before the four PI scalars keeps them at their defaults, as the
+ * reference does. */
+typedef struct dns3d_restart_header {
+    int istep;
+    int nx, ny, nz;
+    double time, dt;
+    double re, alpha, beta;
+} dns3d_restart_header;
+int dns3d_restart_write(const char* path, const dns3d_restart_header* hdr, const double* u, const double* v,
+                        const double* w, const double* un, const double* vn, const double* wn,
+                        const double* p_total, const dns3d_pi_state* pi);
+/* hdr->nx, ny, nz give the expected grid on entry; the rest is filled in.
+ * pi fields not in the file (sum, count, average) are left unchanged. */
+int dns3d_restart_read(const char* path, dns3d_restart_header* hdr, double* u, double* v, double* w,
+                       double* un, double* vn, double* wn, double* p_total, dns3d_pi_state* pi);
+/* Handle level: save the current state as a restart file (un, vn, wn are
+ * written equal to u, v, w: the state at the start of a step, which is what
+ * the reference's in-loop writes record, 3D:300-308); load one into the
+ * handle.  Loading sets u, v, w, p_total and the four PI scalars and leaves
+ * the wall gradients grad_p_prev at zero, as the reference's restart does
+ * (it never restores them, 3D:957, 3057-3209). */
+int dns3d_save_restart(dns3d_handle* h, const char* path, int istep, double time);
+int dns3d_load_restart(dns3d_handle* h, const char* path, int* istep, double* time);
+/* The configuration the handle was created with. */
+int dns3d_get_config(dns3d_handle* h, dns3d_config* cfg);
+
 /* Device bytes held by a handle for a given config (admission control). */
 int dns3d_footprint_bytes(const dns3d_config* cfg, unsigned long long* bytes);
 

@@ -41,6 +41,7 @@ def test_library_contains_sm103a_code(built_lib):
 
 
 STRUCTS = {
+    "dns3d_restart_header": capi.CRestartHeader,
     "dns3d_server_opts": capi.CServerOpts,
     "dns3d_request_info": capi.CRequestInfo,
     "dns3d_server_stats": capi.CServerStats,

@@ -165,3 +165,30 @@ def test_state_roundtrip(built_lib):
         d.set_state(u=u)
         st = d.get_state()
     assert np.max(np.abs(st["u"] - u)) < 1e-13
+
+
+def test_restart_save_load_continue(built_lib, tmp_path):
+    """Save after 6 steps, load into a fresh handle, continue 4 steps; the
+    oracle does the same with the reference's restart semantics (grad_p_prev
+    not restored, i.e. zero after the restart)."""
+    wl = dict(C1, flow_control_method=2, target_bulk_velocity=2.0 / 3.0, nx=32, ny=16, nz=17)
+    path = str(tmp_path / "restart.dat")
+    with ChannelDNS(config_from(wl)) as d:
+        d.step(6)
+        d.save_restart(path, 6, 6 * wl["dt"])
+    with ChannelDNS(config_from(wl)) as d:
+        istep, t = d.load_restart(path)
+        assert istep == 6 and abs(t - 6 * wl["dt"]) < 1e-15
+        d.step(4)
+        gst = d.get_state()
+    cfg = oracle_config(wl)
+    g = ref.setup_grid(cfg)
+    st = ref.initial_state(cfg, g)
+    for _ in range(6):
+        ref.step(cfg, g, st)
+    st.gpx[:] = 0.0
+    st.gpy[:] = 0.0
+    for _ in range(4):
+        ref.step(cfg, g, st)
+    err = velocity_errors(gst, st)
+    assert max(err["u"], err["v"], err["w"]) <= TOL, err
