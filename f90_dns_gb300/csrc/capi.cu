@@ -5,6 +5,7 @@
 // boundary condition reads, the PI controller state, the LGL operators and
 // the per-mode operator inverses.  The five stage entry points run the same
 // kernels that dns3d_step() captures into a CUDA graph.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -500,33 +501,79 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
 
     if (c.precision == DNS3D_PREC_MIXED) {
         h->mixed = true;
-        // eigenbasis of the interior Helmholtz problem, S_II V = M_II V Lambda
-        const int ni = nz - 2;
-        std::vector<double> C((size_t)ni * ni), lam, Y;
-        for (int i = 0; i < ni; ++i)
-            for (int j = 0; j < ni; ++j)
-                C[(size_t)i * ni + j] = S[(size_t)(i + 1) * nz + (j + 1)] / std::sqrt(wh[i + 1] * wh[j + 1]);
-        jacobi_eigen(ni, C, lam, Y);
-        const int nip = (ni + 3) / 4 * 4, nzp = (nz + 3) / 4 * 4;
-        std::vector<float> Vf((size_t)ni * nip, 0.f), VtMf((size_t)ni * nip, 0.f), lamf(ni), s0f(ni), snf(ni);
-        for (int i = 0; i < ni; ++i)
-            for (int j = 0; j < ni; ++j) {
-                const double y = Y[(size_t)i * ni + j];
-                Vf[(size_t)j * nip + i] = (float)(y / std::sqrt(wh[i + 1]));     // V[i][j] at [j][i]
-                VtMf[(size_t)i * nip + j] = (float)(y * std::sqrt(wh[i + 1]));   // (V^T M)[j][i] at [i][j]
+        // eigenbasis of the interior Helmholtz problem, S_II V = M_II V Lambda, in
+        // the orthogonal even/odd basis of the (centro-symmetric) interior levels:
+        // C = M^-1/2 S_II M^-1/2 splits into Ce (even) and Co (odd).
+        const int ni = nz - 2, hoi = ni / 2, hei = ni - hoi;
+        const int pe4 = (hei + 3) / 4 * 4, po4 = (hoi + 3) / 4 * 4;
+        const double r2 = std::sqrt(2.0);
+        auto Cint = [&](int i, int j) { return S[(size_t)(i + 1) * nz + (j + 1)] / std::sqrt(wh[i + 1] * wh[j + 1]); };
+        std::vector<double> Ce((size_t)hei * hei), Co((size_t)hoi * hoi), le, lo, Ye, Yo;
+        for (int i = 0; i < hei; ++i)
+            for (int j = 0; j < hei; ++j) {
+                double v;
+                if (i < hoi && j < hoi) v = Cint(i, j) + Cint(i, ni - 1 - j);
+                else if (i < hoi) v = r2 * Cint(i, hoi);   // middle column
+                else if (j < hoi) v = r2 * Cint(hoi, j);   // middle row
+                else v = Cint(hoi, hoi);
+                Ce[(size_t)i * hei + j] = v;
             }
-        for (int j = 0; j < ni; ++j) {
-            double a0 = 0.0, an = 0.0;
-            for (int i = 0; i < ni; ++i) {
-                const double v = Y[(size_t)i * ni + j] / std::sqrt(wh[i + 1]);
-                a0 += v * S[(size_t)(i + 1) * nz + 0];
-                an += v * S[(size_t)(i + 1) * nz + nz - 1];
+        for (int i = 0; i < hoi; ++i)
+            for (int j = 0; j < hoi; ++j) Co[(size_t)i * hoi + j] = Cint(i, j) - Cint(i, ni - 1 - j);
+        jacobi_eigen(hei, Ce, le, Ye);
+        if (hoi > 0) jacobi_eigen(hoi, Co, lo, Yo);
+        auto sq = [&](int i) { return std::sqrt(wh[i + 1]); };  // sqrt(m_i), interior index i
+        std::vector<float> AeT((size_t)hei * pe4, 0.f), AoT((size_t)hoi * po4, 0.f), BeT((size_t)hei * pe4, 0.f),
+            BoT((size_t)hoi * po4, 0.f), lamf(pe4 + po4, 0.f), s0f(pe4 + po4, 0.f), snf(pe4 + po4, 0.f);
+        for (int i = 0; i < hei; ++i) {
+            const double a = (i < hoi) ? sq(i) / r2 : sq(i), b = (i < hoi) ? 1.0 / (sq(i) * r2) : 1.0 / sq(i);
+            for (int j = 0; j < hei; ++j) {
+                const double y = Ye[(size_t)i * hei + j];
+                AeT[(size_t)i * pe4 + j] = (float)(y * a);  // Ae[j][i]
+                BeT[(size_t)j * pe4 + i] = (float)(y * b);  // Be[i][j]
             }
-            lamf[j] = (float)lam[j];
-            s0f[j] = (float)a0;
-            snf[j] = (float)an;
         }
+        for (int i = 0; i < hoi; ++i) {
+            const double a = sq(i) / r2, b = 1.0 / (sq(i) * r2);
+            for (int j = 0; j < hoi; ++j) {
+                const double y = Yo[(size_t)i * hoi + j];
+                AoT[(size_t)i * po4 + j] = (float)(y * a);
+                BoT[(size_t)j * po4 + i] = (float)(y * b);
+            }
+        }
+        // lifting vectors V^T S_I1, V^T S_In: fold M^-1/2 S_I1 orthogonally
+        for (int wall = 0; wall < 2; ++wall) {
+            const int col = wall ? nz - 1 : 0;
+            std::vector<double> gv(ni);
+            for (int i = 0; i < ni; ++i) gv[i] = S[(size_t)(i + 1) * nz + col] / sq(i);
+            std::vector<float>& dst = wall ? snf : s0f;
+            for (int j = 0; j < hei; ++j) {
+                double acc = 0.0;
+                for (int i = 0; i < hei; ++i) {
+                    const double ge = (i < hoi) ? (gv[i] + gv[ni - 1 - i]) / r2 : gv[i];
+                    acc += Ye[(size_t)i * hei + j] * ge;
+                }
+                dst[j] = (float)acc;
+            }
+            for (int j = 0; j < hoi; ++j) {
+                double acc = 0.0;
+                for (int i = 0; i < hoi; ++i) acc += Yo[(size_t)i * hoi + j] * (gv[i] - gv[ni - 1 - i]) / r2;
+                dst[pe4 + j] = (float)acc;
+            }
+        }
+        for (int j = 0; j < hei; ++j) lamf[j] = (float)le[j];
+        for (int j = 0; j < hoi; ++j) lamf[pe4 + j] = (float)lo[j];
+        const int nzp = (nz + 3) / 4 * 4;
         std::vector<float> D1e32(D1e.begin(), D1e.end()), D1o32(D1o.begin(), D1o.end());
+        auto split = [](const std::vector<double>& a) {
+            std::vector<float2> r(a.size());
+            for (size_t i = 0; i < a.size(); ++i) {
+                r[i].x = (float)a[i];
+                r[i].y = (float)(a[i] - (double)r[i].x);
+            }
+            return r;
+        };
+        const std::vector<float2> D1e_df = split(D1e), D1o_df = split(D1o), W1e_df = split(W1e), W1o_df = split(W1o);
         // eigenbasis of the full Neumann problem S V' = M V' Lambda'
         std::vector<double> Cf((size_t)nz * nz), plam, PY;
         for (int i = 0; i < nz; ++i)
@@ -548,22 +595,32 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             }
         for (int j = 0; j < nz; ++j) plamf[j] = (float)plam[j];
         MixedOps& mx = h->mx;
-        mx.nip = nip;
         mx.nzp = nzp;
-        if ((rc = dev_alloc(h, &mx.VT, Vf.size())) || (rc = dev_alloc(h, &mx.VtMT, VtMf.size())) ||
-            (rc = dev_alloc(h, &mx.lam, ni)) || (rc = dev_alloc(h, &mx.s0, ni)) || (rc = dev_alloc(h, &mx.sn, ni)) ||
+        mx.hei = hei;
+        mx.hoi = hoi;
+        mx.pe4 = pe4;
+        mx.po4 = po4;
+        if ((rc = dev_alloc(h, &mx.AeT, AeT.size())) || (rc = dev_alloc(h, &mx.AoT, std::max<size_t>(AoT.size(), 4))) ||
+            (rc = dev_alloc(h, &mx.BeT, BeT.size())) || (rc = dev_alloc(h, &mx.BoT, std::max<size_t>(BoT.size(), 4))) ||
+            (rc = dev_alloc(h, &mx.lam, lamf.size())) || (rc = dev_alloc(h, &mx.s0, s0f.size())) ||
+            (rc = dev_alloc(h, &mx.sn, snf.size())) ||
             (rc = dev_alloc(h, &mx.D1e, D1e32.size())) || (rc = dev_alloc(h, &mx.D1o, D1o32.size())) ||
             (rc = dev_alloc(h, &mx.PV, PV.size())) || (rc = dev_alloc(h, &mx.PVT, PVT.size())) ||
             (rc = dev_alloc(h, &mx.PDVT, PDVT.size())) || (rc = dev_alloc(h, &mx.plam, nz)) ||
+            (rc = dev_alloc(h, &mx.D1e_df, D1e_df.size())) || (rc = dev_alloc(h, &mx.D1o_df, D1o_df.size())) ||
+            (rc = dev_alloc(h, &mx.W1e_df, W1e_df.size())) || (rc = dev_alloc(h, &mx.W1o_df, W1o_df.size())) ||
             (rc = dev_alloc(h, &h->PHIZ, se)))
             return fail(rc);
         struct Up32 { void* d; const void* s; size_t b; } u32[] = {
-            {mx.VT, Vf.data(), Vf.size() * 4}, {mx.VtMT, VtMf.data(), VtMf.size() * 4},
-            {mx.lam, lamf.data(), (size_t)ni * 4}, {mx.s0, s0f.data(), (size_t)ni * 4},
-            {mx.sn, snf.data(), (size_t)ni * 4}, {mx.D1e, D1e32.data(), D1e32.size() * 4},
+            {mx.AeT, AeT.data(), AeT.size() * 4}, {mx.AoT, AoT.data(), AoT.size() * 4},
+            {mx.BeT, BeT.data(), BeT.size() * 4}, {mx.BoT, BoT.data(), BoT.size() * 4},
+            {mx.lam, lamf.data(), lamf.size() * 4}, {mx.s0, s0f.data(), s0f.size() * 4},
+            {mx.sn, snf.data(), snf.size() * 4}, {mx.D1e, D1e32.data(), D1e32.size() * 4},
             {mx.D1o, D1o32.data(), D1o32.size() * 4}, {mx.PV, PV.data(), PV.size() * 4},
             {mx.PVT, PVT.data(), PVT.size() * 4}, {mx.PDVT, PDVT.data(), PDVT.size() * 4},
-            {mx.plam, plamf.data(), (size_t)nz * 4}};
+            {mx.plam, plamf.data(), (size_t)nz * 4},
+            {mx.D1e_df, D1e_df.data(), D1e_df.size() * 8}, {mx.D1o_df, D1o_df.data(), D1o_df.size() * 8},
+            {mx.W1e_df, W1e_df.data(), W1e_df.size() * 8}, {mx.W1o_df, W1o_df.data(), W1o_df.size() * 8}};
         for (auto& u : u32)
             if ((rc = upload(h, u.d, u.s, u.b))) return fail(rc);
         for (int f = 0; f < 6; ++f)

@@ -141,12 +141,25 @@ struct Ops {
 // float4 load feeds four output rows.
 struct MixedOps {
     float* D1e; float* D1o;  // folded (2/ybar) d1, FP32
-    int nip, nzp;            // ni and nz rounded up to multiples of 4
-    float* VtMT;             // [ni][nip]  (V^T M_II)[j][i] stored at [i][j]
-    float* VT;               // [ni][nip]  V[i][j] stored at [j][i]
-    float* lam;              // [ni]       eigenvalues
-    float* s0;               // [ni]       V^T S_I1
-    float* sn;               // [ni]       V^T S_In
+    // folded (2/ybar) d1 and weak-form operator as double-float pairs
+    // (hi = (float)x, lo = (float)(x - hi)) for the divergence right-hand side
+    float2* D1e_df; float2* D1o_df;
+    float2* W1e_df; float2* W1o_df;
+    int nzp;                 // nz rounded up to a multiple of 4
+    // interior eigenbasis, folded: the interior problem is centro-symmetric, so
+    // its eigenvectors are even or odd and the basis splits into an even block
+    // (hei = ni - ni/2 rows) and an odd block (hoi = ni/2), padded to pe4, po4.
+    // Forward: ut_even = Ae [s; u_mid], ut_odd = Ao d (s, d = pair sums and
+    // differences of the interior values); back: pe = Be y_even, po = Bo y_odd,
+    // x_i = pe_i + po_i, x_{ni-1-i} = pe_i - po_i, x_mid = pe_mid.
+    int hei, hoi, pe4, po4;
+    float* AeT;              // [hei][pe4]  Ae[j][i] stored at [i][j]
+    float* AoT;              // [hoi][po4]
+    float* BeT;              // [hei][pe4]  Be[i][j] stored at [j][i]
+    float* BoT;              // [hoi][po4]
+    float* lam;              // [pe4 + po4] eigenvalues (even block, then odd block)
+    float* s0;               // [pe4 + po4] V^T S_I1 in the same order
+    float* sn;               // [pe4 + po4] V^T S_In
     float* PV;               // [nz][nzp]  V'[z][j] stored at [z][j]
     float* PVT;              // [nz][nzp]  V'[z][j] stored at [j][z]
     float* PDVT;             // [nz][nzp]  (D V')[z][j] stored at [j][z]

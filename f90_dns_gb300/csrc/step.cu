@@ -650,39 +650,61 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
                                                        Fields Out, int tc) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int ni = g.nz - 2;
-    const int np = mx.nip;           // ni rounded up to a multiple of 4 (operators zero-padded)
-    const int nb = np / 4;           // row blocks of 4
-    const int tsz = np * tc;
-    float4* sA = reinterpret_cast<float4*>(smraw);   // VtMT [ni][nb] float4
-    float4* sB = sA + (size_t)ni * nb;                // VT   [ni][nb] float4
-    float2* tu = reinterpret_cast<float2*>(sB + (size_t)ni * nb);  // [np][tc] interior u (one component)
-    float2* ts = tu + tsz;                           // [np][tc] interior S
-    float2* ty = ts + tsz;                           // [np][tc] eigen-space update
-    float4* tw = reinterpret_cast<float4*>(ty + tsz);  // [tc] wall terms (x0, y0, xn, yn)
-    float* tk = reinterpret_cast<float*>(tw + tc);     // [tc] k^2 of the column (or -1: skip)
+    const int hei = mx.hei, hoi = mx.hoi, pe4 = mx.pe4, po4 = mx.po4;
+    const int nr = pe4 + po4;        // folded rows (even block, then odd block)
+    const int tsz = nr * tc;
+    float4* sAe = reinterpret_cast<float4*>(smraw);    // AeT [hei][pe4/4]
+    float4* sAo = sAe + (size_t)hei * (pe4 / 4);        // AoT [hoi][po4/4]
+    float4* sBe = sAo + (size_t)hoi * (po4 / 4);        // BeT [hei][pe4/4]
+    float4* sBo = sBe + (size_t)hei * (pe4 / 4);        // BoT [hoi][po4/4]
+    float2* tu = reinterpret_cast<float2*>(sBo + (size_t)hoi * (po4 / 4));  // [nr][tc] folded interior u
+    float2* ts = tu + tsz;                              // [nr][tc] folded interior S
+    float2* ty = ts + tsz;                              // [nr][tc] eigen-space update
+    float4* tw = reinterpret_cast<float4*>(ty + tsz);   // [tc] wall terms
+    float* tk = reinterpret_cast<float*>(tw + tc);      // [tc] k^2 (-1: skip; <= -2: masked source)
     const int m0 = blockIdx.x * tc;
     {
-        const float4* A = reinterpret_cast<const float4*>(mx.VtMT);
-        const float4* B = reinterpret_cast<const float4*>(mx.VT);
-        for (int t = threadIdx.x; t < ni * nb; t += blockDim.x) {
-            sA[t] = __ldg(&A[t]);
-            sB[t] = __ldg(&B[t]);
-        }
+        const float4* A = reinterpret_cast<const float4*>(mx.AeT);
+        for (int t = threadIdx.x; t < hei * (pe4 / 4); t += blockDim.x) sAe[t] = __ldg(&A[t]);
+        A = reinterpret_cast<const float4*>(mx.AoT);
+        for (int t = threadIdx.x; t < hoi * (po4 / 4); t += blockDim.x) sAo[t] = __ldg(&A[t]);
+        A = reinterpret_cast<const float4*>(mx.BeT);
+        for (int t = threadIdx.x; t < hei * (pe4 / 4); t += blockDim.x) sBe[t] = __ldg(&A[t]);
+        A = reinterpret_cast<const float4*>(mx.BoT);
+        for (int t = threadIdx.x; t < hoi * (po4 / 4); t += blockDim.x) sBo[t] = __ldg(&A[t]);
     }
     const float dt = (float)sp.dt, cf = (float)sp.cn_fac, ff = (float)sp.helm_f;
     for (int comp = 0; comp < 3; ++comp) {
-        for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
-            const int i = t / tc, c = t - i * tc;
+        // fold the interior column: even rows k < hei, odd rows pe4 + k
+        for (int t = threadIdx.x; t < pe4 * tc; t += blockDim.x) {
+            const int k = t / tc, c = t - k * tc;
             const int m = m0 + c;
-            float2 a = make_float2(0.f, 0.f), b = a;
-            if (m < g.nm && i < ni) {
-                const size_t o = (size_t)(i + 1) * g.nm + m;
-                const double2 u = F.p[comp][o];
-                a = make_float2((float)u.x, (float)u.y);
-                b = Src.p[comp][o];
+            float2 se = make_float2(0.f, 0.f), de = se, ss = se, ds = se;
+            if (m < g.nm && k < hei) {
+                const size_t o1 = (size_t)(1 + k) * g.nm + m;
+                const double2 a = F.p[comp][o1];
+                const float2 sa = Src.p[comp][o1];
+                const float ax = (float)a.x, ay = (float)a.y;
+                if (k < hoi) {
+                    const size_t o2 = (size_t)(g.nz - 2 - k) * g.nm + m;
+                    const double2 b = F.p[comp][o2];
+                    const float2 sb = Src.p[comp][o2];
+                    const float bx = (float)b.x, by = (float)b.y;
+                    se = make_float2(ax + bx, ay + by);
+                    de = make_float2(ax - bx, ay - by);
+                    ss = make_float2(sa.x + sb.x, sa.y + sb.y);
+                    ds = make_float2(sa.x - sb.x, sa.y - sb.y);
+                } else {
+                    se = make_float2(ax, ay);
+                    ss = sa;
+                }
             }
-            tu[t] = a;
-            ts[t] = b;
+            tu[t] = se;
+            ts[t] = ss;
+            if (k < po4) {
+                tu[(pe4 + k) * tc + c] = de;
+                ts[(pe4 + k) * tc + c] = ds;
+            }
         }
         for (int c = threadIdx.x; c < tc; c += blockDim.x) {
             const int m = m0 + c;
@@ -696,7 +718,7 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
                     keep = !(kx > sp.kx_max || kyi > sp.ky_max);
                 }
                 k2 = (float)__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
-                if (!keep) k2 = -2.f - k2;  // masked source: flag in the sign, k2 recovered below
+                if (!keep) k2 = -2.f - k2;  // masked source: flagged by the sign
                 const double2 u0 = F.p[comp][(size_t)m], un = F.p[comp][(size_t)(g.nz - 1) * g.nm + m];
                 double2 b1 = make_double2(0.0, 0.0), b2 = b1;
                 if (comp < 2) {
@@ -712,8 +734,8 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
             tw[c] = w;
         }
         __syncthreads();
-        // ut = V^T M u, st = V^T M S for 4 eigen-rows j0..j0+3 of one column
-        for (int t = threadIdx.x; t < nb * tc; t += blockDim.x) {
+        // ut, st for 4 eigen-rows of one block (even or odd)
+        for (int t = threadIdx.x; t < (nr / 4) * tc; t += blockDim.x) {
             const int jb = t / tc, c = t - jb * tc;
             const int j0 = 4 * jb;
             float k2 = tk[c];
@@ -723,13 +745,19 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
             }
             const bool keep = k2 >= 0.f;
             if (!keep) k2 = -2.f - k2;
+            const bool even = j0 < pe4;
+            const float4* A = even ? sAe + jb : sAo + (jb - pe4 / 4);
+            const int lda = even ? pe4 / 4 : po4 / 4;
+            const int len = even ? hei : hoi;
+            const float2* cu = tu + (even ? 0 : pe4 * tc);
+            const float2* cs = ts + (even ? 0 : pe4 * tc);
             float2 ut[4], st[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) { ut[q] = make_float2(0.f, 0.f); st[q] = ut[q]; }
-            for (int i = 0; i < ni; ++i) {
-                const float4 e = sA[i * nb + jb];
-                const float2 a = tu[i * tc + c];
-                const float2 b = ts[i * tc + c];
+            for (int i = 0; i < len; ++i) {
+                const float4 e = A[i * lda];
+                const float2 a = cu[i * tc + c];
+                const float2 b = cs[i * tc + c];
                 ut[0].x = fmaf(e.x, a.x, ut[0].x); ut[0].y = fmaf(e.x, a.y, ut[0].y);
                 ut[1].x = fmaf(e.y, a.x, ut[1].x); ut[1].y = fmaf(e.y, a.y, ut[1].y);
                 ut[2].x = fmaf(e.z, a.x, ut[2].x); ut[2].y = fmaf(e.z, a.y, ut[2].y);
@@ -746,8 +774,7 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
             const float4 w = tw[c];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const int j = j0 + q;
-                if (j >= ni) { ty[j * tc + c] = make_float2(0.f, 0.f); continue; }
+                const int j = j0 + q;  // padded rows have lam = s0 = sn = 0 and zero inputs
                 const float k2l = k2 + __ldg(&mx.lam[j]);
                 const float gj = 1.0f / (1.0f + ff * k2l);
                 const float cu_ = -(cf + ff) * k2l * gj;
@@ -758,29 +785,47 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
             }
         }
         __syncthreads();
-        // delta_I = V y for 4 rows i0..i0+3; walls are the boundary values
-        for (int t = threadIdx.x; t < nb * tc; t += blockDim.x) {
+        // back to the interior levels: 4 output pairs per item
+        for (int t = threadIdx.x; t < (pe4 / 4) * tc; t += blockDim.x) {
             const int ib = t / tc, c = t - ib * tc;
             const int m = m0 + c;
             if (tk[c] == -1.f) continue;
-            float2 d[4];
+            const int i0 = 4 * ib;
+            float2 pe[4], po[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) d[q] = make_float2(0.f, 0.f);
-            for (int j = 0; j < ni; ++j) {
-                const float4 e = sB[j * nb + ib];
+            for (int q = 0; q < 4; ++q) { pe[q] = make_float2(0.f, 0.f); po[q] = pe[q]; }
+            for (int j = 0; j < hei; ++j) {
+                const float4 e = sBe[j * (pe4 / 4) + ib];
                 const float2 y = ty[j * tc + c];
-                d[0].x = fmaf(e.x, y.x, d[0].x); d[0].y = fmaf(e.x, y.y, d[0].y);
-                d[1].x = fmaf(e.y, y.x, d[1].x); d[1].y = fmaf(e.y, y.y, d[1].y);
-                d[2].x = fmaf(e.z, y.x, d[2].x); d[2].y = fmaf(e.z, y.y, d[2].y);
-                d[3].x = fmaf(e.w, y.x, d[3].x); d[3].y = fmaf(e.w, y.y, d[3].y);
+                pe[0].x = fmaf(e.x, y.x, pe[0].x); pe[0].y = fmaf(e.x, y.y, pe[0].y);
+                pe[1].x = fmaf(e.y, y.x, pe[1].x); pe[1].y = fmaf(e.y, y.y, pe[1].y);
+                pe[2].x = fmaf(e.z, y.x, pe[2].x); pe[2].y = fmaf(e.z, y.y, pe[2].y);
+                pe[3].x = fmaf(e.w, y.x, pe[3].x); pe[3].y = fmaf(e.w, y.y, pe[3].y);
+            }
+            if (i0 < po4) {
+                for (int j = 0; j < hoi; ++j) {
+                    const float4 e = sBo[j * (po4 / 4) + ib];
+                    const float2 y = ty[(pe4 + j) * tc + c];
+                    po[0].x = fmaf(e.x, y.x, po[0].x); po[0].y = fmaf(e.x, y.y, po[0].y);
+                    po[1].x = fmaf(e.y, y.x, po[1].x); po[1].y = fmaf(e.y, y.y, po[1].y);
+                    po[2].x = fmaf(e.z, y.x, po[2].x); po[2].y = fmaf(e.z, y.y, po[2].y);
+                    po[3].x = fmaf(e.w, y.x, po[3].x); po[3].y = fmaf(e.w, y.y, po[3].y);
+                }
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const int i = 4 * ib + q;
-                if (i >= ni) break;
-                const size_t o = (size_t)(i + 1) * g.nm + m;
-                const double2 u = F.p[comp][o];
-                Out.p[comp][o] = make_double2(u.x + (double)d[q].x, u.y + (double)d[q].y);
+                const int i = i0 + q;
+                if (i >= hei) break;
+                const size_t o1 = (size_t)(1 + i) * g.nm + m;
+                const double2 u1 = F.p[comp][o1];
+                if (i < hoi) {
+                    const size_t o2 = (size_t)(g.nz - 2 - i) * g.nm + m;
+                    const double2 u2 = F.p[comp][o2];
+                    Out.p[comp][o1] = make_double2(u1.x + (double)(pe[q].x + po[q].x), u1.y + (double)(pe[q].y + po[q].y));
+                    Out.p[comp][o2] = make_double2(u2.x + (double)(pe[q].x - po[q].x), u2.y + (double)(pe[q].y - po[q].y));
+                } else {  // middle level (ni odd)
+                    Out.p[comp][o1] = make_double2(u1.x + (double)pe[q].x, u1.y + (double)pe[q].y);
+                }
             }
             if (ib == 0) {  // x_1 = bc1, x_n = bc2 (identity rows)
                 for (int wall = 0; wall < 2; ++wall) {
@@ -795,6 +840,98 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
         }
         __syncthreads();
     }
+}
+
+// ------------------------------------------------------------------ double-float
+// Double-float ("df64") arithmetic on the FP32 pipe for the one contraction of
+// the mixed path that needs FP64 accuracy.  A value is hi + lo with hi the
+// FP32 rounding of x and lo the FP32 rounding of x - hi (~48 significant bits).
+// Products use the exact FMA residual fma(a, b, -a*b); sums use Knuth's
+// two-sum, so an n-term dot product is accurate to ~n 2^-48 relative to
+// sum |a_i b_i|.  On GB300 one such multiply-add is ~11 FP32 instructions,
+// about 6x cheaper than a native FP64 FMA.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_split(double x) {
+    DF r;
+    r.hi = (float)x;
+    r.lo = (float)(x - (double)r.hi);
+    return r;
+}
+// s += a * b, a and b double-float
+// (the _rn intrinsics are never contracted into FMAs, which would break the
+// exactness of the two-sum)
+__device__ __forceinline__ void df_mac(DF& s, float ahi, float alo, float bhi, float blo) {
+    const float p = __fmul_rn(ahi, bhi);
+    float e = fmaf(ahi, bhi, -p);
+    e = fmaf(ahi, blo, e);
+    e = fmaf(alo, bhi, e);
+    const float t = __fadd_rn(s.hi, p);
+    const float z = __fsub_rn(t, s.hi);
+    const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, z)), __fsub_rn(p, z));
+    s.lo += err + e;
+    s.hi = t;
+}
+__device__ __forceinline__ double df_value(DF s) { return (double)s.hi + (double)s.lo; }
+
+// Folded tile of an FP64 field as double-float pairs: [he][tc] even, [ho][tc] odd;
+// each element float4 = (re.hi, re.lo, im.hi, im.lo).
+__device__ __forceinline__ void fold_load_df(float4* tile, const double2* __restrict__ src, const GridDev& g,
+                                             int m0, int tc, int he, int ho) {
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        double2 fe = make_double2(0.0, 0.0), fo = fe;
+        if (m < g.nm) {
+            const double2 a = src[(size_t)k * g.nm + m];
+            if (k < ho) {
+                const double2 b = src[(size_t)(g.nz - 1 - k) * g.nm + m];
+                fe = make_double2(a.x + b.x, a.y + b.y);
+                fo = make_double2(a.x - b.x, a.y - b.y);
+            } else {
+                fe = a;
+            }
+        }
+        const DF ex = df_split(fe.x), ey = df_split(fe.y);
+        tile[t] = make_float4(ex.hi, ex.lo, ey.hi, ey.lo);
+        if (k < ho) {
+            const DF ox = df_split(fo.x), oy = df_split(fo.y);
+            tile[(he + k) * tc + c] = make_float4(ox.hi, ox.lo, oy.hi, oy.lo);
+        }
+    }
+}
+
+// Antisymmetric folded operator (double-float) on a double-float folded tile:
+// the output pair (z = k, z = nz-1-k) as FP64.
+__device__ __forceinline__ Pair anti_apply_df(const float2* __restrict__ De, const float2* __restrict__ Do,
+                                              const float4* tile, int k, int c, int tc, int he, int ho) {
+    DF yex{0.f, 0.f}, yey{0.f, 0.f}, yox{0.f, 0.f}, yoy{0.f, 0.f};
+    const float2* er = De + (size_t)k * ho;
+    const float4* fo = tile + he * tc;
+    for (int j = 0; j < ho; ++j) {
+        const float2 a = __ldg(&er[j]);
+        const float4 b = fo[j * tc + c];
+        df_mac(yex, a.x, a.y, b.x, b.y);
+        df_mac(yey, a.x, a.y, b.z, b.w);
+    }
+    Pair p;
+    if (k < ho) {
+        const float2* orow = Do + (size_t)k * he;
+        for (int j = 0; j < he; ++j) {
+            const float2 a = __ldg(&orow[j]);
+            const float4 b = tile[j * tc + c];
+            df_mac(yox, a.x, a.y, b.x, b.y);
+            df_mac(yoy, a.x, a.y, b.z, b.w);
+        }
+        const double ex = df_value(yex), ey = df_value(yey), ox = df_value(yox), oy = df_value(yoy);
+        p.a = make_double2(ex + ox, ey + oy);
+        p.b = make_double2(ex - ox, ey - oy);
+    } else {
+        p.a = make_double2(df_value(yex), df_value(yey));
+        p.b = p.a;
+    }
+    return p;
 }
 
 // Pressure for the mixed form.  The right-hand side (the collocation
@@ -815,15 +952,15 @@ __global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, 
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nz = g.nz, he = ops.he, ho = ops.ho;
     const int np = mx.nzp, nb = np / 4;
-    double2* tw = reinterpret_cast<double2*>(smraw);   // folded w* (FP64)  [nz][tc]
+    float4* tw = reinterpret_cast<float4*>(smraw);    // folded w* (double-float)  [nz][tc]
     float2* tb = reinterpret_cast<float2*>(tw + nz * tc);   // rhs b (FP32)  [np][tc]
     float2* tp = tb + np * tc;                              // phi~ (FP32)  [np][tc]
     const int m0 = blockIdx.x * tc;
-    fold_load(tw, WS, g, m0, tc, he, ho);
+    fold_load_df(tw, WS, g, m0, tc, he, ho);
     for (int t = threadIdx.x; t < (np - nz) * tc; t += blockDim.x) tb[nz * tc + t] = make_float2(0.f, 0.f);
     __syncthreads();
-    const double* __restrict__ Ae = sp.weak_form ? ops.W1e : ops.D1e;
-    const double* __restrict__ Ao = sp.weak_form ? ops.W1o : ops.D1o;
+    const float2* __restrict__ Ae = sp.weak_form ? mx.W1e_df : mx.D1e_df;
+    const float2* __restrict__ Ao = sp.weak_form ? mx.W1o_df : mx.D1o_df;
     for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
         const int k = t / tc, c = t - k * tc;
         const int m = m0 + c;
@@ -832,7 +969,7 @@ __global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, 
             tb[(nz - 1 - k) * tc + c] = make_float2(0.f, 0.f);
             continue;
         }
-        const Pair dz = anti_apply(Ae, Ao, tw, k, c, tc, he, ho);
+        const Pair dz = anti_apply_df(Ae, Ao, tw, k, c, tc, he, ho);
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
         const double2 b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
         tb[k * tc + c] = make_float2((float)b1.x, (float)b1.y);
@@ -1073,8 +1210,9 @@ cudaError_t set_smem(K kern, size_t bytes) {
 int pad4(int n) { return (n + 3) / 4 * 4; }
 
 size_t viscous_mixed_smem(const GridDev& g, int tc) {
-    const size_t ni = g.nz - 2, np = pad4(g.nz - 2);
-    return 2 * ni * np * sizeof(float) + 3 * np * tc * sizeof(float2) + tc * (sizeof(float4) + sizeof(float));
+    const size_t ni = g.nz - 2, hoi = ni / 2, hei = ni - hoi, pe4 = pad4((int)hei), po4 = pad4((int)hoi);
+    return 2 * (hei * pe4 + hoi * po4) * sizeof(float) + 3 * (pe4 + po4) * tc * sizeof(float2) +
+           tc * (sizeof(float4) + sizeof(float));
 }
 
 int tile_cols_mixed(const GridDev& g) {
@@ -1084,7 +1222,7 @@ int tile_cols_mixed(const GridDev& g) {
 }
 
 size_t pressure_mixed_smem(const GridDev& g, int tc) {
-    return (size_t)g.nz * tc * sizeof(double2) + 2 * (size_t)pad4(g.nz) * tc * sizeof(float2);
+    return (size_t)g.nz * tc * sizeof(float4) + 2 * (size_t)pad4(g.nz) * tc * sizeof(float2);
 }
 
 cudaError_t prepare_step_kernels(const GridDev& g) {
