@@ -24,7 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I", os.path.join(ROOT, "include")]
 
-SOURCES = ["capi.cu", "fft.cu", "step.cu", "setup.cu", "host.cpp", "noalloc.cu", "server.cpp", "restart.cpp"]
+SOURCES = ["capi.cu", "fft.cu", "step.cu", "setup.cu", "host.cpp", "noalloc.cu", "server.cpp", "restart.cpp",
+           "output.cpp"]
 
 
 def _nvcc() -> str:

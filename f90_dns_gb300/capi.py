@@ -50,7 +50,11 @@ EXPORTED_SYMBOLS = (
     "dns3d_server_opts_defaults", "dns3d_server_create", "dns3d_server_submit", "dns3d_server_poll",
     "dns3d_server_wait", "dns3d_server_result_state", "dns3d_server_release", "dns3d_server_get_stats",
     "dns3d_server_destroy", "dns3d_restart_write", "dns3d_restart_read", "dns3d_save_restart",
-    "dns3d_load_restart", "dns3d_get_config",
+    "dns3d_load_restart", "dns3d_get_config", "dns3d_get_clock", "dns3d_lgl_nodes_weights",
+    "dns3d_flow_statistics", "dns3d_output_init", "dns3d_output_time_series_row",
+    "dns3d_output_flow_statistics", "dns3d_output_spanwise_profile", "dns3d_output_velocity_snapshot",
+    "dns3d_output_simulation_summary", "dns3d_write_time_series_data", "dns3d_write_flow_statistics",
+    "dns3d_write_spanwise_averaged_profile", "dns3d_write_velocity_field_snapshot",
 )
 
 
@@ -123,6 +127,21 @@ class CRestartHeader(C.Structure):
                 ("beta", C.c_double)]
 
 
+class CFlowStats(C.Structure):
+    """``dns3d_flow_stats``: the numbers of the reference's output files."""
+
+    _fields_ = [
+        ("umax", C.c_double), ("vmax", C.c_double), ("wmax", C.c_double), ("energy", C.c_double),
+        ("bulk_velocity", C.c_double), ("dpdx", C.c_double), ("dpdx_avg", C.c_double),
+        ("wall_shear_lower", C.c_double), ("wall_shear_upper", C.c_double),
+        ("friction_velocity_avg", C.c_double), ("re_tau", C.c_double), ("time", C.c_double),
+        ("step", C.c_int), ("flow_control_method", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class Dns3DError(RuntimeError):
     """A non-zero status from the C-ABI (the reference would ``stop`` here)."""
 
@@ -189,6 +208,20 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_save_restart.argtypes = [hp, C.c_char_p, ip, C.c_double]
     lib.dns3d_load_restart.argtypes = [hp, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.dns3d_get_config.argtypes = [hp, C.POINTER(CConfig)]
+    lib.dns3d_get_clock.argtypes = [hp, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    lib.dns3d_lgl_nodes_weights.argtypes = [ip, vp, vp]
+    lib.dns3d_flow_statistics.argtypes = [hp, C.POINTER(CFlowStats), vp, vp, vp]
+    lib.dns3d_output_init.argtypes = [C.c_char_p]
+    lib.dns3d_output_time_series_row.argtypes = [C.c_char_p, C.POINTER(CFlowStats)]
+    lib.dns3d_output_flow_statistics.argtypes = [C.c_char_p, C.POINTER(CFlowStats)]
+    lib.dns3d_output_spanwise_profile.argtypes = [C.c_char_p, ip, C.c_double, ip, vp, vp, vp, vp]
+    lib.dns3d_output_velocity_snapshot.argtypes = [C.c_char_p, ip, C.c_double, ip, ip, ip, C.c_double,
+                                                   C.c_double, vp, vp, vp, vp]
+    lib.dns3d_output_simulation_summary.argtypes = [C.c_char_p, C.POINTER(CConfig), C.c_char_p, C.c_char_p,
+                                                    C.c_char_p, ip, ip, C.c_double]
+    for n in ("dns3d_write_time_series_data", "dns3d_write_flow_statistics",
+              "dns3d_write_spanwise_averaged_profile", "dns3d_write_velocity_field_snapshot"):
+        getattr(lib, n).argtypes = [hp, C.c_char_p]
     lib.dns3d_last_error.argtypes = [hp]
     lib.dns3d_last_error.restype = C.c_char_p
     for n in EXPORTED_SYMBOLS:
@@ -425,6 +458,43 @@ class ChannelDNS:
                     "dns3d_load_restart")
         return int(st.value), float(tm.value)
 
+    def get_clock(self) -> tuple:
+        st, tm = C.c_int(0), C.c_double(0.0)
+        self._check(self.lib.dns3d_get_clock(self._h, C.byref(st), C.byref(tm)), "dns3d_get_clock")
+        return int(st.value), float(tm.value)
+
+    def flow_statistics(self, profiles: bool = False):
+        """The numbers of write_flow_statistics / write_time_series_data
+        (dict), and with ``profiles`` the plane means u_avg, v_avg, w_avg
+        per level (arrays of nz)."""
+        st = CFlowStats()
+        nz = self.shape[0]
+        prof = [np.empty(nz) for _ in range(3)] if profiles else [None] * 3
+        rc = self.lib.dns3d_flow_statistics(self._h, C.byref(st), *[_ptr(a) for a in prof])
+        if rc and rc != DNS3D_E_NONFINITE:
+            self._check(rc, "dns3d_flow_statistics")
+        out = st.as_dict()
+        if profiles:
+            out.update(u_avg=prof[0], v_avg=prof[1], w_avg=prof[2])
+        return out
+
+    def write_time_series_data(self, out_dir: str) -> None:
+        self._write("dns3d_write_time_series_data", out_dir)
+
+    def write_flow_statistics(self, out_dir: str) -> None:
+        self._write("dns3d_write_flow_statistics", out_dir)
+
+    def write_spanwise_averaged_profile(self, out_dir: str) -> None:
+        self._write("dns3d_write_spanwise_averaged_profile", out_dir)
+
+    def write_velocity_field_snapshot(self, out_dir: str) -> None:
+        self._write("dns3d_write_velocity_field_snapshot", out_dir)
+
+    def _write(self, fn: str, out_dir: str) -> None:
+        rc = getattr(self.lib, fn)(self._h, os.fsencode(out_dir))
+        if rc and rc != DNS3D_E_NONFINITE:
+            self._check(rc, fn)
+
     def diagnostics(self) -> Diagnostics:
         d = CDiag()
         rc = self.lib.dns3d_diagnostics(self._h, C.byref(d))
@@ -619,3 +689,65 @@ def restart_read(path: str, nx: int, ny: int, nz: int) -> dict:
     out.update({n: getattr(hdr, n) for n, _ in CRestartHeader._fields_})
     out["pi"] = {n: getattr(pi, n) for n, _ in CPIState._fields_ if n != "pad_"}
     return out
+
+
+# ---------------------------------------------------------------- output files
+
+def lgl_nodes_weights(nz: int):
+    """LGL nodes (ascending from -1) and weights of lgl_module.f90:30-80."""
+    z, w = np.empty(nz), np.empty(nz)
+    rc = load_library().dns3d_lgl_nodes_weights(int(nz), _ptr(z), _ptr(w))
+    if rc:
+        raise Dns3DError(rc, "dns3d_lgl_nodes_weights")
+    return z, w
+
+
+def _flow_stats(st) -> CFlowStats:
+    if isinstance(st, CFlowStats):
+        return st
+    c = CFlowStats()
+    for n, _ in CFlowStats._fields_:
+        if n in st:
+            setattr(c, n, st[n])
+    return c
+
+
+def _out_call(fn: str, *args) -> None:
+    rc = getattr(load_library(), fn)(*args)
+    if rc:
+        raise Dns3DError(rc, fn)
+
+
+def output_init(out_dir: str) -> None:
+    """output_time_series.dat and flow_statistics.dat with their headers."""
+    _out_call("dns3d_output_init", os.fsencode(out_dir))
+
+
+def output_time_series_row(out_dir: str, stats) -> None:
+    _out_call("dns3d_output_time_series_row", os.fsencode(out_dir), C.byref(_flow_stats(stats)))
+
+
+def output_flow_statistics(out_dir: str, stats) -> None:
+    _out_call("dns3d_output_flow_statistics", os.fsencode(out_dir), C.byref(_flow_stats(stats)))
+
+
+def output_spanwise_profile(out_dir: str, istep: int, time: float, z, u_avg, v_avg, w_avg) -> None:
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (z, u_avg, v_avg, w_avg)]
+    _out_call("dns3d_output_spanwise_profile", os.fsencode(out_dir), int(istep), float(time), len(arrs[0]),
+              *[_ptr(a) for a in arrs])
+
+
+def output_velocity_snapshot(out_dir: str, istep: int, time: float, xlen: float, ylen: float, z, u, v, w) -> None:
+    """velocity_field_NNNNN.dat from arrays (nz, ny, nx)."""
+    nz, ny, nx = np.shape(u)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (z, u, v, w)]
+    _out_call("dns3d_output_velocity_snapshot", os.fsencode(out_dir), int(istep), float(time), nx, ny, nz,
+              float(xlen), float(ylen), *[_ptr(a) for a in arrs])
+
+
+def output_simulation_summary(out_dir: str, cfg: CConfig, input_filename: str = "", output_directory=None,
+                              restart_filename: str = "restart.dat", restarted: bool = False,
+                              restart_step: int = 0, restart_time: float = 0.0) -> None:
+    _out_call("dns3d_output_simulation_summary", os.fsencode(out_dir), C.byref(cfg), os.fsencode(input_filename),
+              None if output_directory is None else os.fsencode(output_directory), os.fsencode(restart_filename),
+              int(bool(restarted)), int(restart_step), float(restart_time))

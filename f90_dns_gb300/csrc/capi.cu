@@ -21,6 +21,11 @@ struct dns3d_handle {
     dns3d_config cfg{};
     GridDev g{};
     cudaStream_t stream = nullptr;
+    // A second stream for work off the critical path (the PI update during the
+    // nonlinear term; the FP64 mean-mode solves of the mixed form beside their
+    // FP32 mode tiles), forked from and joined back to `stream` by events.
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev[3] = {nullptr, nullptr, nullptr}, join_ev[3] = {nullptr, nullptr, nullptr};
     FftCtx fft{};
     Ops ops{};
     MixedOps mx{};
@@ -161,6 +166,24 @@ void mark(dns3d_handle* h, const char* name) {
 
 void fft_hook(void* ctx, const char* name) { mark(static_cast<dns3d_handle*>(ctx), name); }
 
+// Side-branch work: launched on h->side after everything queued so far on
+// h->stream, and joined back before the next dependent launch.  While the
+// kernels are being profiled one by one the branch stays on h->stream, so
+// each event pair brackets exactly one kernel.
+cudaStream_t side_stream(dns3d_handle* h) { return h->prof ? h->stream : h->side; }
+
+cudaError_t fork_side(dns3d_handle* h, int i) {
+    if (h->prof) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(h->fork_ev[i], h->stream);
+    return e ? e : cudaStreamWaitEvent(h->side, h->fork_ev[i], 0);
+}
+
+cudaError_t join_side(dns3d_handle* h, int i) {
+    if (h->prof) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(h->join_ev[i], h->side);
+    return e ? e : cudaStreamWaitEvent(h->stream, h->join_ev[i], 0);
+}
+
 // Parity folding of a full row-major operator (see step.cu): antisymmetric
 // D -> De [he][ho], Do [ho][he]; symmetric A -> Ae [he][he], Ao [ho][ho].
 void fold_antisymmetric(const std::vector<double>& D, int n, std::vector<double>& De, std::vector<double>& Do) {
@@ -219,11 +242,24 @@ int run_source_terms_mixed(dns3d_handle* h) {
     return DNS3D_OK;
 }
 
+int run_source_terms_fp64(dns3d_handle* h);
+
 int run_source_terms(dns3d_handle* h) {
     const GridDev& g = h->g;
-    CK(h, launch_pi_update(g, h->ops, h->pp, h->U, h->d_pi, h->stream));
+    // the PI update reads only the mean mode of u and writes only the
+    // controller state, which the viscous step reads: it runs beside the
+    // nonlinear term and joins at the end of this stage
+    CK(h, fork_side(h, 0));
+    CK(h, launch_pi_update(g, h->ops, h->pp, h->U, h->d_pi, side_stream(h)));
     mark(h, "pi_update");
-    if (h->mixed) return run_source_terms_mixed(h);
+    int rc = h->mixed ? run_source_terms_mixed(h) : run_source_terms_fp64(h);
+    if (rc) return rc;
+    CK(h, join_side(h, 0));
+    return DNS3D_OK;
+}
+
+int run_source_terms_fp64(dns3d_handle* h) {
+    const GridDev& g = h->g;
     // vorticity into the u*,v*,w* buffers (free until the viscous step)
     CK(h, launch_vorticity(g, h->ops, h->U, h->V, h->W, h->US, h->VS, h->WS, h->stream));
     mark(h, "vorticity");
@@ -250,8 +286,13 @@ int run_viscous(dns3d_handle* h) {
         F.p[0] = h->U; F.p[1] = h->V; F.p[2] = h->W;
         O.p[0] = h->US; O.p[1] = h->VS; O.p[2] = h->WS;
         for (int f = 0; f < 3; ++f) S.p[f] = h->src32[f];
-        CK(h, launch_viscous_mixed(h->g, h->mx, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->stream));
+        // mode (0,0) in FP64 on the side branch, all other modes in FP32 tiles
+        CK(h, fork_side(h, 1));
+        CK(h, launch_viscous_mean_mode(h->g, h->ops, h->sp, F, S, h->GP, h->d_pi, O, side_stream(h)));
+        mark(h, "viscous_mean_mode");
+        CK(h, launch_viscous_mixed(h->g, h->mx, h->ops, h->sp, F, S, h->GP, O, h->stream));
         mark(h, "viscous_mixed");
+        CK(h, join_side(h, 1));
         return DNS3D_OK;
     }
     Fields F{}, S{}, O{};
@@ -265,8 +306,12 @@ int run_viscous(dns3d_handle* h) {
 
 int run_pressure(dns3d_handle* h) {
     if (h->mixed) {
+        CK(h, fork_side(h, 2));
+        CK(h, launch_pressure_mean_mode(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, side_stream(h)));
+        mark(h, "pressure_mean_mode");
         CK(h, launch_pressure_mixed(h->g, h->mx, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->stream));
         mark(h, "pressure_mixed");
+        CK(h, join_side(h, 2));
         return DNS3D_OK;
     }
     CK(h, launch_pressure(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->stream));
@@ -309,6 +354,11 @@ void release(dns3d_handle* h) {
     if (!h) return;
     if (h->graph) cudaGraphExecDestroy(h->graph);
     for (cudaEvent_t e : h->ev) cudaEventDestroy(e);
+    for (int i = 0; i < 3; ++i) {
+        if (h->fork_ev[i]) cudaEventDestroy(h->fork_ev[i]);
+        if (h->join_ev[i]) cudaEventDestroy(h->join_ev[i]);
+    }
+    if (h->side) cudaStreamDestroy(h->side);
     h->ev.clear();
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
@@ -385,7 +435,13 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     const dns3d_config& c = h->cfg;
     auto fail = [&](int code) { release(h); delete h; return code; };
     if (cudaSetDevice(c.device) != cudaSuccess) return fail(DNS3D_E_CUDA);
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(DNS3D_E_CUDA);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(DNS3D_E_CUDA);
+    for (int i = 0; i < 3; ++i)
+        if (cudaEventCreateWithFlags(&h->fork_ev[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->join_ev[i], cudaEventDisableTiming) != cudaSuccess)
+            return fail(DNS3D_E_CUDA);
 
     GridDev& g = h->g;
     g.nx = c.nx; g.ny = c.ny; g.nz = c.nz;
@@ -898,8 +954,14 @@ int dns3d_synchronize(dns3d_handle* h) {
     return DNS3D_OK;
 }
 
-int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out) {
-    if (!h || !out) return DNS3D_E_INVALID;
+}  // extern "C"
+
+namespace {
+
+// output_diagnostics_3d's reductions (and, with `div`, check_divergence_3d's)
+// of the device state; `mean` receives the (0,0) mode of u, v, w per level
+// when non-null (3 * nz values, plane sums of the physical fields).
+int diag_core(dns3d_handle* h, dns3d_diag* out, bool with_div, std::vector<double2>* mean3) {
     CK(h, cudaSetDevice(h->cfg.device));
     const GridDev& g = h->g;
     const dns3d_config& c = h->cfg;
@@ -910,22 +972,30 @@ int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out) {
     CK(h, fft_c2r(h->fft, g, sp, ph, 3, g.nz, h->stream));
     CK(h, launch_diag_reduce(g, h->ops, h->phys[0], h->phys[1], h->phys[2], h->d_red, h->red_blocks, h->d_out,
                              h->stream));
-    // check_divergence_3d: max |DX u + DY v + Dz w| in physical space
-    // (the divergence spectrum goes to the last FFT scratch slot, which a
-    // one-field c2r does not touch, so diagnostics never clobber step state)
-    double2* div = h->fft.tmp + (size_t)5 * spec_elems(c);
-    CK(h, launch_divergence(g, h->ops, h->U, h->V, h->W, div, h->stream));
-    Fields dv{}; dv.p[0] = div;
-    RFields dp{}; dp.p[0] = h->phys[3];
-    CK(h, fft_c2r(h->fft, g, dv, dp, 1, g.nz, h->stream));
-    CK(h, launch_maxabs(g, h->phys[3], phys_elems(c), h->d_red, h->red_blocks, h->d_out + 4, h->stream));
-    double res[5];
+    if (with_div) {
+        // check_divergence_3d: max |DX u + DY v + Dz w| in physical space
+        // (the divergence spectrum goes to the last FFT scratch slot, which a
+        // one-field c2r does not touch, so diagnostics never clobber step state)
+        double2* div = h->fft.tmp + (size_t)5 * spec_elems(c);
+        CK(h, launch_divergence(g, h->ops, h->U, h->V, h->W, div, h->stream));
+        Fields dv{}; dv.p[0] = div;
+        RFields dp{}; dp.p[0] = h->phys[3];
+        CK(h, fft_c2r(h->fft, g, dv, dp, 1, g.nz, h->stream));
+        CK(h, launch_maxabs(g, h->phys[3], phys_elems(c), h->d_red, h->red_blocks, h->d_out + 4, h->stream));
+    }
+    double res[5] = {0, 0, 0, 0, 0};
     dns3d_pi_state pi{};
-    CK(h, cudaMemcpyAsync(res, h->d_out, sizeof(res), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(res, h->d_out, sizeof(double) * (with_div ? 5 : 4), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaMemcpyAsync(&pi, h->d_pi, sizeof(pi), cudaMemcpyDeviceToHost, h->stream));
-    std::vector<double2> mean(g.nz);
-    CK(h, cudaMemcpy2DAsync(mean.data(), sizeof(double2), h->U, (size_t)g.nm * sizeof(double2), sizeof(double2),
-                            g.nz, cudaMemcpyDeviceToHost, h->stream));
+    std::vector<double2> mean_local;
+    std::vector<double2>& mean = mean3 ? *mean3 : mean_local;
+    const int ncomp = mean3 ? 3 : 1;
+    mean.resize((size_t)ncomp * g.nz);
+    const double2* comp[3] = {h->U, h->V, h->W};
+    for (int f = 0; f < ncomp; ++f)
+        CK(h, cudaMemcpy2DAsync(mean.data() + (size_t)f * g.nz, sizeof(double2), comp[f],
+                                (size_t)g.nm * sizeof(double2), sizeof(double2), g.nz, cudaMemcpyDeviceToHost,
+                                h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     const double ybar = 2.0;
     const double fac = (c.xlen / c.nx) * (c.ylen / c.ny) * (ybar / 2.0);
@@ -943,6 +1013,77 @@ int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out) {
     out->step = h->step;
     if (!std::isfinite(out->energy) || !std::isfinite(out->umax) || !std::isfinite(out->max_div))
         return DNS3D_E_NONFINITE;
+    return DNS3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out) {
+    if (!h || !out) return DNS3D_E_INVALID;
+    return diag_core(h, out, true, nullptr);
+}
+
+int dns3d_flow_statistics(dns3d_handle* h, dns3d_flow_stats* out, double* u_avg, double* v_avg, double* w_avg) {
+    if (!h || !out) return DNS3D_E_INVALID;
+    dns3d_diag d{};
+    std::vector<double2> mean;
+    const int rc = diag_core(h, &d, false, &mean);
+    if (rc && rc != DNS3D_E_NONFINITE) return rc;
+    const dns3d_config& c = h->cfg;
+    const int nz = c.nz;
+    const double nxny = (double)c.nx * (double)c.ny;
+    std::memset(out, 0, sizeof(*out));
+    out->umax = d.umax;
+    out->vmax = d.vmax;
+    out->wmax = d.wmax;
+    out->energy = d.energy;
+    out->dpdx = d.dpdx;
+    out->dpdx_avg = d.dpdx_avg;
+    out->flow_control_method = c.flow_control_method;
+    // bulk velocity: calculate_bulk_velocity_3d for method 2 (3D:2434-2464),
+    // sum u*zwts / (nx*ny) / 2 otherwise (3D:2874-2889)
+    if (c.flow_control_method == 2) {
+        out->bulk_velocity = d.u_bulk;
+    } else {
+        double vol = 0.0;
+        for (int k = 0; k < nz; ++k) vol += mean[k].x * h->zwts[k];
+        out->bulk_velocity = vol / nxny / 2.0;
+    }
+    // wall shear by one-sided differences of the plane means (3D:2891-2921)
+    const double nu = 1.0 / c.re;
+    const double* z = h->zpts.data();
+    const double dl = (mean[1].x - mean[0].x) / nxny / (z[1] - z[0]);
+    const double du = (mean[nz - 1].x - mean[nz - 2].x) / nxny / (z[nz - 1] - z[nz - 2]);
+    out->wall_shear_lower = nu * dl;
+    out->wall_shear_upper = nu * du;
+    out->friction_velocity_avg = std::sqrt((std::fabs(out->wall_shear_lower) + std::fabs(out->wall_shear_upper)) / 2.0);
+    out->re_tau = out->friction_velocity_avg * c.re;  // 3D:2948-2949
+    out->time = h->time;
+    out->step = h->step;
+    double* dst[3] = {u_avg, v_avg, w_avg};
+    for (int f = 0; f < 3; ++f)
+        if (dst[f])
+            for (int k = 0; k < nz; ++k) dst[f][k] = mean[(size_t)f * nz + k].x / nxny;  // 3D:2819-2833
+    return rc;
+}
+
+int dns3d_get_clock(dns3d_handle* h, int* step, double* time) {
+    if (!h || !step || !time) return DNS3D_E_INVALID;
+    *step = h->step;
+    *time = h->time;
+    return DNS3D_OK;
+}
+
+int dns3d_lgl_nodes_weights(int nz, double* z, double* w) {
+    if (nz < 3 || !z || !w) return DNS3D_E_INVALID;
+    std::vector<double> x, wt;
+    lgl_nodes_weights(nz, x, wt);
+    for (int k = 0; k < nz; ++k) {
+        z[k] = x[k];
+        w[k] = wt[k];
+    }
     return DNS3D_OK;
 }
 

@@ -199,7 +199,14 @@ cudaError_t launch_correction_mixed(const GridDev& g, const Ops& ops, const Step
 cudaError_t launch_products32(const GridDev& g, FRFields in6, FRFields out3, cudaStream_t s);
 cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops,
                                  const StepParams& sp, Fields F, FFields Src, const double2* GP,
-                                 const dns3d_pi_state* pi, Fields Out, cudaStream_t s);
+                                 Fields Out, cudaStream_t s);
+// The mixed form's mode (0,0) in FP64 (independent of the mode tiles above).
+cudaError_t launch_viscous_mean_mode(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F,
+                                     FFields Src, const double2* GP, const dns3d_pi_state* pi,
+                                     Fields Out, cudaStream_t s);
+cudaError_t launch_pressure_mean_mode(const GridDev& g, const Ops& ops, const StepParams& sp,
+                                      const double2* US, const double2* VS, const double2* WS,
+                                      double2* PHI, double2* PHIZ, cudaStream_t s);
 cudaError_t launch_pressure(const GridDev& g, const Ops& ops, const StepParams& sp,
                             const double2* US, const double2* VS, const double2* WS,
                             double2* PHI, cudaStream_t s);

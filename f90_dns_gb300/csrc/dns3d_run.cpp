@@ -6,8 +6,17 @@
 // advance time and call the five step subroutines in order (3D:286-326),
 // print the diagnostics line every nwrt steps (output_diagnostics_3d,
 // 3D:2134-2143) and the divergence every 50 steps (check_divergence_3d,
-// 3D:2171-2190).  Output files, restart files and timing summaries of the
-// reference are not written.
+// 3D:2171-2190).  Like the reference it writes, into its output directory,
+// simulation_summary.txt, output_time_series.dat and flow_statistics.dat
+// every nwrt steps, velocity_field_NNNNN.dat and spanwise_profile_NNNNN.dat
+// every 10*nwrt steps (3D:329-339), and restart.dat every restart_write_freq
+// steps (at the start of the step, 3D:300-308) and after the last step
+// (3D:367).  Timing summaries are not printed.
+//
+// The output directory is <input base name>_<YYYYMMDD_HHMMSS> in the working
+// directory, as the reference's create_output_directory (3D:2557-2586), or
+// the directory named by DNS3D_OUTPUT_DIR; DNS3D_OUTPUT_DIR=none writes no
+// files.
 //
 // usage: dns3d_run [input_file]      (default input_3d.dat, as the reference)
 // exit status: 0 on success, 1 on a library error (the reference `stop`s).
@@ -15,6 +24,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <ctime>
+#include <string>
+#include <sys/stat.h>
 
 #include "dns3d_capi.h"
 
@@ -46,6 +58,31 @@ void e12_4(char* out, double v) {
     std::snprintf(out, 16, "%12s", buf);
 }
 
+// create_output_directory (3D:2557-2586): base name of the input file up to
+// ".dat", then _YYYYMMDD_HHMMSS.
+std::string output_directory(const char* input) {
+    std::string base = input;
+    const size_t dat = base.find(".dat");
+    if (dat != std::string::npos) base = base.substr(0, dat);
+    const std::time_t now = std::time(nullptr);
+    std::tm t{};
+    localtime_r(&now, &t);
+    char ts[32];
+    std::snprintf(ts, sizeof ts, "_%04d%02d%02d_%02d%02d%02d", t.tm_year + 1900, t.tm_mon + 1, t.tm_mday, t.tm_hour,
+                  t.tm_min, t.tm_sec);
+    return base + ts;
+}
+
+bool make_dirs(const std::string& path) {  // mkdir -p
+    for (size_t i = 1; i <= path.size(); ++i)
+        if (i == path.size() || path[i] == '/') {
+            const std::string p = path.substr(0, i);
+            struct stat st;
+            if (stat(p.c_str(), &st) != 0 && mkdir(p.c_str(), 0755) != 0) return false;
+        }
+    return true;
+}
+
 int check(int rc, const char* where, dns3d_handle* h) {
     if (rc == DNS3D_OK) return 0;
     std::fprintf(stderr, " ERROR in %s: %s%s%s\n", where, dns3d_strerror(rc), h ? ": " : "",
@@ -71,6 +108,22 @@ int main(int argc, char** argv) {
     dns3d_handle* h = nullptr;
     if (check(dns3d_create(&cfg, &h), "dns3d_create", nullptr)) return 1;
 
+    const char* od_env = std::getenv("DNS3D_OUTPUT_DIR");
+    const bool files = !(od_env && std::strcmp(od_env, "none") == 0);
+    const std::string od = od_env && *od_env && files ? std::string(od_env) : output_directory(input);
+    const std::string restart_path = od + "/restart.dat";
+    if (files) {
+        if (!make_dirs(od)) {
+            std::fprintf(stderr, " ERROR: cannot create output directory %s\n", od.c_str());
+            return 1;
+        }
+        std::printf(" Output directory created:\n   %s\n", od.c_str());
+        if (check(dns3d_output_init(od.c_str()), "initialize_output_files", h) ||
+            check(dns3d_output_simulation_summary(od.c_str(), &cfg, input, od.c_str(), "restart.dat", 0, 0, 0.0),
+                  "write_simulation_summary", h))
+            return 1;
+    }
+
     dns3d_diag d;
     if (check(dns3d_diagnostics(h, &d), "check_divergence_3d", h)) return 1;
     char dv[16];
@@ -81,6 +134,9 @@ int main(int argc, char** argv) {
     char a[5][16];
     for (int istep = 1; istep <= cfg.nsteps; ++istep) {
         time = time + cfg.dt;
+        if (files && cfg.restart_write_freq > 0 && istep % cfg.restart_write_freq == 0 &&
+            check(dns3d_save_restart(h, restart_path.c_str(), istep, time), "write_restart_file_3d", h))
+            return 1;
         dns3d_set_clock(h, istep, time);
         if (check(dns3d_compute_source_terms(h), "compute_source_terms_3d", h) ||
             check(dns3d_viscous_step(h), "viscous_step_3d", h) ||
@@ -109,11 +165,25 @@ int main(int argc, char** argv) {
                             time, a[0], a[1], a[2], a[3], a[4]);
             }
         }
+        if (wrt && files) {
+            if (check(dns3d_write_time_series_data(h, od.c_str()), "write_time_series_data", h) ||
+                check(dns3d_write_flow_statistics(h, od.c_str()), "write_flow_statistics", h))
+                return 1;
+            if (istep % (10 * cfg.nwrt) == 0) {
+                if (check(dns3d_write_velocity_field_snapshot(h, od.c_str()), "write_velocity_field_snapshot", h) ||
+                    check(dns3d_write_spanwise_averaged_profile(h, od.c_str()), "write_spanwise_averaged_profile", h))
+                    return 1;
+                std::printf(" Velocity field snapshot written: velocity_field_%05d.dat\n", istep);
+                std::printf(" Spanwise profile written: spanwise_profile_%05d.dat\n", istep);
+            }
+        }
         if (div) {
             e12_4(dv, d.max_div);
             std::printf(" Step %6d, Max divergence: %s\n", istep, dv);
         }
     }
+    if (files && check(dns3d_save_restart(h, restart_path.c_str(), cfg.nsteps, time), "write_restart_file_3d", h))
+        return 1;
     std::printf(" Time integration completed successfully!\n");
     dns3d_destroy(h);
     return 0;

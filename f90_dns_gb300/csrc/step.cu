@@ -1280,12 +1280,18 @@ cudaError_t launch_vorticity_mixed(const GridDev& g, const MixedOps& mx, const O
     return cudaGetLastError();
 }
 
+cudaError_t launch_pressure_mean_mode(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                                      const double2* VS, const double2* WS, double2* PHI, double2* PHIZ,
+                                      cudaStream_t s) {
+    // mode (0,0) of the mixed form in FP64: pinned Poisson, then its dphi/dz
+    k_pressure<<<1, 256, (2 * (size_t)g.nz + g.nz) * sizeof(double2), s>>>(g, ops, sp, US, VS, WS, PHI, 1);
+    k_dz_mean_mode<<<1, 64, (size_t)g.nz * sizeof(double2), s>>>(g, ops, PHI, PHIZ);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pressure_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const StepParams& sp,
                                   const double2* US, const double2* VS, const double2* WS, double2* PHI,
                                   double2* PHIZ, cudaStream_t s) {
-    // mode (0,0) in FP64: pinned Poisson, then its dphi/dz
-    k_pressure<<<1, 256, (2 * (size_t)g.nz + g.nz) * sizeof(double2), s>>>(g, ops, sp, US, VS, WS, PHI, 1);
-    k_dz_mean_mode<<<1, 64, (size_t)g.nz * sizeof(double2), s>>>(g, ops, PHI, PHIZ);
     const int tc = tile_cols(g, 2);
     const size_t sm = pressure_mixed_smem(g, tc);
     k_pressure_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc);
@@ -1310,11 +1316,15 @@ cudaError_t launch_products32(const GridDev& g, FRFields in6, FRFields out3, cud
     return cudaGetLastError();
 }
 
-cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const StepParams& sp,
-                                 Fields F, FFields Src, const double2* GP, const dns3d_pi_state* pi, Fields Out,
-                                 cudaStream_t s) {
-    // mode (0,0): FP64 Helmholtz with the forcing (one CTA, one mode)
+cudaError_t launch_viscous_mean_mode(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F, FFields Src,
+                                     const double2* GP, const dns3d_pi_state* pi, Fields Out, cudaStream_t s) {
+    // mode (0,0) of the mixed form: FP64 Helmholtz with the forcing (one CTA)
     k_viscous<float2><<<1, 256, 6 * (size_t)g.nz * sizeof(double2), s>>>(g, ops, sp, F, Src, GP, pi, Out, 1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const StepParams& sp,
+                                 Fields F, FFields Src, const double2* GP, Fields Out, cudaStream_t s) {
     const int tc = tile_cols_mixed(g);
     const size_t sm = viscous_mixed_smem(g, tc);
     k_viscous_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, F, Src, GP, Out, tc);

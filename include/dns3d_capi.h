@@ -288,6 +288,62 @@ int dns3d_save_restart(dns3d_handle* h, const char* path, int istep, double time
 int dns3d_load_restart(dns3d_handle* h, const char* path, int* istep, double* time);
 /* The configuration the handle was created with. */
 int dns3d_get_config(dns3d_handle* h, dns3d_config* cfg);
+/* The handle's step counter and time (dns3d_set_clock, advanced by dns3d_step). */
+int dns3d_get_clock(dns3d_handle* h, int* step, double* time);
+/* LGL nodes (z, ascending from -1) and weights of lgl_module.f90:30-80. */
+int dns3d_lgl_nodes_weights(int nz, double* z, double* w);
+
+/* ---- Flow statistics and the reference's output files ----------------------
+ * The numbers of write_time_series_data, write_flow_statistics and
+ * write_spanwise_averaged_profile (DNS_pressure_BC_3D.f90:2702-2952),
+ * reduced from the device state at the handle's clock. */
+typedef struct dns3d_flow_stats {
+    double umax, vmax, wmax;     /* max |u|, |v|, |w|                                  */
+    double energy;               /* mean kinetic energy with LGL weights (3D:2710-2730) */
+    double bulk_velocity;        /* method 2: calculate_bulk_velocity_3d (3D:2434-2464);
+                                    otherwise sum u*zwts/(nx*ny)/2 (3D:2874-2889)     */
+    double dpdx, dpdx_avg;       /* current and running-average dP/dx                 */
+    double wall_shear_lower;     /* (1/Re) * plane mean of (u_2 - u_1)/(z_2 - z_1)     */
+    double wall_shear_upper;     /* (1/Re) * plane mean of (u_nz - u_nz-1)/(z_nz - z_nz-1) (3D:2891-2921) */
+    double friction_velocity_avg;/* sqrt((|tau_lower| + |tau_upper|)/2) (3D:2948)      */
+    double re_tau;               /* friction_velocity_avg * Re (3D:2949)              */
+    double time;
+    int step;
+    int flow_control_method;
+} dns3d_flow_stats;
+/* u_avg, v_avg, w_avg (nz each, may be NULL): plane means per level k. */
+int dns3d_flow_statistics(dns3d_handle* h, dns3d_flow_stats* out, double* u_avg, double* v_avg, double* w_avg);
+
+/* Host file writers in the reference's formats (no GPU).  `dir` is an
+ * existing directory (the reference's timestamped output directory is the
+ * caller's choice).
+ *  - output_init: output_time_series.dat and flow_statistics.dat with their
+ *    headers (initialize_output_files, 3D:2667-2694);
+ *  - time_series_row: one '(I8,7(ES15.6))' row (method 2: average dP/dx and
+ *    U_bulk) or '(I8,6(ES15.6))' row (current dP/dx) appended to
+ *    output_time_series.dat, which must exist (3D:2736-2745);
+ *  - flow_statistics: flow_statistics.dat replaced (3D:2925-2951);
+ *  - spanwise_profile: spanwise_profile_NNNNN.dat (3D:2808-2838);
+ *  - velocity_snapshot: velocity_field_NNNNN.dat, '(3I6,6ES15.6)' per point,
+ *    k outermost, i fastest (3D:2765-2786);
+ *  - simulation_summary: simulation_summary.txt (3D:2594-2659), start time
+ *    from the local clock. */
+int dns3d_output_init(const char* dir);
+int dns3d_output_time_series_row(const char* dir, const dns3d_flow_stats* st);
+int dns3d_output_flow_statistics(const char* dir, const dns3d_flow_stats* st);
+int dns3d_output_spanwise_profile(const char* dir, int istep, double time, int nz, const double* z,
+                                  const double* u_avg, const double* v_avg, const double* w_avg);
+int dns3d_output_velocity_snapshot(const char* dir, int istep, double time, int nx, int ny, int nz, double xlen,
+                                   double ylen, const double* z, const double* u, const double* v, const double* w);
+int dns3d_output_simulation_summary(const char* dir, const dns3d_config* cfg, const char* input_filename,
+                                    const char* output_directory, const char* restart_filename, int restarted,
+                                    int restart_step, double restart_time);
+/* Handle level, the reference's subroutine names: reduce the state on the
+ * device and write the file at the handle's step and time. */
+int dns3d_write_time_series_data(dns3d_handle* h, const char* dir);
+int dns3d_write_flow_statistics(dns3d_handle* h, const char* dir);
+int dns3d_write_spanwise_averaged_profile(dns3d_handle* h, const char* dir);
+int dns3d_write_velocity_field_snapshot(dns3d_handle* h, const char* dir);
 
 /* Device bytes held by a handle for a given config (admission control). */
 int dns3d_footprint_bytes(const dns3d_config* cfg, unsigned long long* bytes);

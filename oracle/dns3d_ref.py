@@ -618,3 +618,122 @@ def run(cfg: Config, nsteps: int, record_every: int = 1, noise=None):
             d["step"] = st.istep
             hist.append(d)
     return g, st, hist
+
+
+# --------------------------------------------------------------------------
+# Output files: the numbers and text of write_time_series_data (3D:2702-2748),
+# write_flow_statistics (3D:2849-2952), write_spanwise_averaged_profile
+# (3D:2799-2841) and write_velocity_field_snapshot (3D:2756-2791)
+# --------------------------------------------------------------------------
+def flow_statistics(cfg: Config, g: Grid, st: State) -> dict:
+    """The values write_flow_statistics / write_time_series_data write, by
+    the reference's physical-space loops (as numpy sums)."""
+    d = diagnostics(cfg, g, st)
+    nxny = float(g.nx * g.ny)
+    if cfg.flow_control_method == 2:
+        bulk = calculate_bulk_velocity(g, st.u)                              # 3D:2872
+    else:
+        bulk = float(np.sum(st.u * g.zwts[:, None, None])) / nxny / 2.0     # 3D:2874-2889
+    nu = 1.0 / cfg.re
+    dl = float(np.sum((st.u[1] - st.u[0]) / (g.zpts[1] - g.zpts[0]))) / nxny        # 3D:2898-2905
+    du = float(np.sum((st.u[-1] - st.u[-2]) / (g.zpts[-1] - g.zpts[-2]))) / nxny    # 3D:2909-2916
+    tl, tu = nu * dl, nu * du
+    ut = math.sqrt((abs(tl) + abs(tu)) / 2.0)
+    return dict(umax=d["umax"], vmax=d["vmax"], wmax=d["wmax"], energy=d["energy"], bulk_velocity=bulk,
+                dpdx=d["dpdx"], dpdx_avg=d["dpdx_avg"], wall_shear_lower=tl, wall_shear_upper=tu,
+                friction_velocity_avg=ut, re_tau=ut * cfg.re, time=st.time, step=st.istep,
+                flow_control_method=cfg.flow_control_method)
+
+
+def spanwise_profile(g: Grid, st: State):
+    """Plane means of u, v, w per level k (3D:2817-2834)."""
+    n = float(g.nx * g.ny)
+    return tuple(np.sum(a, axis=(1, 2)) / n for a in (st.u, st.v, st.w))
+
+
+def fortran_es(v: float, w: int, d: int) -> str:
+    """gfortran's ESw.d: one nonzero digit, d decimals, exponent E+dd (three
+    digits without the letter beyond +-99), right-aligned in w; '*' * w when
+    the text does not fit; "Infinity" when it fits, else "Inf".  Rounding is
+    to nearest on the exact binary value."""
+    from decimal import ROUND_HALF_EVEN, Decimal, localcontext
+    if math.isnan(v):
+        s = "NaN"
+    elif math.isinf(v):
+        s = ("-" if v < 0 else "") + ("Infinity" if w >= 8 + (v < 0) else "Inf")
+    else:
+        with localcontext() as ctx:
+            ctx.prec = 1200
+            ctx.Emin, ctx.Emax = -2000, 2000
+            x = Decimal(v)
+            sign = "-" if x.is_signed() else ""
+            x = abs(x)
+            if x == 0:
+                mant, e = Decimal(0).quantize(Decimal(1).scaleb(-d)), 0
+            else:
+                e = x.adjusted()
+                mant = (x.scaleb(-e)).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+                if mant >= 10:
+                    e += 1
+                    mant = (x.scaleb(-e)).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+        es = ("E%+03d" % e) if abs(e) <= 99 else ("%+04d" % e)
+        s = f"{sign}{mant}{es}"
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+def fortran_f(v: float, w: int, d: int) -> str:
+    """gfortran's Fw.d (leading zero kept when it fits)."""
+    from decimal import ROUND_HALF_EVEN, Decimal, localcontext
+    if not math.isfinite(v):
+        return fortran_es(v, w, d)
+    with localcontext() as ctx:
+        ctx.prec = 1200
+        ctx.Emin, ctx.Emax = -2000, 2000
+        x = Decimal(v).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+        s = f"{x:f}"  # a negative value that rounds to zero keeps its sign
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+def time_series_row(s: dict) -> str:
+    """One row of output_time_series.dat (3D:2740-2744)."""
+    cols = [s["time"], s["umax"], s["vmax"], s["wmax"], s["energy"]]
+    cols += [s["dpdx_avg"], s["bulk_velocity"]] if s["flow_control_method"] == 2 else [s["dpdx"]]
+    return f"{s['step']:8d}" + "".join(fortran_es(c, 15, 6) for c in cols)
+
+
+def flow_statistics_text(s: dict) -> str:
+    """flow_statistics.dat (3D:2925-2951)."""
+    es = lambda x: fortran_es(x, 15, 6)
+    pg = s["dpdx_avg"] if s["flow_control_method"] == 2 else s["dpdx"]
+    lines = ["# DNS 3D Flow Statistics Summary", f"# Time step: {s['step']}", "# Time: " + fortran_f(s["time"], 12, 6),
+             "", "# Maximum velocities:", "u_max = " + es(s["umax"]), "v_max = " + es(s["vmax"]),
+             "w_max = " + es(s["wmax"]), "", "# Energy and bulk flow:", "kinetic_energy = " + es(s["energy"]),
+             "bulk_velocity = " + es(s["bulk_velocity"]), "pressure_gradient = " + es(pg), "",
+             "# Wall shear stress:", "tau_wall_lower = " + es(s["wall_shear_lower"]),
+             "tau_wall_upper = " + es(s["wall_shear_upper"]),
+             "friction_velocity_avg = " + es(s["friction_velocity_avg"]), "re_tau = " + es(s["re_tau"])]
+    return "\n".join(lines) + "\n"
+
+
+def spanwise_profile_text(istep: int, time: float, z, ua, va, wa) -> str:
+    """spanwise_profile_NNNNN.dat (3D:2812-2835)."""
+    lines = ["# DNS 3D Spanwise-Averaged Velocity Profile", f"# Time step: {istep}",
+             "# Time: " + fortran_f(time, 12, 6), "# Columns: k, z, u_avg, v_avg, w_avg"]
+    for k in range(len(z)):
+        lines.append(f"{k + 1:6d}" + "".join(fortran_es(float(a[k]), 15, 6) for a in (z, ua, va, wa)))
+    return "\n".join(lines) + "\n"
+
+
+def velocity_snapshot_text(istep: int, time: float, xlen: float, ylen: float, z, u, v, w) -> str:
+    """velocity_field_NNNNN.dat (3D:2769-2786): k outer, i fastest."""
+    nz, ny, nx = u.shape
+    lines = ["# DNS 3D Velocity Field Snapshot", f"# Time step: {istep}", "# Time: " + fortran_f(time, 12, 6),
+             "# Columns: i, j, k, x, y, z, u, v, w"]
+    for k in range(nz):
+        for j in range(ny):
+            y = float(j) * ylen / float(ny)
+            for i in range(nx):
+                x = float(i) * xlen / float(nx)
+                lines.append(f"{i + 1:6d}{j + 1:6d}{k + 1:6d}" + "".join(
+                    fortran_es(float(c), 15, 6) for c in (x, y, z[k], u[k, j, i], v[k, j, i], w[k, j, i])))
+    return "\n".join(lines) + "\n"

@@ -19,7 +19,8 @@ LINE = re.compile(r"Step\s+(\d+), t=\s*([0-9.]+), \|u\|max=\s*(\S+), \|v\|max=\s
 @pytest.mark.parametrize("key", ["standard", "weak_form"])
 def test_driver_prints_reference_trace(built_lib, key):
     inp = os.path.join(HERE, "golden", f"input_trace_32x32x17_{key}.dat")
-    res = subprocess.run([build.RUNNER, inp], capture_output=True, text=True, timeout=300)
+    env = dict(os.environ, DNS3D_OUTPUT_DIR="none")  # stdout only; the files are tested elsewhere
+    res = subprocess.run([build.RUNNER, inp], capture_output=True, text=True, timeout=300, env=env)
     assert res.returncode == 0, res.stderr
     got = [m.groups() for m in map(LINE.search, res.stdout.splitlines()) if m]
     with open(os.path.join(HERE, "golden", "reference_traces.json")) as f:
@@ -35,6 +36,7 @@ def test_driver_prints_reference_trace(built_lib, key):
 def test_driver_rejects_bad_input(built_lib, tmp_path):
     bad = tmp_path / "bad.dat"
     bad.write_text("&grid\n nx_input = 100, ny_input = 32, nz_input = 17\n/\n")
-    res = subprocess.run([build.RUNNER, str(bad)], capture_output=True, text=True, timeout=120)
+    res = subprocess.run([build.RUNNER, str(bad)], capture_output=True, text=True, timeout=120,
+                         env=dict(os.environ, DNS3D_OUTPUT_DIR="none"))
     assert res.returncode == 1
     assert "unsupported grid size" in res.stderr
