@@ -32,6 +32,13 @@ if ROOT not in sys.path:
 
 WORKLOAD = "channel_128x128x65_re180_pi"
 
+# DRAM bytes of one launch of the dominant kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum), from one `ncu --set full --clock-control none`
+# capture of that kernel on the same workload and build; --traffic overrides.
+NCU_TRAFFIC = {
+    ("channel_128x128x65_re180_pi", "viscous_helmholtz"): 162.014976e6 + 46.469376e6,
+}
+
 
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -345,7 +352,9 @@ def run_ours(args) -> None:
     if dom in flops:
         ach = flops[dom] / (kernels[dom]["avg_ms"] * 1e-3) / 1e12
         roofline = {"bound": "fp64", "kernel": dom, "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-                    "frac": ach / fp64_peak, "traffic": args.traffic,
+                    "frac": ach / fp64_peak,
+                    "traffic": args.traffic if args.traffic is not None else NCU_TRAFFIC.get((args.workload, dom)),
+                    "traffic_source": "ncu capture of one launch (dram__bytes_read.sum + dram__bytes_write.sum)",
                     "peak_source": "FP64 FMA probe timed in this run (dns3d_measure_fp64_tflops); "
                                    "MEASURED_PEAKS.json has no FP64 figure",
                     "algorithmic_flops_per_launch": flops[dom]}
