@@ -160,42 +160,50 @@ def algorithmic_flops(wl: dict) -> dict:
 
 
 def cpu_sample(wl_name: str, steps: int, threads: int) -> dict:
-    """Time the CPU oracle (numpy restatement) on `steps` steps of the workload
-    in a subprocess with the given BLAS/OpenMP thread count."""
-    env = dict(os.environ)
-    for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
-        env[k] = str(threads)
+    """Time the C/OpenMP restatement of the reference step (oracle/dns3d_cpu.c:
+    physical-space transforms per plane, per-mode matrices rebuilt and
+    LU-factored every call, as DNS_pressure_BC_3D.f90 does) on `steps` steps of
+    the workload after one warm-up step, in a subprocess with `threads`
+    OpenMP threads."""
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     code = (
         "import json,sys,time; sys.path.insert(0, %r)\n"
         "from f90_dns_gb300.workloads import WORKLOADS\n"
-        "from oracle import dns3d_ref as ref\n"
+        "from oracle import cpu_ref, dns3d_ref as ref\n"
         "wl = WORKLOADS[%r]\n"
         "names = set(ref.Config.__dataclass_fields__)\n"
         "cfg = ref.Config(**{k: v for k, v in wl.items() if k in names})\n"
-        "g = ref.setup_grid(cfg); st = ref.initial_state(cfg, g)\n"
-        "ref.step(cfg, g, st)\n"
+        "c = cpu_ref.CpuChannel(cfg, threads=%d)\n"
+        "c.step(1)\n"
         "t = time.perf_counter()\n"
-        "for _ in range(%d): ref.step(cfg, g, st)\n"
+        "c.step(%d)\n"
         "dt = time.perf_counter() - t\n"
-        "print(json.dumps({'seconds': dt}))\n" % (ROOT, wl_name, steps))
+        "print(json.dumps({'seconds': dt, 'threads': c.threads}))\n" % (ROOT, wl_name, threads, steps))
     res = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
     if res.returncode != 0:
         raise RuntimeError("cpu baseline failed: " + res.stderr[-2000:])
-    sec = json.loads(res.stdout.strip().splitlines()[-1])["seconds"]
-    return {"seconds": sec, "steps": steps}
+    out = json.loads(res.stdout.strip().splitlines()[-1])
+    return {"seconds": out["seconds"], "steps": steps, "threads": out["threads"]}
+
+
+CPU_SAMPLE_TEXT = ("C/OpenMP restatement of DNS_pressure_BC_3D.f90 (oracle/dns3d_cpu.c): per-plane r2c/c2r "
+                   "round trips for every x/y derivative, per-mode Helmholtz and Poisson matrices rebuilt and "
+                   "LU-factored with partial pivoting at every call as the reference's zgesv calls are; the Fortran "
+                   "reference itself needs gfortran, FFTW3 and LAPACK, none of which exist on either machine")
 
 
 def run_reference(args) -> None:
-    """The reference arm: the CPU restatement of the reference algorithm timed
-    on this host with all its cores available to BLAS (rank 0 only)."""
+    """The reference arm: the C/OpenMP restatement of the reference algorithm
+    timed on this host with one OpenMP thread per core (rank 0 only)."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
     from f90_dns_gb300.workloads import WORKLOADS, point_count
     wl = WORKLOADS[args.workload]
     pts = point_count(wl)
     threads = os.cpu_count() or 1
-    nsteps = max(2, int(round(args.ref_sample_frac * args.steps)))
+    nsteps = max(3, int(round(args.ref_sample_frac * args.steps)))
     samp = cpu_sample(args.workload, nsteps, threads)
+    threads = samp["threads"]
     value = pts * samp["steps"] / samp["seconds"]
     line = {
         "impl": "reference", "metric": "point-steps/s", "value": value, "unit": "point-steps/s",
@@ -204,9 +212,8 @@ def run_reference(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload, "grid": [wl["nx"], wl["ny"], wl["nz"]], "precision": "fp64"},
         "cpu_baseline": {"value": value, "unit": "point-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{samp['steps']} steps of {args.workload} after 1 warm-up step: numpy FP64 "
-                                   "restatement of DNS_pressure_BC_3D.f90 (the Fortran reference needs gfortran, "
-                                   "FFTW3 and LAPACK, none of which exist here); BLAS threads = cores"},
+                         "sample": f"{samp['steps']} steps of {args.workload} after 1 warm-up step, "
+                                   f"{threads} threads: " + CPU_SAMPLE_TEXT},
         "e2e": {"value": value, "unit": "point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -393,11 +400,11 @@ def run_ours(args) -> None:
 
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
-        samp = cpu_sample(args.workload, args.cpu_steps, 1)
-        cpu = {"value": pts * samp["steps"] / samp["seconds"], "unit": "point-steps/s", "cores": 1,
+        samp = cpu_sample(args.workload, args.cpu_steps, os.cpu_count() or 1)
+        cpu = {"value": pts * samp["steps"] / samp["seconds"], "unit": "point-steps/s", "cores": samp["threads"],
                "kind": "port",
-               "sample": f"{samp['steps']} steps of {args.workload} after 1 warm-up step, numpy FP64 restatement "
-                         "(oracle/dns3d_ref.py), BLAS threads 1"}
+               "sample": f"{samp['steps']} steps of {args.workload} after 1 warm-up step, {samp['threads']} "
+                         "threads: " + CPU_SAMPLE_TEXT}
     d.close()
     if rank == 0:
         line = {
@@ -425,9 +432,9 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--profile-steps", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--cpu-steps", type=int, default=3)
-    ap.add_argument("--ref-sample-frac", type=float, default=0.01,
-                    help="reference arm: CPU steps timed per requested step (bounded sample, >= 2)")
+    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--ref-sample-frac", type=float, default=0.1,
+                    help="reference arm: CPU steps timed per requested step (bounded sample, >= 3)")
     ap.add_argument("--no-mixed", dest="mixed", action="store_false",
                     help="skip the mixed-precision measurement")
     ap.add_argument("--mixed-err-steps", type=int, default=200)
