@@ -25,7 +25,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
           "-I", os.path.join(ROOT, "include")]
 
 SOURCES = ["capi.cu", "fft.cu", "step.cu", "setup.cu", "host.cpp", "noalloc.cu", "server.cpp", "restart.cpp",
-           "output.cpp"]
+           "output.cpp", "fft_ct.cu"]
 
 
 def _nvcc() -> str:

@@ -46,6 +46,10 @@ struct FftPlan1D {
 FftPlan1D make_plan(int n);
 bool fft_length_supported(int n);
 
+template <typename T> struct Cx;
+template <> struct Cx<double> { using type = double2; };
+template <> struct Cx<float> { using type = float2; };
+
 // Grid constants passed by value to kernels.
 struct GridDev {
     int nx, ny, nz, nxh, nxhp, nm;
@@ -77,10 +81,24 @@ struct FftCtx {
     double2* tmp;        // spectral scratch for nf fields
     float2* tmp32 = nullptr;  // FP32 spectral scratch (mixed path)
     int tmp_fields;
+    bool use_ct = false;  // the grid's lengths have compile-time kernels (fft_ct.cu)
     // optional per-launch hook (profiling): called after each kernel launch
     void (*hook)(void*, const char*) = nullptr;
     void* hook_ctx = nullptr;
 };
+// Compile-time-length plane transforms (fft_ct.cu) for ny in {16..512} and
+// nx/2 in {16..256} of the form 2^a 3^b; fft_ct_supported tells which grids.
+bool fft_ct_supported(int ny, int nxh);
+template <int SIGN, typename C>
+cudaError_t fft_ct_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int nf, const C* tw,
+                     cudaStream_t s);
+template <typename T>
+cudaError_t fft_ct_c2r_x(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst, const GridDev& g, int nrows, int nf,
+                         const typename Cx<T>::type* tw_n, const typename Cx<T>::type* tw_nx, cudaStream_t s);
+template <typename T>
+cudaError_t fft_ct_r2c_x(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, const GridDev& g, int nrows, int nf,
+                         const typename Cx<T>::type* tw_n, const typename Cx<T>::type* tw_nx, cudaStream_t s);
+
 cudaError_t fft_setup(FftCtx& ctx, const GridDev& g);
 void fft_release(FftCtx& ctx);
 // spec[f] (spectral, read only) -> phys[f]; uses ctx.tmp (nf <= tmp_fields).

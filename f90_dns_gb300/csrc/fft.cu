@@ -43,9 +43,6 @@ FftPlan1D make_plan(int n) {
 
 namespace {
 
-template <typename T> struct Cx;
-template <> struct Cx<double> { using type = double2; };
-template <> struct Cx<float> { using type = float2; };
 template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype(C::x) b) { C r; r.x = a; r.y = b; return r; }
 
 template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
@@ -298,6 +295,7 @@ cudaError_t smem_attr(K k, int bytes) {
 cudaError_t fft_setup(FftCtx& ctx, const GridDev& g) {
     ctx.py = make_plan(g.ny);
     ctx.px2 = make_plan(g.nxh);
+    ctx.use_ct = fft_ct_supported(g.ny, g.nxh);
     ctx.tw_ny = upload_table<double2>(g.ny, g.ny);
     ctx.tw_nx2 = upload_table<double2>(g.nxh, g.nxh);
     ctx.tw_nx = upload_table<double2>(g.nx, g.nxh + 1);
@@ -338,12 +336,20 @@ cudaError_t c2r_impl(const FftCtx& ctx, const GridDev& g, FieldsT<typename Cx<T>
                      const typename Cx<T>::type* twy, const typename Cx<T>::type* twx2,
                      const typename Cx<T>::type* twx) {
     using C = typename Cx<T>::type;
+    const int nrows = nplanes * g.ny;
+    if (ctx.use_ct) {
+        cudaError_t e = fft_ct_y<+1, C>(spec, tmp, g, nplanes, nf, twy, s);
+        if (e) return e;
+        if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_inverse" : "fft32_y_inverse");
+        e = fft_ct_c2r_x<T>(tmp, phys, g, nrows, nf, twx2, twx, s);
+        if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_x_c2r" : "fft32_x_c2r");
+        return e;
+    }
     const int cx = pick_cx(g.ny);
     dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
     k_fft_y<+1, C><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(C), s>>>(spec, tmp, g, ctx.py, twy, cx);
     if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_inverse" : "fft32_y_inverse");
     const int rx = pick_rx(g.nxh);
-    const int nrows = nplanes * g.ny;
     dim3 gx((nrows + rx - 1) / rx, nf);
     k_c2r_x<T><<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(C), s>>>(tmp, phys, g, ctx.px2, twx2, twx, rx, nrows);
     if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_x_c2r" : "fft32_x_c2r");
@@ -355,8 +361,16 @@ cudaError_t r2c_impl(const FftCtx& ctx, const GridDev& g, FieldsT<T> phys, Field
                      int nf, int nplanes, cudaStream_t s, const typename Cx<T>::type* twy,
                      const typename Cx<T>::type* twx2, const typename Cx<T>::type* twx) {
     using C = typename Cx<T>::type;
-    const int rx = pick_rx(g.nxh);
     const int nrows = nplanes * g.ny;
+    if (ctx.use_ct) {
+        cudaError_t e = fft_ct_r2c_x<T>(phys, spec, g, nrows, nf, twx2, twx, s);
+        if (e) return e;
+        if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_x_r2c" : "fft32_x_r2c");
+        e = fft_ct_y<-1, C>(spec, spec, g, nplanes, nf, twy, s);
+        if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_forward" : "fft32_y_forward");
+        return e;
+    }
+    const int rx = pick_rx(g.nxh);
     dim3 gx((nrows + rx - 1) / rx, nf);
     k_r2c_x<T><<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(C), s>>>(phys, spec, g, ctx.px2, twx2, twx, rx, nrows);
     if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_x_r2c" : "fft32_x_r2c");

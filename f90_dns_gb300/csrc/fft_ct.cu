@@ -1,0 +1,365 @@
+// Plane transforms with the transform length fixed at compile time: the same
+// transforms as fft.cu (FFTW's r2c / non-Hermitian c2r conventions), for the
+// lengths that the supported grids use, with
+//  - the radix schedule, the per-pass index arithmetic and the loop trip
+//    counts resolved by the compiler (no runtime division in the passes);
+//  - radix-8 butterflies in registers (a length-128 transform is 3 passes
+//    instead of 4, length 512 is 3 instead of 5);
+//  - one shared-memory buffer per CTA: each pass reads all of a thread's
+//    butterfly inputs into registers, synchronises, and writes the outputs
+//    in place, so a CTA holds ~2048 complex values in 16-33 KB (no opt-in);
+//  - the y pass over a flattened (plane, kx) column index, so grids whose
+//    nx/2+1 columns do not fill a CTA waste no lanes.
+// Lengths outside the instantiated set use the generic kernels of fft.cu.
+#include "dns3d_internal.cuh"
+
+namespace dns3d {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype(C::x) b) { C r; r.x = a; r.y = b; return r; }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// (SIGN i) a
+template <int SIGN, typename C> __device__ __forceinline__ C mul_si(C a) {
+    return SIGN > 0 ? mk<C>(-a.y, a.x) : mk<C>(a.y, -a.x);
+}
+
+// Register DFTs, natural-order output, w = e^{SIGN 2 pi i / R}.
+template <int SIGN, typename C> __device__ __forceinline__ void dft2(C* v) {
+    const C a = v[0];
+    v[0] = cadd(a, v[1]);
+    v[1] = csub(a, v[1]);
+}
+
+template <int SIGN, typename C> __device__ __forceinline__ void dft4(C* v) {
+    const C s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    const C s13 = cadd(v[1], v[3]), d13 = mul_si<SIGN>(csub(v[1], v[3]));
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    v[1] = cadd(d02, d13);
+    v[3] = csub(d02, d13);
+}
+
+// y[q] = E[q] + w8^q O[q], y[q+4] = E[q] - w8^q O[q] (E, O: 4-point DFTs of
+// the even and odd inputs); w8 = (1 + SIGN i)/sqrt2, w8^2 = SIGN i,
+// w8^3 = (-1 + SIGN i)/sqrt2.
+template <int SIGN, typename C> __device__ __forceinline__ void dft8(C* v) {
+    using R = decltype(C::x);
+    C e[4] = {v[0], v[2], v[4], v[6]};
+    C o[4] = {v[1], v[3], v[5], v[7]};
+    dft4<SIGN>(e);
+    dft4<SIGN>(o);
+    const R h = (R)0.70710678118654752440;
+    const R s = (R)SIGN;
+    const C t1 = mk<C>(h * (o[1].x - s * o[1].y), h * (o[1].y + s * o[1].x));
+    const C t2 = mul_si<SIGN>(o[2]);
+    const C t3 = mk<C>(h * (-o[3].x - s * o[3].y), h * (-o[3].y + s * o[3].x));
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], t1);
+    v[5] = csub(e[1], t1);
+    v[2] = cadd(e[2], t2);
+    v[6] = csub(e[2], t2);
+    v[3] = cadd(e[3], t3);
+    v[7] = csub(e[3], t3);
+}
+
+template <int SIGN, typename C> __device__ __forceinline__ void dft3(C* v) {
+    using R = decltype(C::x);
+    const R h = (R)0.86602540378443864676;  // sqrt(3)/2
+    const C t1 = cadd(v[1], v[2]);
+    const C d = csub(v[1], v[2]);
+    const C m = mk<C>(v[0].x - (R)0.5 * t1.x, v[0].y - (R)0.5 * t1.y);
+    const C id = SIGN > 0 ? mk<C>(-h * d.y, h * d.x) : mk<C>(h * d.y, -h * d.x);
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(m, id);
+    v[2] = csub(m, id);
+}
+
+template <int R, int SIGN, typename C> __device__ __forceinline__ void dft(C* v) {
+    if constexpr (R == 8) dft8<SIGN>(v);
+    else if constexpr (R == 4) dft4<SIGN>(v);
+    else if constexpr (R == 2) dft2<SIGN>(v);
+    else dft3<SIGN>(v);
+}
+
+__host__ __device__ constexpr int next_radix(int m) { return m % 8 == 0 ? 8 : (m % 4 == 0 ? 4 : (m % 2 == 0 ? 2 : 3)); }
+
+// Transforms per CTA: a power of two near 2048 / N, in [1, 64].
+__host__ __device__ constexpr int per_cta(int n) {
+    int c = 1;
+    while (c * 2 * n <= 2048 && c < 64) c *= 2;
+    return c;
+}
+
+// One Stockham pass (radix R, Ns finished sub-length) over CNT transforms of
+// length N stored at buf[c*LD + t], in place: all inputs of the thread's
+// butterflies are read into registers before a barrier, then written.
+// tw[t] = e^{-2 pi i t / N}.
+template <int N, int R, int NS, int SIGN, int CNT, int LD, typename C>
+__device__ __forceinline__ void ct_pass(C* buf, const C* __restrict__ tw) {
+    constexpr int NB = N / R;
+    constexpr int TSTEP = N / (NS * R);
+    constexpr int TOTAL = CNT * NB;
+    constexpr int PER = (TOTAL + kThreads - 1) / kThreads;
+    C v[PER][R];
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+        const int t = threadIdx.x + p * kThreads;
+        if (TOTAL % kThreads == 0 || t < TOTAL) {
+            const int c = t / NB, j = t - c * NB;
+            const C* src = buf + c * LD;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[p][r] = src[j + r * NB];
+            if constexpr (NS > 1) {
+                const int k = j % NS;
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    C w = __ldg(&tw[r * k * TSTEP]);
+                    if (SIGN > 0) w.y = -w.y;
+                    v[p][r] = cmul(v[p][r], w);
+                }
+            }
+            dft<R, SIGN>(v[p]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+        const int t = threadIdx.x + p * kThreads;
+        if (TOTAL % kThreads == 0 || t < TOTAL) {
+            const int c = t / NB, j = t - c * NB;
+            const int k = j % NS;
+            C* dst = buf + c * LD + (j / NS) * NS * R + k;
+#pragma unroll
+            for (int q = 0; q < R; ++q) dst[q * NS] = v[p][q];
+        }
+    }
+    __syncthreads();
+}
+
+template <int N, int NS, int SIGN, int CNT, int LD, typename C>
+__device__ __forceinline__ void ct_fft(C* buf, const C* __restrict__ tw) {
+    if constexpr (NS < N) {
+        constexpr int R = next_radix(N / NS);
+        ct_pass<N, R, NS, SIGN, CNT, LD>(buf, tw);
+        ct_fft<N, NS * R, SIGN, CNT, LD>(buf, tw);
+    }
+}
+
+// y pass: complex transforms of length N = ny along every (plane, kx) column;
+// CX columns per CTA taken from the flattened index plane * nxhp + kx.
+// grid (ceil(nplanes * nxhp / CX), 1, nf).
+template <int N, int SIGN, typename C>
+__global__ void __launch_bounds__(kThreads) k_fft_y_ct(FieldsT<C> src, FieldsT<C> dst, GridDev g, int nplanes,
+                                                       const C* __restrict__ tw) {
+    constexpr int CX = per_cta(N);
+    constexpr int LD = N + 1;
+    __shared__ C buf[CX * LD];
+    const long long ncols = (long long)nplanes * g.nxhp;
+    const long long vc = (long long)blockIdx.x * CX + (threadIdx.x % CX);
+    const bool live = vc < ncols;
+    size_t base = 0;
+    if (live) {
+        const int p = (int)(vc / g.nxhp);
+        const int kx = (int)(vc - (long long)p * g.nxhp);
+        base = (size_t)p * g.nm + kx;
+    }
+    const C* __restrict__ s = src.p[blockIdx.z];
+    C* d = dst.p[blockIdx.z];
+    constexpr int ROWS_PER_ITER = kThreads / CX;  // CX divides kThreads
+    const int c = threadIdx.x % CX;
+#pragma unroll 4
+    for (int y = threadIdx.x / CX; y < N; y += ROWS_PER_ITER)
+        buf[c * LD + y] = live ? s[base + (size_t)y * g.nxhp] : mk<C>(0, 0);
+    __syncthreads();
+    ct_fft<N, 1, SIGN, CX, LD>(buf, tw);
+    if (live) {
+#pragma unroll 4
+        for (int y = threadIdx.x / CX; y < N; y += ROWS_PER_ITER) d[base + (size_t)y * g.nxhp] = buf[c * LD + y];
+    }
+}
+
+// c2r along x, N = nx/2: RX rows per CTA (row = plane * ny + y).  Packs the
+// nx/2+1 inputs of a row (Re only at kx = 0, nx/2) into Z[k] =
+// (X[k] + conj(X[N-k])) + i e^{+2 pi i k/nx} (X[k] - conj(X[N-k])), runs the
+// inverse length-N transform and writes z[m] = (x[2m], x[2m+1]) / (nx ny).
+template <int N, typename T>
+__global__ void __launch_bounds__(kThreads) k_c2r_x_ct(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst,
+                                                       GridDev g, int nrows,
+                                                       const typename Cx<T>::type* __restrict__ tw_n,
+                                                       const typename Cx<T>::type* __restrict__ tw_nx) {
+    using C = typename Cx<T>::type;
+    constexpr int RX = per_cta(N);
+    constexpr int LD = N + 1;
+    __shared__ C buf[RX * LD];
+    const int row0 = blockIdx.x * RX;
+    const C* __restrict__ s = src.p[blockIdx.y];
+    C* d = reinterpret_cast<C*>(dst.p[blockIdx.y]);
+    const int nxhp = N + 1;
+    for (int t = threadIdx.x; t < RX * N; t += kThreads) {
+        const int r = t / N, k = t - r * N;
+        C z = mk<C>(0, 0);
+        if (row0 + r < nrows) {
+            const C* row = s + (size_t)(row0 + r) * nxhp;
+            C xa = row[k];
+            C xb = row[N - k];
+            if (k == 0) {
+                xa.y = 0;
+                xb.y = 0;
+            }
+            const C sm = mk<C>(xa.x + xb.x, xa.y - xb.y);
+            const C df = mk<C>(xa.x - xb.x, xa.y + xb.y);
+            C w = __ldg(&tw_nx[k]);
+            w.y = -w.y;
+            const C p = cmul(w, df);
+            z = mk<C>(sm.x - p.y, sm.y + p.x);
+        }
+        buf[r * LD + k] = z;
+    }
+    __syncthreads();
+    ct_fft<N, 1, +1, RX, LD>(buf, tw_n);
+    const T sc = (T)g.inv_nxny;
+    for (int t = threadIdx.x; t < RX * N; t += kThreads) {
+        const int r = t / N, k = t - r * N;
+        if (row0 + r < nrows) {
+            const C z = buf[r * LD + k];
+            d[(size_t)(row0 + r) * N + k] = mk<C>(z.x * sc, z.y * sc);
+        }
+    }
+}
+
+// r2c along x, N = nx/2: z[m] = x[2m] + i x[2m+1], forward length-N
+// transform, X[k] = E + e^{-2 pi i k/nx} O with E = (Z[k] + conj(Z[N-k]))/2,
+// O = (Z[k] - conj(Z[N-k]))/(2i), k = 0..N.
+template <int N, typename T>
+__global__ void __launch_bounds__(kThreads) k_r2c_x_ct(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst,
+                                                       GridDev g, int nrows,
+                                                       const typename Cx<T>::type* __restrict__ tw_n,
+                                                       const typename Cx<T>::type* __restrict__ tw_nx) {
+    using C = typename Cx<T>::type;
+    constexpr int RX = per_cta(N);
+    constexpr int LD = N + 1;
+    __shared__ C buf[RX * LD];
+    const int row0 = blockIdx.x * RX;
+    const C* __restrict__ s = reinterpret_cast<const C*>(src.p[blockIdx.y]);
+    C* d = dst.p[blockIdx.y];
+    for (int t = threadIdx.x; t < RX * N; t += kThreads) {
+        const int r = t / N, k = t - r * N;
+        buf[r * LD + k] = (row0 + r < nrows) ? s[(size_t)(row0 + r) * N + k] : mk<C>(0, 0);
+    }
+    __syncthreads();
+    ct_fft<N, 1, -1, RX, LD>(buf, tw_n);
+    for (int t = threadIdx.x; t < RX * (N + 1); t += kThreads) {
+        const int r = t / (N + 1), k = t - r * (N + 1);
+        if (row0 + r < nrows) {
+            const C za = buf[r * LD + (k == N ? 0 : k)];
+            const C zb = buf[r * LD + (k == 0 ? 0 : N - k)];
+            const T hf = (T)0.5;
+            const C e = mk<C>(hf * (za.x + zb.x), hf * (za.y - zb.y));
+            const C o = mk<C>(hf * (za.y + zb.y), -hf * (za.x - zb.x));
+            const C p = cmul(__ldg(&tw_nx[k]), o);
+            d[(size_t)(row0 + r) * (N + 1) + k] = mk<C>(e.x + p.x, e.y + p.y);
+        }
+    }
+}
+
+template <int SIGN, typename C, int N>
+void launch_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int nf, const C* tw, cudaStream_t s) {
+    constexpr int CX = per_cta(N);
+    const long long ncols = (long long)nplanes * g.nxhp;
+    dim3 grid((unsigned)((ncols + CX - 1) / CX), 1, nf);
+    k_fft_y_ct<N, SIGN, C><<<grid, kThreads, 0, s>>>(src, dst, g, nplanes, tw);
+}
+
+template <typename T, int N>
+void launch_c2r(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst, const GridDev& g, int nrows, int nf,
+                const typename Cx<T>::type* tw_n, const typename Cx<T>::type* tw_nx, cudaStream_t s) {
+    constexpr int RX = per_cta(N);
+    dim3 grid((nrows + RX - 1) / RX, nf);
+    k_c2r_x_ct<N, T><<<grid, kThreads, 0, s>>>(src, dst, g, nrows, tw_n, tw_nx);
+}
+
+template <typename T, int N>
+void launch_r2c(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, const GridDev& g, int nrows, int nf,
+                const typename Cx<T>::type* tw_n, const typename Cx<T>::type* tw_nx, cudaStream_t s) {
+    constexpr int RX = per_cta(N);
+    dim3 grid((nrows + RX - 1) / RX, nf);
+    k_r2c_x_ct<N, T><<<grid, kThreads, 0, s>>>(src, dst, g, nrows, tw_n, tw_nx);
+}
+
+}  // namespace
+
+// Instantiated lengths: ny in {16..512}, nx/2 in {16..256}, 2^a 3^b.
+#define DNS3D_CT_Y_LENGTHS(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
+#define DNS3D_CT_X_LENGTHS(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256)
+
+bool fft_ct_supported(int ny, int nxh) {
+    bool y = false, x = false;
+#define Y_CASE(n) y = y || ny == n;
+#define X_CASE(n) x = x || nxh == n;
+    DNS3D_CT_Y_LENGTHS(Y_CASE)
+    DNS3D_CT_X_LENGTHS(X_CASE)
+#undef Y_CASE
+#undef X_CASE
+    return y && x;
+}
+
+template <int SIGN, typename C>
+cudaError_t fft_ct_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int nf, const C* tw,
+                     cudaStream_t s) {
+    switch (g.ny) {
+#define Y_CASE(n) \
+    case n: launch_y<SIGN, C, n>(src, dst, g, nplanes, nf, tw, s); break;
+        DNS3D_CT_Y_LENGTHS(Y_CASE)
+#undef Y_CASE
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t fft_ct_c2r_x(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst, const GridDev& g, int nrows, int nf,
+                         const typename Cx<T>::type* tw_n, const typename Cx<T>::type* tw_nx, cudaStream_t s) {
+    switch (g.nxh) {
+#define X_CASE(n) \
+    case n: launch_c2r<T, n>(src, dst, g, nrows, nf, tw_n, tw_nx, s); break;
+        DNS3D_CT_X_LENGTHS(X_CASE)
+#undef X_CASE
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t fft_ct_r2c_x(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, const GridDev& g, int nrows, int nf,
+                         const typename Cx<T>::type* tw_n, const typename Cx<T>::type* tw_nx, cudaStream_t s) {
+    switch (g.nxh) {
+#define X_CASE(n) \
+    case n: launch_r2c<T, n>(src, dst, g, nrows, nf, tw_n, tw_nx, s); break;
+        DNS3D_CT_X_LENGTHS(X_CASE)
+#undef X_CASE
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template cudaError_t fft_ct_y<-1, double2>(Fields, Fields, const GridDev&, int, int, const double2*, cudaStream_t);
+template cudaError_t fft_ct_y<+1, double2>(Fields, Fields, const GridDev&, int, int, const double2*, cudaStream_t);
+template cudaError_t fft_ct_y<-1, float2>(FFields, FFields, const GridDev&, int, int, const float2*, cudaStream_t);
+template cudaError_t fft_ct_y<+1, float2>(FFields, FFields, const GridDev&, int, int, const float2*, cudaStream_t);
+template cudaError_t fft_ct_c2r_x<double>(Fields, RFields, const GridDev&, int, int, const double2*, const double2*,
+                                          cudaStream_t);
+template cudaError_t fft_ct_c2r_x<float>(FFields, FRFields, const GridDev&, int, int, const float2*, const float2*,
+                                         cudaStream_t);
+template cudaError_t fft_ct_r2c_x<double>(RFields, Fields, const GridDev&, int, int, const double2*, const double2*,
+                                          cudaStream_t);
+template cudaError_t fft_ct_r2c_x<float>(FRFields, FFields, const GridDev&, int, int, const float2*, const float2*,
+                                         cudaStream_t);
+
+}  // namespace dns3d
