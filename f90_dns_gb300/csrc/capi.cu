@@ -57,6 +57,10 @@ struct dns3d_handle {
     std::vector<const char*> evname;
     size_t nev = 0;
     int launches = 0;  // kernel launches of the last step body
+    // Bit f set: phys[f] holds the physical field f (u, v, w, p_total) of the
+    // current state, left by get_state or diagnostics.  Everything that changes
+    // the state or reuses phys[] as scratch clears it.
+    unsigned phys_valid = 0;
 };
 
 namespace {
@@ -245,6 +249,7 @@ int run_source_terms_mixed(dns3d_handle* h) {
 int run_source_terms_fp64(dns3d_handle* h);
 
 int run_source_terms(dns3d_handle* h) {
+    h->phys_valid = 0;
     const GridDev& g = h->g;
     // the PI update reads only the mean mode of u and writes only the
     // controller state, which the viscous step reads: it runs beside the
@@ -280,6 +285,7 @@ int run_source_terms_fp64(dns3d_handle* h) {
 }
 
 int run_viscous(dns3d_handle* h) {
+    h->phys_valid = 0;
     if (h->mixed) {
         Fields F{}, O{};
         FFields S{};
@@ -305,6 +311,7 @@ int run_viscous(dns3d_handle* h) {
 }
 
 int run_pressure(dns3d_handle* h) {
+    h->phys_valid = 0;
     if (h->mixed) {
         CK(h, fork_side(h, 2));
         CK(h, launch_pressure_mean_mode(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, side_stream(h)));
@@ -320,6 +327,7 @@ int run_pressure(dns3d_handle* h) {
 }
 
 int run_correction(dns3d_handle* h) {
+    h->phys_valid = 0;
     if (h->mixed) {
         CK(h, launch_correction_mixed(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->U, h->V, h->W,
                                       h->P, h->GP, h->stream));
@@ -333,6 +341,7 @@ int run_correction(dns3d_handle* h) {
 }
 
 int run_bc(dns3d_handle* h) {
+    h->phys_valid = 0;
     CK(h, launch_apply_bc(h->g, h->U, h->V, h->W, h->stream));
     mark(h, "apply_bc");
     return DNS3D_OK;
@@ -752,13 +761,19 @@ int dns3d_set_state(dns3d_handle* h, const double* u, const double* v, const dou
     const double* src[4] = {u, v, w, p_total};
     double2* dst[4] = {h->U, h->V, h->W, h->P};
     int rc;
+    h->phys_valid = 0;
+    // all uploads, then one batched forward transform of the given fields
+    RFields ph{};
+    Fields sp{};
+    int nf = 0;
     for (int f = 0; f < 4; ++f) {
         if (!src[f]) continue;
         if ((rc = upload(h, h->phys[f], src[f], pe * sizeof(double)))) return rc;
-        RFields ph{}; ph.p[0] = h->phys[f];
-        Fields sp{}; sp.p[0] = dst[f];
-        CK(h, fft_r2c(h->fft, g, ph, sp, 1, g.nz, h->stream));
+        ph.p[nf] = h->phys[f];
+        sp.p[nf] = dst[f];
+        ++nf;
     }
+    if (nf) CK(h, fft_r2c(h->fft, g, ph, sp, nf, g.nz, h->stream));
     const double* gps[4] = {gpx_w1, gpx_w2, gpy_w1, gpy_w2};
     const bool any_gp = gpx_w1 || gpx_w2 || gpy_w1 || gpy_w2;
     const size_t pl = (size_t)g.nx * g.ny;
@@ -789,20 +804,30 @@ int dns3d_get_state(dns3d_handle* h, double* u, double* v, double* w, double* p_
     const size_t pe = phys_elems(h->cfg);
     double* dst[4] = {u, v, w, p_total};
     double2* src[4] = {h->U, h->V, h->W, h->P};
+    // one batched inverse transform of the requested fields not already in
+    // phys[], then the copies
+    Fields sp{};
+    RFields ph{};
+    int nf = 0;
+    for (int f = 0; f < 4; ++f) {
+        if (!dst[f] || (h->phys_valid >> f & 1u)) continue;
+        sp.p[nf] = src[f];
+        ph.p[nf] = h->phys[f];
+        ++nf;
+    }
+    if (nf) CK(h, fft_c2r(h->fft, g, sp, ph, nf, g.nz, h->stream));
     for (int f = 0; f < 4; ++f) {
         if (!dst[f]) continue;
-        Fields sp{}; sp.p[0] = src[f];
-        RFields ph{}; ph.p[0] = h->phys[f];
-        CK(h, fft_c2r(h->fft, g, sp, ph, 1, g.nz, h->stream));
+        h->phys_valid |= 1u << f;
         CK(h, cudaMemcpyAsync(dst[f], h->phys[f], pe * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     }
     double* gps[4] = {gpx_w1, gpx_w2, gpy_w1, gpy_w2};
     const size_t pl = (size_t)g.nx * g.ny;
     for (int i = 0; i < 4; ++i) {
         if (!gps[i]) continue;
-        Fields sp{}; sp.p[0] = h->GP + (size_t)i * g.nm;
-        RFields ph{}; ph.p[0] = h->phys[4];
-        CK(h, fft_c2r(h->fft, g, sp, ph, 1, 1, h->stream));
+        Fields gsp{}; gsp.p[0] = h->GP + (size_t)i * g.nm;
+        RFields gph{}; gph.p[0] = h->phys[4];
+        CK(h, fft_c2r(h->fft, g, gsp, gph, 1, 1, h->stream));
         CK(h, cudaMemcpyAsync(gps[i], h->phys[4], pl * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         CK(h, cudaStreamSynchronize(h->stream));
     }
@@ -871,6 +896,7 @@ int dns3d_step(dns3d_handle* h, int nsteps) {
             return cuda_fail(h, e, "cudaGraphInstantiate");
         }
     }
+    h->phys_valid = 0;
     for (int s = 0; s < nsteps; ++s) {
         CK(h, cudaGraphLaunch(h->graph, h->stream));
         h->step += 1;
@@ -965,11 +991,19 @@ int diag_core(dns3d_handle* h, dns3d_diag* out, bool with_div, std::vector<doubl
     CK(h, cudaSetDevice(h->cfg.device));
     const GridDev& g = h->g;
     const dns3d_config& c = h->cfg;
+    // the physical u, v, w: reuse what get_state left in phys[], transform the rest
+    const double2* spec[3] = {h->U, h->V, h->W};
     Fields sp{};
-    sp.p[0] = h->U; sp.p[1] = h->V; sp.p[2] = h->W;
     RFields ph{};
-    for (int f = 0; f < 3; ++f) ph.p[f] = h->phys[f];
-    CK(h, fft_c2r(h->fft, g, sp, ph, 3, g.nz, h->stream));
+    int nf = 0;
+    for (int f = 0; f < 3; ++f) {
+        if (h->phys_valid >> f & 1u) continue;
+        sp.p[nf] = const_cast<double2*>(spec[f]);
+        ph.p[nf] = h->phys[f];
+        ++nf;
+    }
+    if (nf) CK(h, fft_c2r(h->fft, g, sp, ph, nf, g.nz, h->stream));
+    h->phys_valid |= 7u;
     CK(h, launch_diag_reduce(g, h->ops, h->phys[0], h->phys[1], h->phys[2], h->d_red, h->red_blocks, h->d_out,
                              h->stream));
     if (with_div) {
@@ -980,6 +1014,7 @@ int diag_core(dns3d_handle* h, dns3d_diag* out, bool with_div, std::vector<doubl
         CK(h, launch_divergence(g, h->ops, h->U, h->V, h->W, div, h->stream));
         Fields dv{}; dv.p[0] = div;
         RFields dp{}; dp.p[0] = h->phys[3];
+        h->phys_valid &= ~8u;  // phys[3] now holds the divergence
         CK(h, fft_c2r(h->fft, g, dv, dp, 1, g.nz, h->stream));
         CK(h, launch_maxabs(g, h->phys[3], phys_elems(c), h->d_red, h->red_blocks, h->d_out + 4, h->stream));
     }
@@ -1215,6 +1250,7 @@ int dns3d_ensemble_step(dns3d_ensemble* e, int nsteps) {
         for (auto* h : e->runs) {
             h->step += 1;
             h->time += h->cfg.dt;
+            h->phys_valid = 0;
         }
     }
     CK(h0, cudaStreamSynchronize(e->origin));
@@ -1237,6 +1273,7 @@ int dns3d_ensemble_step_timed(dns3d_ensemble* e, int nsteps, double* elapsed_ms)
         for (auto* h : e->runs) {
             h->step += 1;
             h->time += h->cfg.dt;
+            h->phys_valid = 0;
         }
     }
     CK(h0, cudaEventRecord(b, e->origin));

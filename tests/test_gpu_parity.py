@@ -194,3 +194,33 @@ def test_restart_save_load_continue(built_lib, tmp_path):
         ref.step(cfg, g, st)
     err = velocity_errors(gst, st)
     assert max(err["u"], err["v"], err["w"]) <= TOL, err
+
+
+def test_cached_physical_fields_stay_coherent(built_lib):
+    """get_state and diagnostics share the physical fields they transform;
+    every state change (graph steps, stage calls, set_state) must drop them."""
+    wl = dict(C1, nx=32, ny=24, nz=17)
+    with ChannelDNS(config_from(wl)) as d, ChannelDNS(config_from(wl)) as e:
+        d.step(3)
+        a = d.diagnostics()
+        s1 = d.get_state()
+        assert d.diagnostics() == a
+        d.step(2)
+        d.compute_source_terms_3d()
+        d.viscous_step_3d()
+        d.solve_pressure_3d()
+        d.pressure_correction_3d()
+        d.apply_boundary_conditions_3d()
+        c = d.diagnostics()
+        s2 = d.get_state()
+        e.step(6)
+        se = e.get_state()
+        for k in ("u", "v", "w", "p_total"):
+            np.testing.assert_array_equal(s2[k], se[k])
+        ce = e.diagnostics()
+        for k in ("umax", "vmax", "wmax", "energy", "max_div"):
+            assert getattr(c, k) == getattr(ce, k), k
+        d.set_state(u=s1["u"], v=s1["v"], w=s1["w"], p_total=s1["p_total"])
+        b = d.diagnostics()
+        for k in ("umax", "vmax", "wmax", "energy"):
+            assert abs(getattr(b, k) - getattr(a, k)) <= 1e-13 * abs(getattr(a, k)), k
