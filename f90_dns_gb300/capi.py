@@ -80,6 +80,7 @@ class CConfig(C.Structure):
         ("lgl_dmatrix_guard", C.c_int),
         ("precision", C.c_int),
         ("device", C.c_int),
+        ("perturbation_seed", C.c_longlong),
     ]
 
 

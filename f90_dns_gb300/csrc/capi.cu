@@ -107,7 +107,6 @@ int validate(const dns3d_config* c) {
         if (!(c->target_bulk_velocity > 0.0) || !(c->controller_gain > 0.0) || c->controller_update_freq <= 0)
             return DNS3D_E_INVALID;
     }
-    if (c->enable_perturbations && !c->use_analytical_perturbations) return DNS3D_E_UNSUPPORTED;
     if (c->precision != DNS3D_PREC_FP64 && c->precision != DNS3D_PREC_MIXED) return DNS3D_E_UNSUPPORTED;
     return DNS3D_OK;
 }
@@ -123,7 +122,7 @@ void initial_fields(const dns3d_config& c, const std::vector<double>& z, std::ve
     w.assign(pl * nz, 0.0);
     for (int k = 0; k < nz; ++k)
         for (size_t i = 0; i < pl; ++i) u[k * pl + i] = c.u_centerline * (1.0 - z[k] * z[k]);
-    if (!c.enable_perturbations) return;
+    if (!c.enable_perturbations || !c.use_analytical_perturbations) return;
     const double kx = 2.0 * kPi * (double)c.analytical_mode_x / c.xlen;
     const double ky = 2.0 * kPi * (double)c.analytical_mode_y / c.ylen;
     std::vector<double> up(pl * nz), vp(pl * nz);
@@ -152,6 +151,46 @@ void initial_fields(const dns3d_config& c, const std::vector<double>& z, std::ve
     for (size_t o = 0; o < pl * nz; ++o) { u[o] += up[o]; v[o] += vp[o]; }
     for (int k : {0, nz - 1})  // enforce_wall_boundaries + apply_boundary_conditions_3d (3D:3253)
         for (size_t i = 0; i < pl; ++i) { u[k * pl + i] = 0.0; v[k * pl + i] = 0.0; w[k * pl + i] = 0.0; }
+}
+
+// SplitMix64 (Steele, Lea and Flood, OOPSLA 2014; the finaliser constants
+// of Stafford's Mix13): output i is mix(seed + (i+1) * 0x9E3779B97F4A7C15);
+// a uniform double in [0, 1) takes its top 53 bits.
+struct SplitMix64 {
+    uint64_t s;
+    double uniform() {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * 0x1.0p-53;
+    }
+};
+
+// integrate_with_boundary_conditions_fallback (perturbation_module.f90:
+// 470-517): trapezoid integral of -div upward from w(-1) = 0, a quadratic
+// correction that brings w(+1) to zero, and sin^2 tapers on the three
+// levels next to each wall (with the reference's 3.14159).
+void integrate_w_column(int nz, const double* z, const double* div, double* w) {
+    std::vector<double> up(nz);
+    up[0] = 0.0;
+    for (int k = 1; k < nz; ++k) up[k] = up[k - 1] - 0.5 * (div[k] + div[k - 1]) * (z[k] - z[k - 1]);
+    const double total = up[nz - 1];
+    for (int k = 0; k < nz; ++k) {
+        const double zn = (z[k] - z[0]) / (z[nz - 1] - z[0]);
+        w[k] = up[k] - total * (zn * (2.0 - zn));
+    }
+    w[0] = 0.0;
+    w[nz - 1] = 0.0;
+    for (int k = 2; k <= std::min(4, nz - 1); ++k) {  // Fortran levels
+        const double s = std::sin(0.5 * 3.14159 * (double)(k - 1) / 3.0);
+        w[k - 1] *= s * s;
+    }
+    for (int k = std::max(nz - 3, 2); k <= nz - 1; ++k) {
+        const double s = std::sin(0.5 * 3.14159 * (double)(nz - k) / 3.0);
+        w[k - 1] *= s * s;
+    }
 }
 
 void mark(dns3d_handle* h, const char* name) {
@@ -403,6 +442,7 @@ int dns3d_config_defaults(dns3d_config* c) {
     c->lgl_dmatrix_guard = 1;
     c->precision = DNS3D_PREC_FP64;
     c->device = 0;
+    c->perturbation_seed = 0;
     return DNS3D_OK;
 }
 
@@ -733,10 +773,126 @@ int dns3d_destroy(dns3d_handle* h) {
     return DNS3D_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// generate_channel_solenoidal_perturbations (perturbation_module.f90:42-176)
+// with a seeded stream in place of the clock-seeded random_number: random
+// spectra of u and v (four draws per mode, k, j, i order), high-wavenumber
+// damping, per-mode projection onto kx u + ky v = 0 (real and imaginary
+// parts separately), zero mean mode; c2r to physical space; w from the
+// trapezoid integration of -(du/dx + dv/dy) (or zero); walls zeroed and the
+// interior damped by (1 - z^2)^2; scaled to mean energy amplitude * 0.5 * 1.5^2.
+// The transforms and the x-y divergence run on the device.
+int random_perturbation(dns3d_handle* h, std::vector<double>& up, std::vector<double>& vp, std::vector<double>& wp) {
+    const dns3d_config& c = h->cfg;
+    const GridDev& g = h->g;
+    const int nx = c.nx, ny = c.ny, nz = c.nz, nxhp = nx / 2 + 1;
+    const double pi = 4.0 * std::atan(1.0);
+    const size_t ns = (size_t)nz * ny * nxhp, pl = (size_t)nx * ny, N = pl * nz;
+    std::vector<double2> uh(ns), vh(ns);
+    SplitMix64 rng{(uint64_t)c.perturbation_seed};
+    for (size_t o = 0; o < ns; ++o) {
+        uh[o].x = rng.uniform() - 0.5;
+        uh[o].y = rng.uniform() - 0.5;
+        vh[o].x = rng.uniform() - 0.5;
+        vh[o].y = rng.uniform() - 0.5;
+    }
+    const double kcut = 0.5 * std::min(2.0 * pi * nx / c.xlen, 2.0 * pi * ny / c.ylen);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nxhp; ++i) {
+                double2& a = uh[((size_t)k * ny + (j - 1)) * nxhp + (i - 1)];
+                double2& b = vh[((size_t)k * ny + (j - 1)) * nxhp + (i - 1)];
+                const double kx = 2.0 * pi * (double)(i - 1) / c.xlen;
+                const double ky = 2.0 * pi * (double)(j <= ny / 2 + 1 ? j - 1 : j - 1 - ny) / c.ylen;
+                const double kp = kx * kx + ky * ky;
+                if (std::sqrt(kp) > kcut) {
+                    a.x *= 0.1; a.y *= 0.1;
+                    b.x *= 0.1; b.y *= 0.1;
+                }
+                if (kp > 1.0e-12) {
+                    double kv = kx * a.x + ky * b.x;
+                    a.x -= kx * kv / kp;
+                    b.x -= ky * kv / kp;
+                    kv = kx * a.y + ky * b.y;
+                    a.y -= kx * kv / kp;
+                    b.y -= ky * kv / kp;
+                }
+                if (i == 1 && j == 1) a = b = make_double2(0.0, 0.0);
+            }
+    const size_t sb = ns * sizeof(double2), pb = N * sizeof(double);
+    CK(h, cudaMemcpyAsync(h->U, uh.data(), sb, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->V, vh.data(), sb, cudaMemcpyHostToDevice, h->stream));
+    Fields sp{};
+    sp.p[0] = h->U; sp.p[1] = h->V;
+    RFields ph{};
+    ph.p[0] = h->phys[0]; ph.p[1] = h->phys[1];
+    CK(h, fft_c2r(h->fft, g, sp, ph, 2, nz, h->stream));
+    up.resize(N);
+    vp.resize(N);
+    wp.assign(N, 0.0);
+    CK(h, cudaMemcpyAsync(up.data(), h->phys[0], pb, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(vp.data(), h->phys[1], pb, cudaMemcpyDeviceToHost, h->stream));
+    if (!c.zero_w_perturbations) {
+        // compute_spectral_derivatives_xy: du/dx + dv/dy of the physical fields
+        CK(h, fft_r2c(h->fft, g, ph, sp, 2, nz, h->stream));
+        CK(h, cudaMemsetAsync(h->W, 0, sb, h->stream));
+        double2* div = h->fft.tmp + (size_t)5 * spec_elems(c);
+        CK(h, launch_divergence(g, h->ops, h->U, h->V, h->W, div, h->stream));
+        Fields dv{}; dv.p[0] = div;
+        RFields dp{}; dp.p[0] = h->phys[2];
+        CK(h, fft_c2r(h->fft, g, dv, dp, 1, nz, h->stream));
+        std::vector<double> dxy(N);
+        CK(h, cudaMemcpyAsync(dxy.data(), h->phys[2], pb, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        std::vector<double> col(nz), wc(nz);
+        for (size_t p = 0; p < pl; ++p) {
+            for (int k = 0; k < nz; ++k) col[k] = dxy[k * pl + p];
+            integrate_w_column(nz, h->zpts.data(), col.data(), wc.data());
+            for (int k = 0; k < nz; ++k) wp[k * pl + p] = wc[k];
+        }
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->phys_valid = 0;
+    // enforce_channel_walls (perturbation_module.f90:276-320)
+    for (int k = 0; k < nz; ++k) {
+        const double d = (k == 0 || k == nz - 1) ? 0.0 : (1.0 - h->zpts[k] * h->zpts[k]) * (1.0 - h->zpts[k] * h->zpts[k]);
+        for (size_t p = 0; p < pl; ++p) {
+            up[k * pl + p] *= d;
+            vp[k * pl + p] *= d;
+            wp[k * pl + p] *= d;
+        }
+    }
+    // scale_to_amplitude (perturbation_module.f90:325-372)
+    double su = 0.0, sv = 0.0, sw = 0.0;
+    for (size_t o = 0; o < N; ++o) { su += up[o] * up[o]; sv += vp[o] * vp[o]; sw += wp[o] * wp[o]; }
+    const double cur = 0.5 * (su + sv + sw) / (double)N;
+    const double target = c.perturbation_amplitude * (0.5 * 1.5 * 1.5);
+    const double sc = cur > 1.0e-15 ? std::sqrt(target / cur) : 1.0;
+    for (size_t o = 0; o < N; ++o) { up[o] *= sc; vp[o] *= sc; wp[o] *= sc; }
+    return DNS3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int dns3d_initialize_fields(dns3d_handle* h) {
     if (!h) return DNS3D_E_INVALID;
     std::vector<double> u, v, w;
     initial_fields(h->cfg, h->zpts, u, v, w);
+    if (h->cfg.enable_perturbations && !h->cfg.use_analytical_perturbations) {
+        // apply_solenoidal_perturbations (3D:3219-3259): add, then the walls again
+        std::vector<double> up, vp, wp;
+        const int rp = random_perturbation(h, up, vp, wp);
+        if (rp) return rp;
+        const size_t pl = (size_t)h->cfg.nx * h->cfg.ny;
+        for (size_t o = 0; o < u.size(); ++o) { u[o] += up[o]; v[o] += vp[o]; w[o] += wp[o]; }
+        for (int k : {0, h->cfg.nz - 1})
+            for (size_t i = 0; i < pl; ++i) { u[k * pl + i] = 0.0; v[k * pl + i] = 0.0; w[k * pl + i] = 0.0; }
+    }
     std::vector<double> p(u.size(), 0.0);
     const size_t pl = (size_t)h->cfg.nx * h->cfg.ny;
     std::vector<double> zero(pl, 0.0);

@@ -184,6 +184,13 @@ bool parse_int(const std::string& v, int& out) {
     out = (int)x;
     return true;
 }
+bool parse_int64(const std::string& v, long long& out) {
+    char* end = nullptr;
+    long long x = std::strtoll(v.c_str(), &end, 10);
+    if (!end || end == v.c_str() || !trim(end).empty()) return false;
+    out = x;
+    return true;
+}
 bool parse_logical(const std::string& v, int& out) {
     std::string t = lower(trim(v));
     if (!t.empty() && t[0] == '.') t = t.substr(1);
@@ -218,6 +225,13 @@ bool assign(dns3d_config* c, const std::string& group, const std::string& key, c
         LOG_KEY("zero_w_perturbations", zero_w_perturbations)
         LOG_KEY("use_analytical_perturbations", use_analytical_perturbations)
         INT_KEY("analytical_mode_x", analytical_mode_x) INT_KEY("analytical_mode_y", analytical_mode_y)
+        // extension key of this library: seed of the random perturbation
+        if (key == "perturbation_seed") {
+            long long s64;
+            if (!parse_int64(val, s64)) return false;
+            c->perturbation_seed = s64;
+            return true;
+        }
     } else if (group == "pressure_solver") {
         LOG_KEY("use_weak_form_divergence", use_weak_form_divergence)
     } else if (group == "computational") {

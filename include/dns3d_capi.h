@@ -68,6 +68,13 @@ typedef struct dns3d_config {
     int lgl_dmatrix_guard;
     int precision;                                  /* DNS3D_PREC_*        */
     int device;                                     /* CUDA device ordinal */
+    /* Seed of the random solenoidal perturbation (enable_perturbations with
+     * use_analytical_perturbations = 0, perturbation_module.f90:42-176).  The
+     * reference seeds gfortran's random_number from the clock, so its runs
+     * cannot be repeated; here a SplitMix64 stream started from this seed
+     * supplies the uniform draws, in the reference's order.  Read from
+     * &perturbations as an extension key. */
+    long long perturbation_seed;
 } dns3d_config;
 
 /* PI controller globals (DNS_pressure_BC_3D.f90:75-89). */

@@ -713,6 +713,9 @@ void cpu_destroy(void* h);
 
 void* cpu_create(const cpu_config* c, int nthreads) {
     if (!c || c->nx < 4 || c->ny < 2 || c->nz < 3 || (c->nx % 2)) return NULL;
+    /* only the analytical initial perturbation is restated here; runs with
+     * the random one are set up through cpu_set_state */
+    if (c->enable_perturbations && !c->use_analytical_perturbations) return NULL;
     cpu_run* r = (cpu_run*)calloc(1, sizeof(cpu_run));
     if (!r) return NULL;
     r->c = *c;

@@ -78,6 +78,10 @@ class Config:
     # becomes singular (zgesv info /= 0 -> stop, 3D:1715-1718).  False keeps
     # the same Lagrange formula without the cutoff.
     lgl_dmatrix_guard: bool = True
+    # Not a namelist variable of the reference: seed of the stream that
+    # replaces its clock-seeded random_number in the random solenoidal
+    # perturbation (perturbation_module.f90:78-83).
+    perturbation_seed: int = 0
 
     def with_(self, **kw) -> "Config":
         return replace(self, **kw)
@@ -366,6 +370,90 @@ def analytical_perturbation(g: Grid, amp: float, mx: int, my: int):
     return up, vp, wp
 
 
+def splitmix64_uniform(seed: int, n: int) -> np.ndarray:
+    """n uniforms in [0, 1) from SplitMix64 (Steele, Lea and Flood 2014):
+    output i = mix(seed + (i+1) * 0x9E3779B97F4A7C15), top 53 bits."""
+    gamma = np.uint64(0x9E3779B97F4A7C15)
+    s = np.uint64(seed % (1 << 64)) + (np.arange(n, dtype=np.uint64) + np.uint64(1)) * gamma
+    z = (s ^ (s >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+
+
+def integrate_w_column(z: np.ndarray, div: np.ndarray) -> np.ndarray:
+    """integrate_with_boundary_conditions_fallback (perturbation_module.f90:
+    470-517) for one column: trapezoid integral of -div from w(-1) = 0,
+    quadratic correction to w(+1) = 0, sin^2 tapers (with 3.14159)."""
+    nz = len(z)
+    up = np.zeros(nz)
+    for k in range(1, nz):
+        up[k] = up[k - 1] - 0.5 * (div[k] + div[k - 1]) * (z[k] - z[k - 1])
+    total = up[-1]
+    zn = (z - z[0]) / (z[-1] - z[0])
+    w = up - total * (zn * (2.0 - zn))
+    w[0] = 0.0
+    w[-1] = 0.0
+    for k in range(2, min(4, nz - 1) + 1):           # Fortran levels
+        w[k - 1] *= math.sin(0.5 * 3.14159 * float(k - 1) / 3.0) ** 2
+    for k in range(max(nz - 3, 2), nz):
+        w[k - 1] *= math.sin(0.5 * 3.14159 * float(nz - k) / 3.0) ** 2
+    return w
+
+
+def random_solenoidal_perturbation(cfg: Config, g: Grid):
+    """generate_channel_solenoidal_perturbations (perturbation_module.f90:
+    42-176) with SplitMix64 draws in place of the clock-seeded random_number:
+    four uniforms per mode (Re u, Im u, Re v, Im v; k, j, i order), damping
+    by 0.1 beyond half the smaller Nyquist wavenumber, projection onto
+    kx u + ky v = 0 separately for the real and imaginary parts, zero mean
+    mode, c2r per plane; w from integrating -(du/dx + dv/dy) per column (or
+    zero); walls zeroed and the interior damped by (1 - z^2)^2
+    (enforce_channel_walls :276-320); energy scaled to amplitude * 0.5 * 1.5^2
+    (scale_to_amplitude :325-372)."""
+    nx, ny, nz, nxhp = g.nx, g.ny, g.nz, g.nxhp
+    pi = 4.0 * math.atan(1.0)
+    r = splitmix64_uniform(cfg.perturbation_seed, 4 * nz * ny * nxhp).reshape(nz, ny, nxhp, 4) - 0.5
+    uh = r[..., 0] + 1j * r[..., 1]
+    vh = r[..., 2] + 1j * r[..., 3]
+    kx = 2.0 * pi * np.arange(nxhp) / cfg.xlen
+    jj = np.arange(1, ny + 1)
+    ky = 2.0 * pi * np.where(jj <= ny // 2 + 1, jj - 1, jj - 1 - ny) / cfg.ylen
+    KX, KY = np.meshgrid(kx, ky)                       # [ny][nxhp]
+    kp = KX * KX + KY * KY
+    damp = np.where(np.sqrt(kp) > 0.5 * min(2.0 * pi * nx / cfg.xlen, 2.0 * pi * ny / cfg.ylen), 0.1, 1.0)
+    ur, ui, vr, vi = uh.real * damp, uh.imag * damp, vh.real * damp, vh.imag * damp
+    proj = kp > 1.0e-12
+    kps = np.where(proj, kp, 1.0)
+    kv = KX * ur + KY * vr
+    ur = np.where(proj, ur - KX * kv / kps, ur)
+    vr = np.where(proj, vr - KY * kv / kps, vr)
+    kv = KX * ui + KY * vi
+    ui = np.where(proj, ui - KX * kv / kps, ui)
+    vi = np.where(proj, vi - KY * kv / kps, vi)
+    uh = ur + 1j * ui
+    vh = vr + 1j * vi
+    uh[:, 0, 0] = 0.0
+    vh[:, 0, 0] = 0.0
+    up = c2r(uh, nx, ny)
+    vp = c2r(vh, nx, ny)
+    if cfg.zero_w_perturbations:
+        wp = np.zeros_like(up)
+    else:
+        dxy = ddx(g, up) + ddy(g, vp)
+        wp = np.empty_like(up)
+        for j in range(ny):
+            for i in range(nx):
+                wp[:, j, i] = integrate_w_column(g.zpts, dxy[:, j, i])
+    d = (1.0 - g.zpts ** 2) ** 2
+    d[0] = d[-1] = 0.0
+    up, vp, wp = (a * d[:, None, None] for a in (up, vp, wp))
+    cur = 0.5 * (np.sum(up ** 2) + np.sum(vp ** 2) + np.sum(wp ** 2)) / float(nx * ny * nz)
+    target = cfg.perturbation_amplitude * (0.5 * 1.5 ** 2)
+    sc = math.sqrt(target / cur) if cur > 1.0e-15 else 1.0
+    return up * sc, vp * sc, wp * sc
+
+
 def initial_state(cfg: Config, g: Grid, noise=None) -> State:
     """initialize_fields_3d (3D:909-962) with the analytical perturbation.
 
@@ -378,10 +466,11 @@ def initial_state(cfg: Config, g: Grid, noise=None) -> State:
     v = np.zeros(shape)
     w = np.zeros(shape)
     if cfg.enable_perturbations:
-        if not cfg.use_analytical_perturbations:
-            raise NotImplementedError("random solenoidal perturbations are not reproducible")
-        up, vp, wp = analytical_perturbation(g, cfg.perturbation_amplitude,
-                                             cfg.analytical_mode_x, cfg.analytical_mode_y)
+        if cfg.use_analytical_perturbations:
+            up, vp, wp = analytical_perturbation(g, cfg.perturbation_amplitude,
+                                                 cfg.analytical_mode_x, cfg.analytical_mode_y)
+        else:
+            up, vp, wp = random_solenoidal_perturbation(cfg, g)
         u, v, w = u + up, v + vp, w + wp
     if noise is not None:
         u, v, w = u + noise[0], v + noise[1], w + noise[2]

@@ -107,6 +107,12 @@ def test_namelist_partial_and_errors(built_lib, tmp_path):
     c = capi.read_namelist(str(p))
     assert (c.nx, c.ny, c.nz) == (64, 32, 17)  # ny keeps its default
     assert c.flow_control_method == 2 and c.target_bulk_velocity == 0.6667
+    seeded = tmp_path / "seeded.dat"
+    seeded.write_text("&perturbations\n enable_perturbations = .true., use_analytical_perturbations = .false.,\n"
+                      " perturbation_seed = 12345678901\n/\n")
+    c = capi.read_namelist(str(seeded))
+    assert c.perturbation_seed == 12345678901 and c.enable_perturbations == 1
+    assert c.use_analytical_perturbations == 0
     bad = tmp_path / "bad.dat"
     bad.write_text("&grid\n nx_input = sixty\n/\n")
     with pytest.raises(capi.Dns3DError) as ei:
@@ -125,7 +131,6 @@ def test_namelist_partial_and_errors(built_lib, tmp_path):
     (dict(nx=100), capi.DNS3D_E_UNSUPPORTED),   # nx/2 = 50 is not 2^a 3^b
     (dict(ny=40), capi.DNS3D_E_UNSUPPORTED),
     (dict(nz=200), capi.DNS3D_E_UNSUPPORTED),
-    (dict(enable_perturbations=1, use_analytical_perturbations=0), capi.DNS3D_E_UNSUPPORTED),
     (dict(precision=7), capi.DNS3D_E_UNSUPPORTED),
     (dict(dt=0.0), capi.DNS3D_E_INVALID),
 ])
@@ -200,3 +205,37 @@ def test_server_rejects_request_larger_than_budget(built_lib):
         with pytest.raises(capi.Dns3DError) as ei:
             srv.submit(cfg, 10)
         assert ei.value.code == capi.DNS3D_E_OOM
+
+
+def test_ctypes_structs_match_the_c_layout(tmp_path):
+    """Every struct the Python binding mirrors has the C compiler's size and
+    field offsets (a mismatch would make the library read past the end)."""
+    import ctypes as C
+    import shutil
+    import subprocess
+
+    from f90_dns_gb300 import capi
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no gcc")
+    pairs = [("dns3d_config", capi.CConfig), ("dns3d_pi_state", capi.CPIState), ("dns3d_diag", capi.CDiag),
+             ("dns3d_kernel_time", capi.CKernelTime), ("dns3d_server_opts", capi.CServerOpts),
+             ("dns3d_request_info", capi.CRequestInfo), ("dns3d_server_stats", capi.CServerStats),
+             ("dns3d_restart_header", capi.CRestartHeader), ("dns3d_flow_stats", capi.CFlowStats)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "dns3d_capi.h"', 'int main(void) {']
+    for cname, py in pairs:
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([gcc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = dict(ln.split() for ln in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                    check=True).stdout.splitlines())
+    for cname, py in pairs:
+        assert int(got[cname]) == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got[f"{cname}.{f}"]) == getattr(py, f).offset, (cname, f)

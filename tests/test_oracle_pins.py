@@ -208,3 +208,40 @@ def test_zero_mode_y_gives_no_perturbation():
     assert np.max(np.abs(st.v)) == 0.0
     assert np.max(np.abs(st.u - (1 - g.zpts ** 2)[:, None, None] * np.where(
         (np.arange(g.nz) == 0) | (np.arange(g.nz) == g.nz - 1), 0, 1)[:, None, None])) < 1e-15
+
+
+def test_splitmix64_known_answer():
+    """SplitMix64 with seed 0 (the reference implementation's first outputs)."""
+    u = ref.splitmix64_uniform(0, 3)
+    want = [0xE220A8397B1DCDAF, 0x6E789E6AA1B965F4, 0x06C45D188009454F]
+    assert [int(x * 2.0 ** 53) for x in u] == [w >> 11 for w in want]
+
+
+@pytest.mark.parametrize("zero_w", [False, True])
+def test_random_solenoidal_perturbation_properties(zero_w):
+    """generate_channel_solenoidal_perturbations restated with a seeded
+    stream: walls zero, mean energy = amplitude * 0.5 * 1.5^2, the seed
+    decides the field, zero_w_perturbations gives w = 0, and the x-y
+    projection makes each mode's (kx, ky) . (u^, v^) vanish before damping."""
+    cfg = ref.Config(nx=16, ny=12, nz=17, xlen=4 * ref.PI, ylen=2 * ref.PI, enable_perturbations=True,
+                     use_analytical_perturbations=False, perturbation_amplitude=0.02,
+                     zero_w_perturbations=zero_w, perturbation_seed=11)
+    g = ref.setup_grid(cfg)
+    up, vp, wp = ref.random_solenoidal_perturbation(cfg, g)
+    for a in (up, vp, wp):
+        assert np.all(a[0] == 0.0) and np.all(a[-1] == 0.0)
+    e = 0.5 * (np.sum(up ** 2) + np.sum(vp ** 2) + np.sum(wp ** 2)) / up.size
+    assert abs(e - 0.02 * 0.5 * 1.5 ** 2) < 1e-14
+    assert np.all(wp == 0.0) == zero_w
+    up2, _, _ = ref.random_solenoidal_perturbation(cfg.with_(perturbation_seed=12), g)
+    assert np.max(np.abs(up2 - up)) > 1e-3
+    up3, _, _ = ref.random_solenoidal_perturbation(cfg, g)
+    np.testing.assert_array_equal(up3, up)
+    # u, v of each level: r2c gives spectra with kx u^ + ky v^ = 0 up to the
+    # round-off of the transforms (the kx = 0, nx/2 columns are Hermitian-
+    # projected by the c2r, which keeps the constraint)
+    uh, vh = ref.r2c(up), ref.r2c(vp)
+    kd = g.xw[None, None, :] * uh + g.yw[None, :, None] * vh
+    keep = np.ones(g.ny, bool)
+    keep[g.ny // 2] = False  # ky = ny/2 is not symmetric in the FFTW order
+    assert np.max(np.abs(kd[:, keep, :-1])) < 1e-12 * np.max(np.abs(uh))
