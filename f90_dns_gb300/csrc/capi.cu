@@ -586,7 +586,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     if ((rc = dev_alloc(h, &h->d_pi, 1))) return fail(rc);
     h->red_blocks = 152 * 4;
     if ((rc = dev_alloc(h, &h->d_red, (size_t)4 * h->red_blocks))) return fail(rc);
-    if ((rc = dev_alloc(h, &h->d_out, 16))) return fail(rc);
+    if ((rc = dev_alloc(h, &h->d_out, 16 + 6 * (size_t)c.nz))) return fail(rc);
     if ((rc = dev_alloc(h, &h->d_flag, 4))) return fail(rc);
 
     cudaError_t e;
@@ -918,18 +918,32 @@ int dns3d_set_state(dns3d_handle* h, const double* u, const double* v, const dou
     double2* dst[4] = {h->U, h->V, h->W, h->P};
     int rc;
     h->phys_valid = 0;
-    // all uploads, then one batched forward transform of the given fields
-    RFields ph{};
-    Fields sp{};
-    int nf = 0;
-    for (int f = 0; f < 4; ++f) {
-        if (!src[f]) continue;
-        if ((rc = upload(h, h->phys[f], src[f], pe * sizeof(double)))) return rc;
-        ph.p[nf] = h->phys[f];
-        sp.p[nf] = dst[f];
-        ++nf;
+    // Two batches: the first half of the given fields is uploaded on the
+    // handle's stream and transformed there while the second half is still
+    // being copied on the side stream; the second batch's transform waits
+    // for its copies.
+    int idx[4], n = 0;
+    for (int f = 0; f < 4; ++f)
+        if (src[f]) idx[n++] = f;
+    const int na = (n + 1) / 2;
+    if (n > na) CK(h, fork_side(h, 0));  // the side copies wait for prior work on phys[]
+    for (int i = 0; i < n; ++i) {
+        const int f = idx[i];
+        CK(h, cudaMemcpyAsync(h->phys[f], src[f], pe * sizeof(double), cudaMemcpyHostToDevice,
+                              i < na ? h->stream : side_stream(h)));
     }
-    if (nf) CK(h, fft_r2c(h->fft, g, ph, sp, nf, g.nz, h->stream));
+    for (int b = 0; b < 2; ++b) {
+        const int lo = b ? na : 0, hi = b ? n : na;
+        if (lo == hi) continue;
+        if (b) CK(h, join_side(h, 0));
+        RFields ph{};
+        Fields sp{};
+        for (int i = lo; i < hi; ++i) {
+            ph.p[i - lo] = h->phys[idx[i]];
+            sp.p[i - lo] = dst[idx[i]];
+        }
+        CK(h, fft_r2c(h->fft, g, ph, sp, hi - lo, g.nz, h->stream));
+    }
     const double* gps[4] = {gpx_w1, gpx_w2, gpy_w1, gpy_w2};
     const bool any_gp = gpx_w1 || gpx_w2 || gpy_w1 || gpy_w2;
     const size_t pl = (size_t)g.nx * g.ny;
@@ -960,23 +974,39 @@ int dns3d_get_state(dns3d_handle* h, double* u, double* v, double* w, double* p_
     const size_t pe = phys_elems(h->cfg);
     double* dst[4] = {u, v, w, p_total};
     double2* src[4] = {h->U, h->V, h->W, h->P};
-    // one batched inverse transform of the requested fields not already in
-    // phys[], then the copies
-    Fields sp{};
-    RFields ph{};
-    int nf = 0;
-    for (int f = 0; f < 4; ++f) {
-        if (!dst[f] || (h->phys_valid >> f & 1u)) continue;
-        sp.p[nf] = src[f];
-        ph.p[nf] = h->phys[f];
-        ++nf;
-    }
-    if (nf) CK(h, fft_c2r(h->fft, g, sp, ph, nf, g.nz, h->stream));
+    // Requested fields already in phys[] are copied at once on the side
+    // stream; the others are transformed in two batches, the first batch's
+    // copies (side stream) overlapping the second batch's transform.
+    int need[4], n = 0, have[4], nh = 0;
     for (int f = 0; f < 4; ++f) {
         if (!dst[f]) continue;
-        h->phys_valid |= 1u << f;
-        CK(h, cudaMemcpyAsync(dst[f], h->phys[f], pe * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        if (h->phys_valid >> f & 1u) have[nh++] = f;
+        else need[n++] = f;
     }
+    const int na = (n + 1) / 2;
+    const bool side = nh > 0 || n > 1;
+    if (side) CK(h, fork_side(h, 0));
+    for (int i = 0; i < nh; ++i)
+        CK(h, cudaMemcpyAsync(dst[have[i]], h->phys[have[i]], pe * sizeof(double), cudaMemcpyDeviceToHost,
+                              side_stream(h)));
+    for (int b = 0; b < 2; ++b) {
+        const int lo = b ? na : 0, hi = b ? n : na;
+        if (lo == hi) continue;
+        Fields sp{};
+        RFields ph{};
+        for (int i = lo; i < hi; ++i) {
+            sp.p[i - lo] = src[need[i]];
+            ph.p[i - lo] = h->phys[need[i]];
+        }
+        CK(h, fft_c2r(h->fft, g, sp, ph, hi - lo, g.nz, h->stream));
+        if (b == 0 && n > 1) CK(h, fork_side(h, 1));  // the side stream copies batch 0 after its transform
+        for (int i = lo; i < hi; ++i)
+            CK(h, cudaMemcpyAsync(dst[need[i]], h->phys[need[i]], pe * sizeof(double), cudaMemcpyDeviceToHost,
+                                  (b == 0 && n > 1) ? side_stream(h) : h->stream));
+    }
+    if (side) CK(h, join_side(h, 0));
+    for (int f = 0; f < 4; ++f)
+        if (dst[f]) h->phys_valid |= 1u << f;
     double* gps[4] = {gpx_w1, gpx_w2, gpy_w1, gpy_w2};
     const size_t pl = (size_t)g.nx * g.ny;
     for (int i = 0; i < 4; ++i) {
@@ -1174,20 +1204,20 @@ int diag_core(dns3d_handle* h, dns3d_diag* out, bool with_div, std::vector<doubl
         CK(h, fft_c2r(h->fft, g, dv, dp, 1, g.nz, h->stream));
         CK(h, launch_maxabs(g, h->phys[3], phys_elems(c), h->d_red, h->red_blocks, h->d_out + 4, h->stream));
     }
-    double res[5] = {0, 0, 0, 0, 0};
+    // results, controller state and the (0,0) modes in one block, one copy:
+    // d_out = [5 reductions, 3 spare][dns3d_pi_state (8 doubles)][3 nz complex]
+    constexpr int kPiDoubles = (int)(sizeof(dns3d_pi_state) / sizeof(double));
+    CK(h, launch_diag_gather(g, h->U, h->V, h->W, h->d_pi, h->d_out + 8, h->stream));
+    std::vector<double> blk(8 + kPiDoubles + 6 * (size_t)g.nz);
+    CK(h, cudaMemcpyAsync(blk.data(), h->d_out, blk.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    double res[5] = {blk[0], blk[1], blk[2], blk[3], with_div ? blk[4] : 0.0};
     dns3d_pi_state pi{};
-    CK(h, cudaMemcpyAsync(res, h->d_out, sizeof(double) * (with_div ? 5 : 4), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaMemcpyAsync(&pi, h->d_pi, sizeof(pi), cudaMemcpyDeviceToHost, h->stream));
+    std::memcpy(&pi, blk.data() + 8, sizeof(pi));
     std::vector<double2> mean_local;
     std::vector<double2>& mean = mean3 ? *mean3 : mean_local;
-    const int ncomp = mean3 ? 3 : 1;
-    mean.resize((size_t)ncomp * g.nz);
-    const double2* comp[3] = {h->U, h->V, h->W};
-    for (int f = 0; f < ncomp; ++f)
-        CK(h, cudaMemcpy2DAsync(mean.data() + (size_t)f * g.nz, sizeof(double2), comp[f],
-                                (size_t)g.nm * sizeof(double2), sizeof(double2), g.nz, cudaMemcpyDeviceToHost,
-                                h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
+    mean.resize((size_t)3 * g.nz);
+    std::memcpy(mean.data(), blk.data() + 8 + kPiDoubles, mean.size() * sizeof(double2));
     const double ybar = 2.0;
     const double fac = (c.xlen / c.nx) * (c.ylen / c.ny) * (ybar / 2.0);
     out->umax = res[0];

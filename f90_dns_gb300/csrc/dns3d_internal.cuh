@@ -244,6 +244,10 @@ cudaError_t launch_grad_walls(const GridDev& g, const Ops& ops, const double2* P
 cudaError_t launch_diag_reduce(const GridDev& g, const Ops& ops, const double* u,
                                const double* v, const double* w, double* partial,
                                int nblocks, double* out, cudaStream_t s);
+// controller state (8 doubles) and the (0,0) modes of u, v, w (3 nz complex)
+// into out, for one copy back
+cudaError_t launch_diag_gather(const GridDev& g, const double2* U, const double2* V, const double2* W,
+                               const dns3d_pi_state* pi, double* out, cudaStream_t s);
 cudaError_t launch_maxabs(const GridDev& g, const double* f, size_t n, double* partial,
                           int nblocks, double* out, cudaStream_t s);
 cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaStream_t s);

@@ -1134,16 +1134,33 @@ __global__ void __launch_bounds__(256) k_diag_partial(GridDev g, const double* _
     }
 }
 
+// One warp: lane l folds partials l, l+32, ...; then a butterfly.
 __global__ void k_diag_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
-    if (threadIdx.x != 0) return;
     double mu = 0.0, mv = 0.0, mw = 0.0, e = 0.0;
-    for (int b = 0; b < nb; ++b) {
+    for (int b = threadIdx.x; b < nb; b += 32) {
         mu = fmax(mu, partial[4 * b]);
         mv = fmax(mv, partial[4 * b + 1]);
         mw = fmax(mw, partial[4 * b + 2]);
         e += partial[4 * b + 3];
     }
-    out[0] = mu; out[1] = mv; out[2] = mw; out[3] = e;
+    mu = warp_max(mu); mv = warp_max(mv); mw = warp_max(mw); e = warp_sum(e);
+    if (threadIdx.x == 0) { out[0] = mu; out[1] = mv; out[2] = mw; out[3] = e; }
+}
+
+// The controller state and the (0,0) mode of u, v, w per level, gathered
+// next to the reductions so that one copy brings all diagnostics back.
+__global__ void k_diag_gather(GridDev g, const double2* __restrict__ U, const double2* __restrict__ V,
+                              const double2* __restrict__ W, const dns3d_pi_state* __restrict__ pi,
+                              double* __restrict__ out) {
+    const double* ps = reinterpret_cast<const double*>(pi);
+    constexpr int npi = (int)(sizeof(dns3d_pi_state) / sizeof(double));
+    for (int t = threadIdx.x; t < npi; t += blockDim.x) out[t] = ps[t];
+    double2* mean = reinterpret_cast<double2*>(out + npi);
+    const double2* f[3] = {U, V, W};
+    for (int t = threadIdx.x; t < 3 * g.nz; t += blockDim.x) {
+        const int c = t / g.nz, k = t - c * g.nz;
+        mean[t] = f[c][(size_t)k * g.nm];
+    }
 }
 
 __global__ void __launch_bounds__(256) k_maxabs_partial(const double* __restrict__ f, size_t n,
@@ -1162,10 +1179,10 @@ __global__ void __launch_bounds__(256) k_maxabs_partial(const double* __restrict
 }
 
 __global__ void k_max_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
-    if (threadIdx.x != 0) return;
     double m = 0.0;
-    for (int b = 0; b < nb; ++b) m = fmax(m, partial[b]);
-    out[0] = m;
+    for (int b = threadIdx.x; b < nb; b += 32) m = fmax(m, partial[b]);
+    m = warp_max(m);
+    if (threadIdx.x == 0) out[0] = m;
 }
 
 __global__ void k_nonfinite(const double2* __restrict__ f, size_t n, int* flag) {
@@ -1372,6 +1389,12 @@ cudaError_t launch_diag_reduce(const GridDev& g, const Ops& ops, const double* u
                                cudaStream_t s) {
     k_diag_partial<<<nblocks, 256, 0, s>>>(g, ops.zw, u, v, w, partial);
     k_diag_final<<<1, 32, 0, s>>>(partial, nblocks, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diag_gather(const GridDev& g, const double2* U, const double2* V, const double2* W,
+                               const dns3d_pi_state* pi, double* out, cudaStream_t s) {
+    k_diag_gather<<<1, 128, 0, s>>>(g, U, V, W, pi, out);
     return cudaGetLastError();
 }
 
