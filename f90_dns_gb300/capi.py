@@ -81,6 +81,8 @@ class CConfig(C.Structure):
         ("precision", C.c_int),
         ("device", C.c_int),
         ("perturbation_seed", C.c_longlong),
+        ("convection_scheme", C.c_int), ("linear_solver", C.c_int),
+        ("cgstol", C.c_double),
     ]
 
 

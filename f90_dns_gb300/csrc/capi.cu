@@ -39,6 +39,7 @@ struct dns3d_handle {
     double2 *SU = nullptr, *SV = nullptr, *SW = nullptr;
     double2 *US = nullptr, *VS = nullptr, *WS = nullptr, *PHI = nullptr;
     double2* PHIZ = nullptr;  // mixed: dphi/dz
+    double2* RK[3] = {nullptr, nullptr, nullptr};  // jst4 stage state (convection_scheme 1)
     double* phys[6] = {nullptr};
     dns3d_pi_state* d_pi = nullptr;
     double* d_red = nullptr;
@@ -108,6 +109,10 @@ int validate(const dns3d_config* c) {
             return DNS3D_E_INVALID;
     }
     if (c->precision != DNS3D_PREC_FP64 && c->precision != DNS3D_PREC_MIXED) return DNS3D_E_UNSUPPORTED;
+    if (c->convection_scheme != 0 && c->convection_scheme != 1) return DNS3D_E_INVALID;
+    if (c->linear_solver != 0 && c->linear_solver != 1) return DNS3D_E_INVALID;
+    if (c->linear_solver == 1 && !(c->cgstol > 0.0)) return DNS3D_E_INVALID;
+    if (c->linear_solver == 1 && c->precision != DNS3D_PREC_FP64) return DNS3D_E_UNSUPPORTED;
     return DNS3D_OK;
 }
 
@@ -266,11 +271,13 @@ int upload(dns3d_handle* h, void* dst, const void* src, size_t bytes) {
     return DNS3D_OK;
 }
 
-int run_source_terms_mixed(dns3d_handle* h) {
+// The nonlinear term of the velocity spectra in[0..2] (the state, or a jst4
+// stage state): FP32 sources in src32 (mixed) or FP64 sources in SU..SW.
+int run_source_terms_mixed(dns3d_handle* h, double2* const* in) {
     const GridDev& g = h->g;
     FFields sp{};
     for (int f = 0; f < 6; ++f) sp.p[f] = h->spec32[f];
-    CK(h, launch_vorticity_mixed(g, h->mx, h->ops, h->U, h->V, h->W, sp, h->stream));
+    CK(h, launch_vorticity_mixed(g, h->mx, h->ops, in[0], in[1], in[2], sp, h->stream));
     mark(h, "vorticity32");
     FRFields ph{};
     for (int f = 0; f < 6; ++f) ph.p[f] = h->phys32[f];
@@ -285,7 +292,7 @@ int run_source_terms_mixed(dns3d_handle* h) {
     return DNS3D_OK;
 }
 
-int run_source_terms_fp64(dns3d_handle* h);
+int run_source_terms_fp64(dns3d_handle* h, double2* const* in);
 
 int run_source_terms(dns3d_handle* h) {
     h->phys_valid = 0;
@@ -296,19 +303,45 @@ int run_source_terms(dns3d_handle* h) {
     CK(h, fork_side(h, 0));
     CK(h, launch_pi_update(g, h->ops, h->pp, h->U, h->d_pi, side_stream(h)));
     mark(h, "pi_update");
-    int rc = h->mixed ? run_source_terms_mixed(h) : run_source_terms_fp64(h);
+    double2* state[3] = {h->U, h->V, h->W};
+    double2* const* in = state;
+    int rc;
+    if (h->cfg.convection_scheme == 1) {
+        // jst4 (DNS_pressure_BC_2D.f90:931-1014 lifted to 3D): three stage
+        // states u^n + (1/irk) dt S(previous), irk = 4, 3, 2; the step's
+        // source is S of the last one
+        Fields F{}, R{};
+        for (int f = 0; f < 3; ++f) { F.p[f] = state[f]; R.p[f] = h->RK[f]; }
+        for (int irk = 4; irk >= 2; --irk) {
+            rc = h->mixed ? run_source_terms_mixed(h, in) : run_source_terms_fp64(h, in);
+            if (rc) return rc;
+            const double coef = (1.0 / (double)irk) * h->cfg.dt;
+            if (h->mixed) {
+                FFields S{};
+                for (int f = 0; f < 3; ++f) S.p[f] = h->src32[f];
+                CK(h, launch_rk_stage(g, h->sp, coef, F, S, R, h->stream));
+            } else {
+                Fields S{};
+                S.p[0] = h->SU; S.p[1] = h->SV; S.p[2] = h->SW;
+                CK(h, launch_rk_stage(g, h->sp, coef, F, S, R, h->stream));
+            }
+            mark(h, "jst4_stage");
+            in = h->RK;
+        }
+    }
+    rc = h->mixed ? run_source_terms_mixed(h, in) : run_source_terms_fp64(h, in);
     if (rc) return rc;
     CK(h, join_side(h, 0));
     return DNS3D_OK;
 }
 
-int run_source_terms_fp64(dns3d_handle* h) {
+int run_source_terms_fp64(dns3d_handle* h, double2* const* in) {
     const GridDev& g = h->g;
     // vorticity into the u*,v*,w* buffers (free until the viscous step)
-    CK(h, launch_vorticity(g, h->ops, h->U, h->V, h->W, h->US, h->VS, h->WS, h->stream));
+    CK(h, launch_vorticity(g, h->ops, in[0], in[1], in[2], h->US, h->VS, h->WS, h->stream));
     mark(h, "vorticity");
     Fields spec{};
-    spec.p[0] = h->U; spec.p[1] = h->V; spec.p[2] = h->W;
+    spec.p[0] = in[0]; spec.p[1] = in[1]; spec.p[2] = in[2];
     spec.p[3] = h->US; spec.p[4] = h->VS; spec.p[5] = h->WS;
     RFields phys{};
     for (int f = 0; f < 6; ++f) phys.p[f] = h->phys[f];
@@ -344,6 +377,15 @@ int run_viscous(dns3d_handle* h) {
     F.p[0] = h->U; F.p[1] = h->V; F.p[2] = h->W;
     S.p[0] = h->SU; S.p[1] = h->SV; S.p[2] = h->SW;
     O.p[0] = h->US; O.p[1] = h->VS; O.p[2] = h->WS;
+    if (h->cfg.linear_solver == 1) {  // jacgs on the right-hand sides
+        StepParams sr = h->sp;
+        sr.rhs_only = 1;
+        CK(h, launch_viscous(h->g, h->ops, sr, F, S, h->GP, h->d_pi, O, h->stream));
+        mark(h, "viscous_rhs");
+        CK(h, launch_pcg_helmholtz(h->g, h->ops, h->sp, O, h->cfg.cgstol, h->stream));
+        mark(h, "viscous_jacgs");
+        return DNS3D_OK;
+    }
     CK(h, launch_viscous(h->g, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->stream));
     mark(h, "viscous_helmholtz");
     return DNS3D_OK;
@@ -358,6 +400,15 @@ int run_pressure(dns3d_handle* h) {
         CK(h, launch_pressure_mixed(h->g, h->mx, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->stream));
         mark(h, "pressure_mixed");
         CK(h, join_side(h, 2));
+        return DNS3D_OK;
+    }
+    if (h->cfg.linear_solver == 1) {  // jacgs; the pinned (0,0) mode stays direct
+        StepParams sr = h->sp;
+        sr.rhs_only = 1;
+        CK(h, launch_pressure(h->g, h->ops, sr, h->US, h->VS, h->WS, h->PHI, h->stream));
+        mark(h, "pressure_rhs");
+        CK(h, launch_pcg_poisson(h->g, h->ops, h->PHI, h->cfg.cgstol, h->stream));
+        mark(h, "pressure_jacgs");
         return DNS3D_OK;
     }
     CK(h, launch_pressure(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->stream));
@@ -443,6 +494,9 @@ int dns3d_config_defaults(dns3d_config* c) {
     c->precision = DNS3D_PREC_FP64;
     c->device = 0;
     c->perturbation_seed = 0;
+    c->convection_scheme = 0;
+    c->linear_solver = 0;
+    c->cgstol = 1.0e-6;  // 3D:575
     return DNS3D_OK;
 }
 
@@ -459,6 +513,7 @@ int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
     const size_t nz2 = (size_t)c->nz * c->nz;
     size_t b = 0;
     b += 11 * se * sizeof(double2);          // U V W P SU SV SW US VS WS PHI
+    if (c->convection_scheme == 1) b += 3 * se * sizeof(double2);  // jst4 stage state
     b += 4 * nm * sizeof(double2);           // GP
     b += 6 * se * sizeof(double2);           // FFT scratch
     b += 6 * pe * sizeof(double);            // physical fields
@@ -572,6 +627,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
         {ops.ksq, ksq.data(), (size_t)nq * 8}, {dS, S.data(), nz2 * 8}};
     for (auto& u : ups)
         if ((rc = upload(h, u.d, u.s, u.b))) return fail(rc);
+    ops.S = dS;
 
     // state and work buffers
     const size_t se = spec_elems(c), pe = phys_elems(c);
@@ -579,6 +635,9 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     for (auto p : specs)
         if ((rc = dev_alloc(h, p, se))) return fail(rc);
     if ((rc = dev_alloc(h, &h->GP, (size_t)4 * g.nm))) return fail(rc);
+    if (c.convection_scheme == 1)
+        for (int f = 0; f < 3; ++f)
+            if ((rc = dev_alloc(h, &h->RK[f], se))) return fail(rc);
     for (int f = 0; f < 6; ++f)
         if ((rc = dev_alloc(h, &h->phys[f], pe))) return fail(rc);
     h->fft.tmp_fields = 6;

@@ -122,6 +122,7 @@ struct StepParams {
     int dealias;          // use_dealias_23_rule
     int kx_max, ky_max;   // 2/3 limits (3D:1169-1170)
     int weak_form;        // use_weak_form_divergence
+    int rhs_only;         // viscous/pressure kernels: write the right-hand sides (for jacgs), not the solutions
 };
 
 // z-operators in parity-folded form (see step.cu): for nz levels,
@@ -142,6 +143,7 @@ struct Ops {
     double* xw;      // [nxhp]
     double* yw;      // [ny]
     double* ksq;     // xsq+ysq per unique q     [nq]
+    double* S;       // stiffness (2/ybar) sum_m d1(m,k) d1(m,n) zwts(m), [nz][nz] (jacgs)
     double* HinvF;   // folded Helmholtz inverses      [nq][he*he + ho*ho]
     double* PinvF;   // folded Poisson inverses        [nq][he*he + ho*ho]
     double* PpinT;   // pinned (0,0) Poisson inverse, unfolded, transposed [nz][nz]
@@ -218,6 +220,18 @@ cudaError_t launch_products32(const GridDev& g, FRFields in6, FRFields out3, cud
 cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops,
                                  const StepParams& sp, Fields F, FFields Src, const double2* GP,
                                  Fields Out, cudaStream_t s);
+// jacgs (Jacobi-preconditioned CG) on the right-hand sides the viscous and
+// pressure kernels left in place with StepParams::rhs_only: every non-pinned
+// Poisson system (S + k^2 w ybar/2) phi = -b and every interior Helmholtz
+// system, one warp per real system, at most 500 iterations, stopping at
+// residual <= tol * initial residual.
+cudaError_t launch_pcg_poisson(const GridDev& g, const Ops& ops, double2* PHI, double tol, cudaStream_t s);
+cudaError_t launch_pcg_helmholtz(const GridDev& g, const Ops& ops, const StepParams& sp, Fields Out, double tol,
+                                 cudaStream_t s);
+// jst4 stage state: out = F + coef * mask(S) with the wall levels zeroed.
+template <typename SrcC>
+cudaError_t launch_rk_stage(const GridDev& g, const StepParams& sp, double coef, Fields F, FieldsT<SrcC> Src,
+                            Fields Out, cudaStream_t s);
 // The mixed form's mode (0,0) in FP64 (independent of the mode tiles above).
 cudaError_t launch_viscous_mean_mode(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F,
                                      FFields Src, const double2* GP, const dns3d_pi_state* pi,

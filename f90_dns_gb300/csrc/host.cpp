@@ -214,6 +214,7 @@ bool assign(dns3d_config* c, const std::string& group, const std::string& key, c
     } else if (group == "simulation") {
         REAL_KEY("re", re) REAL_KEY("xlen", xlen) REAL_KEY("ylen", ylen)
         REAL_KEY("u_centerline", u_centerline) LOG_KEY("use_crank_nicolson", use_crank_nicolson)
+        REAL_KEY("cgstol", cgstol)
     } else if (group == "flow_control") {
         INT_KEY("flow_control_method", flow_control_method)
         REAL_KEY("target_pressure_gradient", target_pressure_gradient)
@@ -238,11 +239,12 @@ bool assign(dns3d_config* c, const std::string& group, const std::string& key, c
         LOG_KEY("use_dealias_23_rule", use_dealias_23_rule)
         // extension keys of this library (not read by the reference)
         LOG_KEY("lgl_dmatrix_guard", lgl_dmatrix_guard)
+        INT_KEY("convection_scheme", convection_scheme) INT_KEY("linear_solver", linear_solver)
     }
 #undef INT_KEY
 #undef REAL_KEY
 #undef LOG_KEY
-    return true;  // keys the step does not use (alpha, beta, ta, ybar, cgstol, ...) are accepted
+    return true;  // keys the step does not use (alpha, beta, ta, ybar, cs, ...) are accepted
 }
 
 }  // namespace

@@ -325,12 +325,15 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
         if (k < ho) {
             const double2 b2 = viscous_rhs(g, ops, sp, comp, z2, m, ky, kx, F.p[comp][o2],
                                            to_d2(Src.p[comp][o2]), lap.b, bc1, bc2, dpdx);
+            if (sp.rhs_only) Out.p[comp][o2] = b2;
             bt[k * tc + c] = make_double2(b1.x + b2.x, b1.y + b2.y);
             bt[(he + k) * tc + c] = make_double2(b1.x - b2.x, b1.y - b2.y);
         } else {
             bt[k * tc + c] = b1;
         }
+        if (sp.rhs_only) Out.p[comp][o1] = b1;
     }
+    if (sp.rhs_only) return;  // uniform over the block
     __syncthreads();
     const size_t qstride = (size_t)he * he + (size_t)ho * ho;
     for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
@@ -405,17 +408,19 @@ __global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams
             tb[t] = make_double2(b1.x + b2.x, b1.y + b2.y);
             tb[(he + k) * tc + c] = make_double2(b1.x - b2.x, b1.y - b2.y);
             if (m == 0) { bpin[k] = b1; bpin[nz - 1 - k] = b2; }
+            if (sp.rhs_only && m != 0) PHI[(size_t)(nz - 1 - k) * g.nm + m] = b2;
         } else {
             tb[t] = b1;
             if (m == 0) bpin[k] = b1;
         }
+        if (sp.rhs_only && m != 0) PHI[(size_t)k * g.nm + m] = b1;
     }
     __syncthreads();
     const size_t qstride = (size_t)he * he + (size_t)ho * ho;
     for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
         const int c = t / he, k = t - c * he;
         const int m = m0 + c;
-        if (m >= g.nm) continue;
+        if (m >= g.nm || (sp.rhs_only && m != 0)) continue;
         Pair x;
         if (m == 0) {
             double2 a = make_double2(0.0, 0.0), b = a;
@@ -434,6 +439,189 @@ __global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams
         }
         PHI[(size_t)k * g.nm + m] = x.a;
         if (k < ho) PHI[(size_t)(nz - 1 - k) * g.nm + m] = x.b;
+    }
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ------------------------------------------------------------------ jacgs
+// jacgs (DNS_pressure_BC_2D.f90:2361-2476) for one real system per warp:
+// (a S[off+i][off+j] + diag(dg)) x = b, n <= 160 unknowns, rows i = lane +
+// 32 s held in registers, the search direction shared through the warp's
+// shared-memory vector for the product with S (S staged in shared memory).
+// Jacobi preconditioner, x0 = 0, small = 1e-30 guards, at most 500
+// iterations, stop when |r|_2 <= tol |r0|_2 (every lane takes the same
+// decision: the reductions are butterflies).  A system that does not
+// converge keeps its last iterate, as the reference uses its partial result.
+constexpr int kPcgWarps = 8;
+constexpr int kPcgRows = 5;  // ceil(160 / 32)
+
+__device__ void warp_pcg(const double* __restrict__ S, int lds, int off, int n, double a, const double* dg,
+                         const double* bl, double* xl, double* pw, double tol) {
+    const int lane = threadIdx.x & 31;
+    const double small = 1.0e-30;
+    double r[kPcgRows], q[kPcgRows], p[kPcgRows], dinv[kPcgRows], ap[kPcgRows];
+    double rr = 0.0;
+#pragma unroll
+    for (int s = 0; s < kPcgRows; ++s) {
+        const int i = lane + 32 * s;
+        xl[s] = 0.0;
+        r[s] = q[s] = p[s] = dinv[s] = ap[s] = 0.0;
+        if (i < n) {
+            const double d = a * S[(size_t)(off + i) * lds + off + i] + dg[s];
+            dinv[s] = fabs(d) > small ? 1.0 / d : 1.0;
+            r[s] = bl[s];
+            q[s] = r[s] * dinv[s];
+            p[s] = q[s];
+            rr = fma(r[s], r[s], rr);
+        }
+    }
+    const double res0 = sqrt(warp_sum(rr));
+    if (!(res0 > 0.0)) return;
+    for (int it = 0; it < 500; ++it) {
+#pragma unroll
+        for (int s = 0; s < kPcgRows; ++s)
+            if (lane + 32 * s < n) pw[lane + 32 * s] = p[s];
+        __syncwarp();
+        double qr = 0.0, pa = 0.0;
+#pragma unroll
+        for (int s = 0; s < kPcgRows; ++s) {
+            const int i = lane + 32 * s;
+            if (i < n) {
+                const double* row = S + (size_t)(off + i) * lds + off;
+                double acc = 0.0;
+                for (int j = 0; j < n; ++j) acc = fma(row[j], pw[j], acc);
+                ap[s] = fma(a, acc, dg[s] * p[s]);
+                qr = fma(q[s], r[s], qr);
+                pa = fma(p[s], ap[s], pa);
+            }
+        }
+        __syncwarp();
+        const double qdr = warp_sum(qr);
+        const double alfa = qdr / (warp_sum(pa) + small);
+        double qn = 0.0, rn = 0.0;
+#pragma unroll
+        for (int s = 0; s < kPcgRows; ++s) {
+            if (lane + 32 * s < n) {
+                xl[s] = fma(alfa, p[s], xl[s]);
+                r[s] = fma(-alfa, ap[s], r[s]);
+                q[s] = r[s] * dinv[s];
+                qn = fma(q[s], r[s], qn);
+                rn = fma(r[s], r[s], rn);
+            }
+        }
+        const double beta = warp_sum(qn) / (qdr + small);
+#pragma unroll
+        for (int s = 0; s < kPcgRows; ++s)
+            if (lane + 32 * s < n) p[s] = fma(beta, p[s], q[s]);
+        if (sqrt(warp_sum(rn)) <= tol * res0) break;
+    }
+}
+
+// Poisson, every mode but (0,0): (S + k^2 w ybar/2) phi = -b, b in PHI.
+__global__ void __launch_bounds__(32 * kPcgWarps) k_pcg_poisson(GridDev g, Ops ops, double2* PHI, double tol) {
+    extern __shared__ double psm[];
+    const int nz = g.nz;
+    for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) psm[t] = ops.S[t];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* pw = psm + nz * nz + warp * nz;
+    const long long sid = (long long)blockIdx.x * kPcgWarps + warp;
+    if (sid >= 2LL * (g.nm - 1)) return;
+    const int m = 1 + (int)(sid >> 1), part = (int)(sid & 1);
+    const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+    const double k2 = __ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+    double* ph = reinterpret_cast<double*>(PHI);
+    double dg[kPcgRows], bl[kPcgRows], xl[kPcgRows];
+#pragma unroll
+    for (int s = 0; s < kPcgRows; ++s) {
+        const int i = lane + 32 * s;
+        dg[s] = bl[s] = 0.0;
+        if (i < nz) {
+            dg[s] = k2 * __ldg(&ops.wh[i]);
+            bl[s] = -ph[2 * ((size_t)i * g.nm + m) + part];
+        }
+    }
+    warp_pcg(psm, nz, 0, nz, 1.0, dg, bl, xl, pw, tol);
+#pragma unroll
+    for (int s = 0; s < kPcgRows; ++s) {
+        const int i = lane + 32 * s;
+        if (i < nz) ph[2 * ((size_t)i * g.nm + m) + part] = xl[s];
+    }
+}
+
+// Helmholtz, every mode, component and part: the interior system
+// (f S_II + diag((1 + f k^2) w ybar/2)) x_I = b_I - (f S_I1 x_1 + f S_In x_n),
+// b and the wall values x_1, x_n as the viscous kernel left them in Out.
+__global__ void __launch_bounds__(32 * kPcgWarps) k_pcg_helmholtz(GridDev g, Ops ops, StepParams sp, Fields Out,
+                                                                   double tol) {
+    extern __shared__ double psm[];
+    const int nz = g.nz;
+    for (int t = threadIdx.x; t < nz * nz; t += blockDim.x) psm[t] = ops.S[t];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* pw = psm + nz * nz + warp * nz;
+    const long long sid = (long long)blockIdx.x * kPcgWarps + warp;
+    if (sid >= 6LL * g.nm) return;
+    const int m = (int)(sid / 6), rem = (int)(sid % 6), comp = rem >> 1, part = rem & 1;
+    const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+    const double k2 = __ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+    const double f = sp.helm_f;
+    double* o = reinterpret_cast<double*>(Out.p[comp]);
+    const double bc1 = o[2 * (size_t)m + part];
+    const double bc2 = o[2 * ((size_t)(nz - 1) * g.nm + m) + part];
+    double dg[kPcgRows], bl[kPcgRows], xl[kPcgRows];
+    const int n = nz - 2;
+#pragma unroll
+    for (int s = 0; s < kPcgRows; ++s) {
+        const int i = lane + 32 * s, z = i + 1;
+        dg[s] = bl[s] = 0.0;
+        if (i < n) {
+            dg[s] = (1.0 + f * k2) * __ldg(&ops.wh[z]);
+            bl[s] = o[2 * ((size_t)z * g.nm + m) + part] - (__ldg(&ops.S0[z]) * bc1 + __ldg(&ops.Sn[z]) * bc2);
+        }
+    }
+    warp_pcg(psm, nz, 1, n, f, dg, bl, xl, pw, tol);
+#pragma unroll
+    for (int s = 0; s < kPcgRows; ++s) {
+        const int i = lane + 32 * s;
+        if (i < n) o[2 * ((size_t)(i + 1) * g.nm + m) + part] = xl[s];
+    }
+}
+
+// dynamic shared memory of the jacgs kernels: S and one vector per warp
+size_t pcg_smem(const GridDev& g) { return ((size_t)g.nz * g.nz + (size_t)kPcgWarps * g.nz) * sizeof(double); }
+
+// ------------------------------------------------------------------ jst4 stages
+// stage state of runge_kutta_convection (DNS_pressure_BC_2D.f90:985-993)
+// lifted to 3D: out = F + coef * mask(S), wall levels zeroed (apply_wall_bc).
+template <typename SrcC>
+__global__ void k_rk_stage(GridDev g, StepParams sp, double coef, Fields F, FieldsT<SrcC> Src, Fields Out) {
+    const size_t per = (size_t)g.nz * g.nm, total = 3 * per;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const int comp = (int)(t / per);
+        const size_t o = t - comp * per;
+        const int z = (int)(o / g.nm), m = (int)(o - (size_t)z * g.nm);
+        double2 r = make_double2(0.0, 0.0);
+        if (z != 0 && z != g.nz - 1) {
+            double2 sv = to_d2(Src.p[comp][o]);
+            if (sp.dealias) {
+                const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+                const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
+                if (kx > sp.kx_max || kyi > sp.ky_max) sv = make_double2(0.0, 0.0);
+            }
+            const double2 fv = F.p[comp][o];
+            r = make_double2(fv.x + coef * sv.x, fv.y + coef * sv.y);
+        }
+        Out.p[comp][o] = r;
     }
 }
 
@@ -1092,14 +1280,6 @@ __global__ void k_correction_mixed(GridDev g, Ops ops, StepParams sp, const doub
 }
 
 // ------------------------------------------------------------------ reductions
-__device__ __forceinline__ double warp_max(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 // Per-block partials of max|u|, max|v|, max|w| and sum 0.5|u|^2 zwts[k].
 __global__ void __launch_bounds__(256) k_diag_partial(GridDev g, const double* __restrict__ zw,
@@ -1255,6 +1435,8 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
     if ((e = set_smem(k_pressure, (2 * (size_t)g.nz * tile_cols(g, 2) + g.nz) * sizeof(double2)))) return e;
     if ((e = set_smem(k_correction, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
     if ((e = set_smem(k_divergence, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_pcg_poisson, pcg_smem(g)))) return e;
+    if ((e = set_smem(k_pcg_helmholtz, pcg_smem(g)))) return e;
     return cudaSuccess;
 }
 
@@ -1364,6 +1546,36 @@ cudaError_t launch_correction(const GridDev& g, const Ops& ops, const StepParams
     k_correction<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, US, VS, WS, PHI, U, V, W, P, GP, tc);
     return cudaGetLastError();
 }
+
+cudaError_t launch_pcg_poisson(const GridDev& g, const Ops& ops, double2* PHI, double tol, cudaStream_t s) {
+    const long long nsys = 2LL * (g.nm - 1);
+    if (nsys <= 0) return cudaSuccess;
+    k_pcg_poisson<<<(unsigned)((nsys + kPcgWarps - 1) / kPcgWarps), 32 * kPcgWarps, pcg_smem(g), s>>>(g, ops, PHI,
+                                                                                                       tol);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pcg_helmholtz(const GridDev& g, const Ops& ops, const StepParams& sp, Fields Out, double tol,
+                                 cudaStream_t s) {
+    const long long nsys = 6LL * g.nm;
+    k_pcg_helmholtz<<<(unsigned)((nsys + kPcgWarps - 1) / kPcgWarps), 32 * kPcgWarps, pcg_smem(g), s>>>(
+        g, ops, sp, Out, tol);
+    return cudaGetLastError();
+}
+
+template <typename SrcC>
+cudaError_t launch_rk_stage(const GridDev& g, const StepParams& sp, double coef, Fields F, FieldsT<SrcC> Src,
+                            Fields Out, cudaStream_t s) {
+    const size_t n = 3 * (size_t)g.nz * g.nm;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_rk_stage<SrcC><<<blocks, 256, 0, s>>>(g, sp, coef, F, Src, Out);
+    return cudaGetLastError();
+}
+template cudaError_t launch_rk_stage<double2>(const GridDev&, const StepParams&, double, Fields, Fields, Fields,
+                                              cudaStream_t);
+template cudaError_t launch_rk_stage<float2>(const GridDev&, const StepParams&, double, Fields, FFields, Fields,
+                                             cudaStream_t);
 
 cudaError_t launch_apply_bc(const GridDev& g, double2* U, double2* V, double2* W, cudaStream_t s) {
     k_apply_bc<<<(2 * g.nm + 255) / 256, 256, 0, s>>>(g, U, V, W);

@@ -75,6 +75,24 @@ typedef struct dns3d_config {
      * supplies the uniform draws, in the reference's order.  Read from
      * &perturbations as an extension key. */
     long long perturbation_seed;
+    /* Optional schemes (extension keys of &computational; the reference's 3D
+     * solver has neither, its 2D solver has both):
+     * convection_scheme 0 = the 3D step's single explicit evaluation of the
+     *   nonlinear term (3D:1032-1098); 1 = jst4, the four-stage scheme of
+     *   runge_kutta_convection (DNS_pressure_BC_2D.f90:931-1014) lifted to 3D:
+     *   for a = 1/4, 1/3, 1/2 the stage state is u^n + a dt S(previous stage)
+     *   with S the (filtered) rotational nonlinear term and the walls zeroed,
+     *   and the step uses S of the last stage state (forcing added once).
+     * linear_solver 0 = the per-mode Helmholtz and Poisson systems solved
+     *   directly (the reference's zgesv); 1 = jacgs, Jacobi-preconditioned
+     *   conjugate gradients (DNS_pressure_BC_2D.f90:2361-2476) on every
+     *   non-pinned Poisson system and on the interior Helmholtz systems, FP64,
+     *   at most 500 iterations, stopping when the residual 2-norm falls to
+     *   cgstol times its initial value (a relative test: the spectra here are
+     *   unnormalised sums).  FP64 precision only. */
+    int convection_scheme;
+    int linear_solver;
+    double cgstol;                                  /* &simulation cgstol (default 1e-6, 3D:575) */
 } dns3d_config;
 
 /* PI controller globals (DNS_pressure_BC_3D.f90:75-89). */

@@ -82,6 +82,13 @@ class Config:
     # replaces its clock-seeded random_number in the random solenoidal
     # perturbation (perturbation_module.f90:78-83).
     perturbation_seed: int = 0
+    # Optional schemes (not in the reference's 3D solver; from its 2D solver):
+    # convection_scheme 1 = jst4 (DNS_pressure_BC_2D.f90:931-1014 lifted to
+    # 3D), linear_solver 1 = jacgs (DNS_pressure_BC_2D.f90:2361-2476) with a
+    # relative stopping test at cgstol (3D default 1e-6, 3D:575).
+    convection_scheme: int = 0
+    linear_solver: int = 0
+    cgstol: float = 1.0e-6
 
     def with_(self, **kw) -> "Config":
         return replace(self, **kw)
@@ -522,9 +529,49 @@ def update_pressure_gradient(cfg: Config, g: Grid, st: State, istep: int) -> Non
     pi.avg_pressure_gradient = pi.pressure_gradient_sum / float(pi.pressure_gradient_count)
 
 
-def compute_source_terms(cfg: Config, g: Grid, st: State):
-    """compute_source_terms_3d (3D:1032-1045) -> (su, sv, sw)."""
-    u, v, w = st.u, st.v, st.w
+def jacgs(A: np.ndarray, b: np.ndarray, tol: float, maxit: int = 500) -> np.ndarray:
+    """jacgs (DNS_pressure_BC_2D.f90:2361-2476) on a batch of real systems
+    A[s] x[s] = b[s]: Jacobi-preconditioned conjugate gradients from x = 0,
+    small = 1e-30 guards, at most `maxit` iterations; a system stops when its
+    residual 2-norm is <= tol * (initial residual 2-norm) (the reference tests
+    the absolute norm against tol).  Converged systems are left unchanged."""
+    small = 1.0e-30
+    d = np.diagonal(A, axis1=1, axis2=2)
+    dinv = np.where(np.abs(d) > small, 1.0 / np.where(d == 0.0, 1.0, d), 1.0)
+    x = np.zeros_like(b)
+    r = b.copy()
+    q = r * dinv
+    p = q.copy()
+    res0 = np.sqrt(np.sum(r * r, axis=1))
+    active = res0 > 0.0
+    for _ in range(maxit):
+        if not active.any():
+            break
+        ap = np.einsum("sij,sj->si", A, p)
+        qdr = np.sum(q * r, axis=1)
+        alfa = qdr / (np.sum(p * ap, axis=1) + small)
+        a = active[:, None]
+        x = np.where(a, x + alfa[:, None] * p, x)
+        r = np.where(a, r - alfa[:, None] * ap, r)
+        q = r * dinv
+        beta = np.sum(q * r, axis=1) / (qdr + small)
+        p = np.where(a, q + beta[:, None] * p, p)
+        res1 = np.sqrt(np.sum(r * r, axis=1))
+        active = active & ~(res1 <= tol * res0)
+    return x
+
+
+def _solve_real_systems(A: np.ndarray, b: np.ndarray, tol: float) -> np.ndarray:
+    """jacgs on complex right-hand sides: real and imaginary parts apart."""
+    xr = jacgs(A, np.ascontiguousarray(b.real), tol)
+    xi = jacgs(A, np.ascontiguousarray(b.imag), tol)
+    return xr + 1j * xi
+
+
+def nonlinear_source(cfg: Config, g: Grid, u, v, w):
+    """compute_source_terms_3d_standard (3D:1054-1098) and, with the 2/3 rule,
+    the filtering of compute_source_terms_3d_dealiased (3D:1233-1261):
+    S = u x omega (the gradient part is absorbed into p)."""
     ux, uy, uz = derivatives(g, u)
     vx, vy, vz = derivatives(g, v)
     wx, wy, wz = derivatives(g, w)
@@ -539,6 +586,32 @@ def compute_source_terms(cfg: Config, g: Grid, st: State):
         su = c2r(np.where(keep, r2c(su), 0.0), g.nx, g.ny)
         sv = c2r(np.where(keep, r2c(sv), 0.0), g.nx, g.ny)
         sw = c2r(np.where(keep, r2c(sw), 0.0), g.nx, g.ny)
+    return su, sv, sw
+
+
+def jst4_source(cfg: Config, g: Grid, st: State):
+    """runge_kutta_convection (DNS_pressure_BC_2D.f90:931-1014) lifted to 3D:
+    for irk = 4, 3, 2 the stage state is u^n + (1/irk) dt S(previous stage
+    state) with the walls zeroed (apply_wall_bc); the source of the step is S
+    of the last stage state (the 2D routine keeps the irk = 1 evaluation and
+    resets u to u^n)."""
+    cu, cv, cw = st.u, st.v, st.w
+    for irk in (4, 3, 2):
+        su, sv, sw = nonlinear_source(cfg, g, cu, cv, cw)
+        a = (1.0 / float(irk)) * cfg.dt
+        cu, cv, cw = st.u + a * su, st.v + a * sv, st.w + a * sw
+        for f in (cu, cv, cw):
+            f[0] = 0.0
+            f[-1] = 0.0
+    return nonlinear_source(cfg, g, cu, cv, cw)
+
+
+def compute_source_terms(cfg: Config, g: Grid, st: State):
+    """compute_source_terms_3d (3D:1032-1045) -> (su, sv, sw)."""
+    if cfg.convection_scheme == 1:
+        su, sv, sw = jst4_source(cfg, g, st)
+    else:
+        su, sv, sw = nonlinear_source(cfg, g, st.u, st.v, st.w)
     # apply_flow_control_forcing (3D:1107-1148); method 2 is called with the
     # namelist istart, not the step number (3D:1118)
     if cfg.flow_control_method == 1:
@@ -576,6 +649,13 @@ def solve_viscous_helmholtz(cfg: Config, g: Grid, rhs: np.ndarray, theta: float,
     b[:, 1:nz - 1] -= H[:, 1:nz - 1, 0] * b1f[:, None] + H[:, 1:nz - 1, nz - 1] * b2f[:, None]
     b[:, 0] = b1f
     b[:, nz - 1] = b2f
+    if cfg.linear_solver == 1:
+        # jacgs on the interior system: the identity rows fix x_1, x_nz and the
+        # kept columns subtract the wall data a second time
+        r = b[:, 1:nz - 1] - (H[:, 1:nz - 1, 0] * b1f[:, None] + H[:, 1:nz - 1, nz - 1] * b2f[:, None])
+        xi = _solve_real_systems(np.ascontiguousarray(H[:, 1:nz - 1, 1:nz - 1]), r, cfg.cgstol)
+        x = np.concatenate([b1f[:, None], xi, b2f[:, None]], axis=1)
+        return c2r(x.T.reshape(nz, ny, nxhp), g.nx, g.ny)
     H[:, 0, :] = 0.0
     H[:, 0, 0] = 1.0
     H[:, nz - 1, :] = 0.0
@@ -639,6 +719,9 @@ def solve_pressure(cfg: Config, g: Grid, us, vs, ws) -> np.ndarray:
     b = b.astype(np.complex128)
     b[0, 0] = 0.0
     x = np.linalg.solve(P, b[:, :, None])[:, :, 0]
+    if cfg.linear_solver == 1:
+        # jacgs on every non-pinned mode: (S + k^2 w ybar/2) phi = -b
+        x[1:] = _solve_real_systems(np.ascontiguousarray(-P[1:].real), -b[1:], cfg.cgstol)
     return c2r(x.T.reshape(nz, ny, nxhp), g.nx, g.ny)
 
 
