@@ -288,7 +288,8 @@ int run_source_terms_mixed(dns3d_handle* h, double2* const* in) {
     mark(h, "products32");
     FFields src{};
     for (int f = 0; f < 3; ++f) src.p[f] = h->src32[f];
-    CK(h, fft_r2c32(h->fft, g, prod, src, 3, g.nz, h->stream));
+    // the 2/3 filter discards kx > kx_max: those columns skip the y pass
+    CK(h, fft_r2c32(h->fft, g, prod, src, 3, g.nz, h->stream, h->sp.dealias ? h->sp.kx_max + 1 : 0));
     return DNS3D_OK;
 }
 
@@ -352,7 +353,8 @@ int run_source_terms_fp64(dns3d_handle* h, double2* const* in) {
     mark(h, "products");
     Fields src{};
     src.p[0] = h->SU; src.p[1] = h->SV; src.p[2] = h->SW;
-    CK(h, fft_r2c(h->fft, g, prod, src, 3, g.nz, h->stream));
+    // the 2/3 filter discards kx > kx_max: those columns skip the y pass
+    CK(h, fft_r2c(h->fft, g, prod, src, 3, g.nz, h->stream, h->sp.dealias ? h->sp.kx_max + 1 : 0));
     return DNS3D_OK;
 }
 

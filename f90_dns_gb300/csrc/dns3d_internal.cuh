@@ -90,7 +90,7 @@ struct FftCtx {
 // nx/2 in {16..256} of the form 2^a 3^b; fft_ct_supported tells which grids.
 bool fft_ct_supported(int ny, int nxh);
 template <int SIGN, typename C>
-cudaError_t fft_ct_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int nf, const C* tw,
+cudaError_t fft_ct_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int ncol, int nf, const C* tw,
                      cudaStream_t s);
 template <typename T>
 cudaError_t fft_ct_c2r_x(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst, const GridDev& g, int nrows, int nf,
@@ -104,14 +104,16 @@ void fft_release(FftCtx& ctx);
 // spec[f] (spectral, read only) -> phys[f]; uses ctx.tmp (nf <= tmp_fields).
 cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, int nf,
                     int nplanes, cudaStream_t s);
-// phys[f] -> spec[f].
+// phys[f] -> spec[f].  With ncol > 0 only the kx < ncol columns of spec are
+// completed (the others keep the x transform's output): for sources that the
+// 2/3 filter truncates at kx_max = ncol - 1 anyway.
 cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf,
-                    int nplanes, cudaStream_t s);
+                    int nplanes, cudaStream_t s, int ncol = 0);
 // FP32 versions (same transform definitions), scratch ctx.tmp32.
 cudaError_t fft_c2r32(const FftCtx& ctx, const GridDev& g, FFields spec, FRFields phys, int nf,
                       int nplanes, cudaStream_t s);
 cudaError_t fft_r2c32(const FftCtx& ctx, const GridDev& g, FRFields phys, FFields spec, int nf,
-                      int nplanes, cudaStream_t s);
+                      int nplanes, cudaStream_t s, int ncol = 0);
 
 // ---------------------------------------------------------------- step.cu
 struct StepParams {

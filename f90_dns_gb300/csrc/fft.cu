@@ -131,7 +131,7 @@ __device__ C* stockham(C* a, C* b, int count, int ld, const FftPlan1D& pl, const
 // grid (ceil(nxhp/cx), nplanes, nf); smem 2*cx*(ny+1) double2.
 template <int SIGN, typename C>
 __global__ void __launch_bounds__(256) k_fft_y(FieldsT<C> src, FieldsT<C> dst, GridDev g, FftPlan1D pl,
-                                               const C* __restrict__ tw, int cx) {
+                                               const C* __restrict__ tw, int cx, int ncols_total) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* smem = reinterpret_cast<C*>(smem_raw);
     const int ld = g.ny + 1;
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(256) k_fft_y(FieldsT<C> src, FieldsT<C> dst, G
     const size_t plane = (size_t)blockIdx.y * g.nm;
     const C* __restrict__ s = src.p[blockIdx.z] + plane;
     C* d = dst.p[blockIdx.z] + plane;
-    const int ncol = min(cx, g.nxhp - kx0);
+    const int ncol = min(cx, ncols_total - kx0);
     for (int t = threadIdx.x; t < g.ny * cx; t += blockDim.x) {
         const int y = t / cx, c = t - y * cx;
         if (c < ncol) a[c * ld + y] = s[(size_t)y * g.nxhp + kx0 + c];
@@ -338,7 +338,7 @@ cudaError_t c2r_impl(const FftCtx& ctx, const GridDev& g, FieldsT<typename Cx<T>
     using C = typename Cx<T>::type;
     const int nrows = nplanes * g.ny;
     if (ctx.use_ct) {
-        cudaError_t e = fft_ct_y<+1, C>(spec, tmp, g, nplanes, nf, twy, s);
+        cudaError_t e = fft_ct_y<+1, C>(spec, tmp, g, nplanes, g.nxhp, nf, twy, s);
         if (e) return e;
         if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_inverse" : "fft32_y_inverse");
         e = fft_ct_c2r_x<T>(tmp, phys, g, nrows, nf, twx2, twx, s);
@@ -347,7 +347,7 @@ cudaError_t c2r_impl(const FftCtx& ctx, const GridDev& g, FieldsT<typename Cx<T>
     }
     const int cx = pick_cx(g.ny);
     dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
-    k_fft_y<+1, C><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(C), s>>>(spec, tmp, g, ctx.py, twy, cx);
+    k_fft_y<+1, C><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(C), s>>>(spec, tmp, g, ctx.py, twy, cx, g.nxhp);
     if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_inverse" : "fft32_y_inverse");
     const int rx = pick_rx(g.nxh);
     dim3 gx((nrows + rx - 1) / rx, nf);
@@ -359,14 +359,15 @@ cudaError_t c2r_impl(const FftCtx& ctx, const GridDev& g, FieldsT<typename Cx<T>
 template <typename T>
 cudaError_t r2c_impl(const FftCtx& ctx, const GridDev& g, FieldsT<T> phys, FieldsT<typename Cx<T>::type> spec,
                      int nf, int nplanes, cudaStream_t s, const typename Cx<T>::type* twy,
-                     const typename Cx<T>::type* twx2, const typename Cx<T>::type* twx) {
+                     const typename Cx<T>::type* twx2, const typename Cx<T>::type* twx, int ncol) {
     using C = typename Cx<T>::type;
     const int nrows = nplanes * g.ny;
+    if (ncol <= 0 || ncol > g.nxhp) ncol = g.nxhp;
     if (ctx.use_ct) {
         cudaError_t e = fft_ct_r2c_x<T>(phys, spec, g, nrows, nf, twx2, twx, s);
         if (e) return e;
         if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_x_r2c" : "fft32_x_r2c");
-        e = fft_ct_y<-1, C>(spec, spec, g, nplanes, nf, twy, s);
+        e = fft_ct_y<-1, C>(spec, spec, g, nplanes, ncol, nf, twy, s);
         if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_forward" : "fft32_y_forward");
         return e;
     }
@@ -375,8 +376,8 @@ cudaError_t r2c_impl(const FftCtx& ctx, const GridDev& g, FieldsT<T> phys, Field
     k_r2c_x<T><<<gx, 256, 2 * rx * (g.nxh + 2) * sizeof(C), s>>>(phys, spec, g, ctx.px2, twx2, twx, rx, nrows);
     if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_x_r2c" : "fft32_x_r2c");
     const int cx = pick_cx(g.ny);
-    dim3 gy((g.nxhp + cx - 1) / cx, nplanes, nf);
-    k_fft_y<-1, C><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(C), s>>>(spec, spec, g, ctx.py, twy, cx);
+    dim3 gy((ncol + cx - 1) / cx, nplanes, nf);
+    k_fft_y<-1, C><<<gy, 256, 2 * cx * (g.ny + 1) * sizeof(C), s>>>(spec, spec, g, ctx.py, twy, cx, ncol);
     if (ctx.hook) ctx.hook(ctx.hook_ctx, sizeof(T) == 8 ? "fft_y_forward" : "fft32_y_forward");
     return cudaGetLastError();
 }
@@ -392,9 +393,9 @@ cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields ph
 }
 
 cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf, int nplanes,
-                    cudaStream_t s) {
+                    cudaStream_t s, int ncol) {
     if (nf > kMaxFields) return cudaErrorInvalidValue;
-    return r2c_impl<double>(ctx, g, phys, spec, nf, nplanes, s, ctx.tw_ny, ctx.tw_nx2, ctx.tw_nx);
+    return r2c_impl<double>(ctx, g, phys, spec, nf, nplanes, s, ctx.tw_ny, ctx.tw_nx2, ctx.tw_nx, ncol);
 }
 
 cudaError_t fft_c2r32(const FftCtx& ctx, const GridDev& g, FFields spec, FRFields phys, int nf, int nplanes,
@@ -406,9 +407,9 @@ cudaError_t fft_c2r32(const FftCtx& ctx, const GridDev& g, FFields spec, FRField
 }
 
 cudaError_t fft_r2c32(const FftCtx& ctx, const GridDev& g, FRFields phys, FFields spec, int nf, int nplanes,
-                      cudaStream_t s) {
+                      cudaStream_t s, int ncol) {
     if (nf > kMaxFields) return cudaErrorInvalidValue;
-    return r2c_impl<float>(ctx, g, phys, spec, nf, nplanes, s, ctx.tw32_ny, ctx.tw32_nx2, ctx.tw32_nx);
+    return r2c_impl<float>(ctx, g, phys, spec, nf, nplanes, s, ctx.tw32_ny, ctx.tw32_nx2, ctx.tw32_nx, ncol);
 }
 
 }  // namespace dns3d

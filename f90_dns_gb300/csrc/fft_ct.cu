@@ -88,6 +88,16 @@ template <int R, int SIGN, typename C> __device__ __forceinline__ void dft(C* v)
     else dft3<SIGN>(v);
 }
 
+// field pointer i of a by-value FieldsT without a dynamic index into the
+// parameter block (which would copy the array to local memory)
+template <typename P> __device__ __forceinline__ P* field_ptr(const FieldsT<P>& f, int i) {
+    P* r = f.p[0];
+#pragma unroll
+    for (int k = 1; k < kMaxFields; ++k)
+        if (i == k) r = f.p[k];
+    return r;
+}
+
 __host__ __device__ constexpr int next_radix(int m) { return m % 8 == 0 ? 8 : (m % 4 == 0 ? 4 : (m % 2 == 0 ? 2 : 3)); }
 
 // Transforms per CTA: a power of two near 2048 / N, in [1, 64].
@@ -152,36 +162,44 @@ __device__ __forceinline__ void ct_fft(C* buf, const C* __restrict__ tw) {
     }
 }
 
-// y pass: complex transforms of length N = ny along every (plane, kx) column;
-// CX columns per CTA taken from the flattened index plane * nxhp + kx.
-// grid (ceil(nplanes * nxhp / CX), 1, nf).
+// y pass: complex transforms of length N = ny along the (plane, kx) columns
+// with kx < ncol (ncol = nx/2+1, or fewer when the 2/3 filter discards the
+// rest); CX columns per CTA taken from the flattened index plane * ncol + kx.
+// grid (ceil(nplanes * ncol / CX), 1, nf).
 template <int N, int SIGN, typename C>
 __global__ void __launch_bounds__(kThreads) k_fft_y_ct(FieldsT<C> src, FieldsT<C> dst, GridDev g, int nplanes,
-                                                       const C* __restrict__ tw) {
+                                                       int ncol, const C* __restrict__ tw) {
     constexpr int CX = per_cta(N);
     constexpr int LD = N + 1;
     __shared__ C buf[CX * LD];
-    const long long ncols = (long long)nplanes * g.nxhp;
+    const long long ncols = (long long)nplanes * ncol;
     const long long vc = (long long)blockIdx.x * CX + (threadIdx.x % CX);
     const bool live = vc < ncols;
     size_t base = 0;
     if (live) {
-        const int p = (int)(vc / g.nxhp);
-        const int kx = (int)(vc - (long long)p * g.nxhp);
+        const int p = (int)(vc / ncol);
+        const int kx = (int)(vc - (long long)p * ncol);
         base = (size_t)p * g.nm + kx;
     }
-    const C* __restrict__ s = src.p[blockIdx.z];
-    C* d = dst.p[blockIdx.z];
+    const C* __restrict__ s = field_ptr(src, blockIdx.z);
+    C* d = field_ptr(dst, blockIdx.z);
     constexpr int ROWS_PER_ITER = kThreads / CX;  // CX divides kThreads
-    const int c = threadIdx.x % CX;
-#pragma unroll 4
-    for (int y = threadIdx.x / CX; y < N; y += ROWS_PER_ITER)
-        buf[c * LD + y] = live ? s[base + (size_t)y * g.nxhp] : mk<C>(0, 0);
+    constexpr int ITERS = N / ROWS_PER_ITER;
+    static_assert(N % ROWS_PER_ITER == 0, "rows split evenly over the threads");
+    const int c = threadIdx.x % CX, y0 = threadIdx.x / CX;
+    // all of a thread's loads are issued before any is used
+    C v[ITERS];
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it)
+        v[it] = live ? s[base + (size_t)(y0 + it * ROWS_PER_ITER) * g.nxhp] : mk<C>(0, 0);
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) buf[c * LD + y0 + it * ROWS_PER_ITER] = v[it];
     __syncthreads();
     ct_fft<N, 1, SIGN, CX, LD>(buf, tw);
     if (live) {
-#pragma unroll 4
-        for (int y = threadIdx.x / CX; y < N; y += ROWS_PER_ITER) d[base + (size_t)y * g.nxhp] = buf[c * LD + y];
+#pragma unroll
+        for (int it = 0; it < ITERS; ++it)
+            d[base + (size_t)(y0 + it * ROWS_PER_ITER) * g.nxhp] = buf[c * LD + y0 + it * ROWS_PER_ITER];
     }
 }
 
@@ -199,33 +217,46 @@ __global__ void __launch_bounds__(kThreads) k_c2r_x_ct(FieldsT<typename Cx<T>::t
     constexpr int LD = N + 1;
     __shared__ C buf[RX * LD];
     const int row0 = blockIdx.x * RX;
-    const C* __restrict__ s = src.p[blockIdx.y];
-    C* d = reinterpret_cast<C*>(dst.p[blockIdx.y]);
+    const C* __restrict__ s = field_ptr(src, blockIdx.y);
+    C* d = reinterpret_cast<C*>(field_ptr(dst, blockIdx.y));
     const int nxhp = N + 1;
-    for (int t = threadIdx.x; t < RX * N; t += kThreads) {
+    constexpr int ITERS = RX * N / kThreads;
+    static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
+    // all of a thread's loads are issued before any is used
+    C xa[ITERS], xb[ITERS];
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
-        C z = mk<C>(0, 0);
+        xa[it] = xb[it] = mk<C>(0, 0);
         if (row0 + r < nrows) {
             const C* row = s + (size_t)(row0 + r) * nxhp;
-            C xa = row[k];
-            C xb = row[N - k];
-            if (k == 0) {
-                xa.y = 0;
-                xb.y = 0;
-            }
-            const C sm = mk<C>(xa.x + xb.x, xa.y - xb.y);
-            const C df = mk<C>(xa.x - xb.x, xa.y + xb.y);
-            C w = __ldg(&tw_nx[k]);
-            w.y = -w.y;
-            const C p = cmul(w, df);
-            z = mk<C>(sm.x - p.y, sm.y + p.x);
+            xa[it] = row[k];
+            xb[it] = row[N - k];
         }
-        buf[r * LD + k] = z;
+    }
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        const int r = t / N, k = t - r * N;
+        C a = xa[it], b = xb[it];
+        if (k == 0) {
+            a.y = 0;
+            b.y = 0;
+        }
+        const C sm = mk<C>(a.x + b.x, a.y - b.y);
+        const C df = mk<C>(a.x - b.x, a.y + b.y);
+        C w = __ldg(&tw_nx[k]);
+        w.y = -w.y;
+        const C p = cmul(w, df);
+        buf[r * LD + k] = mk<C>(sm.x - p.y, sm.y + p.x);
     }
     __syncthreads();
     ct_fft<N, 1, +1, RX, LD>(buf, tw_n);
     const T sc = (T)g.inv_nxny;
-    for (int t = threadIdx.x; t < RX * N; t += kThreads) {
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
         if (row0 + r < nrows) {
             const C z = buf[r * LD + k];
@@ -247,11 +278,22 @@ __global__ void __launch_bounds__(kThreads) k_r2c_x_ct(FieldsT<T> src, FieldsT<t
     constexpr int LD = N + 1;
     __shared__ C buf[RX * LD];
     const int row0 = blockIdx.x * RX;
-    const C* __restrict__ s = reinterpret_cast<const C*>(src.p[blockIdx.y]);
-    C* d = dst.p[blockIdx.y];
-    for (int t = threadIdx.x; t < RX * N; t += kThreads) {
+    const C* __restrict__ s = reinterpret_cast<const C*>(field_ptr(src, blockIdx.y));
+    C* d = field_ptr(dst, blockIdx.y);
+    constexpr int ITERS = RX * N / kThreads;
+    static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
+    C v[ITERS];
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
-        buf[r * LD + k] = (row0 + r < nrows) ? s[(size_t)(row0 + r) * N + k] : mk<C>(0, 0);
+        v[it] = (row0 + r < nrows) ? s[(size_t)(row0 + r) * N + k] : mk<C>(0, 0);
+    }
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        const int r = t / N, k = t - r * N;
+        buf[r * LD + k] = v[it];
     }
     __syncthreads();
     ct_fft<N, 1, -1, RX, LD>(buf, tw_n);
@@ -270,11 +312,12 @@ __global__ void __launch_bounds__(kThreads) k_r2c_x_ct(FieldsT<T> src, FieldsT<t
 }
 
 template <int SIGN, typename C, int N>
-void launch_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int nf, const C* tw, cudaStream_t s) {
+void launch_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int ncol, int nf, const C* tw,
+              cudaStream_t s) {
     constexpr int CX = per_cta(N);
-    const long long ncols = (long long)nplanes * g.nxhp;
+    const long long ncols = (long long)nplanes * ncol;
     dim3 grid((unsigned)((ncols + CX - 1) / CX), 1, nf);
-    k_fft_y_ct<N, SIGN, C><<<grid, kThreads, 0, s>>>(src, dst, g, nplanes, tw);
+    k_fft_y_ct<N, SIGN, C><<<grid, kThreads, 0, s>>>(src, dst, g, nplanes, ncol, tw);
 }
 
 template <typename T, int N>
@@ -311,11 +354,12 @@ bool fft_ct_supported(int ny, int nxh) {
 }
 
 template <int SIGN, typename C>
-cudaError_t fft_ct_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int nf, const C* tw,
+cudaError_t fft_ct_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int ncol, int nf, const C* tw,
                      cudaStream_t s) {
+    if (ncol < 1 || ncol > g.nxhp) return cudaErrorInvalidValue;
     switch (g.ny) {
 #define Y_CASE(n) \
-    case n: launch_y<SIGN, C, n>(src, dst, g, nplanes, nf, tw, s); break;
+    case n: launch_y<SIGN, C, n>(src, dst, g, nplanes, ncol, nf, tw, s); break;
         DNS3D_CT_Y_LENGTHS(Y_CASE)
 #undef Y_CASE
         default: return cudaErrorInvalidValue;
@@ -349,10 +393,14 @@ cudaError_t fft_ct_r2c_x(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, cons
     return cudaGetLastError();
 }
 
-template cudaError_t fft_ct_y<-1, double2>(Fields, Fields, const GridDev&, int, int, const double2*, cudaStream_t);
-template cudaError_t fft_ct_y<+1, double2>(Fields, Fields, const GridDev&, int, int, const double2*, cudaStream_t);
-template cudaError_t fft_ct_y<-1, float2>(FFields, FFields, const GridDev&, int, int, const float2*, cudaStream_t);
-template cudaError_t fft_ct_y<+1, float2>(FFields, FFields, const GridDev&, int, int, const float2*, cudaStream_t);
+template cudaError_t fft_ct_y<-1, double2>(Fields, Fields, const GridDev&, int, int, int, const double2*,
+                                         cudaStream_t);
+template cudaError_t fft_ct_y<+1, double2>(Fields, Fields, const GridDev&, int, int, int, const double2*,
+                                         cudaStream_t);
+template cudaError_t fft_ct_y<-1, float2>(FFields, FFields, const GridDev&, int, int, int, const float2*,
+                                         cudaStream_t);
+template cudaError_t fft_ct_y<+1, float2>(FFields, FFields, const GridDev&, int, int, int, const float2*,
+                                         cudaStream_t);
 template cudaError_t fft_ct_c2r_x<double>(Fields, RFields, const GridDev&, int, int, const double2*, const double2*,
                                           cudaStream_t);
 template cudaError_t fft_ct_c2r_x<float>(FFields, FRFields, const GridDev&, int, int, const float2*, const float2*,

@@ -39,6 +39,16 @@ __device__ __forceinline__ ModeInfo mode_info(const GridDev& g, int m, const dou
     return mi;
 }
 
+// Field pointer `i` of a by-value FieldsT, selected without a dynamic index
+// into the parameter block (which would copy the array to local memory).
+template <typename P> __device__ __forceinline__ P* fptr(const FieldsT<P>& f, int i) {
+    P* r = f.p[0];
+#pragma unroll
+    for (int k = 1; k < kMaxFields; ++k)
+        if (i == k) r = f.p[k];
+    return r;
+}
+
 // tile[f][z][c] <- field f at (z, m0 + c); zero beyond nm.
 __device__ __forceinline__ void load_tile(double2* tile, const double2* __restrict__ src,
                                           const GridDev& g, int m0, int tc) {
@@ -293,7 +303,7 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
     double2* tf = sm;             // [3] folded F tiles
     double2* tb = sm + 3 * tsz;   // [3] folded rhs tiles
     const int m0 = blockIdx.x * tc;
-    for (int comp = 0; comp < 3; ++comp) fold_load(tf + comp * tsz, F.p[comp], g, m0, tc, he, ho);
+    for (int comp = 0; comp < 3; ++comp) fold_load(tf + comp * tsz, fptr(F, comp), g, m0, tc, he, ho);
     __syncthreads();
     const double dpdx = pi->current_pressure_gradient;
     for (int t = threadIdx.x; t < 3 * he * tc; t += blockDim.x) {
@@ -320,18 +330,18 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
         if (sp.cn_fac != 0.0) lap = sym_apply(ops.D2e, ops.D2o, tf + comp * tsz, k, c, tc, he, ho);
         const int z1 = k, z2 = nz - 1 - k;
         const size_t o1 = (size_t)z1 * g.nm + m, o2 = (size_t)z2 * g.nm + m;
-        const double2 b1 = viscous_rhs(g, ops, sp, comp, z1, m, ky, kx, F.p[comp][o1], to_d2(Src.p[comp][o1]),
+        const double2 b1 = viscous_rhs(g, ops, sp, comp, z1, m, ky, kx, fptr(F, comp)[o1], to_d2(fptr(Src, comp)[o1]),
                                        lap.a, bc1, bc2, dpdx);
         if (k < ho) {
-            const double2 b2 = viscous_rhs(g, ops, sp, comp, z2, m, ky, kx, F.p[comp][o2],
-                                           to_d2(Src.p[comp][o2]), lap.b, bc1, bc2, dpdx);
-            if (sp.rhs_only) Out.p[comp][o2] = b2;
+            const double2 b2 = viscous_rhs(g, ops, sp, comp, z2, m, ky, kx, fptr(F, comp)[o2],
+                                           to_d2(fptr(Src, comp)[o2]), lap.b, bc1, bc2, dpdx);
+            if (sp.rhs_only) fptr(Out, comp)[o2] = b2;
             bt[k * tc + c] = make_double2(b1.x + b2.x, b1.y + b2.y);
             bt[(he + k) * tc + c] = make_double2(b1.x - b2.x, b1.y - b2.y);
         } else {
             bt[k * tc + c] = b1;
         }
-        if (sp.rhs_only) Out.p[comp][o1] = b1;
+        if (sp.rhs_only) fptr(Out, comp)[o1] = b1;
     }
     if (sp.rhs_only) return;  // uniform over the block
     __syncthreads();
@@ -344,8 +354,8 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
         const double* __restrict__ GT = ops.HinvF + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * qstride;
         for (int comp = 0; comp < 3; ++comp) {
             const Pair x = inv_apply(GT, tb + comp * tsz, k, c, tc, he, ho);
-            Out.p[comp][(size_t)k * g.nm + m] = x.a;
-            if (k < ho) Out.p[comp][(size_t)(nz - 1 - k) * g.nm + m] = x.b;
+            fptr(Out, comp)[(size_t)k * g.nm + m] = x.a;
+            if (k < ho) fptr(Out, comp)[(size_t)(nz - 1 - k) * g.nm + m] = x.b;
         }
     }
 }
@@ -574,7 +584,7 @@ __global__ void __launch_bounds__(32 * kPcgWarps) k_pcg_helmholtz(GridDev g, Ops
     const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
     const double k2 = __ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
     const double f = sp.helm_f;
-    double* o = reinterpret_cast<double*>(Out.p[comp]);
+    double* o = reinterpret_cast<double*>(fptr(Out, comp));
     const double bc1 = o[2 * (size_t)m + part];
     const double bc2 = o[2 * ((size_t)(nz - 1) * g.nm + m) + part];
     double dg[kPcgRows], bl[kPcgRows], xl[kPcgRows];
@@ -612,16 +622,16 @@ __global__ void k_rk_stage(GridDev g, StepParams sp, double coef, Fields F, Fiel
         const int z = (int)(o / g.nm), m = (int)(o - (size_t)z * g.nm);
         double2 r = make_double2(0.0, 0.0);
         if (z != 0 && z != g.nz - 1) {
-            double2 sv = to_d2(Src.p[comp][o]);
+            double2 sv = to_d2(fptr(Src, comp)[o]);
             if (sp.dealias) {
                 const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
                 const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
                 if (kx > sp.kx_max || kyi > sp.ky_max) sv = make_double2(0.0, 0.0);
             }
-            const double2 fv = F.p[comp][o];
+            const double2 fv = fptr(F, comp)[o];
             r = make_double2(fv.x + coef * sv.x, fv.y + coef * sv.y);
         }
-        Out.p[comp][o] = r;
+        fptr(Out, comp)[o] = r;
     }
 }
 
@@ -870,13 +880,13 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
             float2 se = make_float2(0.f, 0.f), de = se, ss = se, ds = se;
             if (m < g.nm && k < hei) {
                 const size_t o1 = (size_t)(1 + k) * g.nm + m;
-                const double2 a = F.p[comp][o1];
-                const float2 sa = Src.p[comp][o1];
+                const double2 a = fptr(F, comp)[o1];
+                const float2 sa = fptr(Src, comp)[o1];
                 const float ax = (float)a.x, ay = (float)a.y;
                 if (k < hoi) {
                     const size_t o2 = (size_t)(g.nz - 2 - k) * g.nm + m;
-                    const double2 b = F.p[comp][o2];
-                    const float2 sb = Src.p[comp][o2];
+                    const double2 b = fptr(F, comp)[o2];
+                    const float2 sb = fptr(Src, comp)[o2];
                     const float bx = (float)b.x, by = (float)b.y;
                     se = make_float2(ax + bx, ay + by);
                     de = make_float2(ax - bx, ay - by);
@@ -907,7 +917,7 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
                 }
                 k2 = (float)__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
                 if (!keep) k2 = -2.f - k2;  // masked source: flagged by the sign
-                const double2 u0 = F.p[comp][(size_t)m], un = F.p[comp][(size_t)(g.nz - 1) * g.nm + m];
+                const double2 u0 = fptr(F, comp)[(size_t)m], un = fptr(F, comp)[(size_t)(g.nz - 1) * g.nm + m];
                 double2 b1 = make_double2(0.0, 0.0), b2 = b1;
                 if (comp < 2) {
                     const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
@@ -1005,14 +1015,14 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
                 const int i = i0 + q;
                 if (i >= hei) break;
                 const size_t o1 = (size_t)(1 + i) * g.nm + m;
-                const double2 u1 = F.p[comp][o1];
+                const double2 u1 = fptr(F, comp)[o1];
                 if (i < hoi) {
                     const size_t o2 = (size_t)(g.nz - 2 - i) * g.nm + m;
-                    const double2 u2 = F.p[comp][o2];
-                    Out.p[comp][o1] = make_double2(u1.x + (double)(pe[q].x + po[q].x), u1.y + (double)(pe[q].y + po[q].y));
-                    Out.p[comp][o2] = make_double2(u2.x + (double)(pe[q].x - po[q].x), u2.y + (double)(pe[q].y - po[q].y));
+                    const double2 u2 = fptr(F, comp)[o2];
+                    fptr(Out, comp)[o1] = make_double2(u1.x + (double)(pe[q].x + po[q].x), u1.y + (double)(pe[q].y + po[q].y));
+                    fptr(Out, comp)[o2] = make_double2(u2.x + (double)(pe[q].x - po[q].x), u2.y + (double)(pe[q].y - po[q].y));
                 } else {  // middle level (ni odd)
-                    Out.p[comp][o1] = make_double2(u1.x + (double)pe[q].x, u1.y + (double)pe[q].y);
+                    fptr(Out, comp)[o1] = make_double2(u1.x + (double)pe[q].x, u1.y + (double)pe[q].y);
                 }
             }
             if (ib == 0) {  // x_1 = bc1, x_n = bc2 (identity rows)
@@ -1022,7 +1032,7 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
                         const double2 gp = GP[(size_t)(2 * comp + wall) * g.nm + m];
                         bc = make_double2(-sp.dt * gp.x, -sp.dt * gp.y);
                     }
-                    Out.p[comp][(size_t)(wall ? g.nz - 1 : 0) * g.nm + m] = bc;
+                    fptr(Out, comp)[(size_t)(wall ? g.nz - 1 : 0) * g.nm + m] = bc;
                 }
             }
         }
