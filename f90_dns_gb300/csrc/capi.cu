@@ -740,28 +740,80 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             return r;
         };
         const std::vector<float2> D1e_df = split(D1e), D1o_df = split(D1o), W1e_df = split(W1e), W1o_df = split(W1o);
-        // eigenbasis of the full Neumann problem S V' = M V' Lambda'
-        std::vector<double> Cf((size_t)nz * nz), plam, PY;
-        for (int i = 0; i < nz; ++i)
-            for (int j = 0; j < nz; ++j) Cf[(size_t)i * nz + j] = S[(size_t)i * nz + j] / std::sqrt(wh[i] * wh[j]);
-        jacobi_eigen(nz, Cf, plam, PY);
-        std::vector<float> PV((size_t)nz * nzp, 0.f), PVT((size_t)nz * nzp, 0.f), PDVT((size_t)nz * nzp, 0.f),
-            plamf(nz);
-        for (int z = 0; z < nz; ++z)
-            for (int j = 0; j < nz; ++j) {
-                const double v = PY[(size_t)z * nz + j] / std::sqrt(wh[z]);
-                PV[(size_t)z * nzp + j] = (float)v;
-                PVT[(size_t)j * nzp + z] = (float)v;
+        // eigenbasis of the full Neumann problem S V' = M V' Lambda':
+        // C = M^-1/2 S M^-1/2 is centro-symmetric; the orthogonal fold
+        // e_i = (x_i + x_{n-1-i})/sqrt2, o_i = (x_i - x_{n-1-i})/sqrt2 (middle
+        // kept) splits it into Cne (he x he) and Cno (ho x ho)
+        const int he = nz - nz / 2, ho = nz / 2;
+        auto Cn = [&](int i, int j) { return S[(size_t)i * nz + j] / std::sqrt(wh[i] * wh[j]); };
+        std::vector<double> Cne((size_t)he * he), Cno((size_t)std::max(ho, 1) * std::max(ho, 1), 0.0);
+        for (int i = 0; i < he; ++i)
+            for (int j = 0; j < he; ++j) {
+                double v;
+                if (i < ho && j < ho) v = Cn(i, j) + Cn(i, nz - 1 - j);
+                else if (i < ho) v = r2 * Cn(i, ho);  // middle column
+                else if (j < ho) v = r2 * Cn(ho, j);  // middle row
+                else v = Cn(ho, ho);
+                Cne[(size_t)i * he + j] = v;
             }
-        for (int z = 0; z < nz; ++z)
-            for (int j = 0; j < nz; ++j) {
-                double a = 0.0;
-                for (int q = 0; q < nz; ++q) a += D1s[(size_t)z * nz + q] * PY[(size_t)q * nz + j] / std::sqrt(wh[q]);
-                PDVT[(size_t)j * nzp + z] = (float)a;
+        for (int i = 0; i < ho; ++i)
+            for (int j = 0; j < ho; ++j) Cno[(size_t)i * ho + j] = Cn(i, j) - Cn(i, nz - 1 - j);
+        std::vector<double> lne, lno, Yne, Yno;
+        jacobi_eigen(he, Cne, lne, Yne);
+        if (ho > 0) jacobi_eigen(ho, Cno, lno, Yno);
+        const int phe4 = (he + 3) / 4 * 4, pho4 = (ho + 3) / 4 * 4;
+        // v = M^-1/2 Q y: folded weight of row i of an even / odd eigenvector
+        auto fe = [&](int i) { return i < ho ? 1.0 / (r2 * std::sqrt(wh[i])) : 1.0 / std::sqrt(wh[i]); };
+        auto fo = [&](int i) { return 1.0 / (r2 * std::sqrt(wh[i])); };
+        std::vector<float> PAe((size_t)he * phe4, 0.f), PBe((size_t)he * phe4, 0.f), PAo((size_t)std::max(ho, 1) * pho4 + 4, 0.f),
+            PBo((size_t)std::max(ho, 1) * pho4 + 4, 0.f), PDe((size_t)std::max(ho, 1) * phe4 + 4, 0.f),
+            PDo((size_t)he * pho4 + 4, 0.f), plame(phe4, 1.f), plamo(pho4 + 4, 1.f);
+        for (int i = 0; i < he; ++i)
+            for (int j = 0; j < he; ++j) {
+                const double a = Yne[(size_t)i * he + j] * fe(i);
+                PAe[(size_t)i * phe4 + j] = (float)a;  // forward: out j, sum over i
+                PBe[(size_t)j * phe4 + i] = (float)a;  // back: out i, sum over j
             }
-        for (int j = 0; j < nz; ++j) plamf[j] = (float)plam[j];
+        for (int i = 0; i < ho; ++i)
+            for (int j = 0; j < ho; ++j) {
+                const double a = Yno[(size_t)i * ho + j] * fo(i);
+                PAo[(size_t)i * pho4 + j] = (float)a;
+                PBo[(size_t)j * pho4 + i] = (float)a;
+            }
+        // D v for each eigenvector, in FP64 before the one rounding to FP32:
+        // even v -> odd D v (values at i < ho), odd v -> even D v (i < he)
+        {
+            std::vector<double> v(nz), dv(nz);
+            for (int j = 0; j < he; ++j) {
+                for (int i = 0; i < he; ++i) v[i] = Yne[(size_t)i * he + j] * fe(i);
+                for (int i = 0; i < ho; ++i) v[nz - 1 - i] = v[i];
+                for (int z = 0; z < nz; ++z) {
+                    double a = 0.0;
+                    for (int q = 0; q < nz; ++q) a += D1s[(size_t)z * nz + q] * v[q];
+                    dv[z] = a;
+                }
+                for (int i = 0; i < ho; ++i) PDo[(size_t)j * pho4 + i] = (float)dv[i];
+            }
+            for (int j = 0; j < ho; ++j) {
+                std::fill(v.begin(), v.end(), 0.0);
+                for (int i = 0; i < ho; ++i) {
+                    v[i] = Yno[(size_t)i * ho + j] * fo(i);
+                    v[nz - 1 - i] = -v[i];
+                }
+                for (int z = 0; z < nz; ++z) {
+                    double a = 0.0;
+                    for (int q = 0; q < nz; ++q) a += D1s[(size_t)z * nz + q] * v[q];
+                    dv[z] = a;
+                }
+                for (int i = 0; i < he; ++i) PDe[(size_t)j * phe4 + i] = (float)dv[i];
+            }
+        }
+        for (int j = 0; j < he; ++j) plame[j] = (float)lne[j];
+        for (int j = 0; j < ho; ++j) plamo[j] = (float)lno[j];
         MixedOps& mx = h->mx;
         mx.nzp = nzp;
+        mx.phe4 = phe4;
+        mx.pho4 = pho4;
         mx.hei = hei;
         mx.hoi = hoi;
         mx.pe4 = pe4;
@@ -771,8 +823,10 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             (rc = dev_alloc(h, &mx.lam, lamf.size())) || (rc = dev_alloc(h, &mx.s0, s0f.size())) ||
             (rc = dev_alloc(h, &mx.sn, snf.size())) ||
             (rc = dev_alloc(h, &mx.D1e, D1e32.size())) || (rc = dev_alloc(h, &mx.D1o, D1o32.size())) ||
-            (rc = dev_alloc(h, &mx.PV, PV.size())) || (rc = dev_alloc(h, &mx.PVT, PVT.size())) ||
-            (rc = dev_alloc(h, &mx.PDVT, PDVT.size())) || (rc = dev_alloc(h, &mx.plam, nz)) ||
+            (rc = dev_alloc(h, &mx.PAe, PAe.size())) || (rc = dev_alloc(h, &mx.PAo, PAo.size())) ||
+            (rc = dev_alloc(h, &mx.PBe, PBe.size())) || (rc = dev_alloc(h, &mx.PBo, PBo.size())) ||
+            (rc = dev_alloc(h, &mx.PDe, PDe.size())) || (rc = dev_alloc(h, &mx.PDo, PDo.size())) ||
+            (rc = dev_alloc(h, &mx.plame, plame.size())) || (rc = dev_alloc(h, &mx.plamo, plamo.size())) ||
             (rc = dev_alloc(h, &mx.D1e_df, D1e_df.size())) || (rc = dev_alloc(h, &mx.D1o_df, D1o_df.size())) ||
             (rc = dev_alloc(h, &mx.W1e_df, W1e_df.size())) || (rc = dev_alloc(h, &mx.W1o_df, W1o_df.size())) ||
             (rc = dev_alloc(h, &h->PHIZ, se)))
@@ -782,9 +836,11 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             {mx.BeT, BeT.data(), BeT.size() * 4}, {mx.BoT, BoT.data(), BoT.size() * 4},
             {mx.lam, lamf.data(), lamf.size() * 4}, {mx.s0, s0f.data(), s0f.size() * 4},
             {mx.sn, snf.data(), snf.size() * 4}, {mx.D1e, D1e32.data(), D1e32.size() * 4},
-            {mx.D1o, D1o32.data(), D1o32.size() * 4}, {mx.PV, PV.data(), PV.size() * 4},
-            {mx.PVT, PVT.data(), PVT.size() * 4}, {mx.PDVT, PDVT.data(), PDVT.size() * 4},
-            {mx.plam, plamf.data(), (size_t)nz * 4},
+            {mx.D1o, D1o32.data(), D1o32.size() * 4},
+            {mx.PAe, PAe.data(), PAe.size() * 4}, {mx.PAo, PAo.data(), PAo.size() * 4},
+            {mx.PBe, PBe.data(), PBe.size() * 4}, {mx.PBo, PBo.data(), PBo.size() * 4},
+            {mx.PDe, PDe.data(), PDe.size() * 4}, {mx.PDo, PDo.data(), PDo.size() * 4},
+            {mx.plame, plame.data(), plame.size() * 4}, {mx.plamo, plamo.data(), plamo.size() * 4},
             {mx.D1e_df, D1e_df.data(), D1e_df.size() * 8}, {mx.D1o_df, D1o_df.data(), D1o_df.size() * 8},
             {mx.W1e_df, W1e_df.data(), W1e_df.size() * 8}, {mx.W1o_df, W1o_df.data(), W1o_df.size() * 8}};
         for (auto& u : u32)

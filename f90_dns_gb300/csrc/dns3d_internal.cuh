@@ -182,10 +182,21 @@ struct MixedOps {
     float* lam;              // [pe4 + po4] eigenvalues (even block, then odd block)
     float* s0;               // [pe4 + po4] V^T S_I1 in the same order
     float* sn;               // [pe4 + po4] V^T S_In
-    float* PV;               // [nz][nzp]  V'[z][j] stored at [z][j]
-    float* PVT;              // [nz][nzp]  V'[z][j] stored at [j][z]
-    float* PDVT;             // [nz][nzp]  (D V')[z][j] stored at [j][z]
-    float* plam;             // [nz]       eigenvalues l'_j
+    // Neumann eigenbasis S V' = M V' Lambda', folded like the interior one:
+    // even eigenvectors (he of them) act on the folded sums of the right-hand
+    // side, odd ones (ho) on the differences; D V' maps even eigenvectors to
+    // odd functions and odd ones to even functions.  Row blocks padded to
+    // phe4 = pad4(he), pho4 = pad4(ho); every matrix is stored with its
+    // output index innermost:
+    //   PAe [he][phe4]: phi~e_j = sum_i PAe[i][j] s_i   (forward, even)
+    //   PAo [ho][pho4]: phi~o_j = sum_i PAo[i][j] d_i   (forward, odd)
+    //   PBe [he][phe4]: pe_i = sum_j PBe[j][i] phi~e_j  (back, even part)
+    //   PBo [ho][pho4]: po_i = sum_j PBo[j][i] phi~o_j  (back, odd part)
+    //   PDe [ho][phe4]: (dphi/dz) even part from phi~o; PDo [he][pho4]: odd part from phi~e
+    int phe4, pho4;
+    float* PAe; float* PAo; float* PBe; float* PBo; float* PDe; float* PDo;
+    float* plame;            // [phe4] eigenvalues of the even block
+    float* plamo;            // [pho4] eigenvalues of the odd block
 };
 
 struct PIParams {

@@ -1138,9 +1138,10 @@ __device__ __forceinline__ Pair anti_apply_df(const float2* __restrict__ De, con
 // The Neumann Poisson operator is diagonal in the eigenbasis of the full
 // problem, S V' = M V' Lambda', V'^T M V' = I:
 //   phi = -V' diag(1/(l'_j + k^2)) V'^T b,   dphi/dz = -(D V') diag(...) V'^T b
-// evaluated in FP32; computing dphi/dz through the precomputed D V' keeps its
-// FP32 error relative to dphi/dz itself.  Mode (0,0) (pinned) is left to the
-// FP64 kernels.
+// evaluated in FP32 on the folded basis (even eigenvectors on the pair sums
+// of b, odd ones on the differences, MixedOps); computing dphi/dz through the
+// precomputed D V' keeps its FP32 error relative to dphi/dz itself.  Mode
+// (0,0) (pinned) is left to the FP64 kernels.
 __global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
                                                         const double2* __restrict__ US,
                                                         const double2* __restrict__ VS,
@@ -1149,95 +1150,141 @@ __global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, 
                                                         int tc) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nz = g.nz, he = ops.he, ho = ops.ho;
-    const int np = mx.nzp, nb = np / 4;
-    float4* tw = reinterpret_cast<float4*>(smraw);    // folded w* (double-float)  [nz][tc]
-    float2* tb = reinterpret_cast<float2*>(tw + nz * tc);   // rhs b (FP32)  [np][tc]
-    float2* tp = tb + np * tc;                              // phi~ (FP32)  [np][tc]
+    const int pe4 = mx.phe4, po4 = mx.pho4, nbe = pe4 / 4, nbo = po4 / 4;
+    float4* tw = reinterpret_cast<float4*>(smraw);              // folded w* (double-float)  [nz][tc]
+    float2* tb = reinterpret_cast<float2*>(tw + nz * tc);       // folded rhs: s [pe4][tc], d [po4][tc]
+    float2* tp = tb + (pe4 + po4) * tc;                         // phi~: even [pe4][tc], odd [po4][tc]
     const int m0 = blockIdx.x * tc;
     fold_load_df(tw, WS, g, m0, tc, he, ho);
-    for (int t = threadIdx.x; t < (np - nz) * tc; t += blockDim.x) tb[nz * tc + t] = make_float2(0.f, 0.f);
+    for (int t = threadIdx.x; t < (pe4 - he) * tc; t += blockDim.x) tb[he * tc + t] = make_float2(0.f, 0.f);
+    for (int t = threadIdx.x; t < (po4 - ho) * tc; t += blockDim.x) tb[(pe4 + ho) * tc + t] = make_float2(0.f, 0.f);
     __syncthreads();
     const float2* __restrict__ Ae = sp.weak_form ? mx.W1e_df : mx.D1e_df;
     const float2* __restrict__ Ao = sp.weak_form ? mx.W1o_df : mx.D1o_df;
+    // right-hand side pair (k, nz-1-k), folded in FP64 before the rounding
     for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
         const int k = t / tc, c = t - k * tc;
         const int m = m0 + c;
-        if (m >= g.nm || m == 0) {
-            tb[k * tc + c] = make_float2(0.f, 0.f);
-            tb[(nz - 1 - k) * tc + c] = make_float2(0.f, 0.f);
-            continue;
+        float2 fs = make_float2(0.f, 0.f), fd = fs;
+        if (m < g.nm && m != 0) {
+            const Pair dz = anti_apply_df(Ae, Ao, tw, k, c, tc, he, ho);
+            const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+            const double2 b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
+            if (k < ho) {
+                const double2 b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
+                fs = make_float2((float)(b1.x + b2.x), (float)(b1.y + b2.y));
+                fd = make_float2((float)(b1.x - b2.x), (float)(b1.y - b2.y));
+            } else {
+                fs = make_float2((float)b1.x, (float)b1.y);
+            }
         }
-        const Pair dz = anti_apply_df(Ae, Ao, tw, k, c, tc, he, ho);
-        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-        const double2 b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
-        tb[k * tc + c] = make_float2((float)b1.x, (float)b1.y);
-        if (k < ho) {
-            const double2 b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
-            tb[(nz - 1 - k) * tc + c] = make_float2((float)b2.x, (float)b2.y);
-        }
+        tb[k * tc + c] = fs;
+        if (k < ho) tb[(pe4 + k) * tc + c] = fd;
     }
     __syncthreads();
-    // phi~_j = -(V'^T b)_j / (l'_j + k^2) for 4 rows j0..j0+3
-    for (int t = threadIdx.x; t < nb * tc; t += blockDim.x) {
+    // phi~_j = -(V'^T b)_j / (l'_j + k^2), 4 eigen-rows of one block per thread
+    for (int t = threadIdx.x; t < (nbe + nbo) * tc; t += blockDim.x) {
         const int jb = t / tc, c = t - jb * tc;
         const int m = m0 + c;
-        const int j0 = 4 * jb;
+        const bool even = jb < nbe;
+        const int j0 = even ? 4 * jb : 4 * (jb - nbe);
         float2 acc[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[q] = make_float2(0.f, 0.f);
         if (m < g.nm && m != 0) {
-            const float4* __restrict__ A = reinterpret_cast<const float4*>(mx.PV) + jb;  // V'[z][j0..j0+3]
-            for (int z = 0; z < nz; ++z) {
-                const float4 e = __ldg(&A[(size_t)z * nb]);
-                const float2 b = tb[z * tc + c];
-                acc[0].x = fmaf(e.x, b.x, acc[0].x); acc[0].y = fmaf(e.x, b.y, acc[0].y);
-                acc[1].x = fmaf(e.y, b.x, acc[1].x); acc[1].y = fmaf(e.y, b.y, acc[1].y);
-                acc[2].x = fmaf(e.z, b.x, acc[2].x); acc[2].y = fmaf(e.z, b.y, acc[2].y);
-                acc[3].x = fmaf(e.w, b.x, acc[3].x); acc[3].y = fmaf(e.w, b.y, acc[3].y);
+            const int len = even ? he : ho, ld4 = even ? nbe : nbo;
+            const float4* __restrict__ A = reinterpret_cast<const float4*>(even ? mx.PAe : mx.PAo) + j0 / 4;
+            const float2* b = tb + (even ? 0 : pe4 * tc) + c;
+            for (int i = 0; i < len; ++i) {
+                const float4 e = __ldg(&A[(size_t)i * ld4]);
+                const float2 v = b[i * tc];
+                acc[0].x = fmaf(e.x, v.x, acc[0].x); acc[0].y = fmaf(e.x, v.y, acc[0].y);
+                acc[1].x = fmaf(e.y, v.x, acc[1].x); acc[1].y = fmaf(e.y, v.y, acc[1].y);
+                acc[2].x = fmaf(e.z, v.x, acc[2].x); acc[2].y = fmaf(e.z, v.y, acc[2].y);
+                acc[3].x = fmaf(e.w, v.x, acc[3].x); acc[3].y = fmaf(e.w, v.y, acc[3].y);
             }
             const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
             const float k2 = (float)__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+            const float* lam = even ? mx.plame : mx.plamo;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int j = j0 + q;
-                const float sc = j < nz ? -1.0f / (__ldg(&mx.plam[j]) + k2) : 0.f;
+                const float sc = j < len ? -1.0f / (__ldg(&lam[j]) + k2) : 0.f;
                 acc[q] = make_float2(sc * acc[q].x, sc * acc[q].y);
             }
         }
+        float2* dst = tp + (even ? 0 : pe4 * tc) + c;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) tp[(j0 + q) * tc + c] = acc[q];
+        for (int q = 0; q < 4; ++q) dst[(j0 + q) * tc] = acc[q];
     }
     __syncthreads();
-    // phi = V' phi~, dphi/dz = (D V') phi~ for 4 rows z0..z0+3
-    for (int t = threadIdx.x; t < nb * tc; t += blockDim.x) {
-        const int zb = t / tc, c = t - zb * tc;
+    // phi = pe + po, dphi/dz = dze + dzo at levels (i, nz-1-i), 4 rows i per thread:
+    //   pe = PBe phi~e, po = PBo phi~o, dze = PDe phi~o, dzo = PDo phi~e
+    for (int t = threadIdx.x; t < nbe * tc; t += blockDim.x) {
+        const int ib = t / tc, c = t - ib * tc;
         const int m = m0 + c;
         if (m >= g.nm || m == 0) continue;
-        float2 ph[4], pz[4];
+        const int i0 = 4 * ib;
+        float2 pe[4], po[4], de[4], dd[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) { ph[q] = make_float2(0.f, 0.f); pz[q] = ph[q]; }
-        const float4* __restrict__ A = reinterpret_cast<const float4*>(mx.PVT) + zb;    // V'[z0..z0+3][j]
-        const float4* __restrict__ B = reinterpret_cast<const float4*>(mx.PDVT) + zb;   // (D V')[z0..z0+3][j]
-        for (int j = 0; j < nz; ++j) {
-            const float4 a = __ldg(&A[(size_t)j * nb]);
-            const float4 d = __ldg(&B[(size_t)j * nb]);
-            const float2 q2 = tp[j * tc + c];
-            ph[0].x = fmaf(a.x, q2.x, ph[0].x); ph[0].y = fmaf(a.x, q2.y, ph[0].y);
-            ph[1].x = fmaf(a.y, q2.x, ph[1].x); ph[1].y = fmaf(a.y, q2.y, ph[1].y);
-            ph[2].x = fmaf(a.z, q2.x, ph[2].x); ph[2].y = fmaf(a.z, q2.y, ph[2].y);
-            ph[3].x = fmaf(a.w, q2.x, ph[3].x); ph[3].y = fmaf(a.w, q2.y, ph[3].y);
-            pz[0].x = fmaf(d.x, q2.x, pz[0].x); pz[0].y = fmaf(d.x, q2.y, pz[0].y);
-            pz[1].x = fmaf(d.y, q2.x, pz[1].x); pz[1].y = fmaf(d.y, q2.y, pz[1].y);
-            pz[2].x = fmaf(d.z, q2.x, pz[2].x); pz[2].y = fmaf(d.z, q2.y, pz[2].y);
-            pz[3].x = fmaf(d.w, q2.x, pz[3].x); pz[3].y = fmaf(d.w, q2.y, pz[3].y);
+        for (int q = 0; q < 4; ++q) { pe[q] = make_float2(0.f, 0.f); po[q] = pe[q]; de[q] = pe[q]; dd[q] = pe[q]; }
+        const float2* qe = tp + c;
+        const float2* qo = tp + pe4 * tc + c;
+        {
+            const float4* __restrict__ B = reinterpret_cast<const float4*>(mx.PBe) + ib;
+            for (int j = 0; j < he; ++j) {
+                const float4 a = __ldg(&B[(size_t)j * nbe]);
+                const float2 v = qe[j * tc];
+                pe[0].x = fmaf(a.x, v.x, pe[0].x); pe[0].y = fmaf(a.x, v.y, pe[0].y);
+                pe[1].x = fmaf(a.y, v.x, pe[1].x); pe[1].y = fmaf(a.y, v.y, pe[1].y);
+                pe[2].x = fmaf(a.z, v.x, pe[2].x); pe[2].y = fmaf(a.z, v.y, pe[2].y);
+                pe[3].x = fmaf(a.w, v.x, pe[3].x); pe[3].y = fmaf(a.w, v.y, pe[3].y);
+            }
+            const float4* __restrict__ D = reinterpret_cast<const float4*>(mx.PDe) + ib;
+            for (int j = 0; j < ho; ++j) {
+                const float4 a = __ldg(&D[(size_t)j * nbe]);
+                const float2 v = qo[j * tc];
+                de[0].x = fmaf(a.x, v.x, de[0].x); de[0].y = fmaf(a.x, v.y, de[0].y);
+                de[1].x = fmaf(a.y, v.x, de[1].x); de[1].y = fmaf(a.y, v.y, de[1].y);
+                de[2].x = fmaf(a.z, v.x, de[2].x); de[2].y = fmaf(a.z, v.y, de[2].y);
+                de[3].x = fmaf(a.w, v.x, de[3].x); de[3].y = fmaf(a.w, v.y, de[3].y);
+            }
+        }
+        if (ib < nbo) {
+            const float4* __restrict__ B = reinterpret_cast<const float4*>(mx.PBo) + ib;
+            for (int j = 0; j < ho; ++j) {
+                const float4 a = __ldg(&B[(size_t)j * nbo]);
+                const float2 v = qo[j * tc];
+                po[0].x = fmaf(a.x, v.x, po[0].x); po[0].y = fmaf(a.x, v.y, po[0].y);
+                po[1].x = fmaf(a.y, v.x, po[1].x); po[1].y = fmaf(a.y, v.y, po[1].y);
+                po[2].x = fmaf(a.z, v.x, po[2].x); po[2].y = fmaf(a.z, v.y, po[2].y);
+                po[3].x = fmaf(a.w, v.x, po[3].x); po[3].y = fmaf(a.w, v.y, po[3].y);
+            }
+            const float4* __restrict__ D = reinterpret_cast<const float4*>(mx.PDo) + ib;
+            for (int j = 0; j < he; ++j) {
+                const float4 a = __ldg(&D[(size_t)j * nbo]);
+                const float2 v = qe[j * tc];
+                dd[0].x = fmaf(a.x, v.x, dd[0].x); dd[0].y = fmaf(a.x, v.y, dd[0].y);
+                dd[1].x = fmaf(a.y, v.x, dd[1].x); dd[1].y = fmaf(a.y, v.y, dd[1].y);
+                dd[2].x = fmaf(a.z, v.x, dd[2].x); dd[2].y = fmaf(a.z, v.y, dd[2].y);
+                dd[3].x = fmaf(a.w, v.x, dd[3].x); dd[3].y = fmaf(a.w, v.y, dd[3].y);
+            }
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const int z = 4 * zb + q;
-            if (z >= nz) break;
-            const size_t o = (size_t)z * g.nm + m;
-            PHI[o] = make_double2((double)ph[q].x, (double)ph[q].y);
-            PHIZ[o] = make_double2((double)pz[q].x, (double)pz[q].y);
+            const int i = i0 + q;
+            if (i >= he) break;
+            const size_t o1 = (size_t)i * g.nm + m;
+            if (i < ho) {
+                const size_t o2 = (size_t)(nz - 1 - i) * g.nm + m;
+                PHI[o1] = make_double2((double)(pe[q].x + po[q].x), (double)(pe[q].y + po[q].y));
+                PHI[o2] = make_double2((double)(pe[q].x - po[q].x), (double)(pe[q].y - po[q].y));
+                PHIZ[o1] = make_double2((double)(de[q].x + dd[q].x), (double)(de[q].y + dd[q].y));
+                PHIZ[o2] = make_double2((double)(de[q].x - dd[q].x), (double)(de[q].y - dd[q].y));
+            } else {
+                PHI[o1] = make_double2((double)pe[q].x, (double)pe[q].y);
+                PHIZ[o1] = make_double2((double)de[q].x, (double)de[q].y);
+            }
         }
     }
 }
@@ -1429,7 +1476,8 @@ int tile_cols_mixed(const GridDev& g) {
 }
 
 size_t pressure_mixed_smem(const GridDev& g, int tc) {
-    return (size_t)g.nz * tc * sizeof(float4) + 2 * (size_t)pad4(g.nz) * tc * sizeof(float2);
+    const int ho = g.nz / 2, he = g.nz - ho;
+    return (size_t)g.nz * tc * sizeof(float4) + 2 * (size_t)(pad4(he) + pad4(ho)) * tc * sizeof(float2);
 }
 
 cudaError_t prepare_step_kernels(const GridDev& g) {
