@@ -55,7 +55,11 @@ EXPORTED_SYMBOLS = (
     "dns3d_output_flow_statistics", "dns3d_output_spanwise_profile", "dns3d_output_velocity_snapshot",
     "dns3d_output_simulation_summary", "dns3d_write_time_series_data", "dns3d_write_flow_statistics",
     "dns3d_write_spanwise_averaged_profile", "dns3d_write_velocity_field_snapshot",
+    "dns3d_autotune", "dns3d_set_tiles",
 )
+
+TILE_KERNELS = ("vorticity", "viscous", "pressure", "correction", "divergence", "vorticity_mixed",
+                "viscous_mixed", "pressure_mixed")
 
 
 class CConfig(C.Structure):
@@ -225,6 +229,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     for n in ("dns3d_write_time_series_data", "dns3d_write_flow_statistics",
               "dns3d_write_spanwise_averaged_profile", "dns3d_write_velocity_field_snapshot"):
         getattr(lib, n).argtypes = [hp, C.c_char_p]
+    lib.dns3d_autotune.argtypes = [hp, ip, C.POINTER(C.c_int), ip]
+    lib.dns3d_set_tiles.argtypes = [hp, C.POINTER(C.c_int), ip]
     lib.dns3d_last_error.argtypes = [hp]
     lib.dns3d_last_error.restype = C.c_char_p
     for n in EXPORTED_SYMBOLS:
@@ -460,6 +466,25 @@ class ChannelDNS:
         self._check(self.lib.dns3d_load_restart(self._h, os.fsencode(path), C.byref(st), C.byref(tm)),
                     "dns3d_load_restart")
         return int(st.value), float(tm.value)
+
+    def autotune(self, force: bool = False) -> dict:
+        """Re-run the tile autotuner; returns the widths in use per kernel."""
+        t = (C.c_int * len(TILE_KERNELS))()
+        self._check(self.lib.dns3d_autotune(self._h, int(force), t, len(TILE_KERNELS)), "dns3d_autotune")
+        return dict(zip(TILE_KERNELS, list(t)))
+
+    def tiles(self) -> dict:
+        """Tile widths in use per kernel (no tuning)."""
+        t = (C.c_int * len(TILE_KERNELS))()
+        self._check(self.lib.dns3d_autotune(self._h, -1, t, len(TILE_KERNELS)), "dns3d_autotune")
+        return dict(zip(TILE_KERNELS, list(t)))
+
+    def set_tiles(self, **widths) -> None:
+        """Set tile widths by kernel name (0 = built-in heuristic)."""
+        cur = self.tiles()
+        cur.update(widths)
+        t = (C.c_int * len(TILE_KERNELS))(*[int(cur[k]) for k in TILE_KERNELS])
+        self._check(self.lib.dns3d_set_tiles(self._h, t, len(TILE_KERNELS)), "dns3d_set_tiles")
 
     def get_clock(self) -> tuple:
         st, tm = C.c_int(0), C.c_double(0.0)

@@ -6,7 +6,11 @@
 // the per-mode operator inverses.  The five stage entry points run the same
 // kernels that dns3d_step() captures into a CUDA graph.
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -87,6 +91,9 @@ int dev_alloc(dns3d_handle* h, T** p, size_t count) {
     cudaError_t e = cudaMalloc(&q, count * sizeof(T) > 0 ? count * sizeof(T) : 1);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
     h->allocs.push_back(q);
+    // every buffer starts zeroed (work buffers are read by the tile autotuner)
+    e = h->stream ? cudaMemsetAsync(q, 0, count * sizeof(T), h->stream) : cudaMemset(q, 0, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemset");
     *p = static_cast<T*>(q);
     return DNS3D_OK;
 }
@@ -528,6 +535,134 @@ int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
     return DNS3D_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// ------------------------------------------------------------------ autotuner
+// Tile widths (mode columns per CTA) of the mode-tile kernels a handle runs,
+// chosen by timing each candidate width on the handle's own buffers (one
+// warm launch, then three between events on the handle's stream) and kept per
+// (grid, precision, device) for the process, so ensembles and the server tune
+// each grid once.  A width changes only the schedule: every output is one
+// thread's fixed-order sum, so results are bitwise the same for any width.
+using TuneKey = std::tuple<int, int, int, int, int>;
+std::mutex g_tune_mu;
+std::map<TuneKey, std::array<int, kTileKernels>> g_tune;
+
+int tile_launch(dns3d_handle* h, int k) {
+    const GridDev& g = h->g;
+    Fields F{}, S{}, O{}, T{};
+    F.p[0] = h->U; F.p[1] = h->V; F.p[2] = h->W;
+    S.p[0] = h->SU; S.p[1] = h->SV; S.p[2] = h->SW;
+    O.p[0] = h->US; O.p[1] = h->VS; O.p[2] = h->WS;
+    const size_t se = spec_elems(h->cfg);
+    for (int f = 0; f < 5; ++f) T.p[f] = h->fft.tmp + (size_t)f * se;  // scratch for outputs that are state
+    FFields S32{};
+    for (int f = 0; f < 6; ++f) S32.p[f] = h->spec32[f];
+    FFields src32{};
+    for (int f = 0; f < 3; ++f) src32.p[f] = h->src32[f];
+    cudaError_t e = cudaSuccess;
+    switch (k) {
+        case kTileVort: e = launch_vorticity(g, h->ops, h->U, h->V, h->W, h->US, h->VS, h->WS, h->stream); break;
+        case kTileVisc: e = launch_viscous(g, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->stream); break;
+        case kTilePres: e = launch_pressure(g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->stream); break;
+        case kTileCorr:
+            e = launch_correction(g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, T.p[0], T.p[1], T.p[2], T.p[3],
+                                  T.p[4], h->stream);
+            break;
+        case kTileVortM: e = launch_vorticity_mixed(g, h->mx, h->ops, h->U, h->V, h->W, S32, h->stream); break;
+        case kTileViscM: e = launch_viscous_mixed(g, h->mx, h->ops, h->sp, F, src32, h->GP, O, h->stream); break;
+        case kTilePresM:
+            e = launch_pressure_mixed(g, h->mx, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->stream);
+            break;
+        default: return DNS3D_E_INVALID;
+    }
+    CK(h, e);
+    return DNS3D_OK;
+}
+
+int autotune(dns3d_handle* h, bool force) {
+    CK(h, cudaSetDevice(h->cfg.device));
+    const TuneKey key{h->cfg.nx, h->cfg.ny, h->cfg.nz, h->mixed ? 1 : 0, h->cfg.device};
+    if (!force) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            for (int k = 0; k < kTileKernels; ++k) h->g.tc[k] = it->second[k];
+            return DNS3D_OK;
+        }
+    }
+    static const int kFp64[] = {kTileVort, kTileVisc, kTilePres, kTileCorr};
+    static const int kMixed[] = {kTileVortM, kTileViscM, kTilePresM};
+    const int* ks = h->mixed ? kMixed : kFp64;
+    const int nk = h->mixed ? 3 : 4;
+    cudaEvent_t e0, e1;
+    CK(h, cudaEventCreate(&e0));
+    CK(h, cudaEventCreate(&e1));
+    int rc = DNS3D_OK;
+    for (int i = 0; i < nk && !rc; ++i) {
+        const int k = ks[i];
+        int best = 0;
+        float best_ms = 0.f;
+        for (int cand : {4, 8, 16, 32, 64}) {
+            if (!tile_fits(h->g, k, cand)) continue;
+            h->g.tc[k] = cand;
+            if ((rc = tile_launch(h, k))) break;
+            cudaEventRecord(e0, h->stream);
+            for (int r = 0; r < 3 && !rc; ++r) rc = tile_launch(h, k);
+            cudaEventRecord(e1, h->stream);
+            if (rc) break;
+            if (cudaEventSynchronize(e1) != cudaSuccess) { rc = cuda_fail(h, cudaGetLastError(), "autotune"); break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (best == 0 || ms < best_ms) { best = cand; best_ms = ms; }
+        }
+        h->g.tc[k] = best;  // 0 (heuristic) if no candidate fitted
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    h->phys_valid = 0;  // the timing launches reused work buffers
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    std::array<int, kTileKernels> tiles{};
+    for (int k = 0; k < kTileKernels; ++k) tiles[k] = h->g.tc[k];
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = tiles;
+    return DNS3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dns3d_autotune(dns3d_handle* h, int force, int* tiles, int ntiles) {
+    if (!h || ntiles < 0 || (ntiles > 0 && !tiles)) return DNS3D_E_INVALID;
+    if (force >= 0) {
+        const int rc = autotune(h, force != 0);
+        if (rc) return rc;
+    }
+    for (int k = 0; k < ntiles && k < kTileKernels; ++k) tiles[k] = tile_width(h->g, k);
+    return DNS3D_OK;
+}
+
+int dns3d_set_tiles(dns3d_handle* h, const int* tiles, int ntiles) {
+    if (!h || !tiles || ntiles < 0) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    for (int k = 0; k < ntiles && k < kTileKernels; ++k)
+        if (tiles[k] != 0 && !tile_fits(h->g, k, tiles[k])) return DNS3D_E_INVALID;
+    for (int k = 0; k < ntiles && k < kTileKernels; ++k) h->g.tc[k] = tiles[k];
+    if (h->graph) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    return DNS3D_OK;
+}
+
 int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     if (!out) return DNS3D_E_INVALID;
     *out = nullptr;
@@ -877,6 +1012,9 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     pp.inv_nxny_wsum = 1.0 / ((double)c.nx * (double)c.ny * wsum);
 
     if ((rc = dns3d_initialize_fields(h))) return fail(rc);
+    const char* at = std::getenv("DNS3D_AUTOTUNE");
+    if (!(at && std::strcmp(at, "0") == 0))
+        if ((rc = autotune(h, false))) return fail(rc);
     *out = h;
     return DNS3D_OK;
 }

@@ -51,10 +51,16 @@ template <> struct Cx<double> { using type = double2; };
 template <> struct Cx<float> { using type = float2; };
 
 // Grid constants passed by value to kernels.
+// Mode-tile kernels whose tile width (mode columns per CTA) is tunable; the
+// results do not depend on it (every output is one thread's fixed-order sum).
+enum TileKernel { kTileVort = 0, kTileVisc, kTilePres, kTileCorr, kTileDiv, kTileVortM, kTileViscM, kTilePresM,
+                  kTileKernels };
+
 struct GridDev {
     int nx, ny, nz, nxh, nxhp, nm;
     int nkyu;            // ny/2 + 1 unique |ky|
     double inv_nxny;     // 1/(nx*ny), c2r normalisation
+    int tc[kTileKernels];  // chosen tile widths (0: built-in heuristic)
 };
 
 // Maps a spectral mode (ky, kx) to the index of its per-mode operator: the
@@ -210,6 +216,10 @@ struct PIParams {
 // Sets the dynamic shared-memory limits of the kernels below (call once per
 // grid, outside stream capture).
 cudaError_t prepare_step_kernels(const GridDev& g);
+// Tile width of a mode-tile kernel: g.tc[k] if set, else the heuristic; and
+// whether width tc fits the kernel's shared-memory limit.
+int tile_width(const GridDev& g, int k);
+bool tile_fits(const GridDev& g, int k, int tc);
 cudaError_t launch_pi_update(const GridDev& g, const Ops& ops, const PIParams& pp,
                              const double2* U, dns3d_pi_state* pi, cudaStream_t s);
 cudaError_t launch_vorticity(const GridDev& g, const Ops& ops, const double2* U,

@@ -1480,6 +1480,64 @@ size_t pressure_mixed_smem(const GridDev& g, int tc) {
     return (size_t)g.nz * tc * sizeof(float4) + 2 * (size_t)(pad4(he) + pad4(ho)) * tc * sizeof(float2);
 }
 
+namespace {
+
+size_t tile_smem(const GridDev& g, int k, int tc) {
+    const size_t nz = g.nz;
+    switch (k) {
+        case kTileVort: return 2 * nz * tc * sizeof(double2);
+        case kTileVisc: return 6 * nz * tc * sizeof(double2);
+        case kTilePres: return (2 * nz * tc + nz) * sizeof(double2);
+        case kTileCorr: return nz * tc * sizeof(double2);
+        case kTileDiv: return nz * tc * sizeof(double2);
+        case kTileVortM: return 2 * nz * tc * sizeof(float2);
+        case kTileViscM: return viscous_mixed_smem(g, tc);
+        case kTilePresM: return pressure_mixed_smem(g, tc);
+    }
+    return 0;
+}
+
+template <typename K>
+size_t smem_limit(K kern) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) return 0;
+    return (size_t)fa.maxDynamicSharedSizeBytes;
+}
+
+}  // namespace
+
+int tile_width(const GridDev& g, int k) {
+    if (k >= 0 && k < kTileKernels && g.tc[k] > 0) return g.tc[k];
+    switch (k) {
+        case kTileVort: return tile_cols(g, 2);
+        case kTileVisc: return tile_cols(g, 6);
+        case kTilePres: return tile_cols(g, 2);
+        case kTileCorr: return tile_cols(g, 1);
+        case kTileDiv: return tile_cols(g, 1);
+        case kTileVortM: return tile_cols(g, 1);
+        case kTileViscM: return tile_cols_mixed(g);
+        case kTilePresM: return tile_cols(g, 2);
+    }
+    return 8;
+}
+
+bool tile_fits(const GridDev& g, int k, int tc) {
+    if (tc < 1) return false;
+    size_t lim = 0;
+    switch (k) {
+        case kTileVort: lim = smem_limit(k_vorticity); break;
+        case kTileVisc: lim = smem_limit(k_viscous<double2>); break;
+        case kTilePres: lim = smem_limit(k_pressure); break;
+        case kTileCorr: lim = smem_limit(k_correction); break;
+        case kTileDiv: lim = smem_limit(k_divergence); break;
+        case kTileVortM: lim = smem_limit(k_vorticity_mixed); break;
+        case kTileViscM: lim = smem_limit(k_viscous_mixed); break;
+        case kTilePresM: lim = smem_limit(k_pressure_mixed); break;
+        default: return false;
+    }
+    return tile_smem(g, k, tc) <= lim;
+}
+
 cudaError_t prepare_step_kernels(const GridDev& g) {
     cudaError_t e;
     if ((e = set_smem(k_pressure, (2 * (size_t)g.nz + g.nz) * sizeof(double2)))) return e;
@@ -1506,7 +1564,7 @@ cudaError_t launch_pi_update(const GridDev& g, const Ops& ops, const PIParams& p
 
 cudaError_t launch_vorticity(const GridDev& g, const Ops& ops, const double2* U, const double2* V,
                              const double2* W, double2* OX, double2* OY, double2* OZ, cudaStream_t s) {
-    const int tc = tile_cols(g, 2);
+    const int tc = tile_width(g, kTileVort);
     const size_t sm = 2 * (size_t)g.nz * tc * sizeof(double2);
     k_vorticity<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, U, V, W, OX, OY, OZ, tc);
     return cudaGetLastError();
@@ -1523,7 +1581,7 @@ cudaError_t launch_products(const GridDev& g, RFields in6, RFields out3, cudaStr
 cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F,
                            Fields Src, const double2* GP, const dns3d_pi_state* pi, Fields Out,
                            cudaStream_t s) {
-    const int tc = tile_cols(g, 6);
+    const int tc = tile_width(g, kTileVisc);
     const size_t sm = 6 * (size_t)g.nz * tc * sizeof(double2);
     k_viscous<double2><<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, F, Src, GP, pi, Out, tc);
     return cudaGetLastError();
@@ -1531,7 +1589,7 @@ cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& s
 
 cudaError_t launch_vorticity_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const double2* U,
                                    const double2* V, const double2* W, FFields out, cudaStream_t s) {
-    const int tc = tile_cols(g, 1);
+    const int tc = tile_width(g, kTileVortM);
     const size_t sm = 2 * (size_t)g.nz * tc * sizeof(float2);
     k_vorticity_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, U, V, W, out, tc);
     return cudaGetLastError();
@@ -1549,7 +1607,7 @@ cudaError_t launch_pressure_mean_mode(const GridDev& g, const Ops& ops, const St
 cudaError_t launch_pressure_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const StepParams& sp,
                                   const double2* US, const double2* VS, const double2* WS, double2* PHI,
                                   double2* PHIZ, cudaStream_t s) {
-    const int tc = tile_cols(g, 2);
+    const int tc = tile_width(g, kTilePresM);
     const size_t sm = pressure_mixed_smem(g, tc);
     k_pressure_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc);
     return cudaGetLastError();
@@ -1582,7 +1640,7 @@ cudaError_t launch_viscous_mean_mode(const GridDev& g, const Ops& ops, const Ste
 
 cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const StepParams& sp,
                                  Fields F, FFields Src, const double2* GP, Fields Out, cudaStream_t s) {
-    const int tc = tile_cols_mixed(g);
+    const int tc = tile_width(g, kTileViscM);
     const size_t sm = viscous_mixed_smem(g, tc);
     k_viscous_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, F, Src, GP, Out, tc);
     return cudaGetLastError();
@@ -1590,7 +1648,7 @@ cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops
 
 cudaError_t launch_pressure(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
                             const double2* VS, const double2* WS, double2* PHI, cudaStream_t s) {
-    const int tc = tile_cols(g, 2);
+    const int tc = tile_width(g, kTilePres);
     const size_t sm = (2 * (size_t)g.nz * tc + g.nz) * sizeof(double2);
     k_pressure<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, US, VS, WS, PHI, tc);
     return cudaGetLastError();
@@ -1599,7 +1657,7 @@ cudaError_t launch_pressure(const GridDev& g, const Ops& ops, const StepParams& 
 cudaError_t launch_correction(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
                               const double2* VS, const double2* WS, const double2* PHI, double2* U,
                               double2* V, double2* W, double2* P, double2* GP, cudaStream_t s) {
-    const int tc = tile_cols(g, 1);
+    const int tc = tile_width(g, kTileCorr);
     const size_t sm = (size_t)g.nz * tc * sizeof(double2);
     k_correction<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, US, VS, WS, PHI, U, V, W, P, GP, tc);
     return cudaGetLastError();
@@ -1642,7 +1700,7 @@ cudaError_t launch_apply_bc(const GridDev& g, double2* U, double2* V, double2* W
 
 cudaError_t launch_divergence(const GridDev& g, const Ops& ops, const double2* U, const double2* V,
                               const double2* W, double2* DIV, cudaStream_t s) {
-    const int tc = tile_cols(g, 1);
+    const int tc = tile_width(g, kTileDiv);
     const size_t sm = (size_t)g.nz * tc * sizeof(double2);
     k_divergence<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, U, V, W, DIV, tc);
     return cudaGetLastError();

@@ -313,6 +313,22 @@ int dns3d_save_restart(dns3d_handle* h, const char* path, int istep, double time
 int dns3d_load_restart(dns3d_handle* h, const char* path, int* istep, double* time);
 /* The configuration the handle was created with. */
 int dns3d_get_config(dns3d_handle* h, dns3d_config* cfg);
+/* Tile autotuner.  The mode-tile kernels (vorticity, viscous, pressure,
+ * correction, divergence and their mixed forms; DNS3D_TILE_KERNELS of them, in
+ * that order) process a number of mode columns per CTA.  dns3d_create times
+ * the candidate widths 4..64 of the kernels the handle runs on its own buffers
+ * and keeps the fastest, remembered per (grid, precision, device) for the
+ * process; set DNS3D_AUTOTUNE=0 in the environment to keep the built-in
+ * widths.  Results do not depend on the widths (every output is one thread's
+ * fixed-order sum).  dns3d_autotune re-runs the tuning (force = 1 ignores the
+ * remembered choice, force < 0 only reports) and reports the widths in use
+ * (tiles[k], k < ntiles); dns3d_set_tiles sets
+ * them (0 = built-in), DNS3D_E_INVALID if one does not fit the kernel's
+ * shared memory. */
+#define DNS3D_TILE_KERNELS 8
+int dns3d_autotune(dns3d_handle* h, int force, int* tiles, int ntiles);
+int dns3d_set_tiles(dns3d_handle* h, const int* tiles, int ntiles);
+
 /* The handle's step counter and time (dns3d_set_clock, advanced by dns3d_step). */
 int dns3d_get_clock(dns3d_handle* h, int* step, double* time);
 /* LGL nodes (z, ascending from -1) and weights of lgl_module.f90:30-80. */
