@@ -134,6 +134,7 @@ __device__ __forceinline__ void fold_load(double2* tile, const double2* __restri
 __device__ __forceinline__ double2 fold_dot(const double* __restrict__ erow, const double2* in, int len, int tc,
                                             int c) {
     double2 acc = make_double2(0.0, 0.0);
+#pragma unroll 4
     for (int j = 0; j < len; ++j) {
         const double e = __ldg(&erow[j]);
         const double2 a = in[j * tc + c];
@@ -235,6 +236,7 @@ __global__ void k_products(RFields in, RFields out, size_t n) {
 __device__ __forceinline__ Pair inv_apply(const double* __restrict__ GT, const double2* bt, int k, int c, int tc,
                                           int he, int ho) {
     double2 xe = make_double2(0.0, 0.0), xo = xe;
+#pragma unroll 4
     for (int j = 0; j < he; ++j) {
         const double gv = __ldg(&GT[(size_t)j * he + k]);
         const double2 b = bt[j * tc + c];
@@ -244,6 +246,7 @@ __device__ __forceinline__ Pair inv_apply(const double* __restrict__ GT, const d
     Pair p;
     if (k < ho) {
         const double* __restrict__ GoT = GT + (size_t)he * he;
+#pragma unroll 4
         for (int j = 0; j < ho; ++j) {
             const double gv = __ldg(&GoT[(size_t)j * ho + k]);
             const double2 b = bt[(he + j) * tc + c];
@@ -346,6 +349,19 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
     if (sp.rhs_only) return;  // uniform over the block
     __syncthreads();
     const size_t qstride = (size_t)he * he + (size_t)ho * ho;
+    if (tc == 1) {  // a single mode (the mixed form's (0,0) launch): components in parallel
+        for (int t = threadIdx.x; t < 3 * he; t += blockDim.x) {
+            const int comp = t / he, k = t - comp * he;
+            const int m = m0;
+            if (m >= g.nm) continue;
+            const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+            const double* __restrict__ GT = ops.HinvF + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * qstride;
+            const Pair x = inv_apply(GT, tb + comp * tsz, k, 0, 1, he, ho);
+            fptr(Out, comp)[(size_t)k * g.nm + m] = x.a;
+            if (k < ho) fptr(Out, comp)[(size_t)(nz - 1 - k) * g.nm + m] = x.b;
+        }
+        return;
+    }
     for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
         const int c = t / he, k = t - c * he;
         const int m = m0 + c;
@@ -427,6 +443,20 @@ __global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams
     }
     __syncthreads();
     const size_t qstride = (size_t)he * he + (size_t)ho * ho;
+    if (tc == 1 && m0 == 0) {  // the pinned mode alone (the mixed form's launch): one output level per thread
+        for (int z = threadIdx.x; z < nz; z += blockDim.x) {
+            double2 a = make_double2(0.0, 0.0);
+#pragma unroll 4
+            for (int zp = 0; zp < nz; ++zp) {
+                const double2 bb = bpin[zp];
+                const double h1 = __ldg(&ops.PpinT[(size_t)zp * nz + z]);
+                a.x = fma(h1, bb.x, a.x);
+                a.y = fma(h1, bb.y, a.y);
+            }
+            PHI[(size_t)z * g.nm] = a;
+        }
+        return;
+    }
     for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
         const int c = t / he, k = t - c * he;
         const int m = m0 + c;
