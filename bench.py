@@ -269,11 +269,10 @@ def run_ours(args) -> None:
         build.build()
     wl = WORKLOADS[args.workload]
     pts = point_count(wl)
+    if args.noise is not None:
+        wl = dict(wl, noise_amplitude=args.noise)
     cfg = config_from(wl, device=local)
     d = ChannelDNS(cfg)
-    if args.noise > 0:
-        from f90_dns_gb300.workloads import noisy_initial_state
-        noisy_initial_state(d, wl, seed=args.seed, amplitude=args.noise)
     d.step(args.warmup)
     d.synchronize()
 
@@ -441,8 +440,9 @@ def main():
     ap.add_argument("--ensemble-runs", type=int, default=64)
     ap.add_argument("--ensemble-steps", type=int, default=50)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--noise", type=float, default=0.0,
-                    help="seeded white noise amplitude on the initial u, v, w (large workload: 1e-3)")
+    ap.add_argument("--noise", type=float, default=None,
+                    help="white-noise amplitude on the initial u, v, w (default: the workload's; the large "
+                         "workload has 1e-3)")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=4.0)
     ap.add_argument("--serve-round", type=int, default=20)

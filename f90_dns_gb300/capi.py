@@ -87,6 +87,7 @@ class CConfig(C.Structure):
         ("perturbation_seed", C.c_longlong),
         ("convection_scheme", C.c_int), ("linear_solver", C.c_int),
         ("cgstol", C.c_double),
+        ("noise_amplitude", C.c_double),
     ]
 
 

@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "dns3d_internal.cuh"
@@ -120,6 +121,7 @@ int validate(const dns3d_config* c) {
     if (c->linear_solver != 0 && c->linear_solver != 1) return DNS3D_E_INVALID;
     if (c->linear_solver == 1 && !(c->cgstol > 0.0)) return DNS3D_E_INVALID;
     if (c->linear_solver == 1 && c->precision != DNS3D_PREC_FP64) return DNS3D_E_UNSUPPORTED;
+    if (!(c->noise_amplitude >= 0.0)) return DNS3D_E_INVALID;
     return DNS3D_OK;
 }
 
@@ -179,6 +181,36 @@ struct SplitMix64 {
         return (double)(z >> 11) * 0x1.0p-53;
     }
 };
+
+// Philox4x32-10 (Salmon, Moraes, Dror and Shaw, SC'11): ten rounds of
+// (c0, c1, c2, c3) -> (hi(B c2) ^ c1 ^ k0, lo(B c2), hi(A c0) ^ c3 ^ k1, lo(A c0))
+// with A = 0xD2511F53, B = 0xCD9E8D57 and the key bumped by the Weyl
+// constants (0x9E3779B9, 0xBB67AE85) between rounds.
+void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+    }
+}
+
+// The white-noise sample of component comp at point n (C order k, j, i).
+double noise_sample(uint64_t seed, uint64_t n, int comp, double amplitude) {
+    uint32_t c[4] = {(uint32_t)n, (uint32_t)(n >> 32), (uint32_t)comp, 0u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint64_t a = c[0] >> 5, b = c[1] >> 6;  // 27 + 26 bits
+    const double u = (double)(a * 67108864ull + b) * 0x1.0p-53;
+    return amplitude * (2.0 * u - 1.0);
+}
 
 // integrate_with_boundary_conditions_fallback (perturbation_module.f90:
 // 470-517): trapezoid integral of -div upward from w(-1) = 0, a quadratic
@@ -506,6 +538,7 @@ int dns3d_config_defaults(dns3d_config* c) {
     c->convection_scheme = 0;
     c->linear_solver = 0;
     c->cgstol = 1.0e-6;  // 3D:575
+    c->noise_amplitude = 0.0;
     return DNS3D_OK;
 }
 
@@ -1145,6 +1178,24 @@ int dns3d_initialize_fields(dns3d_handle* h) {
         if (rp) return rp;
         const size_t pl = (size_t)h->cfg.nx * h->cfg.ny;
         for (size_t o = 0; o < u.size(); ++o) { u[o] += up[o]; v[o] += vp[o]; w[o] += wp[o]; }
+        for (int k : {0, h->cfg.nz - 1})
+            for (size_t i = 0; i < pl; ++i) { u[k * pl + i] = 0.0; v[k * pl + i] = 0.0; w[k * pl + i] = 0.0; }
+    }
+    if (h->cfg.noise_amplitude > 0.0) {
+        const uint64_t seed = (uint64_t)h->cfg.perturbation_seed;
+        const double a = h->cfg.noise_amplitude;
+        double* f[3] = {u.data(), v.data(), w.data()};
+        const size_t n = u.size();
+        const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (unsigned t = 0; t < nt; ++t)
+            pool.emplace_back([&, t] {
+                const size_t lo = n * t / nt, hi = n * (t + 1) / nt;
+                for (int comp = 0; comp < 3; ++comp)
+                    for (size_t o = lo; o < hi; ++o) f[comp][o] += noise_sample(seed, o, comp, a);
+            });
+        for (auto& th : pool) th.join();
+        const size_t pl = (size_t)h->cfg.nx * h->cfg.ny;
         for (int k : {0, h->cfg.nz - 1})
             for (size_t i = 0; i < pl; ++i) { u[k * pl + i] = 0.0; v[k * pl + i] = 0.0; w[k * pl + i] = 0.0; }
     }

@@ -226,7 +226,8 @@ bool assign(dns3d_config* c, const std::string& group, const std::string& key, c
         LOG_KEY("zero_w_perturbations", zero_w_perturbations)
         LOG_KEY("use_analytical_perturbations", use_analytical_perturbations)
         INT_KEY("analytical_mode_x", analytical_mode_x) INT_KEY("analytical_mode_y", analytical_mode_y)
-        // extension key of this library: seed of the random perturbation
+        // extension keys of this library: white-noise amplitude, perturbation seed
+        REAL_KEY("noise_amplitude", noise_amplitude)
         if (key == "perturbation_seed") {
             long long s64;
             if (!parse_int64(val, s64)) return false;

@@ -53,11 +53,13 @@ WORKLOADS = {
         nx=256, ny=256, nz=97, re=180.0, dt=0.002, flow_control_method=1,
         target_pressure_gradient=2.0 / 180.0, perturbation_amplitude=0.02,
         analytical_mode_x=1, analytical_mode_y=1, nsteps=200),
-    # 512x384x129, Re 180, dt 0.001, PI to 2/3, amplitude 0.08, mode (2,2), 2000 steps
+    # 512x384x129, Re 180, dt 0.001, PI to 2/3, amplitude 0.08, mode (2,2), 2000 steps,
+    # plus seeded white noise of amplitude 1e-3 on u, v, w (Philox, seed 0)
     "channel_512x384x129_re180_pi": _wl(
         nx=512, ny=384, nz=129, re=180.0, dt=0.001, flow_control_method=2,
         target_bulk_velocity=2.0 / 3.0, target_pressure_gradient=2.0 / 180.0,
-        perturbation_amplitude=0.08, analytical_mode_x=2, analytical_mode_y=2, nsteps=2000),
+        perturbation_amplitude=0.08, analytical_mode_x=2, analytical_mode_y=2, nsteps=2000,
+        noise_amplitude=1.0e-3, perturbation_seed=0),
 }
 
 
@@ -82,27 +84,3 @@ def ensemble_draws(n: int = 64, seed: int = 0) -> list[dict]:
 
 def point_count(wl: dict) -> int:
     return int(wl["nx"]) * int(wl["ny"]) * int(wl["nz"])
-
-
-def white_noise(wl: dict, seed: int = 0, amplitude: float = 1.0e-3):
-    """Seeded white noise for the large workload: uniform in [-amplitude,
-    amplitude) on u, v, w at every point (numpy PCG64 stream of `seed`),
-    arrays (nz, ny, nx).  Not a reference feature; it is added to the
-    analytical initial condition and the walls are zeroed again."""
-    rng = np.random.default_rng(seed)
-    shp = (int(wl["nz"]), int(wl["ny"]), int(wl["nx"]))
-    return tuple(rng.uniform(-amplitude, amplitude, shp) for _ in range(3))
-
-
-def noisy_initial_state(d, wl: dict, seed: int = 0, amplitude: float = 1.0e-3) -> None:
-    """Add white_noise() to the analytical initial condition held by the
-    ChannelDNS `d` and re-impose the no-slip walls (planes k=1, nz)."""
-    st = d.get_state(walls=False)
-    noise = white_noise(wl, seed, amplitude)
-    out = {}
-    for k, nz_ in zip(("u", "v", "w"), noise):
-        a = st[k] + nz_
-        a[0] = 0.0
-        a[-1] = 0.0
-        out[k] = a
-    d.set_state(u=out["u"], v=out["v"], w=out["w"])

@@ -93,6 +93,13 @@ typedef struct dns3d_config {
     int convection_scheme;
     int linear_solver;
     double cgstol;                                  /* &simulation cgstol (default 1e-6, 3D:575) */
+    /* Seeded white noise added to the initial u, v, w after the perturbation
+     * (walls zeroed again): uniform in [-noise_amplitude, noise_amplitude),
+     * from Philox4x32-10 (Salmon et al., SC'11) with key perturbation_seed and
+     * counter (point index low, high, component, 0), top 53 bits of the first
+     * two outputs.  Not a reference feature (the large-grid workload's
+     * initial condition); 0 = none.  Extension key of &perturbations. */
+    double noise_amplitude;
 } dns3d_config;
 
 /* PI controller globals (DNS_pressure_BC_3D.f90:75-89). */

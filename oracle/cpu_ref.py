@@ -58,10 +58,20 @@ class CpuChannel:
             setattr(c, n, type(getattr(c, n))(getattr(cfg, n)) if isinstance(getattr(c, n), float)
                     else int(getattr(cfg, n)))
         self.lib = load()
+        # the C restatement builds the analytical initial condition itself;
+        # the random perturbation and the white noise come from dns3d_ref
+        special = (cfg.enable_perturbations and not cfg.use_analytical_perturbations) or \
+            getattr(cfg, "noise_amplitude", 0.0) > 0.0
+        if special:
+            c.enable_perturbations = 0
         self.h = self.lib.cpu_create(C.byref(c), int(threads))
         if not self.h:
             raise RuntimeError("cpu_create failed")
         self.shape = (cfg.nz, cfg.ny, cfg.nx)
+        if special:
+            from . import dns3d_ref as ref
+            st = ref.initial_state(cfg, ref.setup_grid(cfg))
+            self.set_state(u=st.u, v=st.v, w=st.w)
 
     @property
     def threads(self) -> int:

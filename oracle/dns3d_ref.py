@@ -89,6 +89,9 @@ class Config:
     convection_scheme: int = 0
     linear_solver: int = 0
     cgstol: float = 1.0e-6
+    # Not a reference feature: seeded white noise on the initial u, v, w
+    # (the large-grid workload), Philox4x32-10 keyed by perturbation_seed.
+    noise_amplitude: float = 0.0
 
     def with_(self, **kw) -> "Config":
         return replace(self, **kw)
@@ -461,6 +464,37 @@ def random_solenoidal_perturbation(cfg: Config, g: Grid):
     return up * sc, vp * sc, wp * sc
 
 
+def philox4x32_10(ctr, key):
+    """Philox4x32-10 (Salmon, Moraes, Dror and Shaw, SC'11) on arrays of
+    counters ctr = (c0, c1, c2, c3) (uint32 arrays) with key (k0, k1)."""
+    m32 = np.uint64(0xFFFFFFFF)
+    c0, c1, c2, c3 = (np.asarray(x, dtype=np.uint64) for x in ctr)
+    k0, k1 = np.uint64(key[0]), np.uint64(key[1])
+    for r in range(10):
+        if r:
+            k0 = (k0 + np.uint64(0x9E3779B9)) & m32
+            k1 = (k1 + np.uint64(0xBB67AE85)) & m32
+        p0 = np.uint64(0xD2511F53) * c0
+        p1 = np.uint64(0xCD9E8D57) * c2
+        hi0, lo0 = p0 >> np.uint64(32), p0 & m32
+        hi1, lo1 = p1 >> np.uint64(32), p1 & m32
+        c0, c1, c2, c3 = (hi1 ^ c1 ^ k0) & m32, lo1, (hi0 ^ c3 ^ k1) & m32, lo0
+    return c0, c1, c2, c3
+
+
+def philox_noise(seed: int, shape, comp: int, amplitude: float) -> np.ndarray:
+    """Uniform noise in [-amplitude, amplitude) for component comp at every
+    point of `shape` (C order index n): counter (n low, n high, comp, 0), key
+    (seed low, seed high), 53 bits from the first two outputs."""
+    n = np.arange(int(np.prod(shape)), dtype=np.uint64)
+    s = int(seed) % (1 << 64)
+    x0, x1, _, _ = philox4x32_10((n & np.uint64(0xFFFFFFFF), n >> np.uint64(32),
+                                  np.full(n.shape, comp, np.uint64), np.zeros(n.shape, np.uint64)),
+                                 (s & 0xFFFFFFFF, s >> 32))
+    u = ((x0 >> np.uint64(5)) * np.uint64(67108864) + (x1 >> np.uint64(6))).astype(np.float64) * 2.0 ** -53
+    return (amplitude * (2.0 * u - 1.0)).reshape(shape)
+
+
 def initial_state(cfg: Config, g: Grid, noise=None) -> State:
     """initialize_fields_3d (3D:909-962) with the analytical perturbation.
 
@@ -479,6 +513,8 @@ def initial_state(cfg: Config, g: Grid, noise=None) -> State:
         else:
             up, vp, wp = random_solenoidal_perturbation(cfg, g)
         u, v, w = u + up, v + vp, w + wp
+    if noise is None and cfg.noise_amplitude > 0.0:
+        noise = tuple(philox_noise(cfg.perturbation_seed, shape, c, cfg.noise_amplitude) for c in range(3))
     if noise is not None:
         u, v, w = u + noise[0], v + noise[1], w + noise[2]
     if cfg.enable_perturbations or noise is not None:

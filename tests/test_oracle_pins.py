@@ -245,3 +245,22 @@ def test_random_solenoidal_perturbation_properties(zero_w):
     keep = np.ones(g.ny, bool)
     keep[g.ny // 2] = False  # ky = ny/2 is not symmetric in the FFTW order
     assert np.max(np.abs(kd[:, keep, :-1])) < 1e-12 * np.max(np.abs(uh))
+
+
+def test_philox_known_answers():
+    """Philox4x32-10, the published known-answer vectors (Random123 kat_vectors)."""
+    cases = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+             ((0xFFFFFFFF,) * 4, (0xFFFFFFFF, 0xFFFFFFFF), (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+             ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+              (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
+    for ctr, key, want in cases:
+        out = ref.philox4x32_10(tuple(np.array([c], np.uint64) for c in ctr), key)
+        assert tuple(int(o[0]) for o in out) == want
+
+
+def test_philox_noise_range_and_seed():
+    a = ref.philox_noise(3, (5, 6, 7), 0, 1e-3)
+    assert a.shape == (5, 6, 7) and np.all(np.abs(a) <= 1e-3)
+    assert abs(np.mean(a)) < 2e-4 and np.std(a) > 5e-4
+    assert np.max(np.abs(ref.philox_noise(4, (5, 6, 7), 0, 1e-3) - a)) > 1e-4
+    assert np.max(np.abs(ref.philox_noise(3, (5, 6, 7), 1, 1e-3) - a)) > 1e-4
