@@ -139,9 +139,11 @@ def algorithmic_flops(wl: dict) -> dict:
     Per complex mode column (Nm = (nx/2+1) ny columns per z-level) one nz x nz
     real operator costs, folded into its even/odd blocks (he = nz - nz/2,
     ho = nz/2): symmetric 4 (he^2 + ho^2) flops, antisymmetric 8 he ho flops.
-    Per step: vorticity 2 antisymmetric (D.u, D.v); viscous 6 symmetric
-    (3 x D2, 3 x Helmholtz inverse); pressure 1 antisymmetric + 1 symmetric
-    (D.w*, Poisson inverse); correction 1 antisymmetric (D.phi).
+    Per step: vorticity 2 antisymmetric (D.u, D.v); viscous 3 symmetric (the
+    Helmholtz inverse of u, v, w; with Crank-Nicolson the explicit half is
+    folded into the solve, see step.cu, so no D2 application remains);
+    pressure 1 antisymmetric + 1 symmetric (D.w*, Poisson inverse);
+    correction 1 antisymmetric (D.phi).
     Transforms: 9 real 2D FFTs per z-plane at 2.5 n log2 n flops (n = nx ny).
     """
     nx, ny, nz = wl["nx"], wl["ny"], wl["nz"]
@@ -152,7 +154,7 @@ def algorithmic_flops(wl: dict) -> dict:
     anti = 8.0 * he * ho * nm
     n = nx * ny
     fft = 2.5 * n * math.log2(n) * nz
-    out = {"vorticity": 2 * anti, "viscous_helmholtz": 6 * sym, "pressure_poisson": anti + sym,
+    out = {"vorticity": 2 * anti, "viscous_helmholtz": 3 * sym, "pressure_poisson": anti + sym,
            "pressure_correction": anti, "fft_total": 9 * fft}
     out["z_total"] = out["vorticity"] + out["viscous_helmholtz"] + out["pressure_poisson"] + out["pressure_correction"]
     out["total"] = out["z_total"] + out["fft_total"]

@@ -1026,6 +1026,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     sp.dt = c.dt;
     sp.cn_fac = c.use_crank_nicolson ? 0.5 * c.dt / c.re : 0.0;
     sp.helm_f = helm_f;
+    sp.cn_identity = (sp.cn_fac != 0.0 && sp.cn_fac == helm_f) ? 1 : 0;
     sp.forcing_scale = (double)c.nx * (double)c.ny;
     sp.dealias = c.use_dealias_23_rule;
     sp.kx_max = (c.nx / 2) * 2 / 3;

@@ -131,6 +131,7 @@ struct StepParams {
     int kx_max, ky_max;   // 2/3 limits (3D:1169-1170)
     int weak_form;        // use_weak_form_divergence
     int rhs_only;         // viscous/pressure kernels: write the right-hand sides (for jacgs), not the solutions
+    int cn_identity;      // Crank-Nicolson: explicit half folded into the implicit solve (step.cu)
 };
 
 // z-operators in parity-folded form (see step.cu): for nz levels,

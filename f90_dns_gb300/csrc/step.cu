@@ -292,6 +292,41 @@ __device__ __forceinline__ double2 viscous_rhs(const GridDev& g, const Ops& ops,
     return make_double2(rr.x * whz - (s0 * bc1.x + sn * bc2.x), rr.y * whz - (s0 * bc1.y + sn * bc2.y));
 }
 
+// Crank-Nicolson with the explicit half folded into the solve.  LGL
+// quadrature makes the collocation second derivative and the Galerkin
+// stiffness agree on interior rows, w_k (D2 f)_k = -(S f)_k (integration by
+// parts; the Lagrange basis vanishes at the walls), so with the CN factor
+// equal to the implicit one, R_k w_k = 2 w_k f_k - (H f)_k + dt w_k s_k and
+//   F*_I = H_II^{-1} r_I - f_I,
+//   r_k = w_k (2 f_k + dt s_k) - f S_k1 (f_1 + 2 bc1) - f S_kn (f_nz + 2 bc2),
+// the wall data entering twice as in the reference's lifting: one folded
+// inverse per component instead of D2 and the inverse.  H_II^{-1} is A_q^{-1}
+// applied with zero wall entries.  Wall levels of r are zero.
+__device__ __forceinline__ double2 viscous_rhs_cn(const GridDev& g, const Ops& ops, const StepParams& sp, int comp,
+                                                  int z, int m, int ky, int kx, double2 f, double2 s, double2 f1,
+                                                  double2 fn, double2 bc1, double2 bc2, double dpdx) {
+    if (z == 0 || z == g.nz - 1) return make_double2(0.0, 0.0);
+    if (sp.dealias) {  // apply_dealias_truncation (3D:1163-1193)
+        const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
+        if (kx > sp.kx_max || kyi > sp.ky_max) s = make_double2(0.0, 0.0);
+    }
+    if (comp == 0 && m == 0) s.x += dpdx * sp.forcing_scale;  // 3D:1123-1145
+    const double whz = __ldg(&ops.wh[z]);
+    const double s0 = __ldg(&ops.S0[z]), sn = __ldg(&ops.Sn[z]);
+    const double2 l1 = make_double2(f1.x + 2.0 * bc1.x, f1.y + 2.0 * bc1.y);
+    const double2 ln = make_double2(fn.x + 2.0 * bc2.x, fn.y + 2.0 * bc2.y);
+    return make_double2(whz * (2.0 * f.x + sp.dt * s.x) - (s0 * l1.x + sn * ln.x),
+                        whz * (2.0 * f.y + sp.dt * s.y) - (s0 * l1.y + sn * ln.y));
+}
+
+// x_I - f_I at an interior level, the wall value at the walls
+__device__ __forceinline__ double2 viscous_out_cn(const GridDev& g, int z, double2 x, double2 f, double2 bc1,
+                                                  double2 bc2) {
+    if (z == 0) return bc1;
+    if (z == g.nz - 1) return bc2;
+    return make_double2(x.x - f.x, x.y - f.y);
+}
+
 __device__ __forceinline__ double2 to_d2(double2 a) { return a; }
 __device__ __forceinline__ double2 to_d2(float2 a) { return make_double2((double)a.x, (double)a.y); }
 
@@ -306,9 +341,76 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
     double2* tf = sm;             // [3] folded F tiles
     double2* tb = sm + 3 * tsz;   // [3] folded rhs tiles
     const int m0 = blockIdx.x * tc;
-    for (int comp = 0; comp < 3; ++comp) fold_load(tf + comp * tsz, fptr(F, comp), g, m0, tc, he, ho);
+    const bool cn_id = sp.cn_identity && !sp.rhs_only;
+    if (!cn_id)
+        for (int comp = 0; comp < 3; ++comp) fold_load(tf + comp * tsz, fptr(F, comp), g, m0, tc, he, ho);
     __syncthreads();
     const double dpdx = pi->current_pressure_gradient;
+    if (cn_id) {
+        for (int t = threadIdx.x; t < 3 * he * tc; t += blockDim.x) {
+            const int comp = t / (he * tc);
+            const int r = t - comp * he * tc;
+            const int k = r / tc, c = r - k * tc;
+            const int m = m0 + c;
+            double2* bt = tb + comp * tsz;
+            if (m >= g.nm) {
+                bt[k * tc + c] = make_double2(0.0, 0.0);
+                if (k < ho) bt[(he + k) * tc + c] = make_double2(0.0, 0.0);
+                continue;
+            }
+            const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+            double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
+            if (comp < 2) {
+                const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
+                const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
+                bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
+            }
+            const double2* fc = fptr(F, comp);
+            const double2 f1 = fc[m], fn = fc[(size_t)(nz - 1) * g.nm + m];
+            const int z1 = k, z2 = nz - 1 - k;
+            const size_t o1 = (size_t)z1 * g.nm + m, o2 = (size_t)z2 * g.nm + m;
+            const double2 b1 = viscous_rhs_cn(g, ops, sp, comp, z1, m, ky, kx, fc[o1],
+                                              to_d2(fptr(Src, comp)[o1]), f1, fn, bc1, bc2, dpdx);
+            if (k < ho) {
+                const double2 b2 = viscous_rhs_cn(g, ops, sp, comp, z2, m, ky, kx, fc[o2],
+                                                  to_d2(fptr(Src, comp)[o2]), f1, fn, bc1, bc2, dpdx);
+                bt[k * tc + c] = make_double2(b1.x + b2.x, b1.y + b2.y);
+                bt[(he + k) * tc + c] = make_double2(b1.x - b2.x, b1.y - b2.y);
+            } else {
+                bt[k * tc + c] = b1;
+            }
+        }
+        __syncthreads();
+        const size_t qs = (size_t)he * he + (size_t)ho * ho;
+        // one output pair (k, nz-1-k) of one component per thread
+        for (int t = threadIdx.x; t < 3 * he * tc; t += blockDim.x) {
+            const int comp = t / (he * tc);
+            const int r = t - comp * he * tc;
+            const int c = r / he, k = r - c * he;
+            const int m = m0 + c;
+            if (m >= g.nm) continue;
+            const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+            const double* __restrict__ GT = ops.HinvF + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * qs;
+            const Pair x = inv_apply(GT, tb + comp * tsz, k, c, tc, he, ho);
+            double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
+            if (comp < 2 && k == 0) {
+                const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
+                const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
+                bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
+            }
+            const double2* fc = fptr(F, comp);
+            double2* oc = fptr(Out, comp);
+            const size_t o1 = (size_t)k * g.nm + m;
+            oc[o1] = viscous_out_cn(g, k, x.a, fc[o1], bc1, bc2);
+            if (k < ho) {
+                const size_t o2 = (size_t)(nz - 1 - k) * g.nm + m;
+                oc[o2] = viscous_out_cn(g, nz - 1 - k, x.b, fc[o2], bc1, bc2);
+            }
+        }
+        return;
+    }
     for (int t = threadIdx.x; t < 3 * he * tc; t += blockDim.x) {
         const int comp = t / (he * tc);
         const int r = t - comp * he * tc;
