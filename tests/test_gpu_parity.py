@@ -224,3 +224,38 @@ def test_cached_physical_fields_stay_coherent(built_lib):
         b = d.diagnostics()
         for k in ("umax", "vmax", "wmax", "energy"):
             assert abs(getattr(b, k) - getattr(a, k)) <= 1e-13 * abs(getattr(a, k)), k
+
+
+def test_taylor_green_divergence_on_device(built_lib):
+    """test_taylor_green_divergence.f90:64-145 on the library: the divergence
+    diagnostic of a w = 0 Taylor-Green field (spectral dx, dy, LGL dz) is
+    below 1e-12."""
+    wl = dict(C1, nx=32, ny=32, nz=17, xlen=2 * ref.PI, ylen=2 * ref.PI, enable_perturbations=False)
+    cfg = oracle_config(wl)
+    g = ref.setup_grid(cfg)
+    x = np.arange(g.nx) * g.xlen / g.nx
+    y = np.arange(g.ny) * g.ylen / g.ny
+    cz = np.cos(np.pi * g.zpts / 2.0)
+    u = 0.1 * np.sin(x)[None, None, :] * np.cos(y)[None, :, None] * cz[:, None, None]
+    v = -0.1 * np.cos(x)[None, None, :] * np.sin(y)[None, :, None] * cz[:, None, None]
+    with ChannelDNS(config_from(wl)) as d:
+        d.set_state(u=u, v=v, w=np.zeros_like(u))
+        assert d.diagnostics().max_div < 1e-12
+
+
+def test_nonfinite_state_is_reported(built_lib):
+    """A NaN in a host buffer handed to set_state makes the diagnostics return
+    DNS3D_E_NONFINITE (a status, not a fault); the handle stays usable."""
+    from f90_dns_gb300.capi import DNS3D_E_NONFINITE
+    wl = dict(C1, nx=32, ny=16, nz=17)
+    with ChannelDNS(config_from(wl)) as d:
+        st = d.get_state()
+        bad = st["u"].copy()
+        bad[5, 3, 7] = np.nan
+        d.set_state(u=bad)
+        with pytest.raises(Dns3DError) as ei:
+            d.diagnostics()
+        assert ei.value.code == DNS3D_E_NONFINITE
+        d.set_state(u=st["u"])
+        d.step(2)
+        assert np.isfinite(d.diagnostics().energy)

@@ -110,3 +110,32 @@ def test_simulation_summary(tmp_path, method):
         assert "   Restart time:     0.080000" in lines
     else:
         assert "   Restart mode: DISABLED (new simulation)" in lines
+
+
+def test_es_format_property():
+    """Property check over random doubles of all magnitudes: the writer's
+    ES15.6 text equals the oracle's, reads back within half a unit in the
+    sixth decimal, and is always 15 characters."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=300, deadline=None)
+    @hyp.given(st.floats(allow_nan=False, allow_infinity=False, width=64))
+    def check(v):
+        s = _stats(np.random.default_rng(0), 1, [v] * 12)
+        d = capi.CFlowStats()
+        for n, _ in capi.CFlowStats._fields_:
+            setattr(d, n, s[n])
+        import tempfile
+        with tempfile.TemporaryDirectory() as td:
+            capi.output_init(td)
+            capi.output_time_series_row(td, d)
+            row = open(os.path.join(td, "output_time_series.dat")).read().splitlines()[2]
+        assert row == ref.time_series_row(s)
+        field = ref.fortran_es(v, 15, 6)
+        assert len(field) == 15
+        if "*" not in field and abs(v) >= 1e-99 and abs(v) < 1e99:
+            back = float(field)
+            assert abs(back - v) <= 0.5e-6 * abs(v) * 10 + 1e-300
+
+    check()
