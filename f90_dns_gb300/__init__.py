@@ -7,6 +7,7 @@ PI bulk-velocity control) runs on one GPU behind the C-ABI declared in
 ``include/dns3d_capi.h``; :mod:`f90_dns_gb300.capi` binds it from Python.
 """
 from .capi import (  # noqa: F401
+    Batch,
     ChannelDNS,
     Dns3DError,
     Ensemble,

@@ -46,7 +46,9 @@ EXPORTED_SYMBOLS = (
     "dns3d_last_error", "dns3d_step_timed", "dns3d_profile_kernels", "dns3d_launches_per_step",
     "dns3d_measure_fp64_tflops", "dns3d_flow_stats_noalloc",
     "dns3d_ensemble_create", "dns3d_ensemble_destroy", "dns3d_ensemble_size", "dns3d_ensemble_run",
-    "dns3d_ensemble_step", "dns3d_ensemble_step_timed",
+    "dns3d_ensemble_step", "dns3d_ensemble_step_timed", "dns3d_ensemble_info",
+    "dns3d_batch_create", "dns3d_batch_step", "dns3d_batch_synchronize", "dns3d_batch_info",
+    "dns3d_batch_destroy",
     "dns3d_server_opts_defaults", "dns3d_server_create", "dns3d_server_submit", "dns3d_server_poll",
     "dns3d_server_wait", "dns3d_server_result_state", "dns3d_server_release", "dns3d_server_get_stats",
     "dns3d_server_destroy", "dns3d_restart_write", "dns3d_restart_read", "dns3d_save_restart",
@@ -202,6 +204,12 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_ensemble_run.argtypes = [hp, ip, C.POINTER(hp)]
     lib.dns3d_ensemble_step.argtypes = [hp, ip]
     lib.dns3d_ensemble_step_timed.argtypes = [hp, ip, C.POINTER(C.c_double)]
+    lib.dns3d_ensemble_info.argtypes = [hp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.dns3d_batch_create.argtypes = [C.POINTER(hp), ip, ip, C.POINTER(hp)]
+    lib.dns3d_batch_step.argtypes = [hp, ip]
+    lib.dns3d_batch_synchronize.argtypes = [hp]
+    lib.dns3d_batch_info.argtypes = [hp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.dns3d_batch_destroy.argtypes = [hp]
     lib.dns3d_server_opts_defaults.argtypes = [C.POINTER(CServerOpts)]
     lib.dns3d_server_create.argtypes = [C.POINTER(CServerOpts), C.POINTER(hp)]
     lib.dns3d_server_submit.argtypes = [hp, C.POINTER(CConfig), ip, ip, C.POINTER(C.c_longlong)]
@@ -532,10 +540,60 @@ class ChannelDNS:
                            d.max_div, d.time, d.step)
 
 
+BATCH_TUNE = 1
+
+
+class Batch:
+    """Joint stepping of existing runs (``dns3d_batch``): every stage of the
+    step is one ragged kernel launch over all eligible runs of a precision.
+    The runs stay owned by the caller and must outlive the batch."""
+
+    def __init__(self, runs, tune: bool = True):
+        self.lib = load_library()
+        self.runs = list(runs)
+        arr = (C.c_void_p * len(self.runs))(*[r._h for r in self.runs])
+        self._b = C.c_void_p()
+        rc = self.lib.dns3d_batch_create(arr, len(self.runs), BATCH_TUNE if tune else 0, C.byref(self._b))
+        if rc:
+            msg = "; ".join(m for m in (self.lib.dns3d_last_error(r._h).decode() for r in self.runs) if m)
+            raise Dns3DError(rc, "dns3d_batch_create", msg)
+
+    def step(self, nsteps: int = 1) -> None:
+        rc = self.lib.dns3d_batch_step(self._b, int(nsteps))
+        if rc:
+            raise Dns3DError(rc, "dns3d_batch_step")
+
+    def synchronize(self) -> None:
+        rc = self.lib.dns3d_batch_synchronize(self._b)
+        if rc:
+            raise Dns3DError(rc, "dns3d_batch_synchronize")
+
+    def info(self) -> tuple[int, int]:
+        """(kernel launches per step, runs in ragged launches)."""
+        n, r = C.c_int(0), C.c_int(0)
+        rc = self.lib.dns3d_batch_info(self._b, C.byref(n), C.byref(r))
+        if rc:
+            raise Dns3DError(rc, "dns3d_batch_info")
+        return n.value, r.value
+
+    def close(self) -> None:
+        if self._b:
+            self.lib.dns3d_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 class Ensemble:
-    """Independent runs of any grids advanced together: one CUDA graph with a
-    branch per run, launched once per step.  ``run(i)`` is a view of run i
-    (a :class:`ChannelDNS` that the ensemble owns)."""
+    """Independent runs of any grids advanced together: each stage of the
+    step is one ragged kernel launch over all runs of a precision (runs with
+    options outside the ragged stages keep their own launches), one CUDA graph
+    per step.  ``run(i)`` is a view of run i (a :class:`ChannelDNS` that the
+    ensemble owns)."""
 
     def __init__(self, cfgs):
         self.lib = load_library()
@@ -574,6 +632,12 @@ class Ensemble:
         self._check(self.lib.dns3d_ensemble_step_timed(self._e, int(nsteps), C.byref(ms)),
                     "dns3d_ensemble_step_timed")
         return float(ms.value)
+
+    def info(self) -> tuple[int, int]:
+        """(kernel launches per step, runs in ragged launches)."""
+        n, r = C.c_int(0), C.c_int(0)
+        self._check(self.lib.dns3d_ensemble_info(self._e, C.byref(n), C.byref(r)), "dns3d_ensemble_info")
+        return n.value, r.value
 
     def close(self) -> None:
         if self._e:

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "dns3d_internal.cuh"
+#include "ragged.cuh"
 
 using namespace dns3d;
 
@@ -1617,58 +1618,443 @@ int dns3d_lgl_nodes_weights(int nz, double* z, double* w) {
 
 }  // extern "C"
 
+// ------------------------------------------------------------------ batches
+// Joint stepping of independent runs.  Eligible runs of one precision form a
+// group whose step is ten ragged stage launches (ragged.cuh); the others keep
+// their own step bodies, captured beside the groups into the same graph.
+struct dns3d_batch {
+    struct Group {
+        bool mixed = false;
+        std::vector<int> idx;         // runs of the group (indices into runs)
+        std::vector<RunDesc> desc;    // host copies of the descriptors
+        std::vector<int> own_tc;      // per run, the tile widths of its own launches [kTileKernels]
+        RunDesc* d_desc = nullptr;    // [n]
+        int* d_map = nullptr;         // per stage: start [n + 1], order [n]
+        int total[kRsStages] = {};    // CTAs of each stage launch
+        size_t smem[kRsStages] = {};  // dynamic shared memory of each stage launch
+    };
+    std::vector<dns3d_handle*> runs;  // not owned
+    int device = 0;
+    cudaStream_t stream = nullptr;    // the batch's graph runs here
+    cudaStream_t lane[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr, done = nullptr;
+    cudaEvent_t lane_join[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> run_in, run_join;
+    Group grp[2];                     // FP64, mixed
+    std::vector<int> loose;           // runs stepped by their own launches
+    cudaGraphExec_t graph = nullptr;
+    int launches = 0;                 // kernel launches per step
+    std::string err;
+};
+
+namespace {
+
+size_t stage_smem_limit(StageKernel k) {
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, (const void*)k) != cudaSuccess)
+        return 0;
+    return (size_t)optin - fa.sharedSizeBytes;
+}
+
+// Raises every stage kernel's dynamic shared-memory limit to the device's
+// opt-in maximum (a property of the kernel, shared by all batches).
+cudaError_t prepare_stage_kernels() {
+    for (int m = 0; m < 2; ++m)
+        for (int s = 0; s < kRsStages; ++s) {
+            StageKernel k = ragged_kernel(s, m == 1);
+            const size_t lim = stage_smem_limit(k);
+            if (!lim) return cudaErrorInvalidValue;
+            cudaError_t e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim);
+            if (e) return e;
+        }
+    return cudaSuccess;
+}
+
+bool ragged_eligible(const dns3d_handle* h) {
+    return h->fft.use_ct && h->cfg.convection_scheme == 0 && h->cfg.linear_solver == 0;
+}
+
+RunDesc make_desc(const dns3d_handle* h) {
+    RunDesc d{};
+    d.g = h->g;
+    for (int k = 0; k < kTileKernels; ++k) d.g.tc[k] = tile_width(h->g, k);
+    d.ops = h->ops;
+    d.mx = h->mx;
+    d.sp = h->sp;
+    d.pp = h->pp;
+    d.pi = h->d_pi;
+    d.U = h->U; d.V = h->V; d.W = h->W; d.P = h->P; d.GP = h->GP;
+    d.US = h->US; d.VS = h->VS; d.WS = h->WS; d.PHI = h->PHI; d.PHIZ = h->PHIZ;
+    const size_t se = spec_elems(h->cfg);
+    if (h->mixed) {
+        for (int f = 0; f < 6; ++f) {
+            d.spec[f] = h->spec32[f];
+            d.tmp[f] = h->fft.tmp32 + (size_t)f * se;
+            d.phys[f] = h->phys32[f];
+        }
+        for (int f = 0; f < 3; ++f) d.src[f] = h->src32[f];
+        d.tw_ny = h->fft.tw32_ny; d.tw_nx2 = h->fft.tw32_nx2; d.tw_nx = h->fft.tw32_nx;
+    } else {
+        double2* spec[6] = {h->U, h->V, h->W, h->US, h->VS, h->WS};
+        for (int f = 0; f < 6; ++f) {
+            d.spec[f] = spec[f];
+            d.tmp[f] = h->fft.tmp + (size_t)f * se;
+            d.phys[f] = h->phys[f];
+        }
+        d.src[0] = h->SU; d.src[1] = h->SV; d.src[2] = h->SW;
+        d.tw_ny = h->fft.tw_ny; d.tw_nx2 = h->fft.tw_nx2; d.tw_nx = h->fft.tw_nx;
+    }
+    d.ncol = h->sp.dealias ? std::min(h->sp.kx_max + 1, h->g.nxhp) : h->g.nxhp;
+    if (d.ncol < 1) d.ncol = h->g.nxhp;
+    ragged_geometry(d);
+    return d;
+}
+
+int batch_fail(dns3d_batch* b, cudaError_t e, const char* what) {
+    b->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return (e == cudaErrorMemoryAllocation) ? DNS3D_E_OOM : DNS3D_E_CUDA;
+}
+
+#define BK(b, call)                                               \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return batch_fail((b), e_, #call); \
+    } while (0)
+
+// Work maps of every stage for the group's current tile widths: runs ordered
+// by descending nz (the costliest virtual blocks first), then uploaded with
+// the descriptors.
+int group_upload(dns3d_batch* b, dns3d_batch::Group& G) {
+    const int n = (int)G.idx.size();
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int c) { return G.desc[a].g.nz > G.desc[c].g.nz; });
+    std::vector<int> host((size_t)kRsStages * (2 * n + 1));
+    for (int s = 0; s < kRsStages; ++s) {
+        int* start = host.data() + (size_t)s * (2 * n + 1);
+        int* ord = start + n + 1;
+        start[0] = 0;
+        size_t smem = 0;
+        for (int j = 0; j < n; ++j) {
+            const RunDesc& d = G.desc[order[j]];
+            ord[j] = order[j];
+            start[j + 1] = start[j] + ragged_blocks(s, G.mixed, d);
+            smem = std::max(smem, ragged_smem(s, G.mixed, d));
+        }
+        G.total[s] = start[n];
+        G.smem[s] = smem;
+    }
+    BK(b, cudaMemcpyAsync(G.d_desc, G.desc.data(), (size_t)n * sizeof(RunDesc), cudaMemcpyHostToDevice, b->stream));
+    BK(b, cudaMemcpyAsync(G.d_map, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    BK(b, cudaStreamSynchronize(b->stream));
+    return DNS3D_OK;
+}
+
+cudaError_t group_launch(dns3d_batch::Group& G, int s, cudaStream_t st) {
+    const int n = (int)G.idx.size();
+    if (G.total[s] < 1) return cudaSuccess;
+    StageMap map;
+    map.start = G.d_map + (size_t)s * (2 * n + 1);
+    map.order = map.start + n + 1;
+    map.nruns = n;
+    RunDesc* runs = G.d_desc;
+    void* args[] = {&runs, &map};
+    return cudaLaunchKernel((const void*)ragged_kernel(s, G.mixed), dim3((unsigned)G.total[s]),
+                            dim3(kStageThreads), args, G.smem[s], st);
+}
+
+// Stage tile widths for the group: each run's own widths, or one width for
+// all runs, whichever launch is fastest (one warm launch, then three between
+// events).  The stages timed write only work buffers, apart from the PI
+// update in front of the vorticity tiles, whose controller states the caller
+// restores.
+int group_tune(dns3d_batch* b, dns3d_batch::Group& G) {
+    const int n = (int)G.idx.size();
+    cudaEvent_t e0, e1;
+    BK(b, cudaEventCreate(&e0));
+    BK(b, cudaEventCreate(&e1));
+    int rc = DNS3D_OK;
+    for (int s : {(int)kRsVort, (int)kRsVisc, (int)kRsPres}) {
+        const int k = ragged_tile_kernel(s, G.mixed);
+        const size_t lim = stage_smem_limit(ragged_kernel(s, G.mixed));
+        int best = -1;
+        float best_ms = 0.f;
+        for (int cand : {0, 4, 8, 16, 32}) {
+            bool ok = true;
+            for (int i = 0; i < n && ok; ++i) {
+                const int w = cand ? cand : G.own_tc[(size_t)i * kTileKernels + k];
+                G.desc[i].g.tc[k] = w;
+                ok = ragged_smem(s, G.mixed, G.desc[i]) <= lim;
+            }
+            if (!ok) continue;
+            if ((rc = group_upload(b, G))) break;
+            cudaError_t ce = group_launch(G, s, b->stream);
+            if (!ce) ce = cudaEventRecord(e0, b->stream);
+            for (int r = 0; r < 3 && !ce; ++r) ce = group_launch(G, s, b->stream);
+            if (!ce) ce = cudaEventRecord(e1, b->stream);
+            if (!ce) ce = cudaEventSynchronize(e1);
+            if (ce) {
+                rc = batch_fail(b, ce, "batch tuning");
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (best < 0 || ms < best_ms) {
+                best = cand;
+                best_ms = ms;
+            }
+        }
+        if (rc) break;
+        for (int i = 0; i < n; ++i)
+            G.desc[i].g.tc[k] = best > 0 ? best : G.own_tc[(size_t)i * kTileKernels + k];
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    return group_upload(b, G);
+}
+
+void batch_release(dns3d_batch* b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto& G : b->grp) {
+        cudaFree(G.d_desc);
+        cudaFree(G.d_map);
+    }
+    for (auto ev : b->run_in) cudaEventDestroy(ev);
+    for (auto ev : b->run_join) cudaEventDestroy(ev);
+    for (auto ev : b->lane_join)
+        if (ev) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->done) cudaEventDestroy(b->done);
+    for (auto st : b->lane)
+        if (st) cudaStreamDestroy(st);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// One graph per step: fork -> (each group's ten stage launches on its lane,
+// each loose run's step body on its own stream) -> join.
+int batch_capture(dns3d_batch* b) {
+    cudaGraph_t graph = nullptr;
+    BK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = DNS3D_OK;
+    int launches = 0;
+    cudaError_t ce = cudaEventRecord(b->fork, b->stream);
+    for (int gi = 0; gi < 2 && !ce; ++gi) {
+        dns3d_batch::Group& G = b->grp[gi];
+        if (G.idx.empty()) continue;
+        ce = cudaStreamWaitEvent(b->lane[gi], b->fork, 0);
+        for (int s = 0; s < kRsStages && !ce; ++s) {
+            ce = group_launch(G, s, b->lane[gi]);
+            launches += G.total[s] > 0;
+        }
+        if (!ce) ce = cudaEventRecord(b->lane_join[gi], b->lane[gi]);
+        if (!ce) ce = cudaStreamWaitEvent(b->stream, b->lane_join[gi], 0);
+    }
+    for (size_t j = 0; j < b->loose.size() && !ce && !rc; ++j) {
+        const int i = b->loose[j];
+        dns3d_handle* h = b->runs[i];
+        ce = cudaStreamWaitEvent(h->stream, b->fork, 0);
+        if (!ce) rc = run_step_body(h);
+        launches += h->launches;
+        if (!rc && !ce) ce = cudaEventRecord(b->run_join[i], h->stream);
+        if (!rc && !ce) ce = cudaStreamWaitEvent(b->stream, b->run_join[i], 0);
+    }
+    cudaError_t ee = cudaStreamEndCapture(b->stream, &graph);
+    if (rc || ce || ee) {
+        if (graph) cudaGraphDestroy(graph);
+        if (rc) {
+            b->err = b->runs[b->loose.empty() ? 0 : b->loose[0]]->err;
+            return rc;
+        }
+        return batch_fail(b, ce ? ce : ee, "batch capture");
+    }
+    cudaError_t ie = cudaGraphInstantiate(&b->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie) {
+        b->graph = nullptr;
+        return batch_fail(b, ie, "cudaGraphInstantiate (batch)");
+    }
+    BK(b, cudaGraphUpload(b->graph, b->stream));
+    b->launches = launches;
+    return DNS3D_OK;
+}
+
+int batch_create(dns3d_handle* const* runs, int nruns, int flags, dns3d_batch** out) {
+    if (!runs || nruns < 1 || !out) return DNS3D_E_INVALID;
+    *out = nullptr;
+    for (int i = 0; i < nruns; ++i)
+        if (!runs[i] || runs[i]->cfg.device != runs[0]->cfg.device) return DNS3D_E_INVALID;
+    dns3d_batch* b = new dns3d_batch();
+    b->runs.assign(runs, runs + nruns);
+    b->device = runs[0]->cfg.device;
+    int rc = DNS3D_OK;
+    auto fail = [&](int code) {
+        batch_release(b);
+        delete b;
+        return code;
+    };
+    if (cudaSetDevice(b->device) != cudaSuccess) return fail(DNS3D_E_CUDA);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) ||
+        cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming))
+        return fail(DNS3D_E_CUDA);
+    b->run_in.assign(nruns, nullptr);
+    b->run_join.assign(nruns, nullptr);
+    for (int i = 0; i < nruns; ++i)
+        if (cudaEventCreateWithFlags(&b->run_in[i], cudaEventDisableTiming) ||
+            cudaEventCreateWithFlags(&b->run_join[i], cudaEventDisableTiming))
+            return fail(DNS3D_E_CUDA);
+    if (prepare_stage_kernels()) return fail(DNS3D_E_CUDA);
+    // group the eligible runs by precision; a run whose stage launches would
+    // not fit the stage kernels' shared memory keeps its own launches
+    for (int i = 0; i < nruns; ++i) {
+        dns3d_handle* h = runs[i];
+        bool ok = ragged_eligible(h);
+        RunDesc d{};
+        if (ok) {
+            d = make_desc(h);
+            for (int s = 0; s < kRsStages && ok; ++s)
+                ok = ragged_smem(s, h->mixed, d) <= stage_smem_limit(ragged_kernel(s, h->mixed));
+        }
+        if (!ok) {
+            b->loose.push_back(i);
+            continue;
+        }
+        dns3d_batch::Group& G = b->grp[h->mixed ? 1 : 0];
+        G.mixed = h->mixed;
+        G.idx.push_back(i);
+        G.desc.push_back(d);
+        for (int k = 0; k < kTileKernels; ++k) G.own_tc.push_back(d.g.tc[k]);
+    }
+    for (int gi = 0; gi < 2; ++gi) {
+        dns3d_batch::Group& G = b->grp[gi];
+        if (G.idx.empty()) continue;
+        const int n = (int)G.idx.size();
+        if (cudaStreamCreateWithFlags(&b->lane[gi], cudaStreamNonBlocking) ||
+            cudaEventCreateWithFlags(&b->lane_join[gi], cudaEventDisableTiming))
+            return fail(DNS3D_E_CUDA);
+        if (cudaMalloc(&G.d_desc, (size_t)n * sizeof(RunDesc)) ||
+            cudaMalloc(&G.d_map, (size_t)kRsStages * (2 * n + 1) * sizeof(int)))
+            return fail(DNS3D_E_OOM);
+    }
+    // the runs' queued work (state uploads, initial conditions) comes first
+    for (int i = 0; i < nruns; ++i)
+        if (cudaStreamSynchronize(runs[i]->stream)) return fail(DNS3D_E_CUDA);
+    const char* env = std::getenv("DNS3D_AUTOTUNE");
+    const bool tune = (flags & DNS3D_BATCH_TUNE) && !(env && std::strcmp(env, "0") == 0);
+    std::vector<dns3d_pi_state> pis;
+    if (tune) {
+        pis.resize(nruns);
+        for (int i = 0; i < nruns; ++i)
+            if (cudaMemcpy(&pis[i], runs[i]->d_pi, sizeof(dns3d_pi_state), cudaMemcpyDeviceToHost))
+                return fail(DNS3D_E_CUDA);
+    }
+    for (auto& G : b->grp) {
+        if (G.idx.empty()) continue;
+        rc = tune ? group_tune(b, G) : group_upload(b, G);
+        if (rc) {
+            for (dns3d_handle* h : b->runs) h->err = b->err;
+            return fail(rc);
+        }
+    }
+    if (tune) {
+        for (int i = 0; i < nruns; ++i)
+            if (cudaMemcpy(runs[i]->d_pi, &pis[i], sizeof(dns3d_pi_state), cudaMemcpyHostToDevice))
+                return fail(DNS3D_E_CUDA);
+        for (dns3d_handle* h : b->runs) h->phys_valid = 0;
+    }
+    if ((rc = batch_capture(b))) {
+        for (dns3d_handle* h : b->runs) h->err = b->err;
+        return fail(rc);
+    }
+    *out = b;
+    return DNS3D_OK;
+}
+
+int batch_step(dns3d_batch* b, int nsteps) {
+    BK(b, cudaSetDevice(b->device));
+    for (size_t i = 0; i < b->runs.size(); ++i) {
+        BK(b, cudaEventRecord(b->run_in[i], b->runs[i]->stream));
+        BK(b, cudaStreamWaitEvent(b->stream, b->run_in[i], 0));
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        BK(b, cudaGraphLaunch(b->graph, b->stream));
+        for (dns3d_handle* h : b->runs) {
+            h->step += 1;
+            h->time += h->cfg.dt;  // 3D:296
+            h->phys_valid = 0;
+        }
+    }
+    BK(b, cudaEventRecord(b->done, b->stream));
+    for (dns3d_handle* h : b->runs) BK(b, cudaStreamWaitEvent(h->stream, b->done, 0));
+    return DNS3D_OK;
+}
+
+}  // namespace
+
 // ------------------------------------------------------------------ ensembles
 struct dns3d_ensemble {
     std::vector<dns3d_handle*> runs;
-    cudaStream_t origin = nullptr;
-    cudaEvent_t fork = nullptr;
-    std::vector<cudaEvent_t> joins;
-    cudaGraphExec_t graph = nullptr;
+    dns3d_batch* batch = nullptr;  // created at the first step
     int device = 0;
 };
 
 namespace {
 
 void ensemble_release(dns3d_ensemble* e) {
-    if (e->graph) cudaGraphExecDestroy(e->graph);
+    if (e->batch) {
+        cudaStreamSynchronize(e->batch->stream);
+        batch_release(e->batch);
+        delete e->batch;
+        e->batch = nullptr;
+    }
     for (auto* h : e->runs) dns3d_destroy(h);
-    for (auto ev : e->joins) cudaEventDestroy(ev);
-    if (e->fork) cudaEventDestroy(e->fork);
-    if (e->origin) cudaStreamDestroy(e->origin);
 }
 
-// One graph: origin -> fork -> (run i's loop body on run i's stream) -> join.
-int ensemble_capture(dns3d_ensemble* e) {
-    cudaGraph_t graph = nullptr;
-    dns3d_handle* h0 = e->runs[0];
-    CK(h0, cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeThreadLocal));
-    int rc = DNS3D_OK;
-    cudaError_t ce = cudaEventRecord(e->fork, e->origin);
-    for (size_t i = 0; i < e->runs.size() && !rc && ce == cudaSuccess; ++i) {
-        dns3d_handle* h = e->runs[i];
-        ce = cudaStreamWaitEvent(h->stream, e->fork, 0);
-        if (ce == cudaSuccess) rc = run_step_body(h);
-        if (!rc && ce == cudaSuccess) ce = cudaEventRecord(e->joins[i], h->stream);
-        if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(e->origin, e->joins[i], 0);
-    }
-    cudaError_t ee = cudaStreamEndCapture(e->origin, &graph);
-    if (rc || ce != cudaSuccess || ee != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        if (rc) return rc;
-        return cuda_fail(h0, ce != cudaSuccess ? ce : ee, "ensemble capture");
-    }
-    cudaError_t ie = cudaGraphInstantiate(&e->graph, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ie != cudaSuccess) {
-        e->graph = nullptr;
-        return cuda_fail(h0, ie, "cudaGraphInstantiate (ensemble)");
-    }
-    return DNS3D_OK;
+int ensemble_batch(dns3d_ensemble* e) {
+    if (e->batch) return DNS3D_OK;
+    return batch_create(e->runs.data(), (int)e->runs.size(), DNS3D_BATCH_TUNE, &e->batch);
 }
 
 }  // namespace
 
 extern "C" {
+
+int dns3d_batch_create(dns3d_handle* const* runs, int nruns, int flags, dns3d_batch** out) {
+    return batch_create(runs, nruns, flags, out);
+}
+
+int dns3d_batch_step(dns3d_batch* b, int nsteps) {
+    if (!b || nsteps < 0) return DNS3D_E_INVALID;
+    return nsteps ? batch_step(b, nsteps) : DNS3D_OK;
+}
+
+int dns3d_batch_synchronize(dns3d_batch* b) {
+    if (!b) return DNS3D_E_INVALID;
+    BK(b, cudaSetDevice(b->device));
+    BK(b, cudaStreamSynchronize(b->stream));
+    return DNS3D_OK;
+}
+
+int dns3d_batch_info(dns3d_batch* b, int* launches_per_step, int* ragged_runs) {
+    if (!b) return DNS3D_E_INVALID;
+    if (launches_per_step) *launches_per_step = b->launches;
+    if (ragged_runs) *ragged_runs = (int)(b->grp[0].idx.size() + b->grp[1].idx.size());
+    return DNS3D_OK;
+}
+
+int dns3d_batch_destroy(dns3d_batch* b) {
+    if (!b) return DNS3D_E_INVALID;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_release(b);
+    delete b;
+    return DNS3D_OK;
+}
 
 int dns3d_ensemble_create(const dns3d_config* cfgs, int nruns, dns3d_ensemble** out) {
     if (!cfgs || nruns < 1 || !out) return DNS3D_E_INVALID;
@@ -1687,20 +2073,6 @@ int dns3d_ensemble_create(const dns3d_config* cfgs, int nruns, dns3d_ensemble** 
         }
         e->runs.push_back(h);
     }
-    cudaSetDevice(e->device);
-    if (cudaStreamCreateWithFlags(&e->origin, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
-        ensemble_release(e);
-        delete e;
-        return DNS3D_E_CUDA;
-    }
-    e->joins.resize(nruns, nullptr);
-    for (int i = 0; i < nruns; ++i)
-        if (cudaEventCreateWithFlags(&e->joins[i], cudaEventDisableTiming) != cudaSuccess) {
-            ensemble_release(e);
-            delete e;
-            return DNS3D_E_CUDA;
-        }
     *out = e;
     return DNS3D_OK;
 }
@@ -1708,7 +2080,6 @@ int dns3d_ensemble_create(const dns3d_config* cfgs, int nruns, dns3d_ensemble** 
 int dns3d_ensemble_destroy(dns3d_ensemble* e) {
     if (!e) return DNS3D_E_INVALID;
     cudaSetDevice(e->device);
-    if (e->origin) cudaStreamSynchronize(e->origin);
     ensemble_release(e);
     delete e;
     return DNS3D_OK;
@@ -1731,52 +2102,48 @@ int dns3d_ensemble_step(dns3d_ensemble* e, int nsteps) {
     dns3d_handle* h0 = e->runs[0];
     CK(h0, cudaSetDevice(e->device));
     if (nsteps == 0) return DNS3D_OK;
-    // the runs' own streams must be idle before the graph (which orders after
-    // the origin stream only) touches their state
-    for (auto* h : e->runs) CK(h, cudaStreamSynchronize(h->stream));
-    if (!e->graph) {
-        const int rc = ensemble_capture(e);
-        if (rc) return rc;
+    int rc = ensemble_batch(e);
+    if (!rc) rc = batch_step(e->batch, nsteps);
+    if (rc) {
+        if (e->batch) h0->err = e->batch->err;
+        return rc;
     }
-    for (int s = 0; s < nsteps; ++s) {
-        CK(h0, cudaGraphLaunch(e->graph, e->origin));
-        for (auto* h : e->runs) {
-            h->step += 1;
-            h->time += h->cfg.dt;
-            h->phys_valid = 0;
-        }
-    }
-    CK(h0, cudaStreamSynchronize(e->origin));
+    CK(h0, cudaStreamSynchronize(e->batch->stream));
     return DNS3D_OK;
 }
 
 int dns3d_ensemble_step_timed(dns3d_ensemble* e, int nsteps, double* elapsed_ms) {
     if (!e || !elapsed_ms || nsteps < 1) return DNS3D_E_INVALID;
     dns3d_handle* h0 = e->runs[0];
-    if (!e->graph) {
-        const int rc = dns3d_ensemble_step(e, 1);
-        if (rc) return rc;
+    CK(h0, cudaSetDevice(e->device));
+    int rc = ensemble_batch(e);
+    if (rc) return rc;
+    dns3d_batch* b = e->batch;
+    // the runs' own queued work is ordered before the first event
+    for (size_t i = 0; i < b->runs.size(); ++i) {
+        CK(h0, cudaEventRecord(b->run_in[i], b->runs[i]->stream));
+        CK(h0, cudaStreamWaitEvent(b->stream, b->run_in[i], 0));
     }
-    cudaEvent_t a, b;
+    cudaEvent_t a, c;
     CK(h0, cudaEventCreate(&a));
-    CK(h0, cudaEventCreate(&b));
-    CK(h0, cudaEventRecord(a, e->origin));
-    for (int s = 0; s < nsteps; ++s) {
-        CK(h0, cudaGraphLaunch(e->graph, e->origin));
-        for (auto* h : e->runs) {
-            h->step += 1;
-            h->time += h->cfg.dt;
-            h->phys_valid = 0;
-        }
-    }
-    CK(h0, cudaEventRecord(b, e->origin));
-    CK(h0, cudaEventSynchronize(b));
+    CK(h0, cudaEventCreate(&c));
+    CK(h0, cudaEventRecord(a, b->stream));
+    rc = batch_step(b, nsteps);
+    CK(h0, cudaEventRecord(c, b->stream));
+    CK(h0, cudaEventSynchronize(c));
     float ms = 0.f;
-    CK(h0, cudaEventElapsedTime(&ms, a, b));
+    CK(h0, cudaEventElapsedTime(&ms, a, c));
     cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    cudaEventDestroy(c);
     *elapsed_ms = ms;
-    return DNS3D_OK;
+    return rc;
+}
+
+int dns3d_ensemble_info(dns3d_ensemble* e, int* launches_per_step, int* ragged_runs) {
+    if (!e) return DNS3D_E_INVALID;
+    const int rc = ensemble_batch(e);
+    if (rc) return rc;
+    return dns3d_batch_info(e->batch, launches_per_step, ragged_runs);
 }
 
 const char* dns3d_strerror(int code) {

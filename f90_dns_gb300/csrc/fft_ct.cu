@@ -12,8 +12,14 @@
 //    nx/2+1 columns do not fill a CTA waste no lanes.
 // Lengths outside the instantiated set use the generic kernels of fft.cu.
 #include "dns3d_internal.cuh"
+#include "ragged.cuh"
 
 namespace dns3d {
+
+// Instantiated lengths: ny in {16..512}, nx/2 in {16..256}, 2^a 3^b.
+#define DNS3D_CT_Y_LENGTHS(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
+#define DNS3D_CT_X_LENGTHS(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256)
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -166,14 +172,15 @@ __device__ __forceinline__ void ct_fft(C* buf, const C* __restrict__ tw) {
 // with kx < ncol (ncol = nx/2+1, or fewer when the 2/3 filter discards the
 // rest); CX columns per CTA taken from the flattened index plane * ncol + kx.
 // grid (ceil(nplanes * ncol / CX), 1, nf).
+// Block bx of field f; buf holds at least ct_buf_elems(N) values.
 template <int N, int SIGN, typename C>
-__global__ void __launch_bounds__(kThreads) k_fft_y_ct(FieldsT<C> src, FieldsT<C> dst, GridDev g, int nplanes,
-                                                       int ncol, const C* __restrict__ tw) {
+__device__ __forceinline__ void fft_y_body(const FieldsT<C>& src, const FieldsT<C>& dst, const GridDev& g,
+                                           int nplanes, int ncol, const C* __restrict__ tw, int bx, int f,
+                                           C* buf) {
     constexpr int CX = per_cta(N);
     constexpr int LD = N + 1;
-    __shared__ C buf[CX * LD];
     const long long ncols = (long long)nplanes * ncol;
-    const long long vc = (long long)blockIdx.x * CX + (threadIdx.x % CX);
+    const long long vc = (long long)bx * CX + (threadIdx.x % CX);
     const bool live = vc < ncols;
     size_t base = 0;
     if (live) {
@@ -181,8 +188,8 @@ __global__ void __launch_bounds__(kThreads) k_fft_y_ct(FieldsT<C> src, FieldsT<C
         const int kx = (int)(vc - (long long)p * ncol);
         base = (size_t)p * g.nm + kx;
     }
-    const C* __restrict__ s = field_ptr(src, blockIdx.z);
-    C* d = field_ptr(dst, blockIdx.z);
+    const C* __restrict__ s = field_ptr(src, f);
+    C* d = field_ptr(dst, f);
     constexpr int ROWS_PER_ITER = kThreads / CX;  // CX divides kThreads
     constexpr int ITERS = N / ROWS_PER_ITER;
     static_assert(N % ROWS_PER_ITER == 0, "rows split evenly over the threads");
@@ -203,22 +210,29 @@ __global__ void __launch_bounds__(kThreads) k_fft_y_ct(FieldsT<C> src, FieldsT<C
     }
 }
 
+template <int N, int SIGN, typename C>
+__global__ void __launch_bounds__(kThreads) k_fft_y_ct(FieldsT<C> src, FieldsT<C> dst, GridDev g, int nplanes,
+                                                       int ncol, const C* __restrict__ tw) {
+    __shared__ C buf[per_cta(N) * (N + 1)];
+    fft_y_body<N, SIGN, C>(src, dst, g, nplanes, ncol, tw, blockIdx.x, blockIdx.z, buf);
+}
+
 // c2r along x, N = nx/2: RX rows per CTA (row = plane * ny + y).  Packs the
 // nx/2+1 inputs of a row (Re only at kx = 0, nx/2) into Z[k] =
 // (X[k] + conj(X[N-k])) + i e^{+2 pi i k/nx} (X[k] - conj(X[N-k])), runs the
 // inverse length-N transform and writes z[m] = (x[2m], x[2m+1]) / (nx ny).
 template <int N, typename T>
-__global__ void __launch_bounds__(kThreads) k_c2r_x_ct(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst,
-                                                       GridDev g, int nrows,
-                                                       const typename Cx<T>::type* __restrict__ tw_n,
-                                                       const typename Cx<T>::type* __restrict__ tw_nx) {
+__device__ __forceinline__ void c2r_x_body(const FieldsT<typename Cx<T>::type>& src, const FieldsT<T>& dst,
+                                           const GridDev& g, int nrows,
+                                           const typename Cx<T>::type* __restrict__ tw_n,
+                                           const typename Cx<T>::type* __restrict__ tw_nx, int bx, int f,
+                                           typename Cx<T>::type* buf) {
     using C = typename Cx<T>::type;
     constexpr int RX = per_cta(N);
     constexpr int LD = N + 1;
-    __shared__ C buf[RX * LD];
-    const int row0 = blockIdx.x * RX;
-    const C* __restrict__ s = field_ptr(src, blockIdx.y);
-    C* d = reinterpret_cast<C*>(field_ptr(dst, blockIdx.y));
+    const int row0 = bx * RX;
+    const C* __restrict__ s = field_ptr(src, f);
+    C* d = reinterpret_cast<C*>(field_ptr(dst, f));
     const int nxhp = N + 1;
     constexpr int ITERS = RX * N / kThreads;
     static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
@@ -265,21 +279,30 @@ __global__ void __launch_bounds__(kThreads) k_c2r_x_ct(FieldsT<typename Cx<T>::t
     }
 }
 
+template <int N, typename T>
+__global__ void __launch_bounds__(kThreads) k_c2r_x_ct(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst,
+                                                       GridDev g, int nrows,
+                                                       const typename Cx<T>::type* __restrict__ tw_n,
+                                                       const typename Cx<T>::type* __restrict__ tw_nx) {
+    __shared__ typename Cx<T>::type buf[per_cta(N) * (N + 1)];
+    c2r_x_body<N, T>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf);
+}
+
 // r2c along x, N = nx/2: z[m] = x[2m] + i x[2m+1], forward length-N
 // transform, X[k] = E + e^{-2 pi i k/nx} O with E = (Z[k] + conj(Z[N-k]))/2,
 // O = (Z[k] - conj(Z[N-k]))/(2i), k = 0..N.
 template <int N, typename T>
-__global__ void __launch_bounds__(kThreads) k_r2c_x_ct(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst,
-                                                       GridDev g, int nrows,
-                                                       const typename Cx<T>::type* __restrict__ tw_n,
-                                                       const typename Cx<T>::type* __restrict__ tw_nx) {
+__device__ __forceinline__ void r2c_x_body(const FieldsT<T>& src, const FieldsT<typename Cx<T>::type>& dst,
+                                           const GridDev& g, int nrows,
+                                           const typename Cx<T>::type* __restrict__ tw_n,
+                                           const typename Cx<T>::type* __restrict__ tw_nx, int bx, int f,
+                                           typename Cx<T>::type* buf) {
     using C = typename Cx<T>::type;
     constexpr int RX = per_cta(N);
     constexpr int LD = N + 1;
-    __shared__ C buf[RX * LD];
-    const int row0 = blockIdx.x * RX;
-    const C* __restrict__ s = reinterpret_cast<const C*>(field_ptr(src, blockIdx.y));
-    C* d = field_ptr(dst, blockIdx.y);
+    const int row0 = bx * RX;
+    const C* __restrict__ s = reinterpret_cast<const C*>(field_ptr(src, f));
+    C* d = field_ptr(dst, f);
     constexpr int ITERS = RX * N / kThreads;
     static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
     C v[ITERS];
@@ -311,6 +334,123 @@ __global__ void __launch_bounds__(kThreads) k_r2c_x_ct(FieldsT<T> src, FieldsT<t
     }
 }
 
+template <int N, typename T>
+__global__ void __launch_bounds__(kThreads) k_r2c_x_ct(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst,
+                                                       GridDev g, int nrows,
+                                                       const typename Cx<T>::type* __restrict__ tw_n,
+                                                       const typename Cx<T>::type* __restrict__ tw_nx) {
+    __shared__ typename Cx<T>::type buf[per_cta(N) * (N + 1)];
+    r2c_x_body<N, T>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf);
+}
+
+// ------------------------------------------------------------------ ragged stages
+// The four transform passes of the nonlinear term over many runs in one launch
+// (k_stage, ragged.cuh): the transform length is a run property, so each CTA
+// switches to the compile-time kernel body of its run's length and uses one
+// shared buffer sized for the longest.
+__host__ __device__ constexpr int ct_buf_max() {
+    int m = 0;
+#define BUF_MAX(n) m = (per_cta(n) * (n + 1) > m) ? per_cta(n) * (n + 1) : m;
+    DNS3D_CT_Y_LENGTHS(BUF_MAX)
+    DNS3D_CT_X_LENGTHS(BUF_MAX)
+#undef BUF_MAX
+    return m;
+}
+
+// Field f of a descriptor pointer list as field 0 of a FieldsT: the bodies
+// then select field 0, and only the one pointer is held in registers.
+template <typename P>
+__device__ __forceinline__ FieldsT<P> one_field(void* const* p, int f) {
+    FieldsT<P> r;
+#pragma unroll
+    for (int i = 0; i < kMaxFields; ++i) r.p[i] = nullptr;
+    r.p[0] = static_cast<P*>(p[f]);
+    return r;
+}
+
+// y pass: inverse over the six inputs into the scratch fields, or forward in
+// place over the three sources (2/3-filtered columns only).
+template <int SIGN, typename T>
+struct RsFftY {
+    static constexpr int kMinCtas = 3;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        using C = typename Cx<T>::type;
+        __shared__ C buf[ct_buf_max()];
+        const int gx = d.gx[SIGN > 0 ? kRsFftYInv : kRsFftYFwd];
+        const int f = b / gx, bx = b - f * gx;
+        const FieldsT<C> src = one_field<C>(SIGN > 0 ? d.spec : d.src, f);
+        const FieldsT<C> dst = one_field<C>(SIGN > 0 ? d.tmp : d.src, f);
+        const int ncol = SIGN > 0 ? d.g.nxhp : d.ncol;
+        const C* tw = static_cast<const C*>(d.tw_ny);
+        switch (d.g.ny) {
+#define Y_CASE(n) \
+    case n: fft_y_body<n, SIGN, C>(src, dst, d.g, d.g.nz, ncol, tw, bx, 0, buf); break;
+            DNS3D_CT_Y_LENGTHS(Y_CASE)
+#undef Y_CASE
+        }
+    }
+};
+
+template <typename T>
+struct RsC2R {
+    static constexpr int kMinCtas = sizeof(T) == 8 ? 2 : 3;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        using C = typename Cx<T>::type;
+        __shared__ C buf[ct_buf_max()];
+        const int gx = d.gx[kRsFftC2R];
+        const int f = b / gx, bx = b - f * gx;
+        const C* twn = static_cast<const C*>(d.tw_nx2);
+        const C* twx = static_cast<const C*>(d.tw_nx);
+        switch (d.g.nxh) {
+#define X_CASE(n)                                                                                              \
+    case n:                                                                                                    \
+        c2r_x_body<n, T>(one_field<C>(d.tmp, f), one_field<T>(d.phys, f), d.g, d.g.nz * d.g.ny, twn, twx, bx, \
+                         0, buf);                                                                              \
+        break;
+            DNS3D_CT_X_LENGTHS(X_CASE)
+#undef X_CASE
+        }
+    }
+};
+
+template <typename T>
+struct RsR2C {
+    static constexpr int kMinCtas = 3;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        using C = typename Cx<T>::type;
+        __shared__ C buf[ct_buf_max()];
+        const int gx = d.gx[kRsFftR2C];
+        const int f = b / gx, bx = b - f * gx;
+        const C* twn = static_cast<const C*>(d.tw_nx2);
+        const C* twx = static_cast<const C*>(d.tw_nx);
+        switch (d.g.nxh) {
+#define X_CASE(n)                                                                                              \
+    case n:                                                                                                    \
+        r2c_x_body<n, T>(one_field<T>(d.phys, f), one_field<C>(d.src, f), d.g, d.g.nz * d.g.ny, twn, twx, bx, \
+                         0, buf);                                                                              \
+        break;
+            DNS3D_CT_X_LENGTHS(X_CASE)
+#undef X_CASE
+        }
+    }
+};
+
+}  // namespace
+
+int fft_ct_per_cta(int n) { return per_cta(n); }
+
+StageKernel ragged_fft_kernel(int stage, bool mixed) {
+    switch (stage) {
+        case kRsFftYInv: return mixed ? k_stage<RsFftY<+1, float>> : k_stage<RsFftY<+1, double>>;
+        case kRsFftC2R: return mixed ? k_stage<RsC2R<float>> : k_stage<RsC2R<double>>;
+        case kRsFftR2C: return mixed ? k_stage<RsR2C<float>> : k_stage<RsR2C<double>>;
+        case kRsFftYFwd: return mixed ? k_stage<RsFftY<-1, float>> : k_stage<RsFftY<-1, double>>;
+    }
+    return nullptr;
+}
+
+namespace {
+
 template <int SIGN, typename C, int N>
 void launch_y(FieldsT<C> src, FieldsT<C> dst, const GridDev& g, int nplanes, int ncol, int nf, const C* tw,
               cudaStream_t s) {
@@ -338,9 +478,6 @@ void launch_r2c(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, const GridDev
 
 }  // namespace
 
-// Instantiated lengths: ny in {16..512}, nx/2 in {16..256}, 2^a 3^b.
-#define DNS3D_CT_Y_LENGTHS(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
-#define DNS3D_CT_X_LENGTHS(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256)
 
 bool fft_ct_supported(int ny, int nxh) {
     bool y = false, x = false;

@@ -16,6 +16,9 @@
 // and the per-mode solves run out of shared memory with coalesced HBM access
 // along m.
 #include "dns3d_internal.cuh"
+#include "ragged.cuh"
+
+#include <algorithm>
 
 namespace dns3d {
 namespace {
@@ -63,9 +66,9 @@ __device__ __forceinline__ void load_tile(double2* tile, const double2* __restri
 // update_pressure_gradient_3d (3D:2488-2549) called with the namelist istart
 // (3D:1118), and calculate_bulk_velocity_3d (3D:2434-2464) from the (0,0) mode:
 // sum_ij u(i,j,k) = Re U[k][0][0].
-__global__ void k_pi_update(GridDev g, const double* __restrict__ zw, PIParams pp,
-                            const double2* __restrict__ U, dns3d_pi_state* pi) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void pi_update_body(GridDev g, const double* __restrict__ zw, PIParams pp,
+                                               const double2* __restrict__ U, dns3d_pi_state* pi, int bx) {
+    if (threadIdx.x != 0 || bx != 0) return;
     if (pp.method == 1) {
         pi->current_pressure_gradient = pp.target_dpdx;
         return;
@@ -92,6 +95,11 @@ __global__ void k_pi_update(GridDev g, const double* __restrict__ zw, PIParams p
     pi->pressure_gradient_sum += clamped;
     pi->pressure_gradient_count += 1;
     pi->avg_pressure_gradient = pi->pressure_gradient_sum / (double)pi->pressure_gradient_count;
+}
+
+__global__ void k_pi_update(GridDev g, const double* __restrict__ zw, PIParams pp,
+                            const double2* __restrict__ U, dns3d_pi_state* pi) {
+    pi_update_body(g, zw, pp, U, pi, blockIdx.x);
 }
 
 // ------------------------------------------------------------------ parity folding
@@ -182,16 +190,16 @@ __device__ __forceinline__ double2 c2sub(double2 a, double2 b) { return make_dou
 
 // ------------------------------------------------------------------ vorticity
 // omega = (wy - vz, uz - wx, vx - uy)  (3D:1077-1079), spectrally.
-__global__ void __launch_bounds__(256) k_vorticity(GridDev g, Ops ops, const double2* __restrict__ U,
-                                                   const double2* __restrict__ V,
-                                                   const double2* __restrict__ W,
-                                                   double2* __restrict__ OX, double2* __restrict__ OY,
-                                                   double2* __restrict__ OZ, int tc) {
+__device__ __forceinline__ void vorticity_body(GridDev g, Ops ops, const double2* __restrict__ U,
+                                               const double2* __restrict__ V,
+                                               const double2* __restrict__ W,
+                                               double2* __restrict__ OX, double2* __restrict__ OY,
+                                               double2* __restrict__ OZ, int tc, int bx) {
     extern __shared__ double2 sm[];
     const int nz = g.nz, he = ops.he, ho = ops.ho;
     double2* tu = sm;
     double2* tv = sm + nz * tc;
-    const int m0 = blockIdx.x * tc;
+    const int m0 = bx * tc;
     fold_load(tu, U, g, m0, tc, he, ho);
     fold_load(tv, V, g, m0, tc, he, ho);
     __syncthreads();
@@ -216,17 +224,29 @@ __global__ void __launch_bounds__(256) k_vorticity(GridDev g, Ops ops, const dou
     }
 }
 
+__global__ void __launch_bounds__(256) k_vorticity(GridDev g, Ops ops, const double2* __restrict__ U,
+                                                   const double2* __restrict__ V,
+                                                   const double2* __restrict__ W,
+                                                   double2* __restrict__ OX, double2* __restrict__ OY,
+                                                   double2* __restrict__ OZ, int tc) {
+    vorticity_body(g, ops, U, V, W, OX, OY, OZ, tc, blockIdx.x);
+}
+
 // ------------------------------------------------------------------ products
 // S = u x omega (3D:1085-1095) on physical fields: in = u,v,w,ox,oy,oz.
-__global__ void k_products(RFields in, RFields out, size_t n) {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+__device__ __forceinline__ void products_body(RFields in, RFields out, size_t n, int bx, int gx) {
+    const size_t stride = (size_t)gx * blockDim.x;
+    for (size_t i = (size_t)bx * blockDim.x + threadIdx.x; i < n; i += stride) {
         const double u = in.p[0][i], v = in.p[1][i], w = in.p[2][i];
         const double ox = in.p[3][i], oy = in.p[4][i], oz = in.p[5][i];
         out.p[0][i] = v * oz - w * oy;
         out.p[1][i] = w * ox - u * oz;
         out.p[2][i] = u * oy - v * ox;
     }
+}
+
+__global__ void k_products(RFields in, RFields out, size_t n) {
+    products_body(in, out, n, blockIdx.x, gridDim.x);
 }
 
 // Per-mode folded inverse x = G b for the output pair k of column c:
@@ -331,16 +351,16 @@ __device__ __forceinline__ double2 to_d2(double2 a) { return a; }
 __device__ __forceinline__ double2 to_d2(float2 a) { return make_double2((double)a.x, (double)a.y); }
 
 template <typename SrcC>
-__global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams sp, Fields F,
-                                                 FieldsT<SrcC> Src, const double2* __restrict__ GP,
-                                                 const dns3d_pi_state* __restrict__ pi, Fields Out,
-                                                 int tc) {
+__device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, Fields F,
+                                             FieldsT<SrcC> Src, const double2* __restrict__ GP,
+                                             const dns3d_pi_state* __restrict__ pi, Fields Out,
+                                             int tc, int bx) {
     extern __shared__ double2 sm[];
     const int nz = g.nz, he = ops.he, ho = ops.ho;
     const int tsz = nz * tc;
     double2* tf = sm;             // [3] folded F tiles
     double2* tb = sm + 3 * tsz;   // [3] folded rhs tiles
-    const int m0 = blockIdx.x * tc;
+    const int m0 = bx * tc;
     const bool cn_id = sp.cn_identity && !sp.rhs_only;
     if (!cn_id)
         for (int comp = 0; comp < 3; ++comp) fold_load(tf + comp * tsz, fptr(F, comp), g, m0, tc, he, ho);
@@ -478,6 +498,14 @@ __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams 
     }
 }
 
+template <typename SrcC>
+__global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams sp, Fields F,
+                                                 FieldsT<SrcC> Src, const double2* __restrict__ GP,
+                                                 const dns3d_pi_state* __restrict__ pi, Fields Out,
+                                                 int tc) {
+    viscous_body<SrcC>(g, ops, sp, F, Src, GP, pi, Out, tc, blockIdx.x);
+}
+
 // ------------------------------------------------------------------ pressure
 // solve_pressure_3d_standard (3D:1654-1733): b = (DX u* + DY v* + Dz w*)/dt *
 // w ybar/2; or _weak_form (3D:1749-1835): b = (-(DX u* + DY v*) w ybar/2 -
@@ -504,18 +532,18 @@ __device__ __forceinline__ double2 pressure_rhs(const GridDev& g, const Ops& ops
     return b;
 }
 
-__global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams sp,
-                                                  const double2* __restrict__ US,
-                                                  const double2* __restrict__ VS,
-                                                  const double2* __restrict__ WS,
-                                                  double2* __restrict__ PHI, int tc) {
+__device__ __forceinline__ void pressure_body(GridDev g, Ops ops, StepParams sp,
+                                              const double2* __restrict__ US,
+                                              const double2* __restrict__ VS,
+                                              const double2* __restrict__ WS,
+                                              double2* __restrict__ PHI, int tc, int bx) {
     extern __shared__ double2 sm[];
     const int nz = g.nz, he = ops.he, ho = ops.ho;
     const int tsz = nz * tc;
     double2* tw = sm;            // folded w* tile
     double2* tb = sm + tsz;      // folded rhs tile
     double2* bpin = sm + 2 * tsz;  // unfolded rhs of mode (0,0)
-    const int m0 = blockIdx.x * tc;
+    const int m0 = bx * tc;
     fold_load(tw, WS, g, m0, tc, he, ho);
     __syncthreads();
     const double* __restrict__ Ae = sp.weak_form ? ops.W1e : ops.D1e;
@@ -582,6 +610,14 @@ __global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams
         PHI[(size_t)k * g.nm + m] = x.a;
         if (k < ho) PHI[(size_t)(nz - 1 - k) * g.nm + m] = x.b;
     }
+}
+
+__global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams sp,
+                                                  const double2* __restrict__ US,
+                                                  const double2* __restrict__ VS,
+                                                  const double2* __restrict__ WS,
+                                                  double2* __restrict__ PHI, int tc) {
+    pressure_body(g, ops, sp, US, VS, WS, PHI, tc, blockIdx.x);
 }
 
 __device__ __forceinline__ double warp_max(double v) {
@@ -770,18 +806,18 @@ __global__ void k_rk_stage(GridDev g, StepParams sp, double coef, Fields F, Fiel
 // ------------------------------------------------------------------ correction
 // pressure_correction_3d (3D:1903-1929): u = u* - dt grad(phi), p += phi,
 // grad_p_prev = grad(p_total); only its wall planes are consumed (3D:1325-1326).
-__global__ void __launch_bounds__(256) k_correction(GridDev g, Ops ops, StepParams sp,
-                                                    const double2* __restrict__ US,
-                                                    const double2* __restrict__ VS,
-                                                    const double2* __restrict__ WS,
-                                                    const double2* __restrict__ PHI,
-                                                    double2* __restrict__ U, double2* __restrict__ V,
-                                                    double2* __restrict__ W, double2* __restrict__ P,
-                                                    double2* __restrict__ GP, int tc) {
+__device__ __forceinline__ void correction_body(GridDev g, Ops ops, StepParams sp,
+                                                const double2* __restrict__ US,
+                                                const double2* __restrict__ VS,
+                                                const double2* __restrict__ WS,
+                                                const double2* __restrict__ PHI,
+                                                double2* __restrict__ U, double2* __restrict__ V,
+                                                double2* __restrict__ W, double2* __restrict__ P,
+                                                double2* __restrict__ GP, int tc, int bx) {
     extern __shared__ double2 sm[];
     const int nz = g.nz, he = ops.he, ho = ops.ho;
     double2* tp = sm;
-    const int m0 = blockIdx.x * tc;
+    const int m0 = bx * tc;
     fold_load(tp, PHI, g, m0, tc, he, ho);
     __syncthreads();
     const double dt = sp.dt;
@@ -815,6 +851,17 @@ __global__ void __launch_bounds__(256) k_correction(GridDev g, Ops ops, StepPara
     }
 }
 
+__global__ void __launch_bounds__(256) k_correction(GridDev g, Ops ops, StepParams sp,
+                                                    const double2* __restrict__ US,
+                                                    const double2* __restrict__ VS,
+                                                    const double2* __restrict__ WS,
+                                                    const double2* __restrict__ PHI,
+                                                    double2* __restrict__ U, double2* __restrict__ V,
+                                                    double2* __restrict__ W, double2* __restrict__ P,
+                                                    double2* __restrict__ GP, int tc) {
+    correction_body(g, ops, sp, US, VS, WS, PHI, U, V, W, P, GP, tc, blockIdx.x);
+}
+
 // Wall-plane gradients of p_total alone (used when the state is set).
 __global__ void k_grad_walls(GridDev g, Ops ops, const double2* __restrict__ P, double2* __restrict__ GP) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -829,8 +876,8 @@ __global__ void k_grad_walls(GridDev g, Ops ops, const double2* __restrict__ P, 
 
 // apply_boundary_conditions_3d (3D:1953-1972): wall planes := 0 (the wall
 // arrays are all zero, 3D:987-999), i.e. spectral planes k=1, nz := 0.
-__global__ void k_apply_bc(GridDev g, double2* U, double2* V, double2* W) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void apply_bc_body(GridDev g, double2* U, double2* V, double2* W, int bx) {
+    const int i = bx * blockDim.x + threadIdx.x;
     if (i >= 2 * g.nm) return;
     const int wall = i / g.nm, m = i - wall * g.nm;
     const size_t o = (size_t)(wall ? g.nz - 1 : 0) * g.nm + m;
@@ -838,6 +885,10 @@ __global__ void k_apply_bc(GridDev g, double2* U, double2* V, double2* W) {
     U[o] = z;
     V[o] = z;
     W[o] = z;
+}
+
+__global__ void k_apply_bc(GridDev g, double2* U, double2* V, double2* W) {
+    apply_bc_body(g, U, V, W, blockIdx.x);
 }
 
 // Divergence spectrum DX u + DY v + Dz w (compute_divergence_3d, 3D:1858-1879).
@@ -907,15 +958,15 @@ __device__ __forceinline__ float2 fold_dot32(const float* __restrict__ erow, con
     return acc;
 }
 
-__global__ void __launch_bounds__(256) k_vorticity_mixed(GridDev g, MixedOps mx, Ops ops,
-                                                         const double2* __restrict__ U,
-                                                         const double2* __restrict__ V,
-                                                         const double2* __restrict__ W, FFields out, int tc) {
+__device__ __forceinline__ void vorticity_mixed_body(GridDev g, MixedOps mx, Ops ops,
+                                                     const double2* __restrict__ U,
+                                                     const double2* __restrict__ V,
+                                                     const double2* __restrict__ W, FFields out, int tc, int bx) {
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* tu = reinterpret_cast<float2*>(smraw);
     const int nz = g.nz, he = ops.he, ho = ops.ho;
     float2* tv = tu + nz * tc;
-    const int m0 = blockIdx.x * tc;
+    const int m0 = bx * tc;
     fold_load32(tu, U, g, m0, tc, he, ho);
     fold_load32(tv, V, g, m0, tc, he, ho);
     __syncthreads();
@@ -953,15 +1004,26 @@ __global__ void __launch_bounds__(256) k_vorticity_mixed(GridDev g, MixedOps mx,
     }
 }
 
-__global__ void k_products32(FRFields in, FRFields out, size_t n) {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+__global__ void __launch_bounds__(256) k_vorticity_mixed(GridDev g, MixedOps mx, Ops ops,
+                                                         const double2* __restrict__ U,
+                                                         const double2* __restrict__ V,
+                                                         const double2* __restrict__ W, FFields out, int tc) {
+    vorticity_mixed_body(g, mx, ops, U, V, W, out, tc, blockIdx.x);
+}
+
+__device__ __forceinline__ void products32_body(FRFields in, FRFields out, size_t n, int bx, int gx) {
+    const size_t stride = (size_t)gx * blockDim.x;
+    for (size_t i = (size_t)bx * blockDim.x + threadIdx.x; i < n; i += stride) {
         const float u = in.p[0][i], v = in.p[1][i], w = in.p[2][i];
         const float ox = in.p[3][i], oy = in.p[4][i], oz = in.p[5][i];
         out.p[0][i] = v * oz - w * oy;
         out.p[1][i] = w * ox - u * oz;
         out.p[2][i] = u * oy - v * ox;
     }
+}
+
+__global__ void k_products32(FRFields in, FRFields out, size_t n) {
+    products32_body(in, out, n, blockIdx.x, gridDim.x);
 }
 
 // Viscous step as an increment in the eigenbasis of the interior Helmholtz
@@ -975,9 +1037,9 @@ __global__ void k_products32(FRFields in, FRFields out, size_t n) {
 // All products are FP32; the increment is added to the FP64 state, so the
 // FP32 error scales with the (small) increment.  Mode (0,0) is skipped: it is
 // advanced in FP64 by k_viscous.
-__global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
-                                                       Fields F, FFields Src, const double2* __restrict__ GP,
-                                                       Fields Out, int tc) {
+__device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops ops, StepParams sp,
+                                                   Fields F, FFields Src, const double2* __restrict__ GP,
+                                                   Fields Out, int tc, int bx) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int ni = g.nz - 2;
     const int hei = mx.hei, hoi = mx.hoi, pe4 = mx.pe4, po4 = mx.po4;
@@ -992,7 +1054,7 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
     float2* ty = ts + tsz;                              // [nr][tc] eigen-space update
     float4* tw = reinterpret_cast<float4*>(ty + tsz);   // [tc] wall terms
     float* tk = reinterpret_cast<float*>(tw + tc);      // [tc] k^2 (-1: skip; <= -2: masked source)
-    const int m0 = blockIdx.x * tc;
+    const int m0 = bx * tc;
     {
         const float4* A = reinterpret_cast<const float4*>(mx.AeT);
         for (int t = threadIdx.x; t < hei * (pe4 / 4); t += blockDim.x) sAe[t] = __ldg(&A[t]);
@@ -1172,6 +1234,12 @@ __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, O
     }
 }
 
+__global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
+                                                       Fields F, FFields Src, const double2* __restrict__ GP,
+                                                       Fields Out, int tc) {
+    viscous_mixed_body(g, mx, ops, sp, F, Src, GP, Out, tc, blockIdx.x);
+}
+
 // ------------------------------------------------------------------ double-float
 // Double-float ("df64") arithmetic on the FP32 pipe for the one contraction of
 // the mixed path that needs FP64 accuracy.  A value is hi + lo with hi the
@@ -1274,19 +1342,19 @@ __device__ __forceinline__ Pair anti_apply_df(const float2* __restrict__ De, con
 // of b, odd ones on the differences, MixedOps); computing dphi/dz through the
 // precomputed D V' keeps its FP32 error relative to dphi/dz itself.  Mode
 // (0,0) (pinned) is left to the FP64 kernels.
-__global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
-                                                        const double2* __restrict__ US,
-                                                        const double2* __restrict__ VS,
-                                                        const double2* __restrict__ WS,
-                                                        double2* __restrict__ PHI, double2* __restrict__ PHIZ,
-                                                        int tc) {
+__device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops ops, StepParams sp,
+                                                    const double2* __restrict__ US,
+                                                    const double2* __restrict__ VS,
+                                                    const double2* __restrict__ WS,
+                                                    double2* __restrict__ PHI, double2* __restrict__ PHIZ,
+                                                    int tc, int bx) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nz = g.nz, he = ops.he, ho = ops.ho;
     const int pe4 = mx.phe4, po4 = mx.pho4, nbe = pe4 / 4, nbo = po4 / 4;
     float4* tw = reinterpret_cast<float4*>(smraw);              // folded w* (double-float)  [nz][tc]
     float2* tb = reinterpret_cast<float2*>(tw + nz * tc);       // folded rhs: s [pe4][tc], d [po4][tc]
     float2* tp = tb + (pe4 + po4) * tc;                         // phi~: even [pe4][tc], odd [po4][tc]
-    const int m0 = blockIdx.x * tc;
+    const int m0 = bx * tc;
     fold_load_df(tw, WS, g, m0, tc, he, ho);
     for (int t = threadIdx.x; t < (pe4 - he) * tc; t += blockDim.x) tb[he * tc + t] = make_float2(0.f, 0.f);
     for (int t = threadIdx.x; t < (po4 - ho) * tc; t += blockDim.x) tb[(pe4 + ho) * tc + t] = make_float2(0.f, 0.f);
@@ -1421,9 +1489,18 @@ __global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, 
     }
 }
 
+__global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
+                                                        const double2* __restrict__ US,
+                                                        const double2* __restrict__ VS,
+                                                        const double2* __restrict__ WS,
+                                                        double2* __restrict__ PHI, double2* __restrict__ PHIZ,
+                                                        int tc) {
+    pressure_mixed_body(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc, blockIdx.x);
+}
+
 // dphi/dz of mode (0,0) in FP64 (one CTA), after k_pressure has written phi.
-__global__ void __launch_bounds__(256) k_dz_mean_mode(GridDev g, Ops ops, const double2* __restrict__ PHI,
-                                                      double2* __restrict__ PHIZ) {
+__device__ __forceinline__ void dz_mean_mode_body(GridDev g, Ops ops, const double2* __restrict__ PHI,
+                                                  double2* __restrict__ PHIZ, int bx) {
     extern __shared__ double2 sm[];
     const int he = ops.he, ho = ops.ho;
     fold_load(sm, PHI, g, 0, 1, he, ho);
@@ -1435,18 +1512,23 @@ __global__ void __launch_bounds__(256) k_dz_mean_mode(GridDev g, Ops ops, const 
     }
 }
 
+__global__ void __launch_bounds__(256) k_dz_mean_mode(GridDev g, Ops ops, const double2* __restrict__ PHI,
+                                                      double2* __restrict__ PHIZ) {
+    dz_mean_mode_body(g, ops, PHI, PHIZ, blockIdx.x);
+}
+
 // Pointwise correction of the mixed form (pressure_correction_3d, 3D:1903-1929)
 // with dphi/dz precomputed: u = u* - dt DX phi, v = v* - dt DY phi,
 // w = w* - dt dphi/dz, p += phi, wall gradients of the new p.
-__global__ void k_correction_mixed(GridDev g, Ops ops, StepParams sp, const double2* __restrict__ US,
-                                   const double2* __restrict__ VS, const double2* __restrict__ WS,
-                                   const double2* __restrict__ PHI, const double2* __restrict__ PHIZ,
-                                   double2* __restrict__ U, double2* __restrict__ V, double2* __restrict__ W,
-                                   double2* __restrict__ P, double2* __restrict__ GP) {
+__device__ __forceinline__ void correction_mixed_body(GridDev g, Ops ops, StepParams sp, const double2* __restrict__ US,
+                                                      const double2* __restrict__ VS, const double2* __restrict__ WS,
+                                                      const double2* __restrict__ PHI, const double2* __restrict__ PHIZ,
+                                                      double2* __restrict__ U, double2* __restrict__ V, double2* __restrict__ W,
+                                                      double2* __restrict__ P, double2* __restrict__ GP, int bx, int gx) {
     const size_t n = (size_t)g.nz * g.nm;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t stride = (size_t)gx * blockDim.x;
     const double dt = sp.dt;
-    for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += stride) {
+    for (size_t o = (size_t)bx * blockDim.x + threadIdx.x; o < n; o += stride) {
         const int z = (int)(o / g.nm);
         const int m = (int)(o - (size_t)z * g.nm);
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
@@ -1466,6 +1548,14 @@ __global__ void k_correction_mixed(GridDev g, Ops ops, StepParams sp, const doub
             GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, pp);
         }
     }
+}
+
+__global__ void k_correction_mixed(GridDev g, Ops ops, StepParams sp, const double2* __restrict__ US,
+                                   const double2* __restrict__ VS, const double2* __restrict__ WS,
+                                   const double2* __restrict__ PHI, const double2* __restrict__ PHIZ,
+                                   double2* __restrict__ U, double2* __restrict__ V, double2* __restrict__ W,
+                                   double2* __restrict__ P, double2* __restrict__ GP) {
+    correction_mixed_body(g, ops, sp, US, VS, WS, PHI, PHIZ, U, V, W, P, GP, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ reductions
@@ -1871,6 +1961,202 @@ cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaSt
     if (blocks > 152 * 8) blocks = 152 * 8;
     k_nonfinite<<<blocks, 256, 0, s>>>(f, n, flag);
     return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ ragged stages
+// The non-transform stages of one run's step as k_stage bodies (ragged.cuh):
+// virtual block b of a run is block b of the run's own launch of the same
+// kernel, with the PI update and the mixed form's FP64 mode (0,0) solves as
+// one extra block in front of the mode tiles.
+namespace {
+
+template <typename P, int N>
+__device__ __forceinline__ FieldsT<P> desc_fields(void* const* p) {
+    FieldsT<P> f;
+#pragma unroll
+    for (int i = 0; i < kMaxFields; ++i) f.p[i] = i < N ? static_cast<P*>(p[i]) : nullptr;
+    return f;
+}
+
+__device__ __forceinline__ Fields fields3(double2* a, double2* b, double2* c) {
+    Fields f;
+#pragma unroll
+    for (int i = 0; i < kMaxFields; ++i) f.p[i] = nullptr;
+    f.p[0] = a;
+    f.p[1] = b;
+    f.p[2] = c;
+    return f;
+}
+
+struct RsVort64 {
+    static constexpr int kMinCtas = 2;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        if (b == 0) {
+            pi_update_body(d.g, d.ops.zw, d.pp, d.U, d.pi, 0);
+            return;
+        }
+        vorticity_body(d.g, d.ops, d.U, d.V, d.W, d.US, d.VS, d.WS, d.g.tc[kTileVort], b - 1);
+    }
+};
+
+struct RsVort32 {
+    static constexpr int kMinCtas = 4;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        if (b == 0) {
+            pi_update_body(d.g, d.ops.zw, d.pp, d.U, d.pi, 0);
+            return;
+        }
+        vorticity_mixed_body(d.g, d.mx, d.ops, d.U, d.V, d.W, desc_fields<float2, 6>(d.spec), d.g.tc[kTileVortM],
+                             b - 1);
+    }
+};
+
+template <typename T>
+struct RsProd {
+    static constexpr int kMinCtas = 4;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        const size_t n = (size_t)d.g.nx * d.g.ny * d.g.nz;
+        if constexpr (sizeof(T) == 8)
+            products_body(desc_fields<double, 6>(d.phys), desc_fields<double, 3>(d.phys), n, b, d.gx[kRsProd]);
+        else
+            products32_body(desc_fields<float, 6>(d.phys), desc_fields<float, 3>(d.phys), n, b, d.gx[kRsProd]);
+    }
+};
+
+struct RsVisc64 {
+    static constexpr int kMinCtas = 3;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        viscous_body<double2>(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
+                              fields3(d.US, d.VS, d.WS), d.g.tc[kTileVisc], b);
+    }
+};
+
+struct RsVisc32 {
+    static constexpr int kMinCtas = 2;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        const Fields F = fields3(d.U, d.V, d.W), O = fields3(d.US, d.VS, d.WS);
+        const FFields S = desc_fields<float2, 3>(d.src);
+        if (b == 0) viscous_body<float2>(d.g, d.ops, d.sp, F, S, d.GP, d.pi, O, 1, 0);
+        else viscous_mixed_body(d.g, d.mx, d.ops, d.sp, F, S, d.GP, O, d.g.tc[kTileViscM], b - 1);
+    }
+};
+
+struct RsPres64 {
+    static constexpr int kMinCtas = 4;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        pressure_body(d.g, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.g.tc[kTilePres], b);
+    }
+};
+
+struct RsPres32 {
+    static constexpr int kMinCtas = 3;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        if (b == 0) {
+            pressure_body(d.g, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, 1, 0);
+            __syncthreads();  // phi of mode (0,0) written by this CTA
+            dz_mean_mode_body(d.g, d.ops, d.PHI, d.PHIZ, 0);
+        } else {
+            pressure_mixed_body(d.g, d.mx, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.PHIZ, d.g.tc[kTilePresM], b - 1);
+        }
+    }
+};
+
+struct RsCorr64 {
+    static constexpr int kMinCtas = 4;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        correction_body(d.g, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.U, d.V, d.W, d.P, d.GP, d.g.tc[kTileCorr], b);
+    }
+};
+
+struct RsCorr32 {
+    static constexpr int kMinCtas = 4;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        correction_mixed_body(d.g, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.PHIZ, d.U, d.V, d.W, d.P, d.GP, b,
+                              d.gx[kRsCorr]);
+    }
+};
+
+struct RsBc {
+    static constexpr int kMinCtas = 4;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) { apply_bc_body(d.g, d.U, d.V, d.W, b); }
+};
+
+}  // namespace
+
+StageKernel ragged_kernel(int stage, bool mixed) {
+    switch (stage) {
+        case kRsVort: return mixed ? k_stage<RsVort32> : k_stage<RsVort64>;
+        case kRsProd: return mixed ? k_stage<RsProd<float>> : k_stage<RsProd<double>>;
+        case kRsVisc: return mixed ? k_stage<RsVisc32> : k_stage<RsVisc64>;
+        case kRsPres: return mixed ? k_stage<RsPres32> : k_stage<RsPres64>;
+        case kRsCorr: return mixed ? k_stage<RsCorr32> : k_stage<RsCorr64>;
+        case kRsBc: return k_stage<RsBc>;
+        case kRsFftYInv:
+        case kRsFftC2R:
+        case kRsFftR2C:
+        case kRsFftYFwd: return ragged_fft_kernel(stage, mixed);
+    }
+    return nullptr;
+}
+
+void ragged_geometry(RunDesc& d) {
+    const GridDev& g = d.g;
+    auto cdiv = [](long long a, long long b) { return (int)((a + b - 1) / b); };
+    for (int s = 0; s < kRsStages; ++s) d.gx[s] = 1;
+    const int cy = fft_ct_per_cta(g.ny), rx = fft_ct_per_cta(g.nxh);
+    d.gx[kRsFftYInv] = cdiv((long long)g.nz * g.nxhp, cy);
+    d.gx[kRsFftC2R] = cdiv((long long)g.nz * g.ny, rx);
+    d.gx[kRsProd] = cdiv((long long)g.nx * g.ny * g.nz, 4 * kStageThreads);
+    d.gx[kRsFftR2C] = d.gx[kRsFftC2R];
+    d.gx[kRsFftYFwd] = cdiv((long long)g.nz * d.ncol, cy);
+    d.gx[kRsCorr] = cdiv((long long)g.nz * g.nm, 4 * kStageThreads);
+    d.gx[kRsBc] = cdiv(2LL * g.nm, kStageThreads);
+}
+
+int ragged_tile_kernel(int stage, bool mixed) {
+    switch (stage) {
+        case kRsVort: return mixed ? kTileVortM : kTileVort;
+        case kRsVisc: return mixed ? kTileViscM : kTileVisc;
+        case kRsPres: return mixed ? kTilePresM : kTilePres;
+        case kRsCorr: return mixed ? -1 : kTileCorr;
+    }
+    return -1;
+}
+
+int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
+    const GridDev& g = d.g;
+    const int k = ragged_tile_kernel(stage, mixed);
+    const int tiles = k >= 0 ? (g.nm + g.tc[k] - 1) / g.tc[k] : 0;
+    switch (stage) {
+        case kRsVort: return 1 + tiles;
+        case kRsFftYInv:
+        case kRsFftC2R: return 6 * d.gx[stage];
+        case kRsFftR2C:
+        case kRsFftYFwd: return 3 * d.gx[stage];
+        case kRsProd:
+        case kRsBc: return d.gx[stage];
+        case kRsVisc:
+        case kRsPres: return (mixed ? 1 : 0) + tiles;
+        case kRsCorr: return mixed ? d.gx[stage] : tiles;
+    }
+    return 0;
+}
+
+size_t ragged_smem(int stage, bool mixed, const RunDesc& d) {
+    const GridDev& g = d.g;
+    const size_t nz = g.nz;
+    const int k = ragged_tile_kernel(stage, mixed);
+    const int tc = k >= 0 ? g.tc[k] : 0;
+    switch (stage) {
+        case kRsVort: return 2 * nz * tc * (mixed ? sizeof(float2) : sizeof(double2));
+        case kRsVisc:
+            return mixed ? std::max(6 * nz * sizeof(double2), viscous_mixed_smem(g, tc)) : 6 * nz * tc * sizeof(double2);
+        case kRsPres:
+            return mixed ? std::max(3 * nz * sizeof(double2), pressure_mixed_smem(g, tc))
+                         : (2 * nz * tc + nz) * sizeof(double2);
+        case kRsCorr: return mixed ? 0 : nz * tc * sizeof(double2);
+    }
+    return 0;
 }
 
 }  // namespace dns3d

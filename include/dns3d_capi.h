@@ -218,21 +218,47 @@ int dns3d_measure_fp64_tflops(int device, double* tflops);
 int dns3d_flow_stats_noalloc(const double* u, const double* v, const double* w, int nx, int ny,
                              int nz, double* out4, void* stream);
 
-/* Ensembles: many independent runs (any mix of grids, parameters and
- * precisions) advanced together.  No counterpart in the reference, which runs
- * one channel per process.  Each run keeps its own handle and stream; the
- * ensemble captures every run's loop body into one CUDA graph with one branch
- * per run, so a single graph launch advances all runs by one step and their
- * kernels overlap on the GPU.  Runs are numbered 0..nruns-1 in config order. */
+/* Batches: joint stepping of independent runs (any mix of grids, parameters
+ * and precisions).  No counterpart in the reference, which runs one channel
+ * per process.  Runs whose options allow it (the default convection scheme
+ * and solver, transform lengths with compile-time kernels) advance in ragged
+ * launches: each of the ten stages of a step (vorticity with the PI update,
+ * four plane-transform passes, the products, viscous, pressure, projection,
+ * walls) is ONE kernel launch over the mode tiles / transform columns of all
+ * such runs of one precision, whatever their nx, ny, nz, with every run's
+ * arithmetic that of its own launches (bitwise the same results).  Other runs
+ * are stepped by their own launches beside them.  One step is one CUDA graph;
+ * DNS3D_BATCH_TUNE times the stage tile widths for this set of runs when the
+ * batch is created (the runs' PI states are restored afterwards).  The
+ * handles stay owned by the caller and must outlive the batch; the batch
+ * orders itself after work already queued on each run's stream, and later
+ * work on those streams after the batch's steps. */
+typedef struct dns3d_batch dns3d_batch;
+#define DNS3D_BATCH_TUNE 1
+int dns3d_batch_create(dns3d_handle* const* runs, int nruns, int flags, dns3d_batch** out);
+/* Queues nsteps steps of every run (returns before they finish). */
+int dns3d_batch_step(dns3d_batch* b, int nsteps);
+int dns3d_batch_synchronize(dns3d_batch* b);
+/* Kernel launches per step of the whole batch, and how many runs are in
+ * ragged launches (the rest use their own). */
+int dns3d_batch_info(dns3d_batch* b, int* launches_per_step, int* ragged_runs);
+int dns3d_batch_destroy(dns3d_batch* b);
+
+/* Ensembles: a batch that owns its runs, created from configs.  Runs are
+ * numbered 0..nruns-1 in config order; the stage tile widths are tuned for the
+ * ensemble at its first step unless DNS3D_AUTOTUNE=0. */
 typedef struct dns3d_ensemble dns3d_ensemble;
 int dns3d_ensemble_create(const dns3d_config* cfgs, int nruns, dns3d_ensemble** out);
 int dns3d_ensemble_destroy(dns3d_ensemble* e);
 int dns3d_ensemble_size(dns3d_ensemble* e, int* nruns);
 /* The handle of run i (state transfer, diagnostics); owned by the ensemble. */
 int dns3d_ensemble_run(dns3d_ensemble* e, int i, dns3d_handle** h);
+/* Advances every run nsteps steps; returns when they are done. */
 int dns3d_ensemble_step(dns3d_ensemble* e, int nsteps);
 /* As dns3d_ensemble_step, bracketed by CUDA events; waits, returns device ms. */
 int dns3d_ensemble_step_timed(dns3d_ensemble* e, int nsteps, double* elapsed_ms);
+/* As dns3d_batch_info for the ensemble's batch (created at the first step). */
+int dns3d_ensemble_info(dns3d_ensemble* e, int* launches_per_step, int* ragged_runs);
 
 /* Serving: continuous batching of requested runs on one GPU.  No counterpart
  * in the reference.  A worker thread owned by the server admits requests in
