@@ -1637,8 +1637,10 @@ struct dns3d_batch {
     int device = 0;
     cudaStream_t stream = nullptr;    // the batch's graph runs here
     cudaStream_t lane[2] = {nullptr, nullptr};
+    cudaStream_t side[2] = {nullptr, nullptr};  // the mixed group's mode (0,0) stages
     cudaEvent_t fork = nullptr, done = nullptr;
     cudaEvent_t lane_join[2] = {nullptr, nullptr};
+    cudaEvent_t side_fork[2] = {nullptr, nullptr}, side_join[2] = {nullptr, nullptr};
     std::vector<cudaEvent_t> run_in, run_join;
     Group grp[2];                     // FP64, mixed
     std::vector<int> loose;           // runs stepped by their own launches
@@ -1673,8 +1675,16 @@ cudaError_t prepare_stage_kernels() {
     return cudaSuccess;
 }
 
+// Runs of 2^20 points and more keep their own launches: they fill the GPU by
+// themselves, and their own kernels read every operand from the constant bank
+// where the stage bodies hold descriptor fields in registers (one 256x256x97
+// mixed run: 1.28 ms per step alone, 1.34 ms as a batch of one).
+constexpr long long kRaggedMaxPoints = 1LL << 20;
+
 bool ragged_eligible(const dns3d_handle* h) {
-    return h->fft.use_ct && h->cfg.convection_scheme == 0 && h->cfg.linear_solver == 0;
+    const long long points = (long long)h->cfg.nx * h->cfg.ny * h->cfg.nz;
+    return h->fft.use_ct && h->cfg.convection_scheme == 0 && h->cfg.linear_solver == 0 &&
+           points < kRaggedMaxPoints;
 }
 
 RunDesc make_desc(const dns3d_handle* h) {
@@ -1828,6 +1838,11 @@ void batch_release(dns3d_batch* b) {
     for (auto ev : b->run_join) cudaEventDestroy(ev);
     for (auto ev : b->lane_join)
         if (ev) cudaEventDestroy(ev);
+    for (int i = 0; i < 2; ++i) {
+        if (b->side_fork[i]) cudaEventDestroy(b->side_fork[i]);
+        if (b->side_join[i]) cudaEventDestroy(b->side_join[i]);
+        if (b->side[i]) cudaStreamDestroy(b->side[i]);
+    }
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->done) cudaEventDestroy(b->done);
     for (auto st : b->lane)
@@ -1835,8 +1850,38 @@ void batch_release(dns3d_batch* b) {
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
-// One graph per step: fork -> (each group's ten stage launches on its lane,
-// each loose run's step body on its own stream) -> join.
+// One group's step on its lane: the nonlinear-term stages, then viscous and
+// pressure tiles with (mixed form) the mode (0,0) chain forked beside them,
+// then projection and walls.
+cudaError_t group_capture(dns3d_batch* b, int gi, int* launches) {
+    dns3d_batch::Group& G = b->grp[gi];
+    cudaStream_t lane = b->lane[gi], side = b->side[gi];
+    cudaError_t ce = cudaSuccess;
+    auto stage = [&](int s, cudaStream_t st) {
+        if (!ce && G.total[s] > 0) {
+            ce = group_launch(G, s, st);
+            *launches += 1;
+        }
+    };
+    for (int s : {(int)kRsVort, (int)kRsFftYInv, (int)kRsFftC2R, (int)kRsProd, (int)kRsFftR2C, (int)kRsFftYFwd})
+        stage(s, lane);
+    if (G.mixed) {
+        if (!ce) ce = cudaEventRecord(b->side_fork[gi], lane);
+        if (!ce) ce = cudaStreamWaitEvent(side, b->side_fork[gi], 0);
+        stage(kRsViscMean, side);
+        stage(kRsPresMean, side);
+        if (!ce) ce = cudaEventRecord(b->side_join[gi], side);
+    }
+    stage(kRsVisc, lane);
+    stage(kRsPres, lane);
+    if (G.mixed && !ce) ce = cudaStreamWaitEvent(lane, b->side_join[gi], 0);
+    stage(kRsCorr, lane);
+    stage(kRsBc, lane);
+    return ce;
+}
+
+// One graph per step: fork -> (each group's stage launches on its lane, each
+// loose run's step body on its own stream) -> join.
 int batch_capture(dns3d_batch* b) {
     cudaGraph_t graph = nullptr;
     BK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -1847,10 +1892,7 @@ int batch_capture(dns3d_batch* b) {
         dns3d_batch::Group& G = b->grp[gi];
         if (G.idx.empty()) continue;
         ce = cudaStreamWaitEvent(b->lane[gi], b->fork, 0);
-        for (int s = 0; s < kRsStages && !ce; ++s) {
-            ce = group_launch(G, s, b->lane[gi]);
-            launches += G.total[s] > 0;
-        }
+        if (!ce) ce = group_capture(b, gi, &launches);
         if (!ce) ce = cudaEventRecord(b->lane_join[gi], b->lane[gi]);
         if (!ce) ce = cudaStreamWaitEvent(b->stream, b->lane_join[gi], 0);
     }
@@ -1935,7 +1977,10 @@ int batch_create(dns3d_handle* const* runs, int nruns, int flags, dns3d_batch** 
         if (G.idx.empty()) continue;
         const int n = (int)G.idx.size();
         if (cudaStreamCreateWithFlags(&b->lane[gi], cudaStreamNonBlocking) ||
-            cudaEventCreateWithFlags(&b->lane_join[gi], cudaEventDisableTiming))
+            cudaStreamCreateWithFlags(&b->side[gi], cudaStreamNonBlocking) ||
+            cudaEventCreateWithFlags(&b->lane_join[gi], cudaEventDisableTiming) ||
+            cudaEventCreateWithFlags(&b->side_fork[gi], cudaEventDisableTiming) ||
+            cudaEventCreateWithFlags(&b->side_join[gi], cudaEventDisableTiming))
             return fail(DNS3D_E_CUDA);
         if (cudaMalloc(&G.d_desc, (size_t)n * sizeof(RunDesc)) ||
             cudaMalloc(&G.d_map, (size_t)kRsStages * (2 * n + 1) * sizeof(int)))

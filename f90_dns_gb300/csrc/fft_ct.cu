@@ -372,7 +372,7 @@ __device__ __forceinline__ FieldsT<P> one_field(void* const* p, int f) {
 // place over the three sources (2/3-filtered columns only).
 template <int SIGN, typename T>
 struct RsFftY {
-    static constexpr int kMinCtas = 3;
+    static constexpr int kMinCtas = sizeof(T) == 8 ? 3 : 4;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
         using C = typename Cx<T>::type;
         __shared__ C buf[ct_buf_max()];
@@ -415,7 +415,7 @@ struct RsC2R {
 
 template <typename T>
 struct RsR2C {
-    static constexpr int kMinCtas = 3;
+    static constexpr int kMinCtas = sizeof(T) == 8 ? 3 : 4;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
         using C = typename Cx<T>::type;
         __shared__ C buf[ct_buf_max()];

@@ -27,10 +27,15 @@ enum RaggedStage {
     kRsProd,      // u x omega in physical space
     kRsFftR2C,    // r2c x pass of the three products
     kRsFftYFwd,   // forward y pass of the products (2/3-filtered columns only)
-    kRsVisc,      // viscous step (mixed: FP64 mode (0,0) in block 0, then FP32 tiles)
-    kRsPres,      // pressure solve (mixed: FP64 pinned mode (0,0) and its dphi/dz in block 0)
+    kRsVisc,      // viscous step (mixed: the FP32 mode tiles)
+    kRsPres,      // pressure solve (mixed: the FP32 mode tiles)
     kRsCorr,      // projection and wall gradients of p
     kRsBc,        // wall planes of u, v, w
+    // mixed form only: the FP64 mode (0,0) of the viscous step, then its pinned
+    // Poisson solve and dphi/dz, one CTA per run, on a forked stream beside
+    // kRsVisc and kRsPres (mode (0,0) of w* is all the pinned solve reads)
+    kRsViscMean,
+    kRsPresMean,
     kRsStages
 };
 

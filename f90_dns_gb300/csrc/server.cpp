@@ -4,16 +4,20 @@
 //
 // A worker thread owns all GPU work.  Requests wait in FIFO order until their
 // device footprint (dns3d_footprint_bytes) fits under the byte budget and a
-// slot is free; admitted runs each keep their own handle and stream and are
-// advanced `steps_per_round` steps per round, all runs' graph launches queued
-// before any wait, so their kernels overlap on the device.  A finished run's
-// diagnostics (and, on request, its final u, v, w, p_total) are kept, its
-// handle is destroyed at once so its memory admits the next request.
+// slot is free; admitted runs each keep their own handle and are advanced
+// `steps_per_round` steps per round.  The runs that take a full round form a
+// batch (dns3d_batch: every stage of a step is one ragged launch over all of
+// them), kept while the set of runs is unchanged; a run in its last, shorter
+// round steps on its own stream beside the batch.  A finished run's
+// diagnostics (and, on request, its final u, v, w, p_total) are kept, and the
+// batch and its handle are destroyed at once so its memory admits the next
+// request.
 //
 // Built only on the public entry points of include/dns3d_capi.h.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -62,8 +66,13 @@ struct dns3d_server {
     unsigned long long point_steps = 0;
     Clock::time_point t0;
     std::thread worker;
+    // worker-thread state: the batch of the runs taking full rounds
+    dns3d_batch* batch = nullptr;
+    std::vector<dns3d_handle*> batch_runs;
+    bool use_batch = true;  // DNS3D_SERVER_BATCH=0: every run steps on its own stream
 
     void loop();
+    void drop_batch();
     void admit_locked(std::vector<std::shared_ptr<Request>>& to_create);
 };
 
@@ -75,6 +84,12 @@ void dns3d_server::admit_locked(std::vector<std::shared_ptr<Request>>& to_create
         bytes_in_use += r->bytes;
         to_create.push_back(r);
     }
+}
+
+void dns3d_server::drop_batch() {
+    if (batch) dns3d_batch_destroy(batch);
+    batch = nullptr;
+    batch_runs.clear();
 }
 
 void dns3d_server::loop() {
@@ -90,6 +105,7 @@ void dns3d_server::loop() {
                     r->error = DNS3D_E_CANCELLED;
                 }
                 queue.clear();
+                drop_batch();
                 for (auto& r : active) {
                     dns3d_destroy(r->h);
                     r->h = nullptr;
@@ -124,11 +140,30 @@ void dns3d_server::loop() {
         if (active.empty()) continue;
         // one round: queue every run's steps, then wait for all
         std::vector<int> adv(active.size(), 0);
+        std::vector<dns3d_handle*> full;
+        for (auto& r : active)
+            if (r->nsteps - r->steps_done >= opts.steps_per_round) full.push_back(r->h);
+        if (!use_batch) full.clear();
+        if (full != batch_runs) {
+            drop_batch();
+            if (full.size() >= 2 && dns3d_batch_create(full.data(), (int)full.size(), 0, &batch) != DNS3D_OK)
+                batch = nullptr;  // the runs step on their own streams instead
+            batch_runs = full;
+        }
+        bool batch_ok = true;
+        if (batch) batch_ok = dns3d_batch_step(batch, opts.steps_per_round) == DNS3D_OK;
         for (size_t i = 0; i < active.size(); ++i) {
             auto& r = active[i];
             const int k = std::min(opts.steps_per_round, r->nsteps - r->steps_done);
-            if (k > 0 && dns3d_step(r->h, k) == DNS3D_OK) adv[i] = k;
-            else if (k > 0) r->error = DNS3D_E_CUDA;
+            const bool in_batch = batch && k == opts.steps_per_round;
+            if (in_batch) {
+                if (batch_ok) adv[i] = k;
+                else r->error = DNS3D_E_CUDA;
+            } else if (k > 0 && dns3d_step(r->h, k) == DNS3D_OK) {
+                adv[i] = k;
+            } else if (k > 0) {
+                r->error = DNS3D_E_CUDA;
+            }
         }
         for (size_t i = 0; i < active.size(); ++i) {
             auto& r = active[i];
@@ -138,6 +173,7 @@ void dns3d_server::loop() {
         std::vector<std::shared_ptr<Request>> done;
         for (auto& r : active)
             if (r->error || r->steps_done >= r->nsteps) done.push_back(r);
+        if (!done.empty()) drop_batch();  // before any of its handles goes
         for (auto& r : done) {
             if (!r->error) {
                 const int rc = dns3d_diagnostics(r->h, &r->diag);
@@ -198,6 +234,8 @@ int dns3d_server_create(const dns3d_server_opts* opts, dns3d_server** out) {
     auto* s = new dns3d_server();
     s->opts = *opts;
     s->t0 = Clock::now();
+    const char* env = std::getenv("DNS3D_SERVER_BATCH");
+    s->use_batch = !(env && std::strcmp(env, "0") == 0);
     s->worker = std::thread([s] { s->loop(); });
     *out = s;
     return DNS3D_OK;

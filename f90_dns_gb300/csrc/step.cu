@@ -1966,8 +1966,8 @@ cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaSt
 // ------------------------------------------------------------------ ragged stages
 // The non-transform stages of one run's step as k_stage bodies (ragged.cuh):
 // virtual block b of a run is block b of the run's own launch of the same
-// kernel, with the PI update and the mixed form's FP64 mode (0,0) solves as
-// one extra block in front of the mode tiles.
+// kernel, with the PI update as one extra block in front of the vorticity
+// tiles.
 namespace {
 
 template <typename P, int N>
@@ -2032,12 +2032,18 @@ struct RsVisc64 {
 };
 
 struct RsVisc32 {
-    static constexpr int kMinCtas = 2;
+    static constexpr int kMinCtas = 4;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
-        const Fields F = fields3(d.U, d.V, d.W), O = fields3(d.US, d.VS, d.WS);
-        const FFields S = desc_fields<float2, 3>(d.src);
-        if (b == 0) viscous_body<float2>(d.g, d.ops, d.sp, F, S, d.GP, d.pi, O, 1, 0);
-        else viscous_mixed_body(d.g, d.mx, d.ops, d.sp, F, S, d.GP, O, d.g.tc[kTileViscM], b - 1);
+        viscous_mixed_body(d.g, d.mx, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<float2, 3>(d.src), d.GP,
+                           fields3(d.US, d.VS, d.WS), d.g.tc[kTileViscM], b);
+    }
+};
+
+struct RsViscMean {
+    static constexpr int kMinCtas = 1;
+    static __device__ __forceinline__ void run(const RunDesc& d, int) {
+        viscous_body<float2>(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<float2, 3>(d.src), d.GP, d.pi,
+                             fields3(d.US, d.VS, d.WS), 1, 0);
     }
 };
 
@@ -2051,13 +2057,16 @@ struct RsPres64 {
 struct RsPres32 {
     static constexpr int kMinCtas = 3;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
-        if (b == 0) {
-            pressure_body(d.g, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, 1, 0);
-            __syncthreads();  // phi of mode (0,0) written by this CTA
-            dz_mean_mode_body(d.g, d.ops, d.PHI, d.PHIZ, 0);
-        } else {
-            pressure_mixed_body(d.g, d.mx, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.PHIZ, d.g.tc[kTilePresM], b - 1);
-        }
+        pressure_mixed_body(d.g, d.mx, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.PHIZ, d.g.tc[kTilePresM], b);
+    }
+};
+
+struct RsPresMean {
+    static constexpr int kMinCtas = 1;
+    static __device__ __forceinline__ void run(const RunDesc& d, int) {
+        pressure_body(d.g, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, 1, 0);
+        __syncthreads();  // phi of mode (0,0) written by this CTA
+        dz_mean_mode_body(d.g, d.ops, d.PHI, d.PHIZ, 0);
     }
 };
 
@@ -2091,6 +2100,8 @@ StageKernel ragged_kernel(int stage, bool mixed) {
         case kRsPres: return mixed ? k_stage<RsPres32> : k_stage<RsPres64>;
         case kRsCorr: return mixed ? k_stage<RsCorr32> : k_stage<RsCorr64>;
         case kRsBc: return k_stage<RsBc>;
+        case kRsViscMean: return k_stage<RsViscMean>;
+        case kRsPresMean: return k_stage<RsPresMean>;
         case kRsFftYInv:
         case kRsFftC2R:
         case kRsFftR2C:
@@ -2136,8 +2147,10 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
         case kRsProd:
         case kRsBc: return d.gx[stage];
         case kRsVisc:
-        case kRsPres: return (mixed ? 1 : 0) + tiles;
+        case kRsPres: return tiles;
         case kRsCorr: return mixed ? d.gx[stage] : tiles;
+        case kRsViscMean:
+        case kRsPresMean: return mixed ? 1 : 0;
     }
     return 0;
 }
@@ -2149,12 +2162,11 @@ size_t ragged_smem(int stage, bool mixed, const RunDesc& d) {
     const int tc = k >= 0 ? g.tc[k] : 0;
     switch (stage) {
         case kRsVort: return 2 * nz * tc * (mixed ? sizeof(float2) : sizeof(double2));
-        case kRsVisc:
-            return mixed ? std::max(6 * nz * sizeof(double2), viscous_mixed_smem(g, tc)) : 6 * nz * tc * sizeof(double2);
-        case kRsPres:
-            return mixed ? std::max(3 * nz * sizeof(double2), pressure_mixed_smem(g, tc))
-                         : (2 * nz * tc + nz) * sizeof(double2);
+        case kRsVisc: return mixed ? viscous_mixed_smem(g, tc) : 6 * nz * tc * sizeof(double2);
+        case kRsPres: return mixed ? pressure_mixed_smem(g, tc) : (2 * nz * tc + nz) * sizeof(double2);
         case kRsCorr: return mixed ? 0 : nz * tc * sizeof(double2);
+        case kRsViscMean: return mixed ? 6 * nz * sizeof(double2) : 0;
+        case kRsPresMean: return mixed ? 3 * nz * sizeof(double2) : 0;
     }
     return 0;
 }

@@ -221,13 +221,16 @@ int dns3d_flow_stats_noalloc(const double* u, const double* v, const double* w, 
 /* Batches: joint stepping of independent runs (any mix of grids, parameters
  * and precisions).  No counterpart in the reference, which runs one channel
  * per process.  Runs whose options allow it (the default convection scheme
- * and solver, transform lengths with compile-time kernels) advance in ragged
- * launches: each of the ten stages of a step (vorticity with the PI update,
- * four plane-transform passes, the products, viscous, pressure, projection,
- * walls) is ONE kernel launch over the mode tiles / transform columns of all
- * such runs of one precision, whatever their nx, ny, nz, with every run's
- * arithmetic that of its own launches (bitwise the same results).  Other runs
- * are stepped by their own launches beside them.  One step is one CUDA graph;
+ * and solver, transform lengths with compile-time kernels, fewer than 2^20
+ * grid points -- larger runs fill the GPU with their own launches) advance in
+ * ragged launches: each of the ten stages of a step (vorticity with the PI
+ * update, four plane-transform passes, the products, viscous, pressure,
+ * projection, walls) is ONE kernel launch over the mode tiles / transform
+ * columns of all such runs of one precision, whatever their nx, ny, nz, with
+ * every run's arithmetic that of its own launches (bitwise the same results);
+ * the mixed form adds one launch each for the FP64 mode (0,0) viscous and
+ * pressure solves, beside the tiles.  Other runs are stepped by their own
+ * launches beside them.  One step is one CUDA graph;
  * DNS3D_BATCH_TUNE times the stage tile widths for this set of runs when the
  * batch is created (the runs' PI states are restored afterwards).  The
  * handles stay owned by the caller and must outlive the batch; the batch
@@ -264,9 +267,12 @@ int dns3d_ensemble_info(dns3d_ensemble* e, int* launches_per_step, int* ragged_r
  * in the reference.  A worker thread owned by the server admits requests in
  * FIFO order while their device footprint fits under max_bytes and fewer than
  * max_runs are running, advances all running requests steps_per_round steps
- * per round on their own streams (their kernels overlap), and frees a run's
- * device memory as soon as it completes.  Times are seconds since server
- * creation.  dns3d_server_destroy cancels queued and running requests. */
+ * per round (the runs taking a full round as one dns3d_batch, rebuilt when
+ * that set changes; a run's shorter last round on its own stream beside it),
+ * and frees a run's device memory as soon as it completes
+ * (DNS3D_SERVER_BATCH=0 in the environment: every run on its own stream).
+ * Times are seconds since server creation.  dns3d_server_destroy cancels
+ * queued and running requests. */
 #define DNS3D_REQ_QUEUED 0
 #define DNS3D_REQ_RUNNING 1
 #define DNS3D_REQ_DONE 2

@@ -1,5 +1,6 @@
 """GPU: served runs (continuous batching, runs admitted as memory frees up,
-their kernels overlapping) give exactly the result of each run alone."""
+the runs of a full round stepped as one ragged batch) give exactly the result
+of each run alone."""
 import numpy as np
 import pytest
 
@@ -25,6 +26,27 @@ def test_served_results_equal_alone(built_lib):
         assert inf.status == REQ_DONE and inf.steps_done == n and inf.diag.step == n
     # at most ~two footprints were resident at any time: some request started late
     assert max(i.t_start for i in infos) > min(i.t_finish for i in infos) - 1e-9
+    for cfg, n, st in zip(cfgs, steps, states):
+        with ChannelDNS(cfg) as d:
+            d.step(n)
+            solo = d.get_state(walls=False)
+        for k in ("u", "v", "w", "p_total"):
+            assert np.array_equal(st[k], solo[k]), (cfg.nx, cfg.ny, cfg.nz, k)
+
+
+def test_served_batches_rebuilt_as_runs_finish(built_lib):
+    """Ten runs admitted together step as one batch; the batch is rebuilt as
+    runs finish (uneven step counts, a short last round each) and every
+    result is still the run's solo result."""
+    draws = ensemble_draws(10, seed=4)
+    cfgs = [config_from(d, precision=(PREC_MIXED if i % 3 else 0)) for i, d in enumerate(draws)]
+    steps = [3 + 2 * i for i in range(10)]
+    with Server(steps_per_round=4) as srv:
+        ids = [srv.submit(c, n, keep_state=True) for c, n in zip(cfgs, steps)]
+        infos = [srv.wait(i, timeout=300.0) for i in ids]
+        states = [srv.result_state(i) for i in ids]
+    for inf, n in zip(infos, steps):
+        assert inf.status == REQ_DONE and inf.steps_done == n
     for cfg, n, st in zip(cfgs, steps, states):
         with ChannelDNS(cfg) as d:
             d.step(n)
