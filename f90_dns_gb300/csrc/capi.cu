@@ -20,6 +20,7 @@
 
 #include "dns3d_internal.cuh"
 #include "ragged.cuh"
+#include "tc.cuh"
 
 using namespace dns3d;
 
@@ -51,6 +52,11 @@ struct dns3d_handle {
     double* d_red = nullptr;
     double* d_out = nullptr;
     int* d_flag = nullptr;
+    int* d_tcerr = nullptr;  // [2]: set when a tensor-core completion wait ran out
+    // viscous solve on the tensor cores (ops.tcA built): chosen by the tile
+    // autotuner unless DNS3D_TENSOR_CORES forces it (1) or rules it out (0)
+    bool visc_tc = false;
+    bool visc_tc_forced = false;
     int red_blocks = 0;
     std::vector<double> zpts, zwts;
     std::vector<void*> allocs;
@@ -428,6 +434,11 @@ int run_viscous(dns3d_handle* h) {
         mark(h, "viscous_jacgs");
         return DNS3D_OK;
     }
+    if (h->visc_tc && h->ops.tcA && h->sp.cn_identity) {
+        CK(h, launch_viscous_tc(h->g, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->d_tcerr, h->stream));
+        mark(h, "viscous_helmholtz_tc");
+        return DNS3D_OK;
+    }
     CK(h, launch_viscous(h->g, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->stream));
     mark(h, "viscous_helmholtz");
     return DNS3D_OK;
@@ -564,6 +575,10 @@ int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
     b += (2 * nq * (ez * ez + hz * hz) + 2 * nz2) * sizeof(double);  // folded inverses, pinned, S
     if (c->precision == DNS3D_PREC_MIXED)
         b += (6 + 3 + 6) * se * sizeof(float2) + 6 * pe * sizeof(float) + se * sizeof(double2);  // + dphi/dz
+    else if (c->use_crank_nicolson && c->linear_solver == 0 && tc_supported(c->nz)) {
+        const TcGeom t = tc_geom(c->nz);  // digit slices of the Helmholtz inverses
+        b += nq * (tc_q_halves(t) * sizeof(__half) + (size_t)t.m8 * sizeof(int));
+    }
     b += 16ull << 20;                        // operators, tables, reductions
     *bytes = b;
     return DNS3D_OK;
@@ -582,7 +597,8 @@ namespace {
 // thread's fixed-order sum, so results are bitwise the same for any width.
 using TuneKey = std::tuple<int, int, int, int, int>;
 std::mutex g_tune_mu;
-std::map<TuneKey, std::array<int, kTileKernels>> g_tune;
+// the widths, then 1 if the viscous solve runs on the tensor cores
+std::map<TuneKey, std::array<int, kTileKernels + 1>> g_tune;
 
 int tile_launch(dns3d_handle* h, int k) {
     const GridDev& g = h->g;
@@ -618,19 +634,25 @@ int tile_launch(dns3d_handle* h, int k) {
 
 int autotune(dns3d_handle* h, bool force) {
     CK(h, cudaSetDevice(h->cfg.device));
-    const TuneKey key{h->cfg.nx, h->cfg.ny, h->cfg.nz, h->mixed ? 1 : 0, h->cfg.device};
+    // precision, and for FP64 whether the tensor-core solve exists / is forced
+    const int variant = h->mixed ? 1 : (h->ops.tcA ? (h->visc_tc_forced ? 4 : 2) : 0);
+    const TuneKey key{h->cfg.nx, h->cfg.ny, h->cfg.nz, variant, h->cfg.device};
     if (!force) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
             for (int k = 0; k < kTileKernels; ++k) h->g.tc[k] = it->second[k];
+            if (h->ops.tcA && !h->visc_tc_forced) h->visc_tc = it->second[kTileKernels] != 0;
             return DNS3D_OK;
         }
     }
-    static const int kFp64[] = {kTileVort, kTileVisc, kTilePres, kTileCorr};
+    static const int kFp64[] = {kTileVort, kTilePres, kTileCorr, kTileVisc};
     static const int kMixed[] = {kTileVortM, kTileViscM, kTilePresM};
     const int* ks = h->mixed ? kMixed : kFp64;
-    const int nk = h->mixed ? 3 : 4;
+    // the FP64-pipe viscous kernel (last in kFp64) is not timed when the
+    // tensor-core one is forced
+    const int nk = h->mixed ? 3 : (h->visc_tc_forced ? 3 : 4);
+    float visc_ms = 0.f;
     cudaEvent_t e0, e1;
     CK(h, cudaEventCreate(&e0));
     CK(h, cudaEventCreate(&e1));
@@ -653,6 +675,27 @@ int autotune(dns3d_handle* h, bool force) {
             if (best == 0 || ms < best_ms) { best = cand; best_ms = ms; }
         }
         h->g.tc[k] = best;  // 0 (heuristic) if no candidate fitted
+        if (k == kTileVisc) visc_ms = best_ms;
+    }
+    // the tensor-core viscous solve against the best FP64-pipe width
+    if (!rc && !h->mixed && h->ops.tcA && !h->visc_tc_forced) {
+        Fields F{}, S{}, O{};
+        F.p[0] = h->U; F.p[1] = h->V; F.p[2] = h->W;
+        S.p[0] = h->SU; S.p[1] = h->SV; S.p[2] = h->SW;
+        O.p[0] = h->US; O.p[1] = h->VS; O.p[2] = h->WS;
+        auto launch = [&] { return launch_viscous_tc(h->g, h->ops, h->sp, F, S, h->GP, h->d_pi, O, h->d_tcerr, h->stream); };
+        cudaError_t ce = launch();
+        if (!ce) ce = cudaEventRecord(e0, h->stream);
+        for (int r = 0; r < 3 && !ce; ++r) ce = launch();
+        if (!ce) ce = cudaEventRecord(e1, h->stream);
+        if (!ce) ce = cudaEventSynchronize(e1);
+        if (ce) {
+            rc = cuda_fail(h, ce, "autotune (tensor-core viscous)");
+        } else {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            h->visc_tc = visc_ms <= 0.f || ms < visc_ms;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -662,8 +705,9 @@ int autotune(dns3d_handle* h, bool force) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
     }
-    std::array<int, kTileKernels> tiles{};
+    std::array<int, kTileKernels + 1> tiles{};
     for (int k = 0; k < kTileKernels; ++k) tiles[k] = h->g.tc[k];
+    tiles[kTileKernels] = h->visc_tc ? 1 : 0;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[key] = tiles;
     return DNS3D_OK;
@@ -1045,6 +1089,29 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     double wsum = 0.0;
     for (int k = 0; k < nz; ++k) wsum += h->zwts[k];
     pp.inv_nxny_wsum = 1.0 / ((double)c.nx * (double)c.ny * wsum);
+
+    // tensor-core form of the Helmholtz inverses: FP64 Crank-Nicolson runs with
+    // the direct solver (DNS3D_TENSOR_CORES=0 keeps the FP64-pipe kernel)
+    if ((rc = dev_alloc(h, &h->d_tcerr, 2))) return fail(rc);
+    const char* tcenv = std::getenv("DNS3D_TENSOR_CORES");
+    if (!h->mixed && sp.cn_identity && c.linear_solver == 0 && !(tcenv && std::strcmp(tcenv, "0") == 0) &&
+        viscous_tc_fits(g)) {
+        const TcGeom t = tc_geom(nz);
+        __half* sl = nullptr;
+        int* ex = nullptr;
+        if ((rc = dev_alloc(h, &sl, (size_t)nq * tc_q_halves(t))) || (rc = dev_alloc(h, &ex, (size_t)nq * t.m8)))
+            return fail(rc);
+        if ((e = build_tc_slices(g, ops.HinvF, nq, sl, ex, h->stream)) || (e = cudaStreamSynchronize(h->stream))) {
+            cuda_fail(h, e, "build_tc_slices");
+            return fail(DNS3D_E_CUDA);
+        }
+        ops.tcA = sl;
+        ops.tcE = ex;
+        h->visc_tc_forced = tcenv && std::strcmp(tcenv, "1") == 0;
+        // without timing: the tensor-core kernel once the grid has a few waves
+        // of operator pairs and two of its CTAs fit an SM
+        h->visc_tc = h->visc_tc_forced || (nq >= 8 * 152 && viscous_tc_smem(g) <= 113 * 1024);
+    }
 
     if ((rc = dns3d_initialize_fields(h))) return fail(rc);
     const char* at = std::getenv("DNS3D_AUTOTUNE");
@@ -1516,6 +1583,7 @@ int diag_core(dns3d_handle* h, dns3d_diag* out, bool with_div, std::vector<doubl
     // d_out = [5 reductions, 3 spare][dns3d_pi_state (8 doubles)][3 nz complex]
     constexpr int kPiDoubles = (int)(sizeof(dns3d_pi_state) / sizeof(double));
     CK(h, launch_diag_gather(g, h->U, h->V, h->W, h->d_pi, h->d_out + 8, h->stream));
+    CK(h, cudaMemcpyAsync(h->d_out + 5, h->d_tcerr, 2 * sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
     std::vector<double> blk(8 + kPiDoubles + 6 * (size_t)g.nz);
     CK(h, cudaMemcpyAsync(blk.data(), h->d_out, blk.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
@@ -1540,6 +1608,12 @@ int diag_core(dns3d_handle* h, dns3d_diag* out, bool with_div, std::vector<doubl
     out->u_bulk = vol * h->pp.inv_nxny_wsum;
     out->time = h->time;
     out->step = h->step;
+    long long tcerr = 0;
+    std::memcpy(&tcerr, &blk[5], sizeof(tcerr));
+    if (tcerr) {
+        h->err = "a tensor-core completion wait ran out";
+        return DNS3D_E_TIMEOUT;
+    }
     if (!std::isfinite(out->energy) || !std::isfinite(out->umax) || !std::isfinite(out->max_div))
         return DNS3D_E_NONFINITE;
     return DNS3D_OK;
@@ -1692,10 +1766,15 @@ RunDesc make_desc(const dns3d_handle* h) {
     d.g = h->g;
     for (int k = 0; k < kTileKernels; ++k) d.g.tc[k] = tile_width(h->g, k);
     d.ops = h->ops;
+    if (!h->visc_tc) {
+        d.ops.tcA = nullptr;
+        d.ops.tcE = nullptr;
+    }
     d.mx = h->mx;
     d.sp = h->sp;
     d.pp = h->pp;
     d.pi = h->d_pi;
+    d.tcerr = h->d_tcerr;
     d.U = h->U; d.V = h->V; d.W = h->W; d.P = h->P; d.GP = h->GP;
     d.US = h->US; d.VS = h->VS; d.WS = h->WS; d.PHI = h->PHI; d.PHIZ = h->PHIZ;
     const size_t se = spec_elems(h->cfg);

@@ -13,6 +13,7 @@
 // holds nm = nxhp*ny modes.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -157,6 +158,10 @@ struct Ops {
     double* PinvF;   // folded Poisson inverses        [nq][he*he + ho*ho]
     double* PpinT;   // pinned (0,0) Poisson inverse, unfolded, transposed [nz][nz]
     int nq;
+    // tensor-core form of HinvF (tc.cuh), or null: FP16 digit slices
+    // [nq][tc_q_halves] and row exponents [nq][m8]
+    const __half* tcA;
+    const int* tcE;
 };
 
 // Mixed-precision operators (FP32): folded D for the nonlinear term and the
@@ -230,6 +235,13 @@ cudaError_t launch_products(const GridDev& g, RFields in6, RFields out3, cudaStr
 cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& sp,
                            Fields F, Fields Src, const double2* GP,
                            const dns3d_pi_state* pi, Fields Out, cudaStream_t s);
+// The Crank-Nicolson viscous step with the folded inverses applied on the
+// tensor cores in emulated FP64 (ops.tcA set, sp.cn_identity); err receives 1
+// if a tensor-core completion wait ran out.
+cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F, Fields Src,
+                              const double2* GP, const dns3d_pi_state* pi, Fields Out, int* err, cudaStream_t s);
+size_t viscous_tc_smem(const GridDev& g);
+bool viscous_tc_fits(const GridDev& g);
 cudaError_t launch_vorticity_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops,
                                    const double2* U, const double2* V, const double2* W, FFields out,
                                    cudaStream_t s);
@@ -298,6 +310,12 @@ cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaSt
 cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh,
                            double helm_f, const double* ksq, int nq, double* HinvF,
                            double* PinvF, double* PpinT, int* info, cudaStream_t s);
+
+// Digit slices (FP16) and row exponents of the folded per-mode inverses invF
+// ([nq][he*he + ho*ho], the layout of Ops::HinvF) for the tensor-core solve
+// (tc.cuh); slices [nq][tc_q_halves], rowexp [nq][m8].
+cudaError_t build_tc_slices(const GridDev& g, const double* invF, int nq, __half* slices, int* rowexp,
+                            cudaStream_t s);
 
 // Dense FP64 FMA throughput probe (TFLOP/s).
 cudaError_t measure_fp64_tflops(int device, double* tflops);

@@ -56,6 +56,7 @@ struct RunDesc {
     const void* tw_ny;
     const void* tw_nx2;
     const void* tw_nx;
+    int* tcerr;              // tensor-core wait status of the run (viscous stage)
     int ncol;                // columns the forward y pass completes
     int gx[kRsStages];       // virtual blocks per field of each stage (transforms, elementwise passes)
 };

@@ -19,6 +19,7 @@
 // block transposed; the pinned operator is not centro-symmetric and is stored
 // unfolded and transposed: out[z'][z] = inverse[z][z'].
 #include "dns3d_internal.cuh"
+#include "tc.cuh"
 
 namespace dns3d {
 namespace {
@@ -200,7 +201,56 @@ __global__ void __launch_bounds__(256) k_fma_probe(double* out, int iters, doubl
     out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// Digit slices of the folded inverses for the tensor-core solve (tc.cuh):
+// one thread per (q, row of the block-diagonal operator).  Row i of the even
+// block is Ge[i][:] = GeT[:][i]; rows and columns past a block's size stay
+// zero, so the padded core matrices contribute nothing.
+__global__ void k_tc_slices(const double* __restrict__ invF, int nq, int nz, __half* __restrict__ slices,
+                            int* __restrict__ rowexp) {
+    const TcGeom t = tc_geom(nz);
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (long long)nq * t.m8) return;
+    const int q = (int)(id / t.m8), m = (int)(id - (long long)q * t.m8);
+    const bool even = m < t.e8;
+    const int i = even ? m : m - t.e8;
+    const int n = even ? t.he : t.ho;
+    const int w8 = even ? t.e8 : t.o8;
+    const size_t qs = (size_t)t.he * t.he + (size_t)t.ho * t.ho;
+    const double* GT = invF + (size_t)q * qs + (even ? 0 : (size_t)t.he * t.he);
+    __half* S = slices + (size_t)q * tc_q_halves(t);
+    const int ncore = t.ncore_e + t.ncore_o;
+    const int cbase = even ? 0 : t.ncore_e;
+    const int nb = w8 / 8;
+    int e = 0;
+    if (i < n) {
+        unsigned long long mx = 0;
+        for (int j = 0; j < n; ++j) {
+            const unsigned long long ab = (unsigned long long)__double_as_longlong(GT[(size_t)j * n + i]) &
+                                          0x7FFFFFFFFFFFFFFFULL;
+            mx = ab > mx ? ab : mx;
+        }
+        e = tc_exponent(mx);
+    }
+    rowexp[(size_t)q * t.m8 + m] = e;
+    for (int j = 0; j < w8; ++j) {
+        int c[kTcSlices];
+        for (int s = 0; s < kTcSlices; ++s) c[s] = 0;
+        if (i < n && j < n) tc_digits(tc_fixed(GT[(size_t)j * n + i], e), c);
+        const int core = cbase + (i / 8) * nb + (j / 8);
+        const int off = (i % 8) * 8 + (j % 8);
+        for (int s = 0; s < kTcSlices; ++s) S[((size_t)s * ncore + core) * 64 + off] = __int2half_rn(c[s]);
+    }
+}
+
 }  // namespace
+
+cudaError_t build_tc_slices(const GridDev& g, const double* invF, int nq, __half* slices, int* rowexp,
+                            cudaStream_t s) {
+    const TcGeom t = tc_geom(g.nz);
+    const long long n = (long long)nq * t.m8;
+    k_tc_slices<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(invF, nq, g.nz, slices, rowexp);
+    return cudaGetLastError();
+}
 
 cudaError_t measure_fp64_tflops(int device, double* tflops) {
     cudaError_t e;

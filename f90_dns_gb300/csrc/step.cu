@@ -17,6 +17,7 @@
 // along m.
 #include "dns3d_internal.cuh"
 #include "ragged.cuh"
+#include "tc.cuh"
 
 #include <algorithm>
 
@@ -496,6 +497,254 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
             if (k < ho) fptr(Out, comp)[(size_t)(nz - 1 - k) * g.nm + m] = x.b;
         }
     }
+}
+
+// ------------------------------------------------------------------ tensor-core viscous step
+// The Crank-Nicolson viscous step of viscous_body with the folded inverses
+// applied on the tensor cores in emulated FP64 (tc.cuh).  A CTA takes qpb
+// operator indices q; the modes sharing q ((ky, kx) and (ny-ky, kx)) and
+// their three components give 12 right-hand-side columns (re, im), one block
+// of 16.  Per q:
+//  (a) one thread starts bulk copies of the operator's digit slices into their
+//      places of the block-diagonal diag(Ge, Go) (the padding stays zero);
+//  (b) meanwhile the folded right-hand sides are formed in FP64 (viscous_rhs_cn),
+//  (c) each column gets its power-of-two scale and (d) its digits, one
+//      16-byte core-matrix row (8 levels) per thread and digit;
+//  (e) one thread issues 7 x (K/16) MMAs: digit slice sa of the operator
+//      times digit slices 0 .. 6-sa of the right-hand sides side by side
+//      (N = 16 (7-sa)), accumulated into the weight-class columns sa .. 6;
+//  (f) every row's 7 class accumulators are combined in 64-bit integers and
+//      scaled to FP64;
+//  (g) the outputs F* = x - f are written (wall values at the walls).
+__device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops, const StepParams& sp,
+                                                const Fields& F, const Fields& Src,
+                                                const double2* __restrict__ GP,
+                                                const dns3d_pi_state* __restrict__ pi, const Fields& Out,
+                                                int qpb, int bx, int* err) {
+    extern __shared__ __align__(128) unsigned char tcsm[];
+    const TcGeom t = tc_geom(g.nz);
+    const int nz = g.nz, he = t.he, ho = t.ho, m8 = t.m8;
+    const int a_halves = m8 * t.k16, b_halves = kTcN * t.k16;
+    __half* sA = reinterpret_cast<__half*>(tcsm);
+    __half* sB = sA + kTcSlices * a_halves;
+    double* sR = reinterpret_cast<double*>(sB + kTcSlices * b_halves);  // [kTcN][m8]: rhs, then results
+    int* sF = reinterpret_cast<int*>(sR + kTcN * m8);                   // column exponents
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcN);            // [0] MMAs done, [1] slices landed
+    uint32_t* tbase = reinterpret_cast<uint32_t*>(mbar + 2);
+    int* landed = reinterpret_cast<int*>(tbase + 1);                    // the slices of this q arrived
+    {
+        uint4* z = reinterpret_cast<uint4*>(sA);
+        const int n16 = kTcSlices * (a_halves + b_halves) / 8;
+        for (int i = threadIdx.x; i < n16; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (threadIdx.x < 32) tc_alloc(tbase, 128);
+    if (threadIdx.x == 0) {
+        tc_mbar_init(&mbar[0]);
+        tc_mbar_init(&mbar[1]);
+    }
+    tc_fence_proxy();  // the zeroed operands, before any bulk copy or MMA
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tbase;
+    const double dpdx = pi->current_pressure_gradient;
+    const int q0 = bx * qpb, q1 = min(q0 + qpb, ops.nq);
+    const size_t qh = tc_q_halves(t);
+    const int nbe = t.e8 >> 3, nbo = t.o8 >> 3;
+    const int ncore = t.ncore_e + t.ncore_o;
+    const int nv = he + ho;  // valid rows / K indices
+    const int nchunk = m8 >> 3;
+    bool ok = true;
+    for (int q = q0; q < q1 && ok; ++q) {
+        const uint32_t par = (uint32_t)((q - q0) & 1);
+        // (a) digit slices of the operator: per digit, one copy per 8-row group
+        if (threadIdx.x == 0) {
+            tc_mbar_expect(&mbar[1], (uint32_t)(qh * sizeof(__half)));
+            const __half* src = ops.tcA + (size_t)q * qh;
+            for (int s = 0; s < kTcSlices; ++s) {
+                const __half* ss = src + (size_t)s * ncore * 64;
+                __half* ds = sA + s * a_halves;
+                for (int gm = 0; gm < nbe; ++gm)
+                    tc_bulk_g2s(ds + tc_core_off(gm * 8, 0, t.k16), ss + (size_t)gm * nbe * 64, nbe * 128, &mbar[1]);
+                for (int gm = 0; gm < nbo; ++gm)
+                    tc_bulk_g2s(ds + tc_core_off(t.e8 + gm * 8, t.e8, t.k16),
+                                ss + (size_t)(t.ncore_e + gm * nbo) * 64, nbo * 128, &mbar[1]);
+            }
+        }
+        // (b) folded right-hand sides: column 6 mi + 2 comp + (0 re, 1 im)
+        const int kya = q / g.nxhp, kx = q - kya * g.nxhp;
+        const int nmode = (kya > 0 && 2 * kya != g.ny) ? 2 : 1;
+        for (int i = threadIdx.x; i < 6 * he; i += blockDim.x) {
+            const int mi = i / (3 * he);
+            const int r = i - mi * 3 * he;
+            const int comp = r / he, k = r - comp * he;
+            double2 fe = make_double2(0.0, 0.0), fo = fe;
+            if (mi < nmode) {
+                const int ky = mi ? g.ny - kya : kya;
+                const int m = ky * g.nxhp + kx;
+                double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
+                if (comp < 2) {
+                    const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
+                    const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                    bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
+                    bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
+                }
+                const double2* fc = fptr(F, comp);
+                const double2* sc = fptr(Src, comp);
+                const double2 f1 = fc[m], fn = fc[(size_t)(nz - 1) * g.nm + m];
+                const size_t o1 = (size_t)k * g.nm + m, o2 = (size_t)(nz - 1 - k) * g.nm + m;
+                const double2 b1 = viscous_rhs_cn(g, ops, sp, comp, k, m, ky, kx, fc[o1], sc[o1], f1, fn, bc1, bc2, dpdx);
+                if (k < ho) {
+                    const double2 b2 =
+                        viscous_rhs_cn(g, ops, sp, comp, nz - 1 - k, m, ky, kx, fc[o2], sc[o2], f1, fn, bc1, bc2, dpdx);
+                    fe = make_double2(b1.x + b2.x, b1.y + b2.y);
+                    fo = make_double2(b1.x - b2.x, b1.y - b2.y);
+                } else {
+                    fe = b1;
+                }
+            }
+            const int c0 = 6 * mi + 2 * comp;
+            sR[c0 * m8 + k] = fe.x;
+            sR[(c0 + 1) * m8 + k] = fe.y;
+            if (k < ho) {
+                sR[c0 * m8 + t.e8 + k] = fo.x;
+                sR[(c0 + 1) * m8 + t.e8 + k] = fo.y;
+            }
+        }
+        __syncthreads();
+        // (c) column scales, one warp per column
+        {
+            const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+            for (int c = w; c < 12; c += blockDim.x >> 5) {
+                unsigned long long mx = 0;
+                for (int k = l; k < nv; k += 32) {
+                    const int row = k < he ? k : t.e8 + (k - he);
+                    const unsigned long long ab =
+                        (unsigned long long)__double_as_longlong(sR[c * m8 + row]) & 0x7FFFFFFFFFFFFFFFULL;
+                    mx = ab > mx ? ab : mx;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
+                    mx = v > mx ? v : mx;
+                }
+                if (l == 0) sF[c] = tc_exponent(mx);
+            }
+        }
+        __syncthreads();
+        // (d) digits of the right-hand sides, one level of one column per
+        // thread; a warp covers 8 levels of 4 columns, so its 2-byte stores
+        // fall in distinct shared-memory banks (the bank of (n, k) in a core
+        // matrix is 4 (n mod 8) + (k mod 8)/2)
+        for (int i = threadIdx.x; i < 12 * m8; i += blockDim.x) {
+            const int kl = i & 7, cc = i >> 3;
+            const int c = cc % 12, row = (cc / 12) * 8 + kl;
+            const bool valid = row < he || (row >= t.e8 && row < t.e8 + ho);
+            int d[kTcSlices];
+            tc_digits(valid ? tc_fixed(sR[c * m8 + row], sF[c]) : 0, d);
+            __half* dst = sB + tc_core_off(c, row, t.k16);
+#pragma unroll
+            for (int s = 0; s < kTcSlices; ++s) dst[s * b_halves] = __int2half_rn(d[s]);
+        }
+        tc_fence_proxy();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        // (e) the digit-pair products, one thread issues
+        if (threadIdx.x == 0) {
+            *landed = tc_mbar_wait(&mbar[1], par, 1 << 22) ? 1 : 0;
+            if (*landed) {
+                const uint32_t a0 = tc_smem_u32(sA), b0 = tc_smem_u32(sB);
+                const uint32_t sbo = (uint32_t)t.k16 * 16;
+                const int nks = t.k16 / 16;
+                for (int sa = 0; sa < kTcSlices; ++sa) {
+                    const uint32_t idesc = tc_idesc(kTcN * (kTcSlices - sa));
+                    for (int ks = 0; ks < nks; ++ks) {
+                        const uint64_t da = tc_desc(a0 + (uint32_t)(sa * a_halves) * 2 + ks * 256, 128, sbo);
+                        const uint64_t db = tc_desc(b0 + ks * 256, 128, sbo);
+                        tc_mma(tmem + (uint32_t)(sa * kTcN), da, db, idesc, (sa > 0 || ks > 0) ? 1u : 0u);
+                    }
+                }
+            }
+            tc_commit(&mbar[0]);  // also when nothing was issued: the waiters are released
+        }
+        // (f) combine the accumulators of each row
+        const bool done = __syncthreads_and(tc_mbar_wait(&mbar[0], par, 1 << 22)) && *landed;
+        tc_fence_after();
+        if (!done) {
+            if (threadIdx.x == 0) atomicExch(err, 1);
+            ok = false;
+            break;  // uniform: no TMEM read, no further MMA
+        }
+        {
+            // warps w and w + 4 read the same TMEM lane quadrant (rows 32 (w%4)
+            // .. +31); the first combines columns 0..5, the second 6..11
+            const int w = threadIdx.x >> 5, quad = w & 3, half = (w >> 2) & 1;
+            if (w < 8 && 32 * quad < m8) {
+                long long T[6];
+#pragma unroll
+                for (int j = 0; j < 6; ++j) T[j] = 0;
+                for (int c = 0; c < kTcClasses; ++c) {
+                    float v[16];
+                    tc_ld16(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(c * kTcN), v);
+                    const long long wgt = 1LL << (7 * (kTcClasses - 1 - c));
+#pragma unroll
+                    for (int j = 0; j < 6; ++j) T[j] += (long long)tc_f2i(half ? v[6 + j] : v[j]) * wgt;
+                }
+                const int row = 32 * quad + (threadIdx.x & 31);
+                if (row < m8) {
+                    const int e = __ldg(&ops.tcE[(size_t)q * m8 + row]);
+#pragma unroll
+                    for (int j = 0; j < 6; ++j) {
+                        const int col = 6 * half + j;
+                        sR[col * m8 + row] = __ll2double_rn(T[j]) * tc_pow2(e + sF[col] - 52);
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        // (g) F* = x - f at the interior levels, the wall values at the walls
+        for (int i = threadIdx.x; i < nmode * 3 * he; i += blockDim.x) {
+            const int mi = i / (3 * he);
+            const int r = i - mi * 3 * he;
+            const int comp = r / he, k = r - comp * he;
+            const int ky = mi ? g.ny - kya : kya;
+            const int m = ky * g.nxhp + kx;
+            const int c0 = 6 * mi + 2 * comp;
+            const double2 xe = make_double2(sR[c0 * m8 + k], sR[(c0 + 1) * m8 + k]);
+            double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
+            if (comp < 2 && k == 0) {
+                const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
+                const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
+                bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
+            }
+            const double2* fc = fptr(F, comp);
+            double2* oc = fptr(Out, comp);
+            const size_t o1 = (size_t)k * g.nm + m;
+            if (k < ho) {
+                const double2 xo = make_double2(sR[c0 * m8 + t.e8 + k], sR[(c0 + 1) * m8 + t.e8 + k]);
+                const size_t o2 = (size_t)(nz - 1 - k) * g.nm + m;
+                oc[o1] = viscous_out_cn(g, k, make_double2(xe.x + xo.x, xe.y + xo.y), fc[o1], bc1, bc2);
+                oc[o2] = viscous_out_cn(g, nz - 1 - k, make_double2(xe.x - xo.x, xe.y - xo.y), fc[o2], bc1, bc2);
+            } else {
+                oc[o1] = viscous_out_cn(g, k, xe, fc[o1], bc1, bc2);
+            }
+        }
+        __syncthreads();  // shared buffers are reused by the next q
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) tc_dealloc(tmem, 128);
+}
+
+__global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepParams sp, Fields F, Fields Src,
+                                                    const double2* __restrict__ GP,
+                                                    const dns3d_pi_state* __restrict__ pi, Fields Out, int qpb,
+                                                    int* err) {
+    viscous_tc_body(g, ops, sp, F, Src, GP, pi, Out, qpb, blockIdx.x, err);
 }
 
 template <typename SrcC>
@@ -1773,6 +2022,7 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
     if ((e = set_smem(k_pressure, (2 * (size_t)g.nz * tile_cols(g, 2) + g.nz) * sizeof(double2)))) return e;
     if ((e = set_smem(k_correction, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
     if ((e = set_smem(k_divergence, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
+    if ((e = set_smem(k_viscous_tc, 0))) return e;
     if ((e = set_smem(k_pcg_poisson, pcg_smem(g)))) return e;
     if ((e = set_smem(k_pcg_helmholtz, pcg_smem(g)))) return e;
     return cudaSuccess;
@@ -1806,6 +2056,27 @@ cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& s
     const int tc = tile_width(g, kTileVisc);
     const size_t sm = 6 * (size_t)g.nz * tc * sizeof(double2);
     k_viscous<double2><<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, F, Src, GP, pi, Out, tc);
+    return cudaGetLastError();
+}
+
+size_t viscous_tc_smem(const GridDev& g) {
+    const TcGeom t = tc_geom(g.nz);
+    return (size_t)kTcSlices * (t.m8 + kTcN) * t.k16 * sizeof(__half) + (size_t)kTcN * t.m8 * sizeof(double) +
+           kTcN * sizeof(int) + 2 * sizeof(uint64_t) + 16;  // + TMEM address, arrival flag
+}
+
+bool viscous_tc_fits(const GridDev& g) {
+    return tc_supported(g.nz) && viscous_tc_smem(g) <= smem_limit(k_viscous_tc);
+}
+
+// operator indices q per CTA
+constexpr int kTcQPerCta = 2;
+
+cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F, Fields Src,
+                              const double2* GP, const dns3d_pi_state* pi, Fields Out, int* err, cudaStream_t s) {
+    if (!ops.tcA || !ops.tcE || !viscous_tc_fits(g)) return cudaErrorInvalidValue;
+    const int nb = (ops.nq + kTcQPerCta - 1) / kTcQPerCta;
+    k_viscous_tc<<<nb, 256, viscous_tc_smem(g), s>>>(g, ops, sp, F, Src, GP, pi, Out, kTcQPerCta, err);
     return cudaGetLastError();
 }
 
@@ -2024,8 +2295,13 @@ struct RsProd {
 };
 
 struct RsVisc64 {
-    static constexpr int kMinCtas = 3;
+    static constexpr int kMinCtas = 2;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        if (d.ops.tcA && d.sp.cn_identity) {
+            viscous_tc_body(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
+                            fields3(d.US, d.VS, d.WS), kTcQPerCta, b, d.tcerr);
+            return;
+        }
         viscous_body<double2>(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
                               fields3(d.US, d.VS, d.WS), d.g.tc[kTileVisc], b);
     }
@@ -2147,6 +2423,8 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
         case kRsProd:
         case kRsBc: return d.gx[stage];
         case kRsVisc:
+            if (!mixed && d.ops.tcA && d.sp.cn_identity) return (d.ops.nq + kTcQPerCta - 1) / kTcQPerCta;
+            return tiles;
         case kRsPres: return tiles;
         case kRsCorr: return mixed ? d.gx[stage] : tiles;
         case kRsViscMean:
@@ -2162,7 +2440,9 @@ size_t ragged_smem(int stage, bool mixed, const RunDesc& d) {
     const int tc = k >= 0 ? g.tc[k] : 0;
     switch (stage) {
         case kRsVort: return 2 * nz * tc * (mixed ? sizeof(float2) : sizeof(double2));
-        case kRsVisc: return mixed ? viscous_mixed_smem(g, tc) : 6 * nz * tc * sizeof(double2);
+        case kRsVisc:
+            if (!mixed && d.ops.tcA && d.sp.cn_identity) return viscous_tc_smem(g);
+            return mixed ? viscous_mixed_smem(g, tc) : 6 * nz * tc * sizeof(double2);
         case kRsPres: return mixed ? pressure_mixed_smem(g, tc) : (2 * nz * tc + nz) * sizeof(double2);
         case kRsCorr: return mixed ? 0 : nz * tc * sizeof(double2);
         case kRsViscMean: return mixed ? 6 * nz * sizeof(double2) : 0;

@@ -1,0 +1,207 @@
+// Tensor-core (tcgen05, sm_103a) building blocks and the emulated-FP64 layout
+// of the per-mode inverses.
+//
+// Emulated FP64 products (an Ozaki-style split into exact integer slices):
+// a matrix row is scaled by a power of two 2^e with |a_ij| < 2^e, rounded to
+// the integer U = round(a 2^(47-e)) (|U| <= 2^47) and written in 7 balanced
+// base-128 digits, U = sum_s c_s 128^(6-s), c_s in [-64, 63]; a right-hand
+// side column likewise with its own power of two 2^f.  Every digit is an
+// integer that FP16 holds exactly, so one tcgen05.mma (kind::f16, FP32
+// accumulation) of two digit matrices is exact while its sums stay below 2^24:
+// |c d| <= 2^12, times at most 127 terms of K, times at most 7 digit pairs
+// summed into one accumulator, is below 2^22.  The 28 pairs (s, t) with
+// s + t <= 6 go into 7 accumulators by weight class c = s + t, which are
+// combined exactly in 64-bit integers, T = sum_c D_c 128^(6-c), and
+// a b = T 2^(e+f-52) up to the dropped classes (relative 2^-47 of the row and
+// column scales), one int64->FP64 conversion and one power-of-two scaling per
+// output instead of a K-term FP64 dot product.
+//
+// Shared-memory operands: K-major, no swizzle, "core matrices" of 8 rows x 8
+// FP16 (16 bytes per row, 128 bytes per core matrix); K-adjacent core
+// matrices are 128 B apart (LBO), 8-row groups k16*16 B apart (SBO).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cstdint>
+
+namespace dns3d {
+
+constexpr int kTcSlices = 7;    // digits per value
+constexpr int kTcClasses = 7;   // digit-pair weight classes kept (s + t <= 6)
+constexpr int kTcN = 16;        // MMA N: columns of one right-hand-side block
+constexpr int kTcM = 128;       // MMA M (rows beyond m8 are ignored)
+
+// Block-diagonal placement of the folded operator diag(Ge, Go): even rows and
+// K indices at [0, he), odd ones at [e8, e8 + ho), each block padded to a
+// multiple of 8; K padded to a multiple of 16 for the MMA K-steps.
+struct TcGeom {
+    int he, ho, e8, o8, m8, k16, ncore_e, ncore_o;
+};
+
+__host__ __device__ inline TcGeom tc_geom(int nz) {
+    TcGeom t;
+    t.ho = nz / 2;
+    t.he = nz - t.ho;
+    t.e8 = (t.he + 7) / 8 * 8;
+    t.o8 = (t.ho + 7) / 8 * 8;
+    t.m8 = t.e8 + t.o8;
+    t.k16 = (t.m8 + 15) / 16 * 16;
+    t.ncore_e = (t.e8 / 8) * (t.e8 / 8);
+    t.ncore_o = (t.o8 / 8) * (t.o8 / 8);
+    return t;
+}
+
+// The block-diagonal operator must fit one M = 128 MMA.
+__host__ __device__ inline bool tc_supported(int nz) { return tc_geom(nz).m8 <= kTcM; }
+
+// Halves per q of the compact slice store: per digit, the nonzero core
+// matrices (even block row-major, then odd block), 64 halves each.
+__host__ __device__ inline size_t tc_q_halves(const TcGeom& t) {
+    return (size_t)kTcSlices * (t.ncore_e + t.ncore_o) * 64;
+}
+
+// Offset (in halves) of element (r, k) of a K-major operand with k16 columns.
+__host__ __device__ inline int tc_core_off(int r, int k, int k16) {
+    return ((r >> 3) * (k16 >> 3) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+// Balanced base-128 digits of |U| <= 2^47, most significant first.
+__device__ __forceinline__ void tc_digits(long long u, int* c) {
+#pragma unroll
+    for (int s = kTcSlices - 1; s >= 0; --s) {
+        const int r = (int)(u & 127);
+        const int d = r >= 64 ? r - 128 : r;
+        c[s] = d;
+        u = (u - d) >> 7;
+    }
+}
+
+// round(x 2^(47-f)) for |x| < 2^f, from the bits of x (integer operations only).
+__device__ __forceinline__ long long tc_fixed(double x, int f) {
+    const long long b = __double_as_longlong(x);
+    int ex = (int)((b >> 52) & 0x7FF);
+    long long m = b & 0xFFFFFFFFFFFFFLL;
+    if (ex == 0) {
+        if (m == 0) return 0;
+        ex = 1;  // subnormal: no implicit bit
+    } else {
+        m |= 1LL << 52;
+    }
+    const int sh = 1028 + f - ex;  // x = m 2^(ex-1075); U = m 2^(ex-1075+47-f)
+    if (sh >= 62) return 0;
+    const long long u = sh > 0 ? (m + (1LL << (sh - 1))) >> sh : m << (-sh);
+    return b < 0 ? -u : u;
+}
+
+// Smallest f with |x| < 2^f for the largest |x| given by its bits (0 if zero).
+__device__ __forceinline__ int tc_exponent(unsigned long long absbits) {
+    if (absbits == 0) return 0;
+    const int ex = (int)(absbits >> 52);
+    return (ex == 0 ? -1022 : ex - 1023) + 1;
+}
+
+// Exact FP32 integer (|v| < 2^22) to int.
+__device__ __forceinline__ int tc_f2i(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
+
+// 2^e as a double (the few exponents outside the normal range via ldexp).
+__device__ __forceinline__ double tc_pow2(int e) {
+    if (e > -1023 && e < 1024) return __longlong_as_double((long long)(e + 1023) << 52);
+    return ldexp(1.0, e);
+}
+
+__device__ __forceinline__ uint32_t tc_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version of the sm_100 family; no swizzle, base offset 0
+    return d;
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, FP16 A and B, both
+// K-major, M = kTcM, N = n (a multiple of 16 up to 256).
+__device__ __forceinline__ uint32_t tc_idesc(int n) {
+    return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_alloc(uint32_t* dst_smem, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem_u32(dst_smem)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// Arms the barrier's current phase for `bytes` of asynchronous copies (one arrival).
+__device__ __forceinline__ void tc_mbar_expect(uint64_t* mbar, uint32_t bytes) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\t"
+        "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}\n" ::"r"(tc_smem_u32(mbar)),
+        "r"(bytes));
+}
+
+// Bulk copy global -> shared (16-byte aligned, size a multiple of 16),
+// completing on the barrier's transaction count.
+__device__ __forceinline__ void tc_bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            tc_smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(tc_smem_u32(mbar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+        tc_smem_u32(mbar)));
+}
+
+__device__ __forceinline__ void tc_mbar_init(uint64_t* mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem_u32(mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+}
+
+// Waits for phase `parity` of the barrier, at most `limit` polls; true if it completed.
+__device__ __forceinline__ bool tc_mbar_wait(uint64_t* mbar, uint32_t parity, int limit) {
+    uint32_t done = 0;
+    for (int it = 0; it < limit && !done; ++it) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(tc_smem_u32(mbar)), "r"(parity));
+    }
+    return done != 0;
+}
+
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane (the
+// warp reads lanes 32*(warp%4) .. +31).
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;"); }
+// generic-proxy shared-memory writes visible to the tensor cores
+__device__ __forceinline__ void tc_fence_proxy() { asm volatile("fence.proxy.async.shared::cta;"); }
+
+}  // namespace dns3d

@@ -1,0 +1,79 @@
+"""GPU: the Crank-Nicolson viscous solve on the tensor cores (emulated FP64:
+FP16 digit slices of the per-mode inverses and right-hand sides, exact FP32
+tcgen05 accumulation, integer combination) keeps the plain path's parity bar
+against the oracle, agrees with the FP64-pipe kernel to 2^-47 of the operand
+scales, and gives the same bits in a batch as alone."""
+import numpy as np
+import pytest
+
+from f90_dns_gb300 import ChannelDNS, Ensemble, config_from
+from f90_dns_gb300.workloads import WORKLOADS, ensemble_draws
+from oracle import dns3d_ref as ref
+from tests.helpers import oracle_config, velocity_errors
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+C1 = WORKLOADS["channel_32x32x33_re180_dpdx"]
+C2 = WORKLOADS["channel_128x128x65_re180_pi"]
+
+
+def _names(d):
+    return set(d.profile_kernels(1))
+
+
+@pytest.mark.parametrize("wl", [C1, dict(C1, nx=16, ny=24, nz=65, lgl_dmatrix_guard=False, flow_control_method=2,
+                                          target_bulk_velocity=2.0 / 3.0, controller_gain=0.5,
+                                          controller_update_freq=1)])
+def test_tensor_core_viscous_matches_oracle(built_lib, monkeypatch, wl):
+    monkeypatch.setenv("DNS3D_TENSOR_CORES", "1")
+    with ChannelDNS(config_from(wl)) as d:
+        assert "viscous_helmholtz_tc" in _names(d)
+    with ChannelDNS(config_from(wl)) as d:
+        d.step(50)
+        gst = d.get_state()
+        gdiag = d.diagnostics()
+    cfg = oracle_config(wl)
+    g, st, hist = ref.run(cfg, 50, record_every=50)
+    err = velocity_errors(gst, st)
+    assert max(err["u"], err["v"], err["w"]) <= TOL, err
+    assert err["p_total"] <= TOL, err
+    assert abs(gdiag.energy - hist[-1]["energy"]) <= TOL * hist[-1]["energy"]
+
+
+def test_tensor_core_viscous_agrees_with_fp64_pipe(built_lib, monkeypatch):
+    wl = dict(C2, nx=64, ny=64, noise_amplitude=0.0)
+    out = {}
+    for mode, name in (("1", "viscous_helmholtz_tc"), ("0", "viscous_helmholtz")):
+        monkeypatch.setenv("DNS3D_TENSOR_CORES", mode)
+        with ChannelDNS(config_from(wl)) as d:
+            assert name in _names(d)
+        with ChannelDNS(config_from(wl)) as d:
+            d.step(1)
+            one = d.get_state(walls=False)
+            d.step(9)
+            out[mode] = (one, d.get_state(walls=False), d.diagnostics())
+    scale = max(np.max(np.abs(out["0"][1][k])) for k in ("u", "v", "w"))
+    # 2^-47 of the row and column scales per product, K = 65 terms: ~1e-12 of
+    # the velocity scale per step
+    for i, bound in ((0, 3e-12), (1, 2e-11)):
+        for k in ("u", "v", "w"):
+            assert np.max(np.abs(out["1"][i][k] - out["0"][i][k])) <= bound * scale, (i, k)
+    assert abs(out["1"][2].energy - out["0"][2].energy) <= 1e-12 * out["0"][2].energy
+
+
+def test_tensor_core_runs_in_batches_bitwise(built_lib, monkeypatch):
+    monkeypatch.setenv("DNS3D_TENSOR_CORES", "1")
+    draws = ensemble_draws(4, seed=13)
+    cfgs = [config_from(d) for d in draws]
+    with Ensemble(cfgs) as ens:
+        ens.step(3)
+        states = [ens.run(i).get_state(walls=False) for i in range(len(ens))]
+    for cfg, st in zip(cfgs, states):
+        with ChannelDNS(cfg) as d:
+            assert "viscous_helmholtz_tc" in _names(d)
+        with ChannelDNS(cfg) as d:
+            d.step(3)
+            solo = d.get_state(walls=False)
+        for k in ("u", "v", "w", "p_total"):
+            assert np.array_equal(st[k], solo[k]), (cfg.nx, cfg.ny, cfg.nz, k)
