@@ -58,7 +58,8 @@ struct RunDesc {
     const void* tw_nx;
     int* tcerr;              // tensor-core wait status of the run (viscous stage)
     int ncol;                // columns the forward y pass completes
-    int gx[kRsStages];       // virtual blocks per field of each stage (transforms, elementwise passes)
+    int gx[kRsStages];       // virtual blocks per field of each stage (transforms, elementwise passes);
+                             // kRsVisc: operator indices per CTA of the tensor-core viscous body
 };
 
 // Work map of one stage launch (device arrays).

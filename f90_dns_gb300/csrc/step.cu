@@ -557,24 +557,35 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     bool ok = true;
     for (int q = q0; q < q1 && ok; ++q) {
         const uint32_t par = (uint32_t)((q - q0) & 1);
-        // (a) digit slices of the operator: per digit, one copy per 8-row group
-        if (threadIdx.x == 0) {
-            tc_mbar_expect(&mbar[1], (uint32_t)(qh * sizeof(__half)));
+        // (a) digit slices of the operator: per digit, one copy per 8-row
+        // group, issued by the lanes of the last warp (the one with the least
+        // right-hand-side work below)
+        if ((int)threadIdx.x >= (int)blockDim.x - 32) {
+            const int lane = threadIdx.x & 31;
+            if (lane == 0) tc_mbar_expect(&mbar[1], (uint32_t)(qh * sizeof(__half)));
+            __syncwarp();
             const __half* src = ops.tcA + (size_t)q * qh;
-            for (int s = 0; s < kTcSlices; ++s) {
+            const int ngrp = nbe + nbo;
+            for (int j = lane; j < kTcSlices * ngrp; j += 32) {
+                const int s = j / ngrp, gm = j - s * ngrp;
                 const __half* ss = src + (size_t)s * ncore * 64;
                 __half* ds = sA + s * a_halves;
-                for (int gm = 0; gm < nbe; ++gm)
+                if (gm < nbe)
                     tc_bulk_g2s(ds + tc_core_off(gm * 8, 0, t.k16), ss + (size_t)gm * nbe * 64, nbe * 128, &mbar[1]);
-                for (int gm = 0; gm < nbo; ++gm)
-                    tc_bulk_g2s(ds + tc_core_off(t.e8 + gm * 8, t.e8, t.k16),
-                                ss + (size_t)(t.ncore_e + gm * nbo) * 64, nbo * 128, &mbar[1]);
+                else
+                    tc_bulk_g2s(ds + tc_core_off(t.e8 + (gm - nbe) * 8, t.e8, t.k16),
+                                ss + (size_t)(t.ncore_e + (gm - nbe) * nbo) * 64, nbo * 128, &mbar[1]);
             }
         }
         // (b) folded right-hand sides: column 6 mi + 2 comp + (0 re, 1 im)
         const int kya = q / g.nxhp, kx = q - kya * g.nxhp;
         const int nmode = (kya > 0 && 2 * kya != g.ny) ? 2 : 1;
-        for (int i = threadIdx.x; i < 6 * he; i += blockDim.x) {
+        // the state values at the item's two levels, kept for (g) (items
+        // i = threadIdx.x + p blockDim.x, p < 2, hold theirs in registers)
+        double2 keep1[2], keep2[2];
+#pragma unroll
+        for (int p = 0; p < 2; ++p) keep1[p] = keep2[p] = make_double2(0.0, 0.0);
+        for (int i = threadIdx.x, p = 0; i < 6 * he; i += blockDim.x, ++p) {
             const int mi = i / (3 * he);
             const int r = i - mi * 3 * he;
             const int comp = r / he, k = r - comp * he;
@@ -593,10 +604,16 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                 const double2* sc = fptr(Src, comp);
                 const double2 f1 = fc[m], fn = fc[(size_t)(nz - 1) * g.nm + m];
                 const size_t o1 = (size_t)k * g.nm + m, o2 = (size_t)(nz - 1 - k) * g.nm + m;
-                const double2 b1 = viscous_rhs_cn(g, ops, sp, comp, k, m, ky, kx, fc[o1], sc[o1], f1, fn, bc1, bc2, dpdx);
+                const double2 v1 = fc[o1], v2 = k < ho ? fc[o2] : v1;
+                if (p < 2) {
+                    // (p is 0 or 1 here whenever 6 he <= 2 blockDim.x)
+                    if (p == 0) { keep1[0] = v1; keep2[0] = v2; }
+                    else { keep1[1] = v1; keep2[1] = v2; }
+                }
+                const double2 b1 = viscous_rhs_cn(g, ops, sp, comp, k, m, ky, kx, v1, sc[o1], f1, fn, bc1, bc2, dpdx);
                 if (k < ho) {
                     const double2 b2 =
-                        viscous_rhs_cn(g, ops, sp, comp, nz - 1 - k, m, ky, kx, fc[o2], sc[o2], f1, fn, bc1, bc2, dpdx);
+                        viscous_rhs_cn(g, ops, sp, comp, nz - 1 - k, m, ky, kx, v2, sc[o2], f1, fn, bc1, bc2, dpdx);
                     fe = make_double2(b1.x + b2.x, b1.y + b2.y);
                     fo = make_double2(b1.x - b2.x, b1.y - b2.y);
                 } else {
@@ -705,7 +722,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
         tc_fence_before();
         __syncthreads();
         // (g) F* = x - f at the interior levels, the wall values at the walls
-        for (int i = threadIdx.x; i < nmode * 3 * he; i += blockDim.x) {
+        for (int i = threadIdx.x, p = 0; i < nmode * 3 * he; i += blockDim.x, ++p) {
             const int mi = i / (3 * he);
             const int r = i - mi * 3 * he;
             const int comp = r / he, k = r - comp * he;
@@ -722,14 +739,17 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             }
             const double2* fc = fptr(F, comp);
             double2* oc = fptr(Out, comp);
-            const size_t o1 = (size_t)k * g.nm + m;
+            const size_t o1 = (size_t)k * g.nm + m, o2 = (size_t)(nz - 1 - k) * g.nm + m;
+            double2 v1, v2;
+            if (p == 0) { v1 = keep1[0]; v2 = keep2[0]; }
+            else if (p == 1) { v1 = keep1[1]; v2 = keep2[1]; }
+            else { v1 = fc[o1]; v2 = k < ho ? fc[o2] : v1; }
             if (k < ho) {
                 const double2 xo = make_double2(sR[c0 * m8 + t.e8 + k], sR[(c0 + 1) * m8 + t.e8 + k]);
-                const size_t o2 = (size_t)(nz - 1 - k) * g.nm + m;
-                oc[o1] = viscous_out_cn(g, k, make_double2(xe.x + xo.x, xe.y + xo.y), fc[o1], bc1, bc2);
-                oc[o2] = viscous_out_cn(g, nz - 1 - k, make_double2(xe.x - xo.x, xe.y - xo.y), fc[o2], bc1, bc2);
+                oc[o1] = viscous_out_cn(g, k, make_double2(xe.x + xo.x, xe.y + xo.y), v1, bc1, bc2);
+                oc[o2] = viscous_out_cn(g, nz - 1 - k, make_double2(xe.x - xo.x, xe.y - xo.y), v2, bc1, bc2);
             } else {
-                oc[o1] = viscous_out_cn(g, k, xe, fc[o1], bc1, bc2);
+                oc[o1] = viscous_out_cn(g, k, xe, v1, bc1, bc2);
             }
         }
         __syncthreads();  // shared buffers are reused by the next q
@@ -2069,14 +2089,17 @@ bool viscous_tc_fits(const GridDev& g) {
     return tc_supported(g.nz) && viscous_tc_smem(g) <= smem_limit(k_viscous_tc);
 }
 
-// operator indices q per CTA
-constexpr int kTcQPerCta = 2;
+// Operator indices q per CTA: one per four waves of single-q CTAs (two CTAs
+// on each of 152 SMs), at most 4.  Which CTA takes a q does not change its
+// arithmetic.
+int tc_q_per_cta(int nq) { return std::max(1, std::min(4, nq / (4 * 2 * 152))); }
 
 cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F, Fields Src,
                               const double2* GP, const dns3d_pi_state* pi, Fields Out, int* err, cudaStream_t s) {
     if (!ops.tcA || !ops.tcE || !viscous_tc_fits(g)) return cudaErrorInvalidValue;
-    const int nb = (ops.nq + kTcQPerCta - 1) / kTcQPerCta;
-    k_viscous_tc<<<nb, 256, viscous_tc_smem(g), s>>>(g, ops, sp, F, Src, GP, pi, Out, kTcQPerCta, err);
+    const int qpb = tc_q_per_cta(ops.nq);
+    const int nb = (ops.nq + qpb - 1) / qpb;
+    k_viscous_tc<<<nb, 256, viscous_tc_smem(g), s>>>(g, ops, sp, F, Src, GP, pi, Out, qpb, err);
     return cudaGetLastError();
 }
 
@@ -2299,7 +2322,7 @@ struct RsVisc64 {
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
         if (d.ops.tcA && d.sp.cn_identity) {
             viscous_tc_body(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
-                            fields3(d.US, d.VS, d.WS), kTcQPerCta, b, d.tcerr);
+                            fields3(d.US, d.VS, d.WS), d.gx[kRsVisc], b, d.tcerr);
             return;
         }
         viscous_body<double2>(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
@@ -2398,6 +2421,7 @@ void ragged_geometry(RunDesc& d) {
     d.gx[kRsFftYFwd] = cdiv((long long)g.nz * d.ncol, cy);
     d.gx[kRsCorr] = cdiv((long long)g.nz * g.nm, 4 * kStageThreads);
     d.gx[kRsBc] = cdiv(2LL * g.nm, kStageThreads);
+    d.gx[kRsVisc] = tc_q_per_cta(d.ops.nq);  // operator indices per CTA of the tensor-core viscous body
 }
 
 int ragged_tile_kernel(int stage, bool mixed) {
@@ -2423,7 +2447,7 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
         case kRsProd:
         case kRsBc: return d.gx[stage];
         case kRsVisc:
-            if (!mixed && d.ops.tcA && d.sp.cn_identity) return (d.ops.nq + kTcQPerCta - 1) / kTcQPerCta;
+            if (!mixed && d.ops.tcA && d.sp.cn_identity) return (d.ops.nq + d.gx[kRsVisc] - 1) / d.gx[kRsVisc];
             return tiles;
         case kRsPres: return tiles;
         case kRsCorr: return mixed ? d.gx[stage] : tiles;
