@@ -57,6 +57,10 @@ struct dns3d_handle {
     // autotuner unless DNS3D_TENSOR_CORES forces it (1) or rules it out (0)
     bool visc_tc = false;
     bool visc_tc_forced = false;
+    // the vorticity's and the projection's z-derivatives on the tensor cores
+    // (ops.tcD built), chosen likewise
+    bool vort_tc = false;
+    bool corr_tc = false;
     int red_blocks = 0;
     std::vector<double> zpts, zwts;
     std::vector<void*> allocs;
@@ -385,8 +389,13 @@ int run_source_terms(dns3d_handle* h) {
 int run_source_terms_fp64(dns3d_handle* h, double2* const* in) {
     const GridDev& g = h->g;
     // vorticity into the u*,v*,w* buffers (free until the viscous step)
-    CK(h, launch_vorticity(g, h->ops, in[0], in[1], in[2], h->US, h->VS, h->WS, h->stream));
-    mark(h, "vorticity");
+    if (h->vort_tc) {
+        CK(h, launch_vorticity_tc(g, h->ops, in[0], in[1], in[2], h->US, h->VS, h->WS, h->d_tcerr, h->stream));
+        mark(h, "vorticity_tc");
+    } else {
+        CK(h, launch_vorticity(g, h->ops, in[0], in[1], in[2], h->US, h->VS, h->WS, h->stream));
+        mark(h, "vorticity");
+    }
     Fields spec{};
     spec.p[0] = in[0]; spec.p[1] = in[1]; spec.p[2] = in[2];
     spec.p[3] = h->US; spec.p[4] = h->VS; spec.p[5] = h->WS;
@@ -475,6 +484,12 @@ int run_correction(dns3d_handle* h) {
         CK(h, launch_correction_mixed(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->U, h->V, h->W,
                                       h->P, h->GP, h->stream));
         mark(h, "correction_mixed");
+        return DNS3D_OK;
+    }
+    if (h->corr_tc) {
+        CK(h, launch_correction_tc(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
+                                   h->GP, h->d_tcerr, h->stream));
+        mark(h, "pressure_correction_tc");
         return DNS3D_OK;
     }
     CK(h, launch_correction(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
@@ -575,9 +590,11 @@ int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
     b += (2 * nq * (ez * ez + hz * hz) + 2 * nz2) * sizeof(double);  // folded inverses, pinned, S
     if (c->precision == DNS3D_PREC_MIXED)
         b += (6 + 3 + 6) * se * sizeof(float2) + 6 * pe * sizeof(float) + se * sizeof(double2);  // + dphi/dz
-    else if (c->use_crank_nicolson && c->linear_solver == 0 && tc_supported(c->nz)) {
-        const TcGeom t = tc_geom(c->nz);  // digit slices of the Helmholtz inverses
-        b += nq * (tc_q_halves(t) * sizeof(__half) + (size_t)t.m8 * sizeof(int));
+    else if (tc_supported(c->nz)) {
+        const TcGeom t = tc_geom(c->nz);
+        if (c->use_crank_nicolson && c->linear_solver == 0)  // digit slices of the Helmholtz inverses
+            b += nq * (tc_q_halves(t) * sizeof(__half) + (size_t)t.m8 * sizeof(int));
+        b += (size_t)kTcSlices * t.m8 * t.k16 * sizeof(__half);  // digit image of D1
     }
     b += 16ull << 20;                        // operators, tables, reductions
     *bytes = b;
@@ -597,8 +614,8 @@ namespace {
 // thread's fixed-order sum, so results are bitwise the same for any width.
 using TuneKey = std::tuple<int, int, int, int, int>;
 std::mutex g_tune_mu;
-// the widths, then 1 if the viscous solve runs on the tensor cores
-std::map<TuneKey, std::array<int, kTileKernels + 1>> g_tune;
+// the widths, then 1 if the viscous solve, the vorticity, the projection runs on the tensor cores
+std::map<TuneKey, std::array<int, kTileKernels + 3>> g_tune;
 
 int tile_launch(dns3d_handle* h, int k) {
     const GridDev& g = h->g;
@@ -635,7 +652,7 @@ int tile_launch(dns3d_handle* h, int k) {
 int autotune(dns3d_handle* h, bool force) {
     CK(h, cudaSetDevice(h->cfg.device));
     // precision, and for FP64 whether the tensor-core solve exists / is forced
-    const int variant = h->mixed ? 1 : (h->ops.tcA ? (h->visc_tc_forced ? 4 : 2) : 0);
+    const int variant = h->mixed ? 1 : (h->ops.tcA || h->ops.tcD ? (h->visc_tc_forced ? 4 : 2) : 0);
     const TuneKey key{h->cfg.nx, h->cfg.ny, h->cfg.nz, variant, h->cfg.device};
     if (!force) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -643,6 +660,10 @@ int autotune(dns3d_handle* h, bool force) {
         if (it != g_tune.end()) {
             for (int k = 0; k < kTileKernels; ++k) h->g.tc[k] = it->second[k];
             if (h->ops.tcA && !h->visc_tc_forced) h->visc_tc = it->second[kTileKernels] != 0;
+            if (h->ops.tcD && !h->visc_tc_forced) {
+                h->vort_tc = it->second[kTileKernels + 1] != 0;
+                h->corr_tc = it->second[kTileKernels + 2] != 0;
+            }
             return DNS3D_OK;
         }
     }
@@ -652,7 +673,7 @@ int autotune(dns3d_handle* h, bool force) {
     // the FP64-pipe viscous kernel (last in kFp64) is not timed when the
     // tensor-core one is forced
     const int nk = h->mixed ? 3 : (h->visc_tc_forced ? 3 : 4);
-    float visc_ms = 0.f;
+    float visc_ms = 0.f, vort_ms = 0.f, corr_ms = 0.f;
     cudaEvent_t e0, e1;
     CK(h, cudaEventCreate(&e0));
     CK(h, cudaEventCreate(&e1));
@@ -676,6 +697,8 @@ int autotune(dns3d_handle* h, bool force) {
         }
         h->g.tc[k] = best;  // 0 (heuristic) if no candidate fitted
         if (k == kTileVisc) visc_ms = best_ms;
+        if (k == kTileVort) vort_ms = best_ms;
+        if (k == kTileCorr) corr_ms = best_ms;
     }
     // the tensor-core viscous solve against the best FP64-pipe width
     if (!rc && !h->mixed && h->ops.tcA && !h->visc_tc_forced) {
@@ -697,6 +720,47 @@ int autotune(dns3d_handle* h, bool force) {
             h->visc_tc = visc_ms <= 0.f || ms < visc_ms;
         }
     }
+    // the tensor-core vorticity against the best FP64-pipe width
+    if (!rc && !h->mixed && h->ops.tcD && !h->visc_tc_forced) {
+        auto launch = [&] {
+            return launch_vorticity_tc(h->g, h->ops, h->U, h->V, h->W, h->US, h->VS, h->WS, h->d_tcerr, h->stream);
+        };
+        cudaError_t ce = launch();
+        if (!ce) ce = cudaEventRecord(e0, h->stream);
+        for (int r = 0; r < 3 && !ce; ++r) ce = launch();
+        if (!ce) ce = cudaEventRecord(e1, h->stream);
+        if (!ce) ce = cudaEventSynchronize(e1);
+        if (ce) {
+            rc = cuda_fail(h, ce, "autotune (tensor-core vorticity)");
+        } else {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            h->vort_tc = vort_ms <= 0.f || ms < vort_ms;
+        }
+    }
+    // the tensor-core projection against the best FP64-pipe width (outputs
+    // that are state go to scratch, as in tile_launch)
+    if (!rc && !h->mixed && h->ops.tcD && !h->visc_tc_forced) {
+        const size_t se = spec_elems(h->cfg);
+        double2* T[5];
+        for (int f = 0; f < 5; ++f) T[f] = h->fft.tmp + (size_t)f * se;
+        auto launch = [&] {
+            return launch_correction_tc(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, T[0], T[1], T[2], T[3],
+                                        T[4], h->d_tcerr, h->stream);
+        };
+        cudaError_t ce = launch();
+        if (!ce) ce = cudaEventRecord(e0, h->stream);
+        for (int r = 0; r < 3 && !ce; ++r) ce = launch();
+        if (!ce) ce = cudaEventRecord(e1, h->stream);
+        if (!ce) ce = cudaEventSynchronize(e1);
+        if (ce) {
+            rc = cuda_fail(h, ce, "autotune (tensor-core projection)");
+        } else {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            h->corr_tc = corr_ms <= 0.f || ms < corr_ms;
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
@@ -705,9 +769,11 @@ int autotune(dns3d_handle* h, bool force) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
     }
-    std::array<int, kTileKernels + 1> tiles{};
+    std::array<int, kTileKernels + 3> tiles{};
     for (int k = 0; k < kTileKernels; ++k) tiles[k] = h->g.tc[k];
     tiles[kTileKernels] = h->visc_tc ? 1 : 0;
+    tiles[kTileKernels + 1] = h->vort_tc ? 1 : 0;
+    tiles[kTileKernels + 2] = h->corr_tc ? 1 : 0;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[key] = tiles;
     return DNS3D_OK;
@@ -1111,6 +1177,24 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
         // without timing: the tensor-core kernel once the grid has a few waves
         // of operator pairs and two of its CTAs fit an SM
         h->visc_tc = h->visc_tc_forced || (nq >= 8 * 152 && viscous_tc_smem(g) <= 113 * 1024);
+    }
+    // the folded D1 as a digit image for the tensor-core vorticity (FP64 runs)
+    if (!h->mixed && !(tcenv && std::strcmp(tcenv, "0") == 0) && vorticity_tc_fits(g)) {
+        const TcGeom t = tc_geom(nz);
+        __half* im = nullptr;
+        int* ex = nullptr;
+        if ((rc = dev_alloc(h, &im, (size_t)kTcSlices * t.m8 * t.k16)) || (rc = dev_alloc(h, &ex, (size_t)t.m8)))
+            return fail(rc);
+        if ((e = build_tc_anti_image(g, ops.D1e, ops.D1o, im, ex, h->stream)) ||
+            (e = cudaStreamSynchronize(h->stream))) {
+            cuda_fail(h, e, "build_tc_anti_image");
+            return fail(DNS3D_E_CUDA);
+        }
+        ops.tcD = im;
+        ops.tcDE = ex;
+        h->visc_tc_forced = tcenv && std::strcmp(tcenv, "1") == 0;
+        h->vort_tc = h->visc_tc_forced || g.nm >= 4 * 152 * 8;
+        h->corr_tc = h->visc_tc_forced || g.nm >= 4 * 152 * 16;
     }
 
     if ((rc = dns3d_initialize_fields(h))) return fail(rc);
@@ -1769,6 +1853,11 @@ RunDesc make_desc(const dns3d_handle* h) {
     if (!h->visc_tc) {
         d.ops.tcA = nullptr;
         d.ops.tcE = nullptr;
+    }
+    d.tcmask = (h->vort_tc ? 1 : 0) | (h->corr_tc ? 2 : 0);
+    if (!d.tcmask) {
+        d.ops.tcD = nullptr;
+        d.ops.tcDE = nullptr;
     }
     d.mx = h->mx;
     d.sp = h->sp;

@@ -162,6 +162,9 @@ struct Ops {
     // [nq][tc_q_halves] and row exponents [nq][m8]
     const __half* tcA;
     const int* tcE;
+    // tensor-core digit image of the folded D1 ([[0, De], [Do, 0]]), or null
+    const __half* tcD;
+    const int* tcDE;
 };
 
 // Mixed-precision operators (FP32): folded D for the nonlinear term and the
@@ -242,6 +245,16 @@ cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams
                               const double2* GP, const dns3d_pi_state* pi, Fields Out, int* err, cudaStream_t s);
 size_t viscous_tc_smem(const GridDev& g);
 bool viscous_tc_fits(const GridDev& g);
+// The vorticity with the z-derivatives D1.u, D1.v on the tensor cores in
+// emulated FP64 (ops.tcD set); err as for launch_viscous_tc.
+cudaError_t launch_vorticity_tc(const GridDev& g, const Ops& ops, const double2* U, const double2* V,
+                                const double2* W, double2* OX, double2* OY, double2* OZ, int* err, cudaStream_t s);
+// pressure_correction_3d with D1.phi on the tensor cores (ops.tcD set)
+cudaError_t launch_correction_tc(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                                 const double2* VS, const double2* WS, const double2* PHI, double2* U, double2* V,
+                                 double2* W, double2* P, double2* GP, int* err, cudaStream_t s);
+size_t vorticity_tc_smem(const GridDev& g);
+bool vorticity_tc_fits(const GridDev& g);
 cudaError_t launch_vorticity_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops,
                                    const double2* U, const double2* V, const double2* W, FFields out,
                                    cudaStream_t s);
@@ -316,6 +329,11 @@ cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh,
 // (tc.cuh); slices [nq][tc_q_halves], rowexp [nq][m8].
 cudaError_t build_tc_slices(const GridDev& g, const double* invF, int nq, __half* slices, int* rowexp,
                             cudaStream_t s);
+
+// Digit image ([kTcSlices][m8 x k16] FP16, rowexp [m8]) of the folded
+// z-derivative [[0, De], [Do, 0]] for the tensor-core contractions (tc.cuh).
+cudaError_t build_tc_anti_image(const GridDev& g, const double* De, const double* Do, __half* image, int* rowexp,
+                                cudaStream_t s);
 
 // Dense FP64 FMA throughput probe (TFLOP/s).
 cudaError_t measure_fp64_tflops(int device, double* tflops);

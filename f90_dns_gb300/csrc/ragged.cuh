@@ -60,6 +60,8 @@ struct RunDesc {
     int ncol;                // columns the forward y pass completes
     int gx[kRsStages];       // virtual blocks per field of each stage (transforms, elementwise passes);
                              // kRsVisc: operator indices per CTA of the tensor-core viscous body
+    int tcmask;              // z-derivatives on the tensor cores: 1 vorticity, 2 projection
+    int vort_chunk, corr_chunk;  // mode tiles per CTA of those bodies
 };
 
 // Work map of one stage launch (device arrays).

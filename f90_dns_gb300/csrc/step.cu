@@ -767,6 +767,274 @@ __global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepPara
     viscous_tc_body(g, ops, sp, F, Src, GP, pi, Out, qpb, blockIdx.x, err);
 }
 
+// ------------------------------------------------------------------ tensor-core z-derivatives
+// The fixed z-derivative D1 (folded, block anti-diagonal [[0, De], [Do, 0]] on
+// [fe; fo]) applied to Op::kFields spectral fields as emulated-FP64
+// tensor-core products (tc.cuh), then Op::out forms the kernel's outputs from
+// the derivatives exactly as the FP64-pipe kernel does.  D1 is the same for
+// every mode, so its digit image is copied into shared memory once per CTA
+// and a CTA runs tiles of 32 right-hand-side columns (modes x fields x re/im).
+// Per tile: (b) fold the fields; (c) column scales; (d) digits; (e) 35 MMAs
+// (digit slice sa of D1 against right-hand-side digit slices 0..6-sa side by
+// side, N = 32 (7-sa)) into 7 weight-class accumulators (224 TMEM columns);
+// (f) exact int64 combination -> D1.f in FP64; (g) Op::out per level pair.
+constexpr int kTcVortCols = 32;
+constexpr int kTcVortThreads = 512;
+
+template <class Op>
+__device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, const Op& op, int tile0, int tile1,
+                                           int* err) {
+    constexpr int kModes = kTcVortCols / (2 * Op::kFields);
+    extern __shared__ __align__(128) unsigned char tcsm[];
+    const TcGeom t = tc_geom(g.nz);
+    const int nz = g.nz, he = t.he, ho = t.ho, m8 = t.m8;
+    const int a_halves = m8 * t.k16, b_halves = kTcVortCols * t.k16;
+    __half* sA = reinterpret_cast<__half*>(tcsm);
+    __half* sB = sA + kTcSlices * a_halves;
+    double* sR = reinterpret_cast<double*>(sB + kTcSlices * b_halves);  // [32][m8]: folded u, v, then D1.u, D1.v
+    int* sE = reinterpret_cast<int*>(sR + kTcVortCols * m8);            // row exponents of D1
+    int* sF = sE + m8;                                                  // column exponents
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcVortCols);     // [0] MMAs done, [1] D1 landed
+    uint32_t* tbase = reinterpret_cast<uint32_t*>(mbar + 2);
+    int* landed = reinterpret_cast<int*>(tbase + 1);
+    const int tid = threadIdx.x;
+    {
+        uint4* z = reinterpret_cast<uint4*>(sB);
+        for (int i = tid; i < kTcSlices * b_halves / 8; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    for (int i = tid; i < m8; i += blockDim.x) sE[i] = __ldg(&ops.tcDE[i]);
+    if (tid < 32) tc_alloc(tbase, 256);
+    if (tid == 0) {
+        tc_mbar_init(&mbar[0]);
+        tc_mbar_init(&mbar[1]);
+        *landed = 0;
+    }
+    tc_fence_proxy();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tbase;
+    if (tid == 0) {  // the D1 digit image, once
+        tc_mbar_expect(&mbar[1], (uint32_t)(kTcSlices * a_halves * sizeof(__half)));
+        for (int s = 0; s < kTcSlices; ++s)
+            tc_bulk_g2s(sA + s * a_halves, ops.tcD + (size_t)s * a_halves, (uint32_t)(a_halves * sizeof(__half)),
+                        &mbar[1]);
+    }
+    const int nv = he + ho;
+    for (int tile = tile0; tile < tile1; ++tile) {
+        const uint32_t par = (uint32_t)((tile - tile0) & 1);
+        const int m0 = tile * kModes;
+        // (b) folded fields: column 2 (kFields mi + f) + (0 re, 1 im)
+        for (int i = tid; i < Op::kFields * kModes * he; i += blockDim.x) {
+            const int mi = i / (Op::kFields * he);
+            const int r = i - mi * Op::kFields * he;
+            const int f = r / he, k = r - f * he;
+            const int m = m0 + mi;
+            const double2* src = op.field(f);
+            double2 a = make_double2(0.0, 0.0), b = a;
+            if (m < g.nm) {
+                a = src[(size_t)k * g.nm + m];
+                if (k < ho) b = src[(size_t)(nz - 1 - k) * g.nm + m];
+            }
+            const int c0 = 2 * (Op::kFields * mi + f);
+            if (k < ho) {
+                sR[c0 * m8 + k] = a.x + b.x;
+                sR[(c0 + 1) * m8 + k] = a.y + b.y;
+                sR[c0 * m8 + t.e8 + k] = a.x - b.x;
+                sR[(c0 + 1) * m8 + t.e8 + k] = a.y - b.y;
+            } else {
+                sR[c0 * m8 + k] = a.x;
+                sR[(c0 + 1) * m8 + k] = a.y;
+            }
+        }
+        __syncthreads();
+        // (c) column scales
+        {
+            const int w = tid >> 5, l = tid & 31;
+            for (int c = w; c < kTcVortCols; c += blockDim.x >> 5) {
+                unsigned long long mx = 0;
+                for (int k = l; k < nv; k += 32) {
+                    const int row = k < he ? k : t.e8 + (k - he);
+                    const unsigned long long ab =
+                        (unsigned long long)__double_as_longlong(sR[c * m8 + row]) & 0x7FFFFFFFFFFFFFFFULL;
+                    mx = ab > mx ? ab : mx;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
+                    mx = v > mx ? v : mx;
+                }
+                if (l == 0) sF[c] = tc_exponent(mx);
+            }
+        }
+        __syncthreads();
+        // (d) digits, one level of one column per thread (a warp: 8 levels of 4 columns)
+        for (int i = tid; i < kTcVortCols * m8; i += blockDim.x) {
+            const int kl = i & 7, cc = i >> 3;
+            const int c = cc % kTcVortCols, row = (cc / kTcVortCols) * 8 + kl;
+            const bool valid = row < he || (row >= t.e8 && row < t.e8 + ho);
+            int d[kTcSlices];
+            tc_digits(valid ? tc_fixed(sR[c * m8 + row], sF[c]) : 0, d);
+            __half* dst = sB + tc_core_off(c, row, t.k16);
+#pragma unroll
+            for (int s = 0; s < kTcSlices; ++s) dst[s * b_halves] = __int2half_rn(d[s]);
+        }
+        tc_fence_proxy();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        // (e) the digit-pair products
+        if (tid == 0) {
+            if (tile == tile0) *landed = tc_mbar_wait(&mbar[1], 0, 1 << 22) ? 1 : 0;
+            if (*landed) {
+                const uint32_t a0 = tc_smem_u32(sA), b0 = tc_smem_u32(sB);
+                const uint32_t sbo = (uint32_t)t.k16 * 16;
+                const int nks = t.k16 / 16;
+                for (int sa = 0; sa < kTcSlices; ++sa) {
+                    const uint32_t idesc = tc_idesc(kTcVortCols * (kTcSlices - sa));
+                    for (int ks = 0; ks < nks; ++ks) {
+                        const uint64_t da = tc_desc(a0 + (uint32_t)(sa * a_halves) * 2 + ks * 256, 128, sbo);
+                        const uint64_t db = tc_desc(b0 + ks * 256, 128, sbo);
+                        tc_mma(tmem + (uint32_t)(sa * kTcVortCols), da, db, idesc, (sa > 0 || ks > 0) ? 1u : 0u);
+                    }
+                }
+            }
+            tc_commit(&mbar[0]);
+        }
+        // (f) combination: warps w and w + 4k share TMEM lane quadrant w % 4;
+        // warp group w / 4 takes every ngrp-th block of 8 of the 32 columns
+        const bool done = __syncthreads_and(tc_mbar_wait(&mbar[0], par, 1 << 22)) && *landed;
+        tc_fence_after();
+        if (!done) {
+            if (tid == 0) atomicExch(err, 1);
+            break;
+        }
+        {
+            const int w = tid >> 5, quad = w & 3, grp = w >> 2, ngrp = (int)(blockDim.x >> 7);
+            if (32 * quad < m8) {
+                for (int cb = grp; cb < kTcVortCols / 8; cb += ngrp) {
+                    long long T[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) T[j] = 0;
+                    for (int c = 0; c < kTcClasses; ++c) {
+                        float v[8];
+                        tc_ld8(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(c * kTcVortCols + 8 * cb), v);
+                        const long long wgt = 1LL << (7 * (kTcClasses - 1 - c));
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) T[j] += (long long)tc_f2i(v[j]) * wgt;
+                    }
+                    const int row = 32 * quad + (tid & 31);
+                    if (row < m8) {
+                        const int e = sE[row];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const int col = 8 * cb + j;
+                            sR[col * m8 + row] = __ll2double_rn(T[j]) * tc_pow2(e + sF[col] - 52);
+                        }
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        // (g) the outputs at the level pair (k, nz-1-k)
+        for (int i = tid; i < kModes * he; i += blockDim.x) {
+            const int mi = i / he, k = i - mi * he;
+            const int m = m0 + mi;
+            if (m >= g.nm) continue;
+            Pair dz[Op::kFields];
+#pragma unroll
+            for (int f = 0; f < Op::kFields; ++f) {
+                const int c0 = 2 * (Op::kFields * mi + f);
+                const double2 ye = make_double2(sR[c0 * m8 + k], sR[(c0 + 1) * m8 + k]);
+                const double2 yo = k < ho ? make_double2(sR[c0 * m8 + t.e8 + k], sR[(c0 + 1) * m8 + t.e8 + k])
+                                          : make_double2(0.0, 0.0);
+                dz[f].a = make_double2(ye.x + yo.x, ye.y + yo.y);
+                dz[f].b = make_double2(ye.x - yo.x, ye.y - yo.y);
+            }
+            op.out(g, ops, m, k, k < ho ? 2 : 1, dz);
+        }
+        __syncthreads();  // sR and sB are reused by the next tile
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid < 32) tc_dealloc(tmem, 256);
+}
+
+// omega = (wy - vz, uz - wx, vx - uy) from D1.u, D1.v, as vorticity_body forms it
+struct VortTcOp {
+    static constexpr int kFields = 2;
+    const double2* __restrict__ U;
+    const double2* __restrict__ V;
+    const double2* __restrict__ W;
+    double2* __restrict__ OX;
+    double2* __restrict__ OY;
+    double2* __restrict__ OZ;
+    __device__ const double2* field(int f) const { return f ? V : U; }
+    __device__ void out(const GridDev& g, const Ops& ops, int m, int k, int npt, const Pair* dz) const {
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        for (int p = 0; p < npt; ++p) {
+            const int z = p ? g.nz - 1 - k : k;
+            const size_t o = (size_t)z * g.nm + m;
+            const double2 w = W[o], u = U[o], v = V[o];
+            const double2 wy = i_times(mi.ay, w), wx = i_times(mi.ax, w);
+            const double2 vx = i_times(mi.ax, v), uy = i_times(mi.ay, u);
+            OX[o] = c2sub(wy, p ? dz[1].b : dz[1].a);
+            OY[o] = c2sub(p ? dz[0].b : dz[0].a, wx);
+            OZ[o] = c2sub(vx, uy);
+        }
+    }
+};
+
+// pressure_correction_3d from D1.phi, as correction_body forms it
+struct CorrTcOp {
+    static constexpr int kFields = 1;
+    StepParams sp;
+    const double2* __restrict__ US;
+    const double2* __restrict__ VS;
+    const double2* __restrict__ WS;
+    const double2* __restrict__ PHI;
+    double2* __restrict__ U;
+    double2* __restrict__ V;
+    double2* __restrict__ W;
+    double2* __restrict__ P;
+    double2* __restrict__ GP;
+    __device__ const double2* field(int) const { return PHI; }
+    __device__ void out(const GridDev& g, const Ops& ops, int m, int k, int npt, const Pair* dzp) const {
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const double dt = sp.dt;
+        for (int p = 0; p < npt; ++p) {
+            const int z = p ? g.nz - 1 - k : k;
+            const double2 d = p ? dzp[0].b : dzp[0].a;
+            const size_t o = (size_t)z * g.nm + m;
+            const double2 ph = PHI[o];
+            const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
+            const double2 us = US[o], vs = VS[o], ws = WS[o];
+            U[o] = make_double2(us.x - dt * px.x, us.y - dt * px.y);
+            V[o] = make_double2(vs.x - dt * py.x, vs.y - dt * py.y);
+            W[o] = make_double2(ws.x - dt * d.x, ws.y - dt * d.y);
+            double2 pp = P[o];
+            pp.x += ph.x;
+            pp.y += ph.y;
+            P[o] = pp;
+            if (z == 0 || z == g.nz - 1) {
+                const int wall = (z == 0) ? 0 : 1;
+                GP[(size_t)wall * g.nm + m] = i_times(mi.ax, pp);
+                GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, pp);
+            }
+        }
+    }
+};
+
+template <class Op>
+__global__ void __launch_bounds__(kTcVortThreads) k_dz_tc(GridDev g, Ops ops, Op op, int chunk, int* err) {
+    constexpr int kModes = kTcVortCols / (2 * Op::kFields);
+    const int ntiles = (g.nm + kModes - 1) / kModes;
+    const int t0 = blockIdx.x * chunk;
+    dz_tc_body(g, ops, op, t0, min(t0 + chunk, ntiles), err);
+}
+
 template <typename SrcC>
 __global__ void __launch_bounds__(256) k_viscous(GridDev g, Ops ops, StepParams sp, Fields F,
                                                  FieldsT<SrcC> Src, const double2* __restrict__ GP,
@@ -2043,6 +2311,8 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
     if ((e = set_smem(k_correction, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
     if ((e = set_smem(k_divergence, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
     if ((e = set_smem(k_viscous_tc, 0))) return e;
+    if ((e = set_smem(k_dz_tc<VortTcOp>, 0))) return e;
+    if ((e = set_smem(k_dz_tc<CorrTcOp>, 0))) return e;
     if ((e = set_smem(k_pcg_poisson, pcg_smem(g)))) return e;
     if ((e = set_smem(k_pcg_helmholtz, pcg_smem(g)))) return e;
     return cudaSuccess;
@@ -2101,6 +2371,49 @@ cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams
     const int nb = (ops.nq + qpb - 1) / qpb;
     k_viscous_tc<<<nb, 256, viscous_tc_smem(g), s>>>(g, ops, sp, F, Src, GP, pi, Out, qpb, err);
     return cudaGetLastError();
+}
+
+size_t vorticity_tc_smem(const GridDev& g) {
+    const TcGeom t = tc_geom(g.nz);
+    return (size_t)kTcSlices * (t.m8 + kTcVortCols) * t.k16 * sizeof(__half) +
+           (size_t)kTcVortCols * t.m8 * sizeof(double) + (size_t)(t.m8 + kTcVortCols) * sizeof(int) +
+           2 * sizeof(uint64_t) + 16;
+}
+
+bool vorticity_tc_fits(const GridDev& g) {
+    return tc_supported(g.nz) && vorticity_tc_smem(g) <= smem_limit(k_dz_tc<VortTcOp>) &&
+           vorticity_tc_smem(g) <= smem_limit(k_dz_tc<CorrTcOp>);
+}
+
+// Tiles (of `modes` modes) per CTA: at least 4 (the D1 image is copied once
+// per CTA), else one CTA per SM.  The chunking does not change a tile's
+// arithmetic.
+int tc_dz_chunk(int nm, int modes) {
+    const int ntiles = (nm + modes - 1) / modes;
+    return std::max(4, (ntiles + 151) / 152);
+}
+
+template <class Op>
+cudaError_t launch_dz_tc(const GridDev& g, const Ops& ops, const Op& op, int* err, cudaStream_t s) {
+    if (!ops.tcD || !ops.tcDE || !vorticity_tc_fits(g)) return cudaErrorInvalidValue;
+    constexpr int kModes = kTcVortCols / (2 * Op::kFields);
+    const int ntiles = (g.nm + kModes - 1) / kModes;
+    const int chunk = tc_dz_chunk(g.nm, kModes);
+    k_dz_tc<Op><<<(ntiles + chunk - 1) / chunk, kTcVortThreads, vorticity_tc_smem(g), s>>>(g, ops, op, chunk, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vorticity_tc(const GridDev& g, const Ops& ops, const double2* U, const double2* V,
+                                const double2* W, double2* OX, double2* OY, double2* OZ, int* err, cudaStream_t s) {
+    const VortTcOp op{U, V, W, OX, OY, OZ};
+    return launch_dz_tc(g, ops, op, err, s);
+}
+
+cudaError_t launch_correction_tc(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                                 const double2* VS, const double2* WS, const double2* PHI, double2* U, double2* V,
+                                 double2* W, double2* P, double2* GP, int* err, cudaStream_t s) {
+    const CorrTcOp op{sp, US, VS, WS, PHI, U, V, W, P, GP};
+    return launch_dz_tc(g, ops, op, err, s);
 }
 
 cudaError_t launch_vorticity_mixed(const GridDev& g, const MixedOps& mx, const Ops& ops, const double2* U,
@@ -2289,6 +2602,13 @@ struct RsVort64 {
             pi_update_body(d.g, d.ops.zw, d.pp, d.U, d.pi, 0);
             return;
         }
+        if (d.tcmask & 1) {
+            const int ntiles = (d.g.nm + 7) / 8, chunk = d.vort_chunk;  // 8 modes per tile
+            const int t0 = (b - 1) * chunk;
+            const VortTcOp op{d.U, d.V, d.W, d.US, d.VS, d.WS};
+            dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
+            return;
+        }
         vorticity_body(d.g, d.ops, d.U, d.V, d.W, d.US, d.VS, d.WS, d.g.tc[kTileVort], b - 1);
     }
 };
@@ -2370,8 +2690,15 @@ struct RsPresMean {
 };
 
 struct RsCorr64 {
-    static constexpr int kMinCtas = 4;
+    static constexpr int kMinCtas = 2;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        if (d.tcmask & 2) {
+            const int ntiles = (d.g.nm + 15) / 16, chunk = d.corr_chunk;  // 16 modes per tile
+            const int t0 = b * chunk;
+            const CorrTcOp op{d.sp, d.US, d.VS, d.WS, d.PHI, d.U, d.V, d.W, d.P, d.GP};
+            dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
+            return;
+        }
         correction_body(d.g, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.U, d.V, d.W, d.P, d.GP, d.g.tc[kTileCorr], b);
     }
 };
@@ -2422,6 +2749,8 @@ void ragged_geometry(RunDesc& d) {
     d.gx[kRsCorr] = cdiv((long long)g.nz * g.nm, 4 * kStageThreads);
     d.gx[kRsBc] = cdiv(2LL * g.nm, kStageThreads);
     d.gx[kRsVisc] = tc_q_per_cta(d.ops.nq);  // operator indices per CTA of the tensor-core viscous body
+    d.vort_chunk = tc_dz_chunk(g.nm, 8);       // tiles per CTA of the tensor-core z-derivative bodies
+    d.corr_chunk = tc_dz_chunk(g.nm, 16);
 }
 
 int ragged_tile_kernel(int stage, bool mixed) {
@@ -2439,7 +2768,9 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
     const int k = ragged_tile_kernel(stage, mixed);
     const int tiles = k >= 0 ? (g.nm + g.tc[k] - 1) / g.tc[k] : 0;
     switch (stage) {
-        case kRsVort: return 1 + tiles;
+        case kRsVort:
+            if (!mixed && (d.tcmask & 1)) return 1 + ((g.nm + 7) / 8 + d.vort_chunk - 1) / d.vort_chunk;
+            return 1 + tiles;
         case kRsFftYInv:
         case kRsFftC2R: return 6 * d.gx[stage];
         case kRsFftR2C:
@@ -2450,7 +2781,9 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
             if (!mixed && d.ops.tcA && d.sp.cn_identity) return (d.ops.nq + d.gx[kRsVisc] - 1) / d.gx[kRsVisc];
             return tiles;
         case kRsPres: return tiles;
-        case kRsCorr: return mixed ? d.gx[stage] : tiles;
+        case kRsCorr:
+            if (!mixed && (d.tcmask & 2)) return ((g.nm + 15) / 16 + d.corr_chunk - 1) / d.corr_chunk;
+            return mixed ? d.gx[stage] : tiles;
         case kRsViscMean:
         case kRsPresMean: return mixed ? 1 : 0;
     }
@@ -2463,12 +2796,16 @@ size_t ragged_smem(int stage, bool mixed, const RunDesc& d) {
     const int k = ragged_tile_kernel(stage, mixed);
     const int tc = k >= 0 ? g.tc[k] : 0;
     switch (stage) {
-        case kRsVort: return 2 * nz * tc * (mixed ? sizeof(float2) : sizeof(double2));
+        case kRsVort:
+            if (!mixed && (d.tcmask & 1)) return vorticity_tc_smem(g);
+            return 2 * nz * tc * (mixed ? sizeof(float2) : sizeof(double2));
         case kRsVisc:
             if (!mixed && d.ops.tcA && d.sp.cn_identity) return viscous_tc_smem(g);
             return mixed ? viscous_mixed_smem(g, tc) : 6 * nz * tc * sizeof(double2);
         case kRsPres: return mixed ? pressure_mixed_smem(g, tc) : (2 * nz * tc + nz) * sizeof(double2);
-        case kRsCorr: return mixed ? 0 : nz * tc * sizeof(double2);
+        case kRsCorr:
+            if (!mixed && (d.tcmask & 2)) return vorticity_tc_smem(g);
+            return mixed ? 0 : nz * tc * sizeof(double2);
         case kRsViscMean: return mixed ? 6 * nz * sizeof(double2) : 0;
         case kRsPresMean: return mixed ? 3 * nz * sizeof(double2) : 0;
     }
