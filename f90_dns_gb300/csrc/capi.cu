@@ -1777,12 +1777,19 @@ int dns3d_lgl_nodes_weights(int nz, double* z, double* w) {
 }  // extern "C"
 
 // ------------------------------------------------------------------ batches
-// Joint stepping of independent runs.  Eligible runs of one precision form a
-// group whose step is ten ragged stage launches (ragged.cuh); the others keep
-// their own step bodies, captured beside the groups into the same graph.
+// Joint stepping of independent runs.  Eligible runs of one precision and one
+// kernel variant (which stages run their tensor-core bodies) form a group
+// whose step is ten ragged stage launches (ragged.cuh): a group's launch sizes
+// its shared memory for its largest run, so runs of different variants are not
+// mixed.  The others keep their own step bodies; every group and loose run is
+// a branch of the same graph.
 struct dns3d_batch {
     struct Group {
+        int key = 0;                  // precision and variant
         bool mixed = false;
+        int variant = 0;              // RaggedVariant bits (FP64 groups)
+        cudaStream_t lane = nullptr, side = nullptr;  // side: the mixed form's mode (0,0) stages
+        cudaEvent_t lane_join = nullptr, side_fork = nullptr, side_join = nullptr;
         std::vector<int> idx;         // runs of the group (indices into runs)
         std::vector<RunDesc> desc;    // host copies of the descriptors
         std::vector<int> own_tc;      // per run, the tile widths of its own launches [kTileKernels]
@@ -1794,13 +1801,9 @@ struct dns3d_batch {
     std::vector<dns3d_handle*> runs;  // not owned
     int device = 0;
     cudaStream_t stream = nullptr;    // the batch's graph runs here
-    cudaStream_t lane[2] = {nullptr, nullptr};
-    cudaStream_t side[2] = {nullptr, nullptr};  // the mixed group's mode (0,0) stages
     cudaEvent_t fork = nullptr, done = nullptr;
-    cudaEvent_t lane_join[2] = {nullptr, nullptr};
-    cudaEvent_t side_fork[2] = {nullptr, nullptr}, side_join[2] = {nullptr, nullptr};
     std::vector<cudaEvent_t> run_in, run_join;
-    Group grp[2];                     // FP64, mixed
+    std::vector<Group> grp;
     std::vector<int> loose;           // runs stepped by their own launches
     cudaGraphExec_t graph = nullptr;
     int launches = 0;                 // kernel launches per step
@@ -1822,9 +1825,9 @@ size_t stage_smem_limit(StageKernel k) {
 // Raises every stage kernel's dynamic shared-memory limit to the device's
 // opt-in maximum (a property of the kernel, shared by all batches).
 cudaError_t prepare_stage_kernels() {
-    for (int m = 0; m < 2; ++m)
+    for (int m = 0; m < 2 * 8; ++m)
         for (int s = 0; s < kRsStages; ++s) {
-            StageKernel k = ragged_kernel(s, m == 1);
+            StageKernel k = ragged_kernel(s, m & 1, m >> 1);
             const size_t lim = stage_smem_limit(k);
             if (!lim) return cudaErrorInvalidValue;
             cudaError_t e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim);
@@ -1941,7 +1944,7 @@ cudaError_t group_launch(dns3d_batch::Group& G, int s, cudaStream_t st) {
     map.nruns = n;
     RunDesc* runs = G.d_desc;
     void* args[] = {&runs, &map};
-    return cudaLaunchKernel((const void*)ragged_kernel(s, G.mixed), dim3((unsigned)G.total[s]),
+    return cudaLaunchKernel((const void*)ragged_kernel(s, G.mixed, G.variant), dim3((unsigned)G.total[s]),
                             dim3(kStageThreads), args, G.smem[s], st);
 }
 
@@ -1958,7 +1961,7 @@ int group_tune(dns3d_batch* b, dns3d_batch::Group& G) {
     int rc = DNS3D_OK;
     for (int s : {(int)kRsVort, (int)kRsVisc, (int)kRsPres}) {
         const int k = ragged_tile_kernel(s, G.mixed);
-        const size_t lim = stage_smem_limit(ragged_kernel(s, G.mixed));
+        const size_t lim = stage_smem_limit(ragged_kernel(s, G.mixed, G.variant));
         int best = -1;
         float best_ms = 0.f;
         for (int cand : {0, 4, 8, 16, 32}) {
@@ -2001,29 +2004,23 @@ void batch_release(dns3d_batch* b) {
     for (auto& G : b->grp) {
         cudaFree(G.d_desc);
         cudaFree(G.d_map);
+        for (auto ev : {G.lane_join, G.side_fork, G.side_join})
+            if (ev) cudaEventDestroy(ev);
+        for (auto st : {G.lane, G.side})
+            if (st) cudaStreamDestroy(st);
     }
     for (auto ev : b->run_in) cudaEventDestroy(ev);
     for (auto ev : b->run_join) cudaEventDestroy(ev);
-    for (auto ev : b->lane_join)
-        if (ev) cudaEventDestroy(ev);
-    for (int i = 0; i < 2; ++i) {
-        if (b->side_fork[i]) cudaEventDestroy(b->side_fork[i]);
-        if (b->side_join[i]) cudaEventDestroy(b->side_join[i]);
-        if (b->side[i]) cudaStreamDestroy(b->side[i]);
-    }
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->done) cudaEventDestroy(b->done);
-    for (auto st : b->lane)
-        if (st) cudaStreamDestroy(st);
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
 // One group's step on its lane: the nonlinear-term stages, then viscous and
 // pressure tiles with (mixed form) the mode (0,0) chain forked beside them,
 // then projection and walls.
-cudaError_t group_capture(dns3d_batch* b, int gi, int* launches) {
-    dns3d_batch::Group& G = b->grp[gi];
-    cudaStream_t lane = b->lane[gi], side = b->side[gi];
+cudaError_t group_capture(dns3d_batch::Group& G, int* launches) {
+    cudaStream_t lane = G.lane, side = G.side;
     cudaError_t ce = cudaSuccess;
     auto stage = [&](int s, cudaStream_t st) {
         if (!ce && G.total[s] > 0) {
@@ -2034,15 +2031,15 @@ cudaError_t group_capture(dns3d_batch* b, int gi, int* launches) {
     for (int s : {(int)kRsVort, (int)kRsFftYInv, (int)kRsFftC2R, (int)kRsProd, (int)kRsFftR2C, (int)kRsFftYFwd})
         stage(s, lane);
     if (G.mixed) {
-        if (!ce) ce = cudaEventRecord(b->side_fork[gi], lane);
-        if (!ce) ce = cudaStreamWaitEvent(side, b->side_fork[gi], 0);
+        if (!ce) ce = cudaEventRecord(G.side_fork, lane);
+        if (!ce) ce = cudaStreamWaitEvent(side, G.side_fork, 0);
         stage(kRsViscMean, side);
         stage(kRsPresMean, side);
-        if (!ce) ce = cudaEventRecord(b->side_join[gi], side);
+        if (!ce) ce = cudaEventRecord(G.side_join, side);
     }
     stage(kRsVisc, lane);
     stage(kRsPres, lane);
-    if (G.mixed && !ce) ce = cudaStreamWaitEvent(lane, b->side_join[gi], 0);
+    if (G.mixed && !ce) ce = cudaStreamWaitEvent(lane, G.side_join, 0);
     stage(kRsCorr, lane);
     stage(kRsBc, lane);
     return ce;
@@ -2056,13 +2053,12 @@ int batch_capture(dns3d_batch* b) {
     int rc = DNS3D_OK;
     int launches = 0;
     cudaError_t ce = cudaEventRecord(b->fork, b->stream);
-    for (int gi = 0; gi < 2 && !ce; ++gi) {
+    for (size_t gi = 0; gi < b->grp.size() && !ce; ++gi) {
         dns3d_batch::Group& G = b->grp[gi];
-        if (G.idx.empty()) continue;
-        ce = cudaStreamWaitEvent(b->lane[gi], b->fork, 0);
-        if (!ce) ce = group_capture(b, gi, &launches);
-        if (!ce) ce = cudaEventRecord(b->lane_join[gi], b->lane[gi]);
-        if (!ce) ce = cudaStreamWaitEvent(b->stream, b->lane_join[gi], 0);
+        ce = cudaStreamWaitEvent(G.lane, b->fork, 0);
+        if (!ce) ce = group_capture(G, &launches);
+        if (!ce) ce = cudaEventRecord(G.lane_join, G.lane);
+        if (!ce) ce = cudaStreamWaitEvent(b->stream, G.lane_join, 0);
     }
     for (size_t j = 0; j < b->loose.size() && !ce && !rc; ++j) {
         const int i = b->loose[j];
@@ -2128,27 +2124,35 @@ int batch_create(dns3d_handle* const* runs, int nruns, int flags, dns3d_batch** 
         if (ok) {
             d = make_desc(h);
             for (int s = 0; s < kRsStages && ok; ++s)
-                ok = ragged_smem(s, h->mixed, d) <= stage_smem_limit(ragged_kernel(s, h->mixed));
+                ok = ragged_smem(s, h->mixed, d) <=
+                     stage_smem_limit(ragged_kernel(s, h->mixed, h->mixed ? 0 : ragged_variant(d)));
         }
         if (!ok) {
             b->loose.push_back(i);
             continue;
         }
-        dns3d_batch::Group& G = b->grp[h->mixed ? 1 : 0];
+        const int variant = h->mixed ? 0 : ragged_variant(d);
+        const int key = h->mixed ? 1 << 8 : variant;
+        size_t gi = 0;
+        while (gi < b->grp.size() && b->grp[gi].key != key) ++gi;
+        if (gi == b->grp.size()) {
+            b->grp.emplace_back();
+            b->grp.back().key = key;
+        }
+        dns3d_batch::Group& G = b->grp[gi];
         G.mixed = h->mixed;
+        G.variant = variant;
         G.idx.push_back(i);
         G.desc.push_back(d);
         for (int k = 0; k < kTileKernels; ++k) G.own_tc.push_back(d.g.tc[k]);
     }
-    for (int gi = 0; gi < 2; ++gi) {
-        dns3d_batch::Group& G = b->grp[gi];
-        if (G.idx.empty()) continue;
+    for (auto& G : b->grp) {
         const int n = (int)G.idx.size();
-        if (cudaStreamCreateWithFlags(&b->lane[gi], cudaStreamNonBlocking) ||
-            cudaStreamCreateWithFlags(&b->side[gi], cudaStreamNonBlocking) ||
-            cudaEventCreateWithFlags(&b->lane_join[gi], cudaEventDisableTiming) ||
-            cudaEventCreateWithFlags(&b->side_fork[gi], cudaEventDisableTiming) ||
-            cudaEventCreateWithFlags(&b->side_join[gi], cudaEventDisableTiming))
+        if (cudaStreamCreateWithFlags(&G.lane, cudaStreamNonBlocking) ||
+            cudaStreamCreateWithFlags(&G.side, cudaStreamNonBlocking) ||
+            cudaEventCreateWithFlags(&G.lane_join, cudaEventDisableTiming) ||
+            cudaEventCreateWithFlags(&G.side_fork, cudaEventDisableTiming) ||
+            cudaEventCreateWithFlags(&G.side_join, cudaEventDisableTiming))
             return fail(DNS3D_E_CUDA);
         if (cudaMalloc(&G.d_desc, (size_t)n * sizeof(RunDesc)) ||
             cudaMalloc(&G.d_map, (size_t)kRsStages * (2 * n + 1) * sizeof(int)))
@@ -2256,7 +2260,11 @@ int dns3d_batch_synchronize(dns3d_batch* b) {
 int dns3d_batch_info(dns3d_batch* b, int* launches_per_step, int* ragged_runs) {
     if (!b) return DNS3D_E_INVALID;
     if (launches_per_step) *launches_per_step = b->launches;
-    if (ragged_runs) *ragged_runs = (int)(b->grp[0].idx.size() + b->grp[1].idx.size());
+    if (ragged_runs) {
+        int n = 0;
+        for (auto& G : b->grp) n += (int)G.idx.size();
+        *ragged_runs = n;
+    }
     return DNS3D_OK;
 }
 

@@ -110,9 +110,12 @@ static_assert(sizeof(RunDesc) % 8 == 0, "descriptor copied in 8-byte words");
 // ---------------------------------------------------------------- host side
 using StageKernel = void (*)(const RunDesc*, StageMap);
 
-// The k_stage instantiation of a stage for FP64 (mixed = false) or mixed runs
-// (step.cu; the transform passes come from fft_ct.cu).
-StageKernel ragged_kernel(int stage, bool mixed);
+// Kernel variants of FP64 runs: which stages run their tensor-core bodies.
+enum RaggedVariant { kRvVortTc = 1, kRvCorrTc = 2, kRvViscTc = 4 };
+int ragged_variant(const RunDesc& d);
+// The k_stage instantiation of a stage for FP64 (mixed = false, with the
+// variant) or mixed runs (step.cu; the transform passes come from fft_ct.cu).
+StageKernel ragged_kernel(int stage, bool mixed, int variant);
 StageKernel ragged_fft_kernel(int stage, bool mixed);
 // CTA columns (y pass) or rows (x passes) of the compile-time transform of length n.
 int fft_ct_per_cta(int n);

@@ -2602,14 +2602,22 @@ struct RsVort64 {
             pi_update_body(d.g, d.ops.zw, d.pp, d.U, d.pi, 0);
             return;
         }
-        if (d.tcmask & 1) {
-            const int ntiles = (d.g.nm + 7) / 8, chunk = d.vort_chunk;  // 8 modes per tile
-            const int t0 = (b - 1) * chunk;
-            const VortTcOp op{d.U, d.V, d.W, d.US, d.VS, d.WS};
-            dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
+        vorticity_body(d.g, d.ops, d.U, d.V, d.W, d.US, d.VS, d.WS, d.g.tc[kTileVort], b - 1);
+    }
+};
+
+// the same with D1.u, D1.v on the tensor cores (runs with RunDesc::tcmask bit 1)
+struct RsVort64Tc {
+    static constexpr int kMinCtas = 1;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        if (b == 0) {
+            pi_update_body(d.g, d.ops.zw, d.pp, d.U, d.pi, 0);
             return;
         }
-        vorticity_body(d.g, d.ops, d.U, d.V, d.W, d.US, d.VS, d.WS, d.g.tc[kTileVort], b - 1);
+        const int ntiles = (d.g.nm + 7) / 8, chunk = d.vort_chunk;  // 8 modes per tile
+        const int t0 = (b - 1) * chunk;
+        const VortTcOp op{d.U, d.V, d.W, d.US, d.VS, d.WS};
+        dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
     }
 };
 
@@ -2638,15 +2646,19 @@ struct RsProd {
 };
 
 struct RsVisc64 {
-    static constexpr int kMinCtas = 2;
+    static constexpr int kMinCtas = 3;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
-        if (d.ops.tcA && d.sp.cn_identity) {
-            viscous_tc_body(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
-                            fields3(d.US, d.VS, d.WS), d.gx[kRsVisc], b, d.tcerr);
-            return;
-        }
         viscous_body<double2>(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
                               fields3(d.US, d.VS, d.WS), d.g.tc[kTileVisc], b);
+    }
+};
+
+// the Crank-Nicolson solve on the tensor cores (runs with ops.tcA set)
+struct RsVisc64Tc {
+    static constexpr int kMinCtas = 2;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        viscous_tc_body(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
+                        fields3(d.US, d.VS, d.WS), d.gx[kRsVisc], b, d.tcerr);
     }
 };
 
@@ -2690,16 +2702,20 @@ struct RsPresMean {
 };
 
 struct RsCorr64 {
-    static constexpr int kMinCtas = 2;
+    static constexpr int kMinCtas = 4;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
-        if (d.tcmask & 2) {
-            const int ntiles = (d.g.nm + 15) / 16, chunk = d.corr_chunk;  // 16 modes per tile
-            const int t0 = b * chunk;
-            const CorrTcOp op{d.sp, d.US, d.VS, d.WS, d.PHI, d.U, d.V, d.W, d.P, d.GP};
-            dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
-            return;
-        }
         correction_body(d.g, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.U, d.V, d.W, d.P, d.GP, d.g.tc[kTileCorr], b);
+    }
+};
+
+// the projection with D1.phi on the tensor cores (runs with RunDesc::tcmask bit 2)
+struct RsCorr64Tc {
+    static constexpr int kMinCtas = 1;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        const int ntiles = (d.g.nm + 15) / 16, chunk = d.corr_chunk;  // 16 modes per tile
+        const int t0 = b * chunk;
+        const CorrTcOp op{d.sp, d.US, d.VS, d.WS, d.PHI, d.U, d.V, d.W, d.P, d.GP};
+        dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
     }
 };
 
@@ -2718,13 +2734,16 @@ struct RsBc {
 
 }  // namespace
 
-StageKernel ragged_kernel(int stage, bool mixed) {
+StageKernel ragged_kernel(int stage, bool mixed, int variant) {
     switch (stage) {
-        case kRsVort: return mixed ? k_stage<RsVort32> : k_stage<RsVort64>;
+        case kRsVort:
+            return mixed ? k_stage<RsVort32> : ((variant & kRvVortTc) ? k_stage<RsVort64Tc> : k_stage<RsVort64>);
         case kRsProd: return mixed ? k_stage<RsProd<float>> : k_stage<RsProd<double>>;
-        case kRsVisc: return mixed ? k_stage<RsVisc32> : k_stage<RsVisc64>;
+        case kRsVisc:
+            return mixed ? k_stage<RsVisc32> : ((variant & kRvViscTc) ? k_stage<RsVisc64Tc> : k_stage<RsVisc64>);
         case kRsPres: return mixed ? k_stage<RsPres32> : k_stage<RsPres64>;
-        case kRsCorr: return mixed ? k_stage<RsCorr32> : k_stage<RsCorr64>;
+        case kRsCorr:
+            return mixed ? k_stage<RsCorr32> : ((variant & kRvCorrTc) ? k_stage<RsCorr64Tc> : k_stage<RsCorr64>);
         case kRsBc: return k_stage<RsBc>;
         case kRsViscMean: return k_stage<RsViscMean>;
         case kRsPresMean: return k_stage<RsPresMean>;
@@ -2734,6 +2753,11 @@ StageKernel ragged_kernel(int stage, bool mixed) {
         case kRsFftYFwd: return ragged_fft_kernel(stage, mixed);
     }
     return nullptr;
+}
+
+int ragged_variant(const RunDesc& d) {
+    return ((d.tcmask & 1) ? kRvVortTc : 0) | ((d.tcmask & 2) ? kRvCorrTc : 0) |
+           ((d.ops.tcA && d.sp.cn_identity) ? kRvViscTc : 0);
 }
 
 void ragged_geometry(RunDesc& d) {
@@ -2769,7 +2793,7 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
     const int tiles = k >= 0 ? (g.nm + g.tc[k] - 1) / g.tc[k] : 0;
     switch (stage) {
         case kRsVort:
-            if (!mixed && (d.tcmask & 1)) return 1 + ((g.nm + 7) / 8 + d.vort_chunk - 1) / d.vort_chunk;
+            if (!mixed && (ragged_variant(d) & kRvVortTc)) return 1 + ((g.nm + 7) / 8 + d.vort_chunk - 1) / d.vort_chunk;
             return 1 + tiles;
         case kRsFftYInv:
         case kRsFftC2R: return 6 * d.gx[stage];
@@ -2778,11 +2802,11 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
         case kRsProd:
         case kRsBc: return d.gx[stage];
         case kRsVisc:
-            if (!mixed && d.ops.tcA && d.sp.cn_identity) return (d.ops.nq + d.gx[kRsVisc] - 1) / d.gx[kRsVisc];
+            if (!mixed && (ragged_variant(d) & kRvViscTc)) return (d.ops.nq + d.gx[kRsVisc] - 1) / d.gx[kRsVisc];
             return tiles;
         case kRsPres: return tiles;
         case kRsCorr:
-            if (!mixed && (d.tcmask & 2)) return ((g.nm + 15) / 16 + d.corr_chunk - 1) / d.corr_chunk;
+            if (!mixed && (ragged_variant(d) & kRvCorrTc)) return ((g.nm + 15) / 16 + d.corr_chunk - 1) / d.corr_chunk;
             return mixed ? d.gx[stage] : tiles;
         case kRsViscMean:
         case kRsPresMean: return mixed ? 1 : 0;
@@ -2797,14 +2821,14 @@ size_t ragged_smem(int stage, bool mixed, const RunDesc& d) {
     const int tc = k >= 0 ? g.tc[k] : 0;
     switch (stage) {
         case kRsVort:
-            if (!mixed && (d.tcmask & 1)) return vorticity_tc_smem(g);
+            if (!mixed && (ragged_variant(d) & kRvVortTc)) return vorticity_tc_smem(g);
             return 2 * nz * tc * (mixed ? sizeof(float2) : sizeof(double2));
         case kRsVisc:
-            if (!mixed && d.ops.tcA && d.sp.cn_identity) return viscous_tc_smem(g);
+            if (!mixed && (ragged_variant(d) & kRvViscTc)) return viscous_tc_smem(g);
             return mixed ? viscous_mixed_smem(g, tc) : 6 * nz * tc * sizeof(double2);
         case kRsPres: return mixed ? pressure_mixed_smem(g, tc) : (2 * nz * tc + nz) * sizeof(double2);
         case kRsCorr:
-            if (!mixed && (d.tcmask & 2)) return vorticity_tc_smem(g);
+            if (!mixed && (ragged_variant(d) & kRvCorrTc)) return vorticity_tc_smem(g);
             return mixed ? 0 : nz * tc * sizeof(double2);
         case kRsViscMean: return mixed ? 6 * nz * sizeof(double2) : 0;
         case kRsPresMean: return mixed ? 3 * nz * sizeof(double2) : 0;

@@ -226,7 +226,8 @@ int dns3d_flow_stats_noalloc(const double* u, const double* v, const double* w, 
  * ragged launches: each of the ten stages of a step (vorticity with the PI
  * update, four plane-transform passes, the products, viscous, pressure,
  * projection, walls) is ONE kernel launch over the mode tiles / transform
- * columns of all such runs of one precision, whatever their nx, ny, nz, with
+ * columns of all such runs of one precision and kernel variant (which stages
+ * run their tensor-core forms), whatever their nx, ny, nz, with
  * every run's arithmetic that of its own launches (bitwise the same results);
  * the mixed form adds one launch each for the FP64 mode (0,0) viscous and
  * pressure solves, beside the tiles.  Other runs are stepped by their own
