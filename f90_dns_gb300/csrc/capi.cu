@@ -1160,6 +1160,8 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     // the direct solver (DNS3D_TENSOR_CORES=0 keeps the FP64-pipe kernel)
     if ((rc = dev_alloc(h, &h->d_tcerr, 2))) return fail(rc);
     const char* tcenv = std::getenv("DNS3D_TENSOR_CORES");
+    const char* stall = std::getenv("DNS3D_TC_TEST_STALL");
+    ops.tc_stall = stall && std::strcmp(stall, "1") == 0;
     if (!h->mixed && sp.cn_identity && c.linear_solver == 0 && !(tcenv && std::strcmp(tcenv, "0") == 0) &&
         viscous_tc_fits(g)) {
         const TcGeom t = tc_geom(nz);

@@ -165,6 +165,10 @@ struct Ops {
     // tensor-core digit image of the folded D1 ([[0, De], [Do, 0]]), or null
     const __half* tcD;
     const int* tcDE;
+    // failure-detection test: the tensor-core kernels withhold their MMA
+    // commit and poll their completion barrier only 2^10 times, so the bounded
+    // wait runs out and reports its status (0 in normal runs)
+    int tc_stall;
 };
 
 // Mixed-precision operators (FP32): folded D for the nonlinear term and the

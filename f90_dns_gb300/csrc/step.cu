@@ -670,7 +670,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
         // (e) the digit-pair products, one thread issues
         if (threadIdx.x == 0) {
             *landed = tc_mbar_wait(&mbar[1], par, 1 << 22) ? 1 : 0;
-            if (*landed) {
+            if (*landed && !ops.tc_stall) {
                 const uint32_t a0 = tc_smem_u32(sA), b0 = tc_smem_u32(sB);
                 const uint32_t sbo = (uint32_t)t.k16 * 16;
                 const int nks = t.k16 / 16;
@@ -683,10 +683,11 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                     }
                 }
             }
-            tc_commit(&mbar[0]);  // also when nothing was issued: the waiters are released
+            if (!ops.tc_stall) tc_commit(&mbar[0]);  // also when nothing was issued: the waiters are released
         }
         // (f) combine the accumulators of each row
-        const bool done = __syncthreads_and(tc_mbar_wait(&mbar[0], par, 1 << 22)) && *landed;
+        const bool done =
+            __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && *landed;
         tc_fence_after();
         if (!done) {
             if (threadIdx.x == 0) atomicExch(err, 1);
@@ -886,7 +887,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         // (e) the digit-pair products
         if (tid == 0) {
             if (tile == tile0) *landed = tc_mbar_wait(&mbar[1], 0, 1 << 22) ? 1 : 0;
-            if (*landed) {
+            if (*landed && !ops.tc_stall) {
                 const uint32_t a0 = tc_smem_u32(sA), b0 = tc_smem_u32(sB);
                 const uint32_t sbo = (uint32_t)t.k16 * 16;
                 const int nks = t.k16 / 16;
@@ -899,11 +900,12 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
                     }
                 }
             }
-            tc_commit(&mbar[0]);
+            if (!ops.tc_stall) tc_commit(&mbar[0]);
         }
         // (f) combination: warps w and w + 4k share TMEM lane quadrant w % 4;
         // warp group w / 4 takes every ngrp-th block of 8 of the 32 columns
-        const bool done = __syncthreads_and(tc_mbar_wait(&mbar[0], par, 1 << 22)) && *landed;
+        const bool done =
+            __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && *landed;
         tc_fence_after();
         if (!done) {
             if (tid == 0) atomicExch(err, 1);

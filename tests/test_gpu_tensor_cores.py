@@ -79,3 +79,24 @@ def test_tensor_core_runs_in_batches_bitwise(built_lib, monkeypatch):
             solo = d.get_state(walls=False)
         for k in ("u", "v", "w", "p_total"):
             assert np.array_equal(st[k], solo[k]), (cfg.nx, cfg.ny, cfg.nz, k)
+
+
+def test_tensor_core_wait_runs_out_and_reports(built_lib, monkeypatch):
+    """Failure detection without a GPU fault: with the MMA commit withheld
+    (DNS3D_TC_TEST_STALL=1) every tensor-core kernel's bounded completion wait
+    runs out; the kernels write nothing, free their TMEM and return, and
+    diagnostics report DNS3D_E_TIMEOUT.  The context stays usable."""
+    from f90_dns_gb300 import Dns3DError
+    from f90_dns_gb300.capi import DNS3D_E_TIMEOUT
+    wl = dict(C1, nx=16, ny=16)
+    monkeypatch.setenv("DNS3D_TENSOR_CORES", "1")
+    monkeypatch.setenv("DNS3D_TC_TEST_STALL", "1")
+    with ChannelDNS(config_from(wl)) as d:
+        d.step(1)
+        with pytest.raises(Dns3DError) as ei:
+            d.diagnostics()
+        assert ei.value.code == DNS3D_E_TIMEOUT
+    monkeypatch.delenv("DNS3D_TC_TEST_STALL")
+    with ChannelDNS(config_from(wl)) as d:
+        d.step(2)
+        assert np.isfinite(d.diagnostics().energy)
