@@ -1,0 +1,40 @@
+// FP64 <-> FP32 conversions with integer operations.
+//
+// On this GPU the hardware conversions (F2F) issue on the FP64 pipe, which
+// runs at 1/64 of the FP32 rate and is what the mixed-precision kernels are
+// bound by; these run on the integer pipes instead.  d2f rounds to nearest
+// even exactly as the hardware does for results in the normal float range;
+// results below it flush to signed zero (the spectra here never come within
+// many decades of 1e-38), overflow gives infinity, NaN stays NaN.  f2d is
+// exact (it is a widening).
+#pragma once
+
+namespace dns3d {
+
+__device__ __forceinline__ float d2f(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int fe = (int)((hi >> 20) & 0x7FFu) - 896;  // biased float exponent
+    if (fe <= 0) return __uint_as_float(sign);
+    if (fe >= 255) {
+        const bool nan = ((hi >> 20) & 0x7FFu) == 0x7FFu && (((hi & 0xFFFFFu) | lo) != 0u);
+        return __uint_as_float(sign | (nan ? 0x7FC00000u : 0x7F800000u));
+    }
+    unsigned f = sign | ((unsigned)fe << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1FFFFFFFu;  // the 29 dropped bits
+    f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;  // carries into the exponent
+    return __uint_as_float(f);
+}
+
+__device__ __forceinline__ double f2d(float v) {
+    const unsigned f = __float_as_uint(v);
+    const unsigned e = (f >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) return (double)v;  // zero, subnormal, inf, NaN: rare, the hardware path
+    const unsigned hi = (f & 0x80000000u) | ((e + 896u) << 20) | ((f & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(f << 29));
+}
+
+__device__ __forceinline__ float2 d2f(double2 a) { return make_float2(d2f(a.x), d2f(a.y)); }
+
+}  // namespace dns3d

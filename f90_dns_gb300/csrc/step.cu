@@ -18,6 +18,7 @@
 #include "dns3d_internal.cuh"
 #include "ragged.cuh"
 #include "tc.cuh"
+#include "cvt.cuh"
 
 #include <algorithm>
 
@@ -1565,6 +1566,11 @@ __global__ void k_products32(FRFields in, FRFields out, size_t n) {
     products32_body(in, out, n, blockIdx.x, gridDim.x);
 }
 
+// (The viscous and pressure kernels below convert between FP64 and FP32 with
+// cvt.cuh's integer-pipe d2f / f2d: measured 55 -> 51 us and 76 -> 71 us at
+// 128x128x65.  The vorticity above keeps the hardware conversions, which
+// measured faster there.)
+//
 // Viscous step as an increment in the eigenbasis of the interior Helmholtz
 // problem.  With S_II V = M_II V Lambda, V^T M_II V = I, and the identity
 // M_I (d2 u)_I = -(S u)_I (LGL quadrature is exact for these products), the
@@ -1604,7 +1610,7 @@ __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops o
         A = reinterpret_cast<const float4*>(mx.BoT);
         for (int t = threadIdx.x; t < hoi * (po4 / 4); t += blockDim.x) sBo[t] = __ldg(&A[t]);
     }
-    const float dt = (float)sp.dt, cf = (float)sp.cn_fac, ff = (float)sp.helm_f;
+    const float dt = d2f(sp.dt), cf = d2f(sp.cn_fac), ff = d2f(sp.helm_f);
     for (int comp = 0; comp < 3; ++comp) {
         // fold the interior column: even rows k < hei, odd rows pe4 + k
         for (int t = threadIdx.x; t < pe4 * tc; t += blockDim.x) {
@@ -1615,12 +1621,12 @@ __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops o
                 const size_t o1 = (size_t)(1 + k) * g.nm + m;
                 const double2 a = fptr(F, comp)[o1];
                 const float2 sa = fptr(Src, comp)[o1];
-                const float ax = (float)a.x, ay = (float)a.y;
+                const float ax = d2f(a.x), ay = d2f(a.y);
                 if (k < hoi) {
                     const size_t o2 = (size_t)(g.nz - 2 - k) * g.nm + m;
                     const double2 b = fptr(F, comp)[o2];
                     const float2 sb = fptr(Src, comp)[o2];
-                    const float bx = (float)b.x, by = (float)b.y;
+                    const float bx = d2f(b.x), by = d2f(b.y);
                     se = make_float2(ax + bx, ay + by);
                     de = make_float2(ax - bx, ay - by);
                     ss = make_float2(sa.x + sb.x, sa.y + sb.y);
@@ -1648,7 +1654,7 @@ __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops o
                     const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
                     keep = !(kx > sp.kx_max || kyi > sp.ky_max);
                 }
-                k2 = (float)__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+                k2 = d2f(__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]));
                 if (!keep) k2 = -2.f - k2;  // masked source: flagged by the sign
                 const double2 u0 = fptr(F, comp)[(size_t)m], un = fptr(F, comp)[(size_t)(g.nz - 1) * g.nm + m];
                 double2 b1 = make_double2(0.0, 0.0), b2 = b1;
@@ -1658,8 +1664,8 @@ __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops o
                     b1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
                     b2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
                 }
-                w = make_float4(cf * (float)u0.x + 2.0f * ff * (float)b1.x, cf * (float)u0.y + 2.0f * ff * (float)b1.y,
-                                cf * (float)un.x + 2.0f * ff * (float)b2.x, cf * (float)un.y + 2.0f * ff * (float)b2.y);
+                w = make_float4(cf * d2f(u0.x) + 2.0f * ff * d2f(b1.x), cf * d2f(u0.y) + 2.0f * ff * d2f(b1.y),
+                                cf * d2f(un.x) + 2.0f * ff * d2f(b2.x), cf * d2f(un.y) + 2.0f * ff * d2f(b2.y));
             }
             tk[c] = k2;
             tw[c] = w;
@@ -1752,10 +1758,10 @@ __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops o
                 if (i < hoi) {
                     const size_t o2 = (size_t)(g.nz - 2 - i) * g.nm + m;
                     const double2 u2 = fptr(F, comp)[o2];
-                    fptr(Out, comp)[o1] = make_double2(u1.x + (double)(pe[q].x + po[q].x), u1.y + (double)(pe[q].y + po[q].y));
-                    fptr(Out, comp)[o2] = make_double2(u2.x + (double)(pe[q].x - po[q].x), u2.y + (double)(pe[q].y - po[q].y));
+                    fptr(Out, comp)[o1] = make_double2(u1.x + f2d(pe[q].x + po[q].x), u1.y + f2d(pe[q].y + po[q].y));
+                    fptr(Out, comp)[o2] = make_double2(u2.x + f2d(pe[q].x - po[q].x), u2.y + f2d(pe[q].y - po[q].y));
                 } else {  // middle level (ni odd)
-                    fptr(Out, comp)[o1] = make_double2(u1.x + (double)pe[q].x, u1.y + (double)pe[q].y);
+                    fptr(Out, comp)[o1] = make_double2(u1.x + f2d(pe[q].x), u1.y + f2d(pe[q].y));
                 }
             }
             if (ib == 0) {  // x_1 = bc1, x_n = bc2 (identity rows)
@@ -1792,8 +1798,8 @@ struct DF {
 };
 __device__ __forceinline__ DF df_split(double x) {
     DF r;
-    r.hi = (float)x;
-    r.lo = (float)(x - (double)r.hi);
+    r.hi = d2f(x);
+    r.lo = d2f(x - f2d(r.hi));
     return r;
 }
 // s += a * b, a and b double-float
@@ -1810,7 +1816,7 @@ __device__ __forceinline__ void df_mac(DF& s, float ahi, float alo, float bhi, f
     s.lo += err + e;
     s.hi = t;
 }
-__device__ __forceinline__ double df_value(DF s) { return (double)s.hi + (double)s.lo; }
+__device__ __forceinline__ double df_value(DF s) { return f2d(s.hi) + f2d(s.lo); }
 
 // Folded tile of an FP64 field as double-float pairs: [he][tc] even, [ho][tc] odd;
 // each element float4 = (re.hi, re.lo, im.hi, im.lo).
@@ -1911,10 +1917,10 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
             const double2 b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
             if (k < ho) {
                 const double2 b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
-                fs = make_float2((float)(b1.x + b2.x), (float)(b1.y + b2.y));
-                fd = make_float2((float)(b1.x - b2.x), (float)(b1.y - b2.y));
+                fs = make_float2(d2f(b1.x + b2.x), d2f(b1.y + b2.y));
+                fd = make_float2(d2f(b1.x - b2.x), d2f(b1.y - b2.y));
             } else {
-                fs = make_float2((float)b1.x, (float)b1.y);
+                fs = make_float2(d2f(b1.x), d2f(b1.y));
             }
         }
         tb[k * tc + c] = fs;
@@ -1943,7 +1949,7 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
                 acc[3].x = fmaf(e.w, v.x, acc[3].x); acc[3].y = fmaf(e.w, v.y, acc[3].y);
             }
             const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
-            const float k2 = (float)__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]);
+            const float k2 = d2f(__ldg(&ops.ksq[mode_q(ky, kx, g.ny, g.nxhp)]));
             const float* lam = even ? mx.plame : mx.plamo;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -2016,13 +2022,13 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
             const size_t o1 = (size_t)i * g.nm + m;
             if (i < ho) {
                 const size_t o2 = (size_t)(nz - 1 - i) * g.nm + m;
-                PHI[o1] = make_double2((double)(pe[q].x + po[q].x), (double)(pe[q].y + po[q].y));
-                PHI[o2] = make_double2((double)(pe[q].x - po[q].x), (double)(pe[q].y - po[q].y));
-                PHIZ[o1] = make_double2((double)(de[q].x + dd[q].x), (double)(de[q].y + dd[q].y));
-                PHIZ[o2] = make_double2((double)(de[q].x - dd[q].x), (double)(de[q].y - dd[q].y));
+                PHI[o1] = make_double2(f2d(pe[q].x + po[q].x), f2d(pe[q].y + po[q].y));
+                PHI[o2] = make_double2(f2d(pe[q].x - po[q].x), f2d(pe[q].y - po[q].y));
+                PHIZ[o1] = make_double2(f2d(de[q].x + dd[q].x), f2d(de[q].y + dd[q].y));
+                PHIZ[o2] = make_double2(f2d(de[q].x - dd[q].x), f2d(de[q].y - dd[q].y));
             } else {
-                PHI[o1] = make_double2((double)pe[q].x, (double)pe[q].y);
-                PHIZ[o1] = make_double2((double)de[q].x, (double)de[q].y);
+                PHI[o1] = make_double2(f2d(pe[q].x), f2d(pe[q].y));
+                PHIZ[o1] = make_double2(f2d(de[q].x), f2d(de[q].y));
             }
         }
     }
