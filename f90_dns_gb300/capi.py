@@ -44,7 +44,7 @@ EXPORTED_SYMBOLS = (
     "dns3d_pressure_correction", "dns3d_apply_boundary_conditions", "dns3d_step",
     "dns3d_synchronize", "dns3d_diagnostics", "dns3d_footprint_bytes", "dns3d_strerror",
     "dns3d_last_error", "dns3d_step_timed", "dns3d_profile_kernels", "dns3d_launches_per_step",
-    "dns3d_measure_fp64_tflops", "dns3d_flow_stats_noalloc",
+    "dns3d_measure_fp64_tflops", "dns3d_check_conversions", "dns3d_flow_stats_noalloc",
     "dns3d_ensemble_create", "dns3d_ensemble_destroy", "dns3d_ensemble_size", "dns3d_ensemble_run",
     "dns3d_ensemble_step", "dns3d_ensemble_step_timed", "dns3d_ensemble_info",
     "dns3d_batch_create", "dns3d_batch_step", "dns3d_batch_synchronize", "dns3d_batch_info",
@@ -197,6 +197,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_profile_kernels.argtypes = [hp, ip, C.POINTER(CKernelTime), ip, C.POINTER(C.c_int)]
     lib.dns3d_launches_per_step.argtypes = [hp, C.POINTER(C.c_int)]
     lib.dns3d_measure_fp64_tflops.argtypes = [ip, C.POINTER(C.c_double)]
+    lib.dns3d_check_conversions.argtypes = [ip, C.c_longlong, C.POINTER(C.c_ulonglong)]
     lib.dns3d_flow_stats_noalloc.argtypes = [vp, vp, vp, ip, ip, ip, vp, vp]
     lib.dns3d_ensemble_create.argtypes = [C.POINTER(CConfig), ip, C.POINTER(hp)]
     lib.dns3d_ensemble_destroy.argtypes = [hp]

@@ -1615,6 +1615,12 @@ int dns3d_launches_per_step(dns3d_handle* h, int* n) {
     return DNS3D_OK;
 }
 
+int dns3d_check_conversions(int device, long long n, unsigned long long* mismatches) {
+    if (!mismatches || n < 1) return DNS3D_E_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return DNS3D_E_CUDA;
+    return check_conversions(n, mismatches) == cudaSuccess ? DNS3D_OK : DNS3D_E_CUDA;
+}
+
 int dns3d_measure_fp64_tflops(int device, double* tflops) {
     if (!tflops) return DNS3D_E_INVALID;
     cudaError_t e = measure_fp64_tflops(device, tflops);

@@ -2,8 +2,10 @@
 //
 // On this GPU the hardware conversions (F2F) issue on the FP64 pipe, which
 // runs at 1/64 of the FP32 rate and is what the mixed-precision kernels are
-// bound by; these run on the integer pipes instead.  d2f rounds to nearest
-// even exactly as the hardware does for results in the normal float range;
+// bound by; these run on the integer pipes instead, from the IEEE 754 binary64
+// and binary32 encodings.  d2f rounds to nearest even (IEEE 754 default
+// rounding) for results in the normal float range -- checked bit for bit
+// against the hardware conversion by dns3d_check_conversions;
 // results below it flush to signed zero (the spectra here never come within
 // many decades of 1e-38), overflow gives infinity, NaN stays NaN.  f2d is
 // exact (it is a widening).

@@ -339,6 +339,10 @@ cudaError_t build_tc_slices(const GridDev& g, const double* invF, int nq, __half
 cudaError_t build_tc_anti_image(const GridDev& g, const double* De, const double* Do, __half* image, int* rowexp,
                                 cudaStream_t s);
 
+// The integer-pipe conversions (cvt.cuh) against the hardware ones on n
+// pseudo-random values; mismatches counted.
+cudaError_t check_conversions(long long n, unsigned long long* mismatches);
+
 // Dense FP64 FMA throughput probe (TFLOP/s).
 cudaError_t measure_fp64_tflops(int device, double* tflops);
 

@@ -2326,6 +2326,38 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
     return cudaSuccess;
 }
 
+namespace {
+// d2f / f2d (cvt.cuh) against the hardware conversions on n doubles spread
+// over the normal float range (SplitMix64 bits: sign, exponent in
+// [-126, 127], all mantissas), and on every float of a strided sweep for f2d.
+__global__ void k_cvt_check(long long n, unsigned long long seed, unsigned long long* bad) {
+    unsigned long long nb = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long z = seed + (unsigned long long)i * 0x9E3779B97F4A7C15ULL;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        const unsigned long long e = 1023 - 126 + (z >> 52) % 254;  // float exponents -126 .. 127
+        const double x = __longlong_as_double((long long)((z & 0x800FFFFFFFFFFFFFULL) | (e << 52)));
+        if (__float_as_uint(d2f(x)) != __float_as_uint(__double2float_rn(x))) ++nb;
+        const float v = __uint_as_float((unsigned)(z >> 32));
+        if (isfinite(v) && __double_as_longlong(f2d(v)) != __double_as_longlong((double)v)) ++nb;
+    }
+    if (nb) atomicAdd(bad, nb);
+}
+}  // namespace
+
+cudaError_t check_conversions(long long n, unsigned long long* mismatches) {
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(unsigned long long));
+    if (e) return e;
+    cudaMemset(d, 0, sizeof(unsigned long long));
+    k_cvt_check<<<152 * 8, 256>>>(n, 0x5DEECE66DULL, d);
+    e = cudaMemcpy(mismatches, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e;
+}
+
 cudaError_t launch_pi_update(const GridDev& g, const Ops& ops, const PIParams& pp, const double2* U,
                              dns3d_pi_state* pi, cudaStream_t s) {
     k_pi_update<<<1, 32, 0, s>>>(g, ops.zw, pp, U, pi);

@@ -67,3 +67,14 @@ def test_mixed_error_stays_bounded_over_long_run(built_lib):
             da, db = d64.diagnostics(), dmx.diagnostics()
             assert abs(da.max_div - db.max_div) <= DIV_TOL_400
         assert max(errs) <= VEL_TOL, errs
+
+
+def test_integer_pipe_conversions_match_hardware(built_lib):
+    """The mixed kernels' FP64<->FP32 conversions (integer operations on the
+    bits, IEEE 754 round to nearest even) give the hardware conversion's bits
+    on 2^24 random values of the normal float range."""
+    import ctypes as C
+    from f90_dns_gb300.capi import load_library
+    bad = C.c_ulonglong(1)
+    assert load_library().dns3d_check_conversions(0, 1 << 24, C.byref(bad)) == 0
+    assert bad.value == 0
