@@ -347,7 +347,8 @@ def run_ours(args) -> None:
                     "grids": sorted({f"{d['nx']}x{d['ny']}x{d['nz']}" for d in draws}),
                     "mixed": res["mixed"], "fp64": res["fp64"],
                     "mixed_speedup_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"],
-                    "launch": "one CUDA graph per step; each of its ten stages one ragged kernel launch over all runs"}
+                    "launch": "one CUDA graph per step; each stage one ragged kernel launch over the runs of one "
+                              "precision and kernel variant"}
 
     # serving: Poisson arrivals of seed-drawn runs, continuous batching
     serving = None

@@ -54,16 +54,6 @@ template <typename P> __device__ __forceinline__ P* fptr(const FieldsT<P>& f, in
     return r;
 }
 
-// tile[f][z][c] <- field f at (z, m0 + c); zero beyond nm.
-__device__ __forceinline__ void load_tile(double2* tile, const double2* __restrict__ src,
-                                          const GridDev& g, int m0, int tc) {
-    for (int t = threadIdx.x; t < g.nz * tc; t += blockDim.x) {
-        const int z = t / tc, c = t - z * tc;
-        const int m = m0 + c;
-        tile[t] = (m < g.nm) ? src[(size_t)z * g.nm + m] : make_double2(0.0, 0.0);
-    }
-}
-
 // ------------------------------------------------------------------ PI / forcing
 // update_pressure_gradient_3d (3D:2488-2549) called with the namelist istart
 // (3D:1118), and calculate_bulk_velocity_3d (3D:2434-2464) from the (0,0) mode:
@@ -554,7 +544,6 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     const int nbe = t.e8 >> 3, nbo = t.o8 >> 3;
     const int ncore = t.ncore_e + t.ncore_o;
     const int nv = he + ho;  // valid rows / K indices
-    const int nchunk = m8 >> 3;
     bool ok = true;
     for (int q = q0; q < q1 && ok; ++q) {
         const uint32_t par = (uint32_t)((q - q0) & 1);
@@ -1586,7 +1575,6 @@ __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops o
                                                    Fields F, FFields Src, const double2* __restrict__ GP,
                                                    Fields Out, int tc, int bx) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int ni = g.nz - 2;
     const int hei = mx.hei, hoi = mx.hoi, pe4 = mx.pe4, po4 = mx.po4;
     const int nr = pe4 + po4;        // folded rows (even block, then odd block)
     const int tsz = nr * tc;
