@@ -764,12 +764,15 @@ __global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepPara
 // tensor-core products (tc.cuh), then Op::out forms the kernel's outputs from
 // the derivatives exactly as the FP64-pipe kernel does.  D1 is the same for
 // every mode, so its digit image is copied into shared memory once per CTA
-// and a CTA runs tiles of 32 right-hand-side columns (modes x fields x re/im).
+// and a CTA runs tiles of kTcVortCols right-hand-side columns (modes x fields
+// x re/im; 16, so that two 512-thread CTAs share an SM).
 // Per tile: (b) fold the fields; (c) column scales; (d) digits; (e) 35 MMAs
 // (digit slice sa of D1 against right-hand-side digit slices 0..6-sa side by
-// side, N = 32 (7-sa)) into 7 weight-class accumulators (224 TMEM columns);
+// side, N = 16 (7-sa)) into 7 weight-class accumulators (112 TMEM columns);
 // (f) exact int64 combination -> D1.f in FP64; (g) Op::out per level pair.
-constexpr int kTcVortCols = 32;
+constexpr int kTcVortCols = 16;  // right-hand-side columns per tile (2 CTAs of 512 threads per SM)
+constexpr int kTcVortModes = kTcVortCols / 4;  // modes per tile: u, v x re, im
+constexpr int kTcCorrModes = kTcVortCols / 2;  // modes per tile: phi x re, im
 constexpr int kTcVortThreads = 512;
 
 template <class Op>
@@ -794,7 +797,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         for (int i = tid; i < kTcSlices * b_halves / 8; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
     }
     for (int i = tid; i < m8; i += blockDim.x) sE[i] = __ldg(&ops.tcDE[i]);
-    if (tid < 32) tc_alloc(tbase, 256);
+    if (tid < 32) tc_alloc(tbase, kTcClasses * kTcVortCols <= 128 ? 128 : 256);
     if (tid == 0) {
         tc_mbar_init(&mbar[0]);
         tc_mbar_init(&mbar[1]);
@@ -951,7 +954,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (tid < 32) tc_dealloc(tmem, 256);
+    if (tid < 32) tc_dealloc(tmem, kTcClasses * kTcVortCols <= 128 ? 128 : 256);
 }
 
 // omega = (wy - vz, uz - wx, vx - uy) from D1.u, D1.v, as vorticity_body forms it
@@ -2414,11 +2417,11 @@ bool vorticity_tc_fits(const GridDev& g) {
 }
 
 // Tiles (of `modes` modes) per CTA: at least 4 (the D1 image is copied once
-// per CTA), else one CTA per SM.  The chunking does not change a tile's
+// per CTA), else two CTAs per SM.  The chunking does not change a tile's
 // arithmetic.
 int tc_dz_chunk(int nm, int modes) {
     const int ntiles = (nm + modes - 1) / modes;
-    return std::max(4, (ntiles + 151) / 152);
+    return std::max(4, (ntiles + 2 * 152 - 1) / (2 * 152));
 }
 
 template <class Op>
@@ -2642,7 +2645,7 @@ struct RsVort64Tc {
             pi_update_body(d.g, d.ops.zw, d.pp, d.U, d.pi, 0);
             return;
         }
-        const int ntiles = (d.g.nm + 7) / 8, chunk = d.vort_chunk;  // 8 modes per tile
+        const int ntiles = (d.g.nm + kTcVortModes - 1) / kTcVortModes, chunk = d.vort_chunk;
         const int t0 = (b - 1) * chunk;
         const VortTcOp op{d.U, d.V, d.W, d.US, d.VS, d.WS};
         dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
@@ -2740,7 +2743,7 @@ struct RsCorr64 {
 struct RsCorr64Tc {
     static constexpr int kMinCtas = 1;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
-        const int ntiles = (d.g.nm + 15) / 16, chunk = d.corr_chunk;  // 16 modes per tile
+        const int ntiles = (d.g.nm + kTcCorrModes - 1) / kTcCorrModes, chunk = d.corr_chunk;
         const int t0 = b * chunk;
         const CorrTcOp op{d.sp, d.US, d.VS, d.WS, d.PHI, d.U, d.V, d.W, d.P, d.GP};
         dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
@@ -2801,8 +2804,8 @@ void ragged_geometry(RunDesc& d) {
     d.gx[kRsCorr] = cdiv((long long)g.nz * g.nm, 4 * kStageThreads);
     d.gx[kRsBc] = cdiv(2LL * g.nm, kStageThreads);
     d.gx[kRsVisc] = tc_q_per_cta(d.ops.nq);  // operator indices per CTA of the tensor-core viscous body
-    d.vort_chunk = tc_dz_chunk(g.nm, 8);       // tiles per CTA of the tensor-core z-derivative bodies
-    d.corr_chunk = tc_dz_chunk(g.nm, 16);
+    d.vort_chunk = tc_dz_chunk(g.nm, kTcVortModes);  // tiles per CTA of the tensor-core z-derivative bodies
+    d.corr_chunk = tc_dz_chunk(g.nm, kTcCorrModes);
 }
 
 int ragged_tile_kernel(int stage, bool mixed) {
@@ -2821,7 +2824,8 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
     const int tiles = k >= 0 ? (g.nm + g.tc[k] - 1) / g.tc[k] : 0;
     switch (stage) {
         case kRsVort:
-            if (!mixed && (ragged_variant(d) & kRvVortTc)) return 1 + ((g.nm + 7) / 8 + d.vort_chunk - 1) / d.vort_chunk;
+            if (!mixed && (ragged_variant(d) & kRvVortTc))
+                return 1 + ((g.nm + kTcVortModes - 1) / kTcVortModes + d.vort_chunk - 1) / d.vort_chunk;
             return 1 + tiles;
         case kRsFftYInv:
         case kRsFftC2R: return 6 * d.gx[stage];
@@ -2834,7 +2838,8 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
             return tiles;
         case kRsPres: return tiles;
         case kRsCorr:
-            if (!mixed && (ragged_variant(d) & kRvCorrTc)) return ((g.nm + 15) / 16 + d.corr_chunk - 1) / d.corr_chunk;
+            if (!mixed && (ragged_variant(d) & kRvCorrTc))
+                return ((g.nm + kTcCorrModes - 1) / kTcCorrModes + d.corr_chunk - 1) / d.corr_chunk;
             return mixed ? d.gx[stage] : tiles;
         case kRsViscMean:
         case kRsPresMean: return mixed ? 1 : 0;
