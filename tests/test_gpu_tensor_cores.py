@@ -25,7 +25,9 @@ def _names(d):
 
 @pytest.mark.parametrize("wl", [C1, dict(C1, nx=16, ny=24, nz=65, lgl_dmatrix_guard=False, flow_control_method=2,
                                           target_bulk_velocity=2.0 / 3.0, controller_gain=0.5,
-                                          controller_update_freq=1)])
+                                          controller_update_freq=1),
+                                dict(C1, nx=16, ny=16, nz=97, lgl_dmatrix_guard=False),
+                                dict(C1, nx=24, ny=16, nz=17)])
 def test_tensor_core_viscous_matches_oracle(built_lib, monkeypatch, wl):
     monkeypatch.setenv("DNS3D_TENSOR_CORES", "1")
     with ChannelDNS(config_from(wl)) as d:
@@ -99,4 +101,18 @@ def test_tensor_core_wait_runs_out_and_reports(built_lib, monkeypatch):
     monkeypatch.delenv("DNS3D_TC_TEST_STALL")
     with ChannelDNS(config_from(wl)) as d:
         d.step(2)
+        assert np.isfinite(d.diagnostics().energy)
+
+
+def test_tensor_core_forms_fall_back_where_operands_do_not_fit(built_lib, monkeypatch):
+    """nz = 127 puts the operands past the shared memory of one CTA: even when
+    forced, the handle keeps the FP64-pipe kernels and steps normally."""
+    monkeypatch.setenv("DNS3D_TENSOR_CORES", "1")
+    wl = dict(C1, nx=16, ny=16, nz=127, lgl_dmatrix_guard=False)
+    with ChannelDNS(config_from(wl)) as d:
+        names = _names(d)
+    assert {"viscous_helmholtz", "vorticity", "pressure_correction"} <= names
+    assert not any(n.endswith("_tc") for n in names)
+    with ChannelDNS(config_from(wl)) as d:
+        d.step(3)
         assert np.isfinite(d.diagnostics().energy)
