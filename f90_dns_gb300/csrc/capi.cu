@@ -61,6 +61,7 @@ struct dns3d_handle {
     // (ops.tcD built), chosen likewise
     bool vort_tc = false;
     bool corr_tc = false;
+    bool pres_tc = false;  // the strong-form pressure right-hand side's D1.w*
     int red_blocks = 0;
     std::vector<double> zpts, zwts;
     std::vector<void*> allocs;
@@ -473,6 +474,11 @@ int run_pressure(dns3d_handle* h) {
         mark(h, "pressure_jacgs");
         return DNS3D_OK;
     }
+    if (h->pres_tc) {
+        CK(h, launch_pressure_tc(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->d_tcerr, h->stream));
+        mark(h, "pressure_poisson_tc");
+        return DNS3D_OK;
+    }
     CK(h, launch_pressure(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->stream));
     mark(h, "pressure_poisson");
     return DNS3D_OK;
@@ -614,8 +620,9 @@ namespace {
 // thread's fixed-order sum, so results are bitwise the same for any width.
 using TuneKey = std::tuple<int, int, int, int, int>;
 std::mutex g_tune_mu;
-// the widths, then 1 if the viscous solve, the vorticity, the projection runs on the tensor cores
-std::map<TuneKey, std::array<int, kTileKernels + 3>> g_tune;
+// the widths, then 1 if the viscous solve, the vorticity, the projection, the
+// pressure right-hand side runs on the tensor cores
+std::map<TuneKey, std::array<int, kTileKernels + 4>> g_tune;
 
 int tile_launch(dns3d_handle* h, int k) {
     const GridDev& g = h->g;
@@ -663,6 +670,7 @@ int autotune(dns3d_handle* h, bool force) {
             if (h->ops.tcD && !h->visc_tc_forced) {
                 h->vort_tc = it->second[kTileKernels + 1] != 0;
                 h->corr_tc = it->second[kTileKernels + 2] != 0;
+                h->pres_tc = it->second[kTileKernels + 3] != 0;
             }
             return DNS3D_OK;
         }
@@ -673,7 +681,7 @@ int autotune(dns3d_handle* h, bool force) {
     // the FP64-pipe viscous kernel (last in kFp64) is not timed when the
     // tensor-core one is forced
     const int nk = h->mixed ? 3 : (h->visc_tc_forced ? 3 : 4);
-    float visc_ms = 0.f, vort_ms = 0.f, corr_ms = 0.f;
+    float visc_ms = 0.f, vort_ms = 0.f, corr_ms = 0.f, pres_ms = 0.f;
     cudaEvent_t e0, e1;
     CK(h, cudaEventCreate(&e0));
     CK(h, cudaEventCreate(&e1));
@@ -699,6 +707,7 @@ int autotune(dns3d_handle* h, bool force) {
         if (k == kTileVisc) visc_ms = best_ms;
         if (k == kTileVort) vort_ms = best_ms;
         if (k == kTileCorr) corr_ms = best_ms;
+        if (k == kTilePres) pres_ms = best_ms;
     }
     // the tensor-core viscous solve against the best FP64-pipe width
     if (!rc && !h->mixed && h->ops.tcA && !h->visc_tc_forced) {
@@ -761,6 +770,25 @@ int autotune(dns3d_handle* h, bool force) {
             h->corr_tc = corr_ms <= 0.f || ms < corr_ms;
         }
     }
+    // the tensor-core pressure (right-hand side and solve) against the best
+    // FP64-pipe width; the strong form only
+    if (!rc && !h->mixed && h->ops.tcD && !h->visc_tc_forced && !h->sp.weak_form) {
+        auto launch = [&] {
+            return launch_pressure_tc(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->d_tcerr, h->stream);
+        };
+        cudaError_t ce = launch();
+        if (!ce) ce = cudaEventRecord(e0, h->stream);
+        for (int r = 0; r < 3 && !ce; ++r) ce = launch();
+        if (!ce) ce = cudaEventRecord(e1, h->stream);
+        if (!ce) ce = cudaEventSynchronize(e1);
+        if (ce) {
+            rc = cuda_fail(h, ce, "autotune (tensor-core pressure)");
+        } else {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            h->pres_tc = pres_ms <= 0.f || ms < pres_ms;
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
@@ -769,11 +797,12 @@ int autotune(dns3d_handle* h, bool force) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
     }
-    std::array<int, kTileKernels + 3> tiles{};
+    std::array<int, kTileKernels + 4> tiles{};
     for (int k = 0; k < kTileKernels; ++k) tiles[k] = h->g.tc[k];
     tiles[kTileKernels] = h->visc_tc ? 1 : 0;
     tiles[kTileKernels + 1] = h->vort_tc ? 1 : 0;
     tiles[kTileKernels + 2] = h->corr_tc ? 1 : 0;
+    tiles[kTileKernels + 3] = h->pres_tc ? 1 : 0;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[key] = tiles;
     return DNS3D_OK;
@@ -1197,6 +1226,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
         h->visc_tc_forced = tcenv && std::strcmp(tcenv, "1") == 0;
         h->vort_tc = h->visc_tc_forced || g.nm >= 4 * 152 * 8;
         h->corr_tc = h->visc_tc_forced || g.nm >= 4 * 152 * 16;
+        h->pres_tc = !c.use_weak_form_divergence && (h->visc_tc_forced || g.nm >= 4 * 152 * 16);
     }
 
     if ((rc = dns3d_initialize_fields(h))) return fail(rc);
@@ -1833,7 +1863,7 @@ size_t stage_smem_limit(StageKernel k) {
 // Raises every stage kernel's dynamic shared-memory limit to the device's
 // opt-in maximum (a property of the kernel, shared by all batches).
 cudaError_t prepare_stage_kernels() {
-    for (int m = 0; m < 2 * 8; ++m)
+    for (int m = 0; m < 2 * 16; ++m)  // precision x RaggedVariant bits
         for (int s = 0; s < kRsStages; ++s) {
             StageKernel k = ragged_kernel(s, m & 1, m >> 1);
             const size_t lim = stage_smem_limit(k);
@@ -1865,7 +1895,7 @@ RunDesc make_desc(const dns3d_handle* h) {
         d.ops.tcA = nullptr;
         d.ops.tcE = nullptr;
     }
-    d.tcmask = (h->vort_tc ? 1 : 0) | (h->corr_tc ? 2 : 0);
+    d.tcmask = (h->vort_tc ? 1 : 0) | (h->corr_tc ? 2 : 0) | (h->pres_tc ? 4 : 0);
     if (!d.tcmask) {
         d.ops.tcD = nullptr;
         d.ops.tcDE = nullptr;
@@ -2046,6 +2076,7 @@ cudaError_t group_capture(dns3d_batch::Group& G, int* launches) {
         if (!ce) ce = cudaEventRecord(G.side_join, side);
     }
     stage(kRsVisc, lane);
+    stage(kRsPresRhs, lane);
     stage(kRsPres, lane);
     if (G.mixed && !ce) ce = cudaStreamWaitEvent(lane, G.side_join, 0);
     stage(kRsCorr, lane);

@@ -253,6 +253,10 @@ bool viscous_tc_fits(const GridDev& g);
 // emulated FP64 (ops.tcD set); err as for launch_viscous_tc.
 cudaError_t launch_vorticity_tc(const GridDev& g, const Ops& ops, const double2* U, const double2* V,
                                 const double2* W, double2* OX, double2* OY, double2* OZ, int* err, cudaStream_t s);
+// solve_pressure_3d (strong form) with D1.w* on the tensor cores (ops.tcD
+// set): the right-hand side into PHI, then the per-mode Poisson solve in place
+cudaError_t launch_pressure_tc(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                               const double2* VS, const double2* WS, double2* PHI, int* err, cudaStream_t s);
 // pressure_correction_3d with D1.phi on the tensor cores (ops.tcD set)
 cudaError_t launch_correction_tc(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
                                  const double2* VS, const double2* WS, const double2* PHI, double2* U, double2* V,

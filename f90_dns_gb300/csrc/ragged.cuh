@@ -36,6 +36,9 @@ enum RaggedStage {
     // kRsVisc and kRsPres (mode (0,0) of w* is all the pinned solve reads)
     kRsViscMean,
     kRsPresMean,
+    // FP64 runs with the tensor-core pressure: the divergence right-hand side
+    // (D1.w* on the tensor cores) into PHI, before kRsPres solves it in place
+    kRsPresRhs,
     kRsStages
 };
 
@@ -60,7 +63,7 @@ struct RunDesc {
     int ncol;                // columns the forward y pass completes
     int gx[kRsStages];       // virtual blocks per field of each stage (transforms, elementwise passes);
                              // kRsVisc: operator indices per CTA of the tensor-core viscous body
-    int tcmask;              // z-derivatives on the tensor cores: 1 vorticity, 2 projection
+    int tcmask;              // z-derivatives on the tensor cores: 1 vorticity, 2 projection, 4 pressure
     int vort_chunk, corr_chunk;  // mode tiles per CTA of those bodies
 };
 
@@ -111,7 +114,7 @@ static_assert(sizeof(RunDesc) % 8 == 0, "descriptor copied in 8-byte words");
 using StageKernel = void (*)(const RunDesc*, StageMap);
 
 // Kernel variants of FP64 runs: which stages run their tensor-core bodies.
-enum RaggedVariant { kRvVortTc = 1, kRvCorrTc = 2, kRvViscTc = 4 };
+enum RaggedVariant { kRvVortTc = 1, kRvCorrTc = 2, kRvViscTc = 4, kRvPresTc = 8 };
 int ragged_variant(const RunDesc& d);
 // The k_stage instantiation of a stage for FP64 (mixed = false, with the
 // variant) or mixed runs (step.cu; the transform passes come from fft_ct.cu).

@@ -1144,6 +1144,71 @@ __device__ __forceinline__ void pressure_body(GridDev g, Ops ops, StepParams sp,
     }
 }
 
+// The Poisson solve of pressure_body for a right-hand side already in PHI
+// (unfolded, as pressure_body forms it): fold, apply the per-mode inverses
+// (the pinned mode (0,0) unfolded), write phi over it.  A CTA reads its tile
+// whole before it writes, so the solve is in place.
+__device__ __forceinline__ void pressure_solve_body(const GridDev& g, const Ops& ops, double2* __restrict__ PHI,
+                                                    int tc, int bx) {
+    extern __shared__ double2 sm[];
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
+    const int tsz = nz * tc;
+    double2* tb = sm + tsz;        // folded rhs tile (the layout of pressure_body)
+    double2* bpin = sm + 2 * tsz;  // unfolded rhs of mode (0,0)
+    const int m0 = bx * tc;
+    fold_load(tb, PHI, g, m0, tc, he, ho);
+    if (m0 == 0)
+        for (int z = threadIdx.x; z < nz; z += blockDim.x) bpin[z] = PHI[(size_t)z * g.nm];
+    __syncthreads();
+    const size_t qstride = (size_t)he * he + (size_t)ho * ho;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int c = t / he, k = t - c * he;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        Pair x;
+        if (m == 0) {
+            double2 a = make_double2(0.0, 0.0), b = a;
+            for (int zp = 0; zp < nz; ++zp) {
+                const double2 bb = bpin[zp];
+                const double h1 = __ldg(&ops.PpinT[(size_t)zp * nz + k]);
+                const double h2 = __ldg(&ops.PpinT[(size_t)zp * nz + nz - 1 - k]);
+                a.x = fma(h1, bb.x, a.x); a.y = fma(h1, bb.y, a.y);
+                b.x = fma(h2, bb.x, b.x); b.y = fma(h2, bb.y, b.y);
+            }
+            x.a = a;
+            x.b = b;
+        } else {
+            const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+            x = inv_apply(ops.PinvF + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * qstride, tb, k, c, tc, he, ho);
+        }
+        PHI[(size_t)k * g.nm + m] = x.a;
+        if (k < ho) PHI[(size_t)(nz - 1 - k) * g.nm + m] = x.b;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_pressure_solve(GridDev g, Ops ops, double2* __restrict__ PHI, int tc) {
+    pressure_solve_body(g, ops, PHI, tc, blockIdx.x);
+}
+
+// The divergence right-hand side of pressure_body (strong form) from D1.w*,
+// written unfolded into PHI for pressure_solve_body
+struct PresRhsTcOp {
+    static constexpr int kFields = 1;
+    StepParams sp;
+    const double2* __restrict__ US;
+    const double2* __restrict__ VS;
+    const double2* __restrict__ WS;
+    double2* __restrict__ PHI;
+    __device__ const double2* field(int) const { return WS; }
+    __device__ void out(const GridDev& g, const Ops& ops, int m, int k, int npt, const Pair* dzp) const {
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        for (int p = 0; p < npt; ++p) {
+            const int z = p ? g.nz - 1 - k : k;
+            PHI[(size_t)z * g.nm + m] = pressure_rhs(g, ops, sp, z, m, mi, US, VS, p ? dzp[0].b : dzp[0].a);
+        }
+    }
+};
+
 __global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams sp,
                                                   const double2* __restrict__ US,
                                                   const double2* __restrict__ VS,
@@ -2312,6 +2377,8 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
     if ((e = set_smem(k_viscous_tc, 0))) return e;
     if ((e = set_smem(k_dz_tc<VortTcOp>, 0))) return e;
     if ((e = set_smem(k_dz_tc<CorrTcOp>, 0))) return e;
+    if ((e = set_smem(k_dz_tc<PresRhsTcOp>, 0))) return e;
+    if ((e = set_smem(k_pressure_solve, 0))) return e;
     if ((e = set_smem(k_pcg_poisson, pcg_smem(g)))) return e;
     if ((e = set_smem(k_pcg_helmholtz, pcg_smem(g)))) return e;
     return cudaSuccess;
@@ -2413,7 +2480,8 @@ size_t vorticity_tc_smem(const GridDev& g) {
 
 bool vorticity_tc_fits(const GridDev& g) {
     return tc_supported(g.nz) && vorticity_tc_smem(g) <= smem_limit(k_dz_tc<VortTcOp>) &&
-           vorticity_tc_smem(g) <= smem_limit(k_dz_tc<CorrTcOp>);
+           vorticity_tc_smem(g) <= smem_limit(k_dz_tc<CorrTcOp>) &&
+           vorticity_tc_smem(g) <= smem_limit(k_dz_tc<PresRhsTcOp>);
 }
 
 // Tiles (of `modes` modes) per CTA: at least 4 (the D1 image is copied once
@@ -2438,6 +2506,18 @@ cudaError_t launch_vorticity_tc(const GridDev& g, const Ops& ops, const double2*
                                 const double2* W, double2* OX, double2* OY, double2* OZ, int* err, cudaStream_t s) {
     const VortTcOp op{U, V, W, OX, OY, OZ};
     return launch_dz_tc(g, ops, op, err, s);
+}
+
+cudaError_t launch_pressure_tc(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                               const double2* VS, const double2* WS, double2* PHI, int* err, cudaStream_t s) {
+    if (sp.weak_form) return cudaErrorInvalidValue;  // the weak form's operator has no digit image
+    const PresRhsTcOp op{sp, US, VS, WS, PHI};
+    cudaError_t e = launch_dz_tc(g, ops, op, err, s);
+    if (e) return e;
+    const int tc = tile_width(g, kTilePres);
+    const size_t sm = (2 * (size_t)g.nz * tc + g.nz) * sizeof(double2);
+    k_pressure_solve<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, PHI, tc);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_correction_tc(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
@@ -2716,6 +2796,25 @@ struct RsPres64 {
     }
 };
 
+// the Poisson solve of a right-hand side RsPresRhs left in PHI
+struct RsPres64Tc {
+    static constexpr int kMinCtas = 4;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        pressure_solve_body(d.g, d.ops, d.PHI, d.g.tc[kTilePres], b);
+    }
+};
+
+// the divergence right-hand side with D1.w* on the tensor cores (RunDesc::tcmask bit 4)
+struct RsPresRhs64 {
+    static constexpr int kMinCtas = 1;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        const int ntiles = (d.g.nm + kTcCorrModes - 1) / kTcCorrModes, chunk = d.corr_chunk;
+        const int t0 = b * chunk;
+        const PresRhsTcOp op{d.sp, d.US, d.VS, d.WS, d.PHI};
+        dz_tc_body(d.g, d.ops, op, t0, min(t0 + chunk, ntiles), d.tcerr);
+    }
+};
+
 struct RsPres32 {
     static constexpr int kMinCtas = 3;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
@@ -2772,7 +2871,9 @@ StageKernel ragged_kernel(int stage, bool mixed, int variant) {
         case kRsProd: return mixed ? k_stage<RsProd<float>> : k_stage<RsProd<double>>;
         case kRsVisc:
             return mixed ? k_stage<RsVisc32> : ((variant & kRvViscTc) ? k_stage<RsVisc64Tc> : k_stage<RsVisc64>);
-        case kRsPres: return mixed ? k_stage<RsPres32> : k_stage<RsPres64>;
+        case kRsPres:
+            return mixed ? k_stage<RsPres32> : ((variant & kRvPresTc) ? k_stage<RsPres64Tc> : k_stage<RsPres64>);
+        case kRsPresRhs: return k_stage<RsPresRhs64>;
         case kRsCorr:
             return mixed ? k_stage<RsCorr32> : ((variant & kRvCorrTc) ? k_stage<RsCorr64Tc> : k_stage<RsCorr64>);
         case kRsBc: return k_stage<RsBc>;
@@ -2788,6 +2889,7 @@ StageKernel ragged_kernel(int stage, bool mixed, int variant) {
 
 int ragged_variant(const RunDesc& d) {
     return ((d.tcmask & 1) ? kRvVortTc : 0) | ((d.tcmask & 2) ? kRvCorrTc : 0) |
+           ((d.tcmask & 4) && !d.sp.weak_form ? kRvPresTc : 0) |
            ((d.ops.tcA && d.sp.cn_identity) ? kRvViscTc : 0);
 }
 
@@ -2837,6 +2939,10 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
             if (!mixed && (ragged_variant(d) & kRvViscTc)) return (d.ops.nq + d.gx[kRsVisc] - 1) / d.gx[kRsVisc];
             return tiles;
         case kRsPres: return tiles;
+        case kRsPresRhs:
+            if (!mixed && (ragged_variant(d) & kRvPresTc))
+                return ((g.nm + kTcCorrModes - 1) / kTcCorrModes + d.corr_chunk - 1) / d.corr_chunk;
+            return 0;
         case kRsCorr:
             if (!mixed && (ragged_variant(d) & kRvCorrTc))
                 return ((g.nm + kTcCorrModes - 1) / kTcCorrModes + d.corr_chunk - 1) / d.corr_chunk;
@@ -2860,6 +2966,7 @@ size_t ragged_smem(int stage, bool mixed, const RunDesc& d) {
             if (!mixed && (ragged_variant(d) & kRvViscTc)) return viscous_tc_smem(g);
             return mixed ? viscous_mixed_smem(g, tc) : 6 * nz * tc * sizeof(double2);
         case kRsPres: return mixed ? pressure_mixed_smem(g, tc) : (2 * nz * tc + nz) * sizeof(double2);
+        case kRsPresRhs: return (!mixed && (ragged_variant(d) & kRvPresTc)) ? vorticity_tc_smem(g) : 0;
         case kRsCorr:
             if (!mixed && (ragged_variant(d) & kRvCorrTc)) return vorticity_tc_smem(g);
             return mixed ? 0 : nz * tc * sizeof(double2);

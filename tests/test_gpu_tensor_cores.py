@@ -1,5 +1,5 @@
 """GPU: the Crank-Nicolson viscous solve and the z-derivatives of the
-vorticity and the projection on the tensor cores (emulated FP64: FP16 digit slices of the operators and
+vorticity, the pressure right-hand side and the projection on the tensor cores (emulated FP64: FP16 digit slices of the operators and
 right-hand sides, exact FP32 tcgen05 accumulation, integer combination) keep
 the plain path's parity bar against the oracle, agree with the FP64-pipe
 kernels to 2^-47 of the operand scales, and give the same bits in a batch as
@@ -31,7 +31,7 @@ def _names(d):
 def test_tensor_core_viscous_matches_oracle(built_lib, monkeypatch, wl):
     monkeypatch.setenv("DNS3D_TENSOR_CORES", "1")
     with ChannelDNS(config_from(wl)) as d:
-        assert {"viscous_helmholtz_tc", "vorticity_tc", "pressure_correction_tc"} <= _names(d)
+        assert {"viscous_helmholtz_tc", "vorticity_tc", "pressure_poisson_tc", "pressure_correction_tc"} <= _names(d)
     with ChannelDNS(config_from(wl)) as d:
         d.step(50)
         gst = d.get_state()
@@ -47,8 +47,8 @@ def test_tensor_core_viscous_matches_oracle(built_lib, monkeypatch, wl):
 def test_tensor_core_viscous_agrees_with_fp64_pipe(built_lib, monkeypatch):
     wl = dict(C2, nx=64, ny=64, noise_amplitude=0.0)
     out = {}
-    for mode, names in (("1", {"viscous_helmholtz_tc", "vorticity_tc", "pressure_correction_tc"}),
-                        ("0", {"viscous_helmholtz", "vorticity", "pressure_correction"})):
+    for mode, names in (("1", {"viscous_helmholtz_tc", "vorticity_tc", "pressure_poisson_tc", "pressure_correction_tc"}),
+                        ("0", {"viscous_helmholtz", "vorticity", "pressure_poisson", "pressure_correction"})):
         monkeypatch.setenv("DNS3D_TENSOR_CORES", mode)
         with ChannelDNS(config_from(wl)) as d:
             assert names <= _names(d)
@@ -75,7 +75,7 @@ def test_tensor_core_runs_in_batches_bitwise(built_lib, monkeypatch):
         states = [ens.run(i).get_state(walls=False) for i in range(len(ens))]
     for cfg, st in zip(cfgs, states):
         with ChannelDNS(cfg) as d:
-            assert {"viscous_helmholtz_tc", "vorticity_tc", "pressure_correction_tc"} <= _names(d)
+            assert {"viscous_helmholtz_tc", "vorticity_tc", "pressure_poisson_tc", "pressure_correction_tc"} <= _names(d)
         with ChannelDNS(cfg) as d:
             d.step(3)
             solo = d.get_state(walls=False)
@@ -111,7 +111,7 @@ def test_tensor_core_forms_fall_back_where_operands_do_not_fit(built_lib, monkey
     wl = dict(C1, nx=16, ny=16, nz=127, lgl_dmatrix_guard=False)
     with ChannelDNS(config_from(wl)) as d:
         names = _names(d)
-    assert {"viscous_helmholtz", "vorticity", "pressure_correction"} <= names
+    assert {"viscous_helmholtz", "vorticity", "pressure_poisson", "pressure_correction"} <= names
     assert not any(n.endswith("_tc") for n in names)
     with ChannelDNS(config_from(wl)) as d:
         d.step(3)
