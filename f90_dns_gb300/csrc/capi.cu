@@ -1863,7 +1863,7 @@ size_t stage_smem_limit(StageKernel k) {
 // Raises every stage kernel's dynamic shared-memory limit to the device's
 // opt-in maximum (a property of the kernel, shared by all batches).
 cudaError_t prepare_stage_kernels() {
-    for (int m = 0; m < 2 * 16; ++m)  // precision x RaggedVariant bits
+    for (int m = 0; m < 2 * 32; ++m)  // precision x RaggedVariant bits
         for (int s = 0; s < kRsStages; ++s) {
             StageKernel k = ragged_kernel(s, m & 1, m >> 1);
             const size_t lim = stage_smem_limit(k);
@@ -1924,7 +1924,12 @@ RunDesc make_desc(const dns3d_handle* h) {
             d.phys[f] = h->phys[f];
         }
         d.src[0] = h->SU; d.src[1] = h->SV; d.src[2] = h->SW;
-        d.tw_ny = h->fft.tw_ny; d.tw_nx2 = h->fft.tw_nx2; d.tw_nx = h->fft.tw_nx;
+        d.fftfx = h->fft.fx ? 1 : 0;
+        if (d.fftfx) {
+            d.tw_ny = h->fft.twq_ny; d.tw_nx2 = h->fft.twq_nx2; d.tw_nx = h->fft.twq_nx;
+        } else {
+            d.tw_ny = h->fft.tw_ny; d.tw_nx2 = h->fft.tw_nx2; d.tw_nx = h->fft.tw_nx;
+        }
     }
     d.ncol = h->sp.dealias ? std::min(h->sp.kx_max + 1, h->g.nxhp) : h->g.nxhp;
     if (d.ncol < 1) d.ncol = h->g.nxhp;

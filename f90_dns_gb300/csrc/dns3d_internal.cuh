@@ -85,6 +85,13 @@ struct FftCtx {
     float2* tw32_ny;     // FP32 copies of the tables (mixed path)
     float2* tw32_nx2;
     float2* tw32_nx;
+    longlong2* twq_ny = nullptr;   // Q62 integer copies (fixed-point FP64 transforms)
+    longlong2* twq_nx2 = nullptr;
+    longlong2* twq_nx = nullptr;
+    // FP64 transforms in 64-bit fixed point on the integer pipes (fft_ct.cu);
+    // set for grids with compile-time kernels unless DNS3D_FFT_FP64=1 keeps
+    // them on the FP64 pipe
+    bool fx = false;
     double2* tmp;        // spectral scratch for nf fields
     float2* tmp32 = nullptr;  // FP32 spectral scratch (mixed path)
     int tmp_fields;
@@ -105,6 +112,15 @@ cudaError_t fft_ct_c2r_x(FieldsT<typename Cx<T>::type> src, FieldsT<T> dst, cons
 template <typename T>
 cudaError_t fft_ct_r2c_x(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, const GridDev& g, int nrows, int nf,
                          const typename Cx<T>::type* tw_n, const typename Cx<T>::type* tw_nx, cudaStream_t s);
+
+// The FP64 passes of fft_ct in block fixed point (Q62 twiddle tables).
+template <int SIGN>
+cudaError_t fft_fx_y(Fields src, Fields dst, const GridDev& g, int nplanes, int ncol, int nf, const longlong2* tw,
+                     cudaStream_t s);
+cudaError_t fft_fx_c2r_x(Fields src, RFields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
+                         const longlong2* tw_nx, cudaStream_t s);
+cudaError_t fft_fx_r2c_x(RFields src, Fields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
+                         const longlong2* tw_nx, cudaStream_t s);
 
 cudaError_t fft_setup(FftCtx& ctx, const GridDev& g);
 void fft_release(FftCtx& ctx);

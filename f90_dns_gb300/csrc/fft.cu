@@ -16,6 +16,8 @@
 // real transform as a length-nx/2 complex transform plus a pack/unpack step.
 // Twiddles come from tables built on the host in long double.
 #include <cmath>
+#include <cstdlib>
+#include <vector>
 
 #include "dns3d_internal.cuh"
 
@@ -290,6 +292,24 @@ cudaError_t smem_attr(K k, int bytes) {
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
 }
 
+// round(2^62 e^{-2 pi i t/n}), t < count, from the long double values.
+longlong2* upload_table_q62(int n, int count) {
+    std::vector<longlong2> h(count);
+    const long double pi = 3.141592653589793238462643383279502884L;
+    for (int t = 0; t < count; ++t) {
+        const long double ang = -2.0L * pi * (long double)t / (long double)n;
+        h[t].x = llroundl(ldexpl(cosl(ang), 62));
+        h[t].y = llroundl(ldexpl(sinl(ang), 62));
+    }
+    longlong2* d = nullptr;
+    if (cudaMalloc(&d, sizeof(longlong2) * count) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, h.data(), sizeof(longlong2) * count, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d);
+        return nullptr;
+    }
+    return d;
+}
+
 }  // namespace
 
 cudaError_t fft_setup(FftCtx& ctx, const GridDev& g) {
@@ -304,6 +324,14 @@ cudaError_t fft_setup(FftCtx& ctx, const GridDev& g) {
     ctx.tw32_nx = upload_table<float2>(g.nx, g.nxh + 1);
     if (!ctx.tw_ny || !ctx.tw_nx2 || !ctx.tw_nx || !ctx.tw32_ny || !ctx.tw32_nx2 || !ctx.tw32_nx)
         return cudaErrorMemoryAllocation;
+    const char* f64 = std::getenv("DNS3D_FFT_FP64");
+    ctx.fx = ctx.use_ct && !(f64 && f64[0] == '1');
+    if (ctx.fx) {
+        ctx.twq_ny = upload_table_q62(g.ny, g.ny);
+        ctx.twq_nx2 = upload_table_q62(g.nxh, g.nxh);
+        ctx.twq_nx = upload_table_q62(g.nx, g.nxh + 1);
+        if (!ctx.twq_ny || !ctx.twq_nx2 || !ctx.twq_nx) return cudaErrorMemoryAllocation;
+    }
     const int cx = pick_cx(g.ny);
     const int rx = pick_rx(g.nxh);
     const int sy = 2 * cx * (g.ny + 1) * (int)sizeof(double2);
@@ -324,6 +352,10 @@ void fft_release(FftCtx& ctx) {
     cudaFree(ctx.tw32_ny);
     cudaFree(ctx.tw32_nx2);
     cudaFree(ctx.tw32_nx);
+    cudaFree(ctx.twq_ny);
+    cudaFree(ctx.twq_nx2);
+    cudaFree(ctx.twq_nx);
+    ctx.twq_ny = ctx.twq_nx2 = ctx.twq_nx = nullptr;
     ctx.tw_ny = ctx.tw_nx2 = ctx.tw_nx = nullptr;
     ctx.tw32_ny = ctx.tw32_nx2 = ctx.tw32_nx = nullptr;
 }
@@ -337,6 +369,16 @@ cudaError_t c2r_impl(const FftCtx& ctx, const GridDev& g, FieldsT<typename Cx<T>
                      const typename Cx<T>::type* twx) {
     using C = typename Cx<T>::type;
     const int nrows = nplanes * g.ny;
+    if constexpr (sizeof(T) == 8) {
+        if (ctx.fx) {
+            cudaError_t e = fft_fx_y<+1>(spec, tmp, g, nplanes, g.nxhp, nf, ctx.twq_ny, s);
+            if (e) return e;
+            if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_y_inverse");
+            e = fft_fx_c2r_x(tmp, phys, g, nrows, nf, ctx.twq_nx2, ctx.twq_nx, s);
+            if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_c2r");
+            return e;
+        }
+    }
     if (ctx.use_ct) {
         cudaError_t e = fft_ct_y<+1, C>(spec, tmp, g, nplanes, g.nxhp, nf, twy, s);
         if (e) return e;
@@ -363,6 +405,16 @@ cudaError_t r2c_impl(const FftCtx& ctx, const GridDev& g, FieldsT<T> phys, Field
     using C = typename Cx<T>::type;
     const int nrows = nplanes * g.ny;
     if (ncol <= 0 || ncol > g.nxhp) ncol = g.nxhp;
+    if constexpr (sizeof(T) == 8) {
+        if (ctx.fx) {
+            cudaError_t e = fft_fx_r2c_x(phys, spec, g, nrows, nf, ctx.twq_nx2, ctx.twq_nx, s);
+            if (e) return e;
+            if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_r2c");
+            e = fft_fx_y<-1>(spec, spec, g, nplanes, ncol, nf, ctx.twq_ny, s);
+            if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_y_forward");
+            return e;
+        }
+    }
     if (ctx.use_ct) {
         cudaError_t e = fft_ct_r2c_x<T>(phys, spec, g, nrows, nf, twx2, twx, s);
         if (e) return e;

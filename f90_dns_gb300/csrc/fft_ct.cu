@@ -11,6 +11,8 @@
 //  - the y pass over a flattened (plane, kx) column index, so grids whose
 //    nx/2+1 columns do not fill a CTA waste no lanes.
 // Lengths outside the instantiated set use the generic kernels of fft.cu.
+#include <type_traits>
+
 #include "dns3d_internal.cuh"
 #include "ragged.cuh"
 
@@ -34,6 +36,37 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
 template <int SIGN, typename C> __device__ __forceinline__ C mul_si(C a) {
     return SIGN > 0 ? mk<C>(-a.y, a.x) : mk<C>(a.y, -a.x);
 }
+
+// ------------------------------------------------------------------ 64-bit fixed point
+// The FP64 path's transforms run in block fixed point on the integer pipes:
+// this GPU issues FP64 arithmetic at 1/64 of its FP32 rate, and the FP64
+// plane transforms were bound by it.  One transform (a y column or an x row)
+// is scaled by the power of two that gives its largest input component
+// B <= 53 significant bits (as an FP64 mantissa has), with B small enough
+// that no partial DFT can leave int64 (a length-N DFT grows a modulus at most
+// N-fold); butterflies then add exactly, and every twiddle product is formed
+// exactly in 128 bits and rounded once to the transform's grid.  Twiddles and
+// constants are Q62 integers (value * 2^62).  The result differs from an FP64
+// transform's by the same order as that transform's own rounding error
+// (normwise ~2^-B per rounding step).
+using fx2 = longlong2;
+
+__device__ __forceinline__ long long fx_round62(__int128 v) {
+    return (long long)((v + ((__int128)1 << 61)) >> 62);
+}
+// x c for a Q62 constant c
+__device__ __forceinline__ long long fx_mulq(long long x, long long c) { return fx_round62((__int128)x * c); }
+
+template <> __device__ __forceinline__ fx2 cmul<fx2>(fx2 a, fx2 w) {
+    const __int128 re = (__int128)a.x * w.x - (__int128)a.y * w.y;
+    const __int128 im = (__int128)a.x * w.y + (__int128)a.y * w.x;
+    return mk<fx2>(fx_round62(re), fx_round62(im));
+}
+
+constexpr long long kFxInvSqrt2 = 3260954456333195553LL;  // round(2^62 / sqrt 2)
+constexpr long long kFxSqrt3h = 3993837246235628775LL;    // round(2^62 sqrt(3) / 2)
+
+template <typename C> __host__ __device__ constexpr bool is_fx() { return std::is_same<C, fx2>::value; }
 
 // Register DFTs, natural-order output, w = e^{SIGN 2 pi i / R}.
 template <int SIGN, typename C> __device__ __forceinline__ void dft2(C* v) {
@@ -60,11 +93,18 @@ template <int SIGN, typename C> __device__ __forceinline__ void dft8(C* v) {
     C o[4] = {v[1], v[3], v[5], v[7]};
     dft4<SIGN>(e);
     dft4<SIGN>(o);
-    const R h = (R)0.70710678118654752440;
-    const R s = (R)SIGN;
-    const C t1 = mk<C>(h * (o[1].x - s * o[1].y), h * (o[1].y + s * o[1].x));
+    C t1, t3;
+    if constexpr (is_fx<C>()) {
+        const long long s = SIGN;
+        t1 = mk<C>(fx_mulq(o[1].x - s * o[1].y, kFxInvSqrt2), fx_mulq(o[1].y + s * o[1].x, kFxInvSqrt2));
+        t3 = mk<C>(fx_mulq(-o[3].x - s * o[3].y, kFxInvSqrt2), fx_mulq(-o[3].y + s * o[3].x, kFxInvSqrt2));
+    } else {
+        const R h = (R)0.70710678118654752440;
+        const R s = (R)SIGN;
+        t1 = mk<C>(h * (o[1].x - s * o[1].y), h * (o[1].y + s * o[1].x));
+        t3 = mk<C>(h * (-o[3].x - s * o[3].y), h * (-o[3].y + s * o[3].x));
+    }
     const C t2 = mul_si<SIGN>(o[2]);
-    const C t3 = mk<C>(h * (-o[3].x - s * o[3].y), h * (-o[3].y + s * o[3].x));
     v[0] = cadd(e[0], o[0]);
     v[4] = csub(e[0], o[0]);
     v[1] = cadd(e[1], t1);
@@ -77,11 +117,19 @@ template <int SIGN, typename C> __device__ __forceinline__ void dft8(C* v) {
 
 template <int SIGN, typename C> __device__ __forceinline__ void dft3(C* v) {
     using R = decltype(C::x);
-    const R h = (R)0.86602540378443864676;  // sqrt(3)/2
     const C t1 = cadd(v[1], v[2]);
     const C d = csub(v[1], v[2]);
-    const C m = mk<C>(v[0].x - (R)0.5 * t1.x, v[0].y - (R)0.5 * t1.y);
-    const C id = SIGN > 0 ? mk<C>(-h * d.y, h * d.x) : mk<C>(h * d.y, -h * d.x);
+    C m, id;
+    if constexpr (is_fx<C>()) {
+        // t/2 rounded half up; sqrt(3)/2 as a Q62 constant
+        m = mk<C>(v[0].x - ((t1.x + 1) >> 1), v[0].y - ((t1.y + 1) >> 1));
+        const long long hx = fx_mulq(d.x, kFxSqrt3h), hy = fx_mulq(d.y, kFxSqrt3h);
+        id = SIGN > 0 ? mk<C>(-hy, hx) : mk<C>(hy, -hx);
+    } else {
+        const R h = (R)0.86602540378443864676;  // sqrt(3)/2
+        m = mk<C>(v[0].x - (R)0.5 * t1.x, v[0].y - (R)0.5 * t1.y);
+        id = SIGN > 0 ? mk<C>(-h * d.y, h * d.x) : mk<C>(h * d.y, -h * d.x);
+    }
     v[0] = cadd(v[0], t1);
     v[1] = cadd(m, id);
     v[2] = csub(m, id);
@@ -343,6 +391,279 @@ __global__ void __launch_bounds__(kThreads) k_r2c_x_ct(FieldsT<T> src, FieldsT<t
     r2c_x_body<N, T>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf);
 }
 
+// ------------------------------------------------------------------ fixed-point passes
+// Conversions between FP64 and a transform's fixed-point grid, integer
+// operations only.  A transform whose largest input has biased exponent em
+// (|x| < 2^(em - 1022)) stores x as X = round(x 2^(B - em + 1022)), so that
+// |X| <= 2^B, and an output X stands for X 2^(em - 1022 - B).
+
+// Significant bits of a transform's largest input: 53, less whatever a length
+// n transform (log2 n + 1 bits, the +1 for a complex modulus) and `extra` bits
+// of packing growth need below 2^62.
+__host__ __device__ constexpr int fx_bits(int n, int extra) {
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    return 62 - l - 1 - extra < 53 ? 62 - l - 1 - extra : 53;
+}
+
+__device__ __forceinline__ unsigned fx_expo(double x) { return ((unsigned)__double2hiint(x) >> 20) & 0x7FFu; }
+__device__ __forceinline__ unsigned fx_expo(double2 v) { return max(fx_expo(v.x), fx_expo(v.y)); }
+
+// round(x 2^(B - em + 1022)) given rsb = 53 - B + em (em >= 1, B <= 53): the
+// mantissa m of x = m 2^(ex - 1075) shifted right by rsb - ex >= 0, half up.
+__device__ __forceinline__ long long fx_from(double x, int rsb) {
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    const long long m = (b & 0xFFFFFFFFFFFFFLL) | (ex ? (1LL << 52) : 0LL);
+    const int rs = rsb - max(ex, 1);
+    long long u = 0;
+    if (rs < 63) u = rs == 0 ? m : ((m >> (rs - 1)) + 1) >> 1;
+    return b < 0 ? -u : u;
+}
+
+// X 2^e2 rounded to the nearest FP64 value (ties to even); below the normal
+// range it is a signed zero, above it an infinity.
+__device__ __forceinline__ double fx_to(long long X, int e2) {
+    if (X == 0) return 0.0;
+    const unsigned long long sg = X < 0 ? 0x8000000000000000ULL : 0ULL;
+    const unsigned long long a = X < 0 ? 0ULL - (unsigned long long)X : (unsigned long long)X;
+    const int p = 63 - __clzll((long long)a);  // a in [2^p, 2^(p+1))
+    const int be = p + e2 + 1023;
+    unsigned long long m;
+    if (p > 52) {
+        const int sh = p - 52;
+        m = a >> sh;
+        const unsigned long long rest = a & ((1ULL << sh) - 1ULL), half = 1ULL << (sh - 1);
+        m += (rest > half || (rest == half && (m & 1ULL))) ? 1ULL : 0ULL;
+    } else {
+        m = a << (52 - p);
+    }
+    if (be <= 0) return __longlong_as_double((long long)sg);
+    if (be >= 2047) return __longlong_as_double((long long)(sg | 0x7FF0000000000000ULL));
+    // m in [2^52, 2^53]: the implicit bit (or a rounding carry) adds into the exponent field
+    return __longlong_as_double((long long)(sg | (((unsigned long long)(be - 1) << 52) + m)));
+}
+
+__device__ __forceinline__ double fx_nan() { return __longlong_as_double(0x7FF8000000000000LL); }
+
+// emax[key] = max(emax[key], e) over the calling warp's lanes, one shared
+// atomic per distinct key.  Every lane of the warp must call it.
+__device__ __forceinline__ void fx_key_max(unsigned* emax, int key, unsigned e) {
+    const unsigned grp = __match_any_sync(0xFFFFFFFFu, key);
+    e = __reduce_max_sync(grp, e);
+    if ((threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&emax[key], e);
+}
+
+// y pass in fixed point (FP64 fields); emax holds per_cta(N) exponents.
+template <int N, int SIGN>
+__device__ __forceinline__ void fft_y_body_fx(const Fields& src, const Fields& dst, const GridDev& g, int nplanes,
+                                              int ncol, const fx2* __restrict__ tw, int bx, int f, fx2* buf,
+                                              unsigned* emax) {
+    constexpr int CX = per_cta(N);
+    constexpr int LD = N + 1;
+    constexpr int B = fx_bits(N, 0);
+    const long long ncols = (long long)nplanes * ncol;
+    const long long vc = (long long)bx * CX + (threadIdx.x % CX);
+    const bool live = vc < ncols;
+    size_t base = 0;
+    if (live) {
+        const int p = (int)(vc / ncol);
+        const int kx = (int)(vc - (long long)p * ncol);
+        base = (size_t)p * g.nm + kx;
+    }
+    const double2* __restrict__ s = field_ptr(src, f);
+    double2* d = field_ptr(dst, f);
+    constexpr int ROWS_PER_ITER = kThreads / CX;
+    constexpr int ITERS = N / ROWS_PER_ITER;
+    static_assert(N % ROWS_PER_ITER == 0, "rows split evenly over the threads");
+    const int c = threadIdx.x % CX, y0 = threadIdx.x / CX;
+    if (threadIdx.x < CX) emax[threadIdx.x] = 1u;
+    double2 v[ITERS];
+    unsigned e = 1u;
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        v[it] = live ? s[base + (size_t)(y0 + it * ROWS_PER_ITER) * g.nxhp] : make_double2(0.0, 0.0);
+        e = max(e, fx_expo(v[it]));
+    }
+    __syncthreads();
+    fx_key_max(emax, c, e);
+    __syncthreads();
+    const int em = (int)emax[c];
+    const int rsb = 53 - B + em;
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it)
+        buf[c * LD + y0 + it * ROWS_PER_ITER] = mk<fx2>(fx_from(v[it].x, rsb), fx_from(v[it].y, rsb));
+    __syncthreads();
+    ct_fft<N, 1, SIGN, CX, LD>(buf, tw);
+    if (live) {
+        const int e2 = em - 1022 - B;
+#pragma unroll
+        for (int it = 0; it < ITERS; ++it) {
+            const fx2 z = buf[c * LD + y0 + it * ROWS_PER_ITER];
+            d[base + (size_t)(y0 + it * ROWS_PER_ITER) * g.nxhp] =
+                em == 0x7FF ? make_double2(fx_nan(), fx_nan()) : make_double2(fx_to(z.x, e2), fx_to(z.y, e2));
+        }
+    }
+}
+
+template <int N, int SIGN>
+__global__ void __launch_bounds__(kThreads) k_fft_y_fx(Fields src, Fields dst, GridDev g, int nplanes, int ncol,
+                                                       const fx2* __restrict__ tw) {
+    __shared__ fx2 buf[per_cta(N) * (N + 1)];
+    __shared__ unsigned emax[per_cta(N)];
+    fft_y_body_fx<N, SIGN>(src, dst, g, nplanes, ncol, tw, blockIdx.x, blockIdx.z, buf, emax);
+}
+
+// c2r along x in fixed point: the packing of c2r_x_body (inputs of one row
+// scaled together, the packing's growth of 4 within the headroom), the
+// inverse transform, and the 1/(nx ny) scaling as an exact multiple of the
+// FP64 constant's mantissa rounded once.
+template <int N>
+__device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& dst, const GridDev& g, int nrows,
+                                              const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx, int bx,
+                                              int f, fx2* buf, unsigned* emax) {
+    constexpr int RX = per_cta(N);
+    constexpr int LD = N + 1;
+    constexpr int B = fx_bits(N, 2);
+    const int row0 = bx * RX;
+    const double2* __restrict__ s = field_ptr(src, f);
+    double2* d = reinterpret_cast<double2*>(field_ptr(dst, f));
+    const int nxhp = N + 1;
+    constexpr int ITERS = RX * N / kThreads;
+    static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
+    if (threadIdx.x < RX) emax[threadIdx.x] = 1u;
+    double2 xa[ITERS], xb[ITERS];
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        const int r = t / N, k = t - r * N;
+        xa[it] = xb[it] = make_double2(0.0, 0.0);
+        if (row0 + r < nrows) {
+            const double2* row = s + (size_t)(row0 + r) * nxhp;
+            xa[it] = row[k];
+            xb[it] = row[N - k];
+        }
+        if (k == 0) {  // Im of kx = 0 and kx = nx/2 is ignored
+            xa[it].y = 0.0;
+            xb[it].y = 0.0;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        fx_key_max(emax, t / N, max(fx_expo(xa[it]), fx_expo(xb[it])));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        const int r = t / N, k = t - r * N;
+        const int rsb = 53 - B + (int)emax[r];
+        const fx2 a = mk<fx2>(fx_from(xa[it].x, rsb), fx_from(xa[it].y, rsb));
+        const fx2 b = mk<fx2>(fx_from(xb[it].x, rsb), fx_from(xb[it].y, rsb));
+        const fx2 sm = mk<fx2>(a.x + b.x, a.y - b.y);
+        const fx2 df = mk<fx2>(a.x - b.x, a.y + b.y);
+        fx2 w = __ldg(&tw_nx[k]);
+        w.y = -w.y;
+        const fx2 p = cmul(w, df);
+        buf[r * LD + k] = mk<fx2>(sm.x - p.y, sm.y + p.x);
+    }
+    __syncthreads();
+    ct_fft<N, 1, +1, RX, LD>(buf, tw_n);
+    // 1/(nx ny) = M 2^(E - 1075), M its 53-bit mantissa: Y = round(Z M / 2^52)
+    const long long sb = __double_as_longlong(g.inv_nxny);
+    const long long M = (sb & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+    const int E = (int)((sb >> 52) & 0x7FF);
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        const int r = t / N, k = t - r * N;
+        if (row0 + r < nrows) {
+            const int em = (int)emax[r];
+            const int e2 = em + E - 2045 - B;
+            const fx2 z = buf[r * LD + k];
+            const long long yx = (long long)(((__int128)z.x * M + ((__int128)1 << 51)) >> 52);
+            const long long yy = (long long)(((__int128)z.y * M + ((__int128)1 << 51)) >> 52);
+            d[(size_t)(row0 + r) * N + k] =
+                em == 0x7FF ? make_double2(fx_nan(), fx_nan()) : make_double2(fx_to(yx, e2), fx_to(yy, e2));
+        }
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_c2r_x_fx(Fields src, RFields dst, GridDev g, int nrows,
+                                                       const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx) {
+    __shared__ fx2 buf[per_cta(N) * (N + 1)];
+    __shared__ unsigned emax[per_cta(N)];
+    c2r_x_body_fx<N>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax);
+}
+
+// r2c along x in fixed point: z[m] = x[2m] + i x[2m+1] of one row scaled
+// together, forward transform, and 2 X[k] = (Z[k] + conj Z[N-k]) +
+// e^{-2 pi i k/nx} (-i)(Z[k] - conj Z[N-k]) formed exactly, the factor 1/2
+// taken into the exponent.
+template <int N>
+__device__ __forceinline__ void r2c_x_body_fx(const RFields& src, const Fields& dst, const GridDev& g, int nrows,
+                                              const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx, int bx,
+                                              int f, fx2* buf, unsigned* emax) {
+    constexpr int RX = per_cta(N);
+    constexpr int LD = N + 1;
+    constexpr int B = fx_bits(N, 2);
+    const int row0 = bx * RX;
+    const double2* __restrict__ s = reinterpret_cast<const double2*>(field_ptr(src, f));
+    double2* d = field_ptr(dst, f);
+    constexpr int ITERS = RX * N / kThreads;
+    static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
+    if (threadIdx.x < RX) emax[threadIdx.x] = 1u;
+    double2 v[ITERS];
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        const int r = t / N, k = t - r * N;
+        v[it] = (row0 + r < nrows) ? s[(size_t)(row0 + r) * N + k] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        fx_key_max(emax, t / N, fx_expo(v[it]));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        const int r = t / N, k = t - r * N;
+        const int rsb = 53 - B + (int)emax[r];
+        buf[r * LD + k] = mk<fx2>(fx_from(v[it].x, rsb), fx_from(v[it].y, rsb));
+    }
+    __syncthreads();
+    ct_fft<N, 1, -1, RX, LD>(buf, tw_n);
+    for (int t = threadIdx.x; t < RX * (N + 1); t += kThreads) {
+        const int r = t / (N + 1), k = t - r * (N + 1);
+        if (row0 + r < nrows) {
+            const fx2 za = buf[r * LD + (k == N ? 0 : k)];
+            const fx2 zb = buf[r * LD + (k == 0 ? 0 : N - k)];
+            const fx2 e = mk<fx2>(za.x + zb.x, za.y - zb.y);
+            const fx2 o = mk<fx2>(za.y + zb.y, zb.x - za.x);
+            const fx2 p = cmul(__ldg(&tw_nx[k]), o);
+            const int em = (int)emax[r];
+            const int e2 = em - 1023 - B;
+            d[(size_t)(row0 + r) * (N + 1) + k] = em == 0x7FF
+                                                      ? make_double2(fx_nan(), fx_nan())
+                                                      : make_double2(fx_to(e.x + p.x, e2), fx_to(e.y + p.y, e2));
+        }
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_r2c_x_fx(RFields src, Fields dst, GridDev g, int nrows,
+                                                       const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx) {
+    __shared__ fx2 buf[per_cta(N) * (N + 1)];
+    __shared__ unsigned emax[per_cta(N)];
+    r2c_x_body_fx<N>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax);
+}
+
 // ------------------------------------------------------------------ ragged stages
 // The four transform passes of the nonlinear term over many runs in one launch
 // (k_stage, ragged.cuh): the transform length is a run property, so each CTA
@@ -435,11 +756,84 @@ struct RsR2C {
     }
 };
 
+// The same passes of FP64 runs in fixed point (RunDesc twiddles: Q62 tables).
+template <int SIGN>
+struct RsFftYFx {
+    static constexpr int kMinCtas = 3;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        __shared__ fx2 buf[ct_buf_max()];
+        __shared__ unsigned emax[64];
+        const int gx = d.gx[SIGN > 0 ? kRsFftYInv : kRsFftYFwd];
+        const int f = b / gx, bx = b - f * gx;
+        const Fields src = one_field<double2>(SIGN > 0 ? d.spec : d.src, f);
+        const Fields dst = one_field<double2>(SIGN > 0 ? d.tmp : d.src, f);
+        const int ncol = SIGN > 0 ? d.g.nxhp : d.ncol;
+        const fx2* tw = static_cast<const fx2*>(d.tw_ny);
+        switch (d.g.ny) {
+#define Y_CASE(n) \
+    case n: fft_y_body_fx<n, SIGN>(src, dst, d.g, d.g.nz, ncol, tw, bx, 0, buf, emax); break;
+            DNS3D_CT_Y_LENGTHS(Y_CASE)
+#undef Y_CASE
+        }
+    }
+};
+
+struct RsC2RFx {
+    static constexpr int kMinCtas = 2;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        __shared__ fx2 buf[ct_buf_max()];
+        __shared__ unsigned emax[64];
+        const int gx = d.gx[kRsFftC2R];
+        const int f = b / gx, bx = b - f * gx;
+        const fx2* twn = static_cast<const fx2*>(d.tw_nx2);
+        const fx2* twx = static_cast<const fx2*>(d.tw_nx);
+        switch (d.g.nxh) {
+#define X_CASE(n)                                                                                               \
+    case n:                                                                                                     \
+        c2r_x_body_fx<n>(one_field<double2>(d.tmp, f), one_field<double>(d.phys, f), d.g, d.g.nz * d.g.ny, twn, \
+                         twx, bx, 0, buf, emax);                                                                \
+        break;
+            DNS3D_CT_X_LENGTHS(X_CASE)
+#undef X_CASE
+        }
+    }
+};
+
+struct RsR2CFx {
+    static constexpr int kMinCtas = 3;
+    static __device__ __forceinline__ void run(const RunDesc& d, int b) {
+        __shared__ fx2 buf[ct_buf_max()];
+        __shared__ unsigned emax[64];
+        const int gx = d.gx[kRsFftR2C];
+        const int f = b / gx, bx = b - f * gx;
+        const fx2* twn = static_cast<const fx2*>(d.tw_nx2);
+        const fx2* twx = static_cast<const fx2*>(d.tw_nx);
+        switch (d.g.nxh) {
+#define X_CASE(n)                                                                                              \
+    case n:                                                                                                    \
+        r2c_x_body_fx<n>(one_field<double>(d.phys, f), one_field<double2>(d.src, f), d.g, d.g.nz * d.g.ny, twn, \
+                         twx, bx, 0, buf, emax);                                                               \
+        break;
+            DNS3D_CT_X_LENGTHS(X_CASE)
+#undef X_CASE
+        }
+    }
+};
+
 }  // namespace
 
 int fft_ct_per_cta(int n) { return per_cta(n); }
 
-StageKernel ragged_fft_kernel(int stage, bool mixed) {
+StageKernel ragged_fft_kernel(int stage, bool mixed, bool fx) {
+    if (!mixed && fx) {
+        switch (stage) {
+            case kRsFftYInv: return k_stage<RsFftYFx<+1>>;
+            case kRsFftC2R: return k_stage<RsC2RFx>;
+            case kRsFftR2C: return k_stage<RsR2CFx>;
+            case kRsFftYFwd: return k_stage<RsFftYFx<-1>>;
+        }
+        return nullptr;
+    }
     switch (stage) {
         case kRsFftYInv: return mixed ? k_stage<RsFftY<+1, float>> : k_stage<RsFftY<+1, double>>;
         case kRsFftC2R: return mixed ? k_stage<RsC2R<float>> : k_stage<RsC2R<double>>;
@@ -474,6 +868,31 @@ void launch_r2c(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, const GridDev
     constexpr int RX = per_cta(N);
     dim3 grid((nrows + RX - 1) / RX, nf);
     k_r2c_x_ct<N, T><<<grid, kThreads, 0, s>>>(src, dst, g, nrows, tw_n, tw_nx);
+}
+
+template <int SIGN, int N>
+void launch_y_fx(Fields src, Fields dst, const GridDev& g, int nplanes, int ncol, int nf, const fx2* tw,
+                 cudaStream_t s) {
+    constexpr int CX = per_cta(N);
+    const long long ncols = (long long)nplanes * ncol;
+    dim3 grid((unsigned)((ncols + CX - 1) / CX), 1, nf);
+    k_fft_y_fx<N, SIGN><<<grid, kThreads, 0, s>>>(src, dst, g, nplanes, ncol, tw);
+}
+
+template <int N>
+void launch_c2r_fx(Fields src, RFields dst, const GridDev& g, int nrows, int nf, const fx2* tw_n, const fx2* tw_nx,
+                   cudaStream_t s) {
+    constexpr int RX = per_cta(N);
+    dim3 grid((nrows + RX - 1) / RX, nf);
+    k_c2r_x_fx<N><<<grid, kThreads, 0, s>>>(src, dst, g, nrows, tw_n, tw_nx);
+}
+
+template <int N>
+void launch_r2c_fx(RFields src, Fields dst, const GridDev& g, int nrows, int nf, const fx2* tw_n, const fx2* tw_nx,
+                   cudaStream_t s) {
+    constexpr int RX = per_cta(N);
+    dim3 grid((nrows + RX - 1) / RX, nf);
+    k_r2c_x_fx<N><<<grid, kThreads, 0, s>>>(src, dst, g, nrows, tw_n, tw_nx);
 }
 
 }  // namespace
@@ -529,6 +948,47 @@ cudaError_t fft_ct_r2c_x(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, cons
     }
     return cudaGetLastError();
 }
+
+template <int SIGN>
+cudaError_t fft_fx_y(Fields src, Fields dst, const GridDev& g, int nplanes, int ncol, int nf, const longlong2* tw,
+                     cudaStream_t s) {
+    if (ncol < 1 || ncol > g.nxhp) return cudaErrorInvalidValue;
+    switch (g.ny) {
+#define Y_CASE(n) \
+    case n: launch_y_fx<SIGN, n>(src, dst, g, nplanes, ncol, nf, tw, s); break;
+        DNS3D_CT_Y_LENGTHS(Y_CASE)
+#undef Y_CASE
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t fft_fx_c2r_x(Fields src, RFields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
+                         const longlong2* tw_nx, cudaStream_t s) {
+    switch (g.nxh) {
+#define X_CASE(n) \
+    case n: launch_c2r_fx<n>(src, dst, g, nrows, nf, tw_n, tw_nx, s); break;
+        DNS3D_CT_X_LENGTHS(X_CASE)
+#undef X_CASE
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t fft_fx_r2c_x(RFields src, Fields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
+                         const longlong2* tw_nx, cudaStream_t s) {
+    switch (g.nxh) {
+#define X_CASE(n) \
+    case n: launch_r2c_fx<n>(src, dst, g, nrows, nf, tw_n, tw_nx, s); break;
+        DNS3D_CT_X_LENGTHS(X_CASE)
+#undef X_CASE
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template cudaError_t fft_fx_y<-1>(Fields, Fields, const GridDev&, int, int, int, const longlong2*, cudaStream_t);
+template cudaError_t fft_fx_y<+1>(Fields, Fields, const GridDev&, int, int, int, const longlong2*, cudaStream_t);
 
 template cudaError_t fft_ct_y<-1, double2>(Fields, Fields, const GridDev&, int, int, int, const double2*,
                                          cudaStream_t);

@@ -64,6 +64,7 @@ struct RunDesc {
     int gx[kRsStages];       // virtual blocks per field of each stage (transforms, elementwise passes);
                              // kRsVisc: operator indices per CTA of the tensor-core viscous body
     int tcmask;              // z-derivatives on the tensor cores: 1 vorticity, 2 projection, 4 pressure
+    int fftfx;               // FP64 transforms in fixed point (twiddles: the Q62 tables)
     int vort_chunk, corr_chunk;  // mode tiles per CTA of those bodies
 };
 
@@ -114,12 +115,12 @@ static_assert(sizeof(RunDesc) % 8 == 0, "descriptor copied in 8-byte words");
 using StageKernel = void (*)(const RunDesc*, StageMap);
 
 // Kernel variants of FP64 runs: which stages run their tensor-core bodies.
-enum RaggedVariant { kRvVortTc = 1, kRvCorrTc = 2, kRvViscTc = 4, kRvPresTc = 8 };
+enum RaggedVariant { kRvVortTc = 1, kRvCorrTc = 2, kRvViscTc = 4, kRvPresTc = 8, kRvFftFx = 16 };
 int ragged_variant(const RunDesc& d);
 // The k_stage instantiation of a stage for FP64 (mixed = false, with the
 // variant) or mixed runs (step.cu; the transform passes come from fft_ct.cu).
 StageKernel ragged_kernel(int stage, bool mixed, int variant);
-StageKernel ragged_fft_kernel(int stage, bool mixed);
+StageKernel ragged_fft_kernel(int stage, bool mixed, bool fx);
 // CTA columns (y pass) or rows (x passes) of the compile-time transform of length n.
 int fft_ct_per_cta(int n);
 // Fills d.gx for the run's grid (d.g, d.ncol set).

@@ -2882,7 +2882,7 @@ StageKernel ragged_kernel(int stage, bool mixed, int variant) {
         case kRsFftYInv:
         case kRsFftC2R:
         case kRsFftR2C:
-        case kRsFftYFwd: return ragged_fft_kernel(stage, mixed);
+        case kRsFftYFwd: return ragged_fft_kernel(stage, mixed, (variant & kRvFftFx) != 0);
     }
     return nullptr;
 }
@@ -2890,7 +2890,7 @@ StageKernel ragged_kernel(int stage, bool mixed, int variant) {
 int ragged_variant(const RunDesc& d) {
     return ((d.tcmask & 1) ? kRvVortTc : 0) | ((d.tcmask & 2) ? kRvCorrTc : 0) |
            ((d.tcmask & 4) && !d.sp.weak_form ? kRvPresTc : 0) |
-           ((d.ops.tcA && d.sp.cn_identity) ? kRvViscTc : 0);
+           ((d.ops.tcA && d.sp.cn_identity) ? kRvViscTc : 0) | (d.fftfx ? kRvFftFx : 0);
 }
 
 void ragged_geometry(RunDesc& d) {
