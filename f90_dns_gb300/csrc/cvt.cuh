@@ -39,4 +39,29 @@ __device__ __forceinline__ double f2d(float v) {
 
 __device__ __forceinline__ float2 d2f(double2 a) { return make_float2(d2f(a.x), d2f(a.y)); }
 
+// X 2^e2 for a 64-bit integer X, rounded to the nearest FP64 value (ties to
+// even), from the integer's bits: the same value as the hardware int64 -> FP64
+// conversion followed by an exact power-of-two scaling, which both issue on
+// the FP64 pipe.  Results below the normal range take that hardware path.
+__device__ __forceinline__ double i2d_scaled(long long X, int e2) {
+    if (X == 0) return 0.0;
+    const unsigned long long sg = X < 0 ? 0x8000000000000000ULL : 0ULL;
+    const unsigned long long a = X < 0 ? 0ULL - (unsigned long long)X : (unsigned long long)X;
+    const int p = 63 - __clzll((long long)a);  // a in [2^p, 2^(p+1))
+    const int be = p + e2 + 1023;
+    if (be <= 0) return ldexp(__ll2double_rn(X), e2);
+    unsigned long long m;
+    if (p > 52) {
+        const int sh = p - 52;
+        m = a >> sh;
+        const unsigned long long rest = a & ((1ULL << sh) - 1ULL), half = 1ULL << (sh - 1);
+        m += (rest > half || (rest == half && (m & 1ULL))) ? 1ULL : 0ULL;
+    } else {
+        m = a << (52 - p);
+    }
+    if (be >= 2047) return __longlong_as_double((long long)(sg | 0x7FF0000000000000ULL));
+    // m in [2^52, 2^53]: the implicit bit (or a rounding carry) adds into the exponent field
+    return __longlong_as_double((long long)(sg | (((unsigned long long)(be - 1) << 52) + m)));
+}
+
 }  // namespace dns3d

@@ -13,6 +13,7 @@
 // Lengths outside the instantiated set use the generic kernels of fft.cu.
 #include <type_traits>
 
+#include "cvt.cuh"
 #include "dns3d_internal.cuh"
 #include "ragged.cuh"
 
@@ -421,28 +422,7 @@ __device__ __forceinline__ long long fx_from(double x, int rsb) {
     return b < 0 ? -u : u;
 }
 
-// X 2^e2 rounded to the nearest FP64 value (ties to even); below the normal
-// range it is a signed zero, above it an infinity.
-__device__ __forceinline__ double fx_to(long long X, int e2) {
-    if (X == 0) return 0.0;
-    const unsigned long long sg = X < 0 ? 0x8000000000000000ULL : 0ULL;
-    const unsigned long long a = X < 0 ? 0ULL - (unsigned long long)X : (unsigned long long)X;
-    const int p = 63 - __clzll((long long)a);  // a in [2^p, 2^(p+1))
-    const int be = p + e2 + 1023;
-    unsigned long long m;
-    if (p > 52) {
-        const int sh = p - 52;
-        m = a >> sh;
-        const unsigned long long rest = a & ((1ULL << sh) - 1ULL), half = 1ULL << (sh - 1);
-        m += (rest > half || (rest == half && (m & 1ULL))) ? 1ULL : 0ULL;
-    } else {
-        m = a << (52 - p);
-    }
-    if (be <= 0) return __longlong_as_double((long long)sg);
-    if (be >= 2047) return __longlong_as_double((long long)(sg | 0x7FF0000000000000ULL));
-    // m in [2^52, 2^53]: the implicit bit (or a rounding carry) adds into the exponent field
-    return __longlong_as_double((long long)(sg | (((unsigned long long)(be - 1) << 52) + m)));
-}
+__device__ __forceinline__ double fx_to(long long X, int e2) { return i2d_scaled(X, e2); }
 
 __device__ __forceinline__ double fx_nan() { return __longlong_as_double(0x7FF8000000000000LL); }
 
@@ -532,42 +512,53 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
     constexpr int ITERS = RX * N / kThreads;
     static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
     if (threadIdx.x < RX) emax[threadIdx.x] = 1u;
-    double2 xa[ITERS], xb[ITERS];
+    // the row's nx/2+1 inputs go to shared memory as they are (FP64 bits in
+    // the fixed-point slots; slot N holds kx = nx/2), so no thread holds them
+    // in registers across the exponent reduction
+    unsigned e[ITERS];
 #pragma unroll
     for (int it = 0; it < ITERS; ++it) {
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
-        xa[it] = xb[it] = make_double2(0.0, 0.0);
+        double2 a = make_double2(0.0, 0.0), b = a;
         if (row0 + r < nrows) {
             const double2* row = s + (size_t)(row0 + r) * nxhp;
-            xa[it] = row[k];
-            xb[it] = row[N - k];
+            a = row[k];
+            if (k == 0) b = row[N];
         }
         if (k == 0) {  // Im of kx = 0 and kx = nx/2 is ignored
-            xa[it].y = 0.0;
-            xb[it].y = 0.0;
+            a.y = 0.0;
+            b.y = 0.0;
+            buf[r * LD + N] = mk<fx2>(__double_as_longlong(b.x), __double_as_longlong(b.y));
         }
+        buf[r * LD + k] = mk<fx2>(__double_as_longlong(a.x), __double_as_longlong(a.y));
+        e[it] = max(fx_expo(a), fx_expo(b));
     }
     __syncthreads();
 #pragma unroll
-    for (int it = 0; it < ITERS; ++it) {
-        const int t = threadIdx.x + it * kThreads;
-        fx_key_max(emax, t / N, max(fx_expo(xa[it]), fx_expo(xb[it])));
-    }
+    for (int it = 0; it < ITERS; ++it) fx_key_max(emax, (threadIdx.x + it * kThreads) / N, e[it]);
     __syncthreads();
+    fx2 z[ITERS];
 #pragma unroll
     for (int it = 0; it < ITERS; ++it) {
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
         const int rsb = 53 - B + (int)emax[r];
-        const fx2 a = mk<fx2>(fx_from(xa[it].x, rsb), fx_from(xa[it].y, rsb));
-        const fx2 b = mk<fx2>(fx_from(xb[it].x, rsb), fx_from(xb[it].y, rsb));
+        const fx2 ra = buf[r * LD + k], rb = buf[r * LD + N - k];
+        const fx2 a = mk<fx2>(fx_from(__longlong_as_double(ra.x), rsb), fx_from(__longlong_as_double(ra.y), rsb));
+        const fx2 b = mk<fx2>(fx_from(__longlong_as_double(rb.x), rsb), fx_from(__longlong_as_double(rb.y), rsb));
         const fx2 sm = mk<fx2>(a.x + b.x, a.y - b.y);
         const fx2 df = mk<fx2>(a.x - b.x, a.y + b.y);
         fx2 w = __ldg(&tw_nx[k]);
         w.y = -w.y;
         const fx2 p = cmul(w, df);
-        buf[r * LD + k] = mk<fx2>(sm.x - p.y, sm.y + p.x);
+        z[it] = mk<fx2>(sm.x - p.y, sm.y + p.x);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITERS; ++it) {
+        const int t = threadIdx.x + it * kThreads;
+        buf[(t / N) * LD + t % N] = z[it];
     }
     __syncthreads();
     ct_fft<N, 1, +1, RX, LD>(buf, tw_n);
@@ -592,7 +583,7 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
 }
 
 template <int N>
-__global__ void __launch_bounds__(kThreads) k_c2r_x_fx(Fields src, RFields dst, GridDev g, int nrows,
+__global__ void __launch_bounds__(kThreads, 3) k_c2r_x_fx(Fields src, RFields dst, GridDev g, int nrows,
                                                        const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx) {
     __shared__ fx2 buf[per_cta(N) * (N + 1)];
     __shared__ unsigned emax[per_cta(N)];
@@ -779,7 +770,7 @@ struct RsFftYFx {
 };
 
 struct RsC2RFx {
-    static constexpr int kMinCtas = 2;
+    static constexpr int kMinCtas = 3;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
         __shared__ fx2 buf[ct_buf_max()];
         __shared__ unsigned emax[64];

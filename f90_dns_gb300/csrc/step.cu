@@ -705,7 +705,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
 #pragma unroll
                     for (int j = 0; j < 6; ++j) {
                         const int col = 6 * half + j;
-                        sR[col * m8 + row] = __ll2double_rn(T[j]) * tc_pow2(e + sF[col] - 52);
+                        sR[col * m8 + row] = i2d_scaled(T[j], e + sF[col] - 52);
                     }
                 }
             }
@@ -924,7 +924,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
 #pragma unroll
                         for (int j = 0; j < 8; ++j) {
                             const int col = 8 * cb + j;
-                            sR[col * m8 + row] = __ll2double_rn(T[j]) * tc_pow2(e + sF[col] - 52);
+                            sR[col * m8 + row] = i2d_scaled(T[j], e + sF[col] - 52);
                         }
                     }
                 }
@@ -2387,7 +2387,8 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
 namespace {
 // d2f / f2d (cvt.cuh) against the hardware conversions on n doubles spread
 // over the normal float range (SplitMix64 bits: sign, exponent in
-// [-126, 127], all mantissas), and on every float of a strided sweep for f2d.
+// [-126, 127], all mantissas), and on every float of a strided sweep for f2d;
+// i2d_scaled against the hardware int64 -> FP64 conversion and ldexp.
 __global__ void k_cvt_check(long long n, unsigned long long seed, unsigned long long* bad) {
     unsigned long long nb = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -2400,6 +2401,10 @@ __global__ void k_cvt_check(long long n, unsigned long long seed, unsigned long 
         if (__float_as_uint(d2f(x)) != __float_as_uint(__double2float_rn(x))) ++nb;
         const float v = __uint_as_float((unsigned)(z >> 32));
         if (isfinite(v) && __double_as_longlong(f2d(v)) != __double_as_longlong((double)v)) ++nb;
+        // i2d_scaled: integers of every bit length, scalings into and out of the normal range
+        const long long X = (long long)(z * 0xD1B54A32D192ED03ULL) >> (int)(z & 63);
+        const int e2 = (int)((z >> 8) % 2200) - 1150;
+        if (__double_as_longlong(i2d_scaled(X, e2)) != __double_as_longlong(ldexp(__ll2double_rn(X), e2))) ++nb;
     }
     if (nb) atomicAdd(bad, nb);
 }

@@ -103,12 +103,6 @@ __device__ __forceinline__ int tc_exponent(unsigned long long absbits) {
 // Exact FP32 integer (|v| < 2^22) to int.
 __device__ __forceinline__ int tc_f2i(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
 
-// 2^e as a double (the few exponents outside the normal range via ldexp).
-__device__ __forceinline__ double tc_pow2(int e) {
-    if (e > -1023 && e < 1024) return __longlong_as_double((long long)(e + 1023) << 52);
-    return ldexp(1.0, e);
-}
-
 __device__ __forceinline__ uint32_t tc_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {

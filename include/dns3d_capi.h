@@ -198,9 +198,12 @@ int dns3d_launches_per_step(dns3d_handle* h, int* n);
 /* Dense FP64 FMA throughput of `device` in TFLOP/s (FMA = 2 flops), timed with
  * CUDA events: the peak that bounds the FP64 kernels. */
 int dns3d_measure_fp64_tflops(int device, double* tflops);
-/* Self-check of the library's integer-pipe FP64<->FP32 conversions (used by
- * the mixed-precision kernels) against the hardware conversions on n
- * pseudo-random values of the normal float range: *mismatches = 0 expected. */
+/* Self-check of the library's integer-pipe conversions against the hardware
+ * ones on n pseudo-random values: FP64<->FP32 (the mixed-precision kernels)
+ * over the normal float range, and int64 -> FP64 with a power-of-two scaling
+ * (the fixed-point transforms and the tensor-core epilogues) over every
+ * integer bit length and scalings into and out of the FP64 range:
+ * *mismatches = 0 expected. */
 int dns3d_check_conversions(int device, long long n, unsigned long long* mismatches);
 
 /* Flow statistics without any device allocation.  No counterpart in the

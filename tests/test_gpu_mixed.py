@@ -70,9 +70,11 @@ def test_mixed_error_stays_bounded_over_long_run(built_lib):
 
 
 def test_integer_pipe_conversions_match_hardware(built_lib):
-    """The mixed kernels' FP64<->FP32 conversions (integer operations on the
-    bits, IEEE 754 round to nearest even) give the hardware conversion's bits
-    on 2^24 random values of the normal float range."""
+    """The integer-pipe conversions (integer operations on the bits, IEEE 754
+    round to nearest even) give the hardware conversions' bits: FP64<->FP32 of
+    the mixed kernels on 2^24 random values of the normal float range, and the
+    scaled int64 -> FP64 of the fixed-point transforms and tensor-core
+    epilogues on 2^24 random integers and scalings."""
     import ctypes as C
     from f90_dns_gb300.capi import load_library
     bad = C.c_ulonglong(1)
