@@ -392,20 +392,27 @@ def run_ours(args) -> None:
         bufs = {k: pin() for k in ("u", "v", "w", "p_total")}
         for k in bufs:
             bufs[k][...] = st[k]
+        step0 = d.get_clock()[0]
+        ndiv = 0
         _barrier(dist)
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
+        for i in range(1, args.e2e_steps + 1):
             d.set_state(u=bufs["u"], v=bufs["v"], w=bufs["w"], p_total=bufs["p_total"])
             d.step(1)
             d.get_state_into(bufs["u"], bufs["v"], bufs["w"], bufs["p_total"])
-            diag = d.diagnostics()
+            diag = d.output_diagnostics_3d()
+            if (step0 + i) % 50 == 0:  # check_divergence_3d on the reference's schedule (3D:341-344)
+                d.check_divergence_3d()
+                ndiv += 1
         _barrier(dist)
         el = _max_over_ranks(dist, time.perf_counter() - t0)
         n = pts * 8
         e2e = {"value": ws * pts * args.e2e_steps / el, "unit": "point-steps/s",
-               "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n + 80,
-               "steps": args.e2e_steps,
-               "path": "dns3d_set_state(u,v,w,p_total) + dns3d_step(1) + dns3d_get_state + dns3d_diagnostics"}
+               "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n + 8 * (16 + 6 * wl["nz"]),
+               "steps": args.e2e_steps, "divergence_checks": ndiv,
+               "path": "dns3d_set_state(u,v,w,p_total) from pinned host buffers + dns3d_step(1) + "
+                       "dns3d_get_state into them + dns3d_output_diagnostics every step, dns3d_check_divergence "
+                       "every 50th step (the reference loop with nwrt = 1, 3D:329-344)"}
         del diag
 
     cpu = None

@@ -51,6 +51,7 @@ struct dns3d_handle {
     dns3d_pi_state* d_pi = nullptr;
     double* d_red = nullptr;
     double* d_out = nullptr;
+    double* h_out = nullptr;  // pinned host copy of d_out (the diagnostics' one read-back)
     int* d_flag = nullptr;
     int* d_tcerr = nullptr;  // [2]: set when a tensor-core completion wait ran out
     // viscous solve on the tensor cores (ops.tcA built): chosen by the tile
@@ -79,6 +80,9 @@ struct dns3d_handle {
     // current state, left by get_state or diagnostics.  Everything that changes
     // the state or reuses phys[] as scratch clears it.
     unsigned phys_valid = 0;
+    // set_state / get_state read and write pinned host buffers in place from
+    // the transform kernels (DNS3D_ZERO_COPY=0 turns this off)
+    bool zero_copy = true;
 };
 
 namespace {
@@ -317,6 +321,21 @@ void fold_symmetric(const std::vector<double>& A, int n, std::vector<double>& Ae
     }
 }
 
+// The device address of host memory that kernels can read and write in
+// place: pinned memory (cudaHostAlloc, cudaHostRegister), which the unified
+// address space maps for the device -- on this machine over NVLink-C2C.
+// Null for pageable memory, which goes through copies.
+double* device_view(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return static_cast<double*>(a.devicePointer);
+}
+
 int upload(dns3d_handle* h, void* dst, const void* src, size_t bytes) {
     CK(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
     return DNS3D_OK;
@@ -536,6 +555,8 @@ void release(dns3d_handle* h) {
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     fft_release(h->fft);
+    if (h->h_out) cudaFreeHost(h->h_out);
+    h->h_out = nullptr;
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -956,6 +977,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     h->red_blocks = 152 * 4;
     if ((rc = dev_alloc(h, &h->d_red, (size_t)4 * h->red_blocks))) return fail(rc);
     if ((rc = dev_alloc(h, &h->d_out, 16 + 6 * (size_t)c.nz))) return fail(rc);
+    if (cudaMallocHost(&h->h_out, (16 + 6 * (size_t)c.nz) * sizeof(double)) != cudaSuccess) return fail(DNS3D_E_OOM);
     if ((rc = dev_alloc(h, &h->d_flag, 4))) return fail(rc);
 
     cudaError_t e;
@@ -1188,6 +1210,8 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     // tensor-core form of the Helmholtz inverses: FP64 Crank-Nicolson runs with
     // the direct solver (DNS3D_TENSOR_CORES=0 keeps the FP64-pipe kernel)
     if ((rc = dev_alloc(h, &h->d_tcerr, 2))) return fail(rc);
+    const char* zcenv = std::getenv("DNS3D_ZERO_COPY");
+    h->zero_copy = !(zcenv && std::strcmp(zcenv, "0") == 0);
     const char* tcenv = std::getenv("DNS3D_TENSOR_CORES");
     const char* stall = std::getenv("DNS3D_TC_TEST_STALL");
     ops.tc_stall = stall && std::strcmp(stall, "1") == 0;
@@ -1416,6 +1440,19 @@ int dns3d_set_state(dns3d_handle* h, const double* u, const double* v, const dou
     int idx[4], n = 0;
     for (int f = 0; f < 4; ++f)
         if (src[f]) idx[n++] = f;
+    // pinned buffers: the x pass of the transform reads them in place
+    bool in_place = h->zero_copy && n > 0;
+    RFields hv{};
+    for (int i = 0; i < n && in_place; ++i) {
+        hv.p[i] = device_view(src[idx[i]]);
+        in_place = hv.p[i] != nullptr;
+    }
+    if (in_place) {
+        Fields sp{};
+        for (int i = 0; i < n; ++i) sp.p[i] = dst[idx[i]];
+        CK(h, fft_r2c(h->fft, g, hv, sp, n, g.nz, h->stream));
+        n = 0;  // nothing left for the copies below
+    }
     const int na = (n + 1) / 2;
     if (n > na) CK(h, fork_side(h, 0));  // the side copies wait for prior work on phys[]
     for (int i = 0; i < n; ++i) {
@@ -1473,6 +1510,25 @@ int dns3d_get_state(dns3d_handle* h, double* u, double* v, double* w, double* p_
         if (!dst[f]) continue;
         if (h->phys_valid >> f & 1u) have[nh++] = f;
         else need[n++] = f;
+    }
+    // pinned buffers and fixed-point transforms: the x pass writes each field
+    // to phys[] (kept for the diagnostics) and to the host buffer in one pass
+    bool in_place = h->zero_copy && h->fft.fx && n > 0;
+    RFields hv{};
+    for (int i = 0; i < n && in_place; ++i) {
+        hv.p[i] = device_view(dst[need[i]]);
+        in_place = hv.p[i] != nullptr;
+    }
+    if (in_place) {
+        Fields sp{};
+        RFields ph{};
+        for (int i = 0; i < n; ++i) {
+            sp.p[i] = src[need[i]];
+            ph.p[i] = h->phys[need[i]];
+        }
+        CK(h, fft_c2r_copy(h->fft, g, sp, ph, hv, n, g.nz, h->stream));
+        for (int i = 0; i < n; ++i) h->phys_valid |= 1u << need[i];
+        n = 0;
     }
     const int na = (n + 1) / 2;
     const bool side = nh > 0 || n > 1;
@@ -1706,9 +1762,10 @@ int diag_core(dns3d_handle* h, dns3d_diag* out, bool with_div, std::vector<doubl
     constexpr int kPiDoubles = (int)(sizeof(dns3d_pi_state) / sizeof(double));
     CK(h, launch_diag_gather(g, h->U, h->V, h->W, h->d_pi, h->d_out + 8, h->stream));
     CK(h, cudaMemcpyAsync(h->d_out + 5, h->d_tcerr, 2 * sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
-    std::vector<double> blk(8 + kPiDoubles + 6 * (size_t)g.nz);
-    CK(h, cudaMemcpyAsync(blk.data(), h->d_out, blk.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    const size_t nblk = 8 + kPiDoubles + 6 * (size_t)g.nz;
+    CK(h, cudaMemcpyAsync(h->h_out, h->d_out, nblk * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    const std::vector<double> blk(h->h_out, h->h_out + nblk);
     double res[5] = {blk[0], blk[1], blk[2], blk[3], with_div ? blk[4] : 0.0};
     dns3d_pi_state pi{};
     std::memcpy(&pi, blk.data() + 8, sizeof(pi));
@@ -1748,6 +1805,28 @@ extern "C" {
 int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out) {
     if (!h || !out) return DNS3D_E_INVALID;
     return diag_core(h, out, true, nullptr);
+}
+
+int dns3d_output_diagnostics(dns3d_handle* h, dns3d_diag* out) {
+    if (!h || !out) return DNS3D_E_INVALID;
+    return diag_core(h, out, false, nullptr);
+}
+
+int dns3d_check_divergence(dns3d_handle* h, double* max_div) {
+    if (!h || !max_div) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    const GridDev& g = h->g;
+    const dns3d_config& c = h->cfg;
+    double2* div = h->fft.tmp + (size_t)5 * spec_elems(c);
+    CK(h, launch_divergence(g, h->ops, h->U, h->V, h->W, div, h->stream));
+    Fields dv{}; dv.p[0] = div;
+    RFields dp{}; dp.p[0] = h->phys[3];
+    h->phys_valid &= ~8u;  // phys[3] now holds the divergence
+    CK(h, fft_c2r(h->fft, g, dv, dp, 1, g.nz, h->stream));
+    CK(h, launch_maxabs(g, h->phys[3], phys_elems(c), h->d_red, h->red_blocks, h->d_out + 4, h->stream));
+    CK(h, cudaMemcpyAsync(max_div, h->d_out + 4, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return std::isfinite(*max_div) ? DNS3D_OK : DNS3D_E_NONFINITE;
 }
 
 int dns3d_flow_statistics(dns3d_handle* h, dns3d_flow_stats* out, double* u_avg, double* v_avg, double* w_avg) {

@@ -117,8 +117,9 @@ cudaError_t fft_ct_r2c_x(FieldsT<T> src, FieldsT<typename Cx<T>::type> dst, cons
 template <int SIGN>
 cudaError_t fft_fx_y(Fields src, Fields dst, const GridDev& g, int nplanes, int ncol, int nf, const longlong2* tw,
                      cudaStream_t s);
-cudaError_t fft_fx_c2r_x(Fields src, RFields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
-                         const longlong2* tw_nx, cudaStream_t s);
+// dst2 (entries may be null): a second destination of the same values
+cudaError_t fft_fx_c2r_x(Fields src, RFields dst, RFields dst2, const GridDev& g, int nrows, int nf,
+                         const longlong2* tw_n, const longlong2* tw_nx, cudaStream_t s);
 cudaError_t fft_fx_r2c_x(RFields src, Fields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
                          const longlong2* tw_nx, cudaStream_t s);
 
@@ -127,6 +128,11 @@ void fft_release(FftCtx& ctx);
 // spec[f] (spectral, read only) -> phys[f]; uses ctx.tmp (nf <= tmp_fields).
 cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, int nf,
                     int nplanes, cudaStream_t s);
+// The same into phys[f] and into copy[f] as well (host memory the device
+// can address, for example), in one pass; only where ctx.fx is set
+// (cudaErrorNotSupported otherwise).
+cudaError_t fft_c2r_copy(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, RFields copy, int nf,
+                         int nplanes, cudaStream_t s);
 // phys[f] -> spec[f].  With ncol > 0 only the kx < ncol columns of spec are
 // completed (the others keep the x transform's output): for sources that the
 // 2/3 filter truncates at kx_max = ncol - 1 anyway.

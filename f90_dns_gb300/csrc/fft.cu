@@ -374,7 +374,7 @@ cudaError_t c2r_impl(const FftCtx& ctx, const GridDev& g, FieldsT<typename Cx<T>
             cudaError_t e = fft_fx_y<+1>(spec, tmp, g, nplanes, g.nxhp, nf, ctx.twq_ny, s);
             if (e) return e;
             if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_y_inverse");
-            e = fft_fx_c2r_x(tmp, phys, g, nrows, nf, ctx.twq_nx2, ctx.twq_nx, s);
+            e = fft_fx_c2r_x(tmp, phys, RFields{}, g, nrows, nf, ctx.twq_nx2, ctx.twq_nx, s);
             if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_c2r");
             return e;
         }
@@ -442,6 +442,20 @@ cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields ph
     Fields tmp{};
     for (int f = 0; f < nf; ++f) tmp.p[f] = ctx.tmp + (size_t)f * g.nm * g.nz;
     return c2r_impl<double>(ctx, g, spec, phys, tmp, nf, nplanes, s, ctx.tw_ny, ctx.tw_nx2, ctx.tw_nx);
+}
+
+cudaError_t fft_c2r_copy(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, RFields copy, int nf,
+                         int nplanes, cudaStream_t s) {
+    if (!ctx.fx) return cudaErrorNotSupported;
+    if (nf > ctx.tmp_fields || nf > kMaxFields) return cudaErrorInvalidValue;
+    Fields tmp{};
+    for (int f = 0; f < nf; ++f) tmp.p[f] = ctx.tmp + (size_t)f * g.nm * g.nz;
+    cudaError_t e = fft_fx_y<+1>(spec, tmp, g, nplanes, g.nxhp, nf, ctx.twq_ny, s);
+    if (e) return e;
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_y_inverse");
+    e = fft_fx_c2r_x(tmp, phys, copy, g, nplanes * g.ny, nf, ctx.twq_nx2, ctx.twq_nx, s);
+    if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_c2r");
+    return e;
 }
 
 cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf, int nplanes,

@@ -499,15 +499,17 @@ __global__ void __launch_bounds__(kThreads) k_fft_y_fx(Fields src, Fields dst, G
 // inverse transform, and the 1/(nx ny) scaling as an exact multiple of the
 // FP64 constant's mantissa rounded once.
 template <int N>
-__device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& dst, const GridDev& g, int nrows,
-                                              const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx, int bx,
-                                              int f, fx2* buf, unsigned* emax) {
+__device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& dst, const RFields& dst2,
+                                              const GridDev& g, int nrows, const fx2* __restrict__ tw_n,
+                                              const fx2* __restrict__ tw_nx, int bx, int f, fx2* buf,
+                                              unsigned* emax) {
     constexpr int RX = per_cta(N);
     constexpr int LD = N + 1;
     constexpr int B = fx_bits(N, 2);
     const int row0 = bx * RX;
     const double2* __restrict__ s = field_ptr(src, f);
     double2* d = reinterpret_cast<double2*>(field_ptr(dst, f));
+    double2* d2 = reinterpret_cast<double2*>(field_ptr(dst2, f));  // optional second copy (null: none)
     const int nxhp = N + 1;
     constexpr int ITERS = RX * N / kThreads;
     static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
@@ -576,18 +578,21 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
             const fx2 z = buf[r * LD + k];
             const long long yx = (long long)(((__int128)z.x * M + ((__int128)1 << 51)) >> 52);
             const long long yy = (long long)(((__int128)z.y * M + ((__int128)1 << 51)) >> 52);
-            d[(size_t)(row0 + r) * N + k] =
+            const double2 o =
                 em == 0x7FF ? make_double2(fx_nan(), fx_nan()) : make_double2(fx_to(yx, e2), fx_to(yy, e2));
+            d[(size_t)(row0 + r) * N + k] = o;
+            if (d2) d2[(size_t)(row0 + r) * N + k] = o;
         }
     }
 }
 
 template <int N>
-__global__ void __launch_bounds__(kThreads, 3) k_c2r_x_fx(Fields src, RFields dst, GridDev g, int nrows,
-                                                       const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx) {
+__global__ void __launch_bounds__(kThreads, 3) k_c2r_x_fx(Fields src, RFields dst, RFields dst2, GridDev g,
+                                                          int nrows, const fx2* __restrict__ tw_n,
+                                                          const fx2* __restrict__ tw_nx) {
     __shared__ fx2 buf[per_cta(N) * (N + 1)];
     __shared__ unsigned emax[per_cta(N)];
-    c2r_x_body_fx<N>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax);
+    c2r_x_body_fx<N>(src, dst, dst2, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax);
 }
 
 // r2c along x in fixed point: z[m] = x[2m] + i x[2m+1] of one row scaled
@@ -781,8 +786,8 @@ struct RsC2RFx {
         switch (d.g.nxh) {
 #define X_CASE(n)                                                                                               \
     case n:                                                                                                     \
-        c2r_x_body_fx<n>(one_field<double2>(d.tmp, f), one_field<double>(d.phys, f), d.g, d.g.nz * d.g.ny, twn, \
-                         twx, bx, 0, buf, emax);                                                                \
+        c2r_x_body_fx<n>(one_field<double2>(d.tmp, f), one_field<double>(d.phys, f), RFields{}, d.g,           \
+                         d.g.nz * d.g.ny, twn, twx, bx, 0, buf, emax);                                          \
         break;
             DNS3D_CT_X_LENGTHS(X_CASE)
 #undef X_CASE
@@ -871,11 +876,11 @@ void launch_y_fx(Fields src, Fields dst, const GridDev& g, int nplanes, int ncol
 }
 
 template <int N>
-void launch_c2r_fx(Fields src, RFields dst, const GridDev& g, int nrows, int nf, const fx2* tw_n, const fx2* tw_nx,
-                   cudaStream_t s) {
+void launch_c2r_fx(Fields src, RFields dst, RFields dst2, const GridDev& g, int nrows, int nf, const fx2* tw_n,
+                   const fx2* tw_nx, cudaStream_t s) {
     constexpr int RX = per_cta(N);
     dim3 grid((nrows + RX - 1) / RX, nf);
-    k_c2r_x_fx<N><<<grid, kThreads, 0, s>>>(src, dst, g, nrows, tw_n, tw_nx);
+    k_c2r_x_fx<N><<<grid, kThreads, 0, s>>>(src, dst, dst2, g, nrows, tw_n, tw_nx);
 }
 
 template <int N>
@@ -954,11 +959,11 @@ cudaError_t fft_fx_y(Fields src, Fields dst, const GridDev& g, int nplanes, int 
     return cudaGetLastError();
 }
 
-cudaError_t fft_fx_c2r_x(Fields src, RFields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
-                         const longlong2* tw_nx, cudaStream_t s) {
+cudaError_t fft_fx_c2r_x(Fields src, RFields dst, RFields dst2, const GridDev& g, int nrows, int nf,
+                         const longlong2* tw_n, const longlong2* tw_nx, cudaStream_t s) {
     switch (g.nxh) {
 #define X_CASE(n) \
-    case n: launch_c2r_fx<n>(src, dst, g, nrows, nf, tw_n, tw_nx, s); break;
+    case n: launch_c2r_fx<n>(src, dst, dst2, g, nrows, nf, tw_n, tw_nx, s); break;
         DNS3D_CT_X_LENGTHS(X_CASE)
 #undef X_CASE
         default: return cudaErrorInvalidValue;

@@ -2162,49 +2162,74 @@ __global__ void k_correction_mixed(GridDev g, Ops ops, StepParams sp, const doub
 // ------------------------------------------------------------------ reductions
 
 // Per-block partials of max|u|, max|v|, max|w| and sum 0.5|u|^2 zwts[k].
+// Block (bx, k) reduces part bx of plane k: max |u|, |v|, |w| as the largest
+// bit pattern of |x| (integer comparisons order non-negative doubles, and a
+// NaN beats every number), and the plane's sum of |u|^2 scaled by 0.5 w_k once.
 __global__ void __launch_bounds__(256) k_diag_partial(GridDev g, const double* __restrict__ zw,
                                                       const double* __restrict__ u,
                                                       const double* __restrict__ v,
                                                       const double* __restrict__ w,
                                                       double* __restrict__ partial) {
-    const size_t n = (size_t)g.nx * g.ny * g.nz;
     const size_t plane = (size_t)g.nx * g.ny;
-    double mu = 0.0, mv = 0.0, mw = 0.0, e = 0.0;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const double a = u[i], b = v[i], c = w[i];
-        mu = fmax(mu, fabs(a));
-        mv = fmax(mv, fabs(b));
-        mw = fmax(mw, fabs(c));
-        e += 0.5 * (a * a + b * b + c * c) * __ldg(&zw[i / plane]);
+    const size_t off = (size_t)blockIdx.y * plane;
+    const unsigned long long am = 0x7FFFFFFFFFFFFFFFULL;
+    unsigned long long mu = 0, mv = 0, mw = 0;
+    double e = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += (size_t)gridDim.x * blockDim.x) {
+        const double a = u[off + i], b = v[off + i], c = w[off + i];
+        mu = max(mu, (unsigned long long)__double_as_longlong(a) & am);
+        mv = max(mv, (unsigned long long)__double_as_longlong(b) & am);
+        mw = max(mw, (unsigned long long)__double_as_longlong(c) & am);
+        e = fma(a, a, e);
+        e = fma(b, b, e);
+        e = fma(c, c, e);
     }
-    __shared__ double red[4][8];
-    mu = warp_max(mu); mv = warp_max(mv); mw = warp_max(mw); e = warp_sum(e);
+    __shared__ unsigned long long redm[3][8];
+    __shared__ double rede[8];
+    for (int o = 16; o > 0; o >>= 1) {
+        mu = max(mu, __shfl_xor_sync(0xffffffffu, mu, o));
+        mv = max(mv, __shfl_xor_sync(0xffffffffu, mv, o));
+        mw = max(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+    }
+    e = warp_sum(e);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { red[0][wid] = mu; red[1][wid] = mv; red[2][wid] = mw; red[3][wid] = e; }
+    if (lane == 0) { redm[0][wid] = mu; redm[1][wid] = mv; redm[2][wid] = mw; rede[wid] = e; }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
-            mu = fmax(mu, red[0][k]); mv = fmax(mv, red[1][k]); mw = fmax(mw, red[2][k]); e += red[3][k];
+            mu = max(mu, redm[0][k]); mv = max(mv, redm[1][k]); mw = max(mw, redm[2][k]); e += rede[k];
         }
-        partial[4 * blockIdx.x + 0] = mu;
-        partial[4 * blockIdx.x + 1] = mv;
-        partial[4 * blockIdx.x + 2] = mw;
-        partial[4 * blockIdx.x + 3] = e;
+        const int b = blockIdx.y * gridDim.x + blockIdx.x;
+        partial[4 * b + 0] = __longlong_as_double((long long)mu);
+        partial[4 * b + 1] = __longlong_as_double((long long)mv);
+        partial[4 * b + 2] = __longlong_as_double((long long)mw);
+        partial[4 * b + 3] = 0.5 * e * __ldg(&zw[blockIdx.y]);
     }
 }
 
 // One warp: lane l folds partials l, l+32, ...; then a butterfly.
+__device__ __forceinline__ unsigned long long bits_of(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
 __global__ void k_diag_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
-    double mu = 0.0, mv = 0.0, mw = 0.0, e = 0.0;
+    unsigned long long mu = 0, mv = 0, mw = 0;  // |x| bit patterns (NaN beats every number)
+    double e = 0.0;
     for (int b = threadIdx.x; b < nb; b += 32) {
-        mu = fmax(mu, partial[4 * b]);
-        mv = fmax(mv, partial[4 * b + 1]);
-        mw = fmax(mw, partial[4 * b + 2]);
+        mu = max(mu, bits_of(partial[4 * b]));
+        mv = max(mv, bits_of(partial[4 * b + 1]));
+        mw = max(mw, bits_of(partial[4 * b + 2]));
         e += partial[4 * b + 3];
     }
-    mu = warp_max(mu); mv = warp_max(mv); mw = warp_max(mw); e = warp_sum(e);
-    if (threadIdx.x == 0) { out[0] = mu; out[1] = mv; out[2] = mw; out[3] = e; }
+    mu = warp_max_bits(mu); mv = warp_max_bits(mv); mw = warp_max_bits(mw); e = warp_sum(e);
+    if (threadIdx.x == 0) {
+        out[0] = __longlong_as_double((long long)mu);
+        out[1] = __longlong_as_double((long long)mv);
+        out[2] = __longlong_as_double((long long)mw);
+        out[3] = e;
+    }
 }
 
 // The controller state and the (0,0) mode of u, v, w per level, gathered
@@ -2223,26 +2248,28 @@ __global__ void k_diag_gather(GridDev g, const double2* __restrict__ U, const do
     }
 }
 
+// max |f| as the largest bit pattern of |f| (integer comparisons; a NaN wins)
 __global__ void __launch_bounds__(256) k_maxabs_partial(const double* __restrict__ f, size_t n,
                                                         double* __restrict__ partial) {
-    double m = 0.0;
+    unsigned long long m = 0;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) m = fmax(m, fabs(f[i]));
-    __shared__ double red[8];
-    m = warp_max(m);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        m = max(m, bits_of(f[i]) & 0x7FFFFFFFFFFFFFFFULL);
+    __shared__ unsigned long long red[8];
+    m = warp_max_bits(m);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = fmax(m, red[k]);
-        partial[blockIdx.x] = m;
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = max(m, red[k]);
+        partial[blockIdx.x] = __longlong_as_double((long long)m);
     }
 }
 
 __global__ void k_max_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
-    double m = 0.0;
-    for (int b = threadIdx.x; b < nb; b += 32) m = fmax(m, partial[b]);
-    m = warp_max(m);
-    if (threadIdx.x == 0) out[0] = m;
+    unsigned long long m = 0;
+    for (int b = threadIdx.x; b < nb; b += 32) m = max(m, bits_of(partial[b]));
+    m = warp_max_bits(m);
+    if (threadIdx.x == 0) out[0] = __longlong_as_double((long long)m);
 }
 
 __global__ void k_nonfinite(const double2* __restrict__ f, size_t n, int* flag) {
@@ -2660,8 +2687,11 @@ cudaError_t launch_grad_walls(const GridDev& g, const Ops& ops, const double2* P
 cudaError_t launch_diag_reduce(const GridDev& g, const Ops& ops, const double* u, const double* v,
                                const double* w, double* partial, int nblocks, double* out,
                                cudaStream_t s) {
-    k_diag_partial<<<nblocks, 256, 0, s>>>(g, ops.zw, u, v, w, partial);
-    k_diag_final<<<1, 32, 0, s>>>(partial, nblocks, out);
+    // blocks per plane: nz of them fit the nblocks partial slots
+    const int bx = std::max(1, std::min(nblocks / g.nz, (g.nx * g.ny + 255) / 256));
+    if (bx * g.nz > nblocks) return cudaErrorInvalidValue;
+    k_diag_partial<<<dim3(bx, g.nz), 256, 0, s>>>(g, ops.zw, u, v, w, partial);
+    k_diag_final<<<1, 32, 0, s>>>(partial, bx * g.nz, out);
     return cudaGetLastError();
 }
 

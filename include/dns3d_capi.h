@@ -177,6 +177,12 @@ int dns3d_synchronize(dns3d_handle* h);
 
 /* output_diagnostics_3d observables plus check_divergence_3d's max |div u|. */
 int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out);
+/* The two reference routines one at a time, for a driver that calls them on
+ * the reference's schedule (every nwrt steps, every 50 steps, 3D:329-344):
+ * output_diagnostics_3d (3D:2094-2146) -- *out as dns3d_diagnostics gives it,
+ * with max_div = 0 -- and check_divergence_3d (3D:2171-2190). */
+int dns3d_output_diagnostics(dns3d_handle* h, dns3d_diag* out);
+int dns3d_check_divergence(dns3d_handle* h, double* max_div);
 
 /* Measurement helpers (no counterpart in the reference, whose only timing is
  * cpu_time around each step, 3D:287-360).

@@ -259,3 +259,18 @@ def test_nonfinite_state_is_reported(built_lib):
         d.set_state(u=st["u"])
         d.step(2)
         assert np.isfinite(d.diagnostics().energy)
+
+
+def test_split_diagnostics_match_combined(built_lib):
+    """dns3d_output_diagnostics and dns3d_check_divergence (the reference's
+    output_diagnostics_3d and check_divergence_3d, called on their own
+    schedules) give exactly what dns3d_diagnostics gives in one call."""
+    wl = dict(C1, nx=32, ny=24, nz=17)
+    with ChannelDNS(config_from(wl)) as d:
+        d.step(3)
+        full = d.diagnostics()
+        out = d.output_diagnostics_3d()
+        div = d.check_divergence_3d()
+    assert out.max_div == 0.0 and div == full.max_div
+    for k in ("umax", "vmax", "wmax", "energy", "u_bulk", "dpdx", "dpdx_avg", "time", "step"):
+        assert getattr(out, k) == getattr(full, k), k
