@@ -1186,6 +1186,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     // step parameters
     StepParams& sp = h->sp;
     sp.dt = c.dt;
+    sp.inv_dt = 1.0 / c.dt;
     sp.cn_fac = c.use_crank_nicolson ? 0.5 * c.dt / c.re : 0.0;
     sp.helm_f = helm_f;
     sp.cn_identity = (sp.cn_fac != 0.0 && sp.cn_fac == helm_f) ? 1 : 0;

@@ -147,6 +147,7 @@ cudaError_t fft_r2c32(const FftCtx& ctx, const GridDev& g, FRFields phys, FField
 // ---------------------------------------------------------------- step.cu
 struct StepParams {
     double dt;
+    double inv_dt;        // 1/dt, formed once on the host (an FP64 division is a long sequence on this GPU)
     double cn_fac;        // 0.5*dt/Re if Crank-Nicolson else 0 (3D:1374)
     double helm_f;        // theta*dt/Re (3D:1459)
     double forcing_scale; // nx*ny: physical constant -> (0,0) coefficient

@@ -162,8 +162,20 @@ __host__ __device__ constexpr int per_cta(int n) {
     return c;
 }
 
+// Shared-memory slot of element t of one transform.  FP32 passes insert one
+// padding slot after every 16 elements, so that a Stockham pass's writes at
+// stride R (8 for the radix-8 passes) fall in distinct banks instead of in
+// two: those passes are bound by shared-memory throughput.  The FP64 and
+// fixed-point passes (16-byte elements, bound by their arithmetic) keep the
+// plain layout, which needs fewer registers.
+template <typename C> __host__ __device__ constexpr int sw(int t) {
+    return std::is_same<C, float2>::value ? t + (t >> 4) : t;
+}
+// Slots per transform: elements 0..N (slot sw(N) holds an x pass's kx = nx/2 input).
+template <typename C> __host__ __device__ constexpr int ld_of(int n) { return sw<C>(n) + 1; }
+
 // One Stockham pass (radix R, Ns finished sub-length) over CNT transforms of
-// length N stored at buf[c*LD + t], in place: all inputs of the thread's
+// length N stored at buf[c*LD + sw(t)], in place: all inputs of the thread's
 // butterflies are read into registers before a barrier, then written.
 // tw[t] = e^{-2 pi i t / N}.
 template <int N, int R, int NS, int SIGN, int CNT, int LD, typename C>
@@ -180,7 +192,7 @@ __device__ __forceinline__ void ct_pass(C* buf, const C* __restrict__ tw) {
             const int c = t / NB, j = t - c * NB;
             const C* src = buf + c * LD;
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[p][r] = src[j + r * NB];
+            for (int r = 0; r < R; ++r) v[p][r] = src[sw<C>(j + r * NB)];
             if constexpr (NS > 1) {
                 const int k = j % NS;
 #pragma unroll
@@ -200,9 +212,10 @@ __device__ __forceinline__ void ct_pass(C* buf, const C* __restrict__ tw) {
         if (TOTAL % kThreads == 0 || t < TOTAL) {
             const int c = t / NB, j = t - c * NB;
             const int k = j % NS;
-            C* dst = buf + c * LD + (j / NS) * NS * R + k;
+            C* dst = buf + c * LD;
+            const int o = (j / NS) * NS * R + k;
 #pragma unroll
-            for (int q = 0; q < R; ++q) dst[q * NS] = v[p][q];
+            for (int q = 0; q < R; ++q) dst[sw<C>(o + q * NS)] = v[p][q];
         }
     }
     __syncthreads();
@@ -227,7 +240,7 @@ __device__ __forceinline__ void fft_y_body(const FieldsT<C>& src, const FieldsT<
                                            int nplanes, int ncol, const C* __restrict__ tw, int bx, int f,
                                            C* buf) {
     constexpr int CX = per_cta(N);
-    constexpr int LD = N + 1;
+    constexpr int LD = ld_of<C>(N);
     const long long ncols = (long long)nplanes * ncol;
     const long long vc = (long long)bx * CX + (threadIdx.x % CX);
     const bool live = vc < ncols;
@@ -249,20 +262,20 @@ __device__ __forceinline__ void fft_y_body(const FieldsT<C>& src, const FieldsT<
     for (int it = 0; it < ITERS; ++it)
         v[it] = live ? s[base + (size_t)(y0 + it * ROWS_PER_ITER) * g.nxhp] : mk<C>(0, 0);
 #pragma unroll
-    for (int it = 0; it < ITERS; ++it) buf[c * LD + y0 + it * ROWS_PER_ITER] = v[it];
+    for (int it = 0; it < ITERS; ++it) buf[c * LD + sw<C>(y0 + it * ROWS_PER_ITER)] = v[it];
     __syncthreads();
     ct_fft<N, 1, SIGN, CX, LD>(buf, tw);
     if (live) {
 #pragma unroll
         for (int it = 0; it < ITERS; ++it)
-            d[base + (size_t)(y0 + it * ROWS_PER_ITER) * g.nxhp] = buf[c * LD + y0 + it * ROWS_PER_ITER];
+            d[base + (size_t)(y0 + it * ROWS_PER_ITER) * g.nxhp] = buf[c * LD + sw<C>(y0 + it * ROWS_PER_ITER)];
     }
 }
 
 template <int N, int SIGN, typename C>
 __global__ void __launch_bounds__(kThreads) k_fft_y_ct(FieldsT<C> src, FieldsT<C> dst, GridDev g, int nplanes,
                                                        int ncol, const C* __restrict__ tw) {
-    __shared__ C buf[per_cta(N) * (N + 1)];
+    __shared__ C buf[per_cta(N) * ld_of<C>(N)];
     fft_y_body<N, SIGN, C>(src, dst, g, nplanes, ncol, tw, blockIdx.x, blockIdx.z, buf);
 }
 
@@ -278,7 +291,7 @@ __device__ __forceinline__ void c2r_x_body(const FieldsT<typename Cx<T>::type>& 
                                            typename Cx<T>::type* buf) {
     using C = typename Cx<T>::type;
     constexpr int RX = per_cta(N);
-    constexpr int LD = N + 1;
+    constexpr int LD = ld_of<C>(N);
     const int row0 = bx * RX;
     const C* __restrict__ s = field_ptr(src, f);
     C* d = reinterpret_cast<C*>(field_ptr(dst, f));
@@ -312,7 +325,7 @@ __device__ __forceinline__ void c2r_x_body(const FieldsT<typename Cx<T>::type>& 
         C w = __ldg(&tw_nx[k]);
         w.y = -w.y;
         const C p = cmul(w, df);
-        buf[r * LD + k] = mk<C>(sm.x - p.y, sm.y + p.x);
+        buf[r * LD + sw<C>(k)] = mk<C>(sm.x - p.y, sm.y + p.x);
     }
     __syncthreads();
     ct_fft<N, 1, +1, RX, LD>(buf, tw_n);
@@ -322,7 +335,7 @@ __device__ __forceinline__ void c2r_x_body(const FieldsT<typename Cx<T>::type>& 
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
         if (row0 + r < nrows) {
-            const C z = buf[r * LD + k];
+            const C z = buf[r * LD + sw<C>(k)];
             d[(size_t)(row0 + r) * N + k] = mk<C>(z.x * sc, z.y * sc);
         }
     }
@@ -333,7 +346,7 @@ __global__ void __launch_bounds__(kThreads) k_c2r_x_ct(FieldsT<typename Cx<T>::t
                                                        GridDev g, int nrows,
                                                        const typename Cx<T>::type* __restrict__ tw_n,
                                                        const typename Cx<T>::type* __restrict__ tw_nx) {
-    __shared__ typename Cx<T>::type buf[per_cta(N) * (N + 1)];
+    __shared__ typename Cx<T>::type buf[per_cta(N) * ld_of<typename Cx<T>::type>(N)];
     c2r_x_body<N, T>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf);
 }
 
@@ -348,7 +361,7 @@ __device__ __forceinline__ void r2c_x_body(const FieldsT<T>& src, const FieldsT<
                                            typename Cx<T>::type* buf) {
     using C = typename Cx<T>::type;
     constexpr int RX = per_cta(N);
-    constexpr int LD = N + 1;
+    constexpr int LD = ld_of<C>(N);
     const int row0 = bx * RX;
     const C* __restrict__ s = reinterpret_cast<const C*>(field_ptr(src, f));
     C* d = field_ptr(dst, f);
@@ -365,15 +378,15 @@ __device__ __forceinline__ void r2c_x_body(const FieldsT<T>& src, const FieldsT<
     for (int it = 0; it < ITERS; ++it) {
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
-        buf[r * LD + k] = v[it];
+        buf[r * LD + sw<C>(k)] = v[it];
     }
     __syncthreads();
     ct_fft<N, 1, -1, RX, LD>(buf, tw_n);
     for (int t = threadIdx.x; t < RX * (N + 1); t += kThreads) {
         const int r = t / (N + 1), k = t - r * (N + 1);
         if (row0 + r < nrows) {
-            const C za = buf[r * LD + (k == N ? 0 : k)];
-            const C zb = buf[r * LD + (k == 0 ? 0 : N - k)];
+            const C za = buf[r * LD + sw<C>(k == N ? 0 : k)];
+            const C zb = buf[r * LD + sw<C>(k == 0 ? 0 : N - k)];
             const T hf = (T)0.5;
             const C e = mk<C>(hf * (za.x + zb.x), hf * (za.y - zb.y));
             const C o = mk<C>(hf * (za.y + zb.y), -hf * (za.x - zb.x));
@@ -388,7 +401,7 @@ __global__ void __launch_bounds__(kThreads) k_r2c_x_ct(FieldsT<T> src, FieldsT<t
                                                        GridDev g, int nrows,
                                                        const typename Cx<T>::type* __restrict__ tw_n,
                                                        const typename Cx<T>::type* __restrict__ tw_nx) {
-    __shared__ typename Cx<T>::type buf[per_cta(N) * (N + 1)];
+    __shared__ typename Cx<T>::type buf[per_cta(N) * ld_of<typename Cx<T>::type>(N)];
     r2c_x_body<N, T>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf);
 }
 
@@ -440,7 +453,7 @@ __device__ __forceinline__ void fft_y_body_fx(const Fields& src, const Fields& d
                                               int ncol, const fx2* __restrict__ tw, int bx, int f, fx2* buf,
                                               unsigned* emax) {
     constexpr int CX = per_cta(N);
-    constexpr int LD = N + 1;
+    constexpr int LD = ld_of<fx2>(N);
     constexpr int B = fx_bits(N, 0);
     const long long ncols = (long long)nplanes * ncol;
     const long long vc = (long long)bx * CX + (threadIdx.x % CX);
@@ -472,14 +485,14 @@ __device__ __forceinline__ void fft_y_body_fx(const Fields& src, const Fields& d
     const int rsb = 53 - B + em;
 #pragma unroll
     for (int it = 0; it < ITERS; ++it)
-        buf[c * LD + y0 + it * ROWS_PER_ITER] = mk<fx2>(fx_from(v[it].x, rsb), fx_from(v[it].y, rsb));
+        buf[c * LD + sw<fx2>(y0 + it * ROWS_PER_ITER)] = mk<fx2>(fx_from(v[it].x, rsb), fx_from(v[it].y, rsb));
     __syncthreads();
     ct_fft<N, 1, SIGN, CX, LD>(buf, tw);
     if (live) {
         const int e2 = em - 1022 - B;
 #pragma unroll
         for (int it = 0; it < ITERS; ++it) {
-            const fx2 z = buf[c * LD + y0 + it * ROWS_PER_ITER];
+            const fx2 z = buf[c * LD + sw<fx2>(y0 + it * ROWS_PER_ITER)];
             d[base + (size_t)(y0 + it * ROWS_PER_ITER) * g.nxhp] =
                 em == 0x7FF ? make_double2(fx_nan(), fx_nan()) : make_double2(fx_to(z.x, e2), fx_to(z.y, e2));
         }
@@ -489,7 +502,7 @@ __device__ __forceinline__ void fft_y_body_fx(const Fields& src, const Fields& d
 template <int N, int SIGN>
 __global__ void __launch_bounds__(kThreads) k_fft_y_fx(Fields src, Fields dst, GridDev g, int nplanes, int ncol,
                                                        const fx2* __restrict__ tw) {
-    __shared__ fx2 buf[per_cta(N) * (N + 1)];
+    __shared__ fx2 buf[per_cta(N) * ld_of<fx2>(N)];
     __shared__ unsigned emax[per_cta(N)];
     fft_y_body_fx<N, SIGN>(src, dst, g, nplanes, ncol, tw, blockIdx.x, blockIdx.z, buf, emax);
 }
@@ -504,7 +517,7 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
                                               const fx2* __restrict__ tw_nx, int bx, int f, fx2* buf,
                                               unsigned* emax) {
     constexpr int RX = per_cta(N);
-    constexpr int LD = N + 1;
+    constexpr int LD = ld_of<fx2>(N);
     constexpr int B = fx_bits(N, 2);
     const int row0 = bx * RX;
     const double2* __restrict__ s = field_ptr(src, f);
@@ -531,9 +544,9 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
         if (k == 0) {  // Im of kx = 0 and kx = nx/2 is ignored
             a.y = 0.0;
             b.y = 0.0;
-            buf[r * LD + N] = mk<fx2>(__double_as_longlong(b.x), __double_as_longlong(b.y));
+            buf[r * LD + sw<fx2>(N)] = mk<fx2>(__double_as_longlong(b.x), __double_as_longlong(b.y));
         }
-        buf[r * LD + k] = mk<fx2>(__double_as_longlong(a.x), __double_as_longlong(a.y));
+        buf[r * LD + sw<fx2>(k)] = mk<fx2>(__double_as_longlong(a.x), __double_as_longlong(a.y));
         e[it] = max(fx_expo(a), fx_expo(b));
     }
     __syncthreads();
@@ -546,7 +559,7 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
         const int rsb = 53 - B + (int)emax[r];
-        const fx2 ra = buf[r * LD + k], rb = buf[r * LD + N - k];
+        const fx2 ra = buf[r * LD + sw<fx2>(k)], rb = buf[r * LD + sw<fx2>(N - k)];
         const fx2 a = mk<fx2>(fx_from(__longlong_as_double(ra.x), rsb), fx_from(__longlong_as_double(ra.y), rsb));
         const fx2 b = mk<fx2>(fx_from(__longlong_as_double(rb.x), rsb), fx_from(__longlong_as_double(rb.y), rsb));
         const fx2 sm = mk<fx2>(a.x + b.x, a.y - b.y);
@@ -560,7 +573,7 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
 #pragma unroll
     for (int it = 0; it < ITERS; ++it) {
         const int t = threadIdx.x + it * kThreads;
-        buf[(t / N) * LD + t % N] = z[it];
+        buf[(t / N) * LD + sw<fx2>(t % N)] = z[it];
     }
     __syncthreads();
     ct_fft<N, 1, +1, RX, LD>(buf, tw_n);
@@ -575,7 +588,7 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
         if (row0 + r < nrows) {
             const int em = (int)emax[r];
             const int e2 = em + E - 2045 - B;
-            const fx2 z = buf[r * LD + k];
+            const fx2 z = buf[r * LD + sw<fx2>(k)];
             const long long yx = (long long)(((__int128)z.x * M + ((__int128)1 << 51)) >> 52);
             const long long yy = (long long)(((__int128)z.y * M + ((__int128)1 << 51)) >> 52);
             const double2 o =
@@ -590,7 +603,7 @@ template <int N>
 __global__ void __launch_bounds__(kThreads, 3) k_c2r_x_fx(Fields src, RFields dst, RFields dst2, GridDev g,
                                                           int nrows, const fx2* __restrict__ tw_n,
                                                           const fx2* __restrict__ tw_nx) {
-    __shared__ fx2 buf[per_cta(N) * (N + 1)];
+    __shared__ fx2 buf[per_cta(N) * ld_of<fx2>(N)];
     __shared__ unsigned emax[per_cta(N)];
     c2r_x_body_fx<N>(src, dst, dst2, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax);
 }
@@ -604,7 +617,7 @@ __device__ __forceinline__ void r2c_x_body_fx(const RFields& src, const Fields& 
                                               const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx, int bx,
                                               int f, fx2* buf, unsigned* emax) {
     constexpr int RX = per_cta(N);
-    constexpr int LD = N + 1;
+    constexpr int LD = ld_of<fx2>(N);
     constexpr int B = fx_bits(N, 2);
     const int row0 = bx * RX;
     const double2* __restrict__ s = reinterpret_cast<const double2*>(field_ptr(src, f));
@@ -631,15 +644,15 @@ __device__ __forceinline__ void r2c_x_body_fx(const RFields& src, const Fields& 
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
         const int rsb = 53 - B + (int)emax[r];
-        buf[r * LD + k] = mk<fx2>(fx_from(v[it].x, rsb), fx_from(v[it].y, rsb));
+        buf[r * LD + sw<fx2>(k)] = mk<fx2>(fx_from(v[it].x, rsb), fx_from(v[it].y, rsb));
     }
     __syncthreads();
     ct_fft<N, 1, -1, RX, LD>(buf, tw_n);
     for (int t = threadIdx.x; t < RX * (N + 1); t += kThreads) {
         const int r = t / (N + 1), k = t - r * (N + 1);
         if (row0 + r < nrows) {
-            const fx2 za = buf[r * LD + (k == N ? 0 : k)];
-            const fx2 zb = buf[r * LD + (k == 0 ? 0 : N - k)];
+            const fx2 za = buf[r * LD + sw<fx2>(k == N ? 0 : k)];
+            const fx2 zb = buf[r * LD + sw<fx2>(k == 0 ? 0 : N - k)];
             const fx2 e = mk<fx2>(za.x + zb.x, za.y - zb.y);
             const fx2 o = mk<fx2>(za.y + zb.y, zb.x - za.x);
             const fx2 p = cmul(__ldg(&tw_nx[k]), o);
@@ -655,7 +668,7 @@ __device__ __forceinline__ void r2c_x_body_fx(const RFields& src, const Fields& 
 template <int N>
 __global__ void __launch_bounds__(kThreads) k_r2c_x_fx(RFields src, Fields dst, GridDev g, int nrows,
                                                        const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx) {
-    __shared__ fx2 buf[per_cta(N) * (N + 1)];
+    __shared__ fx2 buf[per_cta(N) * ld_of<fx2>(N)];
     __shared__ unsigned emax[per_cta(N)];
     r2c_x_body_fx<N>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax);
 }
@@ -667,7 +680,7 @@ __global__ void __launch_bounds__(kThreads) k_r2c_x_fx(RFields src, Fields dst, 
 // shared buffer sized for the longest.
 __host__ __device__ constexpr int ct_buf_max() {
     int m = 0;
-#define BUF_MAX(n) m = (per_cta(n) * (n + 1) > m) ? per_cta(n) * (n + 1) : m;
+#define BUF_MAX(n) m = (per_cta(n) * ld_of<float2>(n) > m) ? per_cta(n) * ld_of<float2>(n) : m;
     DNS3D_CT_Y_LENGTHS(BUF_MAX)
     DNS3D_CT_X_LENGTHS(BUF_MAX)
 #undef BUF_MAX

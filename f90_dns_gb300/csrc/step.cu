@@ -1051,7 +1051,7 @@ __device__ __forceinline__ double2 pressure_rhs(const GridDev& g, const Ops& ops
     const double2 hx = i_times(mi.ax, US[o]);
     const double2 hy = i_times(mi.ay, VS[o]);
     const double whz = __ldg(&ops.wh[z]);
-    const double inv_dt = 1.0 / sp.dt;
+    const double inv_dt = sp.inv_dt;
     double2 b;
     if (!sp.weak_form) {
         b.x = ((hx.x + hy.x) + dz.x) * inv_dt * whz;
