@@ -1451,7 +1451,7 @@ int dns3d_set_state(dns3d_handle* h, const double* u, const double* v, const dou
     if (in_place) {
         Fields sp{};
         for (int i = 0; i < n; ++i) sp.p[i] = dst[idx[i]];
-        CK(h, fft_r2c(h->fft, g, hv, sp, n, g.nz, h->stream));
+        CK(h, fft_r2c(h->fft, g, hv, sp, n, g.nz, h->stream, 0, true));
         n = 0;  // nothing left for the copies below
     }
     const int na = (n + 1) / 2;

@@ -120,8 +120,10 @@ cudaError_t fft_fx_y(Fields src, Fields dst, const GridDev& g, int nplanes, int 
 // dst2 (entries may be null): a second destination of the same values
 cudaError_t fft_fx_c2r_x(Fields src, RFields dst, RFields dst2, const GridDev& g, int nrows, int nf,
                          const longlong2* tw_n, const longlong2* tw_nx, cudaStream_t s);
+// host_src: src is host memory mapped for the device (plain loads instead of
+// bulk copies)
 cudaError_t fft_fx_r2c_x(RFields src, Fields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
-                         const longlong2* tw_nx, cudaStream_t s);
+                         const longlong2* tw_nx, bool host_src, cudaStream_t s);
 
 cudaError_t fft_setup(FftCtx& ctx, const GridDev& g);
 void fft_release(FftCtx& ctx);
@@ -137,7 +139,7 @@ cudaError_t fft_c2r_copy(const FftCtx& ctx, const GridDev& g, Fields spec, RFiel
 // completed (the others keep the x transform's output): for sources that the
 // 2/3 filter truncates at kx_max = ncol - 1 anyway.
 cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf,
-                    int nplanes, cudaStream_t s, int ncol = 0);
+                    int nplanes, cudaStream_t s, int ncol = 0, bool host_src = false);
 // FP32 versions (same transform definitions), scratch ctx.tmp32.
 cudaError_t fft_c2r32(const FftCtx& ctx, const GridDev& g, FFields spec, FRFields phys, int nf,
                       int nplanes, cudaStream_t s);

@@ -401,13 +401,14 @@ cudaError_t c2r_impl(const FftCtx& ctx, const GridDev& g, FieldsT<typename Cx<T>
 template <typename T>
 cudaError_t r2c_impl(const FftCtx& ctx, const GridDev& g, FieldsT<T> phys, FieldsT<typename Cx<T>::type> spec,
                      int nf, int nplanes, cudaStream_t s, const typename Cx<T>::type* twy,
-                     const typename Cx<T>::type* twx2, const typename Cx<T>::type* twx, int ncol) {
+                     const typename Cx<T>::type* twx2, const typename Cx<T>::type* twx, int ncol,
+                     bool host_src = false) {
     using C = typename Cx<T>::type;
     const int nrows = nplanes * g.ny;
     if (ncol <= 0 || ncol > g.nxhp) ncol = g.nxhp;
     if constexpr (sizeof(T) == 8) {
         if (ctx.fx) {
-            cudaError_t e = fft_fx_r2c_x(phys, spec, g, nrows, nf, ctx.twq_nx2, ctx.twq_nx, s);
+            cudaError_t e = fft_fx_r2c_x(phys, spec, g, nrows, nf, ctx.twq_nx2, ctx.twq_nx, host_src, s);
             if (e) return e;
             if (ctx.hook) ctx.hook(ctx.hook_ctx, "fft_x_r2c");
             e = fft_fx_y<-1>(spec, spec, g, nplanes, ncol, nf, ctx.twq_ny, s);
@@ -459,9 +460,9 @@ cudaError_t fft_c2r_copy(const FftCtx& ctx, const GridDev& g, Fields spec, RFiel
 }
 
 cudaError_t fft_r2c(const FftCtx& ctx, const GridDev& g, RFields phys, Fields spec, int nf, int nplanes,
-                    cudaStream_t s, int ncol) {
+                    cudaStream_t s, int ncol, bool host_src) {
     if (nf > kMaxFields) return cudaErrorInvalidValue;
-    return r2c_impl<double>(ctx, g, phys, spec, nf, nplanes, s, ctx.tw_ny, ctx.tw_nx2, ctx.tw_nx, ncol);
+    return r2c_impl<double>(ctx, g, phys, spec, nf, nplanes, s, ctx.tw_ny, ctx.tw_nx2, ctx.tw_nx, ncol, host_src);
 }
 
 cudaError_t fft_c2r32(const FftCtx& ctx, const GridDev& g, FFields spec, FRFields phys, int nf, int nplanes,

@@ -16,6 +16,7 @@
 #include "cvt.cuh"
 #include "dns3d_internal.cuh"
 #include "ragged.cuh"
+#include "tc.cuh"
 
 namespace dns3d {
 
@@ -515,7 +516,7 @@ template <int N>
 __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& dst, const RFields& dst2,
                                               const GridDev& g, int nrows, const fx2* __restrict__ tw_n,
                                               const fx2* __restrict__ tw_nx, int bx, int f, fx2* buf,
-                                              unsigned* emax) {
+                                              unsigned* emax, uint64_t* mbar) {
     constexpr int RX = per_cta(N);
     constexpr int LD = ld_of<fx2>(N);
     constexpr int B = fx_bits(N, 2);
@@ -527,29 +528,36 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
     constexpr int ITERS = RX * N / kThreads;
     static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
     if (threadIdx.x < RX) emax[threadIdx.x] = 1u;
-    // the row's nx/2+1 inputs go to shared memory as they are (FP64 bits in
-    // the fixed-point slots; slot N holds kx = nx/2), so no thread holds them
-    // in registers across the exponent reduction
+    // The CTA's rows are contiguous in memory and the fixed-point slots are
+    // as wide as a complex FP64 value, so one bulk copy (TMA engine, completion
+    // on an mbarrier) stages the rows' nx/2+1 inputs into the slots as they
+    // are; a copy that does not land within the wait limit marks the rows
+    // non-finite.
+    const int nvalid = min(RX, nrows - row0);
+    if (threadIdx.x == 0) tc_mbar_init(mbar);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)nvalid * (uint32_t)nxhp * (uint32_t)sizeof(fx2);
+        tc_mbar_expect(mbar, bytes);
+        tc_bulk_g2s(buf, s + (size_t)row0 * nxhp, bytes, mbar);
+    }
+    const bool landed = __syncthreads_and(tc_mbar_wait(mbar, 0, 1 << 22));
     unsigned e[ITERS];
 #pragma unroll
     for (int it = 0; it < ITERS; ++it) {
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
-        double2 a = make_double2(0.0, 0.0), b = a;
-        if (row0 + r < nrows) {
-            const double2* row = s + (size_t)(row0 + r) * nxhp;
-            a = row[k];
-            if (k == 0) b = row[N];
-        }
+        fx2 ra = buf[r * LD + sw<fx2>(k)], rb = mk<fx2>(0, 0);
         if (k == 0) {  // Im of kx = 0 and kx = nx/2 is ignored
-            a.y = 0.0;
-            b.y = 0.0;
-            buf[r * LD + sw<fx2>(N)] = mk<fx2>(__double_as_longlong(b.x), __double_as_longlong(b.y));
+            rb = buf[r * LD + sw<fx2>(N)];
+            ra.y = 0;
+            rb.y = 0;
         }
-        buf[r * LD + sw<fx2>(k)] = mk<fx2>(__double_as_longlong(a.x), __double_as_longlong(a.y));
-        e[it] = max(fx_expo(a), fx_expo(b));
+        e[it] = landed ? max(fx_expo(__longlong_as_double(ra.x)), max(fx_expo(__longlong_as_double(ra.y)),
+                                                                      max(fx_expo(__longlong_as_double(rb.x)),
+                                                                          fx_expo(__longlong_as_double(rb.y)))))
+                       : 0x7FFu;
     }
-    __syncthreads();
 #pragma unroll
     for (int it = 0; it < ITERS; ++it) fx_key_max(emax, (threadIdx.x + it * kThreads) / N, e[it]);
     __syncthreads();
@@ -559,7 +567,11 @@ __device__ __forceinline__ void c2r_x_body_fx(const Fields& src, const RFields& 
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
         const int rsb = 53 - B + (int)emax[r];
-        const fx2 ra = buf[r * LD + sw<fx2>(k)], rb = buf[r * LD + sw<fx2>(N - k)];
+        fx2 ra = buf[r * LD + sw<fx2>(k)], rb = buf[r * LD + sw<fx2>(N - k)];
+        if (k == 0) {  // Im of kx = 0 and kx = nx/2 is ignored
+            ra.y = 0;
+            rb.y = 0;
+        }
         const fx2 a = mk<fx2>(fx_from(__longlong_as_double(ra.x), rsb), fx_from(__longlong_as_double(ra.y), rsb));
         const fx2 b = mk<fx2>(fx_from(__longlong_as_double(rb.x), rsb), fx_from(__longlong_as_double(rb.y), rsb));
         const fx2 sm = mk<fx2>(a.x + b.x, a.y - b.y);
@@ -605,7 +617,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_c2r_x_fx(Fields src, RFields ds
                                                           const fx2* __restrict__ tw_nx) {
     __shared__ fx2 buf[per_cta(N) * ld_of<fx2>(N)];
     __shared__ unsigned emax[per_cta(N)];
-    c2r_x_body_fx<N>(src, dst, dst2, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax);
+    __shared__ uint64_t mbar;
+    c2r_x_body_fx<N>(src, dst, dst2, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax, &mbar);
 }
 
 // r2c along x in fixed point: z[m] = x[2m] + i x[2m+1] of one row scaled
@@ -615,9 +628,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_c2r_x_fx(Fields src, RFields ds
 template <int N>
 __device__ __forceinline__ void r2c_x_body_fx(const RFields& src, const Fields& dst, const GridDev& g, int nrows,
                                               const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx, int bx,
-                                              int f, fx2* buf, unsigned* emax) {
+                                              int f, fx2* buf, unsigned* emax, uint64_t* mbar, bool bulk) {
     constexpr int RX = per_cta(N);
-    constexpr int LD = ld_of<fx2>(N);
+    constexpr int LD = N;  // rows back to back, as in memory (no kx = nx/2 slot needed)
     constexpr int B = fx_bits(N, 2);
     const int row0 = bx * RX;
     const double2* __restrict__ s = reinterpret_cast<const double2*>(field_ptr(src, f));
@@ -625,18 +638,47 @@ __device__ __forceinline__ void r2c_x_body_fx(const RFields& src, const Fields& 
     constexpr int ITERS = RX * N / kThreads;
     static_assert((RX * N) % kThreads == 0, "rows split evenly over the threads");
     if (threadIdx.x < RX) emax[threadIdx.x] = 1u;
-    double2 v[ITERS];
+    // the rows' FP64 values go into the fixed-point slots as they are (z[m] =
+    // x[2m] + i x[2m+1] is the row's own memory layout, and the CTA's rows are
+    // contiguous): from device memory by one bulk copy (TMA engine,
+    // completion on an mbarrier; a copy that does not land within the wait
+    // limit marks the rows non-finite), from host memory the device maps
+    // (pinned buffers read in place) by plain loads
+    const int nvalid = min(RX, nrows - row0);
+    bool landed = true;
+    if (bulk) {
+        if (threadIdx.x == 0) tc_mbar_init(mbar);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t bytes = (uint32_t)nvalid * (uint32_t)(N * sizeof(fx2));
+            tc_mbar_expect(mbar, bytes);
+            tc_bulk_g2s(buf, s + (size_t)row0 * N, bytes, mbar);
+        }
+        landed = __syncthreads_and(tc_mbar_wait(mbar, 0, 1 << 22));
+    } else {
+        double2 h[ITERS];
+#pragma unroll
+        for (int it = 0; it < ITERS; ++it) {
+            const int t = threadIdx.x + it * kThreads;
+            const int r = t / N, k = t - r * N;
+            h[it] = r < nvalid ? s[(size_t)(row0 + r) * N + k] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int it = 0; it < ITERS; ++it) {
+            const int t = threadIdx.x + it * kThreads;
+            buf[(t / N) * LD + sw<fx2>(t % N)] = mk<fx2>(__double_as_longlong(h[it].x), __double_as_longlong(h[it].y));
+        }
+        __syncthreads();
+    }
+    fx2 v[ITERS];
 #pragma unroll
     for (int it = 0; it < ITERS; ++it) {
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
-        v[it] = (row0 + r < nrows) ? s[(size_t)(row0 + r) * N + k] : make_double2(0.0, 0.0);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int it = 0; it < ITERS; ++it) {
-        const int t = threadIdx.x + it * kThreads;
-        fx_key_max(emax, t / N, fx_expo(v[it]));
+        v[it] = buf[r * LD + sw<fx2>(k)];
+        fx_key_max(emax, r,
+                   landed ? max(fx_expo(__longlong_as_double(v[it].x)), fx_expo(__longlong_as_double(v[it].y)))
+                          : 0x7FFu);
     }
     __syncthreads();
 #pragma unroll
@@ -644,7 +686,8 @@ __device__ __forceinline__ void r2c_x_body_fx(const RFields& src, const Fields& 
         const int t = threadIdx.x + it * kThreads;
         const int r = t / N, k = t - r * N;
         const int rsb = 53 - B + (int)emax[r];
-        buf[r * LD + sw<fx2>(k)] = mk<fx2>(fx_from(v[it].x, rsb), fx_from(v[it].y, rsb));
+        buf[r * LD + sw<fx2>(k)] = mk<fx2>(fx_from(__longlong_as_double(v[it].x), rsb),
+                                           fx_from(__longlong_as_double(v[it].y), rsb));
     }
     __syncthreads();
     ct_fft<N, 1, -1, RX, LD>(buf, tw_n);
@@ -667,10 +710,12 @@ __device__ __forceinline__ void r2c_x_body_fx(const RFields& src, const Fields& 
 
 template <int N>
 __global__ void __launch_bounds__(kThreads) k_r2c_x_fx(RFields src, Fields dst, GridDev g, int nrows,
-                                                       const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx) {
+                                                       const fx2* __restrict__ tw_n, const fx2* __restrict__ tw_nx,
+                                                       int bulk) {
     __shared__ fx2 buf[per_cta(N) * ld_of<fx2>(N)];
     __shared__ unsigned emax[per_cta(N)];
-    r2c_x_body_fx<N>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax);
+    __shared__ uint64_t mbar;
+    r2c_x_body_fx<N>(src, dst, g, nrows, tw_n, tw_nx, blockIdx.x, blockIdx.y, buf, emax, &mbar, bulk != 0);
 }
 
 // ------------------------------------------------------------------ ragged stages
@@ -792,6 +837,7 @@ struct RsC2RFx {
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
         __shared__ fx2 buf[ct_buf_max()];
         __shared__ unsigned emax[64];
+        __shared__ uint64_t mbar;
         const int gx = d.gx[kRsFftC2R];
         const int f = b / gx, bx = b - f * gx;
         const fx2* twn = static_cast<const fx2*>(d.tw_nx2);
@@ -800,7 +846,7 @@ struct RsC2RFx {
 #define X_CASE(n)                                                                                               \
     case n:                                                                                                     \
         c2r_x_body_fx<n>(one_field<double2>(d.tmp, f), one_field<double>(d.phys, f), RFields{}, d.g,           \
-                         d.g.nz * d.g.ny, twn, twx, bx, 0, buf, emax);                                          \
+                         d.g.nz * d.g.ny, twn, twx, bx, 0, buf, emax, &mbar);                                   \
         break;
             DNS3D_CT_X_LENGTHS(X_CASE)
 #undef X_CASE
@@ -813,6 +859,7 @@ struct RsR2CFx {
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
         __shared__ fx2 buf[ct_buf_max()];
         __shared__ unsigned emax[64];
+        __shared__ uint64_t mbar;
         const int gx = d.gx[kRsFftR2C];
         const int f = b / gx, bx = b - f * gx;
         const fx2* twn = static_cast<const fx2*>(d.tw_nx2);
@@ -821,7 +868,7 @@ struct RsR2CFx {
 #define X_CASE(n)                                                                                              \
     case n:                                                                                                    \
         r2c_x_body_fx<n>(one_field<double>(d.phys, f), one_field<double2>(d.src, f), d.g, d.g.nz * d.g.ny, twn, \
-                         twx, bx, 0, buf, emax);                                                               \
+                         twx, bx, 0, buf, emax, &mbar, true);                                                  \
         break;
             DNS3D_CT_X_LENGTHS(X_CASE)
 #undef X_CASE
@@ -898,10 +945,10 @@ void launch_c2r_fx(Fields src, RFields dst, RFields dst2, const GridDev& g, int 
 
 template <int N>
 void launch_r2c_fx(RFields src, Fields dst, const GridDev& g, int nrows, int nf, const fx2* tw_n, const fx2* tw_nx,
-                   cudaStream_t s) {
+                   bool host_src, cudaStream_t s) {
     constexpr int RX = per_cta(N);
     dim3 grid((nrows + RX - 1) / RX, nf);
-    k_r2c_x_fx<N><<<grid, kThreads, 0, s>>>(src, dst, g, nrows, tw_n, tw_nx);
+    k_r2c_x_fx<N><<<grid, kThreads, 0, s>>>(src, dst, g, nrows, tw_n, tw_nx, host_src ? 0 : 1);
 }
 
 }  // namespace
@@ -985,10 +1032,10 @@ cudaError_t fft_fx_c2r_x(Fields src, RFields dst, RFields dst2, const GridDev& g
 }
 
 cudaError_t fft_fx_r2c_x(RFields src, Fields dst, const GridDev& g, int nrows, int nf, const longlong2* tw_n,
-                         const longlong2* tw_nx, cudaStream_t s) {
+                         const longlong2* tw_nx, bool host_src, cudaStream_t s) {
     switch (g.nxh) {
 #define X_CASE(n) \
-    case n: launch_r2c_fx<n>(src, dst, g, nrows, nf, tw_n, tw_nx, s); break;
+    case n: launch_r2c_fx<n>(src, dst, g, nrows, nf, tw_n, tw_nx, host_src, s); break;
         DNS3D_CT_X_LENGTHS(X_CASE)
 #undef X_CASE
         default: return cudaErrorInvalidValue;
