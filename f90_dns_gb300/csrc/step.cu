@@ -661,16 +661,17 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
         if (threadIdx.x == 0) {
             *landed = tc_mbar_wait(&mbar[1], par, 1 << 22) ? 1 : 0;
             if (*landed && !ops.tc_stall) {
-                const uint32_t a0 = tc_smem_u32(sA), b0 = tc_smem_u32(sB);
+                // the descriptors differ only in their start address (16-byte
+                // units in the low field): one add per MMA
                 const uint32_t sbo = (uint32_t)t.k16 * 16;
                 const int nks = t.k16 / 16;
+                const uint64_t da0 = tc_desc(tc_smem_u32(sA), 128, sbo), db0 = tc_desc(tc_smem_u32(sB), 128, sbo);
                 for (int sa = 0; sa < kTcSlices; ++sa) {
                     const uint32_t idesc = tc_idesc(kTcN * (kTcSlices - sa));
-                    for (int ks = 0; ks < nks; ++ks) {
-                        const uint64_t da = tc_desc(a0 + (uint32_t)(sa * a_halves) * 2 + ks * 256, 128, sbo);
-                        const uint64_t db = tc_desc(b0 + ks * 256, 128, sbo);
-                        tc_mma(tmem + (uint32_t)(sa * kTcN), da, db, idesc, (sa > 0 || ks > 0) ? 1u : 0u);
-                    }
+                    const uint64_t das = da0 + (uint64_t)((sa * a_halves * 2) >> 4);
+                    for (int ks = 0; ks < nks; ++ks)
+                        tc_mma(tmem + (uint32_t)(sa * kTcN), das + (uint64_t)(16 * ks), db0 + (uint64_t)(16 * ks), idesc,
+                               (sa > 0 || ks > 0) ? 1u : 0u);
                 }
             }
             if (!ops.tc_stall) tc_commit(&mbar[0]);  // also when nothing was issued: the waiters are released
@@ -881,16 +882,17 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         if (tid == 0) {
             if (tile == tile0) *landed = tc_mbar_wait(&mbar[1], 0, 1 << 22) ? 1 : 0;
             if (*landed && !ops.tc_stall) {
-                const uint32_t a0 = tc_smem_u32(sA), b0 = tc_smem_u32(sB);
+                // the descriptors differ only in their start address (16-byte
+                // units in the low field): one add per MMA
                 const uint32_t sbo = (uint32_t)t.k16 * 16;
                 const int nks = t.k16 / 16;
+                const uint64_t da0 = tc_desc(tc_smem_u32(sA), 128, sbo), db0 = tc_desc(tc_smem_u32(sB), 128, sbo);
                 for (int sa = 0; sa < kTcSlices; ++sa) {
                     const uint32_t idesc = tc_idesc(kTcVortCols * (kTcSlices - sa));
-                    for (int ks = 0; ks < nks; ++ks) {
-                        const uint64_t da = tc_desc(a0 + (uint32_t)(sa * a_halves) * 2 + ks * 256, 128, sbo);
-                        const uint64_t db = tc_desc(b0 + ks * 256, 128, sbo);
-                        tc_mma(tmem + (uint32_t)(sa * kTcVortCols), da, db, idesc, (sa > 0 || ks > 0) ? 1u : 0u);
-                    }
+                    const uint64_t das = da0 + (uint64_t)((sa * a_halves * 2) >> 4);
+                    for (int ks = 0; ks < nks; ++ks)
+                        tc_mma(tmem + (uint32_t)(sa * kTcVortCols), das + (uint64_t)(16 * ks), db0 + (uint64_t)(16 * ks),
+                               idesc, (sa > 0 || ks > 0) ? 1u : 0u);
                 }
             }
             if (!ops.tc_stall) tc_commit(&mbar[0]);
