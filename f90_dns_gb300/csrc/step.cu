@@ -1219,10 +1219,6 @@ __global__ void __launch_bounds__(256) k_pressure(GridDev g, Ops ops, StepParams
     pressure_body(g, ops, sp, US, VS, WS, PHI, tc, blockIdx.x);
 }
 
-__device__ __forceinline__ double warp_max(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
