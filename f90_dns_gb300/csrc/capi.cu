@@ -503,21 +503,25 @@ int run_pressure(dns3d_handle* h) {
     return DNS3D_OK;
 }
 
-int run_correction(dns3d_handle* h) {
+// pressure_correction_3d; with fuse_bc the projection also writes the wall
+// planes of u, v, w as apply_boundary_conditions_3d does (the fused step)
+int run_correction(dns3d_handle* h, bool fuse_bc = false) {
     h->phys_valid = 0;
+    StepParams sp = h->sp;
+    sp.bc_walls = fuse_bc ? 1 : 0;
     if (h->mixed) {
-        CK(h, launch_correction_mixed(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->U, h->V, h->W,
+        CK(h, launch_correction_mixed(h->g, h->ops, sp, h->US, h->VS, h->WS, h->PHI, h->PHIZ, h->U, h->V, h->W,
                                       h->P, h->GP, h->stream));
         mark(h, "correction_mixed");
         return DNS3D_OK;
     }
     if (h->corr_tc) {
-        CK(h, launch_correction_tc(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
+        CK(h, launch_correction_tc(h->g, h->ops, sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
                                    h->GP, h->d_tcerr, h->stream));
         mark(h, "pressure_correction_tc");
         return DNS3D_OK;
     }
-    CK(h, launch_correction(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
+    CK(h, launch_correction(h->g, h->ops, sp, h->US, h->VS, h->WS, h->PHI, h->U, h->V, h->W, h->P,
                             h->GP, h->stream));
     mark(h, "pressure_correction");
     return DNS3D_OK;
@@ -538,8 +542,8 @@ int run_step_body(dns3d_handle* h) {
     if ((rc = run_source_terms(h))) return rc;
     if ((rc = run_viscous(h))) return rc;
     if ((rc = run_pressure(h))) return rc;
-    if ((rc = run_correction(h))) return rc;
-    return run_bc(h);
+    // apply_boundary_conditions_3d in the projection's pass
+    return run_correction(h, true);
 }
 
 void release(dns3d_handle* h) {
@@ -1982,6 +1986,7 @@ RunDesc make_desc(const dns3d_handle* h) {
     }
     d.mx = h->mx;
     d.sp = h->sp;
+    d.sp.bc_walls = 1;  // batches take whole steps: the projection stage writes the wall planes
     d.pp = h->pp;
     d.pi = h->d_pi;
     d.tcerr = h->d_tcerr;
@@ -2164,8 +2169,7 @@ cudaError_t group_capture(dns3d_batch::Group& G, int* launches) {
     stage(kRsPresRhs, lane);
     stage(kRsPres, lane);
     if (G.mixed && !ce) ce = cudaStreamWaitEvent(lane, G.side_join, 0);
-    stage(kRsCorr, lane);
-    stage(kRsBc, lane);
+    stage(kRsCorr, lane);  // also writes the wall planes (RunDesc sp.bc_walls)
     return ce;
 }
 

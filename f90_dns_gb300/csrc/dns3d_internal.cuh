@@ -158,6 +158,8 @@ struct StepParams {
     int weak_form;        // use_weak_form_divergence
     int rhs_only;         // viscous/pressure kernels: write the right-hand sides (for jacgs), not the solutions
     int cn_identity;      // Crank-Nicolson: explicit half folded into the implicit solve (step.cu)
+    int bc_walls;         // projection: write the wall planes of u, v, w as zero (apply_boundary_conditions_3d
+                          // fused into it; set by the fused step, not by the five-stage calls)
 };
 
 // z-operators in parity-folded form (see step.cu): for nz levels,

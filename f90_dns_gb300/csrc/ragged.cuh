@@ -29,8 +29,7 @@ enum RaggedStage {
     kRsFftYFwd,   // forward y pass of the products (2/3-filtered columns only)
     kRsVisc,      // viscous step (mixed: the FP32 mode tiles)
     kRsPres,      // pressure solve (mixed: the FP32 mode tiles)
-    kRsCorr,      // projection and wall gradients of p
-    kRsBc,        // wall planes of u, v, w
+    kRsCorr,      // projection (zero wall planes of u, v, w) and wall gradients of p
     // mixed form only: the FP64 mode (0,0) of the viscous step, then its pinned
     // Poisson solve and dphi/dz, one CTA per run, on a forked stream beside
     // kRsVisc and kRsPres (mode (0,0) of w* is all the pinned solve reads)

@@ -984,6 +984,18 @@ struct VortTcOp {
     }
 };
 
+// u, v, w of the projection at level z into U, V, W[o]; with sp.bc_walls the
+// wall planes get apply_boundary_conditions_3d's zeros (3D:1953-1972) in the
+// same pass.
+__device__ __forceinline__ void store_projection(const StepParams& sp, int z, int nz, size_t o, double2 u,
+                                                 double2 v, double2 w, double2* __restrict__ U,
+                                                 double2* __restrict__ V, double2* __restrict__ W) {
+    if (sp.bc_walls && (z == 0 || z == nz - 1)) u = v = w = make_double2(0.0, 0.0);
+    U[o] = u;
+    V[o] = v;
+    W[o] = w;
+}
+
 // pressure_correction_3d from D1.phi, as correction_body forms it
 struct CorrTcOp {
     static constexpr int kFields = 1;
@@ -1008,9 +1020,9 @@ struct CorrTcOp {
             const double2 ph = PHI[o];
             const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
             const double2 us = US[o], vs = VS[o], ws = WS[o];
-            U[o] = make_double2(us.x - dt * px.x, us.y - dt * px.y);
-            V[o] = make_double2(vs.x - dt * py.x, vs.y - dt * py.y);
-            W[o] = make_double2(ws.x - dt * d.x, ws.y - dt * d.y);
+            store_projection(sp, z, g.nz, o, make_double2(us.x - dt * px.x, us.y - dt * px.y),
+                             make_double2(vs.x - dt * py.x, vs.y - dt * py.y),
+                             make_double2(ws.x - dt * d.x, ws.y - dt * d.y), U, V, W);
             double2 pp = P[o];
             pp.x += ph.x;
             pp.y += ph.y;
@@ -1430,9 +1442,9 @@ __device__ __forceinline__ void correction_body(GridDev g, Ops ops, StepParams s
             const double2 ph = PHI[o];
             const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
             const double2 us = US[o], vs = VS[o], ws = WS[o];
-            U[o] = make_double2(us.x - dt * px.x, us.y - dt * px.y);
-            V[o] = make_double2(vs.x - dt * py.x, vs.y - dt * py.y);
-            W[o] = make_double2(ws.x - dt * d.x, ws.y - dt * d.y);
+            store_projection(sp, z, g.nz, o, make_double2(us.x - dt * px.x, us.y - dt * px.y),
+                             make_double2(vs.x - dt * py.x, vs.y - dt * py.y),
+                             make_double2(ws.x - dt * d.x, ws.y - dt * d.y), U, V, W);
             double2 pp = P[o];
             pp.x += ph.x;
             pp.y += ph.y;
@@ -2134,9 +2146,9 @@ __device__ __forceinline__ void correction_mixed_body(GridDev g, Ops ops, StepPa
         const double2 ph = PHI[o], pz = PHIZ[o];
         const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
         const double2 us = US[o], vs = VS[o], ws = WS[o];
-        U[o] = make_double2(us.x - dt * px.x, us.y - dt * px.y);
-        V[o] = make_double2(vs.x - dt * py.x, vs.y - dt * py.y);
-        W[o] = make_double2(ws.x - dt * pz.x, ws.y - dt * pz.y);
+        store_projection(sp, z, g.nz, o, make_double2(us.x - dt * px.x, us.y - dt * px.y),
+                         make_double2(vs.x - dt * py.x, vs.y - dt * py.y),
+                         make_double2(ws.x - dt * pz.x, ws.y - dt * pz.y), U, V, W);
         double2 pp = P[o];
         pp.x += ph.x;
         pp.y += ph.y;
@@ -2890,11 +2902,6 @@ struct RsCorr32 {
     }
 };
 
-struct RsBc {
-    static constexpr int kMinCtas = 4;
-    static __device__ __forceinline__ void run(const RunDesc& d, int b) { apply_bc_body(d.g, d.U, d.V, d.W, b); }
-};
-
 }  // namespace
 
 StageKernel ragged_kernel(int stage, bool mixed, int variant) {
@@ -2909,7 +2916,6 @@ StageKernel ragged_kernel(int stage, bool mixed, int variant) {
         case kRsPresRhs: return k_stage<RsPresRhs64>;
         case kRsCorr:
             return mixed ? k_stage<RsCorr32> : ((variant & kRvCorrTc) ? k_stage<RsCorr64Tc> : k_stage<RsCorr64>);
-        case kRsBc: return k_stage<RsBc>;
         case kRsViscMean: return k_stage<RsViscMean>;
         case kRsPresMean: return k_stage<RsPresMean>;
         case kRsFftYInv:
@@ -2937,7 +2943,6 @@ void ragged_geometry(RunDesc& d) {
     d.gx[kRsFftR2C] = d.gx[kRsFftC2R];
     d.gx[kRsFftYFwd] = cdiv((long long)g.nz * d.ncol, cy);
     d.gx[kRsCorr] = cdiv((long long)g.nz * g.nm, 4 * kStageThreads);
-    d.gx[kRsBc] = cdiv(2LL * g.nm, kStageThreads);
     d.gx[kRsVisc] = tc_q_per_cta(d.ops.nq);  // operator indices per CTA of the tensor-core viscous body
     d.vort_chunk = tc_dz_chunk(g.nm, kTcVortModes);  // tiles per CTA of the tensor-core z-derivative bodies
     d.corr_chunk = tc_dz_chunk(g.nm, kTcCorrModes);
@@ -2966,8 +2971,7 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
         case kRsFftC2R: return 6 * d.gx[stage];
         case kRsFftR2C:
         case kRsFftYFwd: return 3 * d.gx[stage];
-        case kRsProd:
-        case kRsBc: return d.gx[stage];
+        case kRsProd: return d.gx[stage];
         case kRsVisc:
             if (!mixed && (ragged_variant(d) & kRvViscTc)) return (d.ops.nq + d.gx[kRsVisc] - 1) / d.gx[kRsVisc];
             return tiles;

@@ -74,7 +74,7 @@ def test_ensemble_ragged_launches_and_loose_runs(built_lib):
         ens.step(4)
         states = [ens.run(i).get_state(walls=False) for i in range(len(ens))]
     assert ragged == 5
-    # ten stage launches per FP64 group, twelve per mixed group, plus the loose runs' own launches
+    # nine stage launches per FP64 group, eleven per mixed group, plus the loose runs' own launches
     assert launches > 20
     for cfg, st in zip(cfgs, states):
         solo, _ = _solo(cfg, 4)
@@ -87,7 +87,7 @@ def test_ensemble_launches_per_step_independent_of_size(built_lib):
         cfgs = [config_from(d, precision=PREC_MIXED) for d in ensemble_draws(n, seed=2)]
         with Ensemble(cfgs) as ens:
             launches, ragged = ens.info()
-        assert (launches, ragged) == (12, n)  # ten stages + the mixed mode (0,0) pair
+        assert (launches, ragged) == (11, n)  # nine stages + the mixed mode (0,0) pair
 
 
 def test_batch_over_existing_runs_with_pi_control(built_lib):
