@@ -408,6 +408,19 @@ int run_source_terms(dns3d_handle* h) {
 
 int run_source_terms_fp64(dns3d_handle* h, double2* const* in) {
     const GridDev& g = h->g;
+    // u, v, w to physical space on the side stream while the vorticity runs:
+    // they need only the state, and the vorticity kernel leaves SMs free
+    // (scratch slots 0-2 and phys[0..2] here, 3-5 and phys[3..5] below)
+    CK(h, fork_side(h, 1));
+    {
+        Fields su{};
+        RFields pu{};
+        for (int f = 0; f < 3; ++f) {
+            su.p[f] = in[f];
+            pu.p[f] = h->phys[f];
+        }
+        CK(h, fft_c2r(h->fft, g, su, pu, 3, g.nz, side_stream(h), 0));
+    }
     // vorticity into the u*,v*,w* buffers (free until the viscous step)
     if (h->vort_tc) {
         CK(h, launch_vorticity_tc(g, h->ops, in[0], in[1], in[2], h->US, h->VS, h->WS, h->d_tcerr, h->stream));
@@ -417,14 +430,16 @@ int run_source_terms_fp64(dns3d_handle* h, double2* const* in) {
         mark(h, "vorticity");
     }
     Fields spec{};
-    spec.p[0] = in[0]; spec.p[1] = in[1]; spec.p[2] = in[2];
-    spec.p[3] = h->US; spec.p[4] = h->VS; spec.p[5] = h->WS;
+    spec.p[0] = h->US; spec.p[1] = h->VS; spec.p[2] = h->WS;
     RFields phys{};
-    for (int f = 0; f < 6; ++f) phys.p[f] = h->phys[f];
-    CK(h, fft_c2r(h->fft, g, spec, phys, 6, g.nz, h->stream));
+    for (int f = 0; f < 3; ++f) phys.p[f] = h->phys[3 + f];
+    CK(h, fft_c2r(h->fft, g, spec, phys, 3, g.nz, h->stream, 3));
+    CK(h, join_side(h, 1));
+    RFields all{};  // u, v, w, ox, oy, oz in physical space
+    for (int f = 0; f < 6; ++f) all.p[f] = h->phys[f];
     RFields prod{};
     for (int f = 0; f < 3; ++f) prod.p[f] = h->phys[f];
-    CK(h, launch_products(g, phys, prod, h->stream));
+    CK(h, launch_products(g, all, prod, h->stream));
     mark(h, "products");
     Fields src{};
     src.p[0] = h->SU; src.p[1] = h->SV; src.p[2] = h->SW;

@@ -127,9 +127,11 @@ cudaError_t fft_fx_r2c_x(RFields src, Fields dst, const GridDev& g, int nrows, i
 
 cudaError_t fft_setup(FftCtx& ctx, const GridDev& g);
 void fft_release(FftCtx& ctx);
-// spec[f] (spectral, read only) -> phys[f]; uses ctx.tmp (nf <= tmp_fields).
+// spec[f] (spectral, read only) -> phys[f]; uses the ctx.tmp slots slot0 ..
+// slot0 + nf - 1 (at most tmp_fields), so that two calls on different slots can
+// run concurrently.
 cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, int nf,
-                    int nplanes, cudaStream_t s);
+                    int nplanes, cudaStream_t s, int slot0 = 0);
 // The same into phys[f] and into copy[f] as well (host memory the device
 // can address, for example), in one pass; only where ctx.fx is set
 // (cudaErrorNotSupported otherwise).

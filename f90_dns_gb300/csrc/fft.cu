@@ -438,10 +438,10 @@ cudaError_t r2c_impl(const FftCtx& ctx, const GridDev& g, FieldsT<T> phys, Field
 }  // namespace
 
 cudaError_t fft_c2r(const FftCtx& ctx, const GridDev& g, Fields spec, RFields phys, int nf, int nplanes,
-                    cudaStream_t s) {
-    if (nf > ctx.tmp_fields || nf > kMaxFields) return cudaErrorInvalidValue;
+                    cudaStream_t s, int slot0) {
+    if (slot0 < 0 || slot0 + nf > ctx.tmp_fields || nf > kMaxFields) return cudaErrorInvalidValue;
     Fields tmp{};
-    for (int f = 0; f < nf; ++f) tmp.p[f] = ctx.tmp + (size_t)f * g.nm * g.nz;
+    for (int f = 0; f < nf; ++f) tmp.p[f] = ctx.tmp + (size_t)(slot0 + f) * g.nm * g.nz;
     return c2r_impl<double>(ctx, g, spec, phys, tmp, nf, nplanes, s, ctx.tw_ny, ctx.tw_nx2, ctx.tw_nx);
 }
 
