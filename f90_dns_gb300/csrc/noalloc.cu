@@ -15,6 +15,7 @@
 // cudaFree or any other allocating routine.
 #include <cmath>
 #include <mutex>
+#include <vector>
 
 #include "dns3d_internal.cuh"
 
@@ -36,39 +37,21 @@ struct Weights {
     double w[DNS3D_NOALLOC_MAX_NZ];
 };
 
-// LGL quadrature weights of n nodes (lgl_module.f90:30-80), computed into a
-// fixed-size array so that the call needs no heap memory.
+// LGL quadrature weights of n nodes from the library's own setup routine
+// (lgl_nodes_weights, lgl_module.f90:30-80), copied into the by-value kernel
+// argument.  The host vector is host memory; no device memory is allocated.
 void lgl_weights_fixed(int n, Weights& out) {
-    const double pi = 3.14159265358979323846;
-    if (n == 2) { out.w[0] = out.w[1] = 1.0; return; }
-    out.w[0] = out.w[n - 1] = 2.0 / (double)(n * (n - 1));
-    for (int i = 2; i <= n - 1; ++i) {
-        double x = -std::cos(pi * (double)(i - 1) / (double)(n - 1));
-        for (int it = 0; it < 100; ++it) {
-            const double xo = x;
-            double p0 = 1.0, dp0 = 0.0, d2p0 = 0.0, p1 = x, dp1 = 1.0, d2p1 = 0.0;
-            for (int k = 2; k <= n - 1; ++k) {
-                const double a = (double)(2 * k - 1), b = (double)(k - 1), c = (double)k;
-                const double p2 = (a * x * p1 - b * p0) / c;
-                const double dp2 = (a * (x * dp1 + p1) - b * dp0) / c;
-                const double d2p2 = (a * (x * d2p1 + 2.0 * dp1) - b * d2p0) / c;
-                p0 = p1; p1 = p2; dp0 = dp1; dp1 = dp2; d2p0 = d2p1; d2p1 = d2p2;
-            }
-            x = xo - dp1 / d2p1;
-            if (std::fabs(x - xo) < 1.0e-15) break;
-        }
-        double q0 = 1.0, q1 = x;
-        for (int k = 2; k <= n - 1; ++k) {
-            const double q2 = ((double)(2 * k - 1) * x * q1 - (double)(k - 1) * q0) / (double)k;
-            q0 = q1;
-            q1 = q2;
-        }
-        out.w[i - 1] = 2.0 / ((double)(n * (n - 1)) * q1 * q1);
-    }
+    std::vector<double> x, w;
+    lgl_nodes_weights(n, x, w);
+    for (int i = 0; i < n; ++i) out.w[i] = w[i];
 }
 
+// max that keeps a NaN: once either operand is NaN the result is NaN, so a
+// non-finite field shows up in out4[0..2] (the fmax builtin would drop it).
+__device__ __forceinline__ double nanmax(double m, double a) { return (a != a || a > m) ? a : m; }
+
 __device__ __forceinline__ double wmax(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
 __device__ __forceinline__ double wsum(double v) {
@@ -84,9 +67,9 @@ __global__ void __launch_bounds__(kThreads) k_stats_partial(const double* __rest
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const double a = u[i], b = v[i], c = w[i];
-        mu = fmax(mu, fabs(a));
-        mv = fmax(mv, fabs(b));
-        mw = fmax(mw, fabs(c));
+        mu = nanmax(mu, fabs(a));
+        mv = nanmax(mv, fabs(b));
+        mw = nanmax(mw, fabs(c));
         e += 0.5 * (a * a + b * b + c * c) * zw.w[i / plane];
     }
     __shared__ double red[4][kThreads / 32];
@@ -96,7 +79,7 @@ __global__ void __launch_bounds__(kThreads) k_stats_partial(const double* __rest
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int k = 1; k < kThreads / 32; ++k) {
-            mu = fmax(mu, red[0][k]); mv = fmax(mv, red[1][k]); mw = fmax(mw, red[2][k]); e += red[3][k];
+            mu = nanmax(mu, red[0][k]); mv = nanmax(mv, red[1][k]); mw = nanmax(mw, red[2][k]); e += red[3][k];
         }
         part[4 * blockIdx.x + 0] = mu;
         part[4 * blockIdx.x + 1] = mv;
@@ -109,9 +92,9 @@ __global__ void k_stats_final(const double* __restrict__ part, double scale, dou
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double mu = 0.0, mv = 0.0, mw = 0.0, e = 0.0;
     for (int b = 0; b < kBlocks; ++b) {
-        mu = fmax(mu, part[4 * b]);
-        mv = fmax(mv, part[4 * b + 1]);
-        mw = fmax(mw, part[4 * b + 2]);
+        mu = nanmax(mu, part[4 * b]);
+        mv = nanmax(mv, part[4 * b + 1]);
+        mw = nanmax(mw, part[4 * b + 2]);
         e += part[4 * b + 3];
     }
     out[0] = mu;
@@ -122,7 +105,10 @@ __global__ void k_stats_final(const double* __restrict__ part, double scale, dou
 
 // Device address of g_stats_scratch on the current device, looked up once per
 // device.  A host-side reference to g_stats_scratch names a host stand-in, not
-// device memory, so kernels must be given this address instead.
+// device memory, so kernels must be given this address instead.  The cache is
+// keyed by device ordinal for the life of the process: it does not survive
+// cudaDeviceReset() or a switch to another context on the same device (the
+// module is loaded again there, at another address).
 int scratch_address(double** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return DNS3D_E_NODEVICE;

@@ -220,12 +220,16 @@ int dns3d_check_conversions(int device, long long n, unsigned long long* mismatc
  * of dns3d_get_state), writes to the caller-owned device buffer out4:
  *   out4[0..2] = max|u|, max|v|, max|w|,
  *   out4[3]    = kinetic energy, as dns3d_diagnostics() reports them.
+ * A NaN in out4 means a non-finite value in the fields (the maxima keep NaN).
  * Runs on the calling thread's current device, asynchronously on `stream`
  * (a cudaStream_t; NULL = legacy default stream).  Its scratch is a fixed
  * 32 KB array inside the library, present on every GPU that loads it until
  * the process exits; it allocates nothing.  The first call on a device looks
  * up that array's device address (make that first call before any stream
- * capture).  All calls share the array, so calls that overlap on the GPU race.
+ * capture); that address is kept per device ordinal for the life of the
+ * process, so it does not survive cudaDeviceReset() or a change of context on
+ * the device.  All calls share the array, so calls that overlap on the GPU
+ * race.
  * nz above DNS3D_NOALLOC_MAX_NZ is rejected with DNS3D_E_UNSUPPORTED. */
 #define DNS3D_NOALLOC_MAX_NZ 129
 int dns3d_flow_stats_noalloc(const double* u, const double* v, const double* w, int nx, int ny,

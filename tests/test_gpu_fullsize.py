@@ -1,0 +1,160 @@
+"""GPU parity at full size: the benchmarked grid (128x128x65, PI control) over
+the 50-step horizon and the largest grid (512x384x129, PI control, white
+noise) over 5 steps, against the C/OpenMP restatement of the reference step
+(oracle/dns3d_cpu.c, run on all host cores), with the diagnostics of
+output_diagnostics_3d (DNS_pressure_BC_3D.f90:2094-2146) and
+check_divergence_3d (3D:2171-2190) compared at EVERY step.
+
+Bars, all written here:
+* fields u, v, w, p_total: max|GPU - oracle| <= 1e-10 x that component's own
+  max|.|, floored at 1e-4 x the velocity scale U = max(|u|,|v|,|w|) (w starts
+  at zero: while |w| < 1e-4 U its error is held to 1e-14 U, tens of ulps of
+  U; two FP64 restatements of the step, numpy and C, differ by 3e-16 U in w);
+* histories: kinetic energy, max|u|, max|v|, max|w| (same floor), dP/dx and
+  the bulk velocity <= 1e-10 relative at every step;
+* max|div u| at every step <= 1e-10 relative to its own value plus
+  DIV_ABS x U (the divergence is a derivative of the state, so the state's
+  round-off is amplified by |D1| ~ nz^2/4 at the wall rows where the maximum
+  sits).
+"""
+import numpy as np
+import pytest
+
+from f90_dns_gb300 import ChannelDNS, config_from
+from f90_dns_gb300.capi import PREC_MIXED
+from f90_dns_gb300.workloads import WORKLOADS, ensemble_draws
+from tests.helpers import component_errors, oracle_config
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+FLOOR = 1e-4
+DIV_ABS = 1e-12
+C2 = WORKLOADS["channel_128x128x65_re180_pi"]
+C5 = WORKLOADS["channel_512x384x129_re180_pi"]
+HIST_KEYS = ("energy", "umax", "vmax", "wmax", "dpdx", "u_bulk")
+
+
+def gpu_history(wl, nsteps, precision=0):
+    hist = []
+    with ChannelDNS(config_from(wl, precision=precision)) as d:
+        for _ in range(nsteps):
+            d.step(1)
+            g = d.diagnostics()
+            hist.append({k: getattr(g, k) for k in HIST_KEYS + ("max_div",)})
+        st = d.get_state(walls=False)
+    return st, hist
+
+
+def cpu_history(wl, nsteps):
+    from oracle.cpu_ref import CpuChannel
+    hist = []
+    with CpuChannel(oracle_config(wl)) as c:
+        for _ in range(nsteps):
+            c.step(1)
+            hist.append(c.diagnostics())
+        st = c.get_state()
+    return st, hist
+
+
+def history_errors(gh, ch, floor=FLOOR):
+    """Per-key max over steps of |GPU - oracle| / max(|oracle|, floor x umax)
+    (the floor only for the velocity maxima); max_div separately."""
+    out = {}
+    for k in HIST_KEYS:
+        e = 0.0
+        for g, c in zip(gh, ch):
+            sc = max(abs(c[k]), floor * c["umax"]) if k in ("vmax", "wmax") else max(abs(c[k]), 1e-300)
+            e = max(e, abs(g[k] - c[k]) / sc)
+        out[k] = e
+    out["max_div_rel"] = max(abs(g["max_div"] - c["max_div"]) / max(c["max_div"], 1e-300) for g, c in zip(gh, ch))
+    out["max_div_abs_over_u"] = max(abs(g["max_div"] - c["max_div"]) / c["umax"] for g, c in zip(gh, ch))
+    return out
+
+
+def compare(wl, nsteps, precision=0):
+    gst, gh = gpu_history(wl, nsteps, precision)
+    cst, ch = cpu_history(wl, nsteps)
+    return component_errors(gst, cst, FLOOR), history_errors(gh, ch), gh, ch
+
+
+def assert_fp64_parity(fe, he, gh, ch):
+    for k in ("u", "v", "w", "p_total"):
+        assert fe[k] <= TOL, (k, fe)
+    for k in HIST_KEYS:
+        assert he[k] <= TOL, (k, he)
+    for i, (g, c) in enumerate(zip(gh, ch)):
+        assert abs(g["max_div"] - c["max_div"]) <= TOL * c["max_div"] + DIV_ABS * c["umax"], (i + 1, g["max_div"], c["max_div"])
+
+
+def test_benchmark_grid_50_steps_matches_oracle(built_lib):
+    """128x128x65, Re 180, dt 0.002, PI control to U_b = 2/3, amplitude 0.05,
+    mode (2,1): the bench workload with the kernels the autotuner picks."""
+    fe, he, gh, ch = compare(C2, 50)
+    print("fullsize C2 fields", fe, "histories", he)
+    assert_fp64_parity(fe, he, gh, ch)
+
+
+def test_largest_grid_5_steps_matches_oracle(built_lib):
+    """512x384x129, Re 180, dt 0.001, PI control, amplitude 0.08, mode (2,2),
+    seeded white noise 1e-3 (the oracle's Philox stream)."""
+    fe, he, gh, ch = compare(C5, 5)
+    print("fullsize C5 fields", fe, "histories", he)
+    assert_fp64_parity(fe, he, gh, ch)
+
+
+def test_largest_grid_mixed_5_steps_against_fp64_oracle(built_lib):
+    """The mixed form on the largest grid: velocity within 1e-6 of U and the
+    energy history within 1e-8 of the FP64 oracle's."""
+    gst, gh = gpu_history(C5, 5, PREC_MIXED)
+    cst, ch = cpu_history(C5, 5)
+    U = max(np.max(np.abs(cst[k])) for k in ("u", "v", "w"))
+    err = max(np.max(np.abs(gst[k] - cst[k])) for k in ("u", "v", "w")) / U
+    print("fullsize C5 mixed velocity error", err)
+    assert err <= 1e-6
+    for g, c in zip(gh, ch):
+        assert abs(g["energy"] - c["energy"]) <= 1e-8 * c["energy"]
+
+
+@pytest.mark.parametrize("nz", [49, 65])
+def test_ensemble_draws_match_oracle(built_lib, nz):
+    """One seed-drawn ensemble run of each larger nz, stepped inside an
+    ensemble with other draws, against the oracle over 20 steps."""
+    from f90_dns_gb300 import Ensemble
+    draws = [d for d in ensemble_draws(64, seed=0) if d["nz"] == nz and d["analytical_mode_y"] > 0]
+    wls = [dict(d, lgl_dmatrix_guard=d["nz"] < 58) for d in draws[:3]]
+    with Ensemble([config_from(d) for d in wls]) as ens:
+        ens.step(20)
+        states = [ens.run(i).get_state(walls=False) for i in range(len(wls))]
+    for wl, st in zip(wls, states):
+        cst, _ = cpu_history(wl, 20)
+        fe = component_errors(st, cst, FLOOR)
+        print("ensemble draw", wl["nx"], wl["ny"], wl["nz"], fe)
+        for k in ("u", "v", "w", "p_total"):
+            assert fe[k] <= TOL, (wl["nx"], wl["ny"], wl["nz"], k, fe)
+
+
+def test_long_run_statistics_match_oracle(built_lib):
+    """1200 steps of the 32x32x33 channel (constant forcing): the plane-mean
+    profile and the kinetic-energy statistics (mean, minimum, maximum, last)
+    of the FP64 path against the oracle's."""
+    from oracle.cpu_ref import CpuChannel
+    wl = WORKLOADS["channel_32x32x33_re180_dpdx"]
+    n, every = 1200, 10
+    ge, ce = [], []
+    with ChannelDNS(config_from(wl)) as d, CpuChannel(oracle_config(wl)) as c:
+        for _ in range(n // every):
+            d.step(every)
+            c.step(every)
+            ge.append(d.diagnostics().energy)
+            ce.append(c.diagnostics()["energy"])
+        gp = d.flow_statistics(profiles=True)
+        cs = c.get_state()
+    ge, ce = np.array(ge), np.array(ce)
+    prof = {k: cs[k].mean(axis=(1, 2)) for k in ("u", "v", "w")}
+    U = np.max(np.abs(prof["u"]))
+    perr = max(np.max(np.abs(gp[f"{k}_avg"] - prof[k])) for k in ("u", "v", "w")) / U
+    serr = max(abs(f(ge) - f(ce)) / abs(f(ce)) for f in (np.mean, np.min, np.max, lambda a: a[-1]))
+    print("long run: profile error", perr, "energy statistics error", serr)
+    assert perr <= 1e-8
+    assert serr <= 1e-8

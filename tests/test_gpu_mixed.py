@@ -17,7 +17,7 @@ from f90_dns_gb300 import ChannelDNS, config_from
 from f90_dns_gb300.capi import PREC_MIXED
 from f90_dns_gb300.workloads import WORKLOADS
 from oracle import dns3d_ref as ref
-from tests.helpers import oracle_config, velocity_errors
+from tests.helpers import oracle_config, scaled_velocity_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -45,7 +45,7 @@ def test_mixed_matches_fp64_oracle(built_lib, wl, nsteps):
     gst, gdiag = run_mixed(wl, nsteps)
     cfg = oracle_config(wl)
     g, st, hist = ref.run(cfg, nsteps, record_every=nsteps)
-    err = velocity_errors(gst, st)
+    err = scaled_velocity_errors(gst, st)
     assert max(err["u"], err["v"], err["w"]) <= VEL_TOL, err
     div_ref = ref.max_divergence(g, st)
     assert abs(gdiag.max_div - div_ref) <= DIV_TOL, (gdiag.max_div, div_ref)

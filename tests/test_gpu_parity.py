@@ -1,7 +1,12 @@
 """GPU parity: the sm_103a library against the CPU oracle (FP64).
 
-Bar: max |GPU - oracle| <= 1e-10 x (velocity scale max(|u|,|v|,|w|)) per
-velocity component over the 50-step horizon, p_total relative to max|p|.
+Bars: max |GPU - oracle| <= 1e-10 of each field's own max|.| (u, v, w floored
+at 1e-4 of the velocity scale U = max(|u|,|v|,|w|), p_total on max|p_total|)
+after the horizon; the diagnostics of output_diagnostics_3d and
+check_divergence_3d (DNS_pressure_BC_3D.f90:2094-2146, 2171-2190) at EVERY
+step: kinetic energy, max|u|, max|v|, max|w| within 1e-10 relative (the same
+floor), dP/dx within 1e-12, max|div u| within 1e-10 relative plus 1e-12 U
+(the divergence differentiates the state, amplifying its round-off by |D1|).
 """
 import json
 import os
@@ -21,38 +26,59 @@ TOL = 1e-10
 C1 = WORKLOADS["channel_32x32x33_re180_dpdx"]
 
 
-def gpu_run(wl, nsteps, stage_api=False):
+def gpu_run(wl, nsteps, stage_api=False, history=False):
+    hist = []
     with ChannelDNS(config_from(wl)) as d:
-        if stage_api:
-            for _ in range(nsteps):
-                d.compute_source_terms_3d()
-                d.viscous_step_3d()
-                d.solve_pressure_3d()
-                d.pressure_correction_3d()
-                d.apply_boundary_conditions_3d()
-        else:
-            d.step(nsteps)
+        for _ in range(nsteps if history else 1):
+            n = 1 if history else nsteps
+            if stage_api:
+                for _ in range(n):
+                    d.compute_source_terms_3d()
+                    d.viscous_step_3d()
+                    d.solve_pressure_3d()
+                    d.pressure_correction_3d()
+                    d.apply_boundary_conditions_3d()
+            else:
+                d.step(n)
+            if history:
+                hist.append(d.diagnostics())
         st = d.get_state()
         diag = d.diagnostics()
-    return st, diag
+    return (st, diag, hist) if history else (st, diag)
 
 
 def oracle_run(wl, nsteps):
+    """The oracle's run with its diagnostics and max|div u| at every step."""
     cfg = oracle_config(wl)
-    g, st, hist = ref.run(cfg, nsteps, record_every=nsteps)
+    g = ref.setup_grid(cfg)
+    st = ref.initial_state(cfg, g)
+    hist = []
+    for _ in range(nsteps):
+        ref.step(cfg, g, st)
+        d = ref.diagnostics(cfg, g, st)
+        d["max_div"] = ref.max_divergence(g, st)
+        hist.append(d)
     return cfg, g, st, hist
 
 
+def check_history(ghist, hist, tol=TOL, floor=1e-4):
+    assert len(ghist) == len(hist)
+    for i, (gd, d) in enumerate(zip(ghist, hist)):
+        for k in ("umax", "vmax", "wmax", "energy"):
+            sc = max(abs(d[k]), floor * d["umax"])
+            assert abs(getattr(gd, k) - d[k]) <= tol * sc, (i + 1, k, getattr(gd, k), d[k])
+        assert abs(gd.dpdx - d["dpdx"]) <= 1e-12 * max(1.0, abs(d["dpdx"])), (i + 1, gd.dpdx, d["dpdx"])
+        assert abs(gd.max_div - d["max_div"]) <= tol * d["max_div"] + 1e-12 * d["umax"], \
+            (i + 1, gd.max_div, d["max_div"])
+
+
 def check(wl, nsteps, tol=TOL):
-    gst, gdiag = gpu_run(wl, nsteps)
+    gst, gdiag, ghist = gpu_run(wl, nsteps, history=True)
     cfg, g, st, hist = oracle_run(wl, nsteps)
     err = velocity_errors(gst, st)
     assert max(err["u"], err["v"], err["w"]) <= tol, err
     assert err["p_total"] <= tol, err
-    d = hist[-1]
-    for k in ("umax", "vmax", "wmax", "energy"):
-        assert abs(getattr(gdiag, k) - d[k]) <= tol * max(abs(d[k]), d["umax"]), (k, getattr(gdiag, k), d[k])
-    assert abs(gdiag.dpdx - d["dpdx"]) <= 1e-12 * max(1.0, abs(d["dpdx"]))
+    check_history(ghist, hist, tol)
     return gst, st, err
 
 

@@ -18,7 +18,7 @@ from f90_dns_gb300 import ChannelDNS, Dns3DError, config_from
 from f90_dns_gb300.capi import DNS3D_E_UNSUPPORTED, PREC_MIXED
 from f90_dns_gb300.workloads import WORKLOADS
 from oracle import dns3d_ref as ref
-from tests.helpers import oracle_config, velocity_errors
+from tests.helpers import oracle_config, scaled_velocity_errors, velocity_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -58,7 +58,7 @@ def test_jst4_mixed_close_to_fp64(built_lib):
 
 def test_jacgs_tight_tolerance_matches_direct_oracle(built_lib):
     wl = dict(BASE, linear_solver=1, cgstol=1e-12)
-    err = velocity_errors(_gpu(wl, 10), _oracle(dict(BASE), 10))
+    err = scaled_velocity_errors(_gpu(wl, 10), _oracle(dict(BASE), 10))
     assert max(err["u"], err["v"], err["w"]) <= 1e-9, err
 
 
@@ -66,13 +66,13 @@ def test_jacgs_default_tolerance(built_lib):
     wl = dict(BASE, linear_solver=1, cgstol=1e-6)
     got = _gpu(wl, 10)
     for st in (_oracle(wl, 10), _oracle(dict(BASE), 10)):
-        err = velocity_errors(got, st)
+        err = scaled_velocity_errors(got, st)
         assert max(err["u"], err["v"], err["w"]) <= 2e-5, err
 
 
 def test_jacgs_with_jst4_and_weak_form(built_lib):
     wl = dict(BASE, linear_solver=1, cgstol=1e-12, convection_scheme=1, use_weak_form_divergence=True)
-    err = velocity_errors(_gpu(wl, 5), _oracle(dict(wl, linear_solver=0), 5))
+    err = scaled_velocity_errors(_gpu(wl, 5), _oracle(dict(wl, linear_solver=0), 5))
     assert max(err["u"], err["v"], err["w"]) <= 1e-9, err
 
 

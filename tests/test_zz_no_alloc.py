@@ -61,3 +61,17 @@ def test_noalloc_rejects_oversized_nz(built_lib):
     buf = torch.zeros(16, dtype=torch.float64, device="cuda")
     p = C.c_void_p(buf.data_ptr())
     assert built_lib.dns3d_flow_stats_noalloc(p, p, p, 2, 2, 4000, p, None) == 6  # DNS3D_E_UNSUPPORTED
+
+
+def test_noalloc_reports_nan(built_lib):
+    """A NaN in a field must reach out4: the maxima keep NaN, so a blown-up
+    state is not reported with finite maxima."""
+    rng = np.random.default_rng(5)
+    shp = (17, 8, 16)
+    u, v, w = (rng.standard_normal(shp) for _ in range(3))
+    v[3, 2, 5] = np.nan
+    got = _noalloc_stats(built_lib, u, v, w)
+    assert np.isfinite(got[0]) and np.isnan(got[1]) and np.isfinite(got[2]) and np.isnan(got[3]), got
+    v[3, 2, 5] = 0.0
+    got = _noalloc_stats(built_lib, u, v, w)  # the shared scratch keeps no NaN from the call before
+    assert np.all(np.isfinite(got)), got
