@@ -87,10 +87,11 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, log_dir: str | None = None):
+        import tempfile
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        self.path = os.path.join(log_dir or tempfile.gettempdir(), f"dns3d_bench_clocks_rank{index}.csv")
 
     def __enter__(self):
         try:
@@ -281,7 +282,7 @@ def run_ours(args) -> None:
     d.step(args.warmup)
     d.synchronize()
 
-    sampler = ClockSampler(local)
+    sampler = ClockSampler(local, args.clock_log)
     with sampler:
         _barrier(dist)
         ms = d.step_timed(args.steps)
@@ -469,6 +470,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=4.0)
     ap.add_argument("--serve-round", type=int, default=20)
+    ap.add_argument("--clock-log", default=None,
+                    help="directory for the nvidia-smi clock samples of the timed region (default: the temp dir)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu DRAM bytes per launch of the dominant kernel, if captured")
     args = ap.parse_args()

@@ -42,7 +42,7 @@ struct Weights {
 // argument.  The host vector is host memory; no device memory is allocated.
 void lgl_weights_fixed(int n, Weights& out) {
     std::vector<double> x, w;
-    lgl_nodes_weights(n, x, w);
+    dns3d::lgl_nodes_weights(n, x, w);
     for (int i = 0; i < n; ++i) out.w[i] = w[i];
 }
 

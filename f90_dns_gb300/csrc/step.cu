@@ -681,7 +681,14 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && *landed;
         tc_fence_after();
         if (!done) {
-            if (threadIdx.x == 0) atomicExch(err, 1);
+            if (threadIdx.x == 0) {
+                atomicExch(err, 1);
+                // the slices' bulk copies and the MMAs of this q may still be in
+                // flight: give each a second bounded wait before the shared
+                // memory and the TMEM columns they write are released
+                if (!*landed) tc_mbar_wait(&mbar[1], par, 1 << 22);
+                tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22);
+            }
             ok = false;
             break;  // uniform: no TMEM read, no further MMA
         }
@@ -903,7 +910,13 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && *landed;
         tc_fence_after();
         if (!done) {
-            if (tid == 0) atomicExch(err, 1);
+            if (tid == 0) {
+                atomicExch(err, 1);
+                // second bounded waits for copies and MMAs still in flight
+                // (as in viscous_tc_body) before shared memory and TMEM go
+                if (!*landed) tc_mbar_wait(&mbar[1], 0, 1 << 22);
+                tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22);
+            }
             break;
         }
         {
