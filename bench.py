@@ -165,11 +165,72 @@ def algorithmic_flops(wl: dict) -> dict:
     return out
 
 
-def cpu_sample(wl_name: str, steps: int, threads: int) -> dict:
+def algorithmic_bytes(wl: dict) -> dict:
+    """Compulsory DRAM bytes per launch of each profiled kernel of the FP64
+    step (spectral-resident algorithm): every field the kernel must read and
+    write once, plus the per-mode operators it applies.  One spectral field
+    S = (nx/2+1) ny nz complex128 values, one physical field R = nx ny nz
+    float64 values, one per-mode inverse set Inv = nq (he^2 + ho^2) float64
+    values (nq = (ny/2+1)(nx/2+1) distinct k^2, folded even/odd blocks).
+      vorticity: u, v, w -> omega (6 S);
+      inverse y pass: 3 fields per launch, spectrum in and out (6 S);
+      c2r x pass: 3 fields per launch (3 S + 3 R);
+      products: 6 R in, 3 R out;  r2c x pass: 3 R in, 3 S out;
+      forward y pass: the kx <= kx_max columns of 3 fields, in and out;
+      viscous: u, v, w, su, sv, sw in, u*, v*, w* out (9 S) + Helmholtz Inv;
+      pressure: u*, v*, w* in, phi out, phi in and out (6 S) + Poisson Inv;
+      projection: phi, u*, v*, w*, p in, u, v, w, p out (9 S)."""
+    nx, ny, nz = wl["nx"], wl["ny"], wl["nz"]
+    nxhp = nx // 2 + 1
+    S = nxhp * ny * nz * 16.0
+    R = nx * ny * nz * 8.0
+    ho = nz // 2
+    he = nz - ho
+    inv = (ny // 2 + 1) * nxhp * (he * he + ho * ho) * 8.0
+    kxm = ((nx // 2) * 2) // 3 if wl.get("use_dealias_23_rule", True) else nxhp - 1
+    fwd = 6 * S * min(kxm + 1, nxhp) / nxhp
+    b = {"vorticity": 6 * S, "fft_y_inverse": 6 * S, "fft_x_c2r": 3 * S + 3 * R, "products": 9 * R,
+         "fft_x_r2c": 3 * R + 3 * S, "fft_y_forward": fwd, "viscous_helmholtz": 9 * S + inv,
+         "pressure_poisson": 6 * S + inv, "pressure_correction": 9 * S, "pi_update": nz * 16.0 + 64.0}
+    for k in ("vorticity", "viscous_helmholtz", "pressure_poisson", "pressure_correction"):
+        b[k + "_tc"] = b[k]
+    return b
+
+
+def measured_peaks() -> dict:
+    """HBM copy bandwidth and bf16 tensor throughput measured on this machine's
+    GB300s (MEASURED_PEAKS.json beside this file), else the published
+    fallback of one earlier GB300 measurement."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def working_set_note(wl: dict) -> str:
+    """L2 statement of the timed region, from the grid alone (the same text in
+    both arms): the FP64 step re-reads its spectral state, work fields and
+    per-mode inverses every step."""
+    ab = algorithmic_bytes(wl)
+    # the inverse passes run as two 3-field launches per step
+    per_step = sum(v for k, v in ab.items() if not k.endswith("_tc")) + ab["fft_y_inverse"] + ab["fft_x_c2r"]
+    return (f"each step moves >= {per_step / 1e6:.0f} MB of state, work fields and per-mode inverses "
+            + ("> 129 MB L2, re-read every step; no flush" if per_step > 2 * 129e6
+               else "(L2-resident timing; no flush)"))
+
+
+def bench_config(wl_name: str, wl: dict, world_size: int) -> dict:
+    return {"workload": wl_name, "grid": [wl["nx"], wl["ny"], wl["nz"]], "precision": "fp64",
+            "parallelism": "replicas" if world_size > 1 else "single", "l2": working_set_note(wl)}
+
+
+def cpu_sample(wl_name: str, steps: int, threads: int, warmup: int = 1) -> dict:
     """Time the C/OpenMP restatement of the reference step (oracle/dns3d_cpu.c:
     physical-space transforms per plane, per-mode matrices rebuilt and
     LU-factored every call, as DNS_pressure_BC_3D.f90 does) on `steps` steps of
-    the workload after one warm-up step, in a subprocess with `threads`
+    the workload after `warmup` untimed steps, in a subprocess with `threads`
     OpenMP threads."""
     env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     code = (
@@ -180,16 +241,16 @@ def cpu_sample(wl_name: str, steps: int, threads: int) -> dict:
         "names = set(ref.Config.__dataclass_fields__)\n"
         "cfg = ref.Config(**{k: v for k, v in wl.items() if k in names})\n"
         "c = cpu_ref.CpuChannel(cfg, threads=%d)\n"
-        "c.step(1)\n"
+        "c.step(%d)\n"
         "t = time.perf_counter()\n"
         "c.step(%d)\n"
         "dt = time.perf_counter() - t\n"
-        "print(json.dumps({'seconds': dt, 'threads': c.threads}))\n" % (ROOT, wl_name, threads, steps))
+        "print(json.dumps({'seconds': dt, 'threads': c.threads}))\n" % (ROOT, wl_name, threads, warmup, steps))
     res = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
     if res.returncode != 0:
         raise RuntimeError("cpu baseline failed: " + res.stderr[-2000:])
     out = json.loads(res.stdout.strip().splitlines()[-1])
-    return {"seconds": out["seconds"], "steps": steps, "threads": out["threads"]}
+    return {"seconds": out["seconds"], "steps": steps, "warmup": warmup, "threads": out["threads"]}
 
 
 CPU_SAMPLE_TEXT = ("C/OpenMP restatement of DNS_pressure_BC_3D.f90 (oracle/dns3d_cpu.c): per-plane r2c/c2r "
@@ -200,29 +261,127 @@ CPU_SAMPLE_TEXT = ("C/OpenMP restatement of DNS_pressure_BC_3D.f90 (oracle/dns3d
 
 def run_reference(args) -> None:
     """The reference arm: the C/OpenMP restatement of the reference algorithm
-    timed on this host with one OpenMP thread per core (rank 0 only)."""
+    timed on this host with one OpenMP thread per core (rank 0 only), on the
+    same workload, metric and config as the GPU arm.  It times exactly the
+    requested steps after the requested warm-up steps, unless that would take
+    longer than --ref-budget seconds; then it times fewer and its line says how
+    many it timed."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
     from f90_dns_gb300.workloads import WORKLOADS, point_count
     wl = WORKLOADS[args.workload]
     pts = point_count(wl)
     threads = os.cpu_count() or 1
-    nsteps = max(3, int(round(args.ref_sample_frac * args.steps)))
-    samp = cpu_sample(args.workload, nsteps, threads)
+    probe = cpu_sample(args.workload, 1, threads, warmup=0)
+    per_step = probe["seconds"]
+    fit = max(1, int(args.ref_budget / max(per_step, 1e-9)))
+    warm = min(args.warmup, max(0, fit // 4))
+    nsteps = min(args.steps, max(1, fit - warm))
+    samp = cpu_sample(args.workload, nsteps, threads, warmup=warm)
     threads = samp["threads"]
     value = pts * samp["steps"] / samp["seconds"]
     line = {
         "impl": "reference", "metric": "point-steps/s", "value": value, "unit": "point-steps/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": args.gpus, "steps": samp["steps"], "warmup": samp["warmup"],
+        "requested_steps": args.steps, "requested_warmup": args.warmup,
         "ms_per_step": 1e3 * samp["seconds"] / samp["steps"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "grid": [wl["nx"], wl["ny"], wl["nz"]], "precision": "fp64"},
+        "config": bench_config(args.workload, wl, int(os.environ.get("WORLD_SIZE", "1"))),
         "cpu_baseline": {"value": value, "unit": "point-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{samp['steps']} steps of {args.workload} after 1 warm-up step, "
-                                   f"{threads} threads: " + CPU_SAMPLE_TEXT},
+                         "sample": f"{samp['steps']} steps of {args.workload} after {samp['warmup']} warm-up "
+                                   f"steps, {threads} threads: " + CPU_SAMPLE_TEXT},
         "e2e": {"value": value, "unit": "point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# per-launch DRAM traffic (ncu dram__bytes_read.sum + dram__bytes_write.sum)
+# and tensor-pipe activity of the tensor-core kernels, from one capture each
+NCU_TENSOR_PIPE = {
+    ("channel_128x128x65_re180_pi", "viscous_helmholtz_tc"): 7.9,
+}
+
+
+def kernel_rooflines(wl, prof, step_ms, peaks, wl_name, traffic_override=None):
+    """Per-kernel achieved HBM GB/s on algorithmic bytes (algorithmic_bytes)
+    against the measured copy bandwidth; the dominant kernel's entry is the
+    line's `roofline`; the whole step's algorithmic bytes against the same
+    peak is `step_roofline`."""
+    ab = algorithmic_bytes(wl)
+    total = sum(t for _, t in prof.values())
+    kernels = {}
+    for k, (n, t) in prof.items():
+        e = {"launches": n, "avg_ms": t / n, "share": t / total}
+        if k in ab:
+            gbs = ab[k] / (t / n * 1e-3) / 1e9
+            e.update(algorithmic_bytes=ab[k], achieved_gbs=gbs, hbm_frac=gbs / peaks["hbm_gbs"])
+        kernels[k] = e
+    dom = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
+    roofline = None
+    if "achieved_gbs" in kernels[dom]:
+        kd = kernels[dom]
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": kd["achieved_gbs"], "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": kd["hbm_frac"],
+                    "traffic": traffic_override if traffic_override is not None else NCU_TRAFFIC.get((wl_name, dom)),
+                    "algorithmic_bytes_per_launch": kd["algorithmic_bytes"],
+                    "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peaks['source']})",
+                    "traffic_source": "ncu capture of one launch (dram__bytes_read.sum + dram__bytes_write.sum)",
+                    "tensor_pipe_pct": NCU_TENSOR_PIPE.get((wl_name, dom))}
+    per_step = sum(ab[k] * n / max(1, args_steps(prof)) for k, (n, _) in prof.items() if k in ab)
+    t_roof = per_step / (peaks["hbm_gbs"] * 1e9) * 1e3
+    step_roof = {"bound": "hbm", "bytes_per_step": per_step, "t_roof_ms": t_roof, "t_meas_ms": step_ms,
+                 "frac": t_roof / step_ms, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                 "note": "algorithmic DRAM bytes of every kernel of one step against the measured copy bandwidth"}
+    return kernels, roofline, step_roof
+
+
+def args_steps(prof) -> int:
+    """Profiled steps: launches of the once-per-step PI update (or of the
+    viscous stage)."""
+    for k in ("pi_update", "viscous_helmholtz_tc", "viscous_helmholtz", "viscous_mixed"):
+        if k in prof:
+            return prof[k][0]
+    return 1
+
+
+def large_leg(args, device: int, peaks: dict) -> dict:
+    """The largest single run (512x384x129, Re 180, dt 0.001, PI control,
+    amplitude 0.08, mode (2,2), white noise 1e-3): FP64 and mixed step
+    throughput, per-kernel profile and the mixed form's error against FP64
+    after the timed steps."""
+    import numpy as np
+    from f90_dns_gb300 import ChannelDNS, config_from
+    from f90_dns_gb300.capi import PREC_MIXED
+    from f90_dns_gb300.workloads import WORKLOADS, point_count
+    name = "channel_512x384x129_re180_pi"
+    wl = WORKLOADS[name]
+    pts = point_count(wl)
+    out = {"workload": name, "grid": [wl["nx"], wl["ny"], wl["nz"]], "steps": args.large_steps}
+    states = {}
+    for label, prec in (("fp64", 0), ("mixed", PREC_MIXED)):
+        with ChannelDNS(config_from(wl, device=device, precision=prec)) as d:
+            d.step(args.warmup)
+            d.synchronize()
+            ms = d.step_timed(args.large_steps)
+            prof = d.profile_kernels(2)
+            st = d.get_state(walls=False)
+            states[label] = st
+            e = {"value": pts * args.large_steps / (ms * 1e-3), "unit": "point-steps/s",
+                 "ms_per_step": ms / args.large_steps}
+            if prec == 0:
+                kern, roof, sroof = kernel_rooflines(wl, prof, ms / args.large_steps, peaks, name)
+                e.update(kernels=kern, roofline=roof, step_roofline=sroof)
+            else:
+                tot = sum(t for _, t in prof.values())
+                e["kernels"] = {k: {"launches": n, "avg_ms": t / n, "share": t / tot} for k, (n, t) in prof.items()}
+            out[label] = e
+    a, b = states["fp64"], states["mixed"]
+    scale = max(float(np.max(np.abs(a[k]))) for k in ("u", "v", "w"))
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["mixed"]["error_vs_fp64"] = {"steps": args.warmup + args.large_steps + 2,
+                                     "max_rel_velocity": max(float(np.max(np.abs(a[k] - b[k])))
+                                                             for k in ("u", "v", "w")) / scale}
+    return out
 
 
 def serving_leg(args, device: int) -> dict:
@@ -358,30 +517,20 @@ def run_ours(args) -> None:
 
     # per-kernel device times (eager replay, events between launches)
     prof = d.profile_kernels(args.profile_steps)
-    total_prof = sum(t for _, t in prof.values())
-    flops = algorithmic_flops(wl)
-    kernels = {k: {"launches": n, "avg_ms": t / n, "share": t / total_prof} for k, (n, t) in prof.items()}
-    dom = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
+    peaks = measured_peaks()
+    kernels, roofline, step_roof = kernel_rooflines(wl, prof, ms / args.steps, peaks, args.workload, args.traffic)
     fp64_peak = measure_fp64_tflops(local)
-    roofline = None
-    if dom in flops:
-        ach = flops[dom] / (kernels[dom]["avg_ms"] * 1e-3) / 1e12
-        roofline = {"bound": "fp64", "kernel": dom, "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-                    "note": ("FP64-equivalent flops of the solve; its products run as exact FP16 digit-slice "
-                             "MMAs on the tensor cores, so the kernel can exceed the FP64 pipe's rate")
-                    if dom.endswith("_tc") else None,
-                    "frac": ach / fp64_peak,
-                    "traffic": args.traffic if args.traffic is not None else NCU_TRAFFIC.get((args.workload, dom)),
-                    "traffic_source": "ncu capture of one launch (dram__bytes_read.sum + dram__bytes_write.sum)",
-                    "peak_source": "FP64 FMA probe timed in this run (dns3d_measure_fp64_tflops); "
-                                   "MEASURED_PEAKS.json has no FP64 figure",
-                    "algorithmic_flops_per_launch": flops[dom]}
-    step_roof = {"flops_per_step": flops["total"], "t_roof_ms": flops["total"] / (fp64_peak * 1e12) * 1e3,
-                 "t_meas_ms": ms / args.steps,
-                 "frac": (flops["total"] / (fp64_peak * 1e12) * 1e3) / (ms / args.steps),
-                 "note": ("FP64-equivalent flops of the whole step against the FP64 FMA peak; the plane "
-                          "transforms run in 64-bit fixed point on the integer pipes and the z-contractions as "
-                          "exact digit-slice MMAs on the tensor cores, so the step can approach or pass 1")}
+    flops = algorithmic_flops(wl)
+    if roofline is not None and roofline["kernel"] in flops:
+        roofline["fp64_equivalent_tflops"] = flops[roofline["kernel"]] / (kernels[roofline["kernel"]]["avg_ms"] * 1e-3) / 1e12
+        roofline["fp64_fma_peak_tflops"] = fp64_peak
+    step_roof["fp64_equivalent_tflops"] = flops["total"] / (ms / args.steps * 1e-3) / 1e12
+    step_roof["fp64_fma_peak_tflops"] = fp64_peak
+
+    # the largest grid (512x384x129, white noise): FP64 and mixed, own roofline
+    large = None
+    if args.large_steps > 0 and rank == 0:
+        large = large_leg(args, local, peaks)
 
     # end-to-end through the C-ABI with host-resident state (pinned buffers)
     e2e = None
@@ -433,13 +582,11 @@ def run_ours(args) -> None:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": args.workload, "grid": [wl["nx"], wl["ny"], wl["nz"]], "precision": "fp64",
-                       "parallelism": "replicas" if ws > 1 else "single",
-                       "l2": (f"device working set {footprint_bytes(cfg) / 1e9:.2f} GB (fields, per-mode inverses) "
-                              + ("> 129 MB L2, re-read every step; no flush" if footprint_bytes(cfg) > 2 * 129e6
-                                 else "fits in the 129 MB L2 (L2-resident timing; no flush)"))},
+            "config": bench_config(args.workload, wl, ws),
+            "device_footprint_bytes": footprint_bytes(cfg),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "step_roofline": step_roof,
-            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu, "mixed": mixed, "ensemble": ensemble, "serving": serving,
+            "kernels": kernels, "clocks": clocks, "cpu_baseline": cpu, "mixed": mixed, "large": large,
+            "ensemble": ensemble, "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -456,8 +603,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=20)
-    ap.add_argument("--ref-sample-frac", type=float, default=0.1,
-                    help="reference arm: CPU steps timed per requested step (bounded sample, >= 3)")
+    ap.add_argument("--ref-budget", type=float, default=120.0,
+                    help="reference arm: seconds of CPU time allowed for warm-up plus timed steps")
     ap.add_argument("--no-mixed", dest="mixed", action="store_false",
                     help="skip the mixed-precision measurement")
     ap.add_argument("--mixed-err-steps", type=int, default=200)
@@ -467,6 +614,8 @@ def main():
     ap.add_argument("--noise", type=float, default=None,
                     help="white-noise amplitude on the initial u, v, w (default: the workload's; the large "
                          "workload has 1e-3)")
+    ap.add_argument("--large-steps", type=int, default=10,
+                    help="timed steps of the 512x384x129 leg (0 skips it)")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=4.0)
     ap.add_argument("--serve-round", type=int, default=20)
