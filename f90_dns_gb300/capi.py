@@ -43,7 +43,7 @@ EXPORTED_SYMBOLS = (
     "dns3d_compute_source_terms", "dns3d_viscous_step", "dns3d_solve_pressure",
     "dns3d_pressure_correction", "dns3d_apply_boundary_conditions", "dns3d_step",
     "dns3d_synchronize", "dns3d_diagnostics", "dns3d_output_diagnostics", "dns3d_check_divergence",
-    "dns3d_footprint_bytes", "dns3d_strerror",
+    "dns3d_projection_residual", "dns3d_footprint_bytes", "dns3d_strerror",
     "dns3d_last_error", "dns3d_step_timed", "dns3d_profile_kernels", "dns3d_launches_per_step",
     "dns3d_measure_fp64_tflops", "dns3d_check_conversions", "dns3d_flow_stats_noalloc",
     "dns3d_ensemble_create", "dns3d_ensemble_destroy", "dns3d_ensemble_size", "dns3d_ensemble_run",
@@ -193,6 +193,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_diagnostics.argtypes = [hp, C.POINTER(CDiag)]
     lib.dns3d_output_diagnostics.argtypes = [hp, C.POINTER(CDiag)]
     lib.dns3d_check_divergence.argtypes = [hp, C.POINTER(C.c_double)]
+    lib.dns3d_projection_residual.argtypes = [hp, C.POINTER(C.c_double)]
     lib.dns3d_footprint_bytes.argtypes = [C.POINTER(CConfig), C.POINTER(C.c_ulonglong)]
     lib.dns3d_strerror.argtypes = [ip]
     lib.dns3d_strerror.restype = C.c_char_p
@@ -550,6 +551,14 @@ class ChannelDNS:
         self._check(rc, "dns3d_output_diagnostics")
         return Diagnostics(d.umax, d.vmax, d.wmax, d.energy, d.u_bulk, d.dpdx, d.dpdx_avg,
                            d.max_div, d.time, d.step)
+
+    def projection_residual(self) -> float:
+        """Relative residual max|b - P phi| / max|b| of the last pressure
+        solve's Galerkin Poisson system (the divergence the projection
+        controls)."""
+        v = C.c_double(0.0)
+        self._check(self.lib.dns3d_projection_residual(self._h, C.byref(v)), "dns3d_projection_residual")
+        return v.value
 
     def check_divergence_3d(self) -> float:
         """check_divergence_3d: max |div u| of the current state."""

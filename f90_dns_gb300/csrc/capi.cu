@@ -640,7 +640,7 @@ int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
         const TcGeom t = tc_geom(c->nz);
         if (c->use_crank_nicolson && c->linear_solver == 0)  // digit slices of the Helmholtz inverses
             b += nq * (tc_q_halves(t) * sizeof(__half) + (size_t)t.m8 * sizeof(int));
-        b += (size_t)kTcSlices * t.m8 * t.k16 * sizeof(__half);  // digit image of D1
+        b += (size_t)kTcSlices * tc_blocks(t, true).a * sizeof(__half);  // digit image of D1
     }
     b += 16ull << 20;                        // operators, tables, reductions
     *bytes = b;
@@ -1258,7 +1258,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
         const TcGeom t = tc_geom(nz);
         __half* im = nullptr;
         int* ex = nullptr;
-        if ((rc = dev_alloc(h, &im, (size_t)kTcSlices * t.m8 * t.k16)) || (rc = dev_alloc(h, &ex, (size_t)t.m8)))
+        if ((rc = dev_alloc(h, &im, (size_t)kTcSlices * tc_blocks(t, true).a)) || (rc = dev_alloc(h, &ex, (size_t)t.m8)))
             return fail(rc);
         if ((e = build_tc_anti_image(g, ops.D1e, ops.D1o, im, ex, h->stream)) ||
             (e = cudaStreamSynchronize(h->stream))) {
@@ -1847,6 +1847,21 @@ int dns3d_check_divergence(dns3d_handle* h, double* max_div) {
     CK(h, cudaMemcpyAsync(max_div, h->d_out + 4, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return std::isfinite(*max_div) ? DNS3D_OK : DNS3D_E_NONFINITE;
+}
+
+int dns3d_projection_residual(dns3d_handle* h, double* rel) {
+    if (!h || !rel) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    unsigned long long* buf = reinterpret_cast<unsigned long long*>(h->d_red);
+    CK(h, launch_poisson_residual(h->g, h->ops, h->sp, h->US, h->VS, h->WS, h->PHI, buf, h->stream));
+    unsigned long long bits[2] = {0, 0};
+    CK(h, cudaMemcpyAsync(bits, buf, sizeof(bits), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    double r, b;
+    std::memcpy(&r, &bits[0], sizeof(double));
+    std::memcpy(&b, &bits[1], sizeof(double));
+    *rel = b > 0.0 ? r / b : r;
+    return std::isfinite(*rel) ? DNS3D_OK : DNS3D_E_NONFINITE;
 }
 
 int dns3d_flow_statistics(dns3d_handle* h, dns3d_flow_stats* out, double* u_avg, double* v_avg, double* w_avg) {

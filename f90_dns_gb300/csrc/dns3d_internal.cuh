@@ -361,14 +361,21 @@ cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh,
                            double helm_f, const double* ksq, int nq, double* HinvF,
                            double* PinvF, double* PpinT, int* info, cudaStream_t s);
 
+// Residual of the Galerkin Poisson system of the last pressure step: max |b(u*)
+// - P phi| and max |b| (bits of non-negative doubles, out[0], out[1]).
+cudaError_t launch_poisson_residual(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                                    const double2* VS, const double2* WS, const double2* PHI,
+                                    unsigned long long* out, cudaStream_t s);
+
 // Digit slices (FP16) and row exponents of the folded per-mode inverses invF
 // ([nq][he*he + ho*ho], the layout of Ops::HinvF) for the tensor-core solve
 // (tc.cuh); slices [nq][tc_q_halves], rowexp [nq][m8].
 cudaError_t build_tc_slices(const GridDev& g, const double* invF, int nq, __half* slices, int* rowexp,
                             cudaStream_t s);
 
-// Digit image ([kTcSlices][m8 x k16] FP16, rowexp [m8]) of the folded
-// z-derivative [[0, De], [Do, 0]] for the tensor-core contractions (tc.cuh).
+// Digit image ([kTcSlices][block E, block O] FP16, tc_blocks(t, true); rowexp
+// [m8]) of the folded z-derivative [[0, De], [Do, 0]] for the tensor-core
+// contractions (tc.cuh).
 cudaError_t build_tc_anti_image(const GridDev& g, const double* De, const double* Do, __half* image, int* rowexp,
                                 cudaStream_t s);
 

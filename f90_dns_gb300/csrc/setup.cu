@@ -243,20 +243,23 @@ __global__ void k_tc_slices(const double* __restrict__ invF, int nq, int nz, __h
 }
 
 // Digit image of the folded antisymmetric operator [[0, De], [Do, 0]] (the
-// z-derivative on [fe; fo]) in the block layout of tc.cuh, whole (zeros
-// included: it is staged once per CTA): image [kTcSlices][m8 x k16] halves,
-// rowexp [m8].  One thread per row.
+// z-derivative on [fe; fo]) in the two-block layout of tc.cuh, whole (zeros
+// included: it is staged once per CTA): per digit, block E = De (e8 rows x ko
+// K) then block O = Do (o8 rows x ke K); rowexp [m8] (even rows first).  One
+// thread per row.
 __global__ void k_tc_anti_image(const double* __restrict__ De, const double* __restrict__ Do, int nz,
                                 __half* __restrict__ image, int* __restrict__ rowexp) {
     const TcGeom t = tc_geom(nz);
+    const TcBlocks bl = tc_blocks(t, true);
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= t.m8) return;
     const bool even = m < t.e8;
     const int i = even ? m : m - t.e8;
     const int n = even ? t.ho : t.he;          // row length (K of the block)
+    const int kw = even ? bl.kE : bl.kO;       // padded K width of the block
     const bool live = i < (even ? t.he : t.ho);
     const double* row = even ? De + (size_t)i * t.ho : Do + (size_t)i * t.he;
-    const int k0 = even ? t.e8 : 0;            // K offset of the block's input part
+    const size_t base = even ? 0 : (size_t)bl.aE;
     int e = 0;
     if (live) {
         unsigned long long mx = 0;
@@ -267,13 +270,12 @@ __global__ void k_tc_anti_image(const double* __restrict__ De, const double* __r
         e = tc_exponent(mx);
     }
     rowexp[m] = e;
-    const int a_halves = t.m8 * t.k16;
-    for (int k = 0; k < t.k16; ++k) {
+    for (int j = 0; j < kw; ++j) {
         int c[kTcSlices];
         for (int s = 0; s < kTcSlices; ++s) c[s] = 0;
-        const int j = k - k0;
-        if (live && j >= 0 && j < n) tc_digits(tc_fixed(row[j], e), c);
-        for (int s = 0; s < kTcSlices; ++s) image[(size_t)s * a_halves + tc_core_off(m, k, t.k16)] = __int2half_rn(c[s]);
+        if (live && j < n) tc_digits(tc_fixed(row[j], e), c);
+        for (int s = 0; s < kTcSlices; ++s)
+            image[(size_t)s * bl.a + base + tc_core_off(i, j, kw)] = __int2half_rn(c[s]);
     }
 }
 

@@ -496,15 +496,18 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 // operator indices q; the modes sharing q ((ky, kx) and (ny-ky, kx)) and
 // their three components give 12 right-hand-side columns (re, im), one block
 // of 16.  Per q:
-//  (a) one thread starts bulk copies of the operator's digit slices into their
-//      places of the block-diagonal diag(Ge, Go) (the padding stays zero);
+//  (a) the lanes of the last warp start bulk copies of the operator's digit
+//      slices into blocks E (Ge) and O (Go) of each slice (the K padding stays
+//      zero);
 //  (b) meanwhile the folded right-hand sides are formed in FP64 (viscous_rhs_cn),
 //  (c) each column gets its power-of-two scale and (d) its digits, one
 //      16-byte core-matrix row (8 levels) per thread and digit;
-//  (e) one thread issues 7 x (K/16) MMAs: digit slice sa of the operator
-//      times digit slices 0 .. 6-sa of the right-hand sides side by side
-//      (N = 16 (7-sa)), accumulated into the weight-class columns sa .. 6;
-//  (f) every row's 7 class accumulators are combined in 64-bit integers and
+//  (e) one thread issues, per digit slice sa of the operator, the K-steps of
+//      block E (even rows: right-hand-side rows [0, ke)) and of block O (odd
+//      rows: [ke, kt)), each against right-hand-side digit slices
+//      0 .. 7-sa side by side (N = 16 (8-sa)), accumulated into the
+//      weight-class columns sa .. 7 of that block's TMEM region;
+//  (f) every row's 8 class accumulators are combined in 64-bit integers and
 //      scaled to FP64;
 //  (g) the outputs F* = x - f are written (wall values at the walls).
 __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops, const StepParams& sp,
@@ -514,10 +517,11 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                                                 int qpb, int bx, int* err) {
     extern __shared__ __align__(128) unsigned char tcsm[];
     const TcGeom t = tc_geom(g.nz);
+    const TcBlocks bl = tc_blocks(t, false);
     const int nz = g.nz, he = t.he, ho = t.ho, m8 = t.m8;
-    const int a_halves = m8 * t.k16, b_halves = kTcN * t.k16;
+    const int b_halves = kTcN * t.kt;
     __half* sA = reinterpret_cast<__half*>(tcsm);
-    __half* sB = sA + kTcSlices * a_halves;
+    __half* sB = sA + kTcSlices * bl.a;
     double* sR = reinterpret_cast<double*>(sB + kTcSlices * b_halves);  // [kTcN][m8]: rhs, then results
     int* sF = reinterpret_cast<int*>(sR + kTcN * m8);                   // column exponents
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcN);            // [0] MMAs done, [1] slices landed
@@ -525,10 +529,10 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     int* landed = reinterpret_cast<int*>(tbase + 1);                    // the slices of this q arrived
     {
         uint4* z = reinterpret_cast<uint4*>(sA);
-        const int n16 = kTcSlices * (a_halves + b_halves) / 8;
+        const int n16 = kTcSlices * (bl.a + b_halves) / 8;
         for (int i = threadIdx.x; i < n16; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
     }
-    if (threadIdx.x < 32) tc_alloc(tbase, 128);
+    if (threadIdx.x < 32) tc_alloc(tbase, 2 * kTcDCols);
     if (threadIdx.x == 0) {
         tc_mbar_init(&mbar[0]);
         tc_mbar_init(&mbar[1]);
@@ -548,8 +552,9 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     for (int q = q0; q < q1 && ok; ++q) {
         const uint32_t par = (uint32_t)((q - q0) & 1);
         // (a) digit slices of the operator: per digit, one copy per 8-row
-        // group, issued by the lanes of the last warp (the one with the least
-        // right-hand-side work below)
+        // group (its nonzero core matrices are contiguous in the compact store
+        // and in the K-major block), issued by the lanes of the last warp (the
+        // one with the least right-hand-side work below)
         if ((int)threadIdx.x >= (int)blockDim.x - 32) {
             const int lane = threadIdx.x & 31;
             if (lane == 0) tc_mbar_expect(&mbar[1], (uint32_t)(qh * sizeof(__half)));
@@ -559,11 +564,11 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             for (int j = lane; j < kTcSlices * ngrp; j += 32) {
                 const int s = j / ngrp, gm = j - s * ngrp;
                 const __half* ss = src + (size_t)s * ncore * 64;
-                __half* ds = sA + s * a_halves;
+                __half* ds = sA + s * bl.a;
                 if (gm < nbe)
-                    tc_bulk_g2s(ds + tc_core_off(gm * 8, 0, t.k16), ss + (size_t)gm * nbe * 64, nbe * 128, &mbar[1]);
+                    tc_bulk_g2s(ds + tc_core_off(gm * 8, 0, bl.kE), ss + (size_t)gm * nbe * 64, nbe * 128, &mbar[1]);
                 else
-                    tc_bulk_g2s(ds + tc_core_off(t.e8 + (gm - nbe) * 8, t.e8, t.k16),
+                    tc_bulk_g2s(ds + bl.aE + tc_core_off((gm - nbe) * 8, 0, bl.kO),
                                 ss + (size_t)(t.ncore_e + (gm - nbe) * nbo) * 64, nbo * 128, &mbar[1]);
             }
         }
@@ -639,17 +644,18 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             }
         }
         __syncthreads();
-        // (d) digits of the right-hand sides, one level of one column per
-        // thread; a warp covers 8 levels of 4 columns, so its 2-byte stores
-        // fall in distinct shared-memory banks (the bank of (n, k) in a core
-        // matrix is 4 (n mod 8) + (k mod 8)/2)
-        for (int i = threadIdx.x; i < 12 * m8; i += blockDim.x) {
+        // (d) digits of the right-hand sides, one K row of one column per
+        // thread: even levels at K [0, he), odd ones at K [ke, ke + ho); a warp
+        // covers 8 K rows of 4 columns, so its 2-byte stores fall in distinct
+        // shared-memory banks (the bank of (n, k) in a core matrix is
+        // 4 (n mod 8) + (k mod 8)/2)
+        for (int i = threadIdx.x; i < 12 * t.kt; i += blockDim.x) {
             const int kl = i & 7, cc = i >> 3;
-            const int c = cc % 12, row = (cc / 12) * 8 + kl;
-            const bool valid = row < he || (row >= t.e8 && row < t.e8 + ho);
+            const int c = cc % 12, kk = (cc / 12) * 8 + kl;
+            const int row = kk < t.ke ? (kk < he ? kk : -1) : (kk - t.ke < ho ? t.e8 + (kk - t.ke) : -1);
             int d[kTcSlices];
-            tc_digits(valid ? tc_fixed(sR[c * m8 + row], sF[c]) : 0, d);
-            __half* dst = sB + tc_core_off(c, row, t.k16);
+            tc_digits(row >= 0 ? tc_fixed(sR[c * m8 + row], sF[c]) : 0, d);
+            __half* dst = sB + tc_core_off(c, kk, t.kt);
 #pragma unroll
             for (int s = 0; s < kTcSlices; ++s) dst[s * b_halves] = __int2half_rn(d[s]);
         }
@@ -661,17 +667,22 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
         if (threadIdx.x == 0) {
             *landed = tc_mbar_wait(&mbar[1], par, 1 << 22) ? 1 : 0;
             if (*landed && !ops.tc_stall) {
-                // the descriptors differ only in their start address (16-byte
-                // units in the low field): one add per MMA
-                const uint32_t sbo = (uint32_t)t.k16 * 16;
-                const int nks = t.k16 / 16;
-                const uint64_t da0 = tc_desc(tc_smem_u32(sA), 128, sbo), db0 = tc_desc(tc_smem_u32(sB), 128, sbo);
+                // descriptors differ only in their start address (16-byte
+                // units in the low field; a K offset of k elements is k/8
+                // core matrices of 128 B, i.e. k units): one add per MMA
+                const uint64_t dAE = tc_desc(tc_smem_u32(sA), 128, (uint32_t)bl.kE * 16);
+                const uint64_t dAO = tc_desc(tc_smem_u32(sA + bl.aE), 128, (uint32_t)bl.kO * 16);
+                const uint64_t dB = tc_desc(tc_smem_u32(sB), 128, (uint32_t)t.kt * 16);
+                const int nkE = bl.kE / 16, nkO = bl.kO / 16;
                 for (int sa = 0; sa < kTcSlices; ++sa) {
                     const uint32_t idesc = tc_idesc(kTcN * (kTcSlices - sa));
-                    const uint64_t das = da0 + (uint64_t)((sa * a_halves * 2) >> 4);
-                    for (int ks = 0; ks < nks; ++ks)
-                        tc_mma(tmem + (uint32_t)(sa * kTcN), das + (uint64_t)(16 * ks), db0 + (uint64_t)(16 * ks), idesc,
-                               (sa > 0 || ks > 0) ? 1u : 0u);
+                    const uint64_t so = (uint64_t)((sa * bl.a * 2) >> 4);
+                    for (int ks = 0; ks < nkE; ++ks)
+                        tc_mma(tmem + (uint32_t)(sa * kTcN), dAE + so + (uint64_t)(16 * ks),
+                               dB + (uint64_t)(bl.bE + 16 * ks), idesc, (sa > 0 || ks > 0) ? 1u : 0u);
+                    for (int ks = 0; ks < nkO; ++ks)
+                        tc_mma(tmem + (uint32_t)(kTcDCols + sa * kTcN), dAO + so + (uint64_t)(16 * ks),
+                               dB + (uint64_t)(bl.bO + 16 * ks), idesc, (sa > 0 || ks > 0) ? 1u : 0u);
                 }
             }
             if (!ops.tc_stall) tc_commit(&mbar[0]);  // also when nothing was issued: the waiters are released
@@ -693,28 +704,27 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             break;  // uniform: no TMEM read, no further MMA
         }
         {
-            // warps w and w + 4 read the same TMEM lane quadrant (rows 32 (w%4)
-            // .. +31); the first combines columns 0..5, the second 6..11
-            const int w = threadIdx.x >> 5, quad = w & 3, half = (w >> 2) & 1;
-            if (w < 8 && 32 * quad < m8) {
-                long long T[6];
+            // warp w reads TMEM lane quadrant w % 4 (rows 32 (w % 4) .. +31):
+            // warps 0-3 of block E, warps 4-7 of block O, all 12 columns
+            const int w = threadIdx.x >> 5, quad = w & 3, blk = (w >> 2) & 1;
+            const int rows = blk ? t.o8 : t.e8;
+            if (w < 8 && 32 * quad < rows) {
+                long long T[12];
 #pragma unroll
-                for (int j = 0; j < 6; ++j) T[j] = 0;
+                for (int j = 0; j < 12; ++j) T[j] = 0;
+                const uint32_t base = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(blk * kTcDCols);
                 for (int c = 0; c < kTcClasses; ++c) {
                     float v[16];
-                    tc_ld16(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(c * kTcN), v);
-                    const long long wgt = 1LL << (7 * (kTcClasses - 1 - c));
+                    tc_ld16(base + (uint32_t)(c * kTcN), v);
 #pragma unroll
-                    for (int j = 0; j < 6; ++j) T[j] += (long long)tc_f2i(half ? v[6 + j] : v[j]) * wgt;
+                    for (int j = 0; j < 12; ++j) T[j] += tc_class_term(c, v[j]);
                 }
-                const int row = 32 * quad + (threadIdx.x & 31);
-                if (row < m8) {
+                const int r = 32 * quad + (threadIdx.x & 31);
+                if (r < rows) {
+                    const int row = blk ? t.e8 + r : r;
                     const int e = __ldg(&ops.tcE[(size_t)q * m8 + row]);
 #pragma unroll
-                    for (int j = 0; j < 6; ++j) {
-                        const int col = 6 * half + j;
-                        sR[col * m8 + row] = i2d_scaled(T[j], e + sF[col] - 52);
-                    }
+                    for (int j = 0; j < 12; ++j) sR[j * m8 + row] = i2d_scaled(T[j], e + sF[j] - 52);
                 }
             }
         }
@@ -756,7 +766,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (threadIdx.x < 32) tc_dealloc(tmem, 128);
+    if (threadIdx.x < 32) tc_dealloc(tmem, 2 * kTcDCols);
 }
 
 __global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepParams sp, Fields F, Fields Src,
@@ -774,10 +784,12 @@ __global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepPara
 // every mode, so its digit image is copied into shared memory once per CTA
 // and a CTA runs tiles of kTcVortCols right-hand-side columns (modes x fields
 // x re/im; 16, so that two 512-thread CTAs share an SM).
-// Per tile: (b) fold the fields; (c) column scales; (d) digits; (e) 35 MMAs
-// (digit slice sa of D1 against right-hand-side digit slices 0..6-sa side by
-// side, N = 16 (7-sa)) into 7 weight-class accumulators (112 TMEM columns);
-// (f) exact int64 combination -> D1.f in FP64; (g) Op::out per level pair.
+// Per tile: (b) fold the fields; (c) column scales; (d) digits; (e) per digit
+// slice sa of D1, the K-steps of block E (De: even outputs from the odd
+// inputs) and block O (Do: odd outputs from the even inputs) against the
+// right-hand-side digit slices 0..7-sa side by side, N = 16 (8-sa), into 8
+// weight-class accumulators per block (256 TMEM columns); (f) int64
+// combination -> D1.f in FP64; (g) Op::out per level pair.
 constexpr int kTcVortCols = 16;  // right-hand-side columns per tile (2 CTAs of 512 threads per SM)
 constexpr int kTcVortModes = kTcVortCols / 4;  // modes per tile: u, v x re, im
 constexpr int kTcCorrModes = kTcVortCols / 2;  // modes per tile: phi x re, im
@@ -789,10 +801,11 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     constexpr int kModes = kTcVortCols / (2 * Op::kFields);
     extern __shared__ __align__(128) unsigned char tcsm[];
     const TcGeom t = tc_geom(g.nz);
+    const TcBlocks bl = tc_blocks(t, true);
     const int nz = g.nz, he = t.he, ho = t.ho, m8 = t.m8;
-    const int a_halves = m8 * t.k16, b_halves = kTcVortCols * t.k16;
+    const int b_halves = kTcVortCols * t.kt;
     __half* sA = reinterpret_cast<__half*>(tcsm);
-    __half* sB = sA + kTcSlices * a_halves;
+    __half* sB = sA + kTcSlices * bl.a;
     double* sR = reinterpret_cast<double*>(sB + kTcSlices * b_halves);  // [32][m8]: folded u, v, then D1.u, D1.v
     int* sE = reinterpret_cast<int*>(sR + kTcVortCols * m8);            // row exponents of D1
     int* sF = sE + m8;                                                  // column exponents
@@ -805,7 +818,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         for (int i = tid; i < kTcSlices * b_halves / 8; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
     }
     for (int i = tid; i < m8; i += blockDim.x) sE[i] = __ldg(&ops.tcDE[i]);
-    if (tid < 32) tc_alloc(tbase, kTcClasses * kTcVortCols <= 128 ? 128 : 256);
+    if (tid < 32) tc_alloc(tbase, 2 * kTcClasses * kTcVortCols);
     if (tid == 0) {
         tc_mbar_init(&mbar[0]);
         tc_mbar_init(&mbar[1]);
@@ -817,10 +830,9 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     tc_fence_after();
     const uint32_t tmem = *tbase;
     if (tid == 0) {  // the D1 digit image, once
-        tc_mbar_expect(&mbar[1], (uint32_t)(kTcSlices * a_halves * sizeof(__half)));
+        tc_mbar_expect(&mbar[1], (uint32_t)(kTcSlices * bl.a * sizeof(__half)));
         for (int s = 0; s < kTcSlices; ++s)
-            tc_bulk_g2s(sA + s * a_halves, ops.tcD + (size_t)s * a_halves, (uint32_t)(a_halves * sizeof(__half)),
-                        &mbar[1]);
+            tc_bulk_g2s(sA + s * bl.a, ops.tcD + (size_t)s * bl.a, (uint32_t)(bl.a * sizeof(__half)), &mbar[1]);
     }
     const int nv = he + ho;
     for (int tile = tile0; tile < tile1; ++tile) {
@@ -870,14 +882,15 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             }
         }
         __syncthreads();
-        // (d) digits, one level of one column per thread (a warp: 8 levels of 4 columns)
-        for (int i = tid; i < kTcVortCols * m8; i += blockDim.x) {
+        // (d) digits, one K row of one column per thread (a warp: 8 K rows of
+        // 4 columns): even levels at K [0, he), odd ones at K [ke, ke + ho)
+        for (int i = tid; i < kTcVortCols * t.kt; i += blockDim.x) {
             const int kl = i & 7, cc = i >> 3;
-            const int c = cc % kTcVortCols, row = (cc / kTcVortCols) * 8 + kl;
-            const bool valid = row < he || (row >= t.e8 && row < t.e8 + ho);
+            const int c = cc % kTcVortCols, kk = (cc / kTcVortCols) * 8 + kl;
+            const int row = kk < t.ke ? (kk < he ? kk : -1) : (kk - t.ke < ho ? t.e8 + (kk - t.ke) : -1);
             int d[kTcSlices];
-            tc_digits(valid ? tc_fixed(sR[c * m8 + row], sF[c]) : 0, d);
-            __half* dst = sB + tc_core_off(c, row, t.k16);
+            tc_digits(row >= 0 ? tc_fixed(sR[c * m8 + row], sF[c]) : 0, d);
+            __half* dst = sB + tc_core_off(c, kk, t.kt);
 #pragma unroll
             for (int s = 0; s < kTcSlices; ++s) dst[s * b_halves] = __int2half_rn(d[s]);
         }
@@ -890,16 +903,21 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             if (tile == tile0) *landed = tc_mbar_wait(&mbar[1], 0, 1 << 22) ? 1 : 0;
             if (*landed && !ops.tc_stall) {
                 // the descriptors differ only in their start address (16-byte
-                // units in the low field): one add per MMA
-                const uint32_t sbo = (uint32_t)t.k16 * 16;
-                const int nks = t.k16 / 16;
-                const uint64_t da0 = tc_desc(tc_smem_u32(sA), 128, sbo), db0 = tc_desc(tc_smem_u32(sB), 128, sbo);
+                // units; a K offset of k elements is k units): one add per MMA
+                const uint64_t dAE = tc_desc(tc_smem_u32(sA), 128, (uint32_t)bl.kE * 16);
+                const uint64_t dAO = tc_desc(tc_smem_u32(sA + bl.aE), 128, (uint32_t)bl.kO * 16);
+                const uint64_t dB = tc_desc(tc_smem_u32(sB), 128, (uint32_t)t.kt * 16);
+                const int nkE = bl.kE / 16, nkO = bl.kO / 16;
+                constexpr uint32_t kDC = kTcClasses * kTcVortCols;
                 for (int sa = 0; sa < kTcSlices; ++sa) {
                     const uint32_t idesc = tc_idesc(kTcVortCols * (kTcSlices - sa));
-                    const uint64_t das = da0 + (uint64_t)((sa * a_halves * 2) >> 4);
-                    for (int ks = 0; ks < nks; ++ks)
-                        tc_mma(tmem + (uint32_t)(sa * kTcVortCols), das + (uint64_t)(16 * ks), db0 + (uint64_t)(16 * ks),
-                               idesc, (sa > 0 || ks > 0) ? 1u : 0u);
+                    const uint64_t so = (uint64_t)((sa * bl.a * 2) >> 4);
+                    for (int ks = 0; ks < nkE; ++ks)
+                        tc_mma(tmem + (uint32_t)(sa * kTcVortCols), dAE + so + (uint64_t)(16 * ks),
+                               dB + (uint64_t)(bl.bE + 16 * ks), idesc, (sa > 0 || ks > 0) ? 1u : 0u);
+                    for (int ks = 0; ks < nkO; ++ks)
+                        tc_mma(tmem + kDC + (uint32_t)(sa * kTcVortCols), dAO + so + (uint64_t)(16 * ks),
+                               dB + (uint64_t)(bl.bO + 16 * ks), idesc, (sa > 0 || ks > 0) ? 1u : 0u);
                 }
             }
             if (!ops.tc_stall) tc_commit(&mbar[0]);
@@ -920,27 +938,32 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             break;
         }
         {
+            // warp w reads TMEM lane quadrant w % 4; the warps of a quadrant
+            // (w / 4 = 0 .. 3) take the (block, 8-column group) items of it
             const int w = tid >> 5, quad = w & 3, grp = w >> 2, ngrp = (int)(blockDim.x >> 7);
-            if (32 * quad < m8) {
-                for (int cb = grp; cb < kTcVortCols / 8; cb += ngrp) {
-                    long long T[8];
+            for (int it = grp; it < 2 * (kTcVortCols / 8); it += ngrp) {
+                const int blk = it / (kTcVortCols / 8), cb = it - blk * (kTcVortCols / 8);
+                const int rows = blk ? t.o8 : t.e8;
+                if (32 * quad >= rows) continue;
+                long long T[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) T[j] = 0;
-                    for (int c = 0; c < kTcClasses; ++c) {
-                        float v[8];
-                        tc_ld8(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(c * kTcVortCols + 8 * cb), v);
-                        const long long wgt = 1LL << (7 * (kTcClasses - 1 - c));
+                for (int j = 0; j < 8; ++j) T[j] = 0;
+                const uint32_t base = tmem + ((uint32_t)(32 * quad) << 16) +
+                                      (uint32_t)(blk * kTcClasses * kTcVortCols + 8 * cb);
+                for (int c = 0; c < kTcClasses; ++c) {
+                    float v[8];
+                    tc_ld8(base + (uint32_t)(c * kTcVortCols), v);
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) T[j] += (long long)tc_f2i(v[j]) * wgt;
-                    }
-                    const int row = 32 * quad + (tid & 31);
-                    if (row < m8) {
-                        const int e = sE[row];
+                    for (int j = 0; j < 8; ++j) T[j] += tc_class_term(c, v[j]);
+                }
+                const int r = 32 * quad + (tid & 31);
+                if (r < rows) {
+                    const int row = blk ? t.e8 + r : r;
+                    const int e = sE[row];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const int col = 8 * cb + j;
-                            sR[col * m8 + row] = i2d_scaled(T[j], e + sF[col] - 52);
-                        }
+                    for (int j = 0; j < 8; ++j) {
+                        const int col = 8 * cb + j;
+                        sR[col * m8 + row] = i2d_scaled(T[j], e + sF[col] - 52);
                     }
                 }
             }
@@ -969,7 +992,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (tid < 32) tc_dealloc(tmem, kTcClasses * kTcVortCols <= 128 ? 128 : 256);
+    if (tid < 32) tc_dealloc(tmem, 2 * kTcClasses * kTcVortCols);
 }
 
 // omega = (wy - vz, uz - wx, vx - uy) from D1.u, D1.v, as vorticity_body forms it
@@ -1089,6 +1112,72 @@ __device__ __forceinline__ double2 pressure_rhs(const GridDev& g, const Ops& ops
     }
     if (m == 0 && z == 0) b = make_double2(0.0, 0.0);
     return b;
+}
+
+// Residual of the Galerkin Poisson system the pressure step solves
+// (solve_pressure_3d_standard, DNS_pressure_BC_3D.f90:1680-1714, or the weak
+// form 1793-1816): r = b(u*) - P phi with P = -S - diag(k^2 w ybar/2), the
+// right-hand side b formed from u*, v*, w* exactly as the FP64 pressure
+// kernel forms it, and phi the solution the step left in PHI; mode (0,0)
+// without its pinned row and column.  Every row is an equation of the system
+// (the Neumann problem has no boundary rows).  Per CTA a tile of tc modes;
+// max |r| and max |b| (over re and im parts) go to out[0], out[1] as the bits
+// of non-negative doubles (atomicMax on their bit patterns).
+__global__ void __launch_bounds__(256) k_poisson_residual(GridDev g, Ops ops, StepParams sp,
+                                                          const double2* __restrict__ US,
+                                                          const double2* __restrict__ VS,
+                                                          const double2* __restrict__ WS,
+                                                          const double2* __restrict__ PHI, int tc,
+                                                          unsigned long long* out) {
+    extern __shared__ double2 sm[];
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
+    double2* tw = sm;                 // folded w* tile [nz][tc]
+    double2* tp = sm + (size_t)nz * tc;  // phi tile, unfolded [nz][tc]
+    const int m0 = blockIdx.x * tc;
+    fold_load(tw, WS, g, m0, tc, he, ho);
+    for (int t = threadIdx.x; t < nz * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        tp[t] = m < g.nm ? PHI[(size_t)k * g.nm + m] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const double* __restrict__ Ae = sp.weak_form ? ops.W1e : ops.D1e;
+    const double* __restrict__ Ao = sp.weak_form ? ops.W1o : ops.D1o;
+    double rmax = 0.0, bmax = 0.0;
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        if (m >= g.nm) continue;
+        const Pair dz = anti_apply(Ae, Ao, tw, k, c, tc, he, ho);
+        const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const int q = mode_q(mi.ky, mi.kx, g.ny, g.nxhp);
+        const double k2 = __ldg(&ops.ksq[q]);
+        for (int h = 0; h < (k < ho ? 2 : 1); ++h) {
+            const int z = h ? nz - 1 - k : k;
+            if (m == 0 && z == 0) continue;  // the pinned row
+            const double2 b = pressure_rhs(g, ops, sp, z, m, mi, US, VS, h ? dz.b : dz.a);
+            double2 sp_ = make_double2(0.0, 0.0);  // (S phi)_z over the columns kept
+            for (int n = (m == 0 ? 1 : 0); n < nz; ++n) {
+                const double a = __ldg(&ops.S[(size_t)z * nz + n]);
+                const double2 f = tp[n * tc + c];
+                sp_.x = fma(a, f.x, sp_.x);
+                sp_.y = fma(a, f.y, sp_.y);
+            }
+            const double2 f = tp[z * tc + c];
+            const double kw = k2 * __ldg(&ops.wh[z]);
+            const double rx = b.x + sp_.x + kw * f.x, ry = b.y + sp_.y + kw * f.y;
+            rmax = fmax(rmax, fmax(fabs(rx), fabs(ry)));
+            bmax = fmax(bmax, fmax(fabs(b.x), fabs(b.y)));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        bmax = fmax(bmax, __shfl_xor_sync(0xffffffffu, bmax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&out[0], (unsigned long long)__double_as_longlong(rmax));
+        atomicMax(&out[1], (unsigned long long)__double_as_longlong(bmax));
+    }
 }
 
 __device__ __forceinline__ void pressure_body(GridDev g, Ops ops, StepParams sp,
@@ -2502,10 +2591,23 @@ cudaError_t launch_viscous(const GridDev& g, const Ops& ops, const StepParams& s
     return cudaGetLastError();
 }
 
+cudaError_t launch_poisson_residual(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
+                                    const double2* VS, const double2* WS, const double2* PHI,
+                                    unsigned long long* out, cudaStream_t s) {
+    constexpr int tc = 16;
+    const size_t sm = 2 * (size_t)g.nz * tc * sizeof(double2);
+    cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    if ((e = set_smem(k_poisson_residual, sm)) != cudaSuccess) return e;
+    k_poisson_residual<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, sp, US, VS, WS, PHI, tc, out);
+    return cudaGetLastError();
+}
+
 size_t viscous_tc_smem(const GridDev& g) {
     const TcGeom t = tc_geom(g.nz);
-    return (size_t)kTcSlices * (t.m8 + kTcN) * t.k16 * sizeof(__half) + (size_t)kTcN * t.m8 * sizeof(double) +
-           kTcN * sizeof(int) + 2 * sizeof(uint64_t) + 16;  // + TMEM address, arrival flag
+    return (size_t)kTcSlices * (tc_blocks(t, false).a + kTcN * t.kt) * sizeof(__half) +
+           (size_t)kTcN * t.m8 * sizeof(double) + kTcN * sizeof(int) + 2 * sizeof(uint64_t) +
+           16;  // + TMEM address, arrival flag
 }
 
 bool viscous_tc_fits(const GridDev& g) {
@@ -2528,7 +2630,7 @@ cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams
 
 size_t vorticity_tc_smem(const GridDev& g) {
     const TcGeom t = tc_geom(g.nz);
-    return (size_t)kTcSlices * (t.m8 + kTcVortCols) * t.k16 * sizeof(__half) +
+    return (size_t)kTcSlices * (tc_blocks(t, true).a + kTcVortCols * t.kt) * sizeof(__half) +
            (size_t)kTcVortCols * t.m8 * sizeof(double) + (size_t)(t.m8 + kTcVortCols) * sizeof(int) +
            2 * sizeof(uint64_t) + 16;
 }

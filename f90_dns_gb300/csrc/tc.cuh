@@ -3,22 +3,35 @@
 //
 // Emulated FP64 products (an Ozaki-style split into exact integer slices):
 // a matrix row is scaled by a power of two 2^e with |a_ij| < 2^e, rounded to
-// the integer U = round(a 2^(47-e)) (|U| <= 2^47) and written in 7 balanced
-// base-128 digits, U = sum_s c_s 128^(6-s), c_s in [-64, 63]; a right-hand
+// the integer U = round(a 2^(54-e)) (|U| <= 2^54) and written in 8 balanced
+// base-128 digits, U = sum_s c_s 128^(7-s), c_s in [-64, 63]; a right-hand
 // side column likewise with its own power of two 2^f.  Every digit is an
 // integer that FP16 holds exactly, so one tcgen05.mma (kind::f16, FP32
 // accumulation) of two digit matrices is exact while its sums stay below 2^24:
-// |c d| <= 2^12, times at most 127 terms of K, times at most 7 digit pairs
-// summed into one accumulator, is below 2^22.  The 28 pairs (s, t) with
-// s + t <= 6 go into 7 accumulators by weight class c = s + t, which are
-// combined exactly in 64-bit integers, T = sum_c D_c 128^(6-c), and
-// a b = T 2^(e+f-52) up to the dropped classes (relative 2^-47 of the row and
-// column scales), one int64->FP64 conversion and one power-of-two scaling per
-// output instead of a K-term FP64 dot product.
+// |c d| <= 2^12, times at most 128 terms of K, times at most 8 digit pairs
+// summed into one accumulator, is at most 2^22.  The 36 pairs (s, t) with
+// s + t <= 7 go into 8 accumulators by weight class c = s + t, combined in
+// 64-bit integers as T = sum_{c<=6} D_c 128^(6-c) + round(D_7 / 128)
+// (|T| < 2^62), and a b = T 2^(e+f-52) up to the dropped classes and that
+// rounding: an error of about 2^-53 of the product of the row and column
+// scales, one int64->FP64 conversion and one power-of-two scaling per output
+// instead of a K-term FP64 dot product.
+//
+// Operators are folded into even and odd blocks (centro-symmetric: diag(Ge,
+// Go); centro-antisymmetric: [[0, De], [Do, 0]]).  Each block is its own
+// M = 128 MMA on its own rows: block E (the even output rows, e8 of them) and
+// block O (the odd output rows, o8), so a block of up to 128 rows fits, i.e.
+// nz <= 255.  The right-hand sides hold the even input levels at K indices
+// [0, ke) and the odd ones at [ke, ke + ko) (each padded to a multiple of 16
+// for the MMA K-steps); a symmetric block E reads K [0, ke) and block O reads
+// [ke, ke + ko); an antisymmetric block E (De) reads the odd inputs and block
+// O (Do) the even ones.  Rows past a block's e8 or o8 are whatever follows in
+// shared memory: the MMA reads them, and their products land in TMEM lanes
+// that are never read.
 //
 // Shared-memory operands: K-major, no swizzle, "core matrices" of 8 rows x 8
 // FP16 (16 bytes per row, 128 bytes per core matrix); K-adjacent core
-// matrices are 128 B apart (LBO), 8-row groups k16*16 B apart (SBO).
+// matrices are 128 B apart (LBO), 8-row groups (K width x 2) B apart (SBO).
 #pragma once
 
 #include <cuda_fp16.h>
@@ -26,16 +39,19 @@
 
 namespace dns3d {
 
-constexpr int kTcSlices = 7;    // digits per value
-constexpr int kTcClasses = 7;   // digit-pair weight classes kept (s + t <= 6)
+constexpr int kTcSlices = 8;    // digits per value
+constexpr int kTcClasses = 8;   // digit-pair weight classes kept (s + t <= 7)
+constexpr int kTcFixBits = 54;  // U = round(a 2^(54-e))
 constexpr int kTcN = 16;        // MMA N: columns of one right-hand-side block
-constexpr int kTcM = 128;       // MMA M (rows beyond m8 are ignored)
+constexpr int kTcM = 128;       // MMA M (rows beyond a block's size are ignored)
+constexpr int kTcDCols = kTcClasses * kTcN;  // TMEM columns of one block's accumulators
 
-// Block-diagonal placement of the folded operator diag(Ge, Go): even rows and
-// K indices at [0, he), odd ones at [e8, e8 + ho), each block padded to a
-// multiple of 8; K padded to a multiple of 16 for the MMA K-steps.
+// Folded operator geometry: even block he x he (symmetric) or he x ho
+// (antisymmetric), odd block ho x ho or ho x he; rows padded to multiples of
+// 8 (e8, o8; m8 = e8 + o8 rows of row exponents, even rows first), K widths
+// padded to multiples of 16 (ke, ko; kt = ke + ko right-hand-side rows).
 struct TcGeom {
-    int he, ho, e8, o8, m8, k16, ncore_e, ncore_o;
+    int he, ho, e8, o8, m8, ke, ko, kt, ncore_e, ncore_o;
 };
 
 __host__ __device__ inline TcGeom tc_geom(int nz) {
@@ -45,14 +61,36 @@ __host__ __device__ inline TcGeom tc_geom(int nz) {
     t.e8 = (t.he + 7) / 8 * 8;
     t.o8 = (t.ho + 7) / 8 * 8;
     t.m8 = t.e8 + t.o8;
-    t.k16 = (t.m8 + 15) / 16 * 16;
+    t.ke = (t.he + 15) / 16 * 16;
+    t.ko = (t.ho + 15) / 16 * 16;
+    t.kt = t.ke + t.ko;
     t.ncore_e = (t.e8 / 8) * (t.e8 / 8);
     t.ncore_o = (t.o8 / 8) * (t.o8 / 8);
     return t;
 }
 
-// The block-diagonal operator must fit one M = 128 MMA.
-__host__ __device__ inline bool tc_supported(int nz) { return tc_geom(nz).m8 <= kTcM; }
+// Each folded block must fit one M = 128 MMA (and the K of one MMA, 128, in
+// the exactness bound above).
+__host__ __device__ inline bool tc_supported(int nz) { return tc_geom(nz).ke <= kTcM; }
+
+// K widths of blocks E and O and the K offsets of their right-hand-side rows:
+// symmetric E = Ge (ke, inputs at 0), O = Go (ko, inputs at ke); antisymmetric
+// E = De (ko, the odd inputs at ke), O = Do (ke, the even inputs at 0).
+struct TcBlocks {
+    int kE, kO, bE, bO;
+    int aE, a;  // halves of block E, of one digit slice (E then O)
+};
+
+__host__ __device__ inline TcBlocks tc_blocks(const TcGeom& t, bool anti) {
+    TcBlocks b;
+    b.kE = anti ? t.ko : t.ke;
+    b.kO = anti ? t.ke : t.ko;
+    b.bE = anti ? t.ke : 0;
+    b.bO = anti ? 0 : t.ke;
+    b.aE = t.e8 * b.kE;
+    b.a = b.aE + t.o8 * b.kO;
+    return b;
+}
 
 // Halves per q of the compact slice store: per digit, the nonzero core
 // matrices (even block row-major, then odd block), 64 halves each.
@@ -60,12 +98,12 @@ __host__ __device__ inline size_t tc_q_halves(const TcGeom& t) {
     return (size_t)kTcSlices * (t.ncore_e + t.ncore_o) * 64;
 }
 
-// Offset (in halves) of element (r, k) of a K-major operand with k16 columns.
-__host__ __device__ inline int tc_core_off(int r, int k, int k16) {
-    return ((r >> 3) * (k16 >> 3) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+// Offset (in halves) of element (r, k) of a K-major operand of K width kw.
+__host__ __device__ inline int tc_core_off(int r, int k, int kw) {
+    return ((r >> 3) * (kw >> 3) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
 }
 
-// Balanced base-128 digits of |U| <= 2^47, most significant first.
+// Balanced base-128 digits of |U| <= 2^54, most significant first.
 __device__ __forceinline__ void tc_digits(long long u, int* c) {
 #pragma unroll
     for (int s = kTcSlices - 1; s >= 0; --s) {
@@ -76,7 +114,7 @@ __device__ __forceinline__ void tc_digits(long long u, int* c) {
     }
 }
 
-// round(x 2^(47-f)) for |x| < 2^f, from the bits of x (integer operations only).
+// round(x 2^(54-f)) for |x| < 2^f, from the bits of x (integer operations only).
 __device__ __forceinline__ long long tc_fixed(double x, int f) {
     const long long b = __double_as_longlong(x);
     int ex = (int)((b >> 52) & 0x7FF);
@@ -87,7 +125,7 @@ __device__ __forceinline__ long long tc_fixed(double x, int f) {
     } else {
         m |= 1LL << 52;
     }
-    const int sh = 1028 + f - ex;  // x = m 2^(ex-1075); U = m 2^(ex-1075+47-f)
+    const int sh = 1075 - kTcFixBits + f - ex;  // x = m 2^(ex-1075); U = m 2^(ex-1075+54-f)
     if (sh >= 62) return 0;
     const long long u = sh > 0 ? (m + (1LL << (sh - 1))) >> sh : m << (-sh);
     return b < 0 ? -u : u;
@@ -102,6 +140,12 @@ __device__ __forceinline__ int tc_exponent(unsigned long long absbits) {
 
 // Exact FP32 integer (|v| < 2^22) to int.
 __device__ __forceinline__ int tc_f2i(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
+
+// Adds class c's accumulator to the combination T (see the header comment).
+__device__ __forceinline__ long long tc_class_term(int c, float v) {
+    const long long d = (long long)tc_f2i(v);
+    return c < kTcClasses - 1 ? d * (1LL << (7 * (kTcClasses - 2 - c))) : (d + 64) >> 7;
+}
 
 __device__ __forceinline__ uint32_t tc_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 

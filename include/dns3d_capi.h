@@ -184,6 +184,18 @@ int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out);
 int dns3d_output_diagnostics(dns3d_handle* h, dns3d_diag* out);
 int dns3d_check_divergence(dns3d_handle* h, double* max_div);
 
+/* Accuracy of the last pressure solve: the relative residual max|b - P phi| /
+ * max|b| of the Galerkin Poisson system that solve_pressure_3d_standard
+ * builds and solves per mode (3D:1680-1714; the weak form 1793-1816):
+ * P = -S - diag(k^2 w ybar/2), b from the handle's u*, v*, w* and phi its
+ * solution, mode (0,0) without its pinned row and column.  This is the
+ * divergence the projection controls; the collocation max|div u| of
+ * check_divergence_3d also carries the wall rows the boundary conditions
+ * overwrite after the projection.  Valid after a step (or after the
+ * five-stage calls up to dns3d_pressure_correction).  No counterpart in the
+ * reference. */
+int dns3d_projection_residual(dns3d_handle* h, double* rel);
+
 /* Measurement helpers (no counterpart in the reference, whose only timing is
  * cpu_time around each step, 3D:287-360).
  * dns3d_step_timed: dns3d_step with CUDA events recorded on the handle's
