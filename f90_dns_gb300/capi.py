@@ -91,6 +91,7 @@ class CConfig(C.Structure):
         ("convection_scheme", C.c_int), ("linear_solver", C.c_int),
         ("cgstol", C.c_double),
         ("noise_amplitude", C.c_double),
+        ("poisson_refinement", C.c_int), ("pad_", C.c_int),
     ]
 
 

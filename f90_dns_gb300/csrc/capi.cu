@@ -138,6 +138,7 @@ int validate(const dns3d_config* c) {
     if (c->linear_solver == 1 && !(c->cgstol > 0.0)) return DNS3D_E_INVALID;
     if (c->linear_solver == 1 && c->precision != DNS3D_PREC_FP64) return DNS3D_E_UNSUPPORTED;
     if (!(c->noise_amplitude >= 0.0)) return DNS3D_E_INVALID;
+    if (c->poisson_refinement != 0 && c->poisson_refinement != 1) return DNS3D_E_INVALID;
     return DNS3D_OK;
 }
 
@@ -612,6 +613,8 @@ int dns3d_config_defaults(dns3d_config* c) {
     c->linear_solver = 0;
     c->cgstol = 1.0e-6;  // 3D:575
     c->noise_amplitude = 0.0;
+    c->poisson_refinement = 1;
+    c->pad_ = 0;
     return DNS3D_OK;
 }
 
@@ -1089,6 +1092,10 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             return r;
         };
         const std::vector<float2> D1e_df = split(D1e), D1o_df = split(D1o), W1e_df = split(W1e), W1o_df = split(W1o);
+        std::vector<double> Sfe, Sfo;
+        fold_symmetric(S, nz, Sfe, Sfo);
+        std::vector<float2> Se_df = split(Sfe), So_df = split(Sfo);
+        if (So_df.empty()) So_df.assign(1, float2{0.f, 0.f});
         // eigenbasis of the full Neumann problem S V' = M V' Lambda':
         // C = M^-1/2 S M^-1/2 is centro-symmetric; the orthogonal fold
         // e_i = (x_i + x_{n-1-i})/sqrt2, o_i = (x_i - x_{n-1-i})/sqrt2 (middle
@@ -1178,6 +1185,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             (rc = dev_alloc(h, &mx.plame, plame.size())) || (rc = dev_alloc(h, &mx.plamo, plamo.size())) ||
             (rc = dev_alloc(h, &mx.D1e_df, D1e_df.size())) || (rc = dev_alloc(h, &mx.D1o_df, D1o_df.size())) ||
             (rc = dev_alloc(h, &mx.W1e_df, W1e_df.size())) || (rc = dev_alloc(h, &mx.W1o_df, W1o_df.size())) ||
+            (rc = dev_alloc(h, &mx.Se_df, Se_df.size())) || (rc = dev_alloc(h, &mx.So_df, So_df.size())) ||
             (rc = dev_alloc(h, &h->PHIZ, se)))
             return fail(rc);
         struct Up32 { void* d; const void* s; size_t b; } u32[] = {
@@ -1191,7 +1199,8 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             {mx.PDe, PDe.data(), PDe.size() * 4}, {mx.PDo, PDo.data(), PDo.size() * 4},
             {mx.plame, plame.data(), plame.size() * 4}, {mx.plamo, plamo.data(), plamo.size() * 4},
             {mx.D1e_df, D1e_df.data(), D1e_df.size() * 8}, {mx.D1o_df, D1o_df.data(), D1o_df.size() * 8},
-            {mx.W1e_df, W1e_df.data(), W1e_df.size() * 8}, {mx.W1o_df, W1o_df.data(), W1o_df.size() * 8}};
+            {mx.W1e_df, W1e_df.data(), W1e_df.size() * 8}, {mx.W1o_df, W1o_df.data(), W1o_df.size() * 8},
+            {mx.Se_df, Se_df.data(), Se_df.size() * 8}, {mx.So_df, So_df.data(), So_df.size() * 8}};
         for (auto& u : u32)
             if ((rc = upload(h, u.d, u.s, u.b))) return fail(rc);
         for (int f = 0; f < 6; ++f)
@@ -1209,6 +1218,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     sp.cn_fac = c.use_crank_nicolson ? 0.5 * c.dt / c.re : 0.0;
     sp.helm_f = helm_f;
     sp.cn_identity = (sp.cn_fac != 0.0 && sp.cn_fac == helm_f) ? 1 : 0;
+    sp.refine = (h->mixed && c.poisson_refinement) ? 1 : 0;
     sp.forcing_scale = (double)c.nx * (double)c.ny;
     sp.dealias = c.use_dealias_23_rule;
     sp.kx_max = (c.nx / 2) * 2 / 3;

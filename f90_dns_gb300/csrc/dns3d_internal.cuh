@@ -162,6 +162,7 @@ struct StepParams {
     int cn_identity;      // Crank-Nicolson: explicit half folded into the implicit solve (step.cu)
     int bc_walls;         // projection: write the wall planes of u, v, w as zero (apply_boundary_conditions_3d
                           // fused into it; set by the fused step, not by the five-stage calls)
+    int refine;           // mixed pressure: one step of iterative refinement (dns3d_config::poisson_refinement)
 };
 
 // z-operators in parity-folded form (see step.cu): for nz levels,
@@ -245,6 +246,9 @@ struct MixedOps {
     float* PAe; float* PAo; float* PBe; float* PBo; float* PDe; float* PDo;
     float* plame;            // [phe4] eigenvalues of the even block
     float* plamo;            // [pho4] eigenvalues of the odd block
+    // folded stiffness S (symmetric fold of ops.S) as double-float pairs, for
+    // the FP64-accurate residual of the refinement: Se [he][he], So [ho][ho]
+    float2* Se_df; float2* So_df;
 };
 
 struct PIParams {

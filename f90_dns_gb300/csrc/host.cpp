@@ -241,6 +241,7 @@ bool assign(dns3d_config* c, const std::string& group, const std::string& key, c
         // extension keys of this library (not read by the reference)
         LOG_KEY("lgl_dmatrix_guard", lgl_dmatrix_guard)
         INT_KEY("convection_scheme", convection_scheme) INT_KEY("linear_solver", linear_solver)
+        LOG_KEY("poisson_refinement", poisson_refinement)
     }
 #undef INT_KEY
 #undef REAL_KEY

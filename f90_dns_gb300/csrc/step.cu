@@ -1988,13 +1988,14 @@ __device__ __forceinline__ double df_value(DF s) { return f2d(s.hi) + f2d(s.lo);
 
 // Folded tile of an FP64 field as double-float pairs: [he][tc] even, [ho][tc] odd;
 // each element float4 = (re.hi, re.lo, im.hi, im.lo).
+// (skip0: mode 0 is left zero and not read, e.g. while another kernel writes it)
 __device__ __forceinline__ void fold_load_df(float4* tile, const double2* __restrict__ src, const GridDev& g,
-                                             int m0, int tc, int he, int ho) {
+                                             int m0, int tc, int he, int ho, bool skip0 = false) {
     for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
         const int k = t / tc, c = t - k * tc;
         const int m = m0 + c;
         double2 fe = make_double2(0.0, 0.0), fo = fe;
-        if (m < g.nm) {
+        if (m < g.nm && !(skip0 && m == 0)) {
             const double2 a = src[(size_t)k * g.nm + m];
             if (k < ho) {
                 const double2 b = src[(size_t)(g.nz - 1 - k) * g.nm + m];
@@ -2045,57 +2046,44 @@ __device__ __forceinline__ Pair anti_apply_df(const float2* __restrict__ De, con
     return p;
 }
 
-// Pressure for the mixed form.  The right-hand side (the collocation
-// divergence of u*, or the weak form) is formed in FP64: D applied to the
-// full FP64 w* must not see FP32 rounding of w* (|D| ~ nz^2 would amplify it).
-// The Neumann Poisson operator is diagonal in the eigenbasis of the full
-// problem, S V' = M V' Lambda', V'^T M V' = I:
-//   phi = -V' diag(1/(l'_j + k^2)) V'^T b,   dphi/dz = -(D V') diag(...) V'^T b
-// evaluated in FP32 on the folded basis (even eigenvectors on the pair sums
-// of b, odd ones on the differences, MixedOps); computing dphi/dz through the
-// precomputed D V' keeps its FP32 error relative to dphi/dz itself.  Mode
-// (0,0) (pinned) is left to the FP64 kernels.
-__device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops ops, StepParams sp,
-                                                    const double2* __restrict__ US,
-                                                    const double2* __restrict__ VS,
-                                                    const double2* __restrict__ WS,
-                                                    double2* __restrict__ PHI, double2* __restrict__ PHIZ,
-                                                    int tc, int bx) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    const int nz = g.nz, he = ops.he, ho = ops.ho;
-    const int pe4 = mx.phe4, po4 = mx.pho4, nbe = pe4 / 4, nbo = po4 / 4;
-    float4* tw = reinterpret_cast<float4*>(smraw);              // folded w* (double-float)  [nz][tc]
-    float2* tb = reinterpret_cast<float2*>(tw + nz * tc);       // folded rhs: s [pe4][tc], d [po4][tc]
-    float2* tp = tb + (pe4 + po4) * tc;                         // phi~: even [pe4][tc], odd [po4][tc]
-    const int m0 = bx * tc;
-    fold_load_df(tw, WS, g, m0, tc, he, ho);
-    for (int t = threadIdx.x; t < (pe4 - he) * tc; t += blockDim.x) tb[he * tc + t] = make_float2(0.f, 0.f);
-    for (int t = threadIdx.x; t < (po4 - ho) * tc; t += blockDim.x) tb[(pe4 + ho) * tc + t] = make_float2(0.f, 0.f);
-    __syncthreads();
-    const float2* __restrict__ Ae = sp.weak_form ? mx.W1e_df : mx.D1e_df;
-    const float2* __restrict__ Ao = sp.weak_form ? mx.W1o_df : mx.D1o_df;
-    // right-hand side pair (k, nz-1-k), folded in FP64 before the rounding
-    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
-        const int k = t / tc, c = t - k * tc;
-        const int m = m0 + c;
-        float2 fs = make_float2(0.f, 0.f), fd = fs;
-        if (m < g.nm && m != 0) {
-            const Pair dz = anti_apply_df(Ae, Ao, tw, k, c, tc, he, ho);
-            const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-            const double2 b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
-            if (k < ho) {
-                const double2 b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
-                fs = make_float2(d2f(b1.x + b2.x), d2f(b1.y + b2.y));
-                fd = make_float2(d2f(b1.x - b2.x), d2f(b1.y - b2.y));
-            } else {
-                fs = make_float2(d2f(b1.x), d2f(b1.y));
-            }
-        }
-        tb[k * tc + c] = fs;
-        if (k < ho) tb[(pe4 + k) * tc + c] = fd;
+// Symmetric folded operator (double-float) on a double-float folded tile: the
+// output pair (z = k, z = nz-1-k) as FP64 (sym_apply's fold).
+__device__ __forceinline__ Pair sym_apply_df(const float2* __restrict__ Ae, const float2* __restrict__ Ao,
+                                             const float4* tile, int k, int c, int tc, int he, int ho) {
+    DF yex{0.f, 0.f}, yey{0.f, 0.f}, yox{0.f, 0.f}, yoy{0.f, 0.f};
+    const float2* er = Ae + (size_t)k * he;
+    for (int j = 0; j < he; ++j) {
+        const float2 a = __ldg(&er[j]);
+        const float4 b = tile[j * tc + c];
+        df_mac(yex, a.x, a.y, b.x, b.y);
+        df_mac(yey, a.x, a.y, b.z, b.w);
     }
-    __syncthreads();
-    // phi~_j = -(V'^T b)_j / (l'_j + k^2), 4 eigen-rows of one block per thread
+    Pair p;
+    if (k < ho) {
+        const float2* orow = Ao + (size_t)k * ho;
+        const float4* fo = tile + he * tc;
+        for (int j = 0; j < ho; ++j) {
+            const float2 a = __ldg(&orow[j]);
+            const float4 b = fo[j * tc + c];
+            df_mac(yox, a.x, a.y, b.x, b.y);
+            df_mac(yoy, a.x, a.y, b.z, b.w);
+        }
+        const double ex = df_value(yex), ey = df_value(yey), ox = df_value(yox), oy = df_value(yoy);
+        p.a = make_double2(ex + ox, ey + oy);
+        p.b = make_double2(ex - ox, ey - oy);
+    } else {
+        p.a = make_double2(df_value(yex), df_value(yey));
+        p.b = p.a;
+    }
+    return p;
+}
+
+// phi~_j = -(V'^T b)_j / (l'_j + k^2) of the folded right-hand sides tb of a
+// mode tile, 4 eigen-rows of one block per thread, into tp.
+__device__ __forceinline__ void pressure_mixed_forward(const GridDev& g, const MixedOps& mx, const Ops& ops,
+                                                       const float2* tb, float2* tp, int m0, int tc) {
+    const int he = ops.he, ho = ops.ho;
+    const int pe4 = mx.phe4, po4 = mx.pho4, nbe = pe4 / 4, nbo = po4 / 4;
     for (int t = threadIdx.x; t < (nbe + nbo) * tc; t += blockDim.x) {
         const int jb = t / tc, c = t - jb * tc;
         const int m = m0 + c;
@@ -2130,9 +2118,16 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
 #pragma unroll
         for (int q = 0; q < 4; ++q) dst[(j0 + q) * tc] = acc[q];
     }
-    __syncthreads();
-    // phi = pe + po, dphi/dz = dze + dzo at levels (i, nz-1-i), 4 rows i per thread:
-    //   pe = PBe phi~e, po = PBo phi~o, dze = PDe phi~o, dzo = PDo phi~e
+}
+
+// phi = pe + po, dphi/dz = dze + dzo at levels (i, nz-1-i) from tp, 4 rows i
+// per thread: pe = PBe phi~e, po = PBo phi~o, dze = PDe phi~o, dzo = PDo
+// phi~e; stored into PHI, PHIZ, or added to them (a correction).
+__device__ __forceinline__ void pressure_mixed_back(const GridDev& g, const MixedOps& mx, const Ops& ops,
+                                                    const float2* tp, double2* __restrict__ PHI,
+                                                    double2* __restrict__ PHIZ, int m0, int tc, bool add) {
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
+    const int pe4 = mx.phe4, po4 = mx.pho4, nbe = pe4 / 4, nbo = po4 / 4;
     for (int t = threadIdx.x; t < nbe * tc; t += blockDim.x) {
         const int ib = t / tc, c = t - ib * tc;
         const int m = m0 + c;
@@ -2183,6 +2178,15 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
                 dd[3].x = fmaf(a.w, v.x, dd[3].x); dd[3].y = fmaf(a.w, v.y, dd[3].y);
             }
         }
+        auto put = [&](size_t o, double2* F, float x, float y) {
+            const double2 v = make_double2(f2d(x), f2d(y));
+            if (add) {
+                const double2 o0 = F[o];
+                F[o] = make_double2(o0.x + v.x, o0.y + v.y);
+            } else {
+                F[o] = v;
+            }
+        };
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int i = i0 + q;
@@ -2190,16 +2194,116 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
             const size_t o1 = (size_t)i * g.nm + m;
             if (i < ho) {
                 const size_t o2 = (size_t)(nz - 1 - i) * g.nm + m;
-                PHI[o1] = make_double2(f2d(pe[q].x + po[q].x), f2d(pe[q].y + po[q].y));
-                PHI[o2] = make_double2(f2d(pe[q].x - po[q].x), f2d(pe[q].y - po[q].y));
-                PHIZ[o1] = make_double2(f2d(de[q].x + dd[q].x), f2d(de[q].y + dd[q].y));
-                PHIZ[o2] = make_double2(f2d(de[q].x - dd[q].x), f2d(de[q].y - dd[q].y));
+                put(o1, PHI, pe[q].x + po[q].x, pe[q].y + po[q].y);
+                put(o2, PHI, pe[q].x - po[q].x, pe[q].y - po[q].y);
+                put(o1, PHIZ, de[q].x + dd[q].x, de[q].y + dd[q].y);
+                put(o2, PHIZ, de[q].x - dd[q].x, de[q].y - dd[q].y);
             } else {
-                PHI[o1] = make_double2(f2d(pe[q].x), f2d(pe[q].y));
-                PHIZ[o1] = make_double2(f2d(de[q].x), f2d(de[q].y));
+                put(o1, PHI, pe[q].x, pe[q].y);
+                put(o1, PHIZ, de[q].x, de[q].y);
             }
         }
     }
+}
+
+// Pressure for the mixed form.  The right-hand side (the collocation
+// divergence of u*, or the weak form) is formed in FP64: D applied to the
+// full FP64 w* must not see FP32 rounding of w* (|D| ~ nz^2 would amplify it).
+// The Neumann Poisson operator is diagonal in the eigenbasis of the full
+// problem, S V' = M V' Lambda', V'^T M V' = I:
+//   phi = -V' diag(1/(l'_j + k^2)) V'^T b,   dphi/dz = -(D V') diag(...) V'^T b
+// evaluated in FP32 on the folded basis (even eigenvectors on the pair sums
+// of b, odd ones on the differences, MixedOps); computing dphi/dz through the
+// precomputed D V' keeps its FP32 error relative to dphi/dz itself.  Mode
+// (0,0) (pinned) is left to the FP64 kernels.
+// With sp.refine, one step of iterative refinement follows in the same CTA
+// (each mode's system is its own): the residual r = b - P phi of the FP32
+// solution, P = -S - diag(k^2 w ybar/2), is formed from the FP64 b and the
+// stored phi with S applied in double-float (about 2^-48 relative, against
+// the 2^-24 of the FP32 solve), and the FP32 solve of P d = r is added to
+// phi and dphi/dz: the Galerkin residual drops from ~1e-7 to ~1e-13 of b.
+__device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops ops, StepParams sp,
+                                                    const double2* __restrict__ US,
+                                                    const double2* __restrict__ VS,
+                                                    const double2* __restrict__ WS,
+                                                    double2* __restrict__ PHI, double2* __restrict__ PHIZ,
+                                                    int tc, int bx) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int nz = g.nz, he = ops.he, ho = ops.ho;
+    const int pe4 = mx.phe4, po4 = mx.pho4;
+    float4* tw = reinterpret_cast<float4*>(smraw);              // folded w* (double-float)  [nz][tc]
+    float2* tb = reinterpret_cast<float2*>(tw + nz * tc);       // folded rhs: s [pe4][tc], d [po4][tc]
+    float2* tp = tb + (pe4 + po4) * tc;                         // phi~: even [pe4][tc], odd [po4][tc]
+    double2* bt = reinterpret_cast<double2*>(tp + (pe4 + po4) * tc);  // FP64 rhs [nz][tc] (refinement)
+    const int m0 = bx * tc;
+    fold_load_df(tw, WS, g, m0, tc, he, ho);
+    for (int t = threadIdx.x; t < (pe4 - he) * tc; t += blockDim.x) tb[he * tc + t] = make_float2(0.f, 0.f);
+    for (int t = threadIdx.x; t < (po4 - ho) * tc; t += blockDim.x) tb[(pe4 + ho) * tc + t] = make_float2(0.f, 0.f);
+    __syncthreads();
+    const float2* __restrict__ Ae = sp.weak_form ? mx.W1e_df : mx.D1e_df;
+    const float2* __restrict__ Ao = sp.weak_form ? mx.W1o_df : mx.D1o_df;
+    // right-hand side pair (k, nz-1-k), folded in FP64 before the rounding
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        float2 fs = make_float2(0.f, 0.f), fd = fs;
+        double2 b1 = make_double2(0.0, 0.0), b2 = b1;
+        if (m < g.nm && m != 0) {
+            const Pair dz = anti_apply_df(Ae, Ao, tw, k, c, tc, he, ho);
+            const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+            b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
+            if (k < ho) {
+                b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
+                fs = make_float2(d2f(b1.x + b2.x), d2f(b1.y + b2.y));
+                fd = make_float2(d2f(b1.x - b2.x), d2f(b1.y - b2.y));
+            } else {
+                fs = make_float2(d2f(b1.x), d2f(b1.y));
+            }
+        }
+        tb[k * tc + c] = fs;
+        if (k < ho) tb[(pe4 + k) * tc + c] = fd;
+        if (sp.refine) {
+            bt[k * tc + c] = b1;
+            if (k < ho) bt[(nz - 1 - k) * tc + c] = b2;
+        }
+    }
+    __syncthreads();
+    pressure_mixed_forward(g, mx, ops, tb, tp, m0, tc);
+    __syncthreads();
+    pressure_mixed_back(g, mx, ops, tp, PHI, PHIZ, m0, tc, false);
+    if (!sp.refine) return;
+    // refinement: r = b + S phi + k^2 wh phi (phi as stored, FP64)
+    __syncthreads();  // this CTA's PHI writes, then the folded phi in double-float
+    fold_load_df(tw, PHI, g, m0, tc, he, ho, true);
+    __syncthreads();
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        float2 fs = make_float2(0.f, 0.f), fd = fs;
+        if (m < g.nm && m != 0) {
+            const Pair sphi = sym_apply_df(mx.Se_df, mx.So_df, tw, k, c, tc, he, ho);
+            const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+            const double k2 = __ldg(&ops.ksq[mode_q(mi.ky, mi.kx, g.ny, g.nxhp)]);
+            const double2 p1 = PHI[(size_t)k * g.nm + m], c1 = bt[k * tc + c];
+            const double kw1 = k2 * __ldg(&ops.wh[k]);
+            const double2 r1 = make_double2(c1.x + sphi.a.x + kw1 * p1.x, c1.y + sphi.a.y + kw1 * p1.y);
+            if (k < ho) {
+                const double2 p2 = PHI[(size_t)(nz - 1 - k) * g.nm + m], c2 = bt[(nz - 1 - k) * tc + c];
+                const double kw2 = k2 * __ldg(&ops.wh[nz - 1 - k]);
+                const double2 r2 = make_double2(c2.x + sphi.b.x + kw2 * p2.x, c2.y + sphi.b.y + kw2 * p2.y);
+                fs = make_float2(d2f(r1.x + r2.x), d2f(r1.y + r2.y));
+                fd = make_float2(d2f(r1.x - r2.x), d2f(r1.y - r2.y));
+            } else {
+                fs = make_float2(d2f(r1.x), d2f(r1.y));
+            }
+        }
+        tb[k * tc + c] = fs;
+        if (k < ho) tb[(pe4 + k) * tc + c] = fd;
+    }
+    __syncthreads();
+    pressure_mixed_forward(g, mx, ops, tb, tp, m0, tc);
+    __syncthreads();
+    pressure_mixed_back(g, mx, ops, tp, PHI, PHIZ, m0, tc, true);
 }
 
 __global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
@@ -2439,7 +2543,8 @@ int tile_cols_mixed(const GridDev& g) {
 
 size_t pressure_mixed_smem(const GridDev& g, int tc) {
     const int ho = g.nz / 2, he = g.nz - ho;
-    return (size_t)g.nz * tc * sizeof(float4) + 2 * (size_t)(pad4(he) + pad4(ho)) * tc * sizeof(float2);
+    return (size_t)g.nz * tc * sizeof(float4) + 2 * (size_t)(pad4(he) + pad4(ho)) * tc * sizeof(float2) +
+           (size_t)g.nz * tc * sizeof(double2);  // the FP64 right-hand side kept for the refinement
 }
 
 namespace {

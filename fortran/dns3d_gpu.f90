@@ -45,6 +45,8 @@ module dns3d_gpu
         integer(c_int) :: linear_solver
         real(c_double) :: cgstol
         real(c_double) :: noise_amplitude
+        integer(c_int) :: poisson_refinement
+        integer(c_int) :: pad_
     end type dns3d_config
 
     ! PI controller globals (3D:75-89)

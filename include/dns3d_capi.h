@@ -100,6 +100,15 @@ typedef struct dns3d_config {
      * two outputs.  Not a reference feature (the large-grid workload's
      * initial condition); 0 = none.  Extension key of &perturbations. */
     double noise_amplitude;
+    /* Mixed precision only: 1 (default) = one step of iterative refinement of
+     * every mixed-precision Poisson solve (the residual of the FP32 solution
+     * formed with the stiffness matrix in double-float arithmetic, the FP32
+     * correction added), which brings the Galerkin residual of the system
+     * solve_pressure_3d_standard solves (3D:1680-1714) from ~1e-7 to ~1e-13
+     * of its right-hand side; 0 = the FP32 solve alone.  Extension key of
+     * &computational. */
+    int poisson_refinement;
+    int pad_;
 } dns3d_config;
 
 /* PI controller globals (DNS_pressure_BC_3D.f90:75-89). */

@@ -80,3 +80,25 @@ def test_integer_pipe_conversions_match_hardware(built_lib):
     bad = C.c_ulonglong(1)
     assert load_library().dns3d_check_conversions(0, 1 << 24, C.byref(bad)) == 0
     assert bad.value == 0
+
+
+def test_projection_residual_fp64_and_mixed(built_lib):
+    """The divergence the projection controls: the relative residual of the
+    Galerkin Poisson system (solve_pressure_3d_standard, 3D:1680-1714) after
+    every 50th of 200 steps on the benchmarked 128x128x65 grid.  FP64 (LU-free
+    stored inverses): round-off; mixed with one FP64-residual refinement of
+    the FP32 solve: <= 1e-10; mixed without it: the FP32 solve's ~1e-7."""
+    wl = WORKLOADS["channel_128x128x65_re180_pi"]
+    res = {}
+    for label, kw in (("fp64", {}), ("mixed", dict(precision=PREC_MIXED)),
+                      ("mixed_unrefined", dict(precision=PREC_MIXED, poisson_refinement=0))):
+        with ChannelDNS(config_from(wl, **kw)) as d:
+            r = []
+            for _ in range(4):
+                d.step(50)
+                r.append(d.projection_residual())
+        res[label] = max(r)
+    print("projection residuals", res)
+    assert res["fp64"] <= 1e-12, res
+    assert res["mixed"] <= 1e-10, res
+    assert res["mixed_unrefined"] > 10 * res["mixed"], res
