@@ -613,7 +613,7 @@ int dns3d_config_defaults(dns3d_config* c) {
     c->linear_solver = 0;
     c->cgstol = 1.0e-6;  // 3D:575
     c->noise_amplitude = 0.0;
-    c->poisson_refinement = 1;
+    c->poisson_refinement = 0;
     c->pad_ = 0;
     return DNS3D_OK;
 }

@@ -100,13 +100,17 @@ typedef struct dns3d_config {
      * two outputs.  Not a reference feature (the large-grid workload's
      * initial condition); 0 = none.  Extension key of &perturbations. */
     double noise_amplitude;
-    /* Mixed precision only: 1 (default) = one step of iterative refinement of
-     * every mixed-precision Poisson solve (the residual of the FP32 solution
-     * formed with the stiffness matrix in double-float arithmetic, the FP32
+    /* Mixed precision only: 1 = one step of iterative refinement of every
+     * mixed-precision Poisson solve (the residual of the FP32 solution formed
+     * with the stiffness matrix in double-float arithmetic, the FP32
      * correction added), which brings the Galerkin residual of the system
-     * solve_pressure_3d_standard solves (3D:1680-1714) from ~1e-7 to ~1e-13
-     * of its right-hand side; 0 = the FP32 solve alone.  Extension key of
-     * &computational. */
+     * solve_pressure_3d_standard solves (3D:1680-1714) from ~3e-6 to ~5e-12
+     * of its right-hand side at 128x128x65; 0 (default) = the FP32 solve in
+     * the eigenbasis alone, whose error is relative to each eigen-component
+     * and so already small where the system is ill-conditioned.  The
+     * refinement costs about 40% of a mixed step and does not reduce the
+     * velocity error against FP64, which the FP32 transforms set.  Extension
+     * key of &computational. */
     int poisson_refinement;
     int pad_;
 } dns3d_config;
