@@ -2,9 +2,12 @@
 // channel runs on one GPU.  No counterpart in the reference (one run per
 // process, DNS_pressure_BC_3D.f90:184-428).
 //
-// A worker thread owns all GPU work.  Requests wait in FIFO order until their
+// A worker thread runs the rounds.  Requests wait in FIFO order until their
 // device footprint (dns3d_footprint_bytes) fits under the byte budget and a
-// slot is free; admitted runs each keep their own handle and are advanced
+// slot is free; a second thread then builds each admitted run's handle
+// (operators, inverses, tuning) while the rounds of the running ones go on,
+// and the worker takes the built runs in at the start of its next round.
+// Running runs each keep their own handle and are advanced
 // `steps_per_round` steps per round.  The runs that take a full round form a
 // batch (dns3d_batch: every stage of a step is one ragged launch over all of
 // them), kept while the set of runs is unchanged; a run in its last, shorter
@@ -66,23 +69,70 @@ struct dns3d_server {
     unsigned long long point_steps = 0;
     Clock::time_point t0;
     std::thread worker;
+    std::thread builder;
+    std::condition_variable cv_build;
+    std::deque<std::shared_ptr<Request>> to_build;   // admitted, handle not yet created
+    std::vector<std::shared_ptr<Request>> built;     // handle created, not yet running
+    int building = 0;                                 // handles being created now
     // worker-thread state: the batch of the runs taking full rounds
     dns3d_batch* batch = nullptr;
     std::vector<dns3d_handle*> batch_runs;
     bool use_batch = true;  // DNS3D_SERVER_BATCH=0: every run steps on its own stream
 
     void loop();
+    void build_loop();
     void drop_batch();
-    void admit_locked(std::vector<std::shared_ptr<Request>>& to_create);
+    void admit_locked();
 };
 
-void dns3d_server::admit_locked(std::vector<std::shared_ptr<Request>>& to_create) {
-    while (!queue.empty() && (int)(active.size() + to_create.size()) < opts.max_runs) {
+// Admission (under mu): the queue's head while its footprint fits the budget
+// and a slot is free; admitted requests go to the builder thread.
+void dns3d_server::admit_locked() {
+    bool any = false;
+    while (!queue.empty() && (int)(active.size() + to_build.size() + built.size()) < opts.max_runs) {
         auto r = queue.front();
         if (bytes_in_use + r->bytes > opts.max_bytes) break;  // FIFO: the head waits for memory
         queue.pop_front();
         bytes_in_use += r->bytes;
-        to_create.push_back(r);
+        to_build.push_back(r);
+        any = true;
+    }
+    if (any) cv_build.notify_one();
+}
+
+// Builder thread: creates the admitted runs' handles one at a time.  A handle
+// built after the server began to stop is destroyed and its request cancelled.
+void dns3d_server::build_loop() {
+    for (;;) {
+        std::shared_ptr<Request> r;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_build.wait(lk, [&] { return stop || !to_build.empty(); });
+            if (stop) return;
+            r = to_build.front();
+            to_build.pop_front();
+            ++building;
+        }
+        dns3d_config c = r->cfg;
+        c.device = opts.device;
+        dns3d_handle* h = nullptr;
+        const int rc = dns3d_create(&c, &h);
+        std::lock_guard<std::mutex> lk(mu);
+        --building;
+        if (rc || stop) {
+            if (h) dns3d_destroy(h);
+            r->status = DNS3D_REQ_FAILED;
+            r->error = rc ? rc : DNS3D_E_CANCELLED;
+            r->t_finish = Clock::now();
+            bytes_in_use -= r->bytes;
+            cv_done.notify_all();
+        } else {
+            r->h = h;
+            r->status = DNS3D_REQ_RUNNING;
+            r->t_start = Clock::now();
+            built.push_back(r);
+        }
+        cv_work.notify_all();
     }
 }
 
@@ -94,50 +144,46 @@ void dns3d_server::drop_batch() {
 
 void dns3d_server::loop() {
     for (;;) {
-        std::vector<std::shared_ptr<Request>> to_create;
         {
             std::unique_lock<std::mutex> lk(mu);
-            cv_work.wait(lk, [&] { return stop || !active.empty() || !queue.empty(); });
-            if (stop && active.empty() && queue.empty()) return;
-            if (stop) {  // cancel everything: queued and running requests end as failed
+            // with nothing running, wait for a request or a built run
+            cv_work.wait(lk, [&] { return stop || !active.empty() || !queue.empty() || !built.empty(); });
+            if (stop) {  // cancel everything: queued, built and running requests end as failed
                 for (auto& r : queue) {
                     r->status = DNS3D_REQ_FAILED;
                     r->error = DNS3D_E_CANCELLED;
                 }
                 queue.clear();
-                drop_batch();
-                for (auto& r : active) {
-                    dns3d_destroy(r->h);
-                    r->h = nullptr;
+                for (auto& r : to_build) {
                     r->status = DNS3D_REQ_FAILED;
                     r->error = DNS3D_E_CANCELLED;
-                    r->t_finish = Clock::now();
                     bytes_in_use -= r->bytes;
                 }
-                active.clear();
+                to_build.clear();
+                drop_batch();
+                for (auto* list : {&active, &built}) {
+                    for (auto& r : *list) {
+                        dns3d_destroy(r->h);
+                        r->h = nullptr;
+                        r->status = DNS3D_REQ_FAILED;
+                        r->error = DNS3D_E_CANCELLED;
+                        r->t_finish = Clock::now();
+                        bytes_in_use -= r->bytes;
+                    }
+                    list->clear();
+                }
                 cv_done.notify_all();
                 return;
             }
-            admit_locked(to_create);
-        }
-        for (auto& r : to_create) {  // handle creation outside the lock
-            dns3d_config c = r->cfg;
-            c.device = opts.device;
-            const int rc = dns3d_create(&c, &r->h);
-            std::lock_guard<std::mutex> lk(mu);
-            if (rc) {
-                r->status = DNS3D_REQ_FAILED;
-                r->error = rc;
-                r->t_finish = Clock::now();
-                bytes_in_use -= r->bytes;
-                cv_done.notify_all();
-            } else {
-                r->status = DNS3D_REQ_RUNNING;
-                r->t_start = Clock::now();
-                active.push_back(r);
+            admit_locked();
+            for (auto& r : built) active.push_back(r);
+            built.clear();
+            if (active.empty()) {
+                // admitted runs are being built: wait for one (or a stop)
+                cv_work.wait(lk, [&] { return stop || !built.empty() || (to_build.empty() && building == 0); });
+                continue;
             }
         }
-        if (active.empty()) continue;
         // one round: queue every run's steps, then wait for all
         std::vector<int> adv(active.size(), 0);
         std::vector<dns3d_handle*> full;
@@ -237,6 +283,7 @@ int dns3d_server_create(const dns3d_server_opts* opts, dns3d_server** out) {
     const char* env = std::getenv("DNS3D_SERVER_BATCH");
     s->use_batch = !(env && std::strcmp(env, "0") == 0);
     s->worker = std::thread([s] { s->loop(); });
+    s->builder = std::thread([s] { s->build_loop(); });
     *out = s;
     return DNS3D_OK;
 }
@@ -325,7 +372,9 @@ int dns3d_server_destroy(dns3d_server* s) {
         std::lock_guard<std::mutex> lk(s->mu);
         s->stop = true;
         s->cv_work.notify_all();
+        s->cv_build.notify_all();
     }
+    if (s->builder.joinable()) s->builder.join();
     if (s->worker.joinable()) s->worker.join();
     delete s;
     return DNS3D_OK;

@@ -499,7 +499,11 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //  (a) the lanes of the last warp start bulk copies of the operator's digit
 //      slices into blocks E (Ge) and O (Go) of each slice (the K padding stays
 //      zero);
-//  (b) meanwhile the folded right-hand sides are formed in FP64 (viscous_rhs_cn),
+//  (b) meanwhile the folded right-hand sides are formed in FP64 (viscous_rhs_cn)
+//      from the q's inputs staged in shared memory: the 2 x 3 columns of u, v, w
+//      and of the sources, copied with cp.async while the previous q ran
+//      (c)-(g), so the strided column reads (one 16-byte value per level, a
+//      plane apart) overlap that q's tensor-core work,
 //  (c) each column gets its power-of-two scale and (d) its digits, one
 //      16-byte core-matrix row (8 levels) per thread and digit;
 //  (e) one thread issues, per digit slice sa of the operator, the K-steps of
@@ -510,6 +514,25 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //  (f) every row's 8 class accumulators are combined in 64-bit integers and
 //      scaled to FP64;
 //  (g) the outputs F* = x - f are written (wall values at the walls).
+// Byte offset of the staged inputs in the viscous tensor-core kernel's shared
+// memory: after the digit slices, right-hand-side digits, results, column
+// exponents, barriers, TMEM address and arrival flag (16-byte aligned).
+__host__ __device__ inline size_t viscous_tc_stage_offset(const TcGeom& t) {
+    const size_t b = (size_t)kTcSlices * (tc_blocks(t, false).a + kTcN * t.kt) * sizeof(__half) +
+                     (size_t)kTcN * t.m8 * sizeof(double) + kTcN * sizeof(int) + 2 * sizeof(uint64_t) + 16;
+    return (b + 15) / 16 * 16;
+}
+
+// Dynamic shared memory one CTA may use (the sm_100-family opt-in maximum).
+constexpr size_t kTcSmemMax = 227 * 1024;
+
+// Whether the staged inputs (12 columns of nz values) still fit beside the
+// operands: true up to nz = 127; at nz = 129 the kernel reads its inputs
+// from global memory in (b) instead.
+__host__ __device__ inline bool viscous_tc_staged(const TcGeom& t, int nz) {
+    return viscous_tc_stage_offset(t) + (size_t)12 * nz * sizeof(double2) <= kTcSmemMax;
+}
+
 __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops, const StepParams& sp,
                                                 const Fields& F, const Fields& Src,
                                                 const double2* __restrict__ GP,
@@ -527,6 +550,8 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcN);            // [0] MMAs done, [1] slices landed
     uint32_t* tbase = reinterpret_cast<uint32_t*>(mbar + 2);
     int* landed = reinterpret_cast<int*>(tbase + 1);                    // the slices of this q arrived
+    // staged inputs of one q: [F, Src][mode 0, 1][u, v, w][nz levels]
+    double2* sP = reinterpret_cast<double2*>(tcsm + viscous_tc_stage_offset(t));
     {
         uint4* z = reinterpret_cast<uint4*>(sA);
         const int n16 = kTcSlices * (bl.a + b_halves) / 8;
@@ -548,9 +573,29 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     const int nbe = t.e8 >> 3, nbo = t.o8 >> 3;
     const int ncore = t.ncore_e + t.ncore_o;
     const int nv = he + ho;  // valid rows / K indices
+    const bool staged = viscous_tc_staged(t, nz);
+    // cp.async of the inputs of operator index q into sP (both modes' columns
+    // of u, v, w and of the sources; a missing second mode is not read)
+    auto stage = [&](int q) {
+        if (!staged) return;
+        const int kya = q / g.nxhp, kx = q - kya * g.nxhp;
+        const int nmode = (kya > 0 && 2 * kya != g.ny) ? 2 : 1;
+        for (int j = threadIdx.x; j < 2 * nmode * 3 * nz; j += blockDim.x) {
+            const int z = j % nz, r = j / nz;
+            const int comp = r % 3, r2 = r / 3;
+            const int mi = r2 % nmode, fld = r2 / nmode;
+            const int m = (mi ? g.ny - kya : kya) * g.nxhp + kx;
+            const double2* src = fld ? fptr(Src, comp) : fptr(F, comp);
+            cp_async16(sP + (size_t)((fld * 2 + mi) * 3 + comp) * nz + z, src + (size_t)z * g.nm + m);
+        }
+        cp_async_commit();
+    };
+    if (q0 < q1) stage(q0);
     bool ok = true;
     for (int q = q0; q < q1 && ok; ++q) {
         const uint32_t par = (uint32_t)((q - q0) & 1);
+        cp_async_wait_all();
+        __syncthreads();  // this q's staged inputs, from every thread's copies
         // (a) digit slices of the operator: per digit, one copy per 8-row
         // group (its nonzero core matrices are contiguous in the compact store
         // and in the K-major block), issued by the lanes of the last warp (the
@@ -595,20 +640,23 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                     bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
                     bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
                 }
-                const double2* fc = fptr(F, comp);
-                const double2* sc = fptr(Src, comp);
-                const double2 f1 = fc[m], fn = fc[(size_t)(nz - 1) * g.nm + m];
-                const size_t o1 = (size_t)k * g.nm + m, o2 = (size_t)(nz - 1 - k) * g.nm + m;
-                const double2 v1 = fc[o1], v2 = k < ho ? fc[o2] : v1;
+                // the F and source columns of this mode: staged, or read from
+                // global memory one level (a plane) apart
+                const size_t st = staged ? 1 : (size_t)g.nm;
+                const double2* fc = staged ? sP + (size_t)(mi * 3 + comp) * nz : fptr(F, comp) + m;
+                const double2* sc = staged ? sP + (size_t)((2 + mi) * 3 + comp) * nz : fptr(Src, comp) + m;
+                const double2 f1 = fc[0], fn = fc[(size_t)(nz - 1) * st];
+                const double2 v1 = fc[(size_t)k * st], v2 = k < ho ? fc[(size_t)(nz - 1 - k) * st] : v1;
                 if (p < 2) {
                     // (p is 0 or 1 here whenever 6 he <= 2 blockDim.x)
                     if (p == 0) { keep1[0] = v1; keep2[0] = v2; }
                     else { keep1[1] = v1; keep2[1] = v2; }
                 }
-                const double2 b1 = viscous_rhs_cn(g, ops, sp, comp, k, m, ky, kx, v1, sc[o1], f1, fn, bc1, bc2, dpdx);
+                const double2 b1 =
+                    viscous_rhs_cn(g, ops, sp, comp, k, m, ky, kx, v1, sc[(size_t)k * st], f1, fn, bc1, bc2, dpdx);
                 if (k < ho) {
-                    const double2 b2 =
-                        viscous_rhs_cn(g, ops, sp, comp, nz - 1 - k, m, ky, kx, v2, sc[o2], f1, fn, bc1, bc2, dpdx);
+                    const double2 b2 = viscous_rhs_cn(g, ops, sp, comp, nz - 1 - k, m, ky, kx, v2,
+                                                      sc[(size_t)(nz - 1 - k) * st], f1, fn, bc1, bc2, dpdx);
                     fe = make_double2(b1.x + b2.x, b1.y + b2.y);
                     fo = make_double2(b1.x - b2.x, b1.y - b2.y);
                 } else {
@@ -624,6 +672,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             }
         }
         __syncthreads();
+        if (q + 1 < q1) stage(q + 1);  // sP is free again: the next q's inputs arrive during (c)-(g)
         // (c) column scales, one warp per column
         {
             const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -763,6 +812,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
         }
         __syncthreads();  // shared buffers are reused by the next q
     }
+    cp_async_wait_all();  // a stage issued before a timeout lands before the CTA leaves
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -795,6 +845,19 @@ constexpr int kTcVortModes = kTcVortCols / 4;  // modes per tile: u, v x re, im
 constexpr int kTcCorrModes = kTcVortCols / 2;  // modes per tile: phi x re, im
 constexpr int kTcVortThreads = 512;
 
+// Byte offset of the staged input columns in the z-derivative kernels' shared
+// memory (after the D1 image, digits, results, exponents, barriers), and
+// whether they fit (kTcVortCols / 2 columns of nz values).
+__host__ __device__ inline size_t dz_tc_stage_offset(const TcGeom& t) {
+    const size_t b = (size_t)kTcSlices * (tc_blocks(t, true).a + kTcVortCols * t.kt) * sizeof(__half) +
+                     (size_t)kTcVortCols * t.m8 * sizeof(double) + (size_t)(t.m8 + kTcVortCols) * sizeof(int) +
+                     2 * sizeof(uint64_t) + 16;
+    return (b + 15) / 16 * 16;
+}
+__host__ __device__ inline bool dz_tc_staged(const TcGeom& t, int nz) {
+    return dz_tc_stage_offset(t) + (size_t)(kTcVortCols / 2) * nz * sizeof(double2) <= kTcSmemMax;
+}
+
 template <class Op>
 __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, const Op& op, int tile0, int tile1,
                                            int* err) {
@@ -812,6 +875,9 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcVortCols);     // [0] MMAs done, [1] D1 landed
     uint32_t* tbase = reinterpret_cast<uint32_t*>(mbar + 2);
     int* landed = reinterpret_cast<int*>(tbase + 1);
+    // staged input columns of one tile: [mode][field][nz]
+    double2* sP = reinterpret_cast<double2*>(tcsm + dz_tc_stage_offset(t));
+    const bool staged = dz_tc_staged(t, nz);
     const int tid = threadIdx.x;
     {
         uint4* z = reinterpret_cast<uint4*>(sB);
@@ -835,20 +901,41 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             tc_bulk_g2s(sA + s * bl.a, ops.tcD + (size_t)s * bl.a, (uint32_t)(bl.a * sizeof(__half)), &mbar[1]);
     }
     const int nv = he + ho;
+    // cp.async of a tile's input columns into sP, while the tile before it
+    // runs its digits, products and outputs
+    auto stage = [&](int tile) {
+        if (!staged) return;
+        const int m0 = tile * kModes;
+        for (int j = tid; j < kModes * Op::kFields * nz; j += blockDim.x) {
+            const int z = j % nz, r = j / nz;
+            const int f = r % Op::kFields, mi = r / Op::kFields;
+            if (m0 + mi < g.nm) cp_async16(sP + (size_t)r * nz + z, op.field(f) + (size_t)z * g.nm + m0 + mi);
+        }
+        cp_async_commit();
+    };
+    if (tile0 < tile1) stage(tile0);
     for (int tile = tile0; tile < tile1; ++tile) {
         const uint32_t par = (uint32_t)((tile - tile0) & 1);
         const int m0 = tile * kModes;
+        cp_async_wait_all();
+        __syncthreads();  // this tile's staged columns, from every thread's copies
         // (b) folded fields: column 2 (kFields mi + f) + (0 re, 1 im)
         for (int i = tid; i < Op::kFields * kModes * he; i += blockDim.x) {
             const int mi = i / (Op::kFields * he);
             const int r = i - mi * Op::kFields * he;
             const int f = r / he, k = r - f * he;
             const int m = m0 + mi;
-            const double2* src = op.field(f);
             double2 a = make_double2(0.0, 0.0), b = a;
             if (m < g.nm) {
-                a = src[(size_t)k * g.nm + m];
-                if (k < ho) b = src[(size_t)(nz - 1 - k) * g.nm + m];
+                if (staged) {
+                    const double2* col = sP + (size_t)(mi * Op::kFields + f) * nz;
+                    a = col[k];
+                    if (k < ho) b = col[nz - 1 - k];
+                } else {
+                    const double2* src = op.field(f);
+                    a = src[(size_t)k * g.nm + m];
+                    if (k < ho) b = src[(size_t)(nz - 1 - k) * g.nm + m];
+                }
             }
             const int c0 = 2 * (Op::kFields * mi + f);
             if (k < ho) {
@@ -862,6 +949,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             }
         }
         __syncthreads();
+        if (tile + 1 < tile1) stage(tile + 1);  // sP is free again
         // (c) column scales
         {
             const int w = tid >> 5, l = tid & 31;
@@ -989,6 +1077,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         }
         __syncthreads();  // sR and sB are reused by the next tile
     }
+    cp_async_wait_all();  // a stage issued before a timeout lands before the CTA leaves
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -2710,19 +2799,20 @@ cudaError_t launch_poisson_residual(const GridDev& g, const Ops& ops, const Step
 
 size_t viscous_tc_smem(const GridDev& g) {
     const TcGeom t = tc_geom(g.nz);
-    return (size_t)kTcSlices * (tc_blocks(t, false).a + kTcN * t.kt) * sizeof(__half) +
-           (size_t)kTcN * t.m8 * sizeof(double) + kTcN * sizeof(int) + 2 * sizeof(uint64_t) +
-           16;  // + TMEM address, arrival flag
+    // + the staged inputs of one q where they fit
+    return viscous_tc_stage_offset(t) + (viscous_tc_staged(t, g.nz) ? (size_t)12 * g.nz * sizeof(double2) : 0);
 }
 
 bool viscous_tc_fits(const GridDev& g) {
     return tc_supported(g.nz) && viscous_tc_smem(g) <= smem_limit(k_viscous_tc);
 }
 
-// Operator indices q per CTA: one per four waves of single-q CTAs (two CTAs
-// on each of 152 SMs), at most 4.  Which CTA takes a q does not change its
-// arithmetic.
-int tc_q_per_cta(int nq) { return std::max(1, std::min(4, nq / (4 * 2 * 152))); }
+// Operator indices q per CTA: consecutive runs of q spread over one wave of
+// CTAs (two on each of 152 SMs), so every CTA stages its next q's inputs while
+// it works on the current one and no partial wave is left at the end; a CTA's
+// consecutive q (neighbouring kx) share cache sectors.  Which CTA takes a q
+// does not change its arithmetic.
+int tc_q_per_cta(int nq) { return std::max(1, (nq + 2 * 152 - 1) / (2 * 152)); }
 
 cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams& sp, Fields F, Fields Src,
                               const double2* GP, const dns3d_pi_state* pi, Fields Out, int* err, cudaStream_t s) {
@@ -2735,9 +2825,7 @@ cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams
 
 size_t vorticity_tc_smem(const GridDev& g) {
     const TcGeom t = tc_geom(g.nz);
-    return (size_t)kTcSlices * (tc_blocks(t, true).a + kTcVortCols * t.kt) * sizeof(__half) +
-           (size_t)kTcVortCols * t.m8 * sizeof(double) + (size_t)(t.m8 + kTcVortCols) * sizeof(int) +
-           2 * sizeof(uint64_t) + 16;
+    return dz_tc_stage_offset(t) + (dz_tc_staged(t, g.nz) ? (size_t)(kTcVortCols / 2) * g.nz * sizeof(double2) : 0);
 }
 
 bool vorticity_tc_fits(const GridDev& g) {

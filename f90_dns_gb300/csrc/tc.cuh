@@ -199,6 +199,14 @@ __device__ __forceinline__ void tc_bulk_g2s(void* dst, const void* src, uint32_t
         : "memory");
 }
 
+// Asynchronous 16-byte global -> shared copy (L2 only), its commit and the
+// wait for all of this thread's outstanding groups.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc_smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 __device__ __forceinline__ void tc_commit(uint64_t* mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
         tc_smem_u32(mbar)));
