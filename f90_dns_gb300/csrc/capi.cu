@@ -702,7 +702,7 @@ int tile_launch(dns3d_handle* h, int k) {
 int autotune(dns3d_handle* h, bool force) {
     CK(h, cudaSetDevice(h->cfg.device));
     // precision, and for FP64 whether the tensor-core solve exists / is forced
-    const int variant = h->mixed ? 1 : (h->ops.tcA || h->ops.tcD ? (h->visc_tc_forced ? 4 : 2) : 0);
+    const int variant = h->mixed ? 1 + 8 * h->g.refine : (h->ops.tcA || h->ops.tcD ? (h->visc_tc_forced ? 4 : 2) : 0);
     const TuneKey key{h->cfg.nx, h->cfg.ny, h->cfg.nz, variant, h->cfg.device};
     if (!force) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -905,6 +905,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
     g.nxh = c.nx / 2; g.nxhp = c.nx / 2 + 1; g.nm = g.nxhp * c.ny;
     g.nkyu = c.ny / 2 + 1;
     g.inv_nxny = 1.0 / ((double)c.nx * (double)c.ny);
+    g.refine = (c.precision == DNS3D_PREC_MIXED && c.poisson_refinement) ? 1 : 0;
     const int nz = c.nz;
 
     // setup_grid_3d (3D:740-742) and setup_spectral_3d (3D:769-809)

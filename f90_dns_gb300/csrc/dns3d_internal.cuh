@@ -62,6 +62,7 @@ struct GridDev {
     int nkyu;            // ny/2 + 1 unique |ky|
     double inv_nxny;     // 1/(nx*ny), c2r normalisation
     int tc[kTileKernels];  // chosen tile widths (0: built-in heuristic)
+    int refine;            // mixed pressure: keeps its FP64 right-hand side for the refinement step
 };
 
 // Maps a spectral mode (ky, kx) to the index of its per-mode operator: the

@@ -58,17 +58,24 @@ template <typename P> __device__ __forceinline__ P* fptr(const FieldsT<P>& f, in
 // update_pressure_gradient_3d (3D:2488-2549) called with the namelist istart
 // (3D:1118), and calculate_bulk_velocity_3d (3D:2434-2464) from the (0,0) mode:
 // sum_ij u(i,j,k) = Re U[k][0][0].
+// The CTA's threads load the nz values of the mean mode in parallel (one
+// 16-byte load per level, a plane apart); thread 0 then sums them in level
+// order and runs the controller.  Every thread of the CTA must call it.
 __device__ __forceinline__ void pi_update_body(GridDev g, const double* __restrict__ zw, PIParams pp,
                                                const double2* __restrict__ U, dns3d_pi_state* pi, int bx) {
-    if (threadIdx.x != 0 || bx != 0) return;
+    if (bx != 0) return;
     if (pp.method == 1) {
-        pi->current_pressure_gradient = pp.target_dpdx;
+        if (threadIdx.x == 0) pi->current_pressure_gradient = pp.target_dpdx;
         return;
     }
     if (pp.method != 2) return;
     if (pp.istart % pp.update_freq != 0) return;
+    __shared__ double col[129];  // Re U at mode (0,0), every level (nz <= 129)
+    for (int k = threadIdx.x; k < g.nz; k += blockDim.x) col[k] = U[(size_t)k * g.nm].x;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     double vol = 0.0;
-    for (int k = 0; k < g.nz; ++k) vol += U[(size_t)k * g.nm].x * zw[k];
+    for (int k = 0; k < g.nz; ++k) vol = fma(col[k], zw[k], vol);
     const double ub = vol * pp.inv_nxny_wsum;
     pi->current_bulk_velocity = ub;
     const double err = pp.target_ub - ub;
@@ -2633,7 +2640,7 @@ int tile_cols_mixed(const GridDev& g) {
 size_t pressure_mixed_smem(const GridDev& g, int tc) {
     const int ho = g.nz / 2, he = g.nz - ho;
     return (size_t)g.nz * tc * sizeof(float4) + 2 * (size_t)(pad4(he) + pad4(ho)) * tc * sizeof(float2) +
-           (size_t)g.nz * tc * sizeof(double2);  // the FP64 right-hand side kept for the refinement
+           (g.refine ? (size_t)g.nz * tc * sizeof(double2) : 0);  // the FP64 right-hand side kept for the refinement
 }
 
 namespace {
@@ -2756,7 +2763,7 @@ cudaError_t check_conversions(long long n, unsigned long long* mismatches) {
 
 cudaError_t launch_pi_update(const GridDev& g, const Ops& ops, const PIParams& pp, const double2* U,
                              dns3d_pi_state* pi, cudaStream_t s) {
-    k_pi_update<<<1, 32, 0, s>>>(g, ops.zw, pp, U, pi);
+    k_pi_update<<<1, 128, 0, s>>>(g, ops.zw, pp, U, pi);
     return cudaGetLastError();
 }
 
