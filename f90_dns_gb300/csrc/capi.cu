@@ -2007,7 +2007,9 @@ constexpr long long kRaggedMaxPoints = 1LL << 20;
 
 bool ragged_eligible(const dns3d_handle* h) {
     const long long points = (long long)h->cfg.nx * h->cfg.ny * h->cfg.nz;
-    return h->fft.use_ct && h->cfg.convection_scheme == 0 && h->cfg.linear_solver == 0 &&
+    // (a mixed run with the Poisson refinement keeps its own launches: its
+    // pressure body is a separate kernel instantiation)
+    return h->fft.use_ct && h->cfg.convection_scheme == 0 && h->cfg.linear_solver == 0 && !h->sp.refine &&
            points < kRaggedMaxPoints;
 }
 

@@ -2219,9 +2219,10 @@ __device__ __forceinline__ void pressure_mixed_forward(const GridDev& g, const M
 // phi = pe + po, dphi/dz = dze + dzo at levels (i, nz-1-i) from tp, 4 rows i
 // per thread: pe = PBe phi~e, po = PBo phi~o, dze = PDe phi~o, dzo = PDo
 // phi~e; stored into PHI, PHIZ, or added to them (a correction).
+template <bool kAdd>
 __device__ __forceinline__ void pressure_mixed_back(const GridDev& g, const MixedOps& mx, const Ops& ops,
                                                     const float2* tp, double2* __restrict__ PHI,
-                                                    double2* __restrict__ PHIZ, int m0, int tc, bool add) {
+                                                    double2* __restrict__ PHIZ, int m0, int tc) {
     const int nz = g.nz, he = ops.he, ho = ops.ho;
     const int pe4 = mx.phe4, po4 = mx.pho4, nbe = pe4 / 4, nbo = po4 / 4;
     for (int t = threadIdx.x; t < nbe * tc; t += blockDim.x) {
@@ -2276,7 +2277,7 @@ __device__ __forceinline__ void pressure_mixed_back(const GridDev& g, const Mixe
         }
         auto put = [&](size_t o, double2* F, float x, float y) {
             const double2 v = make_double2(f2d(x), f2d(y));
-            if (add) {
+            if (kAdd) {
                 const double2 o0 = F[o];
                 F[o] = make_double2(o0.x + v.x, o0.y + v.y);
             } else {
@@ -2318,6 +2319,7 @@ __device__ __forceinline__ void pressure_mixed_back(const GridDev& g, const Mixe
 // stored phi with S applied in double-float (about 2^-48 relative, against
 // the 2^-24 of the FP32 solve), and the FP32 solve of P d = r is added to
 // phi and dphi/dz: the Galerkin residual drops from ~1e-7 to ~1e-13 of b.
+template <bool kRefine>
 __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops ops, StepParams sp,
                                                     const double2* __restrict__ US,
                                                     const double2* __restrict__ VS,
@@ -2358,7 +2360,7 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
         }
         tb[k * tc + c] = fs;
         if (k < ho) tb[(pe4 + k) * tc + c] = fd;
-        if (sp.refine) {
+        if (kRefine) {
             bt[k * tc + c] = b1;
             if (k < ho) bt[(nz - 1 - k) * tc + c] = b2;
         }
@@ -2366,8 +2368,8 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
     __syncthreads();
     pressure_mixed_forward(g, mx, ops, tb, tp, m0, tc);
     __syncthreads();
-    pressure_mixed_back(g, mx, ops, tp, PHI, PHIZ, m0, tc, false);
-    if (!sp.refine) return;
+    pressure_mixed_back<false>(g, mx, ops, tp, PHI, PHIZ, m0, tc);
+    if (!kRefine) return;
     // refinement: r = b + S phi + k^2 wh phi (phi as stored, FP64)
     __syncthreads();  // this CTA's PHI writes, then the folded phi in double-float
     fold_load_df(tw, PHI, g, m0, tc, he, ho, true);
@@ -2399,16 +2401,17 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
     __syncthreads();
     pressure_mixed_forward(g, mx, ops, tb, tp, m0, tc);
     __syncthreads();
-    pressure_mixed_back(g, mx, ops, tp, PHI, PHIZ, m0, tc, true);
+    pressure_mixed_back<true>(g, mx, ops, tp, PHI, PHIZ, m0, tc);
 }
 
+template <bool kRefine>
 __global__ void __launch_bounds__(256) k_pressure_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
                                                         const double2* __restrict__ US,
                                                         const double2* __restrict__ VS,
                                                         const double2* __restrict__ WS,
                                                         double2* __restrict__ PHI, double2* __restrict__ PHIZ,
                                                         int tc) {
-    pressure_mixed_body(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc, blockIdx.x);
+    pressure_mixed_body<kRefine>(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc, blockIdx.x);
 }
 
 // dphi/dz of mode (0,0) in FP64 (one CTA), after k_pressure has written phi.
@@ -2695,7 +2698,7 @@ bool tile_fits(const GridDev& g, int k, int tc) {
         case kTileDiv: lim = smem_limit(k_divergence); break;
         case kTileVortM: lim = smem_limit(k_vorticity_mixed); break;
         case kTileViscM: lim = smem_limit(k_viscous_mixed); break;
-        case kTilePresM: lim = smem_limit(k_pressure_mixed); break;
+        case kTilePresM: lim = std::min(smem_limit(k_pressure_mixed<false>), smem_limit(k_pressure_mixed<true>)); break;
         default: return false;
     }
     return tile_smem(g, k, tc) <= lim;
@@ -2705,7 +2708,8 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
     cudaError_t e;
     if ((e = set_smem(k_pressure, (2 * (size_t)g.nz + g.nz) * sizeof(double2)))) return e;
     if ((e = set_smem(k_correction, (size_t)g.nz * sizeof(double2)))) return e;
-    if ((e = set_smem(k_pressure_mixed, pressure_mixed_smem(g, tile_cols(g, 2))))) return e;
+    if ((e = set_smem(k_pressure_mixed<false>, pressure_mixed_smem(g, tile_cols(g, 2))))) return e;
+    if ((e = set_smem(k_pressure_mixed<true>, pressure_mixed_smem(g, tile_cols(g, 2))))) return e;
     if ((e = set_smem(k_viscous<float2>, 6 * (size_t)g.nz * sizeof(double2)))) return e;
     if ((e = set_smem(k_vorticity_mixed, 2 * (size_t)g.nz * tile_cols(g, 1) * sizeof(float2)))) return e;
     if ((e = set_smem(k_viscous_mixed, viscous_mixed_smem(g, tile_cols_mixed(g))))) return e;
@@ -2906,7 +2910,10 @@ cudaError_t launch_pressure_mixed(const GridDev& g, const MixedOps& mx, const Op
                                   double2* PHIZ, cudaStream_t s) {
     const int tc = tile_width(g, kTilePresM);
     const size_t sm = pressure_mixed_smem(g, tc);
-    k_pressure_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc);
+    if (sp.refine)
+        k_pressure_mixed<true><<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc);
+    else
+        k_pressure_mixed<false><<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, US, VS, WS, PHI, PHIZ, tc);
     return cudaGetLastError();
 }
 
@@ -3178,7 +3185,8 @@ struct RsPresRhs64 {
 struct RsPres32 {
     static constexpr int kMinCtas = 3;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
-        pressure_mixed_body(d.g, d.mx, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.PHIZ, d.g.tc[kTilePresM], b);
+        // runs with the Poisson refinement are not ragged-eligible (capi.cu)
+        pressure_mixed_body<false>(d.g, d.mx, d.ops, d.sp, d.US, d.VS, d.WS, d.PHI, d.PHIZ, d.g.tc[kTilePresM], b);
     }
 };
 
