@@ -524,8 +524,42 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 // Byte offset of the staged inputs in the viscous tensor-core kernel's shared
 // memory: after the digit slices, right-hand-side digits, results, column
 // exponents, barriers, TMEM address and arrival flag (16-byte aligned).
+// Combination of one warp's TMEM lanes for NC right-hand-side columns from
+// column col0 (NC = 12 from 0, 8 from 0 or 4 from 8): the 8 weight-class
+// accumulators summed in 64-bit integers (tc_class_term), scaled to FP64 and
+// stored to sR at the lane's row.
+template <int NC>
+__device__ __noinline__ void tc_combine_rows(uint32_t lanes, int col0, double* sR, int m8, int row, bool valid,
+                                                int e, const int* sF) {
+    long long T[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) T[j] = 0;
+    for (int c = 0; c < kTcClasses; ++c) {
+        float v[NC > 8 ? 16 : 8];
+        if (NC > 8) tc_ld16(lanes + (uint32_t)(c * kTcN + col0), v);
+        else tc_ld8(lanes + (uint32_t)(c * kTcN + col0), v);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) T[j] += tc_class_term(c, v[j]);
+    }
+    if (valid) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) sR[(col0 + j) * m8 + row] = i2d_scaled(T[j], e + sF[col0 + j] - 52);
+    }
+}
+
+// Bytes of unused shared memory in front of the digit slices: block O's MMA
+// starts 64 rows before its operand (so that its results land in TMEM lanes
+// 64 .. 64 + o8, see viscous_tc_body), and those 64 rows of the first slice
+// must still lie inside the CTA's shared memory.  Rows it reads there only
+// produce accumulator lanes that are never read.
+__host__ __device__ inline size_t viscous_tc_pad(const TcGeom& t) {
+    const TcBlocks bl = tc_blocks(t, false);
+    const long long need = 8LL * bl.kO * 16 - (long long)bl.aE * 2;
+    return need > 0 ? (size_t)((need + 127) / 128 * 128) : 0;
+}
+
 __host__ __device__ inline size_t viscous_tc_stage_offset(const TcGeom& t) {
-    const size_t b = (size_t)kTcSlices * (tc_blocks(t, false).a + kTcN * t.kt) * sizeof(__half) +
+    const size_t b = viscous_tc_pad(t) + (size_t)kTcSlices * (tc_blocks(t, false).a + kTcN * t.kt) * sizeof(__half) +
                      (size_t)kTcN * t.m8 * sizeof(double) + kTcN * sizeof(int) + 2 * sizeof(uint64_t) + 16;
     return (b + 15) / 16 * 16;
 }
@@ -550,7 +584,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     const TcBlocks bl = tc_blocks(t, false);
     const int nz = g.nz, he = t.he, ho = t.ho, m8 = t.m8;
     const int b_halves = kTcN * t.kt;
-    __half* sA = reinterpret_cast<__half*>(tcsm);
+    __half* sA = reinterpret_cast<__half*>(tcsm + viscous_tc_pad(t));
     __half* sB = sA + kTcSlices * bl.a;
     double* sR = reinterpret_cast<double*>(sB + kTcSlices * b_halves);  // [kTcN][m8]: rhs, then results
     int* sF = reinterpret_cast<int*>(sR + kTcN * m8);                   // column exponents
@@ -709,8 +743,9 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             const int kl = i & 7, cc = i >> 3;
             const int c = cc % 12, kk = (cc / 12) * 8 + kl;
             const int row = kk < t.ke ? (kk < he ? kk : -1) : (kk - t.ke < ho ? t.e8 + (kk - t.ke) : -1);
+            if (row < 0) continue;  // padding K rows: zeroed once at the start, never written
             int d[kTcSlices];
-            tc_digits(row >= 0 ? tc_fixed(sR[c * m8 + row], sF[c]) : 0, d);
+            tc_digits(tc_fixed(sR[c * m8 + row], sF[c]), d);
             __half* dst = sB + tc_core_off(c, kk, t.kt);
 #pragma unroll
             for (int s = 0; s < kTcSlices; ++s) dst[s * b_halves] = __int2half_rn(d[s]);
@@ -727,7 +762,13 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                 // units in the low field; a K offset of k elements is k/8
                 // core matrices of 128 B, i.e. k units): one add per MMA
                 const uint64_t dAE = tc_desc(tc_smem_u32(sA), 128, (uint32_t)bl.kE * 16);
-                const uint64_t dAO = tc_desc(tc_smem_u32(sA + bl.aE), 128, (uint32_t)bl.kO * 16);
+                // block O starts 64 rows (8 row groups) before its operand, so
+                // its o8 <= 64 result rows land in TMEM lanes 64 .. 64 + o8
+                // (lane quadrants 2 and 3) while block E's use quadrants 0 and 1
+                // (2 as well at nz = 129): the combination then spreads over
+                // more warps, each reading only its own quadrant
+                const uint64_t dAO =
+                    tc_desc(tc_smem_u32(sA + bl.aE) - (uint32_t)(8 * bl.kO * 16), 128, (uint32_t)bl.kO * 16);
                 const uint64_t dB = tc_desc(tc_smem_u32(sB), 128, (uint32_t)t.kt * 16);
                 const int nkE = bl.kE / 16, nkO = bl.kO / 16;
                 for (int sa = 0; sa < kTcSlices; ++sa) {
@@ -760,27 +801,31 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             break;  // uniform: no TMEM read, no further MMA
         }
         {
-            // warp w reads TMEM lane quadrant w % 4 (rows 32 (w % 4) .. +31):
-            // warps 0-3 of block E, warps 4-7 of block O, all 12 columns
-            const int w = threadIdx.x >> 5, quad = w & 3, blk = (w >> 2) & 1;
-            const int rows = blk ? t.o8 : t.e8;
-            if (w < 8 && 32 * quad < rows) {
-                long long T[12];
-#pragma unroll
-                for (int j = 0; j < 12; ++j) T[j] = 0;
-                const uint32_t base = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(blk * kTcDCols);
-                for (int c = 0; c < kTcClasses; ++c) {
-                    float v[16];
-                    tc_ld16(base + (uint32_t)(c * kTcN), v);
-#pragma unroll
-                    for (int j = 0; j < 12; ++j) T[j] += tc_class_term(c, v[j]);
-                }
-                const int r = 32 * quad + (threadIdx.x & 31);
-                if (r < rows) {
-                    const int row = blk ? t.e8 + r : r;
-                    const int e = __ldg(&ops.tcE[(size_t)q * m8 + row]);
-#pragma unroll
-                    for (int j = 0; j < 12; ++j) sR[j * m8 + row] = i2d_scaled(T[j], e + sF[j] - 52);
+            // warp w reads TMEM lane quadrant w % 4 (lanes 32 (w % 4) .. +31);
+            // block E's rows are lanes 0 .. e8, block O's lanes 64 .. 64 + o8.
+            // A quadrant holding rows of one block splits its 12 columns
+            // between its two warps (8 and 4); one holding rows of both blocks
+            // (nz = 129: lanes 64 .. 71 of E) gives each warp one block.
+            const int w = threadIdx.x >> 5;
+            if (w < 8) {
+                const int quad = w & 3, half = w >> 2;
+                const bool hasE = 32 * quad < t.e8;
+                const bool hasO = quad >= 2 && 32 * quad < 64 + t.o8;
+                const int lane = 32 * quad + (threadIdx.x & 31);
+                const uint32_t lanes = tmem + ((uint32_t)(32 * quad) << 16);
+                if (hasE && hasO) {
+                    const int blk = half;
+                    const bool valid = blk ? (lane >= 64 && lane - 64 < t.o8) : lane < t.e8;
+                    const int row = blk ? t.e8 + (lane - 64) : lane;
+                    const int e = valid ? __ldg(&ops.tcE[(size_t)q * m8 + row]) : 0;
+                    tc_combine_rows<12>(lanes + (uint32_t)(blk * kTcDCols), 0, sR, m8, row, valid, e, sF);
+                } else if (hasE || hasO) {
+                    const int blk = hasO ? 1 : 0;
+                    const bool valid = blk ? (lane >= 64 && lane - 64 < t.o8) : lane < t.e8;
+                    const int row = blk ? t.e8 + (lane - 64) : lane;
+                    const int e = valid ? __ldg(&ops.tcE[(size_t)q * m8 + row]) : 0;
+                    if (half == 0) tc_combine_rows<8>(lanes + (uint32_t)(blk * kTcDCols), 0, sR, m8, row, valid, e, sF);
+                    else tc_combine_rows<4>(lanes + (uint32_t)(blk * kTcDCols), 8, sR, m8, row, valid, e, sF);
                 }
             }
         }
@@ -983,8 +1028,9 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             const int kl = i & 7, cc = i >> 3;
             const int c = cc % kTcVortCols, kk = (cc / kTcVortCols) * 8 + kl;
             const int row = kk < t.ke ? (kk < he ? kk : -1) : (kk - t.ke < ho ? t.e8 + (kk - t.ke) : -1);
+            if (row < 0) continue;  // padding K rows: zeroed once at the start, never written
             int d[kTcSlices];
-            tc_digits(row >= 0 ? tc_fixed(sR[c * m8 + row], sF[c]) : 0, d);
+            tc_digits(tc_fixed(sR[c * m8 + row], sF[c]), d);
             __half* dst = sB + tc_core_off(c, kk, t.kt);
 #pragma unroll
             for (int s = 0; s < kTcSlices; ++s) dst[s * b_halves] = __int2half_rn(d[s]);
