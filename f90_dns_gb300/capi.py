@@ -42,13 +42,13 @@ EXPORTED_SYMBOLS = (
     "dns3d_initialize_fields", "dns3d_set_state", "dns3d_get_state", "dns3d_set_clock",
     "dns3d_compute_source_terms", "dns3d_viscous_step", "dns3d_solve_pressure",
     "dns3d_pressure_correction", "dns3d_apply_boundary_conditions", "dns3d_step",
-    "dns3d_synchronize", "dns3d_diagnostics", "dns3d_output_diagnostics", "dns3d_check_divergence",
+    "dns3d_synchronize", "dns3d_query", "dns3d_diagnostics", "dns3d_output_diagnostics", "dns3d_check_divergence",
     "dns3d_projection_residual", "dns3d_footprint_bytes", "dns3d_strerror",
     "dns3d_last_error", "dns3d_step_timed", "dns3d_profile_kernels", "dns3d_launches_per_step",
     "dns3d_measure_fp64_tflops", "dns3d_check_conversions", "dns3d_flow_stats_noalloc",
     "dns3d_ensemble_create", "dns3d_ensemble_destroy", "dns3d_ensemble_size", "dns3d_ensemble_run",
     "dns3d_ensemble_step", "dns3d_ensemble_step_timed", "dns3d_ensemble_info",
-    "dns3d_batch_create", "dns3d_batch_step", "dns3d_batch_synchronize", "dns3d_batch_info",
+    "dns3d_batch_create", "dns3d_batch_step", "dns3d_batch_synchronize", "dns3d_batch_query", "dns3d_batch_info",
     "dns3d_batch_destroy",
     "dns3d_server_opts_defaults", "dns3d_server_create", "dns3d_server_submit", "dns3d_server_poll",
     "dns3d_server_wait", "dns3d_server_result_state", "dns3d_server_release", "dns3d_server_get_stats",
@@ -214,6 +214,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.dns3d_batch_create.argtypes = [C.POINTER(hp), ip, ip, C.POINTER(hp)]
     lib.dns3d_batch_step.argtypes = [hp, ip]
     lib.dns3d_batch_synchronize.argtypes = [hp]
+    lib.dns3d_batch_query.argtypes = [hp, C.POINTER(C.c_int)]
+    lib.dns3d_query.argtypes = [hp, C.POINTER(C.c_int)]
     lib.dns3d_batch_info.argtypes = [hp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.dns3d_batch_destroy.argtypes = [hp]
     lib.dns3d_server_opts_defaults.argtypes = [C.POINTER(CServerOpts)]

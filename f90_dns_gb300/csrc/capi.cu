@@ -1750,6 +1750,21 @@ int dns3d_synchronize(dns3d_handle* h) {
     return DNS3D_OK;
 }
 
+int dns3d_query(dns3d_handle* h, int* done) {
+    if (!h || !done) return DNS3D_E_INVALID;
+    CK(h, cudaSetDevice(h->cfg.device));
+    const cudaError_t e = cudaStreamQuery(h->stream);
+    if (e == cudaErrorNotReady) {
+        // not an error; make sure a later launch check cannot read it as one
+        if (cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();
+        *done = 0;
+        return DNS3D_OK;
+    }
+    CK(h, e);
+    *done = 1;
+    return DNS3D_OK;
+}
+
 }  // extern "C"
 
 namespace {
@@ -2425,6 +2440,21 @@ int dns3d_batch_synchronize(dns3d_batch* b) {
     if (!b) return DNS3D_E_INVALID;
     BK(b, cudaSetDevice(b->device));
     BK(b, cudaStreamSynchronize(b->stream));
+    return DNS3D_OK;
+}
+
+int dns3d_batch_query(dns3d_batch* b, int* done) {
+    if (!b || !done) return DNS3D_E_INVALID;
+    BK(b, cudaSetDevice(b->device));
+    const cudaError_t e = cudaStreamQuery(b->stream);
+    if (e == cudaErrorNotReady) {
+        // not an error; make sure a later launch check cannot read it as one
+        if (cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();
+        *done = 0;
+        return DNS3D_OK;
+    }
+    BK(b, e);
+    *done = 1;
     return DNS3D_OK;
 }
 

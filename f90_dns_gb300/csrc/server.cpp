@@ -2,16 +2,18 @@
 // channel runs on one GPU.  No counterpart in the reference (one run per
 // process, DNS_pressure_BC_3D.f90:184-428).
 //
-// A worker thread runs the rounds.  Requests wait in FIFO order until their
+// A worker thread advances the runs.  Requests wait in FIFO order until their
 // device footprint (dns3d_footprint_bytes) fits under the byte budget and a
 // slot is free; a second thread then builds each admitted run's handle
-// (operators, inverses, tuning) while the rounds of the running ones go on,
-// and the worker takes the built runs in at the start of its next round.
-// Running runs each keep their own handle and are advanced
-// `steps_per_round` steps per round.  The runs that take a full round form a
-// batch (dns3d_batch: every stage of a step is one ragged launch over all of
-// them), kept while the set of runs is unchanged; a run in its last, shorter
-// round steps on its own stream beside the batch.  A finished run's
+// (operators, inverses, tuning) while the running ones go on, and the worker
+// takes the built runs in as they come.  Work is queued in chunks of
+// `steps_per_round` steps, and every unit gets its next chunk as soon as its
+// previous one has completed (dns3d_query / dns3d_batch_query), so runs of
+// different sizes do not wait for one another: the small runs with at least
+// a full chunk left form a batch (dns3d_batch: every stage of a step is one
+// ragged launch over all of them), re-formed only while it is idle and its
+// membership has changed; large runs and a run's last, shorter chunk step on
+// their own streams beside it.  A finished run's
 // diagnostics (and, on request, its final u, v, w, p_total) are kept, and the
 // batch and its handle are destroyed at once so its memory admits the next
 // request.
@@ -48,7 +50,16 @@ struct Request {
     dns3d_handle* h = nullptr;
     dns3d_diag diag{};
     std::vector<double> state;  // u, v, w, p_total when keep_state
+    int pending = 0;            // steps queued on the run's own stream, not yet counted
+    bool in_batch = false;      // a member of the current batch (stepped only through it)
 };
+
+// Runs at or above this many grid points keep their own launches in a batch
+// (the library's ragged stages take smaller runs only, dns3d_capi.h); the
+// server steps them on their own streams, never inside a batch.
+constexpr long long kLargeRunPoints = 1LL << 20;
+
+bool large_run(const dns3d_config& c) { return (long long)c.nx * c.ny * c.nz >= kLargeRunPoints; }
 
 double seconds(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double>(b - a).count();
@@ -77,6 +88,7 @@ struct dns3d_server {
     // worker-thread state: the batch of the runs taking full rounds
     dns3d_batch* batch = nullptr;
     std::vector<dns3d_handle*> batch_runs;
+    int batch_pending = 0;  // steps queued on the batch, not yet counted
     bool use_batch = true;  // DNS3D_SERVER_BATCH=0: every run steps on its own stream
 
     void loop();
@@ -137,9 +149,13 @@ void dns3d_server::build_loop() {
 }
 
 void dns3d_server::drop_batch() {
-    if (batch) dns3d_batch_destroy(batch);
+    if (batch) {
+        if (batch_pending > 0) dns3d_batch_synchronize(batch);
+        dns3d_batch_destroy(batch);
+    }
     batch = nullptr;
     batch_runs.clear();
+    batch_pending = 0;
 }
 
 void dns3d_server::loop() {
@@ -184,42 +200,46 @@ void dns3d_server::loop() {
                 continue;
             }
         }
-        // one round: queue every run's steps, then wait for all
-        std::vector<int> adv(active.size(), 0);
-        std::vector<dns3d_handle*> full;
-        for (auto& r : active)
-            if (r->nsteps - r->steps_done >= opts.steps_per_round) full.push_back(r->h);
-        if (!use_batch) full.clear();
-        if (full != batch_runs) {
-            drop_batch();
-            if (full.size() >= 2 && dns3d_batch_create(full.data(), (int)full.size(), 0, &batch) != DNS3D_OK)
-                batch = nullptr;  // the runs step on their own streams instead
-            batch_runs = full;
-        }
-        bool batch_ok = true;
-        if (batch) batch_ok = dns3d_batch_step(batch, opts.steps_per_round) == DNS3D_OK;
-        for (size_t i = 0; i < active.size(); ++i) {
-            auto& r = active[i];
-            const int k = std::min(opts.steps_per_round, r->nsteps - r->steps_done);
-            const bool in_batch = batch && k == opts.steps_per_round;
-            if (in_batch) {
-                if (batch_ok) adv[i] = k;
-                else r->error = DNS3D_E_CUDA;
-            } else if (k > 0 && dns3d_step(r->h, k) == DNS3D_OK) {
-                adv[i] = k;
-            } else if (k > 0) {
-                r->error = DNS3D_E_CUDA;
+        bool progressed = false;
+        // (1) count the steps of completed chunks
+        if (batch && batch_pending > 0) {
+            int fin = 0;
+            if (dns3d_batch_query(batch, &fin) != DNS3D_OK) {
+                fin = 1;
+                for (auto& r : active)
+                    if (r->in_batch) r->error = DNS3D_E_CUDA;
+            }
+            if (fin) {
+                for (auto& r : active)
+                    if (r->in_batch && !r->error) r->steps_done += batch_pending;
+                batch_pending = 0;
+                progressed = true;
             }
         }
-        for (size_t i = 0; i < active.size(); ++i) {
-            auto& r = active[i];
-            if (dns3d_synchronize(r->h) != DNS3D_OK && !r->error) r->error = DNS3D_E_CUDA;
-            r->steps_done += adv[i];
+        for (auto& r : active) {
+            if (r->in_batch || r->pending == 0) continue;
+            int fin = 0;
+            if (dns3d_query(r->h, &fin) != DNS3D_OK) {
+                fin = 1;
+                r->error = DNS3D_E_CUDA;
+            }
+            if (fin) {
+                if (!r->error) r->steps_done += r->pending;
+                r->pending = 0;
+                progressed = true;
+            }
         }
+        // (2) finished runs, once nothing of theirs is in flight
         std::vector<std::shared_ptr<Request>> done;
         for (auto& r : active)
-            if (r->error || r->steps_done >= r->nsteps) done.push_back(r);
-        if (!done.empty()) drop_batch();  // before any of its handles goes
+            if ((r->error || r->steps_done >= r->nsteps) && r->pending == 0 && !(r->in_batch && batch_pending > 0))
+                done.push_back(r);
+        for (auto& r : done)
+            if (r->in_batch) {  // the batch is idle here; drop it before its handle goes
+                drop_batch();
+                for (auto& a : active) a->in_batch = false;
+                break;
+            }
         for (auto& r : done) {
             if (!r->error) {
                 const int rc = dns3d_diagnostics(r->h, &r->diag);
@@ -241,6 +261,52 @@ void dns3d_server::loop() {
             point_steps += (unsigned long long)r->steps_done * r->cfg.nx * r->cfg.ny * r->cfg.nz;
             active.erase(std::find(active.begin(), active.end(), r));
             cv_done.notify_all();
+            progressed = true;
+        }
+        // (3) the batch, while idle: re-form it if its membership changed, and
+        // queue its next chunk
+        const int spr = opts.steps_per_round;
+        if (batch_pending == 0) {
+            std::vector<dns3d_handle*> full;
+            if (use_batch)
+                for (auto& r : active)
+                    if (!r->error && !large_run(r->cfg) && r->pending == 0 && r->nsteps - r->steps_done >= spr)
+                        full.push_back(r->h);
+            if (full.size() < 2) full.clear();
+            if (full != batch_runs) {
+                drop_batch();
+                for (auto& r : active) r->in_batch = false;
+                if (!full.empty() && dns3d_batch_create(full.data(), (int)full.size(), 0, &batch) == DNS3D_OK) {
+                    batch_runs = full;
+                    for (auto& r : active)
+                        r->in_batch = std::find(full.begin(), full.end(), r->h) != full.end();
+                } else {
+                    batch = nullptr;  // the runs step on their own streams instead
+                }
+            }
+            if (batch) {
+                if (dns3d_batch_step(batch, spr) == DNS3D_OK) {
+                    batch_pending = spr;
+                } else {
+                    for (auto& r : active)
+                        if (r->in_batch) r->error = DNS3D_E_CUDA;
+                }
+                progressed = true;
+            }
+        }
+        // (4) every idle run outside the batch gets its next chunk
+        for (auto& r : active) {
+            if (r->in_batch || r->pending > 0 || r->error) continue;
+            const int k = std::min(spr, r->nsteps - r->steps_done);
+            if (k <= 0) continue;
+            if (dns3d_step(r->h, k) == DNS3D_OK) r->pending = k;
+            else r->error = DNS3D_E_CUDA;
+            progressed = true;
+        }
+        // (5) all units busy: wait a little (or for a new request or built run)
+        if (!progressed) {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_work.wait_for(lk, std::chrono::microseconds(200), [&] { return stop || !built.empty(); });
         }
     }
 }

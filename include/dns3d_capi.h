@@ -187,6 +187,9 @@ int dns3d_step(dns3d_handle* h, int nsteps);
 
 /* Wait for all work queued on the handle's stream. */
 int dns3d_synchronize(dns3d_handle* h);
+/* Without waiting: *done = 1 if all work queued on the handle has completed,
+ * else 0 (for a driver that overlaps runs, e.g. the request server). */
+int dns3d_query(dns3d_handle* h, int* done);
 
 /* output_diagnostics_3d observables plus check_divergence_3d's max |div u|. */
 int dns3d_diagnostics(dns3d_handle* h, dns3d_diag* out);
@@ -285,6 +288,8 @@ int dns3d_batch_create(dns3d_handle* const* runs, int nruns, int flags, dns3d_ba
 /* Queues nsteps steps of every run (returns before they finish). */
 int dns3d_batch_step(dns3d_batch* b, int nsteps);
 int dns3d_batch_synchronize(dns3d_batch* b);
+/* Without waiting: *done = 1 if the batch's queued steps have completed. */
+int dns3d_batch_query(dns3d_batch* b, int* done);
 /* Kernel launches per step of the whole batch, and how many runs are in
  * ragged launches (the rest use their own). */
 int dns3d_batch_info(dns3d_batch* b, int* launches_per_step, int* ragged_runs);

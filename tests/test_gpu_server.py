@@ -53,3 +53,30 @@ def test_served_batches_rebuilt_as_runs_finish(built_lib):
             solo = d.get_state(walls=False)
         for k in ("u", "v", "w", "p_total"):
             assert np.array_equal(st[k], solo[k]), (cfg.nx, cfg.ny, cfg.nz, k)
+
+
+def test_large_and_small_runs_overlap(built_lib):
+    """A large run (at least 2^20 points: its own launches, never in a batch)
+    beside small batched runs, every unit getting its next chunk as soon as its
+    last one completes: every result is the run's solo result, and
+    dns3d_query reports a handle done once its work has completed."""
+    import ctypes as C
+    small = [config_from(d, precision=PREC_MIXED) for d in ensemble_draws(4, seed=21)]
+    large = config_from(dict(ensemble_draws(1, seed=22)[0], nx=128, ny=96, nz=97, lgl_dmatrix_guard=False),
+                        precision=PREC_MIXED)
+    with Server(steps_per_round=5) as srv:
+        lid = srv.submit(large, 60, keep_state=True)
+        sids = [srv.submit(c, 12, keep_state=True) for c in small]
+        sinfo = [srv.wait(i, timeout=300.0) for i in sids]
+        linfo = srv.wait(lid, timeout=300.0)
+        states = [srv.result_state(i) for i in sids] + [srv.result_state(lid)]
+    assert all(i.status == REQ_DONE for i in sinfo + [linfo])
+    for cfg, n, st in zip(small + [large], [12] * 4 + [60], states):
+        with ChannelDNS(cfg) as d:
+            d.step(n)
+            done = C.c_int(-1)
+            assert d.lib.dns3d_query(d._h, C.byref(done)) == 0 and done.value in (0, 1)
+            solo = d.get_state(walls=False)
+            assert d.lib.dns3d_query(d._h, C.byref(done)) == 0 and done.value == 1
+        for k in ("u", "v", "w", "p_total"):
+            assert np.array_equal(st[k], solo[k]), (cfg.nx, cfg.ny, cfg.nz, k)
