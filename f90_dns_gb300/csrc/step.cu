@@ -511,8 +511,8 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //      and of the sources, copied with cp.async while the previous q ran
 //      (c)-(g), so the strided column reads (one 16-byte value per level, a
 //      plane apart) overlap that q's tensor-core work,
-//  (c) each column gets its power-of-two scale and (d) its digits, one
-//      16-byte core-matrix row (8 levels) per thread and digit;
+//  (c) each column gets its power-of-two scale and (d) its digits, two K
+//      rows of one column per thread (tc_digit_pairs);
 //  (e) one thread issues, per digit slice sa of the operator, the K-steps of
 //      block E (even rows: right-hand-side rows [0, ke)) and of block O (odd
 //      rows: [ke, kt)), each against right-hand-side digit slices
@@ -521,43 +521,54 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //  (f) every row's 8 class accumulators are combined in 64-bit integers and
 //      scaled to FP64;
 //  (g) the outputs F* = x - f are written (wall values at the walls).
-// Byte offset of the staged inputs in the viscous tensor-core kernel's shared
-// memory: after the digit slices, right-hand-side digits, results, column
-// exponents, barriers, TMEM address and arrival flag (16-byte aligned).
-// Combination of one warp's TMEM lanes for NC right-hand-side columns from
-// column col0 (NC = 12 from 0, 8 from 0 or 4 from 8): the 8 weight-class
-// accumulators summed in 64-bit integers (tc_class_term), scaled to FP64 and
-// stored to sR at the lane's row.
-template <int NC>
-__device__ __noinline__ void tc_combine_rows(uint32_t lanes, int col0, double* sR, int m8, int row, bool valid,
-                                                int e, const int* sF) {
-    long long T[NC];
+// Combination of one warp's TMEM lanes for 6 right-hand-side columns (H = 0:
+// columns 0 .. 5, H = 1: 6 .. 11): the 8 weight-class accumulators of each
+// column loaded back to back under one wait, combined in 64-bit integers
+// (tc_combine8), scaled to FP64 and stored to sR at the lane's row.  The two
+// warps of a lane quadrant take one half each.
+template <int H>
+__device__ __noinline__ void tc_combine6(uint32_t lanes, double* sR, int m8, int row, bool valid, int e,
+                                         const int* sF) {
+    uint32_t r[kTcClasses * 6];
 #pragma unroll
-    for (int j = 0; j < NC; ++j) T[j] = 0;
     for (int c = 0; c < kTcClasses; ++c) {
-        float v[NC > 8 ? 16 : 8];
-        if (NC > 8) tc_ld16(lanes + (uint32_t)(c * kTcN + col0), v);
-        else tc_ld8(lanes + (uint32_t)(c * kTcN + col0), v);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) T[j] += tc_class_term(c, v[j]);
+        const uint32_t a = lanes + (uint32_t)(c * kTcN + 6 * H);
+        if (H == 0) {
+            tc_ld4_nw(a, r + 6 * c);
+            tc_ld2_nw(a + 4, r + 6 * c + 4);
+        } else {  // each load's first column a multiple of its width
+            tc_ld2_nw(a, r + 6 * c);
+            tc_ld4_nw(a + 2, r + 6 * c + 2);
+        }
     }
+    tc_ld_wait(r);
     if (valid) {
 #pragma unroll
-        for (int j = 0; j < NC; ++j) sR[(col0 + j) * m8 + row] = i2d_scaled(T[j], e + sF[col0 + j] - 52);
+        for (int j = 0; j < 6; ++j) {
+            const long long T = tc_combine8(r[j], r[6 + j], r[12 + j], r[18 + j], r[24 + j], r[30 + j], r[36 + j],
+                                            r[42 + j]);
+            sR[(6 * H + j) * m8 + row] = i2d_scaled(T, e + sF[6 * H + j] - 52);
+        }
     }
 }
 
 // Bytes of unused shared memory in front of the digit slices: block O's MMA
-// starts 64 rows before its operand (so that its results land in TMEM lanes
-// 64 .. 64 + o8, see viscous_tc_body), and those 64 rows of the first slice
-// must still lie inside the CTA's shared memory.  Rows it reads there only
-// produce accumulator lanes that are never read.
-__host__ __device__ inline size_t viscous_tc_pad(const TcGeom& t) {
-    const TcBlocks bl = tc_blocks(t, false);
+// starts 64 rows (8 row groups) before its operand, so that its o8 <= 64
+// result rows land in TMEM lanes 64 .. 64 + o8 (lane quadrants 2 and 3) while
+// block E's use quadrants 0 and 1 (2 as well at nz = 129), and the
+// combination spreads over more warps, each reading only its own quadrant.
+// Those 64 rows of the first slice must still lie inside the CTA's shared
+// memory; rows an MMA reads there only produce accumulator lanes that are
+// never read.
+__host__ __device__ inline size_t tc_oshift_pad(const TcBlocks& bl) {
     const long long need = 8LL * bl.kO * 16 - (long long)bl.aE * 2;
     return need > 0 ? (size_t)((need + 127) / 128 * 128) : 0;
 }
+__host__ __device__ inline size_t viscous_tc_pad(const TcGeom& t) { return tc_oshift_pad(tc_blocks(t, false)); }
 
+// Byte offset of the staged inputs in the viscous tensor-core kernel's shared
+// memory: after the digit slices, right-hand-side digits, results, column
+// exponents, barriers, TMEM address and arrival flag (16-byte aligned).
 __host__ __device__ inline size_t viscous_tc_stage_offset(const TcGeom& t) {
     const size_t b = viscous_tc_pad(t) + (size_t)kTcSlices * (tc_blocks(t, false).a + kTcN * t.kt) * sizeof(__half) +
                      (size_t)kTcN * t.m8 * sizeof(double) + kTcN * sizeof(int) + 2 * sizeof(uint64_t) + 16;
@@ -616,18 +627,20 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     const int nv = he + ho;  // valid rows / K indices
     const bool staged = viscous_tc_staged(t, nz);
     // cp.async of the inputs of operator index q into sP (both modes' columns
-    // of u, v, w and of the sources; a missing second mode is not read)
+    // of u, v, w and of the sources; a missing second mode is not read): one
+    // warp per column, its lanes over the levels
     auto stage = [&](int q) {
         if (!staged) return;
         const int kya = q / g.nxhp, kx = q - kya * g.nxhp;
         const int nmode = (kya > 0 && 2 * kya != g.ny) ? 2 : 1;
-        for (int j = threadIdx.x; j < 2 * nmode * 3 * nz; j += blockDim.x) {
-            const int z = j % nz, r = j / nz;
+        const int lane = threadIdx.x & 31;
+        for (int r = threadIdx.x >> 5; r < 2 * nmode * 3; r += blockDim.x >> 5) {
             const int comp = r % 3, r2 = r / 3;
             const int mi = r2 % nmode, fld = r2 / nmode;
             const int m = (mi ? g.ny - kya : kya) * g.nxhp + kx;
-            const double2* src = fld ? fptr(Src, comp) : fptr(F, comp);
-            cp_async16(sP + (size_t)((fld * 2 + mi) * 3 + comp) * nz + z, src + (size_t)z * g.nm + m);
+            const double2* src = (fld ? fptr(Src, comp) : fptr(F, comp)) + m;
+            double2* dst = sP + (size_t)((fld * 2 + mi) * 3 + comp) * nz;
+            for (int z = lane; z < nz; z += 32) cp_async16(dst + z, src + (size_t)z * g.nm);
         }
         cp_async_commit();
     };
@@ -734,21 +747,22 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             }
         }
         __syncthreads();
-        // (d) digits of the right-hand sides, one K row of one column per
-        // thread: even levels at K [0, he), odd ones at K [ke, ke + ho); a warp
-        // covers 8 K rows of 4 columns, so its 2-byte stores fall in distinct
-        // shared-memory banks (the bank of (n, k) in a core matrix is
-        // 4 (n mod 8) + (k mod 8)/2)
-        for (int i = threadIdx.x; i < 12 * t.kt; i += blockDim.x) {
-            const int kl = i & 7, cc = i >> 3;
-            const int c = cc % 12, kk = (cc / 12) * 8 + kl;
-            const int row = kk < t.ke ? (kk < he ? kk : -1) : (kk - t.ke < ho ? t.e8 + (kk - t.ke) : -1);
-            if (row < 0) continue;  // padding K rows: zeroed once at the start, never written
-            int d[kTcSlices];
-            tc_digits(tc_fixed(sR[c * m8 + row], sF[c]), d);
-            __half* dst = sB + tc_core_off(c, kk, t.kt);
+        // (d) digits of the right-hand sides, K rows kk, kk + 1 (kk even) of
+        // one column per thread, one half2 per digit slice: even levels at K
+        // [0, he), odd ones at K [ke, ke + ho); a warp covers the 4 row pairs
+        // of an 8-row group for 8 columns, so its 4-byte stores fall in
+        // distinct shared-memory banks but for columns 8 apart (the bank of
+        // (n, k) in a core matrix is 4 (n mod 8) + (k mod 8)/2)
+        for (int i = threadIdx.x; i < 12 * (t.kt / 2); i += blockDim.x) {
+            const int kp = i & 3, cc = i >> 2;
+            const int c = cc % 12, kk = (cc / 12) * 8 + 2 * kp;
+            const int r0 = tc_k_row(t, kk), r1 = tc_k_row(t, kk + 1);
+            if (r0 < 0) continue;  // padding K rows: zeroed once at the start, never written
+            __half2 h[kTcSlices];
+            tc_digit_pairs(tc_fixed(sR[c * m8 + r0], sF[c]), r1 < 0 ? 0 : tc_fixed(sR[c * m8 + r1], sF[c]), h);
+            __half2* dst = reinterpret_cast<__half2*>(sB + tc_core_off(c, kk, t.kt));
 #pragma unroll
-            for (int s = 0; s < kTcSlices; ++s) dst[s * b_halves] = __int2half_rn(d[s]);
+            for (int s = 0; s < kTcSlices; ++s) dst[s * (b_halves / 2)] = h[s];
         }
         tc_fence_proxy();
         tc_fence_before();
@@ -804,7 +818,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             // warp w reads TMEM lane quadrant w % 4 (lanes 32 (w % 4) .. +31);
             // block E's rows are lanes 0 .. e8, block O's lanes 64 .. 64 + o8.
             // A quadrant holding rows of one block splits its 12 columns
-            // between its two warps (8 and 4); one holding rows of both blocks
+            // between its two warps (6 each); one holding rows of both blocks
             // (nz = 129: lanes 64 .. 71 of E) gives each warp one block.
             const int w = threadIdx.x >> 5;
             if (w < 8) {
@@ -813,19 +827,20 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                 const bool hasO = quad >= 2 && 32 * quad < 64 + t.o8;
                 const int lane = 32 * quad + (threadIdx.x & 31);
                 const uint32_t lanes = tmem + ((uint32_t)(32 * quad) << 16);
-                if (hasE && hasO) {
-                    const int blk = half;
+                if (hasE || hasO) {
+                    const int blk = (hasE && hasO) ? half : (hasO ? 1 : 0);
                     const bool valid = blk ? (lane >= 64 && lane - 64 < t.o8) : lane < t.e8;
                     const int row = blk ? t.e8 + (lane - 64) : lane;
                     const int e = valid ? __ldg(&ops.tcE[(size_t)q * m8 + row]) : 0;
-                    tc_combine_rows<12>(lanes + (uint32_t)(blk * kTcDCols), 0, sR, m8, row, valid, e, sF);
-                } else if (hasE || hasO) {
-                    const int blk = hasO ? 1 : 0;
-                    const bool valid = blk ? (lane >= 64 && lane - 64 < t.o8) : lane < t.e8;
-                    const int row = blk ? t.e8 + (lane - 64) : lane;
-                    const int e = valid ? __ldg(&ops.tcE[(size_t)q * m8 + row]) : 0;
-                    if (half == 0) tc_combine_rows<8>(lanes + (uint32_t)(blk * kTcDCols), 0, sR, m8, row, valid, e, sF);
-                    else tc_combine_rows<4>(lanes + (uint32_t)(blk * kTcDCols), 8, sR, m8, row, valid, e, sF);
+                    const uint32_t lb = lanes + (uint32_t)(blk * kTcDCols);
+                    if (hasE && hasO) {
+                        tc_combine6<0>(lb, sR, m8, row, valid, e, sF);
+                        tc_combine6<1>(lb, sR, m8, row, valid, e, sF);
+                    } else if (half == 0) {
+                        tc_combine6<0>(lb, sR, m8, row, valid, e, sF);
+                    } else {
+                        tc_combine6<1>(lb, sR, m8, row, valid, e, sF);
+                    }
                 }
             }
         }
@@ -898,10 +913,12 @@ constexpr int kTcCorrModes = kTcVortCols / 2;  // modes per tile: phi x re, im
 constexpr int kTcVortThreads = 512;
 
 // Byte offset of the staged input columns in the z-derivative kernels' shared
-// memory (after the D1 image, digits, results, exponents, barriers), and
-// whether they fit (kTcVortCols / 2 columns of nz values).
+// memory (after the pad of the shifted block O, the D1 image, digits,
+// results, exponents, barriers), and whether they fit (kTcVortCols / 2
+// columns of nz values).
 __host__ __device__ inline size_t dz_tc_stage_offset(const TcGeom& t) {
-    const size_t b = (size_t)kTcSlices * (tc_blocks(t, true).a + kTcVortCols * t.kt) * sizeof(__half) +
+    const TcBlocks bl = tc_blocks(t, true);
+    const size_t b = tc_oshift_pad(bl) + (size_t)kTcSlices * (bl.a + kTcVortCols * t.kt) * sizeof(__half) +
                      (size_t)kTcVortCols * t.m8 * sizeof(double) + (size_t)(t.m8 + kTcVortCols) * sizeof(int) +
                      2 * sizeof(uint64_t) + 16;
     return (b + 15) / 16 * 16;
@@ -919,7 +936,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     const TcBlocks bl = tc_blocks(t, true);
     const int nz = g.nz, he = t.he, ho = t.ho, m8 = t.m8;
     const int b_halves = kTcVortCols * t.kt;
-    __half* sA = reinterpret_cast<__half*>(tcsm);
+    __half* sA = reinterpret_cast<__half*>(tcsm + tc_oshift_pad(bl));
     __half* sB = sA + kTcSlices * bl.a;
     double* sR = reinterpret_cast<double*>(sB + kTcSlices * b_halves);  // [32][m8]: folded u, v, then D1.u, D1.v
     int* sE = reinterpret_cast<int*>(sR + kTcVortCols * m8);            // row exponents of D1
@@ -958,10 +975,12 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     auto stage = [&](int tile) {
         if (!staged) return;
         const int m0 = tile * kModes;
+        // the tile's modes fastest: adjacent lanes copy adjacent modes of one level
         for (int j = tid; j < kModes * Op::kFields * nz; j += blockDim.x) {
-            const int z = j % nz, r = j / nz;
-            const int f = r % Op::kFields, mi = r / Op::kFields;
-            if (m0 + mi < g.nm) cp_async16(sP + (size_t)r * nz + z, op.field(f) + (size_t)z * g.nm + m0 + mi);
+            const int mi = j % kModes, r = j / kModes;
+            const int f = r % Op::kFields, z = r / Op::kFields;
+            if (m0 + mi < g.nm)
+                cp_async16(sP + (size_t)(mi * Op::kFields + f) * nz + z, op.field(f) + (size_t)z * g.nm + m0 + mi);
         }
         cp_async_commit();
     };
@@ -1022,18 +1041,19 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             }
         }
         __syncthreads();
-        // (d) digits, one K row of one column per thread (a warp: 8 K rows of
-        // 4 columns): even levels at K [0, he), odd ones at K [ke, ke + ho)
-        for (int i = tid; i < kTcVortCols * t.kt; i += blockDim.x) {
-            const int kl = i & 7, cc = i >> 3;
-            const int c = cc % kTcVortCols, kk = (cc / kTcVortCols) * 8 + kl;
-            const int row = kk < t.ke ? (kk < he ? kk : -1) : (kk - t.ke < ho ? t.e8 + (kk - t.ke) : -1);
-            if (row < 0) continue;  // padding K rows: zeroed once at the start, never written
-            int d[kTcSlices];
-            tc_digits(tc_fixed(sR[c * m8 + row], sF[c]), d);
-            __half* dst = sB + tc_core_off(c, kk, t.kt);
+        // (d) digits, K rows kk, kk + 1 (kk even) of one column per thread
+        // (a warp: the 4 row pairs of an 8-row group for 8 columns, distinct
+        // banks): even levels at K [0, he), odd ones at K [ke, ke + ho)
+        for (int i = tid; i < kTcVortCols * (t.kt / 2); i += blockDim.x) {
+            const int kp = i & 3, cc = i >> 2;
+            const int c = cc % kTcVortCols, kk = (cc / kTcVortCols) * 8 + 2 * kp;
+            const int r0 = tc_k_row(t, kk), r1 = tc_k_row(t, kk + 1);
+            if (r0 < 0) continue;  // padding K rows: zeroed once at the start, never written
+            __half2 h[kTcSlices];
+            tc_digit_pairs(tc_fixed(sR[c * m8 + r0], sF[c]), r1 < 0 ? 0 : tc_fixed(sR[c * m8 + r1], sF[c]), h);
+            __half2* dst = reinterpret_cast<__half2*>(sB + tc_core_off(c, kk, t.kt));
 #pragma unroll
-            for (int s = 0; s < kTcSlices; ++s) dst[s * b_halves] = __int2half_rn(d[s]);
+            for (int s = 0; s < kTcSlices; ++s) dst[s * (b_halves / 2)] = h[s];
         }
         tc_fence_proxy();
         tc_fence_before();
@@ -1046,7 +1066,10 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
                 // the descriptors differ only in their start address (16-byte
                 // units; a K offset of k elements is k units): one add per MMA
                 const uint64_t dAE = tc_desc(tc_smem_u32(sA), 128, (uint32_t)bl.kE * 16);
-                const uint64_t dAO = tc_desc(tc_smem_u32(sA + bl.aE), 128, (uint32_t)bl.kO * 16);
+                // block O starts 64 rows before its operand: its results land in
+                // TMEM lanes 64 .. 64 + o8 (tc_oshift_pad)
+                const uint64_t dAO =
+                    tc_desc(tc_smem_u32(sA + bl.aE) - (uint32_t)(8 * bl.kO * 16), 128, (uint32_t)bl.kO * 16);
                 const uint64_t dB = tc_desc(tc_smem_u32(sB), 128, (uint32_t)t.kt * 16);
                 const int nkE = bl.kE / 16, nkO = bl.kO / 16;
                 constexpr uint32_t kDC = kTcClasses * kTcVortCols;
@@ -1079,32 +1102,34 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
             break;
         }
         {
-            // warp w reads TMEM lane quadrant w % 4; the warps of a quadrant
-            // (w / 4 = 0 .. 3) take the (block, 8-column group) items of it
+            // warp w reads TMEM lane quadrant w % 4: block E's rows are lanes
+            // 0 .. e8, block O's lanes 64 .. 64 + o8; the warps of a quadrant
+            // (w / 4 = 0 .. 3) take its (block, 4-column group) items, each
+            // item's 8 class accumulators loaded back to back under one wait
+            constexpr int kGroups = kTcVortCols / 4;
             const int w = tid >> 5, quad = w & 3, grp = w >> 2, ngrp = (int)(blockDim.x >> 7);
-            for (int it = grp; it < 2 * (kTcVortCols / 8); it += ngrp) {
-                const int blk = it / (kTcVortCols / 8), cb = it - blk * (kTcVortCols / 8);
-                const int rows = blk ? t.o8 : t.e8;
-                if (32 * quad >= rows) continue;
-                long long T[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) T[j] = 0;
+            const int lane = 32 * quad + (tid & 31);
+            const bool hasE = 32 * quad < t.e8;
+            const bool hasO = quad >= 2 && 32 * quad < 64 + t.o8;
+            const int nitems = ((int)hasE + (int)hasO) * kGroups;
+            for (int it = grp; it < nitems; it += ngrp) {
+                const int blk = (hasE && it < kGroups) ? 0 : 1, cb = it % kGroups;
                 const uint32_t base = tmem + ((uint32_t)(32 * quad) << 16) +
-                                      (uint32_t)(blk * kTcClasses * kTcVortCols + 8 * cb);
-                for (int c = 0; c < kTcClasses; ++c) {
-                    float v[8];
-                    tc_ld8(base + (uint32_t)(c * kTcVortCols), v);
+                                      (uint32_t)(blk * kTcClasses * kTcVortCols + 4 * cb);
+                uint32_t r[4 * kTcClasses];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) T[j] += tc_class_term(c, v[j]);
-                }
-                const int r = 32 * quad + (tid & 31);
-                if (r < rows) {
-                    const int row = blk ? t.e8 + r : r;
+                for (int c = 0; c < kTcClasses; ++c) tc_ld4_nw(base + (uint32_t)(c * kTcVortCols), r + 4 * c);
+                tc_ld_wait(r);
+                const bool valid = blk ? (lane >= 64 && lane - 64 < t.o8) : lane < t.e8;
+                if (valid) {
+                    const int row = blk ? t.e8 + (lane - 64) : lane;
                     const int e = sE[row];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const int col = 8 * cb + j;
-                        sR[col * m8 + row] = i2d_scaled(T[j], e + sF[col] - 52);
+                    for (int j = 0; j < 4; ++j) {
+                        const int col = 4 * cb + j;
+                        const long long T = tc_combine8(r[j], r[4 + j], r[8 + j], r[12 + j], r[16 + j], r[20 + j],
+                                                        r[24 + j], r[28 + j]);
+                        sR[col * m8 + row] = i2d_scaled(T, e + sF[col] - 52);
                     }
                 }
             }

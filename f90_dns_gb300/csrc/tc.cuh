@@ -92,6 +92,12 @@ __host__ __device__ inline TcBlocks tc_blocks(const TcGeom& t, bool anti) {
     return b;
 }
 
+// Row of the folded value (even rows first, odd ones from e8) behind
+// right-hand-side K index kk, or -1 for a padding K row.
+__host__ __device__ inline int tc_k_row(const TcGeom& t, int kk) {
+    return kk < t.ke ? (kk < t.he ? kk : -1) : (kk - t.ke < t.ho ? t.e8 + (kk - t.ke) : -1);
+}
+
 // Halves per q of the compact slice store: per digit, the nonzero core
 // matrices (even block row-major, then odd block), 64 halves each.
 __host__ __device__ inline size_t tc_q_halves(const TcGeom& t) {
@@ -111,6 +117,36 @@ __device__ __forceinline__ void tc_digits(long long u, int* c) {
         const int d = r >= 64 ? r - 128 : r;
         c[s] = d;
         u = (u - d) >> 7;
+    }
+}
+
+// 64 in each of the 8 base-128 digit places: 64 (1 + 128 + ... + 128^7).
+constexpr unsigned long long kTcDigitBias = 0x0081020408102040ULL;
+
+__device__ __forceinline__ __half2 tc_u32_as_half2(uint32_t w) {
+    __half2 h;
+    memcpy(&h, &w, sizeof(h));
+    return h;
+}
+
+// The digits of two values at once (K rows kk, kk + 1 of one right-hand-side
+// column), slice s as the pair {c_s(u0), c_s(u1)}: the same digits as
+// tc_digits.  V = U + kTcDigitBias holds U's balanced digits plus 64 in its
+// 7-bit fields (0 <= V < 2^56 for |U| <= 2^54, no carries), and for a field
+// value v in [0, 127] the FP16 with bits 0x6400 | v is 1024 + v, so one
+// packed subtraction of 1088 gives a pair of digits.
+__device__ __forceinline__ void tc_digit_pairs(long long u0, long long u1, __half2* h) {
+    const unsigned long long v0 = (unsigned long long)u0 + kTcDigitBias;
+    const unsigned long long v1 = (unsigned long long)u1 + kTcDigitBias;
+    const uint32_t l0 = (uint32_t)v0, m0 = (uint32_t)(v0 >> 28);
+    const uint32_t l1 = (uint32_t)v1, m1 = (uint32_t)(v1 >> 28);
+    const __half2 off = tc_u32_as_half2(0x64406440u);  // {1088, 1088}
+#pragma unroll
+    for (int fi = 0; fi < kTcSlices; ++fi) {  // fi = 0: least significant digit (slice 7)
+        const uint32_t a = fi < 4 ? l0 >> (7 * fi) : m0 >> (7 * (fi - 4));
+        const uint32_t b = fi < 4 ? l1 >> (7 * fi) : m1 >> (7 * (fi - 4));
+        const uint32_t w = __byte_perm((a & 127u) | 0x6400u, (b & 127u) | 0x6400u, 0x5410);
+        h[kTcSlices - 1 - fi] = __hsub2(tc_u32_as_half2(w), off);
     }
 }
 
@@ -145,6 +181,21 @@ __device__ __forceinline__ int tc_f2i(float v) { return __float_as_int(v + 12582
 __device__ __forceinline__ long long tc_class_term(int c, float v) {
     const long long d = (long long)tc_f2i(v);
     return c < kTcClasses - 1 ? d * (1LL << (7 * (kTcClasses - 2 - c))) : (d + 64) >> 7;
+}
+
+// The whole combination T of one output from its 8 class accumulators (as
+// raw TMEM words), the same integer as the sum of tc_class_term: adjacent
+// classes pair up exactly in 32 bits (|D_c 128 + D_c+1| < 2^30), so only
+// three 64-bit steps remain.
+__device__ __forceinline__ long long tc_combine8(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, uint32_t w4,
+                                                 uint32_t w5, uint32_t w6, uint32_t w7) {
+    const int pa = tc_f2i(__uint_as_float(w0)) * 128 + tc_f2i(__uint_as_float(w1));
+    const int pb = tc_f2i(__uint_as_float(w2)) * 128 + tc_f2i(__uint_as_float(w3));
+    const int pc = tc_f2i(__uint_as_float(w4)) * 128 + tc_f2i(__uint_as_float(w5));
+    const int tail = tc_f2i(__uint_as_float(w6)) + ((tc_f2i(__uint_as_float(w7)) + 64) >> 7);
+    long long T = (long long)pa * 16384 + pb;
+    T = T * 16384 + pc;
+    return T * 128 + tail;
 }
 
 __device__ __forceinline__ uint32_t tc_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -254,6 +305,25 @@ __device__ __forceinline__ void tc_ld8(uint32_t taddr, float* v) {
     asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// TMEM loads issued back to back with one wait (tc_ld_wait) for all of them:
+// N = 2 or 4 consecutive columns of this thread's lane, no wait.
+__device__ __forceinline__ void tc_ld2_nw(uint32_t taddr, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
+}
+__device__ __forceinline__ void tc_ld4_nw(uint32_t taddr, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
+// The wait, then every loaded register passed through an empty volatile asm
+// ordered after it, so that no use of a loaded value moves above the wait.
+template <int N>
+__device__ __forceinline__ void tc_ld_wait(uint32_t (&r)[N]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < N; ++i) asm volatile("" : "+r"(r[i]));
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;"); }
