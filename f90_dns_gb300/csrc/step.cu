@@ -338,6 +338,44 @@ __device__ __forceinline__ double2 viscous_rhs_cn(const GridDev& g, const Ops& o
                         whz * (2.0 * f.y + sp.dt * s.y) - (s0 * l1.y + sn * ln.y));
 }
 
+// viscous_rhs_cn folded at the level pair (k, nz-1-k), k >= 1: with the
+// symmetric weights (w_k = w_nz-1-k) and lifting columns (S0_nz-1-k =
+// Sn_k), r_k + r_k' = 2 w_k (a_k + a_k') - (S0_k + Sn_k)(l1 + ln) and
+// r_k - r_k' = 2 w_k (a_k - a_k') - (S0_k - Sn_k)(l1 - ln), with
+// a = f + (dt/2) s and the lifting data l1 = f_1 + 2 bc1, ln = f_nz + 2 bc2;
+// the unpaired mid level (nz odd) gets r_k itself.  A third fewer FP64
+// operations than two viscous_rhs_cn calls and their sum and difference.
+__device__ __forceinline__ Pair viscous_rhs_cn_folded(const GridDev& g, const Ops& ops, const StepParams& sp,
+                                                      int comp, int k, int m, int ky, int kx, double2 f1v,
+                                                      double2 f2v, double2 s1, double2 s2, double2 l1, double2 ln,
+                                                      double dpdx) {
+    if (sp.dealias) {  // apply_dealias_truncation (3D:1163-1193)
+        const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
+        if (kx > sp.kx_max || kyi > sp.ky_max) s1 = s2 = make_double2(0.0, 0.0);
+    }
+    if (comp == 0 && m == 0) {  // 3D:1123-1145
+        s1.x += dpdx * sp.forcing_scale;
+        s2.x += dpdx * sp.forcing_scale;
+    }
+    const double hdt = 0.5 * sp.dt;
+    const double tw = 2.0 * __ldg(&ops.wh[k]);
+    const double s0 = __ldg(&ops.S0[k]), sn = __ldg(&ops.Sn[k]);
+    const double2 a1 = make_double2(fma(hdt, s1.x, f1v.x), fma(hdt, s1.y, f1v.y));
+    Pair r;
+    if (k < g.nz / 2) {
+        const double2 a2 = make_double2(fma(hdt, s2.x, f2v.x), fma(hdt, s2.y, f2v.y));
+        const double sp_ = s0 + sn, sm_ = s0 - sn;
+        r.a = make_double2(fma(tw, a1.x + a2.x, -(sp_ * (l1.x + ln.x))),
+                           fma(tw, a1.y + a2.y, -(sp_ * (l1.y + ln.y))));
+        r.b = make_double2(fma(tw, a1.x - a2.x, -(sm_ * (l1.x - ln.x))),
+                           fma(tw, a1.y - a2.y, -(sm_ * (l1.y - ln.y))));
+    } else {
+        r.a = make_double2(fma(tw, a1.x, -(s0 * l1.x + sn * ln.x)), fma(tw, a1.y, -(s0 * l1.y + sn * ln.y)));
+        r.b = make_double2(0.0, 0.0);
+    }
+    return r;
+}
+
 // x_I - f_I at an interior level, the wall value at the walls
 __device__ __forceinline__ double2 viscous_out_cn(const GridDev& g, int z, double2 x, double2 f, double2 bc1,
                                                   double2 bc2) {
@@ -687,13 +725,6 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             if (mi < nmode) {
                 const int ky = mi ? g.ny - kya : kya;
                 const int m = ky * g.nxhp + kx;
-                double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
-                if (comp < 2) {
-                    const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
-                    const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
-                    bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
-                    bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
-                }
                 // the F and source columns of this mode: staged, or read from
                 // global memory one level (a plane) apart
                 const size_t st = staged ? 1 : (size_t)g.nm;
@@ -706,15 +737,22 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                     if (p == 0) { keep1[0] = v1; keep2[0] = v2; }
                     else { keep1[1] = v1; keep2[1] = v2; }
                 }
-                const double2 b1 =
-                    viscous_rhs_cn(g, ops, sp, comp, k, m, ky, kx, v1, sc[(size_t)k * st], f1, fn, bc1, bc2, dpdx);
-                if (k < ho) {
-                    const double2 b2 = viscous_rhs_cn(g, ops, sp, comp, nz - 1 - k, m, ky, kx, v2,
-                                                      sc[(size_t)(nz - 1 - k) * st], f1, fn, bc1, bc2, dpdx);
-                    fe = make_double2(b1.x + b2.x, b1.y + b2.y);
-                    fo = make_double2(b1.x - b2.x, b1.y - b2.y);
-                } else {
-                    fe = b1;
+                if (k > 0) {  // the wall rows of r are zero
+                    // lifting data l = f_wall + 2 bc, bc = -dt dp/dx|wall (u), -dt dp/dy|wall (v), 0 (w)
+                    double2 l1 = f1, ln = fn;
+                    if (comp < 2) {
+                        const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
+                        const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                        const double m2dt = -2.0 * sp.dt;
+                        l1 = make_double2(fma(m2dt, g1.x, f1.x), fma(m2dt, g1.y, f1.y));
+                        ln = make_double2(fma(m2dt, g2.x, fn.x), fma(m2dt, g2.y, fn.y));
+                    }
+                    const double2 s1 = sc[(size_t)k * st];
+                    const double2 s2 = k < ho ? sc[(size_t)(nz - 1 - k) * st] : s1;
+                    const Pair rf =
+                        viscous_rhs_cn_folded(g, ops, sp, comp, k, m, ky, kx, v1, v2, s1, s2, l1, ln, dpdx);
+                    fe = rf.a;
+                    fo = rf.b;
                 }
             }
             const int c0 = 6 * mi + 2 * comp;
@@ -1137,8 +1175,10 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         tc_fence_before();
         __syncthreads();
         // (g) the outputs at the level pair (k, nz-1-k)
+        // (the tile's modes fastest: adjacent lanes read and write adjacent
+        // modes of one level, kModes x 16 contiguous bytes)
         for (int i = tid; i < kModes * he; i += blockDim.x) {
-            const int mi = i / he, k = i - mi * he;
+            const int mi = i % kModes, k = i / kModes;
             const int m = m0 + mi;
             if (m >= g.nm) continue;
             Pair dz[Op::kFields];
@@ -1178,11 +1218,11 @@ struct VortTcOp {
             const int z = p ? g.nz - 1 - k : k;
             const size_t o = (size_t)z * g.nm + m;
             const double2 w = W[o], u = U[o], v = V[o];
-            const double2 wy = i_times(mi.ay, w), wx = i_times(mi.ax, w);
-            const double2 vx = i_times(mi.ax, v), uy = i_times(mi.ay, u);
-            OX[o] = c2sub(wy, p ? dz[1].b : dz[1].a);
-            OY[o] = c2sub(p ? dz[0].b : dz[0].a, wx);
-            OZ[o] = c2sub(vx, uy);
+            const double2 dv = p ? dz[1].b : dz[1].a, du = p ? dz[0].b : dz[0].a;
+            // (i ay) w - dv, du - (i ax) w, (i ax) v - (i ay) u with fused products
+            OX[o] = make_double2(fma(-mi.ay, w.y, -dv.x), fma(mi.ay, w.x, -dv.y));
+            OY[o] = make_double2(fma(mi.ax, w.y, du.x), fma(-mi.ax, w.x, du.y));
+            OZ[o] = make_double2(fma(-mi.ax, v.y, mi.ay * u.y), fma(mi.ax, v.x, -(mi.ay * u.x)));
         }
     }
 };
@@ -1215,17 +1255,17 @@ struct CorrTcOp {
     __device__ const double2* field(int) const { return PHI; }
     __device__ void out(const GridDev& g, const Ops& ops, int m, int k, int npt, const Pair* dzp) const {
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-        const double dt = sp.dt;
+        const double dt = sp.dt, dax = dt * mi.ax, day = dt * mi.ay;
         for (int p = 0; p < npt; ++p) {
             const int z = p ? g.nz - 1 - k : k;
             const double2 d = p ? dzp[0].b : dzp[0].a;
             const size_t o = (size_t)z * g.nm + m;
             const double2 ph = PHI[o];
-            const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
             const double2 us = US[o], vs = VS[o], ws = WS[o];
-            store_projection(sp, z, g.nz, o, make_double2(us.x - dt * px.x, us.y - dt * px.y),
-                             make_double2(vs.x - dt * py.x, vs.y - dt * py.y),
-                             make_double2(ws.x - dt * d.x, ws.y - dt * d.y), U, V, W);
+            // u* - dt (i ax) phi, v* - dt (i ay) phi, w* - dt dphi/dz
+            store_projection(sp, z, g.nz, o, make_double2(fma(dax, ph.y, us.x), fma(-dax, ph.x, us.y)),
+                             make_double2(fma(day, ph.y, vs.x), fma(-day, ph.x, vs.y)),
+                             make_double2(fma(-dt, d.x, ws.x), fma(-dt, d.y, ws.y)), U, V, W);
             double2 pp = P[o];
             pp.x += ph.x;
             pp.y += ph.y;
