@@ -644,6 +644,8 @@ int dns3d_footprint_bytes(const dns3d_config* c, unsigned long long* bytes) {
         if (c->use_crank_nicolson && c->linear_solver == 0)  // digit slices of the Helmholtz inverses
             b += nq * (tc_q_halves(t) * sizeof(__half) + (size_t)t.m8 * sizeof(int));
         b += (size_t)kTcSlices * tc_blocks(t, true).a * sizeof(__half);  // digit image of D1
+        if (!c->use_weak_form_divergence)  // fixed-point Poisson inverses and row exponents
+            b += nq * (fx_qstride((int)ez, (int)hz) * sizeof(long long) + (size_t)c->nz * sizeof(int));
     }
     b += 16ull << 20;                        // operators, tables, reductions
     *bytes = b;
@@ -1278,10 +1280,25 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
         }
         ops.tcD = im;
         ops.tcDE = ex;
+        // the Poisson inverses in fixed point for the solve after the
+        // tensor-core right-hand side (the strong form)
+        if (!c.use_weak_form_divergence) {
+            const size_t qs = fx_qstride(ops.he, ops.ho);
+            long long* gi = nullptr;
+            int* ge = nullptr;
+            if ((rc = dev_alloc(h, &gi, (size_t)nq * qs)) || (rc = dev_alloc(h, &ge, (size_t)nq * nz)))
+                return fail(rc);
+            if ((e = build_fixed_rows(g, ops.PinvF, nq, gi, ge, h->stream)) || (e = cudaStreamSynchronize(h->stream))) {
+                cuda_fail(h, e, "build_fixed_rows");
+                return fail(DNS3D_E_CUDA);
+            }
+            ops.PinvI = gi;
+            ops.PinvE = ge;
+        }
         h->visc_tc_forced = tcenv && std::strcmp(tcenv, "1") == 0;
         h->vort_tc = h->visc_tc_forced || g.nm >= 4 * 152 * 8;
         h->corr_tc = h->visc_tc_forced || g.nm >= 4 * 152 * 16;
-        h->pres_tc = !c.use_weak_form_divergence && (h->visc_tc_forced || g.nm >= 4 * 152 * 16);
+        h->pres_tc = ops.PinvI && (h->visc_tc_forced || g.nm >= 4 * 152 * 16);
     }
 
     if ((rc = dns3d_initialize_fields(h))) return fail(rc);

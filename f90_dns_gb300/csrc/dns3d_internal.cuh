@@ -188,6 +188,13 @@ struct Ops {
     double* HinvF;   // folded Helmholtz inverses      [nq][he*he + ho*ho]
     double* PinvF;   // folded Poisson inverses        [nq][he*he + ho*ho]
     double* PpinT;   // pinned (0,0) Poisson inverse, unfolded, transposed [nz][nz]
+    // PinvF in 58-bit fixed point for the solve on the integer pipes (FP64
+    // runs with the tensor-core forms), or null: entry (j, k) of a folded
+    // block round(G[k][j] 2^(58 - e_k)) in PinvF's layout but with a per-q
+    // stride of fx_qstride (even), row exponents e_k [nq][he + ho] (block
+    // E's rows, then block O's)
+    const long long* PinvI;
+    const int* PinvE;
     int nq;
     // tensor-core form of HinvF (tc.cuh), or null: FP16 digit slices
     // [nq][tc_q_halves] and row exponents [nq][m8]
@@ -365,6 +372,9 @@ cudaError_t launch_nonfinite_check(const double2* f, size_t n, int* flag, cudaSt
 cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh,
                            double helm_f, const double* ksq, int nq, double* HinvF,
                            double* PinvF, double* PpinT, int* info, cudaStream_t s);
+// The 58-bit fixed-point image of the folded Poisson inverses (Ops::PinvI, PinvE).
+cudaError_t build_fixed_rows(const GridDev& g, const double* PinvF, int nq, long long* PinvI, int* PinvE,
+                             cudaStream_t s);
 
 // Residual of the Galerkin Poisson system of the last pressure step: max |b(u*)
 // - P phi| and max |b| (bits of non-negative doubles, out[0], out[1]).

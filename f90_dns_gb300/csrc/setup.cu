@@ -279,6 +279,29 @@ __global__ void k_tc_anti_image(const double* __restrict__ De, const double* __r
     }
 }
 
+// One thread per (q, folded row): the row's exponent e (smallest with
+// |G[k][j]| < 2^e over the row) and its entries as round(G 2^(58 - e)).
+__global__ void k_fixed_rows(const double* __restrict__ GF, int nq, int he, int ho, long long* __restrict__ GI,
+                             int* __restrict__ GE) {
+    const int nr = he + ho;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nq * nr) return;
+    const int q = (int)(t / nr), r = (int)(t - (long long)q * nr);
+    const bool even = r < he;
+    const int n = even ? he : ho, k = even ? r : r - he;
+    const size_t src = (size_t)q * ((size_t)he * he + (size_t)ho * ho) + (even ? 0 : (size_t)he * he);
+    const size_t dst = (size_t)q * fx_qstride(he, ho) + (even ? 0 : (size_t)he * he);
+    unsigned long long mx = 0;
+    for (int j = 0; j < n; ++j) {
+        const unsigned long long ab = (unsigned long long)__double_as_longlong(GF[src + (size_t)j * n + k]) &
+                                      0x7FFFFFFFFFFFFFFFULL;
+        mx = ab > mx ? ab : mx;
+    }
+    const int e = tc_exponent(mx);
+    GE[t] = e;
+    for (int j = 0; j < n; ++j) GI[dst + (size_t)j * n + k] = tc_fixed_bits<58>(GF[src + (size_t)j * n + k], e);
+}
+
 }  // namespace
 
 cudaError_t build_tc_anti_image(const GridDev& g, const double* De, const double* Do, __half* image, int* rowexp,
@@ -352,6 +375,14 @@ cudaError_t build_inverses(const GridDev& g, const double* S, const double* wh, 
     if ((e = cudaFuncSetAttribute(k_build_pinned, cudaFuncAttributeMaxDynamicSharedMemorySize, limit))) return e;
     k_build_inverses_folded<<<2 * nq, 256, sm_f, s>>>(nz, S, wh, helm_f, ksq, nq, HinvF, PinvF, info);
     k_build_pinned<<<1, 256, sm_p, s>>>(nz, S, PpinT, info);
+    return cudaGetLastError();
+}
+
+cudaError_t build_fixed_rows(const GridDev& g, const double* PinvF, int nq, long long* PinvI, int* PinvE,
+                             cudaStream_t s) {
+    const int ho = g.nz / 2, he = g.nz - ho;
+    const long long n = (long long)nq * (he + ho);
+    k_fixed_rows<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(PinvF, nq, he, ho, PinvI, PinvE);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,7 @@
 #include "cvt.cuh"
 
 #include <algorithm>
+#include <climits>
 
 namespace dns3d {
 namespace {
@@ -1467,50 +1468,203 @@ __device__ __forceinline__ void pressure_body(GridDev g, Ops ops, StepParams sp,
     }
 }
 
+// The per-mode Poisson inverses applied on the integer pipes.  The folded
+// rows are stored in 58-bit fixed point (Ops::PinvI: round(G[k][j]
+// 2^(58 - e_k)), row exponents e_k), each mode column of the right-hand side
+// in 53-bit fixed point before its even/odd fold (B = round(b 2^(54 - f_c)),
+// one power of two 2^(f_c - 1) >= its largest |re|, |im|, so the exact integer
+// fold stays within 2^54), and each row's products are summed exactly and
+// rounded once: x_k = S 2^(e_k + f_c - 112), within 2^-55 of the product of
+// the row and column scales.  The exact products are 32-bit multiply-adds
+// into 64-bit partial sums: A = a1 2^29 + a0, B = b1 2^27 + b0 (a0 in
+// [0, 2^29), b0 in [0, 2^27)), four limb products below 2^56 each, so the
+// partial sums of up to 65 terms stay below 2^63 and are combined in 128 bits
+// once per output.  GB300's integer multiply-add rate is several times its
+// FP64 FMA rate.
+struct FxAcc {
+    long long p00, p01, p10, p11;  // weights 2^0, 2^27, 2^29, 2^56
+};
+
+__device__ __forceinline__ void fx_mad(long long& acc, int a, int b) {  // acc += a b, one 32 x 32 + 64 multiply-add
+    asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(acc) : "r"(a), "r"(b));
+}
+
+__device__ __forceinline__ void fx_mac(FxAcc& acc, int a0, int a1, int b0, int b1) {
+    fx_mad(acc.p00, a0, b0);
+    fx_mad(acc.p01, a0, b1);
+    fx_mad(acc.p10, a1, b0);
+    fx_mad(acc.p11, a1, b1);
+}
+
+__device__ __forceinline__ double fx_row_value(const FxAcc& acc, int e2) {
+    const unsigned __int128 u = (unsigned __int128)(__int128)acc.p00 + ((unsigned __int128)(__int128)acc.p01 << 27) +
+                                ((unsigned __int128)(__int128)acc.p10 << 29) +
+                                ((unsigned __int128)(__int128)acc.p11 << 56) + ((unsigned __int128)1 << 55);
+    const long long T = (long long)((__int128)u >> 56);  // |S| < 2^119: |T| < 2^63
+    return i2d_scaled(T, e2 + 56);
+}
+
+// A folded column value (|U| <= 2^54) as the limbs (b0, b1) of its re and im
+// parts: int4 {re b0, re b1, im b0, im b1}.
+__device__ __forceinline__ int4 fx_limbs(long long re, long long im) {
+    return make_int4((int)(re & 0x7FFFFFF), (int)(re >> 27), (int)(im & 0x7FFFFFF), (int)(im >> 27));
+}
+
+// Modes per CTA of the solve: their fixed-point inverses are staged in shared
+// memory (at most 64 KB of them, at least one mode), and one thread takes one
+// folded row of one mode (at most 512 rows).
+__host__ __device__ inline int fx_solve_modes(int nz) {
+    const int ho = nz / 2, he = nz - ho;
+    int t = (int)(65536 / (fx_qstride(he, ho) * sizeof(long long)));
+    if (t * nz > 512) t = 512 / nz;
+    return t < 1 ? 1 : t;
+}
+__host__ __device__ inline int fx_solve_threads(int nz) { return (nz * fx_solve_modes(nz) + 31) / 32 * 32; }
+__host__ __device__ inline size_t fx_solve_smem(int nz) {
+    const int ho = nz / 2, he = nz - ho, tc = fx_solve_modes(nz);
+    return (size_t)tc * fx_qstride(he, ho) * sizeof(long long) + (2 * (size_t)nz * tc + nz) * sizeof(double2) +
+           (size_t)tc * sizeof(int);
+}
+
 // The Poisson solve of pressure_body for a right-hand side already in PHI
-// (unfolded, as pressure_body forms it): fold, apply the per-mode inverses
-// (the pinned mode (0,0) unfolded), write phi over it.  A CTA reads its tile
-// whole before it writes, so the solve is in place.
+// (unfolded, as pressure_body forms it), fx_solve_modes(nz) modes from
+// bx tc: the modes' fixed-point inverses are copied into shared memory with
+// cp.async (16-byte pieces, all in flight at once) while the CTA stages the
+// unfolded columns, takes each column's power of two and folds it in fixed
+// point; then each thread applies one folded row (above; the pinned mode
+// (0,0) unfolded, with its FP64 inverse), and the results are unfolded over
+// the right-hand side.  A CTA reads its tile whole before it writes, so the
+// solve is in place.  A column with a non-finite entry gets NaN throughout.
 __device__ __forceinline__ void pressure_solve_body(const GridDev& g, const Ops& ops, double2* __restrict__ PHI,
-                                                    int tc, int bx) {
-    extern __shared__ double2 sm[];
+                                                    int bx) {
+    extern __shared__ __align__(16) unsigned char smc[];
     const int nz = g.nz, he = ops.he, ho = ops.ho;
-    const int tsz = nz * tc;
-    double2* tb = sm + tsz;        // folded rhs tile (the layout of pressure_body)
-    double2* bpin = sm + 2 * tsz;  // unfolded rhs of mode (0,0)
+    const int tc = fx_solve_modes(nz), tsz = nz * tc;
+    const size_t qs = fx_qstride(he, ho);
+    long long* sG = reinterpret_cast<long long*>(smc);                  // inverses of the tile's modes [tc][qs]
+    double2* su = reinterpret_cast<double2*>(sG + (size_t)tc * qs);   // unfolded columns [nz][tc], then results
+    int4* tb = reinterpret_cast<int4*>(su + tsz);                      // folded columns in fixed point (limbs)
+    double2* bpin = su + 2 * tsz;                                      // unfolded rhs of mode (0,0)
+    int* sF = reinterpret_cast<int*>(bpin + nz);                       // column exponents
     const int m0 = bx * tc;
-    fold_load(tb, PHI, g, m0, tc, he, ho);
-    if (m0 == 0)
-        for (int z = threadIdx.x; z < nz; z += blockDim.x) bpin[z] = PHI[(size_t)z * g.nm];
+    {
+        const int n16 = (int)(qs / 2);  // 16-byte pieces per mode
+        for (int c = 0; c < tc; ++c) {
+            const int m = m0 + c;
+            if (m >= g.nm || m == 0) continue;
+            const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
+            const long long* src = ops.PinvI + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * qs;
+            long long* dst = sG + (size_t)c * qs;
+            for (int i = threadIdx.x; i < n16; i += blockDim.x) cp_async16(dst + 2 * i, src + 2 * i);
+        }
+        cp_async_commit();
+    }
+    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
+        const int z = t / tc, c = t - z * tc;
+        const int m = m0 + c;
+        const double2 v = m < g.nm ? PHI[(size_t)z * g.nm + m] : make_double2(0.0, 0.0);
+        su[t] = v;
+        if (m == 0) bpin[z] = v;
+    }
     __syncthreads();
-    const size_t qstride = (size_t)he * he + (size_t)ho * ho;
+    {  // one warp per column: the power of two of its largest |re|, |im|
+        const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+        for (int c = w; c < tc; c += blockDim.x >> 5) {
+            unsigned long long mx = 0;
+            for (int z = l; z < nz; z += 32) {
+                const double2 v = su[z * tc + c];
+                const unsigned long long ax = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFULL;
+                const unsigned long long ay = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFULL;
+                mx = ax > mx ? ax : mx;
+                mx = ay > mx ? ay : mx;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
+                mx = v > mx ? v : mx;
+            }
+            if (l == 0) sF[c] = mx >= 0x7FF0000000000000ULL ? INT_MIN : tc_exponent(mx) + 1;
+        }
+    }
+    __syncthreads();
+    // fold in fixed point: even rows k < he (pair sums), odd rows he + k (differences)
     for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
-        const int c = t / he, k = t - c * he;
+        const int k = t / tc, c = t - k * tc;
+        const int f = sF[c];
+        if (f == INT_MIN) continue;  // not read
+        const double2 a = su[k * tc + c];
+        const long long ax = tc_fixed(a.x, f), ay = tc_fixed(a.y, f);
+        if (k < ho) {
+            const double2 b = su[(nz - 1 - k) * tc + c];
+            const long long bx2 = tc_fixed(b.x, f), by = tc_fixed(b.y, f);
+            tb[k * tc + c] = fx_limbs(ax + bx2, ay + by);
+            tb[(he + k) * tc + c] = fx_limbs(ax - bx2, ay - by);
+        } else {
+            tb[k * tc + c] = fx_limbs(ax, ay);
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();  // the folded tile and every thread's operator pieces
+    // one folded row r of one column per thread (rows of a column on adjacent lanes)
+    for (int t = threadIdx.x; t < tsz; t += blockDim.x) {
+        const int c = t / nz, r = t - c * nz;
         const int m = m0 + c;
         if (m >= g.nm) continue;
-        Pair x;
-        if (m == 0) {
-            double2 a = make_double2(0.0, 0.0), b = a;
+        if (m == 0) {  // the pinned mode: output level r, unfolded, FP64
+            double2 a = make_double2(0.0, 0.0);
             for (int zp = 0; zp < nz; ++zp) {
                 const double2 bb = bpin[zp];
-                const double h1 = __ldg(&ops.PpinT[(size_t)zp * nz + k]);
-                const double h2 = __ldg(&ops.PpinT[(size_t)zp * nz + nz - 1 - k]);
-                a.x = fma(h1, bb.x, a.x); a.y = fma(h1, bb.y, a.y);
-                b.x = fma(h2, bb.x, b.x); b.y = fma(h2, bb.y, b.y);
+                const double h1 = __ldg(&ops.PpinT[(size_t)zp * nz + r]);
+                a.x = fma(h1, bb.x, a.x);
+                a.y = fma(h1, bb.y, a.y);
             }
-            x.a = a;
-            x.b = b;
+            PHI[(size_t)r * g.nm] = a;
+            continue;
+        }
+        const int f = sF[c];
+        double2 x;
+        if (f == INT_MIN) {
+            x.x = x.y = __longlong_as_double(0x7FF8000000000000LL);
         } else {
             const int ky = m / g.nxhp, kx = m - ky * g.nxhp;
-            x = inv_apply(ops.PinvF + (size_t)mode_q(ky, kx, g.ny, g.nxhp) * qstride, tb, k, c, tc, he, ho);
+            const size_t q = (size_t)mode_q(ky, kx, g.ny, g.nxhp);
+            const bool even = r < he;
+            const int n = even ? he : ho, k = even ? r : r - he;
+            const long long* G = sG + (size_t)c * qs + (even ? 0 : (size_t)he * he) + k;
+            const int4* bcol = tb + (even ? 0 : he * tc) + c;
+            FxAcc sx{}, sy{};
+#pragma unroll 4
+            for (int j = 0; j < n; ++j, G += n, bcol += tc) {
+                const long long a = *G;
+                const int a0 = (int)(a & 0x1FFFFFFF), a1 = (int)(a >> 29);
+                const int4 b = *bcol;
+                fx_mac(sx, a0, a1, b.x, b.y);
+                fx_mac(sy, a0, a1, b.z, b.w);
+            }
+            const int e2 = __ldg(&ops.PinvE[q * nz + r]) + f - 112;
+            x = make_double2(fx_row_value(sx, e2), fx_row_value(sy, e2));
         }
-        PHI[(size_t)k * g.nm + m] = x.a;
-        if (k < ho) PHI[(size_t)(nz - 1 - k) * g.nm + m] = x.b;
+        su[r * tc + c] = x;  // su's column c was last read by the fold, before the barrier
+    }
+    __syncthreads();
+    // unfold: phi_k = pe_k + po_k, phi_nz-1-k = pe_k - po_k
+    for (int t = threadIdx.x; t < he * tc; t += blockDim.x) {
+        const int k = t / tc, c = t - k * tc;
+        const int m = m0 + c;
+        if (m >= g.nm || m == 0) continue;
+        const double2 pe = su[k * tc + c];
+        if (k < ho) {
+            const double2 po = su[(he + k) * tc + c];
+            PHI[(size_t)k * g.nm + m] = make_double2(pe.x + po.x, pe.y + po.y);
+            PHI[(size_t)(nz - 1 - k) * g.nm + m] = make_double2(pe.x - po.x, pe.y - po.y);
+        } else {
+            PHI[(size_t)k * g.nm + m] = pe;
+        }
     }
 }
 
-__global__ void __launch_bounds__(256) k_pressure_solve(GridDev g, Ops ops, double2* __restrict__ PHI, int tc) {
-    pressure_solve_body(g, ops, PHI, tc, blockIdx.x);
+__global__ void __launch_bounds__(512) k_pressure_solve(GridDev g, Ops ops, double2* __restrict__ PHI) {
+    pressure_solve_body(g, ops, PHI, blockIdx.x);
 }
 
 // The divergence right-hand side of pressure_body (strong form) from D1.w*,
@@ -2982,13 +3136,13 @@ cudaError_t launch_vorticity_tc(const GridDev& g, const Ops& ops, const double2*
 
 cudaError_t launch_pressure_tc(const GridDev& g, const Ops& ops, const StepParams& sp, const double2* US,
                                const double2* VS, const double2* WS, double2* PHI, int* err, cudaStream_t s) {
-    if (sp.weak_form) return cudaErrorInvalidValue;  // the weak form's operator has no digit image
+    // the weak form's operator has no digit image; the solve needs the fixed-point inverses
+    if (sp.weak_form || !ops.PinvI) return cudaErrorInvalidValue;
     const PresRhsTcOp op{sp, US, VS, WS, PHI};
     cudaError_t e = launch_dz_tc(g, ops, op, err, s);
     if (e) return e;
-    const int tc = tile_width(g, kTilePres);
-    const size_t sm = (2 * (size_t)g.nz * tc + g.nz) * sizeof(double2);
-    k_pressure_solve<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, ops, PHI, tc);
+    const int tc = fx_solve_modes(g.nz);
+    k_pressure_solve<<<(g.nm + tc - 1) / tc, fx_solve_threads(g.nz), fx_solve_smem(g.nz), s>>>(g, ops, PHI);
     return cudaGetLastError();
 }
 
@@ -3276,9 +3430,9 @@ struct RsPres64 {
 
 // the Poisson solve of a right-hand side RsPresRhs left in PHI
 struct RsPres64Tc {
-    static constexpr int kMinCtas = 4;
+    static constexpr int kMinCtas = 3;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
-        pressure_solve_body(d.g, d.ops, d.PHI, d.g.tc[kTilePres], b);
+        pressure_solve_body(d.g, d.ops, d.PHI, b);
     }
 };
 
@@ -3409,7 +3563,9 @@ int ragged_blocks(int stage, bool mixed, const RunDesc& d) {
         case kRsVisc:
             if (!mixed && (ragged_variant(d) & kRvViscTc)) return (d.ops.nq + d.gx[kRsVisc] - 1) / d.gx[kRsVisc];
             return tiles;
-        case kRsPres: return tiles;
+        case kRsPres:
+            if (!mixed && (ragged_variant(d) & kRvPresTc)) return (g.nm + fx_solve_modes(g.nz) - 1) / fx_solve_modes(g.nz);
+            return tiles;
         case kRsPresRhs:
             if (!mixed && (ragged_variant(d) & kRvPresTc))
                 return ((g.nm + kTcCorrModes - 1) / kTcCorrModes + d.corr_chunk - 1) / d.corr_chunk;
@@ -3436,7 +3592,9 @@ size_t ragged_smem(int stage, bool mixed, const RunDesc& d) {
         case kRsVisc:
             if (!mixed && (ragged_variant(d) & kRvViscTc)) return viscous_tc_smem(g);
             return mixed ? viscous_mixed_smem(g, tc) : 6 * nz * tc * sizeof(double2);
-        case kRsPres: return mixed ? pressure_mixed_smem(g, tc) : (2 * nz * tc + nz) * sizeof(double2);
+        case kRsPres:
+            if (mixed) return pressure_mixed_smem(g, tc);
+            return (ragged_variant(d) & kRvPresTc) ? fx_solve_smem(g.nz) : (2 * nz * tc + nz) * sizeof(double2);
         case kRsPresRhs: return (!mixed && (ragged_variant(d) & kRvPresTc)) ? vorticity_tc_smem(g) : 0;
         case kRsCorr:
             if (!mixed && (ragged_variant(d) & kRvCorrTc)) return vorticity_tc_smem(g);

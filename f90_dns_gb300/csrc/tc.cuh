@@ -98,6 +98,13 @@ __host__ __device__ inline int tc_k_row(const TcGeom& t, int kk) {
     return kk < t.ke ? (kk < t.he ? kk : -1) : (kk - t.ke < t.ho ? t.e8 + (kk - t.ke) : -1);
 }
 
+// Entries per q of the fixed-point Poisson inverses (folded blocks he x he
+// and ho x ho), padded to an even count so that every q's block starts on a
+// 16-byte boundary (the solve stages them with 16-byte copies).
+__host__ __device__ inline size_t fx_qstride(int he, int ho) {
+    return ((size_t)he * he + (size_t)ho * ho + 1) / 2 * 2;
+}
+
 // Halves per q of the compact slice store: per digit, the nonzero core
 // matrices (even block row-major, then odd block), 64 halves each.
 __host__ __device__ inline size_t tc_q_halves(const TcGeom& t) {
@@ -150,8 +157,10 @@ __device__ __forceinline__ void tc_digit_pairs(long long u0, long long u1, __hal
     }
 }
 
-// round(x 2^(54-f)) for |x| < 2^f, from the bits of x (integer operations only).
-__device__ __forceinline__ long long tc_fixed(double x, int f) {
+// round(x 2^(B-f)) for |x| < 2^f (|result| <= 2^B), from the bits of x
+// (integer operations only).
+template <int B>
+__device__ __forceinline__ long long tc_fixed_bits(double x, int f) {
     const long long b = __double_as_longlong(x);
     int ex = (int)((b >> 52) & 0x7FF);
     long long m = b & 0xFFFFFFFFFFFFFLL;
@@ -161,11 +170,14 @@ __device__ __forceinline__ long long tc_fixed(double x, int f) {
     } else {
         m |= 1LL << 52;
     }
-    const int sh = 1075 - kTcFixBits + f - ex;  // x = m 2^(ex-1075); U = m 2^(ex-1075+54-f)
+    const int sh = 1075 - B + f - ex;  // x = m 2^(ex-1075); U = m 2^(ex-1075+B-f)
     if (sh >= 62) return 0;
     const long long u = sh > 0 ? (m + (1LL << (sh - 1))) >> sh : m << (-sh);
     return b < 0 ? -u : u;
 }
+
+// round(x 2^(54-f)) for |x| < 2^f: the digit scheme's fixed point.
+__device__ __forceinline__ long long tc_fixed(double x, int f) { return tc_fixed_bits<kTcFixBits>(x, f); }
 
 // Smallest f with |x| < 2^f for the largest |x| given by its bits (0 if zero).
 __device__ __forceinline__ int tc_exponent(unsigned long long absbits) {
