@@ -37,7 +37,7 @@ WORKLOAD = "channel_128x128x65_re180_pi"
 # capture of that kernel on the same workload and build; --traffic overrides.
 NCU_TRAFFIC = {
     ("channel_128x128x65_re180_pi", "viscous_helmholtz"): 154.447104e6 + 16.572160e6,
-    ("channel_128x128x65_re180_pi", "viscous_helmholtz_tc"): 257.247488e6 + 18.365696e6,
+    ("channel_128x128x65_re180_pi", "viscous_helmholtz_tc"): 256.986624e6 + 17.730560e6,
 }
 
 
@@ -298,7 +298,7 @@ def run_reference(args) -> None:
 # per-launch DRAM traffic (ncu dram__bytes_read.sum + dram__bytes_write.sum)
 # and tensor-pipe activity of the tensor-core kernels, from one capture each
 NCU_TENSOR_PIPE = {
-    ("channel_128x128x65_re180_pi", "viscous_helmholtz_tc"): 9.1,
+    ("channel_128x128x65_re180_pi", "viscous_helmholtz_tc"): 11.3,
 }
 
 
@@ -384,14 +384,12 @@ def large_leg(args, device: int, peaks: dict) -> dict:
     return out
 
 
-def serving_leg(args, device: int) -> dict:
-    """Serving stream: Poisson arrivals (mean `serve_rate` runs/s, seeded) of
-    runs drawn as in the ensemble, 10% of them 256x256x97, each 200..2000
-    steps, mixed precision, admitted by device footprint under 160 GiB."""
+def serving_requests(args) -> list:
+    """The seeded request stream: Poisson arrivals (mean `serve_rate` runs/s)
+    of runs drawn as in the ensemble, 10% of them 256x256x97, each 200..2000
+    steps."""
     import numpy as np
-    from f90_dns_gb300 import Server, config_from
-    from f90_dns_gb300.capi import PREC_MIXED
-    from f90_dns_gb300.workloads import WORKLOADS, ensemble_draws, point_count
+    from f90_dns_gb300.workloads import WORKLOADS, ensemble_draws
     rng = np.random.default_rng(args.seed + 1)
     draws = ensemble_draws(args.serve_requests, seed=args.seed + 2)
     big = WORKLOADS["channel_256x256x97_re180_dpdx"]
@@ -404,11 +402,22 @@ def serving_leg(args, device: int) -> dict:
                      analytical_mode_x=d["analytical_mode_x"], analytical_mode_y=d["analytical_mode_y"])
         t += float(rng.exponential(1.0 / args.serve_rate))
         reqs.append((t, d, int(rng.integers(200, 2001))))
+    return reqs
+
+
+def serve(args, device: int, reqs: list, burst: bool) -> dict:
+    """Submits `reqs` to a Server (at their arrival times, or all at once for
+    a burst), mixed precision, admitted by device footprint under 160 GiB;
+    latency percentiles and the aggregate point-steps/s over the span."""
+    import numpy as np
+    from f90_dns_gb300 import Server, config_from
+    from f90_dns_gb300.capi import PREC_MIXED
+    from f90_dns_gb300.workloads import point_count
     with Server(max_bytes=160 << 30, steps_per_round=args.serve_round, device=device) as srv:
         t0 = time.perf_counter()
         ids = []
         for at, d, n in reqs:
-            dly = at - (time.perf_counter() - t0)
+            dly = 0.0 if burst else at - (time.perf_counter() - t0)
             if dly > 0:
                 time.sleep(dly)
             ids.append(srv.submit(config_from(d, device=device, precision=PREC_MIXED), n))
@@ -416,13 +425,24 @@ def serving_leg(args, device: int) -> dict:
     lat = np.array([i.latency for i in infos])
     work = sum(point_count(d) * n for (_, d, n) in reqs)
     span = max(i.t_finish for i in infos) - min(i.t_submit for i in infos)
-    return {"requests": len(reqs), "arrival_rate_per_s": args.serve_rate, "seed": args.seed + 1,
-            "large_256x256x97": sum(1 for (_, d, _) in reqs if d["nx"] == 256),
-            "completed": sum(1 for i in infos if i.status == 2),
+    return {"completed": sum(1 for i in infos if i.status == 2),
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-            "aggregate_point_steps_per_s": work / span, "span_s": span,
-            "precision": "mixed", "admission": "device footprint <= 160 GiB, FIFO",
-            "steps_per_round": args.serve_round}
+            "aggregate_point_steps_per_s": work / span, "span_s": span}
+
+
+def serving_leg(args, device: int) -> dict:
+    """Serving: the seeded Poisson stream (latency under the stated arrival
+    rate; its aggregate is bounded by the arrivals), then the same requests
+    submitted at once (the server's capacity: continuous batching with every
+    run resident)."""
+    reqs = serving_requests(args)
+    out = {"requests": len(reqs), "arrival_rate_per_s": args.serve_rate, "seed": args.seed + 1,
+           "large_256x256x97": sum(1 for (_, d, _) in reqs if d["nx"] == 256),
+           "precision": "mixed", "admission": "device footprint <= 160 GiB, FIFO",
+           "steps_per_round": args.serve_round}
+    out.update(serve(args, device, reqs, burst=False))
+    out["burst"] = serve(args, device, reqs, burst=True)
+    return out
 
 
 def run_ours(args) -> None:

@@ -1253,14 +1253,29 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
         const TcGeom t = tc_geom(nz);
         __half* sl = nullptr;
         int* ex = nullptr;
-        if ((rc = dev_alloc(h, &sl, (size_t)nq * tc_q_halves(t))) || (rc = dev_alloc(h, &ex, (size_t)nq * t.m8)))
+        double* tau = nullptr;
+        if ((rc = dev_alloc(h, &sl, (size_t)nq * tc_q_halves(t))) || (rc = dev_alloc(h, &ex, (size_t)nq * t.m8)) ||
+            (rc = dev_alloc(h, &tau, (size_t)2 * t.he)))
             return fail(rc);
-        if ((e = build_tc_slices(g, ops.HinvF, nq, sl, ex, h->stream)) || (e = cudaStreamSynchronize(h->stream))) {
+        std::vector<double> th((size_t)2 * t.he, 0.0);
+        for (int k = 1; k < t.he; ++k) {
+            const double w2 = 2.0 * wh[k];
+            if (k < t.ho) {
+                th[k] = (S0[k] + Sn[k]) / w2;
+                th[t.he + k] = (S0[k] - Sn[k]) / w2;
+            } else {
+                th[k] = S0[k] / w2;  // the unpaired mid level (S0 = Sn there)
+            }
+        }
+        if ((rc = upload(h, tau, th.data(), th.size() * sizeof(double)))) return fail(rc);
+        if ((e = build_tc_slices(g, ops.HinvF, ops.wh, nq, sl, ex, h->stream)) ||
+            (e = cudaStreamSynchronize(h->stream))) {
             cuda_fail(h, e, "build_tc_slices");
             return fail(DNS3D_E_CUDA);
         }
         ops.tcA = sl;
         ops.tcE = ex;
+        ops.tcTau = tau;
         h->visc_tc_forced = tcenv && std::strcmp(tcenv, "1") == 0;
         // without timing: the tensor-core kernel once the grid has a few waves
         // of operator pairs and two of its CTAs fit an SM

@@ -197,9 +197,13 @@ struct Ops {
     const int* PinvE;
     int nq;
     // tensor-core form of HinvF (tc.cuh), or null: FP16 digit slices
-    // [nq][tc_q_halves] and row exponents [nq][m8]
+    // [nq][tc_q_halves] of 2 G[i][j] w_j and row exponents [nq][m8] (rows i
+    // of both blocks share one); tcTau [2][he]: the lifting coefficients of
+    // the weight-free folded right-hand sides, (S0_k + Sn_k) / (2 w_k) and
+    // (S0_k - Sn_k) / (2 w_k) (the unpaired mid level: S0 / (2 w))
     const __half* tcA;
     const int* tcE;
+    const double* tcTau;
     // tensor-core digit image of the folded D1 ([[0, De], [Do, 0]]), or null
     const __half* tcD;
     const int* tcDE;
@@ -383,10 +387,12 @@ cudaError_t launch_poisson_residual(const GridDev& g, const Ops& ops, const Step
                                     unsigned long long* out, cudaStream_t s);
 
 // Digit slices (FP16) and row exponents of the folded per-mode inverses invF
-// ([nq][he*he + ho*ho], the layout of Ops::HinvF) for the tensor-core solve
-// (tc.cuh); slices [nq][tc_q_halves], rowexp [nq][m8].
-cudaError_t build_tc_slices(const GridDev& g, const double* invF, int nq, __half* slices, int* rowexp,
-                            cudaStream_t s);
+// ([nq][he*he + ho*ho], the layout of Ops::HinvF) with their columns scaled
+// by 2 wfold[j] (the folded weights, device [he]) for the tensor-core solve
+// (tc.cuh); slices [nq][tc_q_halves], rowexp [nq][m8], rows i of both blocks
+// sharing one exponent.
+cudaError_t build_tc_slices(const GridDev& g, const double* invF, const double* wfold, int nq, __half* slices,
+                            int* rowexp, cudaStream_t s);
 
 // Digit image ([kTcSlices][block E, block O] FP16, tc_blocks(t, true); rowexp
 // [m8]) of the folded z-derivative [[0, De], [Do, 0]] for the tensor-core

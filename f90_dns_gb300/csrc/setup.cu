@@ -203,10 +203,15 @@ __global__ void __launch_bounds__(256) k_fma_probe(double* out, int iters, doubl
 
 // Digit slices of the folded inverses for the tensor-core solve (tc.cuh):
 // one thread per (q, row of the block-diagonal operator).  Row i of the even
-// block is Ge[i][:] = GeT[:][i]; rows and columns past a block's size stay
-// zero, so the padded core matrices contribute nothing.
-__global__ void k_tc_slices(const double* __restrict__ invF, int nq, int nz, __half* __restrict__ slices,
-                            int* __restrict__ rowexp) {
+// block is Ge[i][:] = GeT[:][i], entered with its columns scaled by 2 w_j
+// (G'[i][j] = 2 w_j G[i][j], w the folded quadrature weights: the kernel's
+// right-hand sides are the weight-free halves of the folded ones).  Rows i of
+// the even and the odd block share one exponent (the larger of the two rows'
+// scales), so that the kernel can form x_i = xe_i + xo_i and x_nz-1-i =
+// xe_i - xo_i exactly in integers.  Rows and columns past a block's size
+// stay zero, so the padded core matrices contribute nothing.
+__global__ void k_tc_slices(const double* __restrict__ invF, const double* __restrict__ wfold, int nq, int nz,
+                            __half* __restrict__ slices, int* __restrict__ rowexp) {
     const TcGeom t = tc_geom(nz);
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= (long long)nq * t.m8) return;
@@ -216,7 +221,9 @@ __global__ void k_tc_slices(const double* __restrict__ invF, int nq, int nz, __h
     const int n = even ? t.he : t.ho;
     const int w8 = even ? t.e8 : t.o8;
     const size_t qs = (size_t)t.he * t.he + (size_t)t.ho * t.ho;
-    const double* GT = invF + (size_t)q * qs + (even ? 0 : (size_t)t.he * t.he);
+    const double* GeT = invF + (size_t)q * qs;
+    const double* GoT = GeT + (size_t)t.he * t.he;
+    const double* GT = even ? GeT : GoT;
     __half* S = slices + (size_t)q * tc_q_halves(t);
     const int ncore = t.ncore_e + t.ncore_o;
     const int cbase = even ? 0 : t.ncore_e;
@@ -224,18 +231,22 @@ __global__ void k_tc_slices(const double* __restrict__ invF, int nq, int nz, __h
     int e = 0;
     if (i < n) {
         unsigned long long mx = 0;
-        for (int j = 0; j < n; ++j) {
-            const unsigned long long ab = (unsigned long long)__double_as_longlong(GT[(size_t)j * n + i]) &
-                                          0x7FFFFFFFFFFFFFFFULL;
-            mx = ab > mx ? ab : mx;
-        }
+        auto scan = [&](const double* G, int len) {
+            for (int j = 0; j < len; ++j) {
+                const double v = 2.0 * wfold[j] * G[(size_t)j * len + i];
+                const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+                mx = ab > mx ? ab : mx;
+            }
+        };
+        scan(GeT, t.he);
+        if (i < t.ho) scan(GoT, t.ho);
         e = tc_exponent(mx);
     }
     rowexp[(size_t)q * t.m8 + m] = e;
     for (int j = 0; j < w8; ++j) {
         int c[kTcSlices];
         for (int s = 0; s < kTcSlices; ++s) c[s] = 0;
-        if (i < n && j < n) tc_digits(tc_fixed(GT[(size_t)j * n + i], e), c);
+        if (i < n && j < n) tc_digits(tc_fixed(2.0 * wfold[j] * GT[(size_t)j * n + i], e), c);
         const int core = cbase + (i / 8) * nb + (j / 8);
         const int off = (i % 8) * 8 + (j % 8);
         for (int s = 0; s < kTcSlices; ++s) S[((size_t)s * ncore + core) * 64 + off] = __int2half_rn(c[s]);
@@ -311,11 +322,11 @@ cudaError_t build_tc_anti_image(const GridDev& g, const double* De, const double
     return cudaGetLastError();
 }
 
-cudaError_t build_tc_slices(const GridDev& g, const double* invF, int nq, __half* slices, int* rowexp,
-                            cudaStream_t s) {
+cudaError_t build_tc_slices(const GridDev& g, const double* invF, const double* wfold, int nq, __half* slices,
+                            int* rowexp, cudaStream_t s) {
     const TcGeom t = tc_geom(g.nz);
     const long long n = (long long)nq * t.m8;
-    k_tc_slices<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(invF, nq, g.nz, slices, rowexp);
+    k_tc_slices<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(invF, wfold, nq, g.nz, slices, rowexp);
     return cudaGetLastError();
 }
 

@@ -339,17 +339,20 @@ __device__ __forceinline__ double2 viscous_rhs_cn(const GridDev& g, const Ops& o
                         whz * (2.0 * f.y + sp.dt * s.y) - (s0 * l1.y + sn * ln.y));
 }
 
-// viscous_rhs_cn folded at the level pair (k, nz-1-k), k >= 1: with the
-// symmetric weights (w_k = w_nz-1-k) and lifting columns (S0_nz-1-k =
-// Sn_k), r_k + r_k' = 2 w_k (a_k + a_k') - (S0_k + Sn_k)(l1 + ln) and
-// r_k - r_k' = 2 w_k (a_k - a_k') - (S0_k - Sn_k)(l1 - ln), with
-// a = f + (dt/2) s and the lifting data l1 = f_1 + 2 bc1, ln = f_nz + 2 bc2;
-// the unpaired mid level (nz odd) gets r_k itself.  A third fewer FP64
-// operations than two viscous_rhs_cn calls and their sum and difference.
-__device__ __forceinline__ Pair viscous_rhs_cn_folded(const GridDev& g, const Ops& ops, const StepParams& sp,
-                                                      int comp, int k, int m, int ky, int kx, double2 f1v,
-                                                      double2 f2v, double2 s1, double2 s2, double2 l1, double2 ln,
-                                                      double dpdx) {
+// viscous_rhs_cn folded at the level pair (k, nz-1-k), k >= 1, with the
+// weights taken out (the tensor-core operator carries 2 w_j G[i][j]): with
+// the symmetric weights (w_k = w_nz-1-k) and lifting columns (S0_nz-1-k =
+// Sn_k), (r_k + r_k') / (2 w_k) = (a_k + a_k') - tau+_k (l1 + ln) and
+// (r_k - r_k') / (2 w_k) = (a_k - a_k') - tau-_k (l1 - ln), with
+// a = f + (dt/2) s, the lifting data l1 = f_1 + 2 bc1, ln = f_nz + 2 bc2 and
+// tau+-_k = (S0_k +- Sn_k) / (2 w_k) (Ops::tcTau); the unpaired mid level
+// (nz odd) gets r_k / (2 w_k) = a_k - (S0_k / 2 w_k)(l1 + ln).  Five FP64
+// operations per value instead of the 14 of two viscous_rhs_cn calls and
+// their sum and difference.
+__device__ __forceinline__ Pair viscous_rhs_cn_half(const GridDev& g, const Ops& ops, const StepParams& sp,
+                                                    int comp, int k, int m, int ky, int kx, double2 f1v,
+                                                    double2 f2v, double2 s1, double2 s2, double2 l1, double2 ln,
+                                                    double dpdx) {
     if (sp.dealias) {  // apply_dealias_truncation (3D:1163-1193)
         const int kyi = ky <= g.ny / 2 ? ky : g.ny - ky;
         if (kx > sp.kx_max || kyi > sp.ky_max) s1 = s2 = make_double2(0.0, 0.0);
@@ -359,19 +362,19 @@ __device__ __forceinline__ Pair viscous_rhs_cn_folded(const GridDev& g, const Op
         s2.x += dpdx * sp.forcing_scale;
     }
     const double hdt = 0.5 * sp.dt;
-    const double tw = 2.0 * __ldg(&ops.wh[k]);
-    const double s0 = __ldg(&ops.S0[k]), sn = __ldg(&ops.Sn[k]);
+    const int he = g.nz - g.nz / 2;
+    const double tp = __ldg(&ops.tcTau[k]);
     const double2 a1 = make_double2(fma(hdt, s1.x, f1v.x), fma(hdt, s1.y, f1v.y));
+    const double2 lp = make_double2(l1.x + ln.x, l1.y + ln.y);
     Pair r;
     if (k < g.nz / 2) {
+        const double tm = __ldg(&ops.tcTau[he + k]);
         const double2 a2 = make_double2(fma(hdt, s2.x, f2v.x), fma(hdt, s2.y, f2v.y));
-        const double sp_ = s0 + sn, sm_ = s0 - sn;
-        r.a = make_double2(fma(tw, a1.x + a2.x, -(sp_ * (l1.x + ln.x))),
-                           fma(tw, a1.y + a2.y, -(sp_ * (l1.y + ln.y))));
-        r.b = make_double2(fma(tw, a1.x - a2.x, -(sm_ * (l1.x - ln.x))),
-                           fma(tw, a1.y - a2.y, -(sm_ * (l1.y - ln.y))));
+        const double2 lm = make_double2(l1.x - ln.x, l1.y - ln.y);
+        r.a = make_double2(fma(-tp, lp.x, a1.x + a2.x), fma(-tp, lp.y, a1.y + a2.y));
+        r.b = make_double2(fma(-tm, lm.x, a1.x - a2.x), fma(-tm, lm.y, a1.y - a2.y));
     } else {
-        r.a = make_double2(fma(tw, a1.x, -(s0 * l1.x + sn * ln.x)), fma(tw, a1.y, -(s0 * l1.y + sn * ln.y)));
+        r.a = make_double2(fma(-tp, lp.x, a1.x), fma(-tp, lp.y, a1.y));
         r.b = make_double2(0.0, 0.0);
     }
     return r;
@@ -560,14 +563,42 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //  (f) every row's 8 class accumulators are combined in 64-bit integers and
 //      scaled to FP64;
 //  (g) the outputs F* = x - f are written (wall values at the walls).
+// (t - round(f 2^-E)) 2^E: an integer result t at the scale 2^E minus an
+// FP64 value f, exactly in integers but for the rounding of f to that scale
+// and of the final conversion; falls back to the FP64 difference where f is
+// non-finite, far above the scale (f 2^-E >= 2^62) or the integer difference
+// would overflow.
+__device__ __forceinline__ double tc_sub_scaled(long long t, double f, int E) {
+    const long long b = __double_as_longlong(f);
+    int ex = (int)((b >> 52) & 0x7FF);
+    if (ex == 0x7FF) return i2d_scaled(t, E) - f;
+    long long m = b & 0xFFFFFFFFFFFFFLL;
+    if (ex == 0) {
+        if (m == 0) return i2d_scaled(t, E);
+        ex = 1;  // subnormal: no implicit bit
+    } else {
+        m |= 1LL << 52;
+    }
+    const int sh = 1075 + E - ex;  // f 2^-E = m 2^-sh
+    long long F;
+    if (sh >= 63) F = 0;  // |f 2^-E| < 2^-10
+    else if (sh > 0) F = (m + (1LL << (sh - 1))) >> sh;
+    else if (sh >= -9) F = m << (-sh);
+    else return i2d_scaled(t, E) - f;
+    if (b < 0) F = -F;
+    const long long d = (long long)((unsigned long long)t - (unsigned long long)F);
+    if (((t ^ F) & (t ^ d)) < 0) return i2d_scaled(t, E) - f;  // overflow
+    return i2d_scaled(d, E);
+}
+
 // Combination of one warp's TMEM lanes for 6 right-hand-side columns (H = 0:
 // columns 0 .. 5, H = 1: 6 .. 11): the 8 weight-class accumulators of each
-// column loaded back to back under one wait, combined in 64-bit integers
-// (tc_combine8), scaled to FP64 and stored to sR at the lane's row.  The two
-// warps of a lane quadrant take one half each.
+// column loaded back to back under one wait and combined in 64-bit integers
+// (tc_combine8), stored to sR at the lane's row as the integer T (its bits in
+// the FP64 slot; the outputs' scale 2^(e + f - 52) is applied in (g)).  The
+// two warps of a lane quadrant take one half each.
 template <int H>
-__device__ __noinline__ void tc_combine6(uint32_t lanes, double* sR, int m8, int row, bool valid, int e,
-                                         const int* sF) {
+__device__ __noinline__ void tc_combine6(uint32_t lanes, double* sR, int m8, int row, bool valid) {
     uint32_t r[kTcClasses * 6];
 #pragma unroll
     for (int c = 0; c < kTcClasses; ++c) {
@@ -586,7 +617,7 @@ __device__ __noinline__ void tc_combine6(uint32_t lanes, double* sR, int m8, int
         for (int j = 0; j < 6; ++j) {
             const long long T = tc_combine8(r[j], r[6 + j], r[12 + j], r[18 + j], r[24 + j], r[30 + j], r[36 + j],
                                             r[42 + j]);
-            sR[(6 * H + j) * m8 + row] = i2d_scaled(T, e + sF[6 * H + j] - 52);
+            sR[(6 * H + j) * m8 + row] = __longlong_as_double(T);  // the integer result, its bits
         }
     }
 }
@@ -751,7 +782,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                     const double2 s1 = sc[(size_t)k * st];
                     const double2 s2 = k < ho ? sc[(size_t)(nz - 1 - k) * st] : s1;
                     const Pair rf =
-                        viscous_rhs_cn_folded(g, ops, sp, comp, k, m, ky, kx, v1, v2, s1, s2, l1, ln, dpdx);
+                        viscous_rhs_cn_half(g, ops, sp, comp, k, m, ky, kx, v1, v2, s1, s2, l1, ln, dpdx);
                     fe = rf.a;
                     fo = rf.b;
                 }
@@ -870,22 +901,25 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                     const int blk = (hasE && hasO) ? half : (hasO ? 1 : 0);
                     const bool valid = blk ? (lane >= 64 && lane - 64 < t.o8) : lane < t.e8;
                     const int row = blk ? t.e8 + (lane - 64) : lane;
-                    const int e = valid ? __ldg(&ops.tcE[(size_t)q * m8 + row]) : 0;
                     const uint32_t lb = lanes + (uint32_t)(blk * kTcDCols);
                     if (hasE && hasO) {
-                        tc_combine6<0>(lb, sR, m8, row, valid, e, sF);
-                        tc_combine6<1>(lb, sR, m8, row, valid, e, sF);
+                        tc_combine6<0>(lb, sR, m8, row, valid);
+                        tc_combine6<1>(lb, sR, m8, row, valid);
                     } else if (half == 0) {
-                        tc_combine6<0>(lb, sR, m8, row, valid, e, sF);
+                        tc_combine6<0>(lb, sR, m8, row, valid);
                     } else {
-                        tc_combine6<1>(lb, sR, m8, row, valid, e, sF);
+                        tc_combine6<1>(lb, sR, m8, row, valid);
                     }
                 }
             }
         }
         tc_fence_before();
         __syncthreads();
-        // (g) F* = x - f at the interior levels, the wall values at the walls
+        // (g) F* = x - f at the interior levels, the wall values at the walls:
+        // rows k of both blocks share the exponent e_k, so x_k - f_k =
+        // (Te + To - F) 2^E and x_nz-1-k - f_nz-1-k = (Te - To - F') 2^E
+        // with E = e_k + f_c - 52 and F = round(f 2^-E), exactly in integers
+        // but for that one rounding of f and the final conversion
         for (int i = threadIdx.x, p = 0; i < nmode * 3 * he; i += blockDim.x, ++p) {
             const int mi = i / (3 * he);
             const int r = i - mi * 3 * he;
@@ -893,28 +927,43 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             const int ky = mi ? g.ny - kya : kya;
             const int m = ky * g.nxhp + kx;
             const int c0 = 6 * mi + 2 * comp;
-            const double2 xe = make_double2(sR[c0 * m8 + k], sR[(c0 + 1) * m8 + k]);
-            double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
-            if (comp < 2 && k == 0) {
-                const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
-                const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
-                bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
-                bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
-            }
-            const double2* fc = fptr(F, comp);
             double2* oc = fptr(Out, comp);
             const size_t o1 = (size_t)k * g.nm + m, o2 = (size_t)(nz - 1 - k) * g.nm + m;
+            if (k == 0) {
+                double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
+                if (comp < 2) {
+                    const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
+                    const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                    bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
+                    bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
+                }
+                oc[o1] = bc1;
+                oc[o2] = bc2;
+                continue;
+            }
+            const double2* fc = fptr(F, comp);
             double2 v1, v2;
             if (p == 0) { v1 = keep1[0]; v2 = keep2[0]; }
             else if (p == 1) { v1 = keep1[1]; v2 = keep2[1]; }
             else { v1 = fc[o1]; v2 = k < ho ? fc[o2] : v1; }
-            if (k < ho) {
-                const double2 xo = make_double2(sR[c0 * m8 + t.e8 + k], sR[(c0 + 1) * m8 + t.e8 + k]);
-                oc[o1] = viscous_out_cn(g, k, make_double2(xe.x + xo.x, xe.y + xo.y), v1, bc1, bc2);
-                oc[o2] = viscous_out_cn(g, nz - 1 - k, make_double2(xe.x - xo.x, xe.y - xo.y), v2, bc1, bc2);
-            } else {
-                oc[o1] = viscous_out_cn(g, k, xe, v1, bc1, bc2);
+            const int e = __ldg(&ops.tcE[(size_t)q * m8 + k]);
+            double o1x, o1y, o2x = 0.0, o2y = 0.0;
+            {
+                const int E = e + sF[c0] - 52;
+                const long long te = __double_as_longlong(sR[c0 * m8 + k]);
+                const long long to = k < ho ? __double_as_longlong(sR[c0 * m8 + t.e8 + k]) : 0;
+                o1x = tc_sub_scaled(te + to, v1.x, E);
+                if (k < ho) o2x = tc_sub_scaled(te - to, v2.x, E);
             }
+            {
+                const int E = e + sF[c0 + 1] - 52;
+                const long long te = __double_as_longlong(sR[(c0 + 1) * m8 + k]);
+                const long long to = k < ho ? __double_as_longlong(sR[(c0 + 1) * m8 + t.e8 + k]) : 0;
+                o1y = tc_sub_scaled(te + to, v1.y, E);
+                if (k < ho) o2y = tc_sub_scaled(te - to, v2.y, E);
+            }
+            oc[o1] = make_double2(o1x, o1y);
+            if (k < ho) oc[o2] = make_double2(o2x, o2y);
         }
         __syncthreads();  // shared buffers are reused by the next q
     }
