@@ -651,8 +651,16 @@ constexpr size_t kTcSmemMax = 227 * 1024;
 // Whether the staged inputs (12 columns of nz values) still fit beside the
 // operands: true up to nz = 127; at nz = 129 the kernel reads its inputs
 // from global memory in (b) instead.
+// Staged inputs of one q: 12 columns of nz values (F and the sources of both
+// modes' u, v, w), and, in two buffers by the parity of q (the next q's are
+// copied while the current one's outputs still read them), the wall
+// pressure gradients of both modes (8 values) and the q's m8 row exponents.
+__host__ __device__ inline size_t viscous_tc_stage_bytes(const TcGeom& t, int nz) {
+    return (size_t)(12 * nz + 16) * sizeof(double2) + (size_t)2 * t.m8 * sizeof(int);
+}
+
 __host__ __device__ inline bool viscous_tc_staged(const TcGeom& t, int nz) {
-    return viscous_tc_stage_offset(t) + (size_t)12 * nz * sizeof(double2) <= kTcSmemMax;
+    return viscous_tc_stage_offset(t) + viscous_tc_stage_bytes(t, nz) <= kTcSmemMax;
 }
 
 __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops, const StepParams& sp,
@@ -672,8 +680,11 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcN);            // [0] MMAs done, [1] slices landed
     uint32_t* tbase = reinterpret_cast<uint32_t*>(mbar + 2);
     int* landed = reinterpret_cast<int*>(tbase + 1);                    // the slices of this q arrived
-    // staged inputs of one q: [F, Src][mode 0, 1][u, v, w][nz levels]
+    // staged inputs of one q: [F, Src][mode 0, 1][u, v, w][nz levels], then
+    // the wall gradients [mode][GP row 0..3] and the q's row exponents
     double2* sP = reinterpret_cast<double2*>(tcsm + viscous_tc_stage_offset(t));
+    double2* sGP2 = sP + 12 * nz;                      // [2][mode][4]
+    int* sEq2 = reinterpret_cast<int*>(sGP2 + 16);      // [2][m8]
     {
         uint4* z = reinterpret_cast<uint4*>(sA);
         const int n16 = kTcSlices * (bl.a + b_halves) / 8;
@@ -712,12 +723,22 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             double2* dst = sP + (size_t)((fld * 2 + mi) * 3 + comp) * nz;
             for (int z = lane; z < nz; z += 32) cp_async16(dst + z, src + (size_t)z * g.nm);
         }
+        const int j = threadIdx.x, b = (q - q0) & 1;
+        if (j < 4 * nmode) {  // the wall gradients GP[4][nm] of the modes
+            const int mi = j >> 2, w = j & 3;
+            const int m = (mi ? g.ny - kya : kya) * g.nxhp + kx;
+            cp_async16(sGP2 + 8 * b + 4 * mi + w, GP + (size_t)w * g.nm + m);
+        } else if (j >= 32 && j < 32 + m8 / 4) {  // the row exponents, 4 per copy
+            cp_async16(sEq2 + b * m8 + 4 * (j - 32), ops.tcE + (size_t)q * m8 + 4 * (j - 32));
+        }
         cp_async_commit();
     };
     if (q0 < q1) stage(q0);
     bool ok = true;
     for (int q = q0; q < q1 && ok; ++q) {
         const uint32_t par = (uint32_t)((q - q0) & 1);
+        const double2* sGP = sGP2 + 8 * par;  // this q's staged wall gradients and row exponents
+        const int* sEq = sEq2 + par * m8;
         cp_async_wait_all();
         __syncthreads();  // this q's staged inputs, from every thread's copies
         // (a) digit slices of the operator: per digit, one copy per 8-row
@@ -773,8 +794,8 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                     // lifting data l = f_wall + 2 bc, bc = -dt dp/dx|wall (u), -dt dp/dy|wall (v), 0 (w)
                     double2 l1 = f1, ln = fn;
                     if (comp < 2) {
-                        const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
-                        const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                        const double2 g1 = staged ? sGP[4 * mi + 2 * comp] : GP[(size_t)(2 * comp) * g.nm + m];
+                        const double2 g2 = staged ? sGP[4 * mi + 2 * comp + 1] : GP[(size_t)(2 * comp + 1) * g.nm + m];
                         const double m2dt = -2.0 * sp.dt;
                         l1 = make_double2(fma(m2dt, g1.x, f1.x), fma(m2dt, g1.y, f1.y));
                         ln = make_double2(fma(m2dt, g2.x, fn.x), fma(m2dt, g2.y, fn.y));
@@ -932,8 +953,8 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             if (k == 0) {
                 double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
                 if (comp < 2) {
-                    const double2 g1 = GP[(size_t)(2 * comp) * g.nm + m];
-                    const double2 g2 = GP[(size_t)(2 * comp + 1) * g.nm + m];
+                    const double2 g1 = staged ? sGP[4 * mi + 2 * comp] : GP[(size_t)(2 * comp) * g.nm + m];
+                    const double2 g2 = staged ? sGP[4 * mi + 2 * comp + 1] : GP[(size_t)(2 * comp + 1) * g.nm + m];
                     bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
                     bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
                 }
@@ -946,7 +967,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             if (p == 0) { v1 = keep1[0]; v2 = keep2[0]; }
             else if (p == 1) { v1 = keep1[1]; v2 = keep2[1]; }
             else { v1 = fc[o1]; v2 = k < ho ? fc[o2] : v1; }
-            const int e = __ldg(&ops.tcE[(size_t)q * m8 + k]);
+            const int e = staged ? sEq[k] : __ldg(&ops.tcE[(size_t)q * m8 + k]);
             double o1x, o1y, o2x = 0.0, o2y = 0.0;
             {
                 const int E = e + sF[c0] - 52;
@@ -3125,7 +3146,7 @@ cudaError_t launch_poisson_residual(const GridDev& g, const Ops& ops, const Step
 size_t viscous_tc_smem(const GridDev& g) {
     const TcGeom t = tc_geom(g.nz);
     // + the staged inputs of one q where they fit
-    return viscous_tc_stage_offset(t) + (viscous_tc_staged(t, g.nz) ? (size_t)12 * g.nz * sizeof(double2) : 0);
+    return viscous_tc_stage_offset(t) + (viscous_tc_staged(t, g.nz) ? viscous_tc_stage_bytes(t, g.nz) : 0);
 }
 
 bool viscous_tc_fits(const GridDev& g) {
