@@ -1,0 +1,117 @@
+"""CPU: the integer identities the emulated-FP64 kernels rely on, restated in
+exact Python integers (f90_dns_gb300/csrc/tc.cuh, step.cu):
+
+* digit pairs (tc_digit_pairs): the 7-bit fields of U + 64 (1 + 128 + ... +
+  128^7), minus 64, are U's balanced base-128 digits (tc_digits), and the
+  FP16 with bits 0x6400 | v is 1024 + v, so one subtraction of 1088 gives the
+  digit exactly;
+* class combination (tc_combine8): pairing adjacent weight classes in 32-bit
+  integers gives the same T as summing every class term in 64 bits;
+* limb products (fx_mac, the fixed-point Poisson solve): four 32 x 32-bit
+  limb products of a 58-bit and a 54-bit integer, summed in 64-bit partial
+  sums over up to 65 terms, recombine to the exact 128-bit dot product
+  without overflow.
+"""
+import random
+
+import numpy as np
+
+BIAS = 0x0081020408102040  # 64 in each of the 8 base-128 digit places
+
+
+def balanced_digits(u):
+    """tc_digits: 8 balanced base-128 digits, most significant first."""
+    c = [0] * 8
+    for s in range(7, -1, -1):
+        r = u & 127
+        d = r - 128 if r >= 64 else r
+        c[s] = d
+        u = (u - d) >> 7
+    assert u == 0
+    return c
+
+
+def biased_field_digits(u):
+    v = u + BIAS
+    assert 0 <= v < 2**56
+    return [((v >> (7 * (7 - s))) & 127) - 64 for s in range(8)]
+
+
+def test_bias_constant():
+    assert BIAS == sum(64 * 128**s for s in range(8))
+
+
+def test_biased_fields_are_the_balanced_digits():
+    rng = random.Random(1)
+    cases = [0, 1, -1, 2**54, -2**54, 63, 64, -64, -65, 2**53 + 12345]
+    cases += [rng.randint(-2**54, 2**54) for _ in range(20000)]
+    for u in cases:
+        d = biased_field_digits(u)
+        assert d == balanced_digits(u), u
+        assert all(-64 <= x <= 63 for x in d)
+        assert sum(x * 128**(7 - s) for s, x in enumerate(d)) == u
+
+
+def test_fp16_field_encoding():
+    for v in range(128):
+        bits = np.array([0x6400 | v], dtype=np.uint16)
+        h = bits.view(np.float16)[0]
+        assert float(h) == 1024.0 + v
+        assert float(np.float16(h) - np.float16(1088.0)) == v - 64  # exact in FP16
+    assert np.array([0x6440], dtype=np.uint16).view(np.float16)[0] == np.float16(1088.0)
+
+
+def class_sum_64(D):
+    t = sum(D[c] * 2**(7 * (6 - c)) for c in range(7))
+    return t + ((D[7] + 64) >> 7)
+
+
+def class_sum_paired(D):
+    def i32(x):
+        assert -2**31 <= x < 2**31
+        return x
+    pa = i32(D[0] * 128 + D[1])
+    pb = i32(D[2] * 128 + D[3])
+    pc = i32(D[4] * 128 + D[5])
+    tail = i32(D[6] + ((D[7] + 64) >> 7))
+    t = pa * 16384 + pb
+    t = t * 16384 + pc
+    return t * 128 + tail
+
+
+def test_paired_class_combination():
+    rng = random.Random(2)
+    lim = 2**22 - 1
+    for _ in range(20000):
+        D = [rng.randint(-lim, lim) for _ in range(8)]
+        assert class_sum_paired(D) == class_sum_64(D)
+    for D in ([lim] * 8, [-lim] * 8, [lim, -lim] * 4):
+        assert class_sum_paired(D) == class_sum_64(D)
+
+
+def limb_dot(A, B):
+    p = [0, 0, 0, 0]  # weights 2^0, 2^27, 2^29, 2^56
+    for a, b in zip(A, B):
+        a0, a1 = a & 0x1FFFFFFF, a >> 29
+        b0, b1 = b & 0x7FFFFFF, b >> 27
+        for x in (a0, a1, b0, b1):
+            assert -2**31 <= x < 2**31
+        p[0] += a0 * b0
+        p[1] += a0 * b1
+        p[2] += a1 * b0
+        p[3] += a1 * b1
+        assert all(-2**63 <= x < 2**63 for x in p)
+    return p[0] + p[1] * 2**27 + p[2] * 2**29 + p[3] * 2**56
+
+
+def test_limb_products_exact_up_to_65_terms():
+    rng = random.Random(3)
+    for n in (1, 17, 33, 49, 65):
+        for _ in range(300):
+            A = [rng.randint(-2**58, 2**58) for _ in range(n)]
+            B = [rng.randint(-2**54, 2**54) for _ in range(n)]
+            assert limb_dot(A, B) == sum(a * b for a, b in zip(A, B))
+        # the extreme magnitudes, all of one sign: the partial sums' worst case
+        A = [2**58] * n
+        B = [-2**54] * n
+        assert limb_dot(A, B) == sum(a * b for a, b in zip(A, B))
