@@ -692,7 +692,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     }
     if (threadIdx.x < 32) tc_alloc(tbase, 2 * kTcDCols);
     if (threadIdx.x == 0) {
-        tc_mbar_init(&mbar[0]);
+        tc_mbar_init(&mbar[0], 2);  // two commits per q: the E and the O issuer
         tc_mbar_init(&mbar[1]);
     }
     tc_fence_proxy();  // the zeroed operands, before any bulk copy or MMA
@@ -859,32 +859,34 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
-        // (e) the digit-pair products, one thread issues
-        if (threadIdx.x == 0) {
-            *landed = tc_mbar_wait(&mbar[1], par, 1 << 22) ? 1 : 0;
-            if (*landed && !ops.tc_stall) {
+        // (e) the digit-pair products: block E issued by thread 0, block O by
+        // thread 32 (independent TMEM columns), each committing to mbar[0]
+        if (threadIdx.x == 0 || threadIdx.x == 32) {
+            const bool blkO = threadIdx.x == 32;
+            const int ld = tc_mbar_wait(&mbar[1], par, 1 << 22) ? 1 : 0;
+            if (!blkO) *landed = ld;
+            if (ld && !ops.tc_stall) {
                 // descriptors differ only in their start address (16-byte
                 // units in the low field; a K offset of k elements is k/8
-                // core matrices of 128 B, i.e. k units): one add per MMA
-                const uint64_t dAE = tc_desc(tc_smem_u32(sA), 128, (uint32_t)bl.kE * 16);
-                // block O starts 64 rows (8 row groups) before its operand, so
+                // core matrices of 128 B, i.e. k units): one add per MMA.
+                // Block O starts 64 rows (8 row groups) before its operand, so
                 // its o8 <= 64 result rows land in TMEM lanes 64 .. 64 + o8
                 // (lane quadrants 2 and 3) while block E's use quadrants 0 and 1
                 // (2 as well at nz = 129): the combination then spreads over
                 // more warps, each reading only its own quadrant
-                const uint64_t dAO =
-                    tc_desc(tc_smem_u32(sA + bl.aE) - (uint32_t)(8 * bl.kO * 16), 128, (uint32_t)bl.kO * 16);
-                const uint64_t dB = tc_desc(tc_smem_u32(sB), 128, (uint32_t)t.kt * 16);
-                const int nkE = bl.kE / 16, nkO = bl.kO / 16;
+                const uint64_t dA = blkO ? tc_desc(tc_smem_u32(sA + bl.aE) - (uint32_t)(8 * bl.kO * 16), 128,
+                                                   (uint32_t)bl.kO * 16)
+                                         : tc_desc(tc_smem_u32(sA), 128, (uint32_t)bl.kE * 16);
+                const uint64_t dB =
+                    tc_desc(tc_smem_u32(sB), 128, (uint32_t)t.kt * 16) + (uint64_t)(blkO ? bl.bO : bl.bE);
+                const int nk = (blkO ? bl.kO : bl.kE) / 16;
+                const uint32_t d0 = tmem + (blkO ? (uint32_t)kTcDCols : 0u);
                 for (int sa = 0; sa < kTcSlices; ++sa) {
                     const uint32_t idesc = tc_idesc(kTcN * (kTcSlices - sa));
                     const uint64_t so = (uint64_t)((sa * bl.a * 2) >> 4);
-                    for (int ks = 0; ks < nkE; ++ks)
-                        tc_mma(tmem + (uint32_t)(sa * kTcN), dAE + so + (uint64_t)(16 * ks),
-                               dB + (uint64_t)(bl.bE + 16 * ks), idesc, (sa > 0 || ks > 0) ? 1u : 0u);
-                    for (int ks = 0; ks < nkO; ++ks)
-                        tc_mma(tmem + (uint32_t)(kTcDCols + sa * kTcN), dAO + so + (uint64_t)(16 * ks),
-                               dB + (uint64_t)(bl.bO + 16 * ks), idesc, (sa > 0 || ks > 0) ? 1u : 0u);
+                    for (int ks = 0; ks < nk; ++ks)
+                        tc_mma(d0 + (uint32_t)(sa * kTcN), dA + so + (uint64_t)(16 * ks), dB + (uint64_t)(16 * ks),
+                               idesc, (sa > 0 || ks > 0) ? 1u : 0u);
                 }
             }
             if (!ops.tc_stall) tc_commit(&mbar[0]);  // also when nothing was issued: the waiters are released
@@ -1064,7 +1066,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     for (int i = tid; i < m8; i += blockDim.x) sE[i] = __ldg(&ops.tcDE[i]);
     if (tid < 32) tc_alloc(tbase, 2 * kTcClasses * kTcVortCols);
     if (tid == 0) {
-        tc_mbar_init(&mbar[0]);
+        tc_mbar_init(&mbar[0], 2);  // two commits per tile: the E and the O issuer
         tc_mbar_init(&mbar[1]);
         *landed = 0;
     }
@@ -1168,29 +1170,32 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
-        // (e) the digit-pair products
-        if (tid == 0) {
-            if (tile == tile0) *landed = tc_mbar_wait(&mbar[1], 0, 1 << 22) ? 1 : 0;
-            if (*landed && !ops.tc_stall) {
+        // (e) the digit-pair products: block E issued by thread 0, block O by
+        // thread 32 (independent TMEM columns), each committing to mbar[0]
+        if (tid == 0 || tid == 32) {
+            const bool blkO = tid == 32;
+            int ld = *landed;
+            if (tile == tile0) {
+                ld = tc_mbar_wait(&mbar[1], 0, 1 << 22) ? 1 : 0;
+                if (!blkO) *landed = ld;
+            }
+            if (ld && !ops.tc_stall) {
                 // the descriptors differ only in their start address (16-byte
-                // units; a K offset of k elements is k units): one add per MMA
-                const uint64_t dAE = tc_desc(tc_smem_u32(sA), 128, (uint32_t)bl.kE * 16);
-                // block O starts 64 rows before its operand: its results land in
+                // units; a K offset of k elements is k units): one add per MMA.
+                // Block O starts 64 rows before its operand: its results land in
                 // TMEM lanes 64 .. 64 + o8 (tc_oshift_pad)
-                const uint64_t dAO =
-                    tc_desc(tc_smem_u32(sA + bl.aE) - (uint32_t)(8 * bl.kO * 16), 128, (uint32_t)bl.kO * 16);
-                const uint64_t dB = tc_desc(tc_smem_u32(sB), 128, (uint32_t)t.kt * 16);
-                const int nkE = bl.kE / 16, nkO = bl.kO / 16;
-                constexpr uint32_t kDC = kTcClasses * kTcVortCols;
+                const uint64_t dA = blkO ? tc_desc(tc_smem_u32(sA + bl.aE) - (uint32_t)(8 * bl.kO * 16), 128,
+                                                   (uint32_t)bl.kO * 16)
+                                         : tc_desc(tc_smem_u32(sA), 128, (uint32_t)bl.kE * 16);
+                const uint64_t dB = tc_desc(tc_smem_u32(sB), 128, (uint32_t)t.kt * 16) + (uint64_t)(blkO ? bl.bO : bl.bE);
+                const int nk = (blkO ? bl.kO : bl.kE) / 16;
+                const uint32_t d0 = tmem + (blkO ? (uint32_t)(kTcClasses * kTcVortCols) : 0u);
                 for (int sa = 0; sa < kTcSlices; ++sa) {
                     const uint32_t idesc = tc_idesc(kTcVortCols * (kTcSlices - sa));
                     const uint64_t so = (uint64_t)((sa * bl.a * 2) >> 4);
-                    for (int ks = 0; ks < nkE; ++ks)
-                        tc_mma(tmem + (uint32_t)(sa * kTcVortCols), dAE + so + (uint64_t)(16 * ks),
-                               dB + (uint64_t)(bl.bE + 16 * ks), idesc, (sa > 0 || ks > 0) ? 1u : 0u);
-                    for (int ks = 0; ks < nkO; ++ks)
-                        tc_mma(tmem + kDC + (uint32_t)(sa * kTcVortCols), dAO + so + (uint64_t)(16 * ks),
-                               dB + (uint64_t)(bl.bO + 16 * ks), idesc, (sa > 0 || ks > 0) ? 1u : 0u);
+                    for (int ks = 0; ks < nk; ++ks)
+                        tc_mma(d0 + (uint32_t)(sa * kTcVortCols), dA + so + (uint64_t)(16 * ks), dB + (uint64_t)(16 * ks),
+                               idesc, (sa > 0 || ks > 0) ? 1u : 0u);
                 }
             }
             if (!ops.tc_stall) tc_commit(&mbar[0]);

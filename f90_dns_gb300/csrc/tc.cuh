@@ -275,8 +275,8 @@ __device__ __forceinline__ void tc_commit(uint64_t* mbar) {
         tc_smem_u32(mbar)));
 }
 
-__device__ __forceinline__ void tc_mbar_init(uint64_t* mbar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem_u32(mbar)));
+__device__ __forceinline__ void tc_mbar_init(uint64_t* mbar, uint32_t count = 1) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem_u32(mbar)), "r"(count));
     asm volatile("fence.mbarrier_init.release.cluster;");
 }
 

@@ -301,6 +301,25 @@ def test_nonfinite_state_is_reported(built_lib):
         assert np.isfinite(d.diagnostics().energy)
 
 
+def test_nonfinite_state_survives_a_step_of_the_integer_kernels(built_lib, monkeypatch):
+    """With the tensor-core and fixed-point forms forced, a NaN in the state is
+    still non-finite after a step (the emulated products and the fixed-point
+    Poisson solve do not turn it into finite values): the diagnostics report
+    DNS3D_E_NONFINITE."""
+    from f90_dns_gb300.capi import DNS3D_E_NONFINITE
+    monkeypatch.setenv("DNS3D_TENSOR_CORES", "1")
+    wl = dict(C1, nx=32, ny=16, nz=17)
+    with ChannelDNS(config_from(wl)) as d:
+        st = d.get_state()
+        bad = st["w"].copy()
+        bad[6, 3, 7] = np.nan
+        d.set_state(w=bad)
+        d.step(1)
+        with pytest.raises(Dns3DError) as ei:
+            d.diagnostics()
+        assert ei.value.code == DNS3D_E_NONFINITE
+
+
 def test_split_diagnostics_match_combined(built_lib):
     """dns3d_output_diagnostics and dns3d_check_divergence (the reference's
     output_diagnostics_3d and check_divergence_3d, called on their own
