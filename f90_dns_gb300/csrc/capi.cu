@@ -1167,6 +1167,14 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
                 for (int i = 0; i < he; ++i) PDe[(size_t)j * phe4 + i] = (float)dv[i];
             }
         }
+        // the same forward operators with input row i scaled by 2 w_i / dt
+        std::vector<float> PAeS(PAe.size(), 0.f), PAoS(PAo.size(), 0.f);
+        for (int i = 0; i < he; ++i)
+            for (int j = 0; j < he; ++j)
+                PAeS[(size_t)i * phe4 + j] = (float)(Yne[(size_t)i * he + j] * fe(i) * 2.0 * wh[i] / c.dt);
+        for (int i = 0; i < ho; ++i)
+            for (int j = 0; j < ho; ++j)
+                PAoS[(size_t)i * pho4 + j] = (float)(Yno[(size_t)i * ho + j] * fo(i) * 2.0 * wh[i] / c.dt);
         for (int j = 0; j < he; ++j) plame[j] = (float)lne[j];
         for (int j = 0; j < ho; ++j) plamo[j] = (float)lno[j];
         MixedOps& mx = h->mx;
@@ -1183,6 +1191,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             (rc = dev_alloc(h, &mx.sn, snf.size())) ||
             (rc = dev_alloc(h, &mx.D1e, D1e32.size())) || (rc = dev_alloc(h, &mx.D1o, D1o32.size())) ||
             (rc = dev_alloc(h, &mx.PAe, PAe.size())) || (rc = dev_alloc(h, &mx.PAo, PAo.size())) ||
+            (rc = dev_alloc(h, &mx.PAeS, PAeS.size())) || (rc = dev_alloc(h, &mx.PAoS, PAoS.size())) ||
             (rc = dev_alloc(h, &mx.PBe, PBe.size())) || (rc = dev_alloc(h, &mx.PBo, PBo.size())) ||
             (rc = dev_alloc(h, &mx.PDe, PDe.size())) || (rc = dev_alloc(h, &mx.PDo, PDo.size())) ||
             (rc = dev_alloc(h, &mx.plame, plame.size())) || (rc = dev_alloc(h, &mx.plamo, plamo.size())) ||
@@ -1198,6 +1207,7 @@ int dns3d_create(const dns3d_config* cfg, dns3d_handle** out) {
             {mx.sn, snf.data(), snf.size() * 4}, {mx.D1e, D1e32.data(), D1e32.size() * 4},
             {mx.D1o, D1o32.data(), D1o32.size() * 4},
             {mx.PAe, PAe.data(), PAe.size() * 4}, {mx.PAo, PAo.data(), PAo.size() * 4},
+            {mx.PAeS, PAeS.data(), PAeS.size() * 4}, {mx.PAoS, PAoS.data(), PAoS.size() * 4},
             {mx.PBe, PBe.data(), PBe.size() * 4}, {mx.PBo, PBo.data(), PBo.size() * 4},
             {mx.PDe, PDe.data(), PDe.size() * 4}, {mx.PDo, PDo.data(), PDo.size() * 4},
             {mx.plame, plame.data(), plame.size() * 4}, {mx.plamo, plamo.data(), plamo.size() * 4},

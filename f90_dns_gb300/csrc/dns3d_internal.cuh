@@ -256,6 +256,10 @@ struct MixedOps {
     //   PDe [ho][phe4]: (dphi/dz) even part from phi~o; PDo [he][pho4]: odd part from phi~e
     int phe4, pho4;
     float* PAe; float* PAo; float* PBe; float* PBo; float* PDe; float* PDo;
+    // PAe, PAo with input row i scaled by 2 w_i / dt: the forward solve of the
+    // strong-form right-hand side, which is then formed without the weights
+    // and the 1/dt (pressure_mixed_body)
+    float* PAeS; float* PAoS;
     float* plame;            // [phe4] eigenvalues of the even block
     float* plamo;            // [pho4] eigenvalues of the odd block
     // folded stiffness S (symmetric fold of ops.S) as double-float pairs, for

@@ -2189,7 +2189,7 @@ __global__ void k_products32(FRFields in, FRFields out, size_t n) {
 // advanced in FP64 by k_viscous.
 __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops ops, StepParams sp,
                                                    Fields F, FFields Src, const double2* __restrict__ GP,
-                                                   Fields Out, int tc, int bx) {
+                                                   Fields Out, int tc, int bx, bool stage_mats = true) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int hei = mx.hei, hoi = mx.hoi, pe4 = mx.pe4, po4 = mx.po4;
     const int nr = pe4 + po4;        // folded rows (even block, then odd block)
@@ -2204,7 +2204,7 @@ __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops o
     float4* tw = reinterpret_cast<float4*>(ty + tsz);   // [tc] wall terms
     float* tk = reinterpret_cast<float*>(tw + tc);      // [tc] k^2 (-1: skip; <= -2: masked source)
     const int m0 = bx * tc;
-    {
+    if (stage_mats) {  // the eigenbasis matrices (a persistent CTA stages them once)
         const float4* A = reinterpret_cast<const float4*>(mx.AeT);
         for (int t = threadIdx.x; t < hei * (pe4 / 4); t += blockDim.x) sAe[t] = __ldg(&A[t]);
         A = reinterpret_cast<const float4*>(mx.AoT);
@@ -2383,10 +2383,15 @@ __device__ __forceinline__ void viscous_mixed_body(GridDev g, MixedOps mx, Ops o
     }
 }
 
+// Persistent: a CTA stages the matrices once and takes every gridDim.x-th tile.
 __global__ void __launch_bounds__(256) k_viscous_mixed(GridDev g, MixedOps mx, Ops ops, StepParams sp,
                                                        Fields F, FFields Src, const double2* __restrict__ GP,
                                                        Fields Out, int tc) {
-    viscous_mixed_body(g, mx, ops, sp, F, Src, GP, Out, tc, blockIdx.x);
+    const int ntiles = (g.nm + tc - 1) / tc;
+    for (int bx = blockIdx.x; bx < ntiles; bx += gridDim.x) {
+        viscous_mixed_body(g, mx, ops, sp, F, Src, GP, Out, tc, bx, bx == (int)blockIdx.x);
+        __syncthreads();  // the tile buffers are reused by the next tile
+    }
 }
 
 // ------------------------------------------------------------------ double-float
@@ -2450,10 +2455,10 @@ __device__ __forceinline__ void fold_load_df(float4* tile, const double2* __rest
     }
 }
 
-// Antisymmetric folded operator (double-float) on a double-float folded tile:
-// the output pair (z = k, z = nz-1-k) as FP64.
-__device__ __forceinline__ Pair anti_apply_df(const float2* __restrict__ De, const float2* __restrict__ Do,
-                                              const float4* tile, int k, int c, int tc, int he, int ho) {
+// anti_apply_df's even and odd parts before their sum and difference:
+// (ye.x, ye.y, yo.x, yo.y), yo zero at the unpaired mid level.
+__device__ __forceinline__ double4 anti_apply_df_parts(const float2* __restrict__ De, const float2* __restrict__ Do,
+                                                       const float4* tile, int k, int c, int tc, int he, int ho) {
     DF yex{0.f, 0.f}, yey{0.f, 0.f}, yox{0.f, 0.f}, yoy{0.f, 0.f};
     const float2* er = De + (size_t)k * ho;
     const float4* fo = tile + he * tc;
@@ -2463,7 +2468,6 @@ __device__ __forceinline__ Pair anti_apply_df(const float2* __restrict__ De, con
         df_mac(yex, a.x, a.y, b.x, b.y);
         df_mac(yey, a.x, a.y, b.z, b.w);
     }
-    Pair p;
     if (k < ho) {
         const float2* orow = Do + (size_t)k * he;
         for (int j = 0; j < he; ++j) {
@@ -2472,13 +2476,19 @@ __device__ __forceinline__ Pair anti_apply_df(const float2* __restrict__ De, con
             df_mac(yox, a.x, a.y, b.x, b.y);
             df_mac(yoy, a.x, a.y, b.z, b.w);
         }
-        const double ex = df_value(yex), ey = df_value(yey), ox = df_value(yox), oy = df_value(yoy);
-        p.a = make_double2(ex + ox, ey + oy);
-        p.b = make_double2(ex - ox, ey - oy);
-    } else {
-        p.a = make_double2(df_value(yex), df_value(yey));
-        p.b = p.a;
+        return make_double4(df_value(yex), df_value(yey), df_value(yox), df_value(yoy));
     }
+    return make_double4(df_value(yex), df_value(yey), 0.0, 0.0);
+}
+
+// Antisymmetric folded operator (double-float) on a double-float folded tile:
+// the output pair (z = k, z = nz-1-k) as FP64.
+__device__ __forceinline__ Pair anti_apply_df(const float2* __restrict__ De, const float2* __restrict__ Do,
+                                              const float4* tile, int k, int c, int tc, int he, int ho) {
+    const double4 y = anti_apply_df_parts(De, Do, tile, k, c, tc, he, ho);
+    Pair p;
+    p.a = make_double2(y.x + y.z, y.y + y.w);
+    p.b = k < ho ? make_double2(y.x - y.z, y.y - y.w) : p.a;
     return p;
 }
 
@@ -2517,7 +2527,8 @@ __device__ __forceinline__ Pair sym_apply_df(const float2* __restrict__ Ae, cons
 // phi~_j = -(V'^T b)_j / (l'_j + k^2) of the folded right-hand sides tb of a
 // mode tile, 4 eigen-rows of one block per thread, into tp.
 __device__ __forceinline__ void pressure_mixed_forward(const GridDev& g, const MixedOps& mx, const Ops& ops,
-                                                       const float2* tb, float2* tp, int m0, int tc) {
+                                                       const float* PAe, const float* PAo, const float2* tb,
+                                                       float2* tp, int m0, int tc) {
     const int he = ops.he, ho = ops.ho;
     const int pe4 = mx.phe4, po4 = mx.pho4, nbe = pe4 / 4, nbo = po4 / 4;
     for (int t = threadIdx.x; t < (nbe + nbo) * tc; t += blockDim.x) {
@@ -2530,7 +2541,7 @@ __device__ __forceinline__ void pressure_mixed_forward(const GridDev& g, const M
         for (int q = 0; q < 4; ++q) acc[q] = make_float2(0.f, 0.f);
         if (m < g.nm && m != 0) {
             const int len = even ? he : ho, ld4 = even ? nbe : nbo;
-            const float4* __restrict__ A = reinterpret_cast<const float4*>(even ? mx.PAe : mx.PAo) + j0 / 4;
+            const float4* __restrict__ A = reinterpret_cast<const float4*>(even ? PAe : PAo) + j0 / 4;
             const float2* b = tb + (even ? 0 : pe4 * tc) + c;
             for (int i = 0; i < len; ++i) {
                 const float4 e = __ldg(&A[(size_t)i * ld4]);
@@ -2687,15 +2698,40 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
         float2 fs = make_float2(0.f, 0.f), fd = fs;
         double2 b1 = make_double2(0.0, 0.0), b2 = b1;
         if (m < g.nm && m != 0) {
-            const Pair dz = anti_apply_df(Ae, Ao, tw, k, c, tc, he, ho);
             const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-            b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
-            if (k < ho) {
-                b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
-                fs = make_float2(d2f(b1.x + b2.x), d2f(b1.y + b2.y));
-                fd = make_float2(d2f(b1.x - b2.x), d2f(b1.y - b2.y));
+            if (!kRefine && !sp.weak_form) {
+                // the folded strong-form right-hand side divided by 2 w_k / dt
+                // (the scaled forward operators PAeS, PAoS carry that factor):
+                // (b_k +- b_k') dt / (2 w_k) = i (ax/2)(u_k +- u_k') +
+                // i (ay/2)(v_k +- v_k') + (ye | yo), the mid level
+                // i (ax/2) u_k + i (ay/2) v_k + ye / 2; ye, yo the even and
+                // odd parts of D1.w* -- 20 FP64 operations per level pair
+                // instead of 36
+                const double4 y = anti_apply_df_parts(Ae, Ao, tw, k, c, tc, he, ho);
+                const double hax = 0.5 * mi.ax, hay = 0.5 * mi.ay;
+                const size_t o1 = (size_t)k * g.nm + m;
+                const double2 u1 = US[o1], v1 = VS[o1];
+                if (k < ho) {
+                    const size_t o2 = (size_t)(nz - 1 - k) * g.nm + m;
+                    const double2 u2 = US[o2], v2 = VS[o2];
+                    const double2 up = make_double2(u1.x + u2.x, u1.y + u2.y), um = make_double2(u1.x - u2.x, u1.y - u2.y);
+                    const double2 vp = make_double2(v1.x + v2.x, v1.y + v2.y), vm = make_double2(v1.x - v2.x, v1.y - v2.y);
+                    fs = make_float2(d2f(fma(-hax, up.y, fma(-hay, vp.y, y.x))), d2f(fma(hax, up.x, fma(hay, vp.x, y.y))));
+                    fd = make_float2(d2f(fma(-hax, um.y, fma(-hay, vm.y, y.z))), d2f(fma(hax, um.x, fma(hay, vm.x, y.w))));
+                } else {
+                    fs = make_float2(d2f(fma(-hax, u1.y, fma(-hay, v1.y, 0.5 * y.x))),
+                                     d2f(fma(hax, u1.x, fma(hay, v1.x, 0.5 * y.y))));
+                }
             } else {
-                fs = make_float2(d2f(b1.x), d2f(b1.y));
+                const Pair dz = anti_apply_df(Ae, Ao, tw, k, c, tc, he, ho);
+                b1 = pressure_rhs(g, ops, sp, k, m, mi, US, VS, dz.a);
+                if (k < ho) {
+                    b2 = pressure_rhs(g, ops, sp, nz - 1 - k, m, mi, US, VS, dz.b);
+                    fs = make_float2(d2f(b1.x + b2.x), d2f(b1.y + b2.y));
+                    fd = make_float2(d2f(b1.x - b2.x), d2f(b1.y - b2.y));
+                } else {
+                    fs = make_float2(d2f(b1.x), d2f(b1.y));
+                }
             }
         }
         tb[k * tc + c] = fs;
@@ -2706,7 +2742,8 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
         }
     }
     __syncthreads();
-    pressure_mixed_forward(g, mx, ops, tb, tp, m0, tc);
+    const bool scaled = !kRefine && !sp.weak_form;
+    pressure_mixed_forward(g, mx, ops, scaled ? mx.PAeS : mx.PAe, scaled ? mx.PAoS : mx.PAo, tb, tp, m0, tc);
     __syncthreads();
     pressure_mixed_back<false>(g, mx, ops, tp, PHI, PHIZ, m0, tc);
     if (!kRefine) return;
@@ -2739,7 +2776,7 @@ __device__ __forceinline__ void pressure_mixed_body(GridDev g, MixedOps mx, Ops 
         if (k < ho) tb[(pe4 + k) * tc + c] = fd;
     }
     __syncthreads();
-    pressure_mixed_forward(g, mx, ops, tb, tp, m0, tc);
+    pressure_mixed_forward(g, mx, ops, mx.PAe, mx.PAo, tb, tp, m0, tc);
     __syncthreads();
     pressure_mixed_back<true>(g, mx, ops, tp, PHI, PHIZ, m0, tc);
 }
@@ -3154,6 +3191,19 @@ size_t viscous_tc_smem(const GridDev& g) {
     return viscous_tc_stage_offset(t) + (viscous_tc_staged(t, g.nz) ? viscous_tc_stage_bytes(t, g.nz) : 0);
 }
 
+// Streaming multiprocessors of the current device (read once per device).
+int num_sms() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (cached[dev] == 0) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
 bool viscous_tc_fits(const GridDev& g) {
     return tc_supported(g.nz) && viscous_tc_smem(g) <= smem_limit(k_viscous_tc);
 }
@@ -3286,7 +3336,12 @@ cudaError_t launch_viscous_mixed(const GridDev& g, const MixedOps& mx, const Ops
                                  Fields F, FFields Src, const double2* GP, Fields Out, cudaStream_t s) {
     const int tc = tile_width(g, kTileViscM);
     const size_t sm = viscous_mixed_smem(g, tc);
-    k_viscous_mixed<<<(g.nm + tc - 1) / tc, 256, sm, s>>>(g, mx, ops, sp, F, Src, GP, Out, tc);
+    const int ntiles = (g.nm + tc - 1) / tc;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_viscous_mixed, 256, sm);
+    if (e) return e;
+    const int nb = std::min(ntiles, std::max(1, per_sm) * num_sms());
+    k_viscous_mixed<<<nb, 256, sm, s>>>(g, mx, ops, sp, F, Src, GP, Out, tc);
     return cudaGetLastError();
 }
 
