@@ -2091,16 +2091,22 @@ __device__ __forceinline__ void fold_load32(float2* tile, const double2* __restr
     }
 }
 
-__device__ __forceinline__ float2 fold_dot32(const float* __restrict__ erow, const float2* in, int len, int tc,
-                                             int c) {
-    float2 acc = make_float2(0.f, 0.f);
+// sum_j erow[j] a[j] and sum_j erow[j] b[j] over j < len for two folded
+// tile parts a, b (column stride tc), each row entry loaded once for both
+__device__ __forceinline__ void fold_dot32x2(const float* __restrict__ erow, const float2* a, const float2* b,
+                                             int len, int tc, int c, float2& ra, float2& rb) {
+    float2 sa = make_float2(0.f, 0.f), sb = sa;
+#pragma unroll 4
     for (int j = 0; j < len; ++j) {
         const float e = __ldg(&erow[j]);
-        const float2 a = in[j * tc + c];
-        acc.x = fmaf(e, a.x, acc.x);
-        acc.y = fmaf(e, a.y, acc.y);
+        const float2 x = a[j * tc + c], y = b[j * tc + c];
+        sa.x = fmaf(e, x.x, sa.x);
+        sa.y = fmaf(e, x.y, sa.y);
+        sb.x = fmaf(e, y.x, sb.x);
+        sb.y = fmaf(e, y.y, sb.y);
     }
-    return acc;
+    ra = sa;
+    rb = sb;
 }
 
 __device__ __forceinline__ void vorticity_mixed_body(GridDev g, MixedOps mx, Ops ops,
@@ -2119,13 +2125,9 @@ __device__ __forceinline__ void vorticity_mixed_body(GridDev g, MixedOps mx, Ops
         const int k = t / tc, c = t - k * tc;
         const int m = m0 + c;
         if (m >= g.nm) continue;
-        float2 due = fold_dot32(mx.D1e + (size_t)k * ho, tu + he * tc, ho, tc, c);
-        float2 dve = fold_dot32(mx.D1e + (size_t)k * ho, tv + he * tc, ho, tc, c);
-        float2 duo = make_float2(0.f, 0.f), dvo = duo;
-        if (k < ho) {
-            duo = fold_dot32(mx.D1o + (size_t)k * he, tu, he, tc, c);
-            dvo = fold_dot32(mx.D1o + (size_t)k * he, tv, he, tc, c);
-        }
+        float2 due, dve, duo = make_float2(0.f, 0.f), dvo = duo;
+        fold_dot32x2(mx.D1e + (size_t)k * ho, tu + he * tc, tv + he * tc, ho, tc, c, due, dve);
+        if (k < ho) fold_dot32x2(mx.D1o + (size_t)k * he, tu, tv, he, tc, c, duo, dvo);
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
         const float ax = (float)mi.ax, ay = (float)mi.ay;
         const int npt = (k < ho) ? 2 : 1;
