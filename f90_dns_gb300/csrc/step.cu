@@ -2827,12 +2827,13 @@ __device__ __forceinline__ void correction_mixed_body(GridDev g, Ops ops, StepPa
         const int z = (int)(o / g.nm);
         const int m = (int)(o - (size_t)z * g.nm);
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
+        const double dax = dt * mi.ax, day = dt * mi.ay;
         const double2 ph = PHI[o], pz = PHIZ[o];
-        const double2 px = i_times(mi.ax, ph), py = i_times(mi.ay, ph);
         const double2 us = US[o], vs = VS[o], ws = WS[o];
-        store_projection(sp, z, g.nz, o, make_double2(us.x - dt * px.x, us.y - dt * px.y),
-                         make_double2(vs.x - dt * py.x, vs.y - dt * py.y),
-                         make_double2(ws.x - dt * pz.x, ws.y - dt * pz.y), U, V, W);
+        // u* - dt (i ax) phi, v* - dt (i ay) phi, w* - dt dphi/dz with fused products
+        store_projection(sp, z, g.nz, o, make_double2(fma(dax, ph.y, us.x), fma(-dax, ph.x, us.y)),
+                         make_double2(fma(day, ph.y, vs.x), fma(-day, ph.x, vs.y)),
+                         make_double2(fma(-dt, pz.x, ws.x), fma(-dt, pz.y, ws.y)), U, V, W);
         double2 pp = P[o];
         pp.x += ph.x;
         pp.y += ph.y;
