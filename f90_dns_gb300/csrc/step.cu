@@ -1007,7 +1007,7 @@ __global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepPara
 // ------------------------------------------------------------------ tensor-core z-derivatives
 // The fixed z-derivative D1 (folded, block anti-diagonal [[0, De], [Do, 0]] on
 // [fe; fo]) applied to Op::kFields spectral fields as emulated-FP64
-// tensor-core products (tc.cuh), then Op::out forms the kernel's outputs from
+// tensor-core products (tc.cuh), then Op::out_level forms the kernel's outputs from
 // the derivatives exactly as the FP64-pipe kernel does.  D1 is the same for
 // every mode, so its digit image is copied into shared memory once per CTA
 // and a CTA runs tiles of kTcVortCols right-hand-side columns (modes x fields
@@ -1017,7 +1017,7 @@ __global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepPara
 // inputs) and block O (Do: odd outputs from the even inputs) against the
 // right-hand-side digit slices 0..7-sa side by side, N = 16 (8-sa), into 8
 // weight-class accumulators per block (256 TMEM columns); (f) int64
-// combination -> D1.f in FP64; (g) Op::out per level pair.
+// combination -> D1.f in FP64; (g) Op::out_level per level.
 constexpr int kTcVortCols = 16;  // right-hand-side columns per tile (2 CTAs of 512 threads per SM)
 constexpr int kTcVortModes = kTcVortCols / 4;  // modes per tile: u, v x re, im
 constexpr int kTcCorrModes = kTcVortCols / 2;  // modes per tile: phi x re, im
@@ -1250,24 +1250,41 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         }
         tc_fence_before();
         __syncthreads();
-        // (g) the outputs at the level pair (k, nz-1-k)
-        // (the tile's modes fastest: adjacent lanes read and write adjacent
-        // modes of one level, kModes x 16 contiguous bytes)
-        for (int i = tid; i < kModes * he; i += blockDim.x) {
-            const int mi = i % kModes, k = i / kModes;
+        // (g) the outputs: one level z of one mode per item when the tile's
+        // levels fit one pass of the CTA (z and its mirror nz-1-z share the
+        // folded row k: ye + yo below the middle, ye - yo above), else one
+        // level pair per item; the tile's modes fastest, so adjacent lanes
+        // read and write adjacent modes of one level (kModes x 16 bytes)
+        const bool per_level = kModes * nz <= (int)blockDim.x;
+        const int nlev = per_level ? nz : he;
+        for (int i = tid; i < kModes * nlev; i += blockDim.x) {
+            const int mi = i % kModes, zi = i / kModes;
             const int m = m0 + mi;
             if (m >= g.nm) continue;
-            Pair dz[Op::kFields];
+            const int k = (per_level && zi >= he) ? nz - 1 - zi : zi;
+            // D1.f at level k (upper = false) or nz-1-k (upper = true)
+            auto level = [&](bool upper, double2* d) {
 #pragma unroll
-            for (int f = 0; f < Op::kFields; ++f) {
-                const int c0 = 2 * (Op::kFields * mi + f);
-                const double2 ye = make_double2(sR[c0 * m8 + k], sR[(c0 + 1) * m8 + k]);
-                const double2 yo = k < ho ? make_double2(sR[c0 * m8 + t.e8 + k], sR[(c0 + 1) * m8 + t.e8 + k])
-                                          : make_double2(0.0, 0.0);
-                dz[f].a = make_double2(ye.x + yo.x, ye.y + yo.y);
-                dz[f].b = make_double2(ye.x - yo.x, ye.y - yo.y);
+                for (int f = 0; f < Op::kFields; ++f) {
+                    const int c0 = 2 * (Op::kFields * mi + f);
+                    const double2 ye = make_double2(sR[c0 * m8 + k], sR[(c0 + 1) * m8 + k]);
+                    const double2 yo = k < ho ? make_double2(sR[c0 * m8 + t.e8 + k], sR[(c0 + 1) * m8 + t.e8 + k])
+                                              : make_double2(0.0, 0.0);
+                    d[f] = upper ? make_double2(ye.x - yo.x, ye.y - yo.y) : make_double2(ye.x + yo.x, ye.y + yo.y);
+                }
+            };
+            double2 d[Op::kFields];
+            if (per_level) {
+                level(zi >= he, d);
+                op.out_level(g, ops, m, zi, d);
+            } else {
+                level(false, d);
+                op.out_level(g, ops, m, k, d);
+                if (k < ho) {
+                    level(true, d);
+                    op.out_level(g, ops, m, nz - 1 - k, d);
+                }
             }
-            op.out(g, ops, m, k, k < ho ? 2 : 1, dz);
         }
         __syncthreads();  // sR and sB are reused by the next tile
     }
@@ -1288,18 +1305,16 @@ struct VortTcOp {
     double2* __restrict__ OY;
     double2* __restrict__ OZ;
     __device__ const double2* field(int f) const { return f ? V : U; }
-    __device__ void out(const GridDev& g, const Ops& ops, int m, int k, int npt, const Pair* dz) const {
+    // the outputs at level z of mode m from d = (D1.u, D1.v) there
+    __device__ void out_level(const GridDev& g, const Ops& ops, int m, int z, const double2* d) const {
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-        for (int p = 0; p < npt; ++p) {
-            const int z = p ? g.nz - 1 - k : k;
-            const size_t o = (size_t)z * g.nm + m;
-            const double2 w = W[o], u = U[o], v = V[o];
-            const double2 dv = p ? dz[1].b : dz[1].a, du = p ? dz[0].b : dz[0].a;
-            // (i ay) w - dv, du - (i ax) w, (i ax) v - (i ay) u with fused products
-            OX[o] = make_double2(fma(-mi.ay, w.y, -dv.x), fma(mi.ay, w.x, -dv.y));
-            OY[o] = make_double2(fma(mi.ax, w.y, du.x), fma(-mi.ax, w.x, du.y));
-            OZ[o] = make_double2(fma(-mi.ax, v.y, mi.ay * u.y), fma(mi.ax, v.x, -(mi.ay * u.x)));
-        }
+        const size_t o = (size_t)z * g.nm + m;
+        const double2 w = W[o], u = U[o], v = V[o];
+        const double2 du = d[0], dv = d[1];
+        // (i ay) w - dv, du - (i ax) w, (i ax) v - (i ay) u with fused products
+        OX[o] = make_double2(fma(-mi.ay, w.y, -dv.x), fma(mi.ay, w.x, -dv.y));
+        OY[o] = make_double2(fma(mi.ax, w.y, du.x), fma(-mi.ax, w.x, du.y));
+        OZ[o] = make_double2(fma(-mi.ax, v.y, mi.ay * u.y), fma(mi.ax, v.x, -(mi.ay * u.x)));
     }
 };
 
@@ -1329,34 +1344,32 @@ struct CorrTcOp {
     double2* __restrict__ P;
     double2* __restrict__ GP;
     __device__ const double2* field(int) const { return PHI; }
-    __device__ void out(const GridDev& g, const Ops& ops, int m, int k, int npt, const Pair* dzp) const {
+    // the projection at level z of mode m from d = D1.phi there
+    __device__ void out_level(const GridDev& g, const Ops& ops, int m, int z, const double2* dd) const {
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
         const double dt = sp.dt, dax = dt * mi.ax, day = dt * mi.ay;
-        for (int p = 0; p < npt; ++p) {
-            const int z = p ? g.nz - 1 - k : k;
-            const double2 d = p ? dzp[0].b : dzp[0].a;
-            const size_t o = (size_t)z * g.nm + m;
-            const double2 ph = PHI[o];
-            const double2 us = US[o], vs = VS[o], ws = WS[o];
-            // u* - dt (i ax) phi, v* - dt (i ay) phi, w* - dt dphi/dz
-            store_projection(sp, z, g.nz, o, make_double2(fma(dax, ph.y, us.x), fma(-dax, ph.x, us.y)),
-                             make_double2(fma(day, ph.y, vs.x), fma(-day, ph.x, vs.y)),
-                             make_double2(fma(-dt, d.x, ws.x), fma(-dt, d.y, ws.y)), U, V, W);
-            double2 pp = P[o];
-            pp.x += ph.x;
-            pp.y += ph.y;
-            P[o] = pp;
-            if (z == 0 || z == g.nz - 1) {
-                const int wall = (z == 0) ? 0 : 1;
-                GP[(size_t)wall * g.nm + m] = i_times(mi.ax, pp);
-                GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, pp);
-            }
+        const double2 d = dd[0];
+        const size_t o = (size_t)z * g.nm + m;
+        const double2 ph = PHI[o];
+        const double2 us = US[o], vs = VS[o], ws = WS[o];
+        // u* - dt (i ax) phi, v* - dt (i ay) phi, w* - dt dphi/dz
+        store_projection(sp, z, g.nz, o, make_double2(fma(dax, ph.y, us.x), fma(-dax, ph.x, us.y)),
+                         make_double2(fma(day, ph.y, vs.x), fma(-day, ph.x, vs.y)),
+                         make_double2(fma(-dt, d.x, ws.x), fma(-dt, d.y, ws.y)), U, V, W);
+        double2 pp = P[o];
+        pp.x += ph.x;
+        pp.y += ph.y;
+        P[o] = pp;
+        if (z == 0 || z == g.nz - 1) {
+            const int wall = (z == 0) ? 0 : 1;
+            GP[(size_t)wall * g.nm + m] = i_times(mi.ax, pp);
+            GP[(size_t)(2 + wall) * g.nm + m] = i_times(mi.ay, pp);
         }
     }
 };
 
 template <class Op>
-__global__ void __launch_bounds__(kTcVortThreads) k_dz_tc(GridDev g, Ops ops, Op op, int chunk, int* err) {
+__global__ void __launch_bounds__(kTcVortThreads, 2) k_dz_tc(GridDev g, Ops ops, Op op, int chunk, int* err) {
     constexpr int kModes = kTcVortCols / (2 * Op::kFields);
     const int ntiles = (g.nm + kModes - 1) / kModes;
     const int t0 = blockIdx.x * chunk;
@@ -1752,12 +1765,10 @@ struct PresRhsTcOp {
     const double2* __restrict__ WS;
     double2* __restrict__ PHI;
     __device__ const double2* field(int) const { return WS; }
-    __device__ void out(const GridDev& g, const Ops& ops, int m, int k, int npt, const Pair* dzp) const {
+    // the right-hand side at level z of mode m from d = D1.w* there
+    __device__ void out_level(const GridDev& g, const Ops& ops, int m, int z, const double2* d) const {
         const ModeInfo mi = mode_info(g, m, ops.xw, ops.yw);
-        for (int p = 0; p < npt; ++p) {
-            const int z = p ? g.nz - 1 - k : k;
-            PHI[(size_t)z * g.nm + m] = pressure_rhs(g, ops, sp, z, m, mi, US, VS, p ? dzp[0].b : dzp[0].a);
-        }
+        PHI[(size_t)z * g.nm + m] = pressure_rhs(g, ops, sp, z, m, mi, US, VS, d[0]);
     }
 };
 
