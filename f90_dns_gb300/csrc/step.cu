@@ -679,7 +679,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     int* sF = reinterpret_cast<int*>(sR + kTcN * m8);                   // column exponents
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcN);            // [0] MMAs done, [1] slices landed
     uint32_t* tbase = reinterpret_cast<uint32_t*>(mbar + 2);
-    int* landed = reinterpret_cast<int*>(tbase + 1);                    // the slices of this q arrived
+    int* landed = reinterpret_cast<int*>(tbase + 1);  // [2]: the slices of this q arrived, as seen by each issuer
     // staged inputs of one q: [F, Src][mode 0, 1][u, v, w][nz levels], then
     // the wall gradients [mode][GP row 0..3] and the q's row exponents
     double2* sP = reinterpret_cast<double2*>(tcsm + viscous_tc_stage_offset(t));
@@ -864,7 +864,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
         if (threadIdx.x == 0 || threadIdx.x == 32) {
             const bool blkO = threadIdx.x == 32;
             const int ld = tc_mbar_wait(&mbar[1], par, 1 << 22) ? 1 : 0;
-            if (!blkO) *landed = ld;
+            landed[blkO ? 1 : 0] = ld;
             if (ld && !ops.tc_stall) {
                 // descriptors differ only in their start address (16-byte
                 // units in the low field; a K offset of k elements is k/8
@@ -893,7 +893,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
         }
         // (f) combine the accumulators of each row
         const bool done =
-            __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && *landed;
+            __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && landed[0] && landed[1];
         tc_fence_after();
         if (!done) {
             if (threadIdx.x == 0) {
@@ -901,7 +901,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                 // the slices' bulk copies and the MMAs of this q may still be in
                 // flight: give each a second bounded wait before the shared
                 // memory and the TMEM columns they write are released
-                if (!*landed) tc_mbar_wait(&mbar[1], par, 1 << 22);
+                if (!landed[0] || !landed[1]) tc_mbar_wait(&mbar[1], par, 1 << 22);
                 tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22);
             }
             ok = false;
@@ -1054,7 +1054,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     int* sF = sE + m8;                                                  // column exponents
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcVortCols);     // [0] MMAs done, [1] D1 landed
     uint32_t* tbase = reinterpret_cast<uint32_t*>(mbar + 2);
-    int* landed = reinterpret_cast<int*>(tbase + 1);
+    int* landed = reinterpret_cast<int*>(tbase + 1);  // [2]: the D1 image arrived, as seen by each issuer
     // staged input columns of one tile: [mode][field][nz]
     double2* sP = reinterpret_cast<double2*>(tcsm + dz_tc_stage_offset(t));
     const bool staged = dz_tc_staged(t, nz);
@@ -1068,7 +1068,7 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
     if (tid == 0) {
         tc_mbar_init(&mbar[0], 2);  // two commits per tile: the E and the O issuer
         tc_mbar_init(&mbar[1]);
-        *landed = 0;
+        landed[0] = landed[1] = 0;
     }
     tc_fence_proxy();
     tc_fence_before();
@@ -1174,10 +1174,10 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         // thread 32 (independent TMEM columns), each committing to mbar[0]
         if (tid == 0 || tid == 32) {
             const bool blkO = tid == 32;
-            int ld = *landed;
+            int ld = landed[blkO ? 1 : 0];
             if (tile == tile0) {
                 ld = tc_mbar_wait(&mbar[1], 0, 1 << 22) ? 1 : 0;
-                if (!blkO) *landed = ld;
+                landed[blkO ? 1 : 0] = ld;
             }
             if (ld && !ops.tc_stall) {
                 // the descriptors differ only in their start address (16-byte
@@ -1203,14 +1203,14 @@ __device__ __forceinline__ void dz_tc_body(const GridDev& g, const Ops& ops, con
         // (f) combination: warps w and w + 4k share TMEM lane quadrant w % 4;
         // warp group w / 4 takes every ngrp-th block of 8 of the 32 columns
         const bool done =
-            __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && *landed;
+            __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && landed[0] && landed[1];
         tc_fence_after();
         if (!done) {
             if (tid == 0) {
                 atomicExch(err, 1);
                 // second bounded waits for copies and MMAs still in flight
                 // (as in viscous_tc_body) before shared memory and TMEM go
-                if (!*landed) tc_mbar_wait(&mbar[1], 0, 1 << 22);
+                if (!landed[0] || !landed[1]) tc_mbar_wait(&mbar[1], 0, 1 << 22);
                 tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22);
             }
             break;
