@@ -189,14 +189,9 @@ __device__ __forceinline__ int tc_exponent(unsigned long long absbits) {
 // Exact FP32 integer (|v| < 2^22) to int.
 __device__ __forceinline__ int tc_f2i(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
 
-// Adds class c's accumulator to the combination T (see the header comment).
-__device__ __forceinline__ long long tc_class_term(int c, float v) {
-    const long long d = (long long)tc_f2i(v);
-    return c < kTcClasses - 1 ? d * (1LL << (7 * (kTcClasses - 2 - c))) : (d + 64) >> 7;
-}
-
 // The whole combination T of one output from its 8 class accumulators (as
-// raw TMEM words), the same integer as the sum of tc_class_term: adjacent
+// raw TMEM words), T = sum_{c<=6} D_c 128^(6-c) + round(D_7 / 128) with
+// D_c = tc_f2i of class c (see the header comment): adjacent
 // classes pair up exactly in 32 bits (|D_c 128 + D_c+1| < 2^30), so only
 // three 64-bit steps remain.
 __device__ __forceinline__ long long tc_combine8(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, uint32_t w4,
@@ -292,31 +287,6 @@ __device__ __forceinline__ bool tc_mbar_wait(uint64_t* mbar, uint32_t parity, in
             : "r"(tc_smem_u32(mbar)), "r"(parity));
     }
     return done != 0;
-}
-
-// 16 consecutive FP32 accumulator columns of this thread's TMEM lane (the
-// warp reads lanes 32*(warp%4) .. +31).
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// 8 consecutive FP32 accumulator columns of this thread's TMEM lane.
-__device__ __forceinline__ void tc_ld8(uint32_t taddr, float* v) {
-    uint32_t r[8];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // TMEM loads issued back to back with one wait (tc_ld_wait) for all of them:
