@@ -548,21 +548,25 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //  (a) the lanes of the last warp start bulk copies of the operator's digit
 //      slices into blocks E (Ge) and O (Go) of each slice (the K padding stays
 //      zero);
-//  (b) meanwhile the folded right-hand sides are formed in FP64 (viscous_rhs_cn)
-//      from the q's inputs staged in shared memory: the 2 x 3 columns of u, v, w
-//      and of the sources, copied with cp.async while the previous q ran
-//      (c)-(g), so the strided column reads (one 16-byte value per level, a
-//      plane apart) overlap that q's tensor-core work,
+//  (b) meanwhile the weight-free folded right-hand sides are formed in FP64
+//      (viscous_rhs_cn_half; the operator carries 2 w_j) from the q's inputs
+//      staged in shared memory: the 2 x 3 columns of u, v, w and of the
+//      sources, the wall gradients and the row exponents, copied with
+//      cp.async while the previous q ran (c)-(g), so the strided column reads
+//      (one 16-byte value per level, a plane apart) overlap that q's
+//      tensor-core work,
 //  (c) each column gets its power-of-two scale and (d) its digits, two K
 //      rows of one column per thread (tc_digit_pairs);
-//  (e) one thread issues, per digit slice sa of the operator, the K-steps of
-//      block E (even rows: right-hand-side rows [0, ke)) and of block O (odd
-//      rows: [ke, kt)), each against right-hand-side digit slices
-//      0 .. 7-sa side by side (N = 16 (8-sa)), accumulated into the
+//  (e) thread 0 for block E (even rows: right-hand-side rows [0, ke)) and
+//      thread 32 for block O (odd rows: [ke, kt)) issue, per digit slice sa
+//      of the operator, the block's K-steps against right-hand-side digit
+//      slices 0 .. 7-sa side by side (N = 16 (8-sa)), accumulated into the
 //      weight-class columns sa .. 7 of that block's TMEM region;
-//  (f) every row's 8 class accumulators are combined in 64-bit integers and
-//      scaled to FP64;
-//  (g) the outputs F* = x - f are written (wall values at the walls).
+//  (f) every row's 8 class accumulators are combined into the 64-bit integer
+//      T (tc_combine8);
+//  (g) the outputs F* = x - f are formed in integers from T of the even and
+//      odd rows (which share an exponent) and written (wall values at the
+//      walls).
 // (t - round(f 2^-E)) 2^E: an integer result t at the scale 2^E minus an
 // FP64 value f, exactly in integers but for the rounding of f to that scale
 // and of the final conversion; falls back to the FP64 difference where f is
