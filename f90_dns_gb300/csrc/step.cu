@@ -1018,10 +1018,11 @@ __global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepPara
 // x re/im; 16, so that two 512-thread CTAs share an SM).
 // Per tile: (b) fold the fields; (c) column scales; (d) digits; (e) per digit
 // slice sa of D1, the K-steps of block E (De: even outputs from the odd
-// inputs) and block O (Do: odd outputs from the even inputs) against the
-// right-hand-side digit slices 0..7-sa side by side, N = 16 (8-sa), into 8
-// weight-class accumulators per block (256 TMEM columns); (f) int64
-// combination -> D1.f in FP64; (g) Op::out_level per level.
+// inputs; issued by thread 0) and block O (Do: odd outputs from the even
+// inputs; thread 32) against the right-hand-side digit slices 0..7-sa side
+// by side, N = 16 (8-sa), into 8 weight-class accumulators per block (256
+// TMEM columns); (f) int64 combination -> D1.f in FP64; (g) Op::out_level
+// per level.
 constexpr int kTcVortCols = 16;  // right-hand-side columns per tile (2 CTAs of 512 threads per SM)
 constexpr int kTcVortModes = kTcVortCols / 4;  // modes per tile: u, v x re, im
 constexpr int kTcCorrModes = kTcVortCols / 2;  // modes per tile: phi x re, im
