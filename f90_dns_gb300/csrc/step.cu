@@ -1567,8 +1567,9 @@ __device__ __forceinline__ void pressure_body(GridDev g, Ops ops, StepParams sp,
 // in 53-bit fixed point before its even/odd fold (B = round(b 2^(54 - f_c)),
 // one power of two 2^(f_c - 1) >= its largest |re|, |im|, so the exact integer
 // fold stays within 2^54), and each row's products are summed exactly and
-// rounded once: x_k = S 2^(e_k + f_c - 112), within 2^-55 of the product of
-// the row and column scales.  The exact products are 32-bit multiply-adds
+// rounded once: x_k = S 2^(e_k + f_c - 112), with the operands' roundings
+// (2^-55 of the column scale, 2^-59 of the row scale per term) and one final
+// rounding of 2^-57 of their product: an FP64 dot product's bound.  The exact products are 32-bit multiply-adds
 // into 64-bit partial sums: A = a1 2^29 + a0, B = b1 2^27 + b0 (a0 in
 // [0, 2^29), b0 in [0, 2^27)), four limb products below 2^56 each, so the
 // partial sums of up to 65 terms stay below 2^63 and are combined in 128 bits

@@ -115,3 +115,52 @@ def test_limb_products_exact_up_to_65_terms():
         A = [2**58] * n
         B = [-2**54] * n
         assert limb_dot(A, B) == sum(a * b for a, b in zip(A, B))
+
+
+def _exponent(x_max):
+    """tc_exponent: the smallest f with |x| < 2^f for the largest |x| (0 if zero)."""
+    if x_max == 0.0:
+        return 0
+    m, e = np.frexp(x_max)  # x = m 2^e, 0.5 <= m < 1
+    return int(e)
+
+
+def _fixed(x, f, bits):
+    """tc_fixed_bits: round(x 2^(bits - f)), ties away from zero, exactly."""
+    from fractions import Fraction
+    v = Fraction(x) * Fraction(2) ** (bits - f)
+    a = abs(v)
+    r = int(a + Fraction(1, 2)) if a.denominator != 1 else int(a)
+    return r if v >= 0 else -r
+
+
+def test_fixed_point_solve_error_bound():
+    """The fixed-point Poisson solve restated (k_fixed_rows, pressure_solve_body):
+    58-bit rows with per-row exponents, a 54-bit column with one exponent over
+    its re and im parts (one more for the exact even/odd fold), exact products,
+    T = round(S / 2^56).  The error of every output is bounded by the operand
+    roundings (half a unit of 2^(f-54) per column entry times |G_kj|, half a
+    unit of 2^(e-58) per row entry times |b_j|) and the one final rounding:
+    the bound of an FP64 dot product, normwise."""
+    from fractions import Fraction
+    rng = np.random.default_rng(5)
+    for n in (9, 33, 65):
+        M = rng.standard_normal((n, n)) + n * np.eye(n)
+        G = np.linalg.inv(M @ M.T)  # a symmetric positive inverse, like the Poisson blocks
+        b = rng.standard_normal(n) * 10.0 ** rng.uniform(-3, 3)
+        f = _exponent(float(np.max(np.abs(b)))) + 1
+        B = [_fixed(v, f, 54) for v in b]
+        assert all(abs(x) <= 2**54 for x in B)
+        for k in range(n):
+            row = G[k]
+            e = _exponent(float(np.max(np.abs(row))))
+            A = [_fixed(v, e, 58) for v in row]
+            assert all(abs(x) <= 2**58 for x in A)
+            S = sum(a * c for a, c in zip(A, B))
+            T = (S + 2**55) >> 56
+            x = Fraction(T) * Fraction(2) ** (e + f - 56)
+            exact = sum(Fraction(float(g)) * Fraction(float(v)) for g, v in zip(row, b))
+            bound = (sum(Fraction(abs(float(g))) for g in row) * Fraction(2) ** (f - 55)
+                     + sum(abs(c) for c in B) * Fraction(2) ** (f - 54) * Fraction(2) ** (e - 59)
+                     + Fraction(2) ** (e + f - 57))
+            assert abs(x - exact) <= bound, (n, k)
