@@ -548,15 +548,15 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //  (a) the lanes of the last warp start bulk copies of the operator's digit
 //      slices into blocks E (Ge) and O (Go) of each slice (the K padding stays
 //      zero);
-//  (b) meanwhile the weight-free folded right-hand sides are formed in FP64
+//  (b) the weight-free folded right-hand sides are formed in FP64
 //      (viscous_rhs_cn_half; the operator carries 2 w_j) from the q's inputs
 //      staged in shared memory: the 2 x 3 columns of u, v, w and of the
 //      sources, the wall gradients and the row exponents, copied with
-//      cp.async while the previous q ran (c)-(g), so the strided column reads
-//      (one 16-byte value per level, a plane apart) overlap that q's
-//      tensor-core work,
-//  (c) each column gets its power-of-two scale and (d) its digits, two K
-//      rows of one column per thread (tc_digit_pairs);
+//      cp.async an operator index ahead, so the strided column reads (one
+//      16-byte value per level, a plane apart) overlap earlier work; each
+//      column's power-of-two scale comes from the largest key (tc_key) of its
+//      values, a warp reduction and one shared atomic per column and warp;
+//  (d) the digits, two K rows of one column per thread (tc_digit_pairs);
 //  (e) thread 0 for block E (even rows: right-hand-side rows [0, ke)) and
 //      thread 32 for block O (odd rows: [ke, kt)) issue, per digit slice sa
 //      of the operator, the block's K-steps against right-hand-side digit
@@ -567,6 +567,16 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //  (g) the outputs F* = x - f are formed in integers from T of the even and
 //      odd rows (which share an exponent) and written (wall values at the
 //      walls).
+// Software pipeline over the CTA's q: while the MMAs of q run, one pass of the
+// CTA writes the outputs (g) of q - 1 and forms the right-hand sides (b) of
+// q + 1 (item for item in the same shared-memory slots: each thread reads its
+// results of q - 1 before it writes its right-hand sides of q + 1); once the
+// MMAs are done, the operator copy (a) of q + 1 starts and the combination
+// (f) of q runs beside the digits (d) of q + 1.  Two barriers per q.  The
+// right-hand sides and results alternate between two buffers, the column keys
+// rotate through three, the staged inputs through two (the wall gradients
+// and row exponents, which the outputs still read, through four); the state
+// values that (g) subtracts stay in registers from (b), two sets in turn.
 // (t - round(f 2^-E)) 2^E: an integer result t at the scale 2^E minus an
 // FP64 value f, exactly in integers but for the rounding of f to that scale
 // and of the final conversion; falls back to the FP64 difference where f is
@@ -640,33 +650,62 @@ __host__ __device__ inline size_t tc_oshift_pad(const TcBlocks& bl) {
 }
 __host__ __device__ inline size_t viscous_tc_pad(const TcGeom& t) { return tc_oshift_pad(tc_blocks(t, false)); }
 
+// Buffers of the viscous tensor-core kernel's two schedules (below): right-
+// hand sides / results kR, column keys kK, staged input columns kP, staged
+// wall gradients and row exponents kG.
+template <bool kPipe>
+struct VtcBufs {
+    static constexpr int kR = kPipe ? 2 : 1, kK = kPipe ? 3 : 2, kP = kPipe ? 2 : 1, kG = kPipe ? 4 : 2;
+};
+
 // Byte offset of the staged inputs in the viscous tensor-core kernel's shared
-// memory: after the digit slices, right-hand-side digits, results, column
-// exponents, barriers, TMEM address and arrival flag (16-byte aligned).
+// memory: after the digit slices, right-hand-side digits, the right-hand-side
+// / result buffers, the column keys, barriers, TMEM address and flags
+// (16-byte aligned).
+template <bool kPipe>
 __host__ __device__ inline size_t viscous_tc_stage_offset(const TcGeom& t) {
+    using B = VtcBufs<kPipe>;
     const size_t b = viscous_tc_pad(t) + (size_t)kTcSlices * (tc_blocks(t, false).a + kTcN * t.kt) * sizeof(__half) +
-                     (size_t)kTcN * t.m8 * sizeof(double) + kTcN * sizeof(int) + 2 * sizeof(uint64_t) + 16;
+                     (size_t)B::kR * kTcN * t.m8 * sizeof(double) + B::kK * kTcN * sizeof(unsigned) +
+                     2 * sizeof(uint64_t) + 16;
     return (b + 15) / 16 * 16;
 }
 
 // Dynamic shared memory one CTA may use (the sm_100-family opt-in maximum).
 constexpr size_t kTcSmemMax = 227 * 1024;
 
-// Whether the staged inputs (12 columns of nz values) still fit beside the
-// operands: true up to nz = 127; at nz = 129 the kernel reads its inputs
-// from global memory in (b) instead.
-// Staged inputs of one q: 12 columns of nz values (F and the sources of both
-// modes' u, v, w), and, in two buffers by the parity of q (the next q's are
-// copied while the current one's outputs still read them), the wall
-// pressure gradients of both modes (8 values) and the q's m8 row exponents.
+// Staged inputs: kP buffers of one q's 12 columns of nz values (F and the
+// sources of both modes' u, v, w), and kG of the wall pressure gradients of
+// both modes (8 values) and the q's m8 row exponents.  Where they do not fit
+// beside the operands (the pipelined schedule at nz >= 127, the phased one at
+// nz = 129) the kernel reads its inputs from global memory in (b) and (g).
+template <bool kPipe>
 __host__ __device__ inline size_t viscous_tc_stage_bytes(const TcGeom& t, int nz) {
-    return (size_t)(12 * nz + 16) * sizeof(double2) + (size_t)2 * t.m8 * sizeof(int);
+    using B = VtcBufs<kPipe>;
+    return (size_t)(B::kP * 12 * nz + 8 * B::kG) * sizeof(double2) + (size_t)B::kG * t.m8 * sizeof(int);
 }
 
+template <bool kPipe>
 __host__ __device__ inline bool viscous_tc_staged(const TcGeom& t, int nz) {
-    return viscous_tc_stage_offset(t) + viscous_tc_stage_bytes(t, nz) <= kTcSmemMax;
+    return viscous_tc_stage_offset<kPipe>(t) + viscous_tc_stage_bytes<kPipe>(t, nz) <= kTcSmemMax;
 }
 
+template <bool kPipe>
+__host__ __device__ inline size_t viscous_tc_smem_nz(int nz) {
+    const TcGeom t = tc_geom(nz);
+    return viscous_tc_stage_offset<kPipe>(t) + (viscous_tc_staged<kPipe>(t, nz) ? viscous_tc_stage_bytes<kPipe>(t, nz) : 0);
+}
+
+// The schedule: phased where two CTAs share an SM (228 KB of shared memory,
+// 1 KB of it reserved per CTA), whose phases then fill each other's waits;
+// pipelined where one CTA has the SM to itself (nz >= 81).  Measured at
+// 128x128x65 (phased): 170 us phased, 174 us pipelined; at 512x384x129: 6.14
+// ms phased, 5.33 ms pipelined.
+__host__ __device__ inline bool viscous_tc_pipelined(int nz) {
+    return 2 * (viscous_tc_smem_nz<false>(nz) + 1024) > 228 * 1024;
+}
+
+template <bool kPipe>
 __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops, const StepParams& sp,
                                                 const Fields& F, const Fields& Src,
                                                 const double2* __restrict__ GP,
@@ -679,20 +718,27 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     const int b_halves = kTcN * t.kt;
     __half* sA = reinterpret_cast<__half*>(tcsm + viscous_tc_pad(t));
     __half* sB = sA + kTcSlices * bl.a;
-    double* sR = reinterpret_cast<double*>(sB + kTcSlices * b_halves);  // [kTcN][m8]: rhs, then results
-    int* sF = reinterpret_cast<int*>(sR + kTcN * m8);                   // column exponents
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(sF + kTcN);            // [0] MMAs done, [1] slices landed
+    using Bf = VtcBufs<kPipe>;
+    double* sR2 = reinterpret_cast<double*>(sB + kTcSlices * b_halves);  // [kR][kTcN][m8]: rhs, then results
+    unsigned* sK3 = reinterpret_cast<unsigned*>(sR2 + Bf::kR * kTcN * m8);  // [kK][kTcN] column keys
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sK3 + Bf::kK * kTcN);      // [0] MMAs done, [1] slices landed
     uint32_t* tbase = reinterpret_cast<uint32_t*>(mbar + 2);
     int* landed = reinterpret_cast<int*>(tbase + 1);  // [2]: the slices of this q arrived, as seen by each issuer
-    // staged inputs of one q: [F, Src][mode 0, 1][u, v, w][nz levels], then
-    // the wall gradients [mode][GP row 0..3] and the q's row exponents
-    double2* sP = reinterpret_cast<double2*>(tcsm + viscous_tc_stage_offset(t));
-    double2* sGP2 = sP + 12 * nz;                      // [2][mode][4]
-    int* sEq2 = reinterpret_cast<int*>(sGP2 + 16);      // [2][m8]
+    int* nextc = landed + 2;                          // the slices of the next q were started
+    // staged inputs: [kP][F, Src][mode 0, 1][u, v, w][nz levels], then the
+    // wall gradients [kG][mode][GP row 0..3] and row exponents [kG][m8]
+    double2* sP2 = reinterpret_cast<double2*>(tcsm + viscous_tc_stage_offset<kPipe>(t));
+    double2* sGP4 = sP2 + Bf::kP * 12 * nz;
+    int* sEq4 = reinterpret_cast<int*>(sGP4 + 8 * Bf::kG);
+    // the buffers of the operator index q0 + rel
+    auto rslot = [&](int rel) { return sR2 + (size_t)(rel % Bf::kR) * kTcN * m8; };
+    auto kslot = [&](int rel) { return sK3 + (rel % Bf::kK) * kTcN; };
+    auto pslot = [&](int rel) { return sP2 + (size_t)(rel % Bf::kP) * 12 * nz; };
     {
         uint4* z = reinterpret_cast<uint4*>(sA);
         const int n16 = kTcSlices * (bl.a + b_halves) / 8;
         for (int i = threadIdx.x; i < n16; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+        if (threadIdx.x < Bf::kK * kTcN) sK3[threadIdx.x] = 0u;
     }
     if (threadIdx.x < 32) tc_alloc(tbase, 2 * kTcDCols);
     if (threadIdx.x == 0) {
@@ -709,46 +755,51 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     const size_t qh = tc_q_halves(t);
     const int nbe = t.e8 >> 3, nbo = t.o8 >> 3;
     const int ncore = t.ncore_e + t.ncore_o;
-    const int nv = he + ho;  // valid rows / K indices
-    const bool staged = viscous_tc_staged(t, nz);
-    // cp.async of the inputs of operator index q into sP (both modes' columns
-    // of u, v, w and of the sources; a missing second mode is not read): one
-    // warp per column, its lanes over the levels
+    const bool staged = viscous_tc_staged<kPipe>(t, nz);
+    const int nitems = 6 * he;  // (b) and (g): (mode, component, level pair)
+    struct QInfo {
+        int kya, kx, nmode;
+    };
+    auto qinfo = [&](int q) {
+        QInfo r;
+        r.kya = q / g.nxhp;
+        r.kx = q - r.kya * g.nxhp;
+        r.nmode = (r.kya > 0 && 2 * r.kya != g.ny) ? 2 : 1;
+        return r;
+    };
+    // cp.async of the inputs of operator index q (both modes' columns of u, v,
+    // w and of the sources; a missing second mode is not read): one warp per
+    // column, its lanes over the levels; one commit group per q, empty past
+    // the CTA's last q or when the inputs are not staged
     auto stage = [&](int q) {
-        if (!staged) return;
-        const int kya = q / g.nxhp, kx = q - kya * g.nxhp;
-        const int nmode = (kya > 0 && 2 * kya != g.ny) ? 2 : 1;
-        const int lane = threadIdx.x & 31;
-        for (int r = threadIdx.x >> 5; r < 2 * nmode * 3; r += blockDim.x >> 5) {
-            const int comp = r % 3, r2 = r / 3;
-            const int mi = r2 % nmode, fld = r2 / nmode;
-            const int m = (mi ? g.ny - kya : kya) * g.nxhp + kx;
-            const double2* src = (fld ? fptr(Src, comp) : fptr(F, comp)) + m;
-            double2* dst = sP + (size_t)((fld * 2 + mi) * 3 + comp) * nz;
-            for (int z = lane; z < nz; z += 32) cp_async16(dst + z, src + (size_t)z * g.nm);
-        }
-        const int j = threadIdx.x, b = (q - q0) & 1;
-        if (j < 4 * nmode) {  // the wall gradients GP[4][nm] of the modes
-            const int mi = j >> 2, w = j & 3;
-            const int m = (mi ? g.ny - kya : kya) * g.nxhp + kx;
-            cp_async16(sGP2 + 8 * b + 4 * mi + w, GP + (size_t)w * g.nm + m);
-        } else if (j >= 32 && j < 32 + m8 / 4) {  // the row exponents, 4 per copy
-            cp_async16(sEq2 + b * m8 + 4 * (j - 32), ops.tcE + (size_t)q * m8 + 4 * (j - 32));
+        if (staged && q < q1) {
+            const int rel = q - q0;
+            const QInfo qi = qinfo(q);
+            double2* sP = pslot(rel);
+            const int lane = threadIdx.x & 31;
+            for (int r = threadIdx.x >> 5; r < 2 * qi.nmode * 3; r += blockDim.x >> 5) {
+                const int comp = r % 3, r2 = r / 3;
+                const int mi = r2 % qi.nmode, fld = r2 / qi.nmode;
+                const int m = (mi ? g.ny - qi.kya : qi.kya) * g.nxhp + qi.kx;
+                const double2* src = (fld ? fptr(Src, comp) : fptr(F, comp)) + m;
+                double2* dst = sP + (size_t)((fld * 2 + mi) * 3 + comp) * nz;
+                for (int z = lane; z < nz; z += 32) cp_async16(dst + z, src + (size_t)z * g.nm);
+            }
+            const int j = threadIdx.x, b = rel % Bf::kG;
+            if (j < 4 * qi.nmode) {  // the wall gradients GP[4][nm] of the modes
+                const int mi = j >> 2, w = j & 3;
+                const int m = (mi ? g.ny - qi.kya : qi.kya) * g.nxhp + qi.kx;
+                cp_async16(sGP4 + 8 * b + 4 * mi + w, GP + (size_t)w * g.nm + m);
+            } else if (j >= 32 && j < 32 + m8 / 4) {  // the row exponents, 4 per copy
+                cp_async16(sEq4 + b * m8 + 4 * (j - 32), ops.tcE + (size_t)q * m8 + 4 * (j - 32));
+            }
         }
         cp_async_commit();
     };
-    if (q0 < q1) stage(q0);
-    bool ok = true;
-    for (int q = q0; q < q1 && ok; ++q) {
-        const uint32_t par = (uint32_t)((q - q0) & 1);
-        const double2* sGP = sGP2 + 8 * par;  // this q's staged wall gradients and row exponents
-        const int* sEq = sEq2 + par * m8;
-        cp_async_wait_all();
-        __syncthreads();  // this q's staged inputs, from every thread's copies
-        // (a) digit slices of the operator: per digit, one copy per 8-row
-        // group (its nonzero core matrices are contiguous in the compact store
-        // and in the K-major block), issued by the lanes of the last warp (the
-        // one with the least right-hand-side work below)
+    // (a) digit slices of the operator of q: per digit, one copy per 8-row
+    // group (its nonzero core matrices are contiguous in the compact store and
+    // in the K-major block), issued by the lanes of the last warp
+    auto copy_op = [&](int q) {
         if ((int)threadIdx.x >= (int)blockDim.x - 32) {
             const int lane = threadIdx.x & 31;
             if (lane == 0) tc_mbar_expect(&mbar[1], (uint32_t)(qh * sizeof(__half)));
@@ -766,107 +817,212 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                                 ss + (size_t)(t.ncore_e + (gm - nbe) * nbo) * 64, nbo * 128, &mbar[1]);
             }
         }
-        // (b) folded right-hand sides: column 6 mi + 2 comp + (0 re, 1 im)
-        const int kya = q / g.nxhp, kx = q - kya * g.nxhp;
-        const int nmode = (kya > 0 && 2 * kya != g.ny) ? 2 : 1;
-        // the state values at the item's two levels, kept for (g) (items
-        // i = threadIdx.x + p blockDim.x, p < 2, hold theirs in registers)
-        double2 keep1[2], keep2[2];
-#pragma unroll
-        for (int p = 0; p < 2; ++p) keep1[p] = keep2[p] = make_double2(0.0, 0.0);
-        for (int i = threadIdx.x, p = 0; i < 6 * he; i += blockDim.x, ++p) {
-            const int mi = i / (3 * he);
-            const int r = i - mi * 3 * he;
-            const int comp = r / he, k = r - comp * he;
-            double2 fe = make_double2(0.0, 0.0), fo = fe;
-            if (mi < nmode) {
-                const int ky = mi ? g.ny - kya : kya;
-                const int m = ky * g.nxhp + kx;
-                // the F and source columns of this mode: staged, or read from
-                // global memory one level (a plane) apart
-                const size_t st = staged ? 1 : (size_t)g.nm;
-                const double2* fc = staged ? sP + (size_t)(mi * 3 + comp) * nz : fptr(F, comp) + m;
-                const double2* sc = staged ? sP + (size_t)((2 + mi) * 3 + comp) * nz : fptr(Src, comp) + m;
-                const double2 f1 = fc[0], fn = fc[(size_t)(nz - 1) * st];
-                const double2 v1 = fc[(size_t)k * st], v2 = k < ho ? fc[(size_t)(nz - 1 - k) * st] : v1;
-                if (p < 2) {
-                    // (p is 0 or 1 here whenever 6 he <= 2 blockDim.x)
-                    if (p == 0) { keep1[0] = v1; keep2[0] = v2; }
-                    else { keep1[1] = v1; keep2[1] = v2; }
+    };
+    // (b) item i of q: the folded right-hand sides of column pair 6 mi + 2 comp
+    // + (0 re, 1 im) at level pair k into the q's buffer; returns the state
+    // values at the two levels (kept for (g)) and the keys of the values
+    auto rhs_item = [&](int q, const QInfo& qi, int i, double2& v1o, double2& v2o, unsigned& kre, unsigned& kim) {
+        const int rel = q - q0;
+        const double2* sP = pslot(rel);
+        const double2* sGP = sGP4 + 8 * (rel % Bf::kG);
+        double* sR = rslot(rel);
+        const int mi = i / (3 * he);
+        const int r = i - mi * 3 * he;
+        const int comp = r / he, k = r - comp * he;
+        double2 fe = make_double2(0.0, 0.0), fo = fe;
+        if (mi < qi.nmode) {
+            const int ky = mi ? g.ny - qi.kya : qi.kya;
+            const int m = ky * g.nxhp + qi.kx;
+            // the F and source columns of this mode: staged, or read from
+            // global memory one level (a plane) apart
+            const size_t st = staged ? 1 : (size_t)g.nm;
+            const double2* fc = staged ? sP + (size_t)(mi * 3 + comp) * nz : fptr(F, comp) + m;
+            const double2* sc = staged ? sP + (size_t)((2 + mi) * 3 + comp) * nz : fptr(Src, comp) + m;
+            const double2 f1 = fc[0], fn = fc[(size_t)(nz - 1) * st];
+            const double2 v1 = fc[(size_t)k * st], v2 = k < ho ? fc[(size_t)(nz - 1 - k) * st] : v1;
+            v1o = v1;
+            v2o = v2;
+            if (k > 0) {  // the wall rows of r are zero
+                // lifting data l = f_wall + 2 bc, bc = -dt dp/dx|wall (u), -dt dp/dy|wall (v), 0 (w)
+                double2 l1 = f1, ln = fn;
+                if (comp < 2) {
+                    const double2 g1 = staged ? sGP[4 * mi + 2 * comp] : GP[(size_t)(2 * comp) * g.nm + m];
+                    const double2 g2 = staged ? sGP[4 * mi + 2 * comp + 1] : GP[(size_t)(2 * comp + 1) * g.nm + m];
+                    const double m2dt = -2.0 * sp.dt;
+                    l1 = make_double2(fma(m2dt, g1.x, f1.x), fma(m2dt, g1.y, f1.y));
+                    ln = make_double2(fma(m2dt, g2.x, fn.x), fma(m2dt, g2.y, fn.y));
                 }
-                if (k > 0) {  // the wall rows of r are zero
-                    // lifting data l = f_wall + 2 bc, bc = -dt dp/dx|wall (u), -dt dp/dy|wall (v), 0 (w)
-                    double2 l1 = f1, ln = fn;
-                    if (comp < 2) {
-                        const double2 g1 = staged ? sGP[4 * mi + 2 * comp] : GP[(size_t)(2 * comp) * g.nm + m];
-                        const double2 g2 = staged ? sGP[4 * mi + 2 * comp + 1] : GP[(size_t)(2 * comp + 1) * g.nm + m];
-                        const double m2dt = -2.0 * sp.dt;
-                        l1 = make_double2(fma(m2dt, g1.x, f1.x), fma(m2dt, g1.y, f1.y));
-                        ln = make_double2(fma(m2dt, g2.x, fn.x), fma(m2dt, g2.y, fn.y));
-                    }
-                    const double2 s1 = sc[(size_t)k * st];
-                    const double2 s2 = k < ho ? sc[(size_t)(nz - 1 - k) * st] : s1;
-                    const Pair rf =
-                        viscous_rhs_cn_half(g, ops, sp, comp, k, m, ky, kx, v1, v2, s1, s2, l1, ln, dpdx);
-                    fe = rf.a;
-                    fo = rf.b;
-                }
-            }
-            const int c0 = 6 * mi + 2 * comp;
-            sR[c0 * m8 + k] = fe.x;
-            sR[(c0 + 1) * m8 + k] = fe.y;
-            if (k < ho) {
-                sR[c0 * m8 + t.e8 + k] = fo.x;
-                sR[(c0 + 1) * m8 + t.e8 + k] = fo.y;
+                const double2 s1 = sc[(size_t)k * st];
+                const double2 s2 = k < ho ? sc[(size_t)(nz - 1 - k) * st] : s1;
+                const Pair rf = viscous_rhs_cn_half(g, ops, sp, comp, k, m, ky, qi.kx, v1, v2, s1, s2, l1, ln, dpdx);
+                fe = rf.a;
+                fo = rf.b;
             }
         }
-        __syncthreads();
-        if (q + 1 < q1) stage(q + 1);  // sP is free again: the next q's inputs arrive during (c)-(g)
-        // (c) column scales, one warp per column
+        const int c0 = 6 * mi + 2 * comp;
+        sR[c0 * m8 + k] = fe.x;
+        sR[(c0 + 1) * m8 + k] = fe.y;
+        kre = tc_key(fe.x);
+        kim = tc_key(fe.y);
+        if (k < ho) {
+            sR[c0 * m8 + t.e8 + k] = fo.x;
+            sR[(c0 + 1) * m8 + t.e8 + k] = fo.y;
+            kre = max(kre, tc_key(fo.x));
+            kim = max(kim, tc_key(fo.y));
+        }
+    };
+    // (g) item i of q: F* = x - f at the interior levels, the wall values at
+    // the walls: rows k of both blocks share the exponent e_k, so x_k - f_k =
+    // (Te + To - F) 2^E and x_nz-1-k - f_nz-1-k = (Te - To - F') 2^E with
+    // E = e_k + f_c - 52 and F = round(f 2^-E), exactly in integers but for
+    // that one rounding of f and the final conversion; v1, v2: the state
+    // values at levels k, nz-1-k (read again from F past the kept items)
+    auto out_item = [&](int q, const QInfo& qi, int i, int p, double2 v1, double2 v2) {
+        const int rel = q - q0;
+        const double2* sGP = sGP4 + 8 * (rel % Bf::kG);
+        const int* sEq = sEq4 + (rel % Bf::kG) * m8;
+        const double* sR = rslot(rel);
+        const unsigned* sK = kslot(rel);
+        const int mi = i / (3 * he);
+        const int r = i - mi * 3 * he;
+        const int comp = r / he, k = r - comp * he;
+        const int ky = mi ? g.ny - qi.kya : qi.kya;
+        const int m = ky * g.nxhp + qi.kx;
+        const int c0 = 6 * mi + 2 * comp;
+        double2* oc = fptr(Out, comp);
+        const size_t o1 = (size_t)k * g.nm + m, o2 = (size_t)(nz - 1 - k) * g.nm + m;
+        if (k == 0) {
+            double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
+            if (comp < 2) {
+                const double2 g1 = staged ? sGP[4 * mi + 2 * comp] : GP[(size_t)(2 * comp) * g.nm + m];
+                const double2 g2 = staged ? sGP[4 * mi + 2 * comp + 1] : GP[(size_t)(2 * comp + 1) * g.nm + m];
+                bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
+                bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
+            }
+            oc[o1] = bc1;
+            oc[o2] = bc2;
+            return;
+        }
+        if (p >= 2) {
+            const double2* fc = fptr(F, comp);
+            v1 = fc[o1];
+            v2 = k < ho ? fc[o2] : v1;
+        }
+        const int e = staged ? sEq[k] : __ldg(&ops.tcE[(size_t)q * m8 + k]);
+        double o1x, o1y, o2x = 0.0, o2y = 0.0;
         {
-            const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-            for (int c = w; c < 12; c += blockDim.x >> 5) {
-                unsigned long long mx = 0;
-                for (int k = l; k < nv; k += 32) {
-                    const int row = k < he ? k : t.e8 + (k - he);
-                    const unsigned long long ab =
-                        (unsigned long long)__double_as_longlong(sR[c * m8 + row]) & 0x7FFFFFFFFFFFFFFFULL;
-                    mx = ab > mx ? ab : mx;
-                }
+            const int E = e + tc_exponent_key(sK[c0]) - 52;
+            const long long te = __double_as_longlong(sR[c0 * m8 + k]);
+            const long long to = k < ho ? __double_as_longlong(sR[c0 * m8 + t.e8 + k]) : 0;
+            o1x = tc_sub_scaled(te + to, v1.x, E);
+            if (k < ho) o2x = tc_sub_scaled(te - to, v2.x, E);
+        }
+        {
+            const int E = e + tc_exponent_key(sK[c0 + 1]) - 52;
+            const long long te = __double_as_longlong(sR[(c0 + 1) * m8 + k]);
+            const long long to = k < ho ? __double_as_longlong(sR[(c0 + 1) * m8 + t.e8 + k]) : 0;
+            o1y = tc_sub_scaled(te + to, v1.y, E);
+            if (k < ho) o2y = tc_sub_scaled(te - to, v2.y, E);
+        }
+        oc[o1] = make_double2(o1x, o1y);
+        if (k < ho) oc[o2] = make_double2(o2x, o2y);
+    };
+    // the state values of items p = 0, 1 (i = threadIdx.x + p blockDim.x):
+    // kA for the q whose outputs the next pass writes, kB (pipelined) for the
+    // one after
+    double2 kA1[2], kA2[2], kB1[2], kB2[2];
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
-                    mx = v > mx ? v : mx;
+    for (int p = 0; p < 2; ++p) kA1[p] = kA2[p] = kB1[p] = kB2[p] = make_double2(0.0, 0.0);
+    // one pass of the CTA: the outputs (g) of qg (if qg >= q0) and the
+    // right-hand sides (b) of qb (if qb < q1), item for item, then the column
+    // keys of qb: per warp and column a warp maximum and one shared atomic;
+    // the pipelined schedule then swaps kA and kB
+    auto pass = [&](int qg, int qb) {
+        const QInfo ig = qinfo(max(qg, q0)), ib = qinfo(min(qb, q1 - 1));
+        const bool dog = qg >= q0, dob = qb < q1;
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int p = 0; p * (int)blockDim.x < nitems; ++p) {
+            const int i = threadIdx.x + p * blockDim.x;
+            unsigned kre = 0u, kim = 0u;
+            if (i < nitems) {
+                double2 v1 = make_double2(0.0, 0.0), v2 = v1;
+                if (p == 0) {
+                    v1 = kA1[0];
+                    v2 = kA2[0];
+                } else if (p == 1) {
+                    v1 = kA1[1];
+                    v2 = kA2[1];
                 }
-                if (l == 0) sF[c] = tc_exponent(mx);
+                if (dog && i < ig.nmode * 3 * he) out_item(qg, ig, i, p, v1, v2);
+                if (dob) {
+                    rhs_item(qb, ib, i, v1, v2, kre, kim);
+                    if (p == 0) {
+                        kA1[0] = v1;
+                        kA2[0] = v2;
+                    } else if (p == 1) {
+                        kA1[1] = v1;
+                        kA2[1] = v2;
+                    }
+                }
+            }
+            const int ifirst = w * 32 + p * (int)blockDim.x;
+            if (dob && ifirst < nitems) {  // uniform over the warp
+                const int glast = min(ifirst + 31, nitems - 1) / he;
+                const int mygrp = i < nitems ? i / he : -1;
+                unsigned* sK = kslot(qb - q0);
+                for (int gi = ifirst / he; gi <= glast; ++gi) {  // column pair 2 gi, 2 gi + 1
+                    const unsigned re = __reduce_max_sync(0xffffffffu, mygrp == gi ? kre : 0u);
+                    const unsigned im = __reduce_max_sync(0xffffffffu, mygrp == gi ? kim : 0u);
+                    if (lane == 0) {
+                        atomicMax(&sK[2 * gi], re);
+                        atomicMax(&sK[2 * gi + 1], im);
+                    }
+                }
             }
         }
-        __syncthreads();
-        // (d) digits of the right-hand sides, K rows kk, kk + 1 (kk even) of
-        // one column per thread, one half2 per digit slice: even levels at K
-        // [0, he), odd ones at K [ke, ke + ho); a warp covers the 4 row pairs
-        // of an 8-row group for 8 columns, so its 4-byte stores fall in
-        // distinct shared-memory banks but for columns 8 apart (the bank of
-        // (n, k) in a core matrix is 4 (n mod 8) + (k mod 8)/2)
+        if (kPipe) {
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {  // kA <-> kB
+                const double2 a1 = kA1[p], a2 = kA2[p];
+                kA1[p] = kB1[p];
+                kA2[p] = kB2[p];
+                kB1[p] = a1;
+                kB2[p] = a2;
+            }
+        }
+    };
+    // (d) digits of the right-hand sides of q, K rows kk, kk + 1 (kk even) of
+    // one column per thread, one half2 per digit slice: even levels at K
+    // [0, he), odd ones at K [ke, ke + ho); a warp covers the 4 row pairs of an
+    // 8-row group for 8 columns, so its 4-byte stores fall in distinct
+    // shared-memory banks but for columns 8 apart (the bank of (n, k) in a
+    // core matrix is 4 (n mod 8) + (k mod 8)/2)
+    auto digits = [&](int q) {
+        const int rel = q - q0;
+        const double* sR = rslot(rel);
+        const unsigned* sK = kslot(rel);
         for (int i = threadIdx.x; i < 12 * (t.kt / 2); i += blockDim.x) {
             const int kp = i & 3, cc = i >> 2;
             const int c = cc % 12, kk = (cc / 12) * 8 + 2 * kp;
             const int r0 = tc_k_row(t, kk), r1 = tc_k_row(t, kk + 1);
             if (r0 < 0) continue;  // padding K rows: zeroed once at the start, never written
+            const int f = tc_exponent_key(sK[c]);
             __half2 h[kTcSlices];
-            tc_digit_pairs(tc_fixed(sR[c * m8 + r0], sF[c]), r1 < 0 ? 0 : tc_fixed(sR[c * m8 + r1], sF[c]), h);
+            tc_digit_pairs(tc_fixed(sR[c * m8 + r0], f), r1 < 0 ? 0 : tc_fixed(sR[c * m8 + r1], f), h);
             __half2* dst = reinterpret_cast<__half2*>(sB + tc_core_off(c, kk, t.kt));
 #pragma unroll
             for (int s = 0; s < kTcSlices; ++s) dst[s * (b_halves / 2)] = h[s];
         }
-        tc_fence_proxy();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        // (e) the digit-pair products: block E issued by thread 0, block O by
-        // thread 32 (independent TMEM columns), each committing to mbar[0]
-        if (threadIdx.x == 0 || threadIdx.x == 32) {
-            const bool blkO = threadIdx.x == 32;
+    };
+    // (e) the digit-pair products of q: block E issued by one thread, block O
+    // by one of the next warp (independent TMEM columns; pipelined: the first
+    // lanes of the last two warps, which have the fewest items in the pass
+    // beside the MMAs), each committing to mbar[0] once the operator's slices
+    // landed
+    auto issue = [&](uint32_t par) {
+        const int ie = kPipe ? (int)blockDim.x - 64 : 0, io = ie + 32;
+        if ((int)threadIdx.x == ie || (int)threadIdx.x == io) {
+            const bool blkO = (int)threadIdx.x == io;
             const int ld = tc_mbar_wait(&mbar[1], par, 1 << 22) ? 1 : 0;
             landed[blkO ? 1 : 0] = ld;
             if (ld && !ops.tc_stall) {
@@ -895,104 +1051,137 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
             }
             if (!ops.tc_stall) tc_commit(&mbar[0]);  // also when nothing was issued: the waiters are released
         }
-        // (f) combine the accumulators of each row
-        const bool done =
-            __syncthreads_and(tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22)) && landed[0] && landed[1];
-        tc_fence_after();
-        if (!done) {
-            if (threadIdx.x == 0) {
-                atomicExch(err, 1);
-                // the slices' bulk copies and the MMAs of this q may still be in
-                // flight: give each a second bounded wait before the shared
-                // memory and the TMEM columns they write are released
-                if (!landed[0] || !landed[1]) tc_mbar_wait(&mbar[1], par, 1 << 22);
-                tc_mbar_wait(&mbar[0], par, ops.tc_stall ? 1 << 10 : 1 << 22);
+    };
+    // (f) combine the accumulators of each row of q into its result buffer:
+    // warp w reads TMEM lane quadrant w % 4 (lanes 32 (w % 4) .. +31); block
+    // E's rows are lanes 0 .. e8, block O's lanes 64 .. 64 + o8.  A quadrant
+    // holding rows of one block splits its 12 columns between its two warps
+    // (6 each); one holding rows of both blocks (nz = 129: lanes 64 .. 71 of
+    // E) gives each warp one block.
+    auto combine = [&](int q) {
+        double* sR = rslot(q - q0);
+        const int w = threadIdx.x >> 5;
+        if (w < 8) {
+            const int quad = w & 3, half = w >> 2;
+            const bool hasE = 32 * quad < t.e8;
+            const bool hasO = quad >= 2 && 32 * quad < 64 + t.o8;
+            const int lane = 32 * quad + (threadIdx.x & 31);
+            const uint32_t lanes = tmem + ((uint32_t)(32 * quad) << 16);
+            if (hasE || hasO) {
+                const int blk = (hasE && hasO) ? half : (hasO ? 1 : 0);
+                const bool valid = blk ? (lane >= 64 && lane - 64 < t.o8) : lane < t.e8;
+                const int row = blk ? t.e8 + (lane - 64) : lane;
+                const uint32_t lb = lanes + (uint32_t)(blk * kTcDCols);
+                if (hasE && hasO) {
+                    tc_combine6<0>(lb, sR, m8, row, valid);
+                    tc_combine6<1>(lb, sR, m8, row, valid);
+                } else if (half == 0) {
+                    tc_combine6<0>(lb, sR, m8, row, valid);
+                } else {
+                    tc_combine6<1>(lb, sR, m8, row, valid);
+                }
             }
-            ok = false;
-            break;  // uniform: no TMEM read, no further MMA
         }
-        {
-            // warp w reads TMEM lane quadrant w % 4 (lanes 32 (w % 4) .. +31);
-            // block E's rows are lanes 0 .. e8, block O's lanes 64 .. 64 + o8.
-            // A quadrant holding rows of one block splits its 12 columns
-            // between its two warps (6 each); one holding rows of both blocks
-            // (nz = 129: lanes 64 .. 71 of E) gives each warp one block.
-            const int w = threadIdx.x >> 5;
-            if (w < 8) {
-                const int quad = w & 3, half = w >> 2;
-                const bool hasE = 32 * quad < t.e8;
-                const bool hasO = quad >= 2 && 32 * quad < 64 + t.o8;
-                const int lane = 32 * quad + (threadIdx.x & 31);
-                const uint32_t lanes = tmem + ((uint32_t)(32 * quad) << 16);
-                if (hasE || hasO) {
-                    const int blk = (hasE && hasO) ? half : (hasO ? 1 : 0);
-                    const bool valid = blk ? (lane >= 64 && lane - 64 < t.o8) : lane < t.e8;
-                    const int row = blk ? t.e8 + (lane - 64) : lane;
-                    const uint32_t lb = lanes + (uint32_t)(blk * kTcDCols);
-                    if (hasE && hasO) {
-                        tc_combine6<0>(lb, sR, m8, row, valid);
-                        tc_combine6<1>(lb, sR, m8, row, valid);
-                    } else if (half == 0) {
-                        tc_combine6<0>(lb, sR, m8, row, valid);
-                    } else {
-                        tc_combine6<1>(lb, sR, m8, row, valid);
+    };
+    bool ok = true;
+    const int mlimit = ops.tc_stall ? 1 << 10 : 1 << 22;
+    // a run-out wait: the flag, then a second bounded wait for each of the
+    // slices' bulk copies and the MMAs of q (and the slices of q + 1, if
+    // started) that may still be in flight, before the shared memory and the
+    // TMEM columns they write are released
+    auto timed_out = [&](uint32_t par, bool next) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, 1);
+            if (!landed[0] || !landed[1]) tc_mbar_wait(&mbar[1], par, 1 << 22);
+            tc_mbar_wait(&mbar[0], par, mlimit);
+            if (next) tc_mbar_wait(&mbar[1], par ^ 1u, 1 << 22);
+        }
+    };
+    if (!kPipe) {
+        // phased: per q, (a) + (b) | (d) | (e) | (f) | (g), the staged inputs
+        // of q + 1 arriving during (d)-(g)
+        if (q0 < q1) stage(q0);
+        for (int q = q0; q < q1; ++q) {
+            const int rel = q - q0;
+            const uint32_t par = (uint32_t)(rel & 1);
+            cp_async_wait_all();
+            __syncthreads();  // this q's staged inputs, from every thread's copies
+            copy_op(q);
+            pass(q0 - 1, q);
+            __syncthreads();
+            if (q + 1 < q1) stage(q + 1);  // the staging buffer is free again
+            if (threadIdx.x < kTcN) kslot(rel + 1)[threadIdx.x] = 0u;  // (g) of q - 1 read them last
+            digits(q);
+            tc_fence_proxy();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            issue(par);
+            const bool done = __syncthreads_and(tc_mbar_wait(&mbar[0], par, mlimit)) && landed[0] && landed[1];
+            tc_fence_after();
+            if (!done) {
+                timed_out(par, false);
+                ok = false;
+                break;  // uniform: no TMEM read, no further MMA
+            }
+            combine(q);
+            tc_fence_before();
+            __syncthreads();
+            pass(q, q1);
+            __syncthreads();  // shared buffers are reused by the next q
+        }
+    } else if (q0 < q1) {
+        // pipelined
+        stage(q0);
+        stage(q0 + 1);
+        cp_async_wait_one();  // q0's inputs
+        __syncthreads();
+        copy_op(q0);
+        pass(q0 - 1, q0);
+        __syncthreads();  // q0's right-hand sides and column keys; its staging buffer is free
+        stage(q0 + 2);
+        digits(q0);
+        cp_async_wait_one();  // q0 + 1's inputs
+        tc_fence_proxy();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        for (int q = q0; q < q1; ++q) {
+            const uint32_t par = (uint32_t)((q - q0) & 1);
+            issue(par);
+            // the last warp: as soon as the slices of q have landed and its
+            // MMAs are done, the slices of q + 1 (flagged in *nextc for the
+            // timeout path)
+            if ((int)threadIdx.x >= (int)blockDim.x - 32) {
+                __syncwarp();  // lane 0 has issued its MMAs
+                if ((threadIdx.x & 31) == 0) *nextc = 0;
+                if (q + 1 < q1) {
+                    const bool rdy = tc_mbar_wait(&mbar[1], par, 1 << 22) && tc_mbar_wait(&mbar[0], par, mlimit);
+                    if (__all_sync(0xffffffffu, rdy)) {
+                        copy_op(q + 1);
+                        if ((threadIdx.x & 31) == 0) *nextc = 1;
                     }
                 }
             }
+            pass(q - 1, q + 1);  // beside the MMAs of q
+            const bool done = __syncthreads_and(tc_mbar_wait(&mbar[0], par, mlimit)) && landed[0] && landed[1];
+            tc_fence_after();
+            if (!done) {
+                timed_out(par, *nextc != 0);
+                ok = false;
+                break;  // uniform: no TMEM read, no further MMA
+            }
+            stage(q + 3);  // into the buffers (b) of q + 1 and (g) of q - 1 read last
+            combine(q);
+            if (threadIdx.x < kTcN) kslot(q + 2 - q0)[threadIdx.x] = 0u;  // (g) of q - 1 read them last
+            if (q + 1 < q1) digits(q + 1);
+            cp_async_wait_one();  // q + 2's inputs
+            tc_fence_proxy();
+            tc_fence_before();
+            __syncthreads();  // results of q, digits of q + 1; TMEM free for the MMAs of q + 1
+            tc_fence_after();
         }
-        tc_fence_before();
-        __syncthreads();
-        // (g) F* = x - f at the interior levels, the wall values at the walls:
-        // rows k of both blocks share the exponent e_k, so x_k - f_k =
-        // (Te + To - F) 2^E and x_nz-1-k - f_nz-1-k = (Te - To - F') 2^E
-        // with E = e_k + f_c - 52 and F = round(f 2^-E), exactly in integers
-        // but for that one rounding of f and the final conversion
-        for (int i = threadIdx.x, p = 0; i < nmode * 3 * he; i += blockDim.x, ++p) {
-            const int mi = i / (3 * he);
-            const int r = i - mi * 3 * he;
-            const int comp = r / he, k = r - comp * he;
-            const int ky = mi ? g.ny - kya : kya;
-            const int m = ky * g.nxhp + kx;
-            const int c0 = 6 * mi + 2 * comp;
-            double2* oc = fptr(Out, comp);
-            const size_t o1 = (size_t)k * g.nm + m, o2 = (size_t)(nz - 1 - k) * g.nm + m;
-            if (k == 0) {
-                double2 bc1 = make_double2(0.0, 0.0), bc2 = bc1;
-                if (comp < 2) {
-                    const double2 g1 = staged ? sGP[4 * mi + 2 * comp] : GP[(size_t)(2 * comp) * g.nm + m];
-                    const double2 g2 = staged ? sGP[4 * mi + 2 * comp + 1] : GP[(size_t)(2 * comp + 1) * g.nm + m];
-                    bc1 = make_double2(-sp.dt * g1.x, -sp.dt * g1.y);
-                    bc2 = make_double2(-sp.dt * g2.x, -sp.dt * g2.y);
-                }
-                oc[o1] = bc1;
-                oc[o2] = bc2;
-                continue;
-            }
-            const double2* fc = fptr(F, comp);
-            double2 v1, v2;
-            if (p == 0) { v1 = keep1[0]; v2 = keep2[0]; }
-            else if (p == 1) { v1 = keep1[1]; v2 = keep2[1]; }
-            else { v1 = fc[o1]; v2 = k < ho ? fc[o2] : v1; }
-            const int e = staged ? sEq[k] : __ldg(&ops.tcE[(size_t)q * m8 + k]);
-            double o1x, o1y, o2x = 0.0, o2y = 0.0;
-            {
-                const int E = e + sF[c0] - 52;
-                const long long te = __double_as_longlong(sR[c0 * m8 + k]);
-                const long long to = k < ho ? __double_as_longlong(sR[c0 * m8 + t.e8 + k]) : 0;
-                o1x = tc_sub_scaled(te + to, v1.x, E);
-                if (k < ho) o2x = tc_sub_scaled(te - to, v2.x, E);
-            }
-            {
-                const int E = e + sF[c0 + 1] - 52;
-                const long long te = __double_as_longlong(sR[(c0 + 1) * m8 + k]);
-                const long long to = k < ho ? __double_as_longlong(sR[(c0 + 1) * m8 + t.e8 + k]) : 0;
-                o1y = tc_sub_scaled(te + to, v1.y, E);
-                if (k < ho) o2y = tc_sub_scaled(te - to, v2.y, E);
-            }
-            oc[o1] = make_double2(o1x, o1y);
-            if (k < ho) oc[o2] = make_double2(o2x, o2y);
-        }
-        __syncthreads();  // shared buffers are reused by the next q
+        if (ok) pass(q1 - 1, q1);  // the outputs of the last q
     }
     cp_async_wait_all();  // a stage issued before a timeout lands before the CTA leaves
     tc_fence_before();
@@ -1001,11 +1190,12 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     if (threadIdx.x < 32) tc_dealloc(tmem, 2 * kTcDCols);
 }
 
-__global__ void __launch_bounds__(256) k_viscous_tc(GridDev g, Ops ops, StepParams sp, Fields F, Fields Src,
-                                                    const double2* __restrict__ GP,
-                                                    const dns3d_pi_state* __restrict__ pi, Fields Out, int qpb,
-                                                    int* err) {
-    viscous_tc_body(g, ops, sp, F, Src, GP, pi, Out, qpb, blockIdx.x, err);
+template <bool kPipe>
+__global__ void __launch_bounds__(256, 2) k_viscous_tc(GridDev g, Ops ops, StepParams sp, Fields F, Fields Src,
+                                                       const double2* __restrict__ GP,
+                                                       const dns3d_pi_state* __restrict__ pi, Fields Out, int qpb,
+                                                       int* err) {
+    viscous_tc_body<kPipe>(g, ops, sp, F, Src, GP, pi, Out, qpb, blockIdx.x, err);
 }
 
 // ------------------------------------------------------------------ tensor-core z-derivatives
@@ -3115,7 +3305,8 @@ cudaError_t prepare_step_kernels(const GridDev& g) {
     if ((e = set_smem(k_pressure, (2 * (size_t)g.nz * tile_cols(g, 2) + g.nz) * sizeof(double2)))) return e;
     if ((e = set_smem(k_correction, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
     if ((e = set_smem(k_divergence, (size_t)g.nz * tile_cols(g, 1) * sizeof(double2)))) return e;
-    if ((e = set_smem(k_viscous_tc, 0))) return e;
+    if ((e = set_smem(k_viscous_tc<false>, 0))) return e;
+    if ((e = set_smem(k_viscous_tc<true>, 0))) return e;
     if ((e = set_smem(k_dz_tc<VortTcOp>, 0))) return e;
     if ((e = set_smem(k_dz_tc<CorrTcOp>, 0))) return e;
     if ((e = set_smem(k_dz_tc<PresRhsTcOp>, 0))) return e;
@@ -3206,9 +3397,8 @@ cudaError_t launch_poisson_residual(const GridDev& g, const Ops& ops, const Step
 }
 
 size_t viscous_tc_smem(const GridDev& g) {
-    const TcGeom t = tc_geom(g.nz);
-    // + the staged inputs of one q where they fit
-    return viscous_tc_stage_offset(t) + (viscous_tc_staged(t, g.nz) ? viscous_tc_stage_bytes(t, g.nz) : 0);
+    // + the staged inputs where they fit
+    return viscous_tc_pipelined(g.nz) ? viscous_tc_smem_nz<true>(g.nz) : viscous_tc_smem_nz<false>(g.nz);
 }
 
 // Streaming multiprocessors of the current device (read once per device).
@@ -3225,7 +3415,9 @@ int num_sms() {
 }
 
 bool viscous_tc_fits(const GridDev& g) {
-    return tc_supported(g.nz) && viscous_tc_smem(g) <= smem_limit(k_viscous_tc);
+    return tc_supported(g.nz) &&
+           viscous_tc_smem(g) <= (viscous_tc_pipelined(g.nz) ? smem_limit(k_viscous_tc<true>)
+                                                             : smem_limit(k_viscous_tc<false>));
 }
 
 // Operator indices q per CTA: consecutive runs of q spread over one wave of
@@ -3240,7 +3432,10 @@ cudaError_t launch_viscous_tc(const GridDev& g, const Ops& ops, const StepParams
     if (!ops.tcA || !ops.tcE || !viscous_tc_fits(g)) return cudaErrorInvalidValue;
     const int qpb = tc_q_per_cta(ops.nq);
     const int nb = (ops.nq + qpb - 1) / qpb;
-    k_viscous_tc<<<nb, 256, viscous_tc_smem(g), s>>>(g, ops, sp, F, Src, GP, pi, Out, qpb, err);
+    if (viscous_tc_pipelined(g.nz))
+        k_viscous_tc<true><<<nb, 256, viscous_tc_smem(g), s>>>(g, ops, sp, F, Src, GP, pi, Out, qpb, err);
+    else
+        k_viscous_tc<false><<<nb, 256, viscous_tc_smem(g), s>>>(g, ops, sp, F, Src, GP, pi, Out, qpb, err);
     return cudaGetLastError();
 }
 
@@ -3550,8 +3745,9 @@ struct RsVisc64 {
 struct RsVisc64Tc {
     static constexpr int kMinCtas = 2;
     static __device__ __forceinline__ void run(const RunDesc& d, int b) {
-        viscous_tc_body(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
-                        fields3(d.US, d.VS, d.WS), d.gx[kRsVisc], b, d.tcerr);
+        // the phased schedule at every nz (one body per stage kernel)
+        viscous_tc_body<false>(d.g, d.ops, d.sp, fields3(d.U, d.V, d.W), desc_fields<double2, 3>(d.src), d.GP, d.pi,
+                               fields3(d.US, d.VS, d.WS), d.gx[kRsVisc], b, d.tcerr);
     }
 };
 
@@ -3740,7 +3936,7 @@ size_t ragged_smem(int stage, bool mixed, const RunDesc& d) {
             if (!mixed && (ragged_variant(d) & kRvVortTc)) return vorticity_tc_smem(g);
             return 2 * nz * tc * (mixed ? sizeof(float2) : sizeof(double2));
         case kRsVisc:
-            if (!mixed && (ragged_variant(d) & kRvViscTc)) return viscous_tc_smem(g);
+            if (!mixed && (ragged_variant(d) & kRvViscTc)) return viscous_tc_smem_nz<false>(g.nz);
             return mixed ? viscous_mixed_smem(g, tc) : 6 * nz * tc * sizeof(double2);
         case kRsPres:
             if (mixed) return pressure_mixed_smem(g, tc);

@@ -186,6 +186,19 @@ __device__ __forceinline__ int tc_exponent(unsigned long long absbits) {
     return (ex == 0 ? -1022 : ex - 1023) + 1;
 }
 
+// A 32-bit key of |x| that orders like |x| (the high word of |x| with the
+// low word's nonzero-ness in its lowest bit), so that the largest key of a
+// column gives tc_exponent of its largest |x|: tc_exponent_key below.
+__device__ __forceinline__ unsigned tc_key(double x) {
+    const unsigned long long ab = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFULL;
+    return (unsigned)(ab >> 32) | ((unsigned)ab != 0u ? 1u : 0u);
+}
+__device__ __forceinline__ int tc_exponent_key(unsigned key) {
+    if (key == 0) return 0;
+    const int ex = (int)(key >> 20);
+    return (ex == 0 ? -1022 : ex - 1023) + 1;
+}
+
 // Exact FP32 integer (|v| < 2^22) to int.
 __device__ __forceinline__ int tc_f2i(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
 
@@ -264,6 +277,8 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// ... all but the most recent group
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 __device__ __forceinline__ void tc_commit(uint64_t* mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
