@@ -731,9 +731,10 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     double2* sGP4 = sP2 + Bf::kP * 12 * nz;
     int* sEq4 = reinterpret_cast<int*>(sGP4 + 8 * Bf::kG);
     // the buffers of the operator index q0 + rel
-    auto rslot = [&](int rel) { return sR2 + (size_t)(rel % Bf::kR) * kTcN * m8; };
-    auto kslot = [&](int rel) { return sK3 + (rel % Bf::kK) * kTcN; };
-    auto pslot = [&](int rel) { return sP2 + (size_t)(rel % Bf::kP) * 12 * nz; };
+    auto rslot = [&](int rel) { return sR2 + (size_t)((unsigned)rel % Bf::kR) * kTcN * m8; };
+    auto kslot = [&](int rel) { return sK3 + ((unsigned)rel % Bf::kK) * kTcN; };
+    auto pslot = [&](int rel) { return sP2 + (size_t)((unsigned)rel % Bf::kP) * 12 * nz; };
+    auto gslot = [&](int rel) { return (int)((unsigned)rel % Bf::kG); };
     {
         uint4* z = reinterpret_cast<uint4*>(sA);
         const int n16 = kTcSlices * (bl.a + b_halves) / 8;
@@ -785,7 +786,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
                 double2* dst = sP + (size_t)((fld * 2 + mi) * 3 + comp) * nz;
                 for (int z = lane; z < nz; z += 32) cp_async16(dst + z, src + (size_t)z * g.nm);
             }
-            const int j = threadIdx.x, b = rel % Bf::kG;
+            const int j = threadIdx.x, b = gslot(rel);
             if (j < 4 * qi.nmode) {  // the wall gradients GP[4][nm] of the modes
                 const int mi = j >> 2, w = j & 3;
                 const int m = (mi ? g.ny - qi.kya : qi.kya) * g.nxhp + qi.kx;
@@ -824,7 +825,7 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     auto rhs_item = [&](int q, const QInfo& qi, int i, double2& v1o, double2& v2o, unsigned& kre, unsigned& kim) {
         const int rel = q - q0;
         const double2* sP = pslot(rel);
-        const double2* sGP = sGP4 + 8 * (rel % Bf::kG);
+        const double2* sGP = sGP4 + 8 * gslot(rel);
         double* sR = rslot(rel);
         const int mi = i / (3 * he);
         const int r = i - mi * 3 * he;
@@ -879,8 +880,8 @@ __device__ __forceinline__ void viscous_tc_body(const GridDev& g, const Ops& ops
     // values at levels k, nz-1-k (read again from F past the kept items)
     auto out_item = [&](int q, const QInfo& qi, int i, int p, double2 v1, double2 v2) {
         const int rel = q - q0;
-        const double2* sGP = sGP4 + 8 * (rel % Bf::kG);
-        const int* sEq = sEq4 + (rel % Bf::kG) * m8;
+        const double2* sGP = sGP4 + 8 * gslot(rel);
+        const int* sEq = sEq4 + gslot(rel) * m8;
         const double* sR = rslot(rel);
         const unsigned* sK = kslot(rel);
         const int mi = i / (3 * he);
