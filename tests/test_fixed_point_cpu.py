@@ -10,7 +10,9 @@ exact Python integers (f90_dns_gb300/csrc/tc.cuh, step.cu):
 * limb products (fx_mac, the fixed-point Poisson solve): four 32 x 32-bit
   limb products of a 58-bit and a 54-bit integer, summed in 64-bit partial
   sums over up to 65 terms, recombine to the exact 128-bit dot product
-  without overflow.
+  without overflow;
+* column keys (tc_key, tc_exponent_key): the largest 32-bit key of a column
+  gives the same power-of-two scale as its largest |x|.
 """
 import random
 
@@ -164,3 +166,49 @@ def test_fixed_point_solve_error_bound():
                      + sum(abs(c) for c in B) * Fraction(2) ** (f - 54) * Fraction(2) ** (e - 59)
                      + Fraction(2) ** (e + f - 57))
             assert abs(x - exact) <= bound, (n, k)
+
+
+def _key(x):
+    """tc_key: the high word of |x| with the low word's nonzero-ness in its lowest bit."""
+    ab = int(np.array([x], dtype=np.float64).view(np.uint64)[0]) & 0x7FFFFFFFFFFFFFFF
+    return (ab >> 32) | (1 if (ab & 0xFFFFFFFF) else 0)
+
+
+def _exponent_bits(absbits):
+    """tc_exponent on the bits of the largest |x|."""
+    if absbits == 0:
+        return 0
+    ex = absbits >> 52
+    return (-1022 if ex == 0 else ex - 1023) + 1
+
+
+def _exponent_key(key):
+    """tc_exponent_key."""
+    if key == 0:
+        return 0
+    ex = key >> 20
+    return (-1022 if ex == 0 else ex - 1023) + 1
+
+
+def test_column_keys_give_the_column_exponent():
+    """The viscous tensor-core kernel takes a column's power-of-two scale from
+    the largest 32-bit key of its values (a warp maximum and a shared atomic)
+    instead of the largest 64-bit |x|: the key orders like |x| and keeps the
+    exponent field and zero-ness, so the exponent is the same, for zeros,
+    subnormals, infinities and NaNs as well."""
+    rng = np.random.default_rng(7)
+    specials = [0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1.0, -1.0, 1.5, 2.0 ** -1022,
+                2.0 ** -1023, np.inf, -np.inf, np.nan, 1.7976931348623157e308, 2.0 ** 52 + 1.0]
+    for trial in range(3000):
+        n = int(rng.integers(1, 80))
+        col = rng.standard_normal(n) * 10.0 ** rng.uniform(-300, 300, n)
+        col[rng.random(n) < 0.2] = 0.0
+        if trial % 3 == 0:
+            col[rng.integers(0, n)] = specials[trial // 3 % len(specials)]
+        bits = col.view(np.uint64) & np.uint64(0x7FFFFFFFFFFFFFFF)
+        ref = _exponent_bits(int(bits.max()))
+        got = _exponent_key(max(_key(float(v)) for v in col))
+        assert got == ref, (col, got, ref)
+    # one column of values that differ only in their low word
+    col = np.array([1.0, np.nextafter(1.0, 2.0), -np.nextafter(2.0, 1.0)])
+    assert _exponent_key(max(_key(v) for v in col)) == 1
