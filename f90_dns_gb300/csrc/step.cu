@@ -552,31 +552,36 @@ __device__ __forceinline__ void viscous_body(GridDev g, Ops ops, StepParams sp, 
 //      (viscous_rhs_cn_half; the operator carries 2 w_j) from the q's inputs
 //      staged in shared memory: the 2 x 3 columns of u, v, w and of the
 //      sources, the wall gradients and the row exponents, copied with
-//      cp.async an operator index ahead, so the strided column reads (one
-//      16-byte value per level, a plane apart) overlap earlier work; each
-//      column's power-of-two scale comes from the largest key (tc_key) of its
-//      values, a warp reduction and one shared atomic per column and warp;
+//      cp.async while earlier work runs, so the strided column reads (one
+//      16-byte value per level, a plane apart) are off the critical path;
+//      each column's power-of-two scale comes from the largest key (tc_key)
+//      of its values, a warp reduction and one shared atomic per column and
+//      warp;
 //  (d) the digits, two K rows of one column per thread (tc_digit_pairs);
-//  (e) thread 0 for block E (even rows: right-hand-side rows [0, ke)) and
-//      thread 32 for block O (odd rows: [ke, kt)) issue, per digit slice sa
-//      of the operator, the block's K-steps against right-hand-side digit
-//      slices 0 .. 7-sa side by side (N = 16 (8-sa)), accumulated into the
-//      weight-class columns sa .. 7 of that block's TMEM region;
+//  (e) one thread for block E (even rows: right-hand-side rows [0, ke)) and
+//      one of the next warp for block O (odd rows: [ke, kt)) issue, per
+//      digit slice sa of the operator, the block's K-steps against
+//      right-hand-side digit slices 0 .. 7-sa side by side (N = 16 (8-sa)),
+//      accumulated into the weight-class columns sa .. 7 of that block's
+//      TMEM region;
 //  (f) every row's 8 class accumulators are combined into the 64-bit integer
 //      T (tc_combine8);
 //  (g) the outputs F* = x - f are formed in integers from T of the even and
 //      odd rows (which share an exponent) and written (wall values at the
 //      walls).
-// Software pipeline over the CTA's q: while the MMAs of q run, one pass of the
-// CTA writes the outputs (g) of q - 1 and forms the right-hand sides (b) of
-// q + 1 (item for item in the same shared-memory slots: each thread reads its
-// results of q - 1 before it writes its right-hand sides of q + 1); once the
-// MMAs are done, the operator copy (a) of q + 1 starts and the combination
-// (f) of q runs beside the digits (d) of q + 1.  Two barriers per q.  The
-// right-hand sides and results alternate between two buffers, the column keys
-// rotate through three, the staged inputs through two (the wall gradients
-// and row exponents, which the outputs still read, through four); the state
-// values that (g) subtracts stay in registers from (b), two sets in turn.
+// Two schedules (viscous_tc_pipelined).  Phased, where two CTAs share an SM:
+// per q (a) + (b) | (d) | (e) | (f) | (g), each behind a barrier, the other
+// CTA filling the waits.  Pipelined, where one CTA has the SM: while the MMAs
+// of q run, one pass of the CTA writes the outputs (g) of q - 1 and forms the
+// right-hand sides (b) of q + 1 (item for item in the same shared-memory
+// slots: each thread reads its results of q - 1 before it writes its
+// right-hand sides of q + 1), and the last warp starts the operator copy (a)
+// of q + 1 the moment the MMAs of q complete; then the combination (f) of q
+// runs beside the digits (d) of q + 1.  Two barriers per q; the right-hand
+// sides and results alternate between two buffers, the column keys rotate
+// through three, the staged inputs through two (the wall gradients and row
+// exponents, which the outputs still read, through four); the state values
+// that (g) subtracts stay in registers from (b), two sets in turn.
 // (t - round(f 2^-E)) 2^E: an integer result t at the scale 2^E minus an
 // FP64 value f, exactly in integers but for the rounding of f to that scale
 // and of the final conversion; falls back to the FP64 difference where f is
